@@ -1,0 +1,314 @@
+"""Seeded unstructured river meshes and their finite-volume geometry records.
+
+The solver consumes the face-based records of the reference's cut-cell
+exporter: per face ``owner/neighbour/bid/normal/length/mid``, per cell
+``area/xy``, a CSR cell->face incidence ``offset/faces/signs`` and the cached
+least-squares stencil geometry. Triangles from a Delaunay triangulation fit
+that layout unchanged.
+
+Geometry formulas follow the reference's Fortran caches:
+- ``bed_ls_delta`` = neighbour centroid - cell centroid per CSR entry
+  (``src/solver/cut_cells/cutcell_solver.f90:8666-8688``);
+- ``hydraulic_ls_weight`` = length / |r|^2 and the 2x2 normal matrix
+  ``[a11, a12, a22, a11*a22 - a12*a12]`` accumulated in CSR order
+  (``cutcell_solver.f90:8639-8662``);
+- ``face_displacement`` = face midpoint - cell centroid per side
+  (``cutcell_solver.f90:8693``);
+- ``distance`` = |(mid - xy_owner).n| and |(xy_neighbour - mid).n|
+  (``src/braids_support/gpu_fwave/resident_update.py:76-78``).
+
+Faces are numbered in first-visit order over Morton-sorted cells, so both the
+cell sweep and the face sweep walk memory with spatial locality.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+import numpy as np
+
+# Hydraulic boundary modes of the reference's exterior owner
+# (src/braids_core/sediment/river_exterior_bed.h:94-156).
+MODE_STAGE = 2          # prescribed water level, half-Riemann outflow
+MODE_TOTAL_Q = 6        # total discharge distributed by conveyance
+
+
+@dataclass
+class Mesh:
+    points: np.ndarray            # (np, 2) vertices
+    tri: np.ndarray               # (nc, 3) CCW vertex ids
+    owner: np.ndarray             # (nf,) int32
+    neighbour: np.ndarray         # (nf,) int32, -1 exterior
+    bid: np.ndarray               # (nf,) int32, boundary segment or -1 (wall / interior)
+    normal: np.ndarray            # (2, nf) unit normal owner -> neighbour
+    length: np.ndarray            # (nf,)
+    mid: np.ndarray               # (2, nf)
+    area: np.ndarray              # (nc,)
+    xy: np.ndarray                # (2, nc) centroids
+    offset: np.ndarray            # (nc+1,) int32
+    faces: np.ndarray             # (nadj,) int32
+    signs: np.ndarray             # (nadj,) int32 +1 owner / -1 neighbour
+    boundary_offset: np.ndarray   # (nb+1,) int32
+    boundary_faces: np.ndarray    # (sum,) int32, faces of each open segment in order
+    records: dict = field(default_factory=dict)
+
+    @property
+    def nc(self):
+        return len(self.area)
+
+    @property
+    def nf(self):
+        return len(self.owner)
+
+    @property
+    def nadj(self):
+        return len(self.faces)
+
+    @property
+    def nb(self):
+        return len(self.boundary_offset) - 1
+
+
+def morton_order(x, y):
+    """Permutation sorting points along a 2-D Morton (Z-order) curve."""
+    def spread(v):
+        v = v.astype(np.uint64) & np.uint64(0xFFFF)
+        v = (v | (v << np.uint64(8))) & np.uint64(0x00FF00FF)
+        v = (v | (v << np.uint64(4))) & np.uint64(0x0F0F0F0F)
+        v = (v | (v << np.uint64(2))) & np.uint64(0x33333333)
+        v = (v | (v << np.uint64(1))) & np.uint64(0x55555555)
+        return v
+    lo = np.array([x.min(), y.min()])
+    span = max(float(x.max() - lo[0]), float(y.max() - lo[1]), 1e-30)
+    qx = np.floor((x - lo[0]) / span * 65535.0).astype(np.int64)
+    qy = np.floor((y - lo[1]) / span * 65535.0).astype(np.int64)
+    key = spread(qx) | (spread(qy) << np.uint64(1))
+    return np.argsort(key, kind="stable")
+
+
+def build_mesh(points, tri, segment_of_edge):
+    """Face/CSR topology of a triangle mesh.
+
+    ``segment_of_edge(a, b)`` receives the end points (arrays (m,2)) of the
+    exterior edges and returns their open-boundary segment id, or -1 for a
+    wall. Triangles are re-oriented counter-clockwise and Morton sorted.
+    """
+    points = np.ascontiguousarray(points, dtype=np.float64)
+    tri = np.asarray(tri, dtype=np.int64).copy()
+    p = points[tri]
+    cross = (p[:, 1, 0] - p[:, 0, 0]) * (p[:, 2, 1] - p[:, 0, 1]) - \
+            (p[:, 2, 0] - p[:, 0, 0]) * (p[:, 1, 1] - p[:, 0, 1])
+    flip = cross < 0
+    tri[flip] = tri[flip][:, [0, 2, 1]]
+    cen = points[tri].mean(axis=1)
+    tri = tri[morton_order(cen[:, 0], cen[:, 1])]
+    nc = len(tri)
+    p = points[tri]
+    # Centroid and area (shoelace), FP64.
+    xy = np.ascontiguousarray(((p[:, 0] + p[:, 1]) + p[:, 2]).T / 3.0)
+    area = 0.5 * ((p[:, 1, 0] - p[:, 0, 0]) * (p[:, 2, 1] - p[:, 0, 1]) -
+                  (p[:, 2, 0] - p[:, 0, 0]) * (p[:, 1, 1] - p[:, 0, 1]))
+    if np.any(area <= 0):
+        raise ValueError("degenerate triangle")
+    # Local edges (v0,v1), (v1,v2), (v2,v0): occurrence index 3*t + e.
+    a = tri[:, [0, 1, 2]].ravel()
+    b = tri[:, [1, 2, 0]].ravel()
+    lo = np.minimum(a, b)
+    hi = np.maximum(a, b)
+    key = lo * np.int64(len(points)) + hi
+    order = np.argsort(key, kind="stable")          # occurrences of one edge are adjacent, ascending
+    ks = key[order]
+    start = np.ones(len(ks), dtype=bool)
+    start[1:] = ks[1:] != ks[:-1]
+    group = np.cumsum(start) - 1                      # edge id in key order
+    first = order[start]                              # first (smallest) occurrence of each edge
+    count = np.bincount(group)
+    if np.any(count > 2):
+        raise ValueError("non-manifold edge")
+    second = np.full(len(first), -1, dtype=np.int64)
+    two = np.flatnonzero(count == 2)
+    second[two] = order[np.flatnonzero(start)[two] + 1]
+    # Faces numbered by first visit over the Morton-sorted cells.
+    face_order = np.argsort(first, kind="stable")
+    first = first[face_order]
+    second = second[face_order]
+    nf = len(first)
+    face_of_edge = np.empty(len(ks), dtype=np.int64)
+    rank = np.empty(nf, dtype=np.int64)
+    rank[face_order] = np.arange(nf)
+    face_of_edge[order] = rank[group]
+    owner = (first // 3).astype(np.int32)
+    neighbour = np.where(second >= 0, second // 3, -1).astype(np.int32)
+    va = a[first]
+    vb = b[first]
+    d = points[vb] - points[va]
+    length = np.hypot(d[:, 0], d[:, 1])
+    normal = np.ascontiguousarray(np.stack((d[:, 1] / length, -d[:, 0] / length)))
+    mid = np.ascontiguousarray((0.5 * (points[va] + points[vb])).T)
+    bid = np.full(nf, -1, dtype=np.int32)
+    ext = np.flatnonzero(neighbour < 0)
+    if len(ext):
+        bid[ext] = np.asarray(segment_of_edge(points[va[ext]], points[vb[ext]]), dtype=np.int32)
+    faces = face_of_edge.astype(np.int32)             # CSR entries 3c+e in local edge order
+    signs = np.where(owner[faces] == np.repeat(np.arange(nc), 3), 1, -1).astype(np.int32)
+    offset = (3 * np.arange(nc + 1)).astype(np.int32)
+    nb = int(bid.max()) + 1 if np.any(bid >= 0) else 0
+    bfaces, boff = [], [0]
+    for s in range(nb):
+        ids = np.flatnonzero(bid == s)
+        # Order the segment along its own direction for reproducible reductions.
+        mids = mid[:, ids]
+        span = np.ptp(mids, axis=1)
+        ids = ids[np.argsort(mids[int(np.argmax(span))], kind="stable")]
+        bfaces.append(ids)
+        boff.append(boff[-1] + len(ids))
+    boundary_faces = (np.concatenate(bfaces) if bfaces else np.zeros(0, np.int64)).astype(np.int32)
+    return Mesh(points=points, tri=tri.astype(np.int32), owner=owner, neighbour=neighbour, bid=bid,
+                normal=normal, length=length, mid=mid, area=area, xy=xy,
+                offset=offset, faces=faces, signs=signs,
+                boundary_offset=np.asarray(boff, dtype=np.int32), boundary_faces=boundary_faces)
+
+
+def geometry_records(mesh: Mesh):
+    """Least-squares stencil geometry cached per CSR entry and face side.
+
+    Accumulation order and expression shape follow the reference caches so
+    that every consumer sees bitwise-identical FP64 weights.
+    """
+    nc, nf = mesh.nc, mesh.nf
+    owner, neighbour, faces, signs, offset = mesh.owner, mesh.neighbour, mesh.faces, mesh.signs, mesh.offset
+    xy = mesh.xy
+    other = np.where(signs < 0, owner[faces], neighbour[faces])
+    has = other >= 0
+    cell_of = np.repeat(np.arange(nc), np.diff(offset))
+    safe = np.where(has, other, 0)
+    r1 = np.where(has, xy[0, safe] - xy[0, cell_of], 0.0)
+    r2 = np.where(has, xy[1, safe] - xy[1, cell_of], 0.0)
+    ls_delta = np.ascontiguousarray(np.stack((r1, r2)))
+    with np.errstate(divide="ignore", invalid="ignore"):
+        w = np.where(has, mesh.length[faces] / (r1 * r1 + r2 * r2), 0.0)
+    a11 = np.zeros(nc)
+    a12 = np.zeros(nc)
+    a22 = np.zeros(nc)
+    degree = np.diff(offset)
+    for slot in range(int(degree.max())):
+        cells = np.flatnonzero(degree > slot)
+        k = offset[cells] + slot
+        m = has[k]
+        cells, k = cells[m], k[m]
+        a11[cells] = a11[cells] + w[k] * (r1[k] * r1[k])
+        a12[cells] = a12[cells] + (w[k] * r1[k]) * r2[k]
+        a22[cells] = a22[cells] + w[k] * (r2[k] * r2[k])
+    ls_matrix = np.ascontiguousarray(np.stack((a11, a12, a22, a11 * a22 - a12 * a12)))
+    disp = np.zeros((2, 2, nf))          # [component, side, face]
+    disp[0, 0] = mesh.mid[0] - xy[0, owner]
+    disp[1, 0] = mesh.mid[1] - xy[1, owner]
+    nb_ = neighbour >= 0
+    nsafe = np.where(nb_, neighbour, 0)
+    disp[0, 1] = np.where(nb_, mesh.mid[0] - xy[0, nsafe], 0.0)
+    disp[1, 1] = np.where(nb_, mesh.mid[1] - xy[1, nsafe], 0.0)
+    disp_len = np.hypot(disp[0], disp[1])        # (2, nf) |mid - xy| per side
+    nx, ny = mesh.normal
+    distance = np.zeros((2, nf))
+    distance[0] = np.abs((mesh.mid[0] - xy[0, owner]) * nx + (mesh.mid[1] - xy[1, owner]) * ny)
+    distance[1] = np.where(nb_, np.abs((xy[0, nsafe] - mesh.mid[0]) * nx + (xy[1, nsafe] - mesh.mid[1]) * ny), 0.0)
+    rec = dict(ls_delta=ls_delta, ls_weight=np.ascontiguousarray(w), ls_matrix=ls_matrix,
+               disp=np.ascontiguousarray(disp), disp_len=np.ascontiguousarray(disp_len),
+               distance=np.ascontiguousarray(distance))
+    mesh.records.update(rec)
+    return rec
+
+
+# ---------------------------------------------------------------------------
+# Synthetic channel meshes
+# ---------------------------------------------------------------------------
+
+def jittered_channel_points(length, width, spacing, jitter, rng, refine=()):
+    """Grid points on [0,L]x[0,W] with uniform jitter; edge points slide only along their edge.
+
+    ``refine`` is a sequence of boxes ``(x0, x1, y0, y1, spacing)``: coarse
+    points inside a box are replaced by a finer jittered grid.
+    """
+    nx = int(round(length / spacing))
+    ny = int(round(width / spacing))
+    xs = np.linspace(0.0, length, nx + 1)
+    ys = np.linspace(0.0, width, ny + 1)
+    X, Y = np.meshgrid(xs, ys, indexing="ij")
+    X = X.ravel()
+    Y = Y.ravel()
+    jx = rng.uniform(-jitter, jitter, X.size)
+    jy = rng.uniform(-jitter, jitter, X.size)
+    onx = (X == 0.0) | (X == length)
+    ony = (Y == 0.0) | (Y == width)
+    X = X + np.where(onx, 0.0, jx)
+    Y = Y + np.where(ony, 0.0, jy)
+    pts = [np.c_[X, Y]]
+    keep = np.ones(len(pts[0]), dtype=bool)
+    for (x0, x1, y0, y1, s) in refine:
+        x0, x1 = max(0.0, x0), min(length, x1)
+        y0, y1 = max(0.0, y0), min(width, y1)
+        inside = (pts[0][:, 0] > x0 - spacing * 0.5) & (pts[0][:, 0] < x1 + spacing * 0.5) & \
+                 (pts[0][:, 1] > y0 - spacing * 0.5) & (pts[0][:, 1] < y1 + spacing * 0.5)
+        keep &= ~inside | onx | ony
+        fx = np.arange(x0, x1 + 1e-9, s)
+        fy = np.arange(y0, y1 + 1e-9, s)
+        FX, FY = np.meshgrid(fx, fy, indexing="ij")
+        FX = FX.ravel()
+        FY = FY.ravel()
+        fj = 0.25 * s
+        FX = FX + rng.uniform(-fj, fj, FX.size)
+        FY = FY + rng.uniform(-fj, fj, FY.size)
+        ok = (FX > 0.0) & (FX < length) & (FY > 0.0) & (FY < width)
+        pts.append(np.c_[FX[ok], FY[ok]])
+    base = pts[0][keep]
+    # Boundary points of refined boxes: keep them on the boundary lines only.
+    out = np.concatenate([base] + pts[1:])
+    _, unique = np.unique(np.round(out, 9), axis=0, return_index=True)
+    return out[np.sort(unique)]
+
+
+def gaussian_field(length, width, sigma, correlation, rng, resolution=1.0):
+    """Stationary Gaussian random field by FFT filtering of white noise.
+
+    Covariance sigma^2 exp(-r^2 / (2 l^2)); the raster is padded by 3 l on
+    every side so the periodic FFT does not correlate opposite edges. Returns
+    ``(x0, y0, res, raster)`` for bilinear sampling.
+    """
+    pad = 3.0 * correlation
+    nx = int(np.ceil((length + 2 * pad) / resolution)) + 1
+    ny = int(np.ceil((width + 2 * pad) / resolution)) + 1
+    noise = rng.standard_normal((nx, ny))
+    kx = 2 * np.pi * np.fft.fftfreq(nx, d=resolution)
+    ky = 2 * np.pi * np.fft.rfftfreq(ny, d=resolution)
+    K2 = kx[:, None] ** 2 + ky[None, :] ** 2
+    filt = np.exp(-K2 * correlation ** 2 / 4.0)
+    field = np.fft.irfft2(np.fft.rfft2(noise) * filt, s=(nx, ny))
+    field *= sigma / field.std()
+    return (-pad, -pad, resolution, field)
+
+
+def sample_field(grid, x, y):
+    x0, y0, res, raster = grid
+    fx = (x - x0) / res
+    fy = (y - y0) / res
+    i = np.clip(np.floor(fx).astype(np.int64), 0, raster.shape[0] - 2)
+    j = np.clip(np.floor(fy).astype(np.int64), 0, raster.shape[1] - 2)
+    tx = fx - i
+    ty = fy - j
+    return ((1 - tx) * (1 - ty) * raster[i, j] + tx * (1 - ty) * raster[i + 1, j] +
+            (1 - tx) * ty * raster[i, j + 1] + tx * ty * raster[i + 1, j + 1])
+
+
+def channel_mesh(length, width, spacing, jitter, seed, refine=()):
+    """Delaunay mesh of a straight channel: inlet segment 0 at x=0, outlet 1 at x=L, walls elsewhere."""
+    from scipy.spatial import Delaunay
+    rng = np.random.default_rng(seed)
+    pts = jittered_channel_points(length, width, spacing, jitter, rng, refine)
+    tri = Delaunay(pts).simplices
+
+    def segment(a, b):
+        tol = 1e-9 * max(length, 1.0)
+        inlet = (np.abs(a[:, 0]) < tol) & (np.abs(b[:, 0]) < tol)
+        outlet = (np.abs(a[:, 0] - length) < tol) & (np.abs(b[:, 0] - length) < tol)
+        return np.where(inlet, 0, np.where(outlet, 1, -1))
+    mesh = build_mesh(pts, tri, segment)
+    geometry_records(mesh)
+    return mesh

@@ -1,0 +1,150 @@
+"""Seeded synthetic river scenarios: mesh, bed, initial state, boundaries, controls.
+
+Every scenario is a plain dict ("case") that both the CUDA solver and the CPU
+oracle consume:
+
+  mesh          Mesh (topology, geometry records)
+  z             (nc,) bed elevation
+  q             (3,nc) initial h, hu, hv
+  seg_mode      (nb,) hydraulic mode per open segment (2 stage, 6 total Q)
+  stage_policy  (nb,) 0 outflow only, 1 subcritical backflow
+  forcing       (2,nb) row 0 discharge Q [m3/s], row 1 stage [m]
+  exterior_bed  (nf,) exterior bed elevation on open faces (0 elsewhere)
+  controls      dict(grav, dry, cfl, speed_limit, roughness_mode, roughness_value)
+  turbines      list of rotor dicts (optional)
+
+Constants follow the reference's physical parameters: g = 9.81, dry = 1e-6
+(src/braids_core/sediment/bend_methods_v1.py:64-66), speed limit 50 m/s
+(src/braids_core/sediment/river_exterior_bed.py:210).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import mesh as M
+
+GRAVITY = 9.81
+DRY = 1e-6
+SPEED_LIMIT = 50.0
+
+
+def controls(cfl=0.9, manning=0.03):
+    return dict(grav=GRAVITY, dry=DRY, cfl=float(cfl), speed_limit=SPEED_LIMIT,
+                roughness_mode=2, roughness_value=float(manning))
+
+
+def _exterior_bed(mesh, z):
+    """Exterior bed on open faces = owner cell bed (no artificial step)."""
+    ext = np.zeros(mesh.nf)
+    openf = (mesh.neighbour < 0) & (mesh.bid >= 0)
+    ext[openf] = z[mesh.owner[openf]]
+    return ext
+
+
+def channel(length=2000.0, width=200.0, spacing=4.0, jitter=1.0, seed=1, sigma=0.2, corr=25.0,
+            slope=1e-3, outlet_bed=-5.0, stage=3.0, discharge=400.0, manning=0.03, cfl=0.9,
+            refine=(), field_resolution=1.0):
+    """Straight channel of the 50k-cell class: jittered-grid Delaunay, sloped bed + Gaussian field.
+
+    Lake at rest at ``stage``; inflow ``discharge`` (mode 6, conveyance
+    weighted) at x=0, stage outlet (mode 2) at x=L. The bed datum puts the
+    outlet bed at ``outlet_bed`` so a 5 m rotor is covered.
+    """
+    mesh = M.channel_mesh(length, width, spacing, jitter, seed, refine)
+    rng = np.random.default_rng(seed + 1000003)
+    grid = M.gaussian_field(length, width, sigma, corr, rng, field_resolution) if sigma > 0 else None
+    x, y = mesh.xy
+    z = outlet_bed + slope * (length - x)
+    if grid is not None:
+        z = z + M.sample_field(grid, x, y)
+    z = np.ascontiguousarray(z)
+    h = np.maximum(stage - z, 0.0)
+    q = np.ascontiguousarray(np.stack((h, np.zeros_like(h), np.zeros_like(h))))
+    return dict(mesh=mesh, z=z, q=q,
+                seg_mode=np.array([M.MODE_TOTAL_Q, M.MODE_STAGE], np.int32),
+                stage_policy=np.zeros(2, np.int32),
+                forcing=np.array([[discharge, 0.0], [0.0, stage]]),
+                exterior_bed=_exterior_bed(mesh, z),
+                controls=controls(cfl, manning), name=f"channel_{length:g}x{width:g}_s{spacing:g}")
+
+
+def config1(seed=1):
+    """Plain method, straight channel 2000 m x 200 m, 4 m jittered grid, about 50k triangles."""
+    return channel(seed=seed)
+
+
+def rotors_on_centreline(length, width, count, spacing, first_x, diameter=5.0, ct=0.8):
+    rows = []
+    for i in range(count):
+        rows.append(dict(turbine_id=i, x=first_x + i * spacing, y=0.5 * width, D=diameter,
+                         thrust_coefficient=ct))
+    return rows
+
+
+def config2(seed=2, refine_spacing=1.0):
+    """Config-1 channel with 3 tandem rotors on the centreline 150 m apart, refined wakes (about 120k cells)."""
+    length, width = 2000.0, 200.0
+    first = 700.0
+    rotors = rotors_on_centreline(length, width, 3, 150.0, first)
+    boxes = [(r["x"] - 10.0, r["x"] + 60.0, r["y"] - 15.0, r["y"] + 15.0, refine_spacing) for r in rotors]
+    case = channel(length, width, seed=seed, refine=boxes)
+    case["turbines"] = rotors
+    case["name"] = "channel_3_rotors"
+    return case
+
+
+def small_channel(length=120.0, width=24.0, spacing=4.0, seed=7, sigma=0.15, corr=8.0,
+                  discharge=20.0, stage=3.0, outlet_bed=-1.0, slope=2e-3, cfl=0.9):
+    """A few hundred cells with the same physics as config 1 (for parity tests)."""
+    return channel(length, width, spacing, 1.0, seed, sigma, corr, slope, outlet_bed, stage,
+                   discharge, 0.03, cfl, field_resolution=0.5)
+
+
+def lake_at_rest(length=80.0, width=40.0, spacing=4.0, seed=11, islands=True):
+    """Variable bed with emerged islands, flat surface at 1.0 m, closed walls (no open segments)."""
+    mesh = M.channel_mesh(length, width, spacing, 1.0, seed)
+    mesh.bid[:] = -1
+    mesh.boundary_offset = np.zeros(1, np.int32)
+    mesh.boundary_faces = np.zeros(0, np.int32)
+    x, y = mesh.xy
+    z = 0.4 * np.sin(x / 9.0) * np.cos(y / 7.0)
+    if islands:
+        z = z + 1.6 * np.exp(-((x - 0.3 * length) ** 2 + (y - 0.5 * width) ** 2) / 40.0)
+        z = z + 1.3 * np.exp(-((x - 0.7 * length) ** 2 + (y - 0.3 * width) ** 2) / 25.0)
+    z = np.ascontiguousarray(z)
+    h = np.maximum(1.0 - z, 0.0)
+    q = np.ascontiguousarray(np.stack((h, np.zeros_like(h), np.zeros_like(h))))
+    return dict(mesh=mesh, z=z, q=q, seg_mode=np.zeros(0, np.int32), stage_policy=np.zeros(0, np.int32),
+                forcing=np.zeros((2, 1)), exterior_bed=np.zeros(mesh.nf),
+                controls=controls(0.9, 0.03), name="lake_at_rest")
+
+
+def dam_break(length=200.0, width=8.0, spacing=2.0, seed=13, h_left=2.0, h_right=0.0):
+    """Dam break on a flat frictionless bed; h_right = 0 gives the dry-bed (Ritter) case."""
+    mesh = M.channel_mesh(length, width, spacing, 0.4, seed)
+    mesh.bid[:] = -1
+    mesh.boundary_offset = np.zeros(1, np.int32)
+    mesh.boundary_faces = np.zeros(0, np.int32)
+    x = mesh.xy[0]
+    z = np.zeros(mesh.nc)
+    h = np.where(x < 0.5 * length, h_left, h_right)
+    q = np.ascontiguousarray(np.stack((h, np.zeros_like(h), np.zeros_like(h))))
+    ctl = controls(0.9, 0.03)
+    ctl["roughness_mode"] = 1
+    ctl["roughness_value"] = 1e12          # Chezy -> infinity: frictionless
+    return dict(mesh=mesh, z=z, q=q, seg_mode=np.zeros(0, np.int32), stage_policy=np.zeros(0, np.int32),
+                forcing=np.zeros((2, 1)), exterior_bed=np.zeros(mesh.nf), controls=ctl, name="dam_break")
+
+
+def perturbed_state(case, seed, amplitude=0.3, velocity=0.6, dry_fraction=0.0):
+    """A random but physical state on the case's bed: surface waves, currents and optional dry cells."""
+    rng = np.random.default_rng(seed)
+    z = case["z"]
+    eta = case["q"][0] + z
+    eta = eta + amplitude * rng.uniform(-1, 1, eta.shape)
+    h = np.maximum(eta - z, 0.0)
+    if dry_fraction > 0:
+        h[rng.random(h.shape) < dry_fraction] = 0.0
+    u = velocity * rng.uniform(-1, 1, h.shape)
+    v = velocity * rng.uniform(-1, 1, h.shape)
+    return np.ascontiguousarray(np.stack((h, h * u, h * v)))

@@ -1,0 +1,1257 @@
+/*
+ * CPU oracle of the BRAIDS-HKT augmented f-wave river step.
+ *
+ * TEST INFRASTRUCTURE ONLY. This file is the checker that the CUDA path is
+ * compared against; nothing in the product links, loads or calls it. It is
+ * used by tests/, by __graft_entry__.smoke() and by bench.py's CPU-baseline
+ * leg.
+ *
+ * It restates, in plain C with FMA contraction disabled (-ffp-contract=off),
+ * the FP64 arithmetic the reference generates for this path after its own
+ * source transforms, and the Python orchestration around it:
+ *
+ *   spatial residual  src/braids_core/sediment/river_midpoint.py:100-176
+ *   SSPRK(2,2) stage  src/braids_core/sediment/river_explicit.py:63-119
+ *   substep control   src/braids_core/sediment/river_explicit.py:121-154
+ *   reconstruction    src/braids_support/gpu_fwave/reconstruction.cu:24-212
+ *                     + wall_bed_hydraulics.cuda_source transforms
+ *                       (src/braids_core/sediment/wall_bed_hydraulics.py:32-36)
+ *   face preparation  src/braids_support/gpu_fwave/resident_update.cu:11-55
+ *                     + hydrostatic reconstruction transform
+ *                       (src/braids_support/sediment/river_morphodynamics/hydrostatic_step_probe.py:37-57,
+ *                        face_activity.py:30-37)
+ *   augmented f-wave  src/braids_support/gpu_fwave/augmented_fwave.cu:28-334
+ *   flux assembly     src/braids_support/gpu_fwave/resident_update.cu:57-148
+ *                     + reflecting wall (src/braids_core/sediment/reflecting_wall.py:10-31,76-79)
+ *   CSR gather        src/braids_gpu/implicit_midpoint_fwave.cu:65-90
+ *   positivity        src/braids_core/sediment/river_midpoint.h:13-41
+ *   boundary budget   src/braids_core/sediment/river_explicit_boundary_budget.py:37-54
+ *   outlet stock      src/braids_core/hydraulics/outlet_feasibility.py:25-38
+ *   exterior traces   src/braids_core/sediment/river_exterior_bed.h:29-174,
+ *                     river_exterior_bed.py:183-233
+ *   CFL frequency     src/braids_core/sediment/river_explicit.h:13-26
+ *   Manning drag      src/braids_core/sediment/river_hydraulic_drag.h:3-16,
+ *                     river_roughness.py:42-47
+ *
+ * Scope: meshes without WENO stencils or virtual-wall triangles (the
+ * generated Delaunay meshes), outlet_extension = 0, cells with at most 32
+ * faces (so the projection limiter always runs). Under those conditions the
+ * dead branches of the reference kernels are omitted here; the surviving
+ * arithmetic is kept operation for operation.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define OM_EPS 2.2204460492503131e-16
+#define OM_DBL_MIN 2.2250738585072014e-308
+
+/* Rejection kinds, mirroring the reference's BendTrialRejected reasons. */
+enum { OM_OK = 0, OM_REJECT_SPATIAL = 1, OM_REJECT_CFL = 2, OM_REJECT_BUDGET = 3, OM_FAIL = 4 };
+
+typedef struct {
+    int nc, nf, nadj, nb;
+    const int *owner, *neighbour, *bid, *bmode, *offset, *faces, *signs;
+    const double *normal, *length, *area;          /* (2,nf) (nf) (nc) */
+    const double *ls_matrix, *ls_weight, *ls_delta; /* (4,nc) (nadj) (2,nadj) */
+    const double *disp, *disp_len, *distance;       /* (2,2,nf) (2,nf) (2,nf) */
+    const int *boundary_offset, *boundary_faces;    /* (nb+1) (sum) */
+    /* controls */
+    double grav, dry, cfl, speed_limit;
+    int roughness_mode;                            /* 1 chezy, 2 manning, 3/4 white-colebrook */
+    double roughness_value;
+    /* open boundaries */
+    const int *seg_mode;                           /* (nb) hydraulic mode per segment */
+    const int *stage_policy;                       /* (nb) */
+    const double *exterior_bed;                    /* (nf) exterior bed elevation on open faces */
+    double *forcing;                               /* (2,nb) row 0 discharge Q, row 1 stage */
+    /* forcing tables (optional): per segment piecewise-linear Q(t) and stage(t) */
+    int table_len;                                 /* 0 = constant forcing */
+    const double *table_time;                      /* (table_len) */
+    const double *table_value;                     /* (2, nb, table_len) */
+    int threads;
+} om_ctx;
+
+/* ------------------------------------------------------------------ */
+/* Small helpers                                                       */
+/* ------------------------------------------------------------------ */
+static inline int om_other(const om_ctx *m, int k)
+{
+    const int f = m->faces[k];
+    return m->signs[k] < 0 ? m->owner[f] : m->neighbour[f];
+}
+
+static inline int om_open(const om_ctx *m, int f)
+{
+    return m->neighbour[f] < 0 && m->bid[f] >= 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* GeoClaw Riemann type (riemanntype, maxiter = 1)                     */
+/* augmented_fwave.cu:33-105                                            */
+/* ------------------------------------------------------------------ */
+typedef struct { double hm, s1m, s2m; } om_rtype;
+
+static om_rtype om_riemann_type(double hL, double hR, double uL, double uR, double drytol, double g)
+{
+    om_rtype o;
+    const double hmin = fmin(hR, hL), hmax = fmax(hR, hL), delu = uR - uL;
+    if (hmin <= drytol) {
+        o.hm = 0.0;
+        o.s1m = uR + uL - 2.0 * sqrt(g * hR) + 2.0 * sqrt(g * hL);
+        o.s2m = o.s1m;
+        return o;
+    }
+    const double fmin_ = delu + 2.0 * (sqrt(g * hmin) - sqrt(g * hmax));
+    const double fmax_ = delu + (hmax - hmin) * sqrt(0.5 * g * (hmax + hmin) / (hmax * hmin));
+    if (fmin_ > 0.0) {                       /* two rarefactions */
+        const double root = fmax(0.0, -delu + 2.0 * (sqrt(g * hL) + sqrt(g * hR)));
+        o.hm = (1.0 / (16.0 * g)) * (root * root);
+        o.s1m = uL + 2.0 * sqrt(g * hL) - 3.0 * sqrt(g * o.hm);
+        o.s2m = uR - 2.0 * sqrt(g * hR) + 3.0 * sqrt(g * o.hm);
+    } else if (fmax_ <= 0.0) {               /* two shocks: one Newton step on sqrt(h) */
+        double h0 = hmax;
+        const double gL = sqrt(0.5 * g * (1.0 / h0 + 1.0 / hL));
+        const double gR = sqrt(0.5 * g * (1.0 / h0 + 1.0 / hR));
+        const double F0 = delu + (h0 - hL) * gL + (h0 - hR) * gR;
+        const double dfdh = gL - g * (h0 - hL) / (4.0 * (h0 * h0) * gL) +
+                            gR - g * (h0 - hR) / (4.0 * (h0 * h0) * gR);
+        const double slope = 2.0 * sqrt(h0) * dfdh;
+        const double root = sqrt(h0) - F0 / slope;
+        h0 = root * root;
+        o.hm = h0;
+        const double u1m = uL - (o.hm - hL) * sqrt((0.5 * g) * (1.0 / o.hm + 1.0 / hL));
+        const double u2m = uR + (o.hm - hR) * sqrt((0.5 * g) * (1.0 / o.hm + 1.0 / hR));
+        o.s1m = u1m - sqrt(g * o.hm);
+        o.s2m = u2m + sqrt(g * o.hm);
+    } else {                                 /* shock + rarefaction: one secant step */
+        double h0 = hmin;
+        const double F0 = delu + 2.0 * (sqrt(g * h0) - sqrt(g * hmax)) +
+                          (h0 - hmin) * sqrt(0.5 * g * (1.0 / h0 + 1.0 / hmin));
+        const double slope = (fmax_ - F0) / (hmax - hmin);
+        h0 = h0 - F0 / slope;
+        o.hm = h0;
+        if (hL > hR) {
+            o.s1m = uL + 2.0 * sqrt(g * hL) - 3.0 * sqrt(g * o.hm);
+            o.s2m = uL + 2.0 * sqrt(g * hL) - sqrt(g * o.hm);
+        } else {
+            o.s2m = uR - 2.0 * sqrt(g * hR) + 3.0 * sqrt(g * o.hm);
+            o.s1m = uR - 2.0 * sqrt(g * hR) + sqrt(g * o.hm);
+        }
+    }
+    return o;
+}
+
+static inline double om_det3(const double a[3][3])
+{
+    const double d1 = a[0][0] * (a[1][1] * a[2][2] - a[1][2] * a[2][1]);
+    const double d2 = a[0][1] * (a[1][0] * a[2][2] - a[1][2] * a[2][0]);
+    const double d3 = a[0][2] * (a[1][0] * a[2][1] - a[1][1] * a[2][0]);
+    return d1 - d2 + d3;
+}
+
+/* ------------------------------------------------------------------ */
+/* Augmented f-wave on one face, local normal/tangent frame.           */
+/* augmented_fwave.cu:115-262 (riemann_aug_JCP, maxiter 1, no rare     */
+/* corrector) and :264-334 (the rpn2 wrapper with dry-wall reflection). */
+/* out: [0:3] amdq, [3:6] apdq, [6:9] speeds, [9+3w+c] fwave(c, w).    */
+/* Returns the status word (0 ok, bit0 clamp, bit1 nonfinite, -1 bad). */
+/* ------------------------------------------------------------------ */
+int om_fwave_face(const double in[8], double grav, double drytol, double out[18])
+{
+    int status = 0;
+    for (int r = 0; r < 18; ++r) out[r] = 0.0;
+    int finite = isfinite(grav) && isfinite(drytol) && grav > 0.0 && drytol >= 0.0;
+    for (int r = 0; r < 8; ++r) finite = finite && isfinite(in[r]);
+    if (!finite) return -1;
+    double hL = in[0], huL = in[1], hvL = in[2], bL = in[3];
+    double hR = in[4], huR = in[5], hvR = in[6], bR = in[7];
+    if (hL < 0.0) { hL = 0.0; huL = 0.0; hvL = 0.0; status |= 1; }
+    if (hR < 0.0) { hR = 0.0; huR = 0.0; hvR = 0.0; status |= 1; }
+    if (hL <= drytol && hR <= drytol) return status;
+
+    double uL, uR, vL, vR, phiL, phiR;
+    if (hR > drytol) {
+        uR = huR / hR; vR = hvR / hR;
+        phiR = 0.5 * grav * (hR * hR) + (huR * huR) / hR;
+    } else { hR = 0.0; huR = 0.0; hvR = 0.0; uR = 0.0; vR = 0.0; phiR = 0.0; }
+    if (hL > drytol) {
+        uL = huL / hL; vL = hvL / hL;
+        phiL = 0.5 * grav * (hL * hL) + (huL * huL) / hL;
+    } else { hL = 0.0; huL = 0.0; hvL = 0.0; uL = 0.0; vL = 0.0; phiL = 0.0; }
+    double wall[3] = {1.0, 1.0, 1.0};
+    if (hR <= drytol) {
+        const om_rtype t = om_riemann_type(hL, hL, uL, -uL, drytol, grav);
+        const double hstar = fmax(hL, t.hm);
+        if (hstar + bL < bR) {
+            wall[1] = 0.0; wall[2] = 0.0;
+            hR = hL; huR = -huL; bR = bL; phiR = phiL; uR = -uL; vR = vL;
+        } else if (hL + bL < bR) bR = hL + bL;
+    } else if (hL <= drytol) {
+        const om_rtype t = om_riemann_type(hR, hR, -uR, uR, drytol, grav);
+        const double hstar = fmax(hR, t.hm);
+        if (hstar + bR < bL) {
+            wall[0] = 0.0; wall[1] = 0.0;
+            hL = hR; huL = -huR; bL = bR; phiL = phiR; uL = -uR; vL = vR;
+        } else if (hR + bR < bL) bL = hR + bR;
+    }
+    const double sL = uL - sqrt(grav * hL), sR = uR + sqrt(grav * hR);
+    const double uhat = (sqrt(grav * hL) * uL + sqrt(grav * hR) * uR) /
+                        (sqrt(grav * hR) + sqrt(grav * hL));
+    const double chat = sqrt(grav * 0.5 * (hR + hL));
+    double sE1 = fmin(sL, uhat - chat), sE2 = fmax(sR, uhat + chat);
+
+    /* riemann_aug_JCP */
+    const double g = grav;
+    double r[3][3], lambda[3], delta[3], beta[3], fw[3][3];
+    const double delh = hR - hL, delhu = huR - huL, delphi = phiR - phiL, delb = bR - bL;
+    const om_rtype t = om_riemann_type(hL, hR, uL, uR, drytol, g);
+    const double s1m = t.s1m, s2m = t.s2m;
+    lambda[0] = fmin(sE1, s2m);
+    lambda[2] = fmax(sE2, s1m);
+    sE1 = lambda[0];
+    sE2 = lambda[2];
+    const double hstarHLL = fmax((huL - huR + sE2 * hR - sE1 * hL) / (sE2 - sE1), 0.0);
+    for (int w = 0; w < 3; ++w) { r[0][w] = 1.0; r[1][w] = lambda[w]; r[2][w] = lambda[w] * lambda[w]; }
+    lambda[1] = 0.5 * (lambda[0] + lambda[2]);
+    r[0][1] = 0.0; r[1][1] = 0.0; r[2][1] = 1.0;
+
+    const double crit = fmax(drytol * g, 1.0e-6);
+    const double crit2 = sqrt(crit);
+    const double hbar = fmax(0.5 * (hL + hR), 0.0);
+    const double usum = uL + uR;
+    const double s1s2bar = 0.25 * (usum * usum) - g * hbar;
+    const double s1s2tilde = fmax(0.0, uL * uR) - g * hbar;
+    int sonic = 0;
+    if (fabs(s1s2bar) <= crit) sonic = 1;
+    else if (s1s2bar * s1s2tilde <= crit * crit) sonic = 1;
+    else if (s1s2bar * sE1 * sE2 <= crit * crit) sonic = 1;
+    else if (fmin(fabs(sE1), fabs(sE2)) < crit2) sonic = 1;
+    else if (sE1 < crit2 && s1m > -crit2) sonic = 1;
+    else if (sE2 > -crit2 && s2m < crit2) sonic = 1;
+    else if ((uL + sqrt(g * hL)) * (uR + sqrt(g * hR)) < 0.0) sonic = 1;
+    else if ((uL - sqrt(g * hL)) * (uR - sqrt(g * hR)) < 0.0) sonic = 1;
+
+    double deldelh = sonic ? -delb : delb * g * hbar / s1s2bar;
+    if (sE1 < -crit && sE2 > crit) {
+        deldelh = fmin(deldelh, hstarHLL * (sE2 - sE1) / sE2);
+        deldelh = fmax(deldelh, hstarHLL * (sE2 - sE1) / sE1);
+    } else if (sE1 >= crit) {
+        deldelh = fmin(deldelh, hstarHLL * (sE2 - sE1) / sE1);
+        deldelh = fmax(deldelh, -hL);
+    } else if (sE2 <= -crit) {
+        deldelh = fmin(deldelh, hR);
+        deldelh = fmax(deldelh, hstarHLL * (sE2 - sE1) / sE2);
+    }
+    double deldelphi = sonic ? -g * hbar * delb : -delb * g * hbar * s1s2tilde / s1s2bar;
+    deldelphi = fmin(deldelphi, g * fmax(-hL * delb, -hR * delb));
+    deldelphi = fmax(deldelphi, g * fmin(-hL * delb, -hR * delb));
+    delta[0] = delh - deldelh;
+    delta[1] = delhu;
+    delta[2] = delphi - deldelphi;
+    const double det = om_det3(r);
+    for (int k = 0; k < 3; ++k) {
+        double a[3][3];
+        for (int w = 0; w < 3; ++w)
+            for (int c = 0; c < 3; ++c) a[c][w] = r[c][w];
+        a[0][k] = delta[0]; a[1][k] = delta[1]; a[2][k] = delta[2];
+        beta[k] = om_det3(a) / det;
+    }
+    for (int w = 0; w < 3; ++w) {
+        fw[w][0] = beta[w] * r[1][w];
+        fw[w][1] = beta[w] * r[2][w];
+        fw[w][2] = beta[w] * r[1][w];
+    }
+    fw[0][2] = fw[0][2] * vL;
+    fw[2][2] = fw[2][2] * vR;
+    fw[1][2] = 0.0;
+    const double hustar = huL + fw[0][0];
+    if (hustar <= 0.0)
+        fw[0][2] = fw[0][2] + (hR * uR * vR - hL * uL * vL - fw[0][2] - fw[2][2]);
+    else
+        fw[2][2] = fw[2][2] + (hR * uR * vR - hL * uL * vL - fw[0][2] - fw[2][2]);
+
+    double am[3] = {0.0, 0.0, 0.0}, ap[3] = {0.0, 0.0, 0.0};
+    for (int w = 0; w < 3; ++w) {
+        const double s = lambda[w] * wall[w];
+        out[6 + w] = s;
+        for (int c = 0; c < 3; ++c) {
+            const double v = fw[w][c] * wall[w];
+            out[9 + 3 * w + c] = v;
+            if (s < -1.0e-14) am[c] = am[c] + v;
+            else if (s > 1.0e-14) ap[c] = ap[c] + v;
+            else { am[c] = am[c] + 0.5 * v; ap[c] = ap[c] + 0.5 * v; }
+        }
+    }
+    for (int c = 0; c < 3; ++c) { out[c] = am[c]; out[3 + c] = ap[c]; }
+    for (int r2 = 0; r2 < 18; ++r2) if (!isfinite(out[r2])) status |= 2;
+    return status;
+}
+
+/* Exact reflecting-wall pressure (reflecting_wall.py:10-31). */
+static double om_wall_pressure(double h, double momentum, double g, double dry)
+{
+    if (h <= dry) return 0.0;
+    const double c = sqrt(g * h), v = momentum / h / c;
+    double ratio;
+    if (v <= 0.0) { const double a = fmax(0.0, 1.0 + 0.5 * v); ratio = a * a; }
+    else {
+        double lo = 1.0, hi = 1.0 + sqrt(2.0) * v, rr = 1.0 + v;
+        for (int k = 0; k < 32; ++k) {
+            const double s = sqrt(0.5 * (1.0 + 1.0 / rr));
+            const double f = (rr - 1.0) * s - v;
+            if (fabs(f) <= 2.e-15 * fmax(1.0, v)) break;
+            if (f > 0.0) hi = rr; else lo = rr;
+            const double df = s - (rr - 1.0) / (4.0 * s * rr * rr);
+            const double trial = rr - f / df;
+            rr = (trial > lo && trial < hi) ? trial : 0.5 * (lo + hi);
+        }
+        ratio = rr;
+    }
+    const double star = h * ratio;
+    return 0.5 * g * star * star;
+}
+
+/* ------------------------------------------------------------------ */
+/* Reconstruction                                                       */
+/* ------------------------------------------------------------------ */
+
+/* Primitive variables (eta, u, v, b), the active mask and the input
+ * status (reconstruction.cu:24-39). */
+void om_primitive(const om_ctx *m, const double *q, const double *z,
+                  double *v, int *active, int *status)
+{
+    const int nc = m->nc;
+#pragma omp parallel for schedule(static)
+    for (int c = 0; c < nc; ++c) {
+        const double h = q[c];
+        v[c] = h + z[c]; v[nc + c] = 0.0; v[2 * nc + c] = 0.0; v[3 * nc + c] = z[c];
+        if (h > m->dry) { v[nc + c] = q[nc + c] / h; v[2 * nc + c] = q[2 * nc + c] / h; }
+        int act = h > m->dry;
+        if (!act)
+            for (int k = m->offset[c]; k < m->offset[c + 1]; ++k) {
+                const int f = m->faces[k], n = om_other(m, k);
+                if (m->bid[f] >= 0 || (n >= 0 && q[n] > m->dry)) { act = 1; break; }
+            }
+        active[c] = act;
+        status[c] = (h < 0.0 || !isfinite(h) || !isfinite(z[c]) || !isfinite(q[nc + c]) ||
+                     !isfinite(q[2 * nc + c])) ? 1 : 0;
+    }
+}
+
+static int om_feasible(double x, double y, int count, const double *ax, const double *ay, const double *b)
+{
+    for (int i = 0; i < count; ++i)
+        if (ax[i] * x + ay[i] * y > b[i] + 2.e-14) return 0;
+    return 1;
+}
+
+/* Nearest point of the bound polygon to the unlimited gradient: candidates
+ * are single-constraint projections and pairwise vertices
+ * (braids_project_pair in the directional hydraulic limiter transform). */
+static void om_project(double *x, double *y, int count, const double *ax, const double *ay, const double *b)
+{
+    const double rx = *x, ry = *y;
+    if (om_feasible(rx, ry, count, ax, ay, b)) return;
+    double bx = 0.0, by = 0.0, best = rx * rx + ry * ry;
+    for (int i = 0; i < count; ++i) {
+        const double dot = ax[i] * rx + ay[i] * ry - b[i];
+        double cx = rx - dot * ax[i], cy = ry - dot * ay[i];
+        double d = (cx - rx) * (cx - rx) + (cy - ry) * (cy - ry);
+        if (d < best && om_feasible(cx, cy, count, ax, ay, b)) { bx = cx; by = cy; best = d; }
+        for (int j = 0; j < i; ++j) {
+            const double det = ax[i] * ay[j] - ay[i] * ax[j];
+            if (fabs(det) < 1.e-12) continue;
+            cx = (b[i] * ay[j] - ay[i] * b[j]) / det;
+            cy = (ax[i] * b[j] - b[i] * ax[j]) / det;
+            d = (cx - rx) * (cx - rx) + (cy - ry) * (cy - ry);
+            if (d < best && om_feasible(cx, cy, count, ax, ay, b)) { bx = cx; by = cy; best = d; }
+        }
+    }
+    *x = bx; *y = by;
+}
+
+/* Limited least-squares gradients and the flattening flag of every cell
+ * (transformed reconstruction_cells). grad is (4,2,nc): row 2m = d/dx, 2m+1 = d/dy. */
+void om_cells(const om_ctx *m, const double *q, const double *v, const int *active,
+              double *grad, int *constant)
+{
+    const int nc = m->nc, nf = m->nf, nadj = m->nadj;
+    const double dry = m->dry, grav = m->grav;
+#pragma omp parallel for schedule(static)
+    for (int c = 0; c < nc; ++c) {
+        double centre[4], lo[4], hi[4], gx[4] = {0, 0, 0, 0}, gy[4] = {0, 0, 0, 0};
+        for (int k = 0; k < 4; ++k) { centre[k] = v[k * nc + c]; lo[k] = centre[k]; hi[k] = centre[k]; }
+        const int k0 = m->offset[c], k1 = m->offset[c + 1];
+        if (active[c]) {
+            double bx[4] = {0, 0, 0, 0}, by[4] = {0, 0, 0, 0};
+            const double a11 = m->ls_matrix[c], a12 = m->ls_matrix[nc + c],
+                         a22 = m->ls_matrix[2 * nc + c], det = m->ls_matrix[3 * nc + c];
+            for (int k = k0; k < k1; ++k) {
+                const int n = om_other(m, k);
+                if (n < 0) continue;
+                const double rx = m->ls_delta[k], ry = m->ls_delta[nadj + k], w = m->ls_weight[k];
+                for (int p = 0; p < 4; ++p) {
+                    double adj = v[p * nc + n];
+                    /* a dry neighbour whose bed rises above the wet surface contributes the surface */
+                    if (p == 0 && centre[0] - centre[3] > dry && v[n] - v[3 * nc + n] <= dry &&
+                        v[3 * nc + n] >= centre[0]) adj = centre[0];
+                    bx[p] += w * rx * (adj - centre[p]);
+                    by[p] += w * ry * (adj - centre[p]);
+                    lo[p] = fmin(lo[p], adj); hi[p] = fmax(hi[p], adj);
+                }
+            }
+            if (a11 + a22 > 0.0) {
+                /* Wall-mirrored velocity bounds (wall_velocity_bounds transform). */
+                if (q[c] > dry)
+                    for (int k = k0; k < k1; ++k) {
+                        const int f = m->faces[k];
+                        if (m->neighbour[f] >= 0 || m->bid[f] >= 0) continue;
+                        const double nx = m->normal[f], ny = m->normal[nf + f];
+                        const double un = centre[1] * nx + centre[2] * ny;
+                        const double mx = centre[1] - 2. * un * nx, my = centre[2] - 2. * un * ny;
+                        lo[1] = fmin(lo[1], mx); hi[1] = fmax(hi[1], mx);
+                        lo[2] = fmin(lo[2], my); hi[2] = fmax(hi[2], my);
+                    }
+                for (int p = 0; p < 4; ++p) {
+                    if (det > 1.e-12 * ((a11 + a22) * (a11 + a22))) {
+                        gx[p] = (a22 * bx[p] - a12 * by[p]) / det;
+                        gy[p] = (a11 * by[p] - a12 * bx[p]) / det;
+                    } else {
+                        gx[p] = (a11 * bx[p] + a12 * by[p]) / ((a11 + a22) * (a11 + a22));
+                        gy[p] = (a12 * bx[p] + a22 * by[p]) / ((a11 + a22) * (a11 + a22));
+                    }
+                }
+                const double h = centre[0] - centre[3];
+                /* Barth-type factor for the velocities; eta and bed go through the projection below. */
+                double theta[4] = {1., 1., 1., 1.};
+                for (int k = k0; k < k1; ++k) {
+                    const int f = m->faces[k];
+                    const int side = m->signs[k] < 0;
+                    const double rx = m->disp[side * nf + f], ry = m->disp[(2 + side) * nf + f];
+                    if (om_open(m, f) && m->bmode[f] == 2 && h > dry &&
+                        fabs(centre[1] * m->normal[f] + centre[2] * m->normal[nf + f]) < sqrt(grav * h) &&
+                        fabs(gx[3] * rx + gy[3] * ry) > 64.0 * OM_EPS * fmax(1.0, fabs(centre[3]))) continue;
+                    for (int p = 1; p < 3; ++p) {
+                        const double d = gx[p] * rx + gy[p] * ry;
+                        if (fabs(d) <= 64.0 * OM_EPS * fmax(1.0, fmax(fabs(centre[p]), fmax(fabs(lo[p]), fabs(hi[p])))))
+                            continue;
+                        if (d > 0.) theta[p] = fmin(theta[p], (hi[p] - centre[p]) / d);
+                        if (d < 0.) theta[p] = fmin(theta[p], (lo[p] - centre[p]) / d);
+                    }
+                }
+                double px[2] = {gx[0], gx[3]}, py[2] = {gy[0], gy[3]};
+                for (int a = 0; a < 2; ++a) {
+                    const int p = a ? 3 : 0;
+                    double ax[64], ay[64], b[64];
+                    int count = 0;
+                    for (int k = k0; k < k1; ++k) {
+                        const int f = m->faces[k];
+                        const int side = m->signs[k] < 0;
+                        const double rx = m->disp[side * nf + f], ry = m->disp[(2 + side) * nf + f];
+                        const double len = m->disp_len[side * nf + f];
+                        if (om_open(m, f) && m->bmode[f] == 2 && h > dry &&
+                            fabs(centre[1] * m->normal[f] + centre[2] * m->normal[nf + f]) < sqrt(grav * h) &&
+                            fabs(gx[3] * rx + gy[3] * ry) > 64.0 * OM_EPS * fmax(1.0, fabs(centre[3]))) continue;
+                        if (len <= 0. || (p == 3 && m->neighbour[f] < 0 && m->bid[f] < 0)) continue;
+                        ax[count] = rx / len; ay[count] = ry / len; b[count++] = fmax(0., hi[p] - centre[p]) / len;
+                        ax[count] = -rx / len; ay[count] = -ry / len; b[count++] = fmax(0., centre[p] - lo[p]) / len;
+                    }
+                    om_project(&px[a], &py[a], count, ax, ay, b);
+                }
+                for (int p = 1; p < 3; ++p) { gx[p] *= fmax(0., theta[p]); gy[p] *= fmax(0., theta[p]); }
+                gx[0] = px[0]; gy[0] = py[0]; gx[3] = px[1]; gy[3] = py[1];
+            }
+        }
+        /* Wet/dry flattening: a reconstructed face depth at or below dry, or a
+         * face bed departing from the cell bed by at least the depth. */
+        int flatten = q[c] <= dry;
+        if (!flatten)
+            for (int k = k0; k < k1; ++k) {
+                const int f = m->faces[k];
+                const int side = (c == m->owner[f]) ? 0 : 1;
+                const double rx = m->disp[side * nf + f], ry = m->disp[(2 + side) * nf + f];
+                const double eta = (centre[0] + gx[0] * rx) + gy[0] * ry;
+                const double zb = (centre[3] + gx[3] * rx) + gy[3] * ry;
+                if (eta - zb <= dry || fabs(zb - centre[3]) >= q[c]) { flatten = 1; break; }
+            }
+        constant[c] = flatten;
+        for (int p = 0; p < 4; ++p) { grad[(2 * p) * nc + c] = gx[p]; grad[(2 * p + 1) * nc + c] = gy[p]; }
+    }
+}
+
+/* Face traces (10,nf) and kinds (reconstruction.cu:170-212): rows 0-3 left
+ * h,hu,hv,b; 4-7 right; 8-9 raw depths. Kind 0 dry, 1 interior, 2 wall, 3 open. */
+void om_faces(const om_ctx *m, const double *q, const double *v, const double *grad,
+              const int *constant, double *trace, int *kind, int *status)
+{
+    const int nc = m->nc, nf = m->nf;
+    const double dry = m->dry;
+#pragma omp parallel for schedule(static)
+    for (int f = 0; f < nf; ++f) {
+        status[f] = 0;
+        for (int j = 0; j < 10; ++j) trace[j * nf + f] = 0.0;
+        const int c = m->owner[f], n = m->neighbour[f];
+        int type = n >= 0 ? 1 : (m->bid[f] < 0 ? 2 : 3);
+        if (m->bid[f] < 0 && q[c] <= dry && (n < 0 || q[n] <= dry)) type = 0;
+        kind[f] = type;
+        for (int side = 0; side < 2; ++side) {
+            const int cell = side == 0 ? c : n;
+            if (cell < 0) continue;
+            double val[4];
+            const double rx = m->disp[side * nf + f], ry = m->disp[(2 + side) * nf + f];
+            for (int p = 0; p < 4; ++p)
+                val[p] = (v[p * nc + cell] + grad[(2 * p) * nc + cell] * rx) + grad[(2 * p + 1) * nc + cell] * ry;
+            if (constant[cell]) {
+                for (int p = 0; p < 3; ++p) val[p] = v[p * nc + cell];
+                if (v[cell] - v[3 * nc + cell] <= dry) val[3] = v[3 * nc + cell];
+            }
+            for (int p = 0; p < 4; ++p) if (!isfinite(val[p])) status[f] |= 1;
+            if (type == 0) continue;
+            double depth = fmax(val[0] - val[3], 0.);
+            trace[(8 + side) * nf + f] = depth;
+            if (q[cell] <= dry || (constant[cell] && depth <= dry)) depth = 0.;
+            trace[(4 * side) * nf + f] = depth;
+            trace[(4 * side + 1) * nf + f] = depth * val[1];
+            trace[(4 * side + 2) * nf + f] = depth * val[2];
+            trace[(4 * side + 3) * nf + f] = val[3];
+        }
+        if (type == 2) {
+            for (int j = 0; j < 4; ++j) trace[(4 + j) * nf + f] = trace[j * nf + f];
+            trace[9 * nf + f] = trace[8 * nf + f];
+        }
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* Face flux                                                            */
+/* ------------------------------------------------------------------ */
+
+/* Rotation, hydrostatic reconstruction at the common face bed and the
+ * closed-face test (transformed resident_prepare_faces). */
+void om_prepare(const om_ctx *m, const double *trace, const double *q, const double *z,
+                const int *kind, double *local, int *closed)
+{
+    const int nf = m->nf;
+    const double dry = m->dry, grav = m->grav;
+#pragma omp parallel for schedule(static)
+    for (int f = 0; f < nf; ++f) {
+        for (int j = 0; j < 8; ++j) local[j * nf + f] = 0.0;
+        closed[f] = 0;
+        if (kind[f] == 0 || kind[f] == 3) continue;
+        const int c = m->owner[f], n = m->neighbour[f];
+        const double nx = m->normal[f], ny = m->normal[nf + f];
+        double hL = trace[f], xL = trace[nf + f], yL = trace[2 * nf + f], bL = trace[3 * nf + f];
+        double hR = trace[4 * nf + f], xR = trace[5 * nf + f], yR = trace[6 * nf + f], bR = trace[7 * nf + f];
+        if (kind[f] == 2) {
+            hR = hL; bR = bL;
+            const double dot = xL * nx + yL * ny;
+            xR = xL - 2.0 * dot * nx; yR = yL - 2.0 * dot * ny;
+        }
+        const double unL = xL * nx + yL * ny, utL = xL * (-ny) + yL * nx;
+        const double unR = xR * nx + yR * ny, utR = xR * (-ny) + yR * nx;
+        local[f] = hL; local[nf + f] = unL; local[2 * nf + f] = utL; local[3 * nf + f] = bL;
+        local[4 * nf + f] = hR; local[5 * nf + f] = unR; local[6 * nf + f] = utR; local[7 * nf + f] = bR;
+        if (kind[f] == 1) {
+            const double top = fmax(bL, bR);
+            const double tol = 16. * OM_EPS * fmax(dry, fmax(fabs(top), fmax(fabs(hL + bL), fabs(hR + bR))));
+            double hl = fmax(0., hL + bL - top), hr = fmax(0., hR + bR - top);
+            if (hl <= dry + tol) hl = 0.;
+            if (hr <= dry + tol) hr = 0.;
+            local[f] = hl; local[3 * nf + f] = top; local[4 * nf + f] = hr; local[7 * nf + f] = top;
+            local[nf + f] = hL > dry ? unL * (hl / hL) : 0.;
+            local[2 * nf + f] = hL > dry ? utL * (hl / hL) : 0.;
+            local[5 * nf + f] = hR > dry ? unR * (hr / hR) : 0.;
+            local[6 * nf + f] = hR > dry ? utR * (hr / hR) : 0.;
+        }
+        if (kind[f] != 1 || fmin(q[c], q[n]) > dry) continue;
+        const double dc = m->distance[f], dn = m->distance[nf + f];
+        double shared;
+        if (dc + dn > OM_DBL_MIN)
+            shared = (dn * (z[c] + q[c]) + dc * (z[n] + q[n])) / (dc + dn) - fmax(z[c], z[n]);
+        else
+            shared = 0.5 * ((z[c] + q[c]) + (z[n] + q[n])) - fmax(z[c], z[n]);
+        int blocked = shared <= dry;
+        if (blocked) {
+            int opens = 0;
+            if (hL > dry && hR <= dry && unL / hL > 0.0) {
+                const om_rtype t = om_riemann_type(hL, hL, unL / hL, -unL / hL, dry, grav);
+                opens = t.hm > hL + dry && t.hm + bL > bR + dry;
+            } else if (hR > dry && hL <= dry && -unR / hR > 0.0) {
+                const om_rtype t = om_riemann_type(hR, hR, -unR / hR, unR / hR, dry, grav);
+                opens = t.hm > hR + dry && t.hm + bR > bL + dry;
+            }
+            blocked = !opens;
+        }
+        closed[f] = blocked;
+    }
+}
+
+void om_fwave(const om_ctx *m, const double *local, double *riemann, int *status)
+{
+    const int nf = m->nf;
+#pragma omp parallel for schedule(static)
+    for (int f = 0; f < nf; ++f) {
+        double in[8], out[18];
+        for (int j = 0; j < 8; ++j) in[j] = local[j * nf + f];
+        status[f] = om_fwave_face(in, m->grav, m->dry, out);
+        for (int j = 0; j < 18; ++j) riemann[j * nf + f] = out[j];
+    }
+}
+
+/* Left/right physical fluxes with the within-cell hydrostatic bed source
+ * (transformed resident_assemble_flux). Open faces (kind 3) are left to the
+ * exterior owner, which replaces them wholesale. */
+void om_assemble(const om_ctx *m, const double *trace, const double *local, const double *riemann,
+                 const double *q, const double *z, const int *kind, const int *hydro_constant,
+                 const int *closed, double *fl, double *fr, double *speed, int *face_status)
+{
+    const int nf = m->nf;
+    const double dry = m->dry, grav = m->grav;
+#pragma omp parallel for schedule(static)
+    for (int f = 0; f < nf; ++f) {
+        face_status[f] = 0; speed[f] = 0.0;
+        for (int j = 0; j < 3; ++j) { fl[j * nf + f] = 0.0; fr[j * nf + f] = 0.0; }
+        if (kind[f] == 0 || kind[f] == 3) continue;
+        const int c = m->owner[f], n = m->neighbour[f];
+        const double nx = m->normal[f], ny = m->normal[nf + f], hL = trace[f];
+        const double hR = kind[f] == 2 ? hL : trace[4 * nf + f];
+        double l[3] = {0, 0, 0}, r[3] = {0, 0, 0}, s = 0.0;
+        if (closed[f]) {
+            l[1] = 0.5 * grav * (hL * hL) * nx; l[2] = 0.5 * grav * (hL * hL) * ny;
+            r[1] = 0.5 * grav * (hR * hR) * nx; r[2] = 0.5 * grav * (hR * hR) * ny;
+            if (hL > dry) s = fmax(s, fabs(local[nf + f] / hL) + sqrt(grav * hL));
+            if (hR > dry) s = fmax(s, fabs(local[5 * nf + f] / hR) + sqrt(grav * hR));
+        } else {
+            const double starL = local[f], starR = local[4 * nf + f];
+            double pl[3] = {0, 0, 0}, pr[3] = {0, 0, 0};
+            if (starL > dry) {
+                const double hu = local[nf + f], hv = local[2 * nf + f];
+                pl[0] = hu; pl[1] = (hu * hu) / starL + 0.5 * grav * (starL * starL); pl[2] = hu * hv / starL;
+            }
+            if (starR > dry) {
+                const double hu = local[5 * nf + f], hv = local[6 * nf + f];
+                pr[0] = hu; pr[1] = (hu * hu) / starR + 0.5 * grav * (starR * starR); pr[2] = hu * hv / starR;
+            }
+            for (int j = 0; j < 3; ++j) { pl[j] += riemann[j * nf + f]; pr[j] -= riemann[(3 + j) * nf + f]; }
+            l[0] = pl[0]; l[1] = pl[1] * nx + pl[2] * (-ny); l[2] = pl[1] * ny + pl[2] * nx;
+            r[0] = pr[0]; r[1] = pr[1] * nx + pr[2] * (-ny); r[2] = pr[1] * ny + pr[2] * nx;
+            if (fabs(l[0] - r[0]) > 1.e-10 * fmax(1.0, fmax(fabs(l[0]), fabs(r[0])))) face_status[f] = 1;
+            l[0] = 0.5 * (l[0] + r[0]); r[0] = l[0];
+            s = fmax(fabs(riemann[6 * nf + f]), fmax(fabs(riemann[7 * nf + f]), fabs(riemann[8 * nf + f])));
+            if (kind[f] == 1) {
+                const double cl = .5 * grav * (hL * hL - starL * starL), cr = .5 * grav * (hR * hR - starR * starR);
+                l[1] += cl * nx; l[2] += cl * ny; r[1] += cr * nx; r[2] += cr * ny;
+            }
+            if (kind[f] == 2) {
+                l[0] = 0.0;
+                const double pressure = om_wall_pressure(hL, local[nf + f], grav, dry);
+                l[1] = pressure * nx; l[2] = pressure * ny;
+                for (int j = 0; j < 3; ++j) r[j] = l[j];
+            }
+        }
+        if (q[c] > dry) {
+            const double corr = hydro_constant[c] ? 0.5 * grav * (q[c] * q[c] - hL * hL)
+                                                  : 0.5 * grav * (q[c] + trace[8 * nf + f]) * (trace[3 * nf + f] - z[c]);
+            l[1] += corr * nx; l[2] += corr * ny;
+        }
+        if (n >= 0) {
+            if (q[n] > dry) {
+                const double corr = hydro_constant[n] ? 0.5 * grav * (q[n] * q[n] - hR * hR)
+                                                      : 0.5 * grav * (q[n] + trace[9 * nf + f]) * (trace[7 * nf + f] - z[n]);
+                r[1] += corr * nx; r[2] += corr * ny;
+            }
+        } else for (int j = 0; j < 3; ++j) r[j] = l[j];
+        speed[f] = s;
+        for (int j = 0; j < 3; ++j) {
+            fl[j * nf + f] = l[j]; fr[j * nf + f] = r[j];
+            if (!isfinite(l[j]) || !isfinite(r[j])) face_status[f] |= 4;
+        }
+    }
+}
+
+/* rate = -sum_k s_k len/A (f - g h^2/2 n) over active cells (implicit_full_rate_from_faces). */
+void om_gather(const om_ctx *m, const double *q, const double *fl, const double *fr,
+               const int *active, double *rate)
+{
+    const int nc = m->nc, nf = m->nf;
+#pragma omp parallel for schedule(static)
+    for (int c = 0; c < nc; ++c) {
+        for (int j = 0; j < 3; ++j) rate[j * nc + c] = 0.0;
+        if (!active[c]) continue;
+        double sum[3] = {0, 0, 0};
+        const double pressure = .5 * m->grav * q[c] * q[c];
+        for (int k = m->offset[c]; k < m->offset[c + 1]; ++k) {
+            const int f = m->faces[k];
+            const double w = m->length[f] / m->area[c];
+            if (m->signs[k] > 0) {
+                sum[0] += w * fl[f];
+                sum[1] += w * (fl[nf + f] - pressure * m->normal[f]);
+                sum[2] += w * (fl[2 * nf + f] - pressure * m->normal[nf + f]);
+            } else {
+                sum[0] -= w * fr[f];
+                sum[1] -= w * (fr[nf + f] - pressure * m->normal[f]);
+                sum[2] -= w * (fr[2 * nf + f] - pressure * m->normal[nf + f]);
+            }
+        }
+        for (int j = 0; j < 3; ++j) rate[j * nc + c] = -sum[j];
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* Open boundaries (exterior owner)                                     */
+/* ------------------------------------------------------------------ */
+
+static double om_exterior_chezy(int mode, double h, double parameter, double floor_, double gravity, int waqua)
+{
+    const double d = fmax(h, floor_);
+    if (mode == 1) return parameter;
+    if (mode == 2) return pow(d, 1. / 6.) / parameter;
+    return waqua ? 18. * log10(12. * fmax(.5, d / parameter))
+                 : sqrt(gravity) / .41 * log1p(30. * d / (exp(1.) * parameter));
+}
+
+/* Outward 1-wave half-Riemann state with a prescribed exterior depth. */
+static int om_stage_wave(double h, double un, double target, double gravity, double *depth, double *velocity)
+{
+    const double c = sqrt(gravity * h);
+    *depth = h; *velocity = un;
+    if (target > h) {
+        const double k = sqrt(.5 * gravity * (1. / target + 1. / h));
+        const double shock = un - target * k;
+        if (shock >= 0.) return 0;
+        *depth = target; *velocity = un - (target - h) * k;
+        return 1;
+    }
+    if (un - c >= 0.) return 0;
+    const double cb = sqrt(gravity * target), ub = un + 2. * (c - cb);
+    if (ub - cb > 0. || target == 0.) {
+        *velocity = (un + 2. * c) / 3.; *depth = (*velocity) * (*velocity) / gravity;
+        return 2;
+    }
+    *depth = target; *velocity = ub;
+    return 1;
+}
+
+/* Per-segment sums in tiles of 64 faces, then over tiles: the fixed
+ * reduction tree of exterior_partial / exterior_totals. */
+static void om_segment_sums(const om_ctx *m, const double *input, int fields, double *result)
+{
+    const int nb = m->nb, nf = m->nf;
+    int longest = 0;
+    for (int b = 0; b < nb; ++b) {
+        const int len = m->boundary_offset[b + 1] - m->boundary_offset[b];
+        if (len > longest) longest = len;
+    }
+    int tiles = (longest + 63) / 64;
+    if (tiles < 1) tiles = 1;
+    for (int field = 0; field < fields; ++field)
+        for (int b = 0; b < nb; ++b) {
+            double total = 0.0;
+            const int end = m->boundary_offset[b + 1];
+            for (int tile = 0; tile < tiles; ++tile) {
+                double sum = 0.0;
+                for (int k = m->boundary_offset[b] + 64 * tile; k < end && k < m->boundary_offset[b] + 64 * (tile + 1); ++k)
+                    sum += input[field * nf + m->boundary_faces[k]];
+                total += sum;
+            }
+            result[field * nb + b] = total;
+        }
+}
+
+/* Sample piecewise-linear forcing tables at time t into forcing (2,nb). */
+void om_sample_forcing(om_ctx *m, double t)
+{
+    if (m->table_len <= 0) return;
+    const int L = m->table_len, nb = m->nb;
+    for (int row = 0; row < 2; ++row)
+        for (int b = 0; b < nb; ++b) {
+            const double *y = m->table_value + ((size_t)row * nb + b) * L;
+            double val;
+            if (t <= m->table_time[0]) val = y[0];
+            else if (t >= m->table_time[L - 1]) val = y[L - 1];
+            else {
+                int i = 0;
+                while (m->table_time[i + 1] < t) ++i;
+                const double s = (t - m->table_time[i]) / (m->table_time[i + 1] - m->table_time[i]);
+                val = y[i] + (y[i + 1] - y[i]) * s;
+            }
+            m->forcing[row * nb + b] = val;
+        }
+}
+
+/* Exterior traces and fluxes on open faces (ExteriorBed.evaluate).
+ * work needs 3*nf doubles; stage_out (2,nb), total_out (nb). Returns 0 or
+ * the first nonzero face status. */
+int om_exterior(om_ctx *m, const double *q, const double *z, double time,
+                double *trace, double *flux, int *status, double *work,
+                double *stage_out, double *total_out)
+{
+    const int nc = m->nc, nf = m->nf, nb = m->nb;
+    const double dry = m->dry, gravity = m->grav;
+    om_sample_forcing(m, time);
+    const double *forcing = m->forcing;
+    double *terms = work, *weights = work + 2 * (size_t)nf;
+    for (int f = 0; f < nf; ++f) {
+        const int c = m->owner[f];
+        const double w = om_open(m, f) && q[c] > dry ? m->length[f] : 0.;
+        terms[f] = (z[c] + q[c]) * w;
+        terms[nf + f] = w;
+    }
+    om_segment_sums(m, terms, 2, stage_out);
+    const int rmode = m->roughness_mode < 3 ? m->roughness_mode : 3;
+    const int waqua = m->roughness_mode == 4;
+    for (int f = 0; f < nf; ++f) {
+        weights[f] = 0.;
+        if (!om_open(m, f)) continue;
+        const int b = m->bid[f], c = m->owner[f];
+        const double *bed = m->exterior_bed;
+        if (m->seg_mode[b] == 9) {
+            const double h = fmax(forcing[nb + b] - bed[f], 0.);
+            if (h > dry) weights[f] = h * m->length[f];
+            continue;
+        }
+        if (m->seg_mode[b] != 6 || stage_out[nb + b] <= 0.) continue;
+        const double h = fmax(q[c] + z[c] - bed[f], 0.);
+        const double section = fmax(stage_out[b] / stage_out[nb + b] - bed[f], 0.);
+        if (h > dry && section > 0.)
+            weights[f] = pow(section, 1.5) * om_exterior_chezy(rmode, h, m->roughness_value, dry, gravity, waqua) * m->length[f];
+    }
+    om_segment_sums(m, weights, 1, total_out);
+    int first = 0;
+    for (int i = 0; i < nf; ++i) {
+        status[i] = 0;
+        for (int k = 0; k < 3; ++k) { trace[k * nf + i] = 0.; flux[k * nf + i] = 0.; }
+        if (!om_open(m, i)) continue;
+        const int b = m->bid[i], c = m->owner[i], mode = m->seg_mode[b];
+        const double h0 = q[c], nx = m->normal[i], ny = m->normal[nf + i], bed = m->exterior_bed[i];
+        if (mode == 4 || mode == 5 || mode == 10 || mode == 11) continue;
+        double h = fmax(h0 + z[c] - bed, 0.), geometric = h, ux = 0., uy = 0.;
+        if (h0 > dry) { ux = q[nc + c] / h0; uy = q[2 * nc + c] / h0; }
+        double un = ux * nx + uy * ny, tx = ux - un * nx, ty = uy - un * ny, normal_speed = 0.;
+        int st = 0;
+        if (mode == 9) {
+            h = fmax(forcing[nb + b] - bed, 0.); tx = ty = 0.;
+            const double Q = forcing[b];
+            if (Q > 0. && total_out[b] <= 0.) st = 1;
+            else if (h > dry && Q > 0.) normal_speed = -Q / total_out[b];
+        } else if (mode == 6) {
+            const double Q = forcing[b];
+            if (Q > 0. && total_out[b] <= 0.) st = 1;
+            else if (h > dry && Q > 0.) normal_speed = -Q * weights[i] / (total_out[b] * h * m->length[i]);
+        } else if (mode == 3) {
+            if (h0 <= dry) h = 0.;
+            else if (h > dry) {
+                if (un < sqrt(gravity * h)) st = 6;
+                else normal_speed = un;
+            }
+        } else if (mode == 2) {
+            const double prescribed = fmax(forcing[nb + b] - bed, 0.);
+            if (m->stage_policy[b] && (h0 <= dry || h <= dry) && prescribed > dry) st = 4;
+            else {
+                if (h0 <= dry) h = 0.;
+                if (h > dry) {
+                    const double wave = sqrt(gravity * h);
+                    if (un <= -wave) {
+                        if (m->stage_policy[b]) st = 5;
+                        else { normal_speed = 0.; tx = ty = 0.; }
+                    } else {
+                        const double target = fmax(forcing[nb + b] - bed, 0.);
+                        double hb, ub;
+                        om_stage_wave(h, un, target, gravity, &hb, &ub);
+                        if (ub < 0. && m->stage_policy[b]) {
+                            if (ub <= -sqrt(gravity * hb)) st = 5;
+                            else { h = hb; normal_speed = ub; tx = ty = 0.; }
+                        } else if (ub < 0.) { normal_speed = 0.; tx = ty = 0.; }
+                        else { h = hb; normal_speed = ub; }
+                    }
+                }
+            }
+        } else st = 2;
+        if (!st && (!isfinite(h) || !isfinite(normal_speed) || h < 0. ||
+                    sqrt(normal_speed * normal_speed + tx * tx + ty * ty) > m->speed_limit)) st = 3;
+        if (st) { status[i] = st; if (!first) first = st; continue; }
+        double water = 0., fx = 0., fy = 0.;
+        if (h > dry) {
+            trace[i] = h;
+            trace[nf + i] = h * (normal_speed * nx + tx);
+            trace[2 * nf + i] = h * (normal_speed * ny + ty);
+            water = trace[nf + i] * nx + trace[2 * nf + i] * ny;
+            fx = water * trace[nf + i] / h + .5 * gravity * h * h * nx;
+            fy = water * trace[2 * nf + i] / h + .5 * gravity * h * h * ny;
+        }
+        double pressure = h0 > dry ? .5 * gravity * (h0 * h0 - geometric * geometric) : 0.;
+        if (mode == 9 && h <= dry) pressure = h0 > dry ? .5 * gravity * h0 * h0 : 0.;
+        flux[i] = water; flux[nf + i] = fx + pressure * nx; flux[2 * nf + i] = fy + pressure * ny;
+    }
+    return first;
+}
+
+static int om_is_outlet(int mode)
+{
+    return mode == 2 || mode == 3 || mode == 4 || mode == 5 || mode == 10 || mode == 11;
+}
+
+/* Cap outward outlet flux by the owner's start-of-stage stock
+ * (OutletFeasibility.__call__). Sums follow the boundary face order.
+ * work needs 3*nc doubles (only boundary owners are touched). */
+void om_outlet_feasibility(const om_ctx *m, const double *base, double dt, double *flux, double *trace,
+                           double *work)
+{
+    const int nc = m->nc, nf = m->nf, nb = m->nb;
+    const int nbf = m->boundary_offset[nb];
+    double *total = work, *reserved = work + nc, *factor = work + 2 * (size_t)nc;
+    for (int k = 0; k < nbf; ++k) { const int c = m->owner[m->boundary_faces[k]]; total[c] = 0.0; reserved[c] = 0.0; }
+    for (int k = 0; k < nbf; ++k) {
+        const int f = m->boundary_faces[k], c = m->owner[f];
+        const int out = om_is_outlet(m->seg_mode[m->bid[f]]);
+        const double debit = fmax(flux[f], 0.) * m->length[f];
+        if (out) total[c] += debit; else reserved[c] += debit;
+    }
+    for (int k = 0; k < nbf; ++k) {
+        const int c = m->owner[m->boundary_faces[k]];
+        const double available = fmax(0., base[c] * m->area[c] / dt - reserved[c]);
+        const double ratio = fmin(1., available / fmax(total[c], 1e-300)) * (1. - 32. * OM_EPS);
+        factor[c] = total[c] > available ? ratio : 1.;
+    }
+    for (int k = 0; k < nbf; ++k) {
+        const int f = m->boundary_faces[k], c = m->owner[f];
+        const int out = om_is_outlet(m->seg_mode[m->bid[f]]);
+        const double water = flux[f];
+        const double scale = (out && water > 0.) ? factor[c] : 1.;
+        const double depth = trace[f], denom = fmax(depth, 1e-300);
+        const double ux = depth > 0. ? trace[nf + f] / denom : 0.;
+        const double uy = depth > 0. ? trace[2 * nf + f] / denom : 0.;
+        flux[nf + f] += (scale * scale - 1.) * water * ux;
+        flux[2 * nf + f] += (scale * scale - 1.) * water * uy;
+        flux[f] = water * scale;
+        trace[nf + f] *= scale;
+        trace[2 * nf + f] *= scale;
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* Positivity: donor inventory, boundary reservation, face limiting     */
+/* ------------------------------------------------------------------ */
+
+void om_inventory(const om_ctx *m, double dt, const double *base, const double *water, double *theta)
+{
+    const int nc = m->nc;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < nc; ++i) {
+        double out = 0.;
+        for (int k = m->offset[i]; k < m->offset[i + 1]; ++k) {
+            const int f = m->faces[k];
+            out += fmax(m->signs[k] * water[f], 0.) * m->length[f];
+        }
+        theta[i] = 1.;
+        if (out > 0. && dt * out >= base[i] * m->area[i])
+            theta[i] = fmin(1., base[i] * m->area[i] / (dt * out)) * (1. - 32. * 2.2204460492503131e-16);
+    }
+}
+
+/* Reserve prescribed boundary debits before limiting interior donors
+ * (ExplicitBoundaryBudget.reserve). Returns OM_REJECT_BUDGET when an open
+ * boundary alone would take more than the owner holds. */
+int om_reserve(const om_ctx *m, double dt, const double *base, const double *water, double *theta)
+{
+    const int nb = m->nb, nbf = m->boundary_offset[nb];
+    int reject = 0;
+    for (int kk = 0; kk < nbf; ++kk) {
+        const int c = m->owner[m->boundary_faces[kk]];
+        /* visit each boundary owner once: the first boundary face it owns */
+        int seen = 0;
+        for (int j = 0; j < kk; ++j) if (m->owner[m->boundary_faces[j]] == c) { seen = 1; break; }
+        if (seen) continue;
+        double ext = 0., interior = 0.;
+        for (int k = m->offset[c]; k < m->offset[c + 1]; ++k) {
+            const int f = m->faces[k];
+            const double debit = fmax(m->signs[k] * water[f], 0.) * m->length[f];
+            if (om_open(m, f)) ext += debit; else interior += debit;
+        }
+        const double available = base[c] * m->area[c] / dt;
+        if (ext > available) reject = 1;
+        const double factor = fmin(1., (available - ext) / fmax(interior, 1e-300)) * (1. - 32. * OM_EPS);
+        theta[c] = (interior > 0. && interior >= available - ext) ? factor : 1.;
+    }
+    return reject ? OM_REJECT_BUDGET : OM_OK;
+}
+
+/* Limit each donor's outgoing water by theta and move the removed
+ * advective momentum with it (midpoint_faces). Open faces keep their
+ * budgeted flux (they are restored by the boundary budget). */
+void om_limit_faces(const om_ctx *m, const double *q, const double *theta, double *water, double *correction)
+{
+    const int nc = m->nc, nf = m->nf;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < nf; ++i) {
+        correction[i] = 0.; correction[nf + i] = 0.;
+        if (water[i] == 0.) continue;
+        if (om_open(m, i)) continue;
+        const int donor = water[i] < 0. ? m->neighbour[i] : m->owner[i];
+        if (donor < 0 || theta[donor] == 1.) continue;
+        const double delta = (theta[donor] - 1.) * water[i];
+        water[i] *= theta[donor];
+        if (q[donor] > m->dry) {
+            correction[i] = delta * q[nc + donor] / q[donor];
+            correction[nf + i] = delta * q[2 * nc + donor] / q[donor];
+        }
+    }
+}
+
+/* Replace the mass rate with the limited water divergence and add the
+ * momentum corrections (midpoint_gather). */
+void om_limit_gather(const om_ctx *m, const double *water, const double *correction, double *rate)
+{
+    const int n = m->nc, nf = m->nf;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; ++i) {
+        double mass = 0., mx = 0., my = 0.;
+        for (int k = m->offset[i]; k < m->offset[i + 1]; ++k) {
+            const int f = m->faces[k];
+            const double w = m->signs[k] * m->length[f] / m->area[i];
+            mass -= w * water[f]; mx -= w * correction[f]; my -= w * correction[nf + f];
+        }
+        rate[i] = mass; rate[n + i] += mx; rate[2 * n + i] += my;
+    }
+}
+
+/* Face-sum CFL frequency per cell; open faces use the larger of the owner
+ * and exterior trace wave speeds (explicit_frequency). */
+double om_frequency(const om_ctx *m, const double *q, const double *speed, const double *ext_trace, double *freq)
+{
+    const int n = m->nc, nf = m->nf;
+    const double dry = m->dry, grav = m->grav;
+    double peak = 0.0;
+    int bad = 0;
+#pragma omp parallel for schedule(static) reduction(max:peak) reduction(|:bad)
+    for (int i = 0; i < n; ++i) {
+        double sum = 0.;
+        for (int k = m->offset[i]; k < m->offset[i + 1]; ++k) {
+            const int f = m->faces[k];
+            double s = speed[f];
+            if (om_open(m, f)) {
+                const int o = m->owner[f];
+                const double h = q[o], hb = ext_trace[f], nx = m->normal[f], ny = m->normal[nf + f];
+                const double a = h > dry ? fabs((q[n + o] * nx + q[2 * n + o] * ny) / h) + sqrt(grav * h) : 0.;
+                const double b = hb > dry ? fabs((ext_trace[nf + f] * nx + ext_trace[2 * nf + f] * ny) / hb) + sqrt(grav * hb) : 0.;
+                s = fmax(a, b);
+            }
+            sum += m->length[f] * s;
+        }
+        freq[i] = sum / m->area[i];
+        if (!isfinite(freq[i])) bad = 1;
+        if (freq[i] > peak) peak = freq[i];
+    }
+    return bad ? NAN : peak;
+}
+
+/* ------------------------------------------------------------------ */
+/* Manning / Chezy cell drag (river_cell_drag)                          */
+/* ------------------------------------------------------------------ */
+static double om_chezy(int method, double depth, double value)
+{
+    if (method == 1) return value;
+    if (method == 2) return pow(depth, 1. / 6.) / value;
+    if (method == 3) return sqrt(9.81) / .41 * log1p(30. * depth / (exp(1.) * value));
+    return 18. * log10(12. * fmax(.5, depth / value));
+}
+
+void om_drag(const om_ctx *m, double dt, double *q)
+{
+    const int n = m->nc;
+    const double g = m->grav, dry = m->dry;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; ++i) {
+        const double h = q[i];
+        if (h <= dry) { q[n + i] = q[2 * n + i] = 0.; continue; }
+        const double c = om_chezy(m->roughness_mode, h, m->roughness_value);
+        const double speed = sqrt(q[n + i] * q[n + i] + q[2 * n + i] * q[2 * n + i]) / h;
+        const double factor = 1. / (1. + dt * g * speed / (c * c * h));
+        q[n + i] *= factor; q[2 * n + i] *= factor;
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* Orchestration                                                        */
+/* ------------------------------------------------------------------ */
+
+/* Scratch for one spatial evaluation. */
+typedef struct {
+    double *v, *grad, *trace, *local, *riemann, *fl, *fr, *speed, *ext_trace, *ext_flux, *work,
+           *theta, *correction, *freq, *stage, *total;
+    int *active, *pstatus, *constant, *kind, *rstatus, *closed, *astatus, *fstatus, *estatus;
+} om_scratch;
+
+static void *om_alloc(size_t bytes) { void *p = calloc(bytes ? bytes : 1, 1); return p; }
+
+om_scratch *om_scratch_create(const om_ctx *m)
+{
+    const size_t nc = m->nc, nf = m->nf;
+    om_scratch *s = (om_scratch *)om_alloc(sizeof(om_scratch));
+    s->v = om_alloc(4 * nc * 8); s->grad = om_alloc(8 * nc * 8); s->trace = om_alloc(10 * nf * 8);
+    s->local = om_alloc(8 * nf * 8); s->riemann = om_alloc(18 * nf * 8); s->fl = om_alloc(3 * nf * 8);
+    s->fr = om_alloc(3 * nf * 8); s->speed = om_alloc(nf * 8); s->ext_trace = om_alloc(3 * nf * 8);
+    s->ext_flux = om_alloc(3 * nf * 8); s->work = om_alloc((3 * nf + 3 * nc) * 8); s->theta = om_alloc(nc * 8);
+    s->correction = om_alloc(2 * nf * 8); s->freq = om_alloc(nc * 8);
+    s->stage = om_alloc((2 * (size_t)m->nb + 1) * 8); s->total = om_alloc(((size_t)m->nb + 1) * 8);
+    s->active = om_alloc(nc * 4); s->pstatus = om_alloc(nc * 4); s->constant = om_alloc(nc * 4);
+    s->kind = om_alloc(nf * 4); s->rstatus = om_alloc(nf * 4); s->closed = om_alloc(nf * 4);
+    s->astatus = om_alloc(nf * 4); s->fstatus = om_alloc(nf * 4); s->estatus = om_alloc(nf * 4);
+    return s;
+}
+
+void om_scratch_destroy(om_scratch *s)
+{
+    if (!s) return;
+    void *all[] = {s->v, s->grad, s->trace, s->local, s->riemann, s->fl, s->fr, s->speed, s->ext_trace,
+                   s->ext_flux, s->work, s->theta, s->correction, s->freq, s->stage, s->total, s->active,
+                   s->pstatus, s->constant, s->kind, s->rstatus, s->closed, s->astatus, s->fstatus, s->estatus};
+    for (size_t i = 0; i < sizeof(all) / sizeof(all[0]); ++i) free(all[i]);
+    free(s);
+}
+
+/* One spatial residual (RiverMidpoint.rate + RiverExplicit.rate).
+ * q is the stage state, base the interval-start stock. Writes rate (3,nc)
+ * and the limited water flux (nf); *freq_out gets the max CFL frequency. */
+int om_rate(om_ctx *m, om_scratch *s, const double *q, const double *z, const double *base,
+            double dt, double time, double *rate, double *water, double *freq_out)
+{
+    const int nc = m->nc, nf = m->nf;
+    *freq_out = 0.0;
+    for (int i = 0; i < 3 * nc; ++i)
+        if (!isfinite(q[i])) return OM_REJECT_SPATIAL;
+    for (int i = 0; i < nc; ++i)
+        if (q[i] < 0) return OM_REJECT_SPATIAL;
+    if (m->nb > 0) {
+        if (om_exterior(m, q, z, time, s->ext_trace, s->ext_flux, s->estatus, s->work, s->stage, s->total))
+            return OM_REJECT_SPATIAL;
+        om_outlet_feasibility(m, base, dt, s->ext_flux, s->ext_trace, s->work);
+    }
+    om_primitive(m, q, z, s->v, s->active, s->pstatus);
+    om_cells(m, q, s->v, s->active, s->grad, s->constant);
+    om_faces(m, q, s->v, s->grad, s->constant, s->trace, s->kind, s->rstatus);
+    for (int f = 0; f < nf; ++f)
+        if (om_open(m, f)) for (int j = 0; j < 3; ++j) s->trace[j * nf + f] = s->ext_trace[j * nf + f];
+    om_prepare(m, s->trace, q, z, s->kind, s->local, s->closed);
+    om_fwave(m, s->local, s->riemann, s->astatus);
+    om_assemble(m, s->trace, s->local, s->riemann, q, z, s->kind, s->constant, s->closed,
+                s->fl, s->fr, s->speed, s->fstatus);
+    for (int f = 0; f < nf; ++f)
+        if (om_open(m, f)) {
+            for (int j = 0; j < 3; ++j) { s->fl[j * nf + f] = s->ext_flux[j * nf + f]; s->fr[j * nf + f] = s->ext_flux[j * nf + f]; }
+            s->fstatus[f] = s->estatus[f];
+        }
+    for (int c = 0; c < nc; ++c) if (s->pstatus[c]) return OM_REJECT_SPATIAL;
+    for (int f = 0; f < nf; ++f)
+        if (s->rstatus[f] || s->astatus[f] || s->fstatus[f]) return OM_REJECT_SPATIAL;
+    om_gather(m, q, s->fl, s->fr, s->active, rate);
+    memcpy(water, s->fl, sizeof(double) * nf);
+    om_inventory(m, dt, base, water, s->theta);
+    if (m->nb > 0 && om_reserve(m, dt, base, water, s->theta)) return OM_REJECT_BUDGET;
+    om_limit_faces(m, q, s->theta, water, s->correction);
+    om_limit_gather(m, water, s->correction, rate);
+    for (int i = 0; i < 3 * nc; ++i) if (!isfinite(rate[i])) return OM_REJECT_SPATIAL;
+    const double freq = om_frequency(m, q, s->speed, s->ext_trace, s->freq);
+    *freq_out = freq;
+    if (!isfinite(freq) || dt * freq > m->cfl * (1 + 1e-12)) return OM_REJECT_CFL;
+    return OM_OK;
+}
+
+/* One SSPRK(2,2) substep with Strang-split drag (RiverExplicit._single).
+ * out gets q2; water (nf) gets the stage-mean limited water flux;
+ * *peak the larger stage frequency seen (also on rejection). */
+int om_single(om_ctx *m, om_scratch *s, const double *base, const double *z, double dt, double time,
+              double *out, double *water, double *peak, double *tmp /* 9*nc + 2*nf */)
+{
+    const int nc = m->nc, nf = m->nf;
+    double *work = tmp, *r = tmp + 3 * (size_t)nc, *q1 = tmp + 6 * (size_t)nc;
+    double *w1 = tmp + 9 * (size_t)nc, *w2 = w1 + nf;
+    double f1 = 0.0, f2 = 0.0;
+    *peak = 0.0;
+    memcpy(work, base, sizeof(double) * 3 * nc);
+    om_drag(m, .5 * dt, work);
+    int st = om_rate(m, s, work, z, work, dt, time, r, w1, &f1);
+    if (isfinite(f1) && f1 > *peak) *peak = f1;
+    if (st) return st;
+    for (int i = 0; i < 3 * nc; ++i) q1[i] = work[i] + dt * r[i];
+    for (int i = 0; i < nc; ++i) if (q1[i] < 0) return OM_REJECT_SPATIAL;
+    for (int i = 0; i < nc; ++i) if (q1[i] <= m->dry) { q1[nc + i] = 0.; q1[2 * nc + i] = 0.; }
+    st = om_rate(m, s, q1, z, q1, dt, time + dt, r, w2, &f2);
+    if (isfinite(f2) && f2 > *peak) *peak = f2;
+    if (st) return st;
+    for (int i = 0; i < 3 * nc; ++i) out[i] = .5 * work[i] + .5 * (q1[i] + dt * r[i]);
+    for (int i = 0; i < 3 * nc; ++i) if (!isfinite(out[i])) return OM_REJECT_SPATIAL;
+    for (int i = 0; i < nc; ++i) if (out[i] < 0) return OM_REJECT_SPATIAL;
+    for (int i = 0; i < nc; ++i) if (out[i] <= m->dry) { out[nc + i] = 0.; out[2 * nc + i] = 0.; }
+    om_drag(m, .5 * dt, out);
+    for (int f = 0; f < nf; ++f) water[f] = .5 * (w1[f] + w2[f]);
+    return OM_OK;
+}
+
+typedef struct {
+    int substeps, rejections, status;
+    double min_dt, max_dt, accepted_cfl_max, hint;
+} om_stats;
+
+/* Adaptive substep loop over one outer interval dt (RiverExplicit.advance).
+ * q is advanced in place; water_mean (nf) gets the time-mean water flux.
+ * *hint carries the controller's step hint between calls (<= 0: none). */
+int om_advance(om_ctx *m, double *q, const double *z, double dt, double time, double *hint,
+               double *water_mean, om_stats *stats)
+{
+    const int nc = m->nc, nf = m->nf;
+    om_scratch *s = om_scratch_create(m);
+    double *tmp = om_alloc(sizeof(double) * (9 * (size_t)nc + 2 * (size_t)nf));
+    double *next = om_alloc(sizeof(double) * 3 * (size_t)nc), *w = om_alloc(sizeof(double) * nf);
+    double elapsed = 0.0, h = *hint > 0 ? *hint : dt;
+    const double floor_ = dt * ldexp(1.0, -20);
+    memset(stats, 0, sizeof(*stats));
+    memset(water_mean, 0, sizeof(double) * nf);
+    int status = OM_OK;
+    while (stats->substeps == 0 || elapsed < dt - 1e-13 * fmax(1., dt)) {
+        const double trial = fmin(h, dt - elapsed);
+        const int truncated = trial < h * (1 - 1e-12);
+        double peak = 0.0;
+        const int st = om_single(m, s, q, z, trial, time + elapsed, next, w, &peak, tmp);
+        if (st) {
+            stats->rejections++;
+            h = peak > 0 ? fmin(.5 * trial, .98 * m->cfl / peak) : .5 * trial;
+            if (h < floor_ || stats->rejections > 100) { status = st; break; }
+            continue;
+        }
+        memcpy(q, next, sizeof(double) * 3 * nc);
+        for (int f = 0; f < nf; ++f) water_mean[f] += trial * w[f];
+        elapsed += trial;
+        stats->substeps++;
+        if (stats->substeps == 1 || trial < stats->min_dt) stats->min_dt = trial;
+        if (trial > stats->max_dt) stats->max_dt = trial;
+        if (trial * peak > stats->accepted_cfl_max) stats->accepted_cfl_max = trial * peak;
+        const double growth = truncated ? h : 2 * trial;
+        h = peak > 0 ? fmin(growth, .98 * m->cfl / peak) : growth;
+        if (stats->substeps > 4096) { status = OM_FAIL; break; }
+    }
+    for (int f = 0; f < nf; ++f) water_mean[f] /= dt;
+    *hint = h;
+    stats->hint = h;
+    stats->status = status;
+    free(tmp); free(next); free(w);
+    om_scratch_destroy(s);
+    return status;
+}
+
+void om_set_threads(int n)
+{
+#ifdef _OPENMP
+    if (n > 0) { omp_set_dynamic(0); omp_set_num_threads(n); }
+#else
+    (void)n;
+#endif
+}
+
+size_t om_ctx_size(void) { return sizeof(om_ctx); }
+size_t om_stats_size(void) { return sizeof(om_stats); }

@@ -1,0 +1,247 @@
+"""Python driver of the C oracle (``braids_oracle.c``).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, ``__graft_entry__.smoke()`` and
+the CPU-baseline leg of ``bench.py`` as the checker. The product never
+imports this module.
+
+The library is compiled with FMA contraction disabled, matching the
+reference's own CPU build flags (src/braids_support/sediment/
+river_morphodynamics/sediment_wave.py:35, ``-ffp-contract=off``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+SOURCE = HERE / "braids_oracle.c"
+LIBRARY = HERE / "_build" / "libbraids_oracle.so"
+FLAGS = ["-O2", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-shared", "-fPIC", "-std=c11"]
+
+
+def build(force=False):
+    """Compile the oracle (idempotent). Returns the library path."""
+    LIBRARY.parent.mkdir(exist_ok=True)
+    if force or not LIBRARY.exists() or LIBRARY.stat().st_mtime < SOURCE.stat().st_mtime:
+        tmp = LIBRARY.with_suffix(".tmp.so")
+        subprocess.run(["gcc", *FLAGS, str(SOURCE), "-o", str(tmp), "-lm"], check=True)
+        os.replace(tmp, LIBRARY)
+    return LIBRARY
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(str(build()))
+        _setup(_lib)
+    return _lib
+
+
+P = C.c_void_p
+I = C.c_int
+D = C.c_double
+
+
+class Ctx(C.Structure):
+    _fields_ = [("nc", I), ("nf", I), ("nadj", I), ("nb", I),
+                ("owner", P), ("neighbour", P), ("bid", P), ("bmode", P), ("offset", P), ("faces", P), ("signs", P),
+                ("normal", P), ("length", P), ("area", P),
+                ("ls_matrix", P), ("ls_weight", P), ("ls_delta", P),
+                ("disp", P), ("disp_len", P), ("distance", P),
+                ("boundary_offset", P), ("boundary_faces", P),
+                ("grav", D), ("dry", D), ("cfl", D), ("speed_limit", D),
+                ("roughness_mode", I), ("roughness_value", D),
+                ("seg_mode", P), ("stage_policy", P), ("exterior_bed", P), ("forcing", P),
+                ("table_len", I), ("table_time", P), ("table_value", P), ("threads", I)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("substeps", I), ("rejections", I), ("status", I),
+                ("min_dt", D), ("max_dt", D), ("accepted_cfl_max", D), ("hint", D)]
+
+
+def _setup(L):
+    L.om_ctx_size.restype = C.c_size_t
+    assert L.om_ctx_size() == C.sizeof(Ctx), "oracle context layout differs"
+    L.om_stats_size.restype = C.c_size_t
+    assert L.om_stats_size() == C.sizeof(Stats)
+    L.om_scratch_create.restype = P
+    L.om_scratch_create.argtypes = [P]
+    L.om_scratch_destroy.argtypes = [P]
+    L.om_fwave_face.argtypes = [P, D, D, P]
+    L.om_fwave_face.restype = I
+    for name in ("om_primitive", "om_cells", "om_faces", "om_prepare", "om_fwave", "om_assemble",
+                 "om_gather", "om_limit_faces", "om_limit_gather"):
+        getattr(L, name).restype = None
+    L.om_exterior.restype = I
+    L.om_exterior.argtypes = [P, P, P, D, P, P, P, P, P, P]
+    L.om_outlet_feasibility.argtypes = [P, P, D, P, P, P]
+    L.om_inventory.argtypes = [P, D, P, P, P]
+    L.om_reserve.argtypes = [P, D, P, P, P]
+    L.om_reserve.restype = I
+    L.om_frequency.restype = D
+    L.om_drag.argtypes = [P, D, P]
+    L.om_rate.argtypes = [P, P, P, P, P, D, D, P, P, P]
+    L.om_rate.restype = I
+    L.om_single.argtypes = [P, P, P, P, D, D, P, P, P, P]
+    L.om_single.restype = I
+    L.om_advance.argtypes = [P, P, P, D, D, P, P, P]
+    L.om_advance.restype = I
+    L.om_set_threads.argtypes = [I]
+
+
+def _p(a):
+    return a.ctypes.data_as(P) if a is not None else None
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class Oracle:
+    """CPU oracle bound to one mesh, boundary set-up and control set.
+
+    ``case`` is the dict produced by ``braids_hkt_gb300.scenarios`` (mesh
+    arrays, records, boundary modes, forcing, controls).
+    """
+
+    def __init__(self, case, threads=None):
+        self.L = lib()
+        m = case["mesh"]
+        r = m.records
+        keep = self._keep = {}
+
+        def k(name, arr):
+            keep[name] = arr
+            return _p(arr)
+        nb = m.nb
+        seg_mode = _i32(case["seg_mode"]) if nb else np.zeros(1, np.int32)
+        bmode = np.zeros(m.nf, np.int32)
+        if nb:
+            openf = (m.neighbour < 0) & (m.bid >= 0)
+            bmode[openf] = seg_mode[m.bid[openf]]
+        self.forcing = _f64(case.get("forcing", np.zeros((2, max(nb, 1))))).copy()
+        ctx = Ctx()
+        ctx.nc, ctx.nf, ctx.nadj, ctx.nb = m.nc, m.nf, m.nadj, nb
+        ctx.owner = k("owner", _i32(m.owner))
+        ctx.neighbour = k("neighbour", _i32(m.neighbour))
+        ctx.bid = k("bid", _i32(m.bid))
+        ctx.bmode = k("bmode", bmode)
+        ctx.offset = k("offset", _i32(m.offset))
+        ctx.faces = k("faces", _i32(m.faces))
+        ctx.signs = k("signs", _i32(m.signs))
+        ctx.normal = k("normal", _f64(m.normal))
+        ctx.length = k("length", _f64(m.length))
+        ctx.area = k("area", _f64(m.area))
+        ctx.ls_matrix = k("ls_matrix", _f64(r["ls_matrix"]))
+        ctx.ls_weight = k("ls_weight", _f64(r["ls_weight"]))
+        ctx.ls_delta = k("ls_delta", _f64(r["ls_delta"]))
+        ctx.disp = k("disp", _f64(r["disp"]))
+        ctx.disp_len = k("disp_len", _f64(r["disp_len"]))
+        ctx.distance = k("distance", _f64(r["distance"]))
+        ctx.boundary_offset = k("boundary_offset", _i32(m.boundary_offset))
+        ctx.boundary_faces = k("boundary_faces", _i32(m.boundary_faces) if len(m.boundary_faces) else np.zeros(1, np.int32))
+        c = case["controls"]
+        ctx.grav, ctx.dry, ctx.cfl, ctx.speed_limit = c["grav"], c["dry"], c["cfl"], c["speed_limit"]
+        ctx.roughness_mode, ctx.roughness_value = c["roughness_mode"], c["roughness_value"]
+        ctx.seg_mode = k("seg_mode", seg_mode)
+        ctx.stage_policy = k("stage_policy", _i32(case.get("stage_policy", np.zeros(max(nb, 1), np.int32))))
+        ctx.exterior_bed = k("exterior_bed", _f64(case.get("exterior_bed", np.zeros(m.nf))))
+        ctx.forcing = _p(self.forcing)
+        tt = case.get("table_time")
+        if tt is not None:
+            ctx.table_len = len(tt)
+            ctx.table_time = k("table_time", _f64(tt))
+            ctx.table_value = k("table_value", _f64(case["table_value"]))
+        ctx.threads = threads or 0
+        self.ctx = ctx
+        self.cp = C.byref(ctx)
+        self.m = m
+        self.z = _f64(case["z"]).copy()
+        self.L.om_set_threads(threads or os.cpu_count() or 1)
+        self._scratch = self.L.om_scratch_create(self.cp)
+        self.hint = C.c_double(0.0)
+
+    def __del__(self):
+        try:
+            self.L.om_scratch_destroy(self._scratch)
+        except Exception:
+            pass
+
+    # --- full steps ------------------------------------------------------
+    def rate(self, q, dt, time=0.0, base=None):
+        q = _f64(q)
+        base = q if base is None else _f64(base)
+        rate = np.zeros_like(q)
+        water = np.zeros(self.m.nf)
+        freq = C.c_double()
+        st = self.L.om_rate(self.cp, self._scratch, _p(q), _p(self.z), _p(base), dt, time,
+                            _p(rate), _p(water), C.byref(freq))
+        return st, rate, water, freq.value
+
+    def single(self, base, dt, time=0.0):
+        base = _f64(base)
+        nc, nf = self.m.nc, self.m.nf
+        out = np.zeros_like(base)
+        water = np.zeros(nf)
+        peak = C.c_double()
+        tmp = np.zeros(9 * nc + 2 * nf)
+        st = self.L.om_single(self.cp, self._scratch, _p(base), _p(self.z), dt, time, _p(out), _p(water),
+                              C.byref(peak), _p(tmp))
+        return st, out, water, peak.value
+
+    def advance(self, q, dt, time=0.0):
+        """Advance q (3,nc) in place over an outer interval; returns (status, water_mean, stats dict)."""
+        assert q.dtype == np.float64 and q.flags.c_contiguous
+        water = np.zeros(self.m.nf)
+        stats = Stats()
+        st = self.L.om_advance(self.cp, _p(q), _p(self.z), dt, time, C.byref(self.hint), _p(water), C.byref(stats))
+        return st, water, {f: getattr(stats, f) for f, _ in Stats._fields_}
+
+    # --- single kernels (for pinning against the reference kernels) -------
+    def kernels(self, q, z=None):
+        """Run primitive -> cells -> faces -> prepare -> fwave -> assemble -> gather on q."""
+        m, L, cp = self.m, self.L, self.cp
+        q = _f64(q)
+        z = self.z if z is None else _f64(z)
+        nc, nf = m.nc, m.nf
+        o = dict(v=np.zeros((4, nc)), active=np.zeros(nc, np.int32), pstatus=np.zeros(nc, np.int32),
+                 grad=np.zeros((4, 2, nc)), constant=np.zeros(nc, np.int32),
+                 trace=np.zeros((10, nf)), kind=np.zeros(nf, np.int32), rstatus=np.zeros(nf, np.int32),
+                 local=np.zeros((8, nf)), closed=np.zeros(nf, np.int32), riemann=np.zeros((18, nf)),
+                 astatus=np.zeros(nf, np.int32), fl=np.zeros((3, nf)), fr=np.zeros((3, nf)),
+                 speed=np.zeros(nf), fstatus=np.zeros(nf, np.int32), rate=np.zeros((3, nc)))
+        L.om_primitive(cp, _p(q), _p(z), _p(o["v"]), _p(o["active"]), _p(o["pstatus"]))
+        L.om_cells(cp, _p(q), _p(o["v"]), _p(o["active"]), _p(o["grad"]), _p(o["constant"]))
+        L.om_faces(cp, _p(q), _p(o["v"]), _p(o["grad"]), _p(o["constant"]), _p(o["trace"]), _p(o["kind"]), _p(o["rstatus"]))
+        L.om_prepare(cp, _p(o["trace"]), _p(q), _p(z), _p(o["kind"]), _p(o["local"]), _p(o["closed"]))
+        L.om_fwave(cp, _p(o["local"]), _p(o["riemann"]), _p(o["astatus"]))
+        L.om_assemble(cp, _p(o["trace"]), _p(o["local"]), _p(o["riemann"]), _p(q), _p(z), _p(o["kind"]),
+                      _p(o["constant"]), _p(o["closed"]), _p(o["fl"]), _p(o["fr"]), _p(o["speed"]), _p(o["fstatus"]))
+        L.om_gather(cp, _p(q), _p(o["fl"]), _p(o["fr"]), _p(o["active"]), _p(o["rate"]))
+        return o
+
+    def fwave_face(self, states, grav, dry):
+        """Augmented f-wave on independent faces: states (8,n) -> (outputs (18,n), status (n))."""
+        states = _f64(states)
+        n = states.shape[1]
+        out = np.zeros((18, n))
+        status = np.zeros(n, np.int32)
+        col = np.zeros(8)
+        res = np.zeros(18)
+        for i in range(n):
+            col[:] = states[:, i]
+            status[i] = self.L.om_fwave_face(_p(col), grav, dry, _p(res))
+            out[:, i] = res
+        return out, status

@@ -1,0 +1,332 @@
+"""Drive the reference's own host-compiled kernels (oracle/_ref) through one river step.
+
+TEST INFRASTRUCTURE ONLY, and only where the reference checkout exists (it
+generates golden fixtures and pins the C oracle). The kernel arithmetic is
+the reference's compiled code; the orchestration between kernels restates
+the reference's Python owners line by line:
+
+  RiverMidpoint.rate, GPU branch       src/braids_core/sediment/river_midpoint.py:100-176
+  RiverExplicit.rate/_single/advance   src/braids_core/sediment/river_explicit.py:63-154
+  ExteriorBed.evaluate/apply_*         src/braids_core/sediment/river_exterior_bed.py:183-233
+
+The stock-budget steps run the reference's own Python classes
+(``OutletFeasibility`` and ``ExplicitBoundaryBudget``) on a minimal stand-in
+owner that carries only the attributes they read.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import sys
+from pathlib import Path
+from types import SimpleNamespace
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REF = HERE / "_ref"
+REFERENCE = Path(os.environ.get("BRAIDS_REFERENCE", "/root/reference"))
+
+
+class Rejected(Exception):
+    pass
+
+
+def _ptr(a):
+    return C.c_void_p(a.ctypes.data)
+
+
+def _arg(x):
+    if isinstance(x, np.ndarray):
+        assert x.flags.c_contiguous
+        return _ptr(x)
+    if isinstance(x, LL):
+        return C.c_longlong(int(x))
+    if isinstance(x, (int, np.integer)):
+        return C.c_int(int(x))
+    return C.c_double(float(x))
+
+
+class LL(int):
+    """Marks a ``long long`` kernel argument."""
+
+
+class Ref:
+    def __init__(self, case, threads=None):
+        if not (REF / "libref_update.so").exists():
+            raise FileNotFoundError("run oracle/ref_build.py first")
+        sys.path.insert(0, str(REFERENCE / "src"))
+        self.libs = {n: C.CDLL(str(REF / f"libref_{n}.so")) for n in
+                     ("reconstruction", "update", "gather", "midpoint", "explicit", "exterior", "drag")}
+        t = threads or os.cpu_count() or 1
+        for n in ("midpoint", "explicit", "exterior", "drag"):
+            self.libs[n].mobile_threads(C.c_int(t))
+        m = case["mesh"]
+        r = m.records
+        self.case, self.m = case, m
+        nc, nf, nadj = m.nc, m.nf, m.nadj
+        i32 = lambda a: np.ascontiguousarray(a, dtype=np.int32)
+        f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+        nb = m.nb
+        self.nb = nb
+        seg_mode = i32(case["seg_mode"]) if nb else np.zeros(1, np.int32)
+        self.seg_mode = seg_mode
+        openf = (m.neighbour < 0) & (m.bid >= 0)
+        self.openf = openf
+        self.open_idx = np.flatnonzero(openf)
+        bmode = np.zeros(nf, np.int32)
+        bmode[openf] = seg_mode[m.bid[openf]]
+        c = case["controls"]
+        self.grav, self.dry, self.cfl = c["grav"], c["dry"], c["cfl"]
+        self.speed_limit = c["speed_limit"]
+        self.rmode, self.rvalue = c["roughness_mode"], c["roughness_value"]
+        self.g = dict(
+            owner=i32(m.owner), neighbour=i32(m.neighbour), bid=i32(m.bid), boundary_mode=bmode,
+            offset=i32(m.offset), faces=i32(m.faces), signs=i32(m.signs),
+            xy=f64(m.xy), mid=f64(m.mid), normal=f64(m.normal), length=f64(m.length), area=f64(m.area),
+            ls_matrix=f64(r["ls_matrix"]), ls_weight=f64(r["ls_weight"]), ls_delta=f64(r["ls_delta"]),
+            displacement=f64(r["disp"]), distance=f64(r["distance"]),
+            rectangle=np.zeros((2, nc)), weno=np.full((5, 2, nf), -1, np.int32),
+            triangle=np.zeros(nc, np.int32), wall_ids=np.full((5, 2, nc), -1, np.int32),
+            wall_kind=np.zeros((5, 2, nc), np.int32), stencil_normal=np.zeros((2, 5, 2, nc)),
+            wall_slot=np.full((2, nf), -1, np.int32), wall_normal=np.zeros((2, nc)),
+            wall_mean_distance=np.ones(nc), wall_box_center=np.zeros((2, nc)),
+            sampled=np.zeros(nf, np.int32), bedoffset=np.zeros(nf),
+            selected=i32(openf), bfaces=i32(m.boundary_faces) if len(m.boundary_faces) else np.zeros(1, np.int32),
+            boffset=i32(m.boundary_offset))
+        self.z = f64(case["z"]).copy()
+        self.exterior_bed = f64(case.get("exterior_bed", np.zeros(nf)))
+        self.forcing = f64(case.get("forcing", np.zeros((2, max(nb, 1))))).copy()
+        self.stage_policy = i32(case.get("stage_policy", np.zeros(max(nb, 1), np.int32)))
+        self.roughness = np.full(nc, self.rvalue)
+        self.tiles = max(1, (int(np.max(np.diff(m.boundary_offset))) + 63) // 64) if nb else 1
+        self.step_hint = None
+        self.frequency_peak = 0.0
+        if nb:
+            self._budget = self._make_budget()
+
+    # -- the reference's own stock-budget classes on a stand-in owner --------
+    def _make_budget(self):
+        from braids_core.sediment.river_explicit_boundary_budget import ExplicitBoundaryBudget
+        m, g = self.m, self.g
+        data = dict(boundary_faces=np.asarray(m.boundary_faces, np.int32), owner=g["owner"], bid=g["bid"])
+        p = SimpleNamespace(g=dict(offset=g["offset"], faces=g["faces"], signs=g["signs"], length=g["length"],
+                                   neighbour=g["neighbour"], bid=g["bid"], area=g["area"]))
+        ext = SimpleNamespace(xp=np, p=p, a=SimpleNamespace(data=data), inlet_compatibility=None,
+                              hydraulic_mode=np.asarray(self.seg_mode[:self.nb], np.int32))
+        self._ext_stub = ext
+        return ExplicitBoundaryBudget(ext)
+
+    def call(self, lib, name, count, *args, launch=False):
+        fn = getattr(self.libs[lib], ("L_" if launch else "") + name)
+        fn.restype = None
+        pre = (C.c_longlong(int(count)),) if launch else ()
+        fn(*pre, *map(_arg, args))
+
+    # -- spatial kernels -----------------------------------------------------
+    def kernels(self, q, boundary_trace=None):
+        m, g = self.m, self.g
+        nc, nf, nadj = m.nc, m.nf, m.nadj
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        o = dict(v=np.zeros((4, nc)), active=np.zeros(nc, np.int32), pstatus=np.zeros(nc, np.int32),
+                 grad=np.zeros((4, 2, nc)), constant=np.zeros(nc, np.int32), vlo=np.zeros((4, nc)),
+                 vhi=np.zeros((4, nc)), wall_values=np.zeros((4, 4, nc)), wall_ready=np.zeros((4, nc), np.int32),
+                 face_value=np.zeros((4, 2, nf)), trace=np.zeros((10, nf)), kind=np.zeros(nf, np.int32),
+                 rstatus=np.zeros(nf, np.int32), local=np.zeros((8, nf)), closed=np.zeros(nf, np.int32),
+                 riemann=np.zeros((18, nf)), astatus=np.zeros(nf, np.int32), fl=np.zeros((3, nf)),
+                 fr=np.zeros((3, nf)), speed=np.zeros(nf), fstatus=np.zeros(nf, np.int32), rate=np.zeros((3, nc)))
+        self.call("reconstruction", "reconstruction_primitive", nc, q, self.z, g["owner"], g["neighbour"], g["bid"],
+                  g["offset"], g["faces"], g["signs"], LL(nc), self.dry, o["v"], o["active"], o["pstatus"], launch=True)
+        self.call("reconstruction", "reconstruction_cells", nc, q, o["v"], g["xy"], g["mid"], g["normal"],
+                  g["owner"], g["neighbour"], g["bid"], g["boundary_mode"], g["offset"], g["faces"], g["signs"],
+                  o["active"], g["ls_matrix"], g["ls_weight"], g["ls_delta"], g["rectangle"], g["weno"],
+                  g["displacement"], g["triangle"], g["wall_ids"], g["wall_kind"], g["stencil_normal"],
+                  g["wall_slot"], g["wall_normal"], g["wall_mean_distance"], g["wall_box_center"],
+                  LL(nc), LL(nf), LL(nadj), self.dry, self.grav, 1.0, 0,
+                  o["grad"], o["vlo"], o["vhi"], o["wall_values"], o["wall_ready"], o["constant"], launch=True)
+        bt = np.zeros((3, nf)) if boundary_trace is None else np.ascontiguousarray(boundary_trace)
+        self.call("reconstruction", "reconstruction_faces", nf, q, o["v"], o["grad"], o["vlo"], o["vhi"],
+                  o["wall_values"], o["wall_ready"], o["constant"], g["owner"], g["neighbour"], g["bid"],
+                  g["wall_slot"], g["weno"], g["displacement"], bt, 0, LL(nc), LL(nf), self.dry,
+                  o["face_value"], o["trace"], o["kind"], o["rstatus"], launch=True)
+        if boundary_trace is not None:
+            o["trace"][:3, self.open_idx] = bt[:, self.open_idx]
+        self.faces_flux(q, o)
+        self.call("gather", "implicit_full_rate_from_faces", nc, q, g["area"], g["length"], g["normal"],
+                  o["fl"], o["fr"], g["offset"], g["faces"], g["signs"], o["active"], LL(nc), LL(nf),
+                  self.grav, o["rate"], launch=True)
+        return o
+
+    def faces_flux(self, q, o):
+        m, g = self.m, self.g
+        nc, nf = m.nc, m.nf
+        self.call("update", "resident_prepare_faces", nf, o["trace"], q, self.z, g["normal"], g["distance"],
+                  g["owner"], g["neighbour"], o["kind"], LL(nc), LL(nf), self.grav, self.dry,
+                  o["local"], o["closed"], launch=True)
+        self.call("update", "augmented_fwave_local", nf, o["local"], LL(nf), self.grav, self.dry,
+                  o["riemann"], o["astatus"], launch=True)
+        self.call("update", "resident_assemble_flux", nf, o["trace"], o["local"], o["riemann"], q, self.z,
+                  g["normal"], g["owner"], g["neighbour"], o["kind"], g["boundary_mode"], g["sampled"],
+                  g["bedoffset"], o["constant"], o["closed"], LL(nc), LL(nf), self.grav, self.dry,
+                  o["fl"], o["fr"], o["speed"], o["fstatus"], launch=True)
+
+    def fwave(self, states):
+        states = np.ascontiguousarray(states, dtype=np.float64)
+        n = states.shape[1]
+        out = np.zeros((18, n))
+        status = np.zeros(n, np.int32)
+        self.call("update", "augmented_fwave_local", n, states, LL(n), self.grav, self.dry, out, status, launch=True)
+        return out, status
+
+    # -- exterior boundary owner ----------------------------------------------
+    def _reduce(self, values, fields, result):
+        nb, nf, tiles = self.nb, self.m.nf, self.tiles
+        n = nb * fields
+        partial = np.zeros(n * tiles)
+        self.call("exterior", "exterior_partial", 0, n * tiles, nf, nb, tiles, fields,
+                  self.g["boffset"], self.g["bfaces"], values, partial)
+        self.call("exterior", "exterior_totals", 0, n, tiles, partial, result)
+
+    def exterior(self, q):
+        m, g = self.m, self.g
+        nf, n, nb = m.nf, m.nc, self.nb
+        terms = np.zeros((2, nf))
+        stage = np.zeros(2 * nb)
+        weights = np.zeros(nf)
+        total = np.zeros(nb)
+        trace = np.zeros((3, nf))
+        flux = np.zeros((3, nf))
+        status = np.zeros(nf, np.int32)
+        self.call("exterior", "exterior_stage_terms", 0, nf, n, self.dry, g["owner"], g["selected"], q, self.z,
+                  g["length"], terms)
+        self._reduce(terms, 2, stage)
+        rmode = min(self.rmode, 3)
+        self.call("exterior", "exterior_weights", 0, nf, n, nb, self.dry, self.grav, rmode, self.dry,
+                  int(self.rmode == 4), g["owner"], g["bid"], g["selected"], self.seg_mode, q, self.z,
+                  self.exterior_bed, g["length"], self.roughness, stage, self.forcing, weights)
+        self._reduce(weights, 1, total)
+        self.call("exterior", "exterior_flux", 0, nf, n, nb, self.grav, self.dry, self.speed_limit,
+                  g["owner"], g["bid"], g["selected"], self.seg_mode, self.stage_policy, q, self.z,
+                  self.exterior_bed, g["normal"], g["length"], self.forcing, weights, total, trace, flux, status)
+        return trace, flux, status
+
+    # -- one spatial residual --------------------------------------------------
+    def rate(self, q, dt, time, base):
+        m, g = self.m, self.g
+        n, nf = m.nc, m.nf
+        q = np.ascontiguousarray(q)
+        if not np.all(np.isfinite(q)) or np.any(q[0] < 0):
+            raise Rejected("spatial")
+        if self.nb:
+            ext_trace, ext_flux, ext_status = self.exterior(q)
+            if np.any(ext_status):
+                raise Rejected("spatial")
+            self._ext_stub.flux, self._ext_stub.trace = ext_flux, ext_trace
+            self._budget.allocate(base, dt)
+        else:
+            ext_trace = np.zeros((3, nf))
+            ext_flux = np.zeros((3, nf))
+            ext_status = np.zeros(nf, np.int32)
+        o = self.kernels(q, boundary_trace=ext_trace if self.nb else None)
+        fl, fr = o["fl"], o["fr"]
+        if self.nb:
+            idx = self.open_idx
+            fl[:, idx] = ext_flux[:, idx]
+            fr[:, idx] = ext_flux[:, idx]
+            o["fstatus"][idx] = ext_status[idx]
+            # the gather ran inside kernels() before the exterior flux replaced the open faces: redo it
+            o["rate"][:] = 0
+            self.call("gather", "implicit_full_rate_from_faces", n, q, g["area"], g["length"], g["normal"],
+                      fl, fr, g["offset"], g["faces"], g["signs"], o["active"], LL(n), LL(nf),
+                      self.grav, o["rate"], launch=True)
+        if any(np.any(o[k]) for k in ("pstatus", "rstatus", "astatus", "fstatus")):
+            raise Rejected("spatial")
+        rate = o["rate"]
+        water = fl[0].copy()
+        theta = np.ones(n)
+        correction = np.zeros((2, nf))
+        status = np.zeros(nf, np.int32)
+        self.call("midpoint", "midpoint_inventory", 0, n, float(dt), base, g["area"], g["length"],
+                  g["offset"], g["faces"], g["signs"], water, theta)
+        saved = None
+        limiter_bid = g["bid"]
+        if self.nb:
+            saved = self._budget.reserve(base, dt, water, theta)
+            limiter_bid = np.ascontiguousarray(self._budget.limiter_bid, dtype=np.int32)
+        self.call("midpoint", "midpoint_faces", 0, nf, n, self.dry, q, theta, g["owner"], g["neighbour"],
+                  limiter_bid, water, correction, status)
+        if self.nb:
+            self._budget.restore(water, correction, saved)
+        if np.any(status):
+            raise Rejected("budget")
+        self.call("midpoint", "midpoint_gather", 0, n, nf, g["area"], g["length"], g["offset"], g["faces"],
+                  g["signs"], water, correction, rate)
+        if not np.all(np.isfinite(rate)):
+            raise Rejected("spatial")
+        freq = np.zeros(n)
+        mask = g["selected"] if self.nb else np.zeros(nf, np.int32)
+        self.call("explicit", "explicit_frequency", 0, n, nf, self.grav, self.dry, q, o["speed"],
+                  np.ascontiguousarray(ext_trace), mask, g["owner"], g["normal"], g["area"], g["length"],
+                  g["offset"], g["faces"], freq)
+        frequency = float(np.max(freq))
+        self.frequency_peak = max(self.frequency_peak, frequency)
+        if not np.isfinite(frequency) or dt * frequency > self.cfl * (1 + 1e-12):
+            raise Rejected("cfl")
+        return rate, water, frequency
+
+    def friction(self, q, dt):
+        chezy = np.zeros(self.m.nc)
+        comps = np.zeros(1)
+        self.call("drag", "river_cell_drag", 0, self.m.nc, float(dt), self.grav, self.dry, self.rmode,
+                  self.rvalue, 0, comps, q, chezy)
+
+    def single(self, base, dt, time):
+        dry = self.dry
+        work = base.copy()
+        self.frequency_peak = 0.0
+        self.friction(work, .5 * dt)
+        r, w, _ = self.rate(work, dt, time, work)
+        q1 = work + dt * r
+        if np.any(q1[0] < 0):
+            raise Rejected("spatial")
+        q1[1:, q1[0] <= dry] = 0.
+        q1 = np.ascontiguousarray(q1)
+        r2, w2, _ = self.rate(q1, dt, time + dt, q1)
+        q2 = .5 * work + .5 * (q1 + dt * r2)
+        if not np.all(np.isfinite(q2)) or np.any(q2[0] < 0):
+            raise Rejected("spatial")
+        q2[1:, q2[0] <= dry] = 0.
+        q2 = np.ascontiguousarray(q2)
+        self.friction(q2, .5 * dt)
+        return q2, .5 * (w + w2), self.frequency_peak
+
+    def advance(self, base, dt, time):
+        q = base
+        water = None
+        used, rejected, freqs = [], [], []
+        elapsed = 0.
+        floor = dt * 2 ** -20
+        hint = dt if self.step_hint is None else self.step_hint
+        while not used or elapsed < dt - 1e-13 * max(1., dt):
+            trial = min(hint, dt - elapsed)
+            truncated = trial < hint * (1 - 1e-12)
+            try:
+                nextq, w, frequency = self.single(q, trial, time + elapsed)
+            except Rejected:
+                rejected.append(trial)
+                hint = min(.5 * trial, .98 * self.cfl / self.frequency_peak) if self.frequency_peak > 0 else .5 * trial
+                if hint < floor or len(rejected) > 100:
+                    raise
+                continue
+            q = nextq
+            water = trial * w if water is None else water + trial * w
+            elapsed += trial
+            used.append(trial)
+            freqs.append(trial * frequency)
+            growth = hint if truncated else 2 * trial
+            hint = min(growth, .98 * self.cfl / frequency) if frequency > 0 else growth
+            if len(used) > 4096:
+                raise Rejected("limit")
+        self.step_hint = float(hint)
+        return q, water / dt, dict(substeps=len(used), rejections=len(rejected), min_dt=min(used),
+                                   max_dt=max(used), accepted_cfl_max=max(freqs), hint=self.step_hint)
