@@ -1,0 +1,309 @@
+"""Benchmark of the GB300 river solver step (one JSON line on rank 0).
+
+Metric: cell-updates/s, one cell-update = one cell advanced by one accepted
+SSPRK(2,2) substep (two spatial evaluations). A bench "step" is one outer
+interval ``brx_advance(dt_outer)`` of the whole workload: the adaptive
+substep loop over every scenario, resident in HBM.
+
+  python bench.py [--gpus N --steps K --warmup W] [--workload config1|config4] [--impl ours|reference]
+
+--impl reference times the reference's own CPU arithmetic of the path (the
+oracle port of its kernels, OpenMP on every host core; the reference's
+compiled kernels cannot be rebuilt where the reference checkout is absent)
+on the same workload and metric. For N > 1, scenarios are independent and
+shard across ranks with no collective on the data path ("weak" scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+METRIC = "cell-updates/s"
+BYTES_PER_CELL_UPDATE = {"fp64": 680.0, "mixed": 384.0}   # algorithmic bytes, two-sweep design
+KERNEL_NAMES = ["drag", "boundary", "cells", "faces", "gather", "limit", "update", "control"]
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def build_workload(name, rank=0, world=1):
+    import braids_hkt_gb300.scenarios as S
+    if name == "config1":
+        return [S.config1()], "fp64", 1.0, dict(workload="config1: straight channel 2000x200 m, 4 m jittered "
+                                               "Delaunay, 50k triangles, Q=400 m3/s, stage 3.0 m, Manning 0.03, "
+                                               "CFL 0.9, FP64 plain form")
+    raise SystemExit(f"unknown workload {name}")
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"),
+                                 parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def flush_l2(torch, buf):
+    buf.fill_(1.0)            # 256 MiB write evicts the 129 MB L2
+
+
+def algorithmic_bytes(kernel, nc, nf, nadj, nslot):
+    """Compulsory unique bytes one launch of each kernel reads and writes (FP64 form)."""
+    i4, d8 = 4, 8
+    if kernel == "faces":
+        return nf * (2 * i4 + 2 * d8 + 4 * d8 + 2 * d8 + i4 + i4) + nc * 128 + nf * (16 + 32)
+    if kernel == "cells":
+        return (nc * (3 * d8 + d8 + i4 + i4 + 4 * d8 + 128) + nadj * (2 * i4 + 3 * d8) +
+                nf * (3 * i4 + 2 * d8 + 2 * 2 * d8 + 2 * 2 * d8 + 2 * d8) + 3 * nc * d8)
+    if kernel == "gather":
+        return nc * (i4 + d8 + 128 // 8 + 3 * d8 + d8 + i4 + i4) + nadj * 2 * i4 + nf * (d8 + 16 + 32) + nc * 3 * d8
+    if kernel == "limit":
+        return nf * (16 + 2 * i4 + i4 + i4 + 32) + nc * (d8 + 3 * d8)
+    if kernel == "update":
+        return nc * (i4 + d8 + 3 * d8 + 3 * d8 + 3 * d8 + 3 * d8 + i4) + nadj * 2 * i4 + nf * (d8 + 32)
+    if kernel == "drag":
+        return nc * (i4 + 6 * d8)
+    return 0
+
+
+def cpu_baseline(cases, outer, seconds=10.0, threads=None):
+    """The oracle port on the host cores over a bounded sample of the workload."""
+    from oracle import Oracle
+    threads = threads or os.cpu_count() or 1
+    o = Oracle(cases[0], threads=threads)
+    q = cases[0]["q"].copy()
+    nc = cases[0]["mesh"].nc
+    updates, t0, sim = 0, time.perf_counter(), 0.0
+    interval = min(outer, 0.5)
+    while time.perf_counter() - t0 < seconds:
+        st, _, stats = o.advance(q, interval, sim)
+        if st:
+            break
+        updates += stats["substeps"] * nc
+        sim += interval
+    el = time.perf_counter() - t0
+    return {"value": updates / el, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"{cases[0].get('name', 'case')}: {sim:g} s simulated ({updates} cell-updates) "
+                      f"from the initial state, oracle port with OpenMP on {threads} threads"}
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cases, precision, outer, cfg = build_workload(args.workload)
+    threads = os.cpu_count() or 1
+    per_step = []
+    for _ in range(args.warmup):
+        cpu_baseline(cases, outer, seconds=2.0, threads=threads)
+    for _ in range(args.steps):
+        per_step.append(cpu_baseline(cases, outer, seconds=max(5.0, 60.0 / max(args.steps, 1)), threads=threads))
+    value = float(np.mean([p["value"] for p in per_step]))
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg, "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
+                             "sample": per_step[-1]["sample"]},
+            "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
+    ap.add_argument("--workload", default="config1")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return reference_arm(args)
+
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from braids_hkt_gb300.solver import RiverSolver
+
+    cases, precision, outer, cfg = build_workload(args.workload, rank, world)
+    solver = RiverSolver(cases, precision=precision)
+    nc, nf = solver.nc, solver.nf
+    nadj = int(solver.packed["nadj"])
+    nslot = len(solver.packed["boundary_faces"])
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    stream = solver.stream
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    sim_time = 0.0
+    for _ in range(args.warmup):
+        solver.advance(outer, sim_time)
+        sim_time += outer
+    # timed region: K outer steps, device time by events on the solver stream
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = solver.launches()
+    updates = 0
+    device_ms = 0.0
+    barrier()
+    wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush_l2(torch, flush)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        diags = solver.advance(outer, sim_time)
+        e1.record(stream)
+        e1.synchronize()
+        device_ms += e0.elapsed_time(e1)
+        sim_time += outer
+        diags = diags if isinstance(diags, list) else [diags]
+        updates += sum(d["hydraulic_substeps"] * (solver.packed["cell_offset"][i + 1] - solver.packed["cell_offset"][i])
+                       for i, d in enumerate(diags))
+    barrier()
+    wall = time.perf_counter() - wall0
+    gpu_launches = solver.launches() - launches0
+    clock_info = clocks.stop()
+    t_max = device_ms / 1e3
+    if dist is not None:
+        t = torch.tensor([t_max, float(updates)], device="cuda", dtype=torch.float64)
+        tmax = t[:1].clone()
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+        dist.all_reduce(t[1:], op=dist.ReduceOp.SUM)
+        t_max, updates = float(tmax.item()), int(t[1].item())
+    value = updates / t_max
+
+    # end to end through the public API with host buffers: H2D of the step's
+    # input state from pinned memory, advance, D2H of the result
+    q_host = torch.empty_like(solver.q, device="cpu").pin_memory()
+    q_host.copy_(solver.q)
+    out_host = torch.empty_like(q_host).pin_memory()
+    e2e_updates = 0
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(max(1, args.steps)):
+        solver.q.copy_(q_host, non_blocking=True)
+        diags = solver.advance(outer, sim_time)
+        out_host.copy_(solver.q, non_blocking=True)
+        torch.cuda.synchronize()
+        sim_time += outer
+        diags = diags if isinstance(diags, list) else [diags]
+        e2e_updates += sum(d["hydraulic_substeps"] * (solver.packed["cell_offset"][i + 1] - solver.packed["cell_offset"][i])
+                           for i, d in enumerate(diags))
+    e2e_s = time.perf_counter() - t0
+    h2d = int(q_host.numel() * 8)
+
+    # live per-kernel timing of one substep for the roofline of the dominant kernel
+    prof = solver.profile_substep(0.5 * diags[0]["hydraulic_next_substep_hint_s"], sim_time)
+    per_kind = {}
+    for name, ms in prof:
+        per_kind.setdefault(name, []).append(ms)
+    dom = max(per_kind, key=lambda k: sum(per_kind[k]))
+    dom_ms = float(np.mean(per_kind[dom]))
+    dom_bytes = algorithmic_bytes(dom, nc, nf, nadj, nslot)
+    peak, peak_kind = peaks()
+    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", f"traffic_{args.workload}.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            traffic = json.load(f).get(dom)
+    total_ms = sum(sum(v) for v in per_kind.values())
+    roofline = {"bound": "hbm", "kernel": f"k_{dom}", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                "kernel_ms": dom_ms, "kernel_share_of_substep": sum(per_kind[dom]) / total_ms,
+                "algorithmic_bytes_per_launch": dom_bytes,
+                "step_bytes_per_cell_update": BYTES_PER_CELL_UPDATE[precision],
+                "step_achieved_gbs": value * BYTES_PER_CELL_UPDATE[precision] / 1e9}
+    if rank != 0:
+        return
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": device_ms / max(args.steps, 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if precision == "fp64" else "f32+f64",
+            "data": "synthetic", "config": dict(cfg, cells=nc, faces=nf, outer_dt_s=outer,
+                                                l2="flushed between steps (256 MiB write)",
+                                                wall_s=wall),
+            "roofline": roofline, "clocks": clock_info, "gpu_launches": int(gpu_launches),
+            "e2e": {"value": e2e_updates / e2e_s, "unit": METRIC, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": h2d}}
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(cases, outer)
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

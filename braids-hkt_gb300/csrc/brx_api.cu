@@ -1,0 +1,659 @@
+// Host runtime and C ABI of the GB300 river solver step.
+//
+// A brx_solver owns the device copy of one packed mesh (one or many
+// scenarios), the boundary tables, the stage work buffers and the per-
+// scenario control blocks. brx_advance runs the adaptive SSPRK(2,2) loop of
+// the reference's RiverExplicit.advance (src/braids_core/sediment/
+// river_explicit.py:121-154) entirely on the device: every substep is a fixed
+// launch sequence whose clock lives in device memory, captured once into a
+// CUDA graph of `chunk` substeps and replayed until every scenario reports
+// done. The host reads the control blocks back once per replay.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/braids_gb300.h"
+#include "brx_kernels.cuh"
+
+using namespace brx;
+
+static thread_local std::string g_error;
+
+static int fail(int code, const std::string &msg)
+{
+    g_error = msg;
+    return code;
+}
+
+#define CK(call)                                                                         \
+    do {                                                                                 \
+        cudaError_t e_ = (call);                                                         \
+        if (e_ != cudaSuccess)                                                           \
+            return fail(BRX_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+struct brx_solver {
+    int precision = BRX_FP64;
+    int nscen = 0, nc = 0, nf = 0, nadj = 0, nseg = 0, nslot = 0, nown = 0, maxdeg = 0;
+    int device = 0, sms = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<void *> allocations;
+    MeshDev mesh{};
+    BoundaryDev bnd{};
+    StateDev state{};
+    Work work{};
+    Ctrl *d_ctrl = nullptr;
+    Ctrl *h_ctrl = nullptr;          // pinned mirror
+    std::vector<double> hint;
+    std::vector<int> active;
+    std::vector<int> cell_offset, face_offset, seg_offset;
+    std::vector<int> h_bid, h_owner, h_neighbour, h_slot_face;
+    int *d_bmode_rw = nullptr;       // writable alias of mesh.bmode
+    int *d_seg_mode_rw = nullptr, *d_stage_policy_rw = nullptr;
+    double *d_ext_bed_rw = nullptr, *d_table_time = nullptr, *d_table_value = nullptr;
+    bool bound = false, boundary_ready = false;
+    cudaGraphExec_t graph = nullptr;
+    int graph_chunk = 8, graph_built_chunk = 0;
+    bool graph_dirty = true;
+    long long launches = 0;
+    int grid_c = 0, grid_f = 0;      // persistent grid sizes (cells / faces kernels)
+    int grid_c256 = 0, grid_f256 = 0;
+    int launches_per_substep = 0;
+
+    template <class T> int alloc(T **p, size_t count)
+    {
+        if (count == 0) count = 1;
+        void *ptr = nullptr;
+        cudaError_t e = cudaMalloc(&ptr, count * sizeof(T));
+        if (e != cudaSuccess) return fail(BRX_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        allocations.push_back(ptr);
+        *p = (T *)ptr;
+        return BRX_OK;
+    }
+    template <class T> int upload(T **p, const T *host, size_t count)
+    {
+        int rc = alloc(p, count);
+        if (rc) return rc;
+        if (count) CK(cudaMemcpy(*p, host, count * sizeof(T), cudaMemcpyHostToDevice));
+        return BRX_OK;
+    }
+};
+
+#define TRY(expr)              \
+    do {                       \
+        int rc_ = (expr);      \
+        if (rc_) return rc_;   \
+    } while (0)
+
+extern "C" const char *brx_last_error(void) { return g_error.c_str(); }
+extern "C" int brx_version(void) { return 1; }
+
+// ---------------------------------------------------------------------------
+// creation
+// ---------------------------------------------------------------------------
+static int validate(int nscen, const int *cell_offset, const int *face_offset, int nc, int nf, int nadj,
+                    const int *owner, const int *neighbour, const int *bid, const int *offset, const int *faces,
+                    const int *signs, int nseg, const int *seg_offset, const int *boundary_offset,
+                    const int *boundary_faces)
+{
+    if (nscen < 1 || nc < 1 || nf < 1 || nadj < 1 || nseg < 0)
+        return fail(BRX_ERR_ARGUMENT, "empty mesh or negative segment count");
+    if (!cell_offset || !face_offset || !owner || !neighbour || !bid || !offset || !faces || !signs)
+        return fail(BRX_ERR_ARGUMENT, "null topology array");
+    if (cell_offset[0] != 0 || cell_offset[nscen] != nc || face_offset[0] != 0 || face_offset[nscen] != nf)
+        return fail(BRX_ERR_ARGUMENT, "scenario partition does not cover the mesh");
+    for (int i = 0; i < nscen; ++i)
+        if (cell_offset[i + 1] <= cell_offset[i] || face_offset[i + 1] <= face_offset[i])
+            return fail(BRX_ERR_ARGUMENT, "empty scenario");
+    if (offset[0] != 0 || offset[nc] != nadj) return fail(BRX_ERR_ARGUMENT, "invalid CSR offsets");
+    for (int c = 0; c < nc; ++c) {
+        if (offset[c + 1] < offset[c]) return fail(BRX_ERR_ARGUMENT, "decreasing CSR offsets");
+        if (offset[c + 1] - offset[c] > MAX_CELL_FACES)
+            return fail(BRX_ERR_UNSUPPORTED, "a cell has more than 32 faces");
+    }
+    std::vector<int> fsid(nf), csid(nc);
+    for (int i = 0; i < nscen; ++i) {
+        for (int c = cell_offset[i]; c < cell_offset[i + 1]; ++c) csid[c] = i;
+        for (int f = face_offset[i]; f < face_offset[i + 1]; ++f) fsid[f] = i;
+    }
+    for (int f = 0; f < nf; ++f) {
+        if (owner[f] < 0 || owner[f] >= nc || neighbour[f] < -1 || neighbour[f] >= nc)
+            return fail(BRX_ERR_ARGUMENT, "face cell index out of range");
+        if (csid[owner[f]] != fsid[f] || (neighbour[f] >= 0 && csid[neighbour[f]] != fsid[f]))
+            return fail(BRX_ERR_ARGUMENT, "face connects cells of another scenario");
+        if (bid[f] < -1 || bid[f] >= nseg || (bid[f] >= 0 && neighbour[f] >= 0))
+            return fail(BRX_ERR_ARGUMENT, "invalid boundary id");
+    }
+    for (int c = 0; c < nc; ++c)
+        for (int k = offset[c]; k < offset[c + 1]; ++k) {
+            const int f = faces[k];
+            if (f < 0 || f >= nf) return fail(BRX_ERR_ARGUMENT, "CSR face index out of range");
+            if (signs[k] != 1 && signs[k] != -1) return fail(BRX_ERR_ARGUMENT, "CSR sign must be +1 or -1");
+            if ((signs[k] > 0 ? owner[f] : neighbour[f]) != c)
+                return fail(BRX_ERR_ARGUMENT, "CSR incidence does not match face ownership");
+        }
+    if (nseg > 0) {
+        if (!seg_offset || !boundary_offset || !boundary_faces) return fail(BRX_ERR_ARGUMENT, "null boundary array");
+        if (seg_offset[0] != 0 || seg_offset[nscen] != nseg || boundary_offset[0] != 0)
+            return fail(BRX_ERR_ARGUMENT, "invalid segment partition");
+        for (int i = 0; i < nscen; ++i)
+            if (seg_offset[i + 1] < seg_offset[i]) return fail(BRX_ERR_ARGUMENT, "decreasing segment offsets");
+        for (int sg = 0; sg < nseg; ++sg) {
+            if (boundary_offset[sg + 1] < boundary_offset[sg]) return fail(BRX_ERR_ARGUMENT, "decreasing boundary offsets");
+            for (int k = boundary_offset[sg]; k < boundary_offset[sg + 1]; ++k) {
+                const int f = boundary_faces[k];
+                if (f < 0 || f >= nf || bid[f] != sg) return fail(BRX_ERR_ARGUMENT, "boundary face not on its segment");
+            }
+        }
+        int open = 0;
+        for (int f = 0; f < nf; ++f) open += bid[f] >= 0;
+        if (open != boundary_offset[nseg]) return fail(BRX_ERR_ARGUMENT, "every open face must be listed once");
+    }
+    return BRX_OK;
+}
+
+extern "C" int brx_solver_create(int nscen, const int *cell_offset, const int *face_offset, int nc, int nf, int nadj,
+                                 const int *owner, const int *neighbour, const int *bid, const int *offset,
+                                 const int *faces, const int *signs, const double *normal, const double *length,
+                                 const double *area, const double *ls_matrix, const double *ls_weight,
+                                 const double *ls_delta, const double *displacement, const double *distance,
+                                 int nseg, const int *seg_offset, const int *boundary_offset,
+                                 const int *boundary_faces, int precision, brx_solver **out)
+{
+    if (!out) return fail(BRX_ERR_ARGUMENT, "null output handle");
+    *out = nullptr;
+    if (precision != BRX_FP64 && precision != BRX_MIXED) return fail(BRX_ERR_ARGUMENT, "unknown precision");
+    if (precision == BRX_MIXED) return fail(BRX_ERR_UNSUPPORTED, "mixed precision form is not built in this library");
+    if (!normal || !length || !area || !ls_matrix || !ls_weight || !ls_delta || !displacement || !distance)
+        return fail(BRX_ERR_ARGUMENT, "null geometry array");
+    TRY(validate(nscen, cell_offset, face_offset, nc, nf, nadj, owner, neighbour, bid, offset, faces, signs, nseg,
+                 seg_offset, boundary_offset, boundary_faces));
+    brx_solver *s = new brx_solver();
+    int rc = [&]() -> int {
+        s->precision = precision;
+        s->nscen = nscen; s->nc = nc; s->nf = nf; s->nadj = nadj; s->nseg = nseg;
+        CK(cudaGetDevice(&s->device));
+        CK(cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, s->device));
+        CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+        s->cell_offset.assign(cell_offset, cell_offset + nscen + 1);
+        s->face_offset.assign(face_offset, face_offset + nscen + 1);
+        s->seg_offset.assign(nscen + 1, 0);
+        if (nseg) s->seg_offset.assign(seg_offset, seg_offset + nscen + 1);
+        s->h_bid.assign(bid, bid + nf);
+        s->h_owner.assign(owner, owner + nf);
+        s->h_neighbour.assign(neighbour, neighbour + nf);
+        // derived host tables
+        std::vector<int> csid(nc), fsid(nf), bslot(nf, -1), cflags(nc, 0);
+        for (int i = 0; i < nscen; ++i) {
+            for (int c = cell_offset[i]; c < cell_offset[i + 1]; ++c) csid[c] = i;
+            for (int f = face_offset[i]; f < face_offset[i + 1]; ++f) fsid[f] = i;
+        }
+        s->nslot = nseg ? boundary_offset[nseg] : 0;
+        for (int k = 0; k < s->nslot; ++k) {
+            bslot[boundary_faces[k]] = k;
+            cflags[owner[boundary_faces[k]]] |= 1;
+        }
+        for (int c = 0; c < nc; ++c) s->maxdeg = std::max(s->maxdeg, offset[c + 1] - offset[c]);
+        // per-face-side displacement length and unit vector (glibc hypot, as the host oracle)
+        std::vector<double> dlen(2 * (size_t)nf), dunit(4 * (size_t)nf);
+        for (int side = 0; side < 2; ++side)
+            for (int f = 0; f < nf; ++f) {
+                const double rx = displacement[side * (size_t)nf + f], ry = displacement[(2 + side) * (size_t)nf + f];
+                const double len = std::hypot(rx, ry);
+                dlen[side * (size_t)nf + f] = len;
+                dunit[side * (size_t)nf + f] = len > 0 ? rx / len : 0.0;
+                dunit[(2 + side) * (size_t)nf + f] = len > 0 ? ry / len : 0.0;
+            }
+        // unique boundary owners per scenario (ascending), with their slots in boundary order
+        std::vector<int> scen_own(nscen + 1, 0), own_cell, own_off(1, 0), own_slot;
+        for (int i = 0; i < nscen; ++i) {
+            std::map<int, std::vector<int>> by_owner;
+            if (nseg)
+                for (int sg = seg_offset[i]; sg < seg_offset[i + 1]; ++sg)
+                    for (int k = boundary_offset[sg]; k < boundary_offset[sg + 1]; ++k)
+                        by_owner[owner[boundary_faces[k]]].push_back(k);
+            for (auto &kv : by_owner) {
+                own_cell.push_back(kv.first);
+                std::vector<int> ks = kv.second;
+                std::sort(ks.begin(), ks.end());
+                own_slot.insert(own_slot.end(), ks.begin(), ks.end());
+                own_off.push_back((int)own_slot.size());
+            }
+            scen_own[i + 1] = (int)own_cell.size();
+            // boundary kernel shared tile buffer: tiles of 64 faces per scenario
+            int tiles = 0;
+            if (nseg)
+                for (int sg = seg_offset[i]; sg < seg_offset[i + 1]; ++sg)
+                    tiles += std::max(1, (boundary_offset[sg + 1] - boundary_offset[sg] + 63) / 64);
+            if (tiles > BOUNDARY_TILES) return fail(BRX_ERR_UNSUPPORTED, "too many open faces in one scenario");
+        }
+        s->nown = (int)own_cell.size();
+        MeshDev &m = s->mesh;
+        m.nc = nc; m.nf = nf; m.nadj = nadj; m.nscen = nscen;
+        int *p_owner, *p_nb, *p_bid, *p_off, *p_faces, *p_signs, *p_bslot, *p_csid, *p_fsid, *p_cflags;
+        double *p_normal, *p_length, *p_area, *p_lsm, *p_lsw, *p_lsd, *p_disp, *p_dunit, *p_dlen, *p_dist;
+        TRY(s->upload(&p_owner, owner, nf)); TRY(s->upload(&p_nb, neighbour, nf)); TRY(s->upload(&p_bid, bid, nf));
+        TRY(s->upload(&p_off, offset, nc + 1)); TRY(s->upload(&p_faces, faces, nadj)); TRY(s->upload(&p_signs, signs, nadj));
+        TRY(s->upload(&p_bslot, bslot.data(), nf)); TRY(s->upload(&p_csid, csid.data(), nc));
+        TRY(s->upload(&p_fsid, fsid.data(), nf)); TRY(s->upload(&p_cflags, cflags.data(), nc));
+        TRY(s->alloc(&s->d_bmode_rw, nf));
+        CK(cudaMemset(s->d_bmode_rw, 0, sizeof(int) * nf));
+        TRY(s->upload(&p_normal, normal, 2 * (size_t)nf)); TRY(s->upload(&p_length, length, nf));
+        TRY(s->upload(&p_area, area, nc)); TRY(s->upload(&p_lsm, ls_matrix, 4 * (size_t)nc));
+        TRY(s->upload(&p_lsw, ls_weight, nadj)); TRY(s->upload(&p_lsd, ls_delta, 2 * (size_t)nadj));
+        TRY(s->upload(&p_disp, displacement, 4 * (size_t)nf)); TRY(s->upload(&p_dunit, dunit.data(), 4 * (size_t)nf));
+        TRY(s->upload(&p_dlen, dlen.data(), 2 * (size_t)nf)); TRY(s->upload(&p_dist, distance, 2 * (size_t)nf));
+        m.owner = p_owner; m.neighbour = p_nb; m.bid = p_bid; m.offset = p_off; m.faces = p_faces; m.signs = p_signs;
+        m.bslot = p_bslot; m.bmode = s->d_bmode_rw; m.cell_sid = p_csid; m.face_sid = p_fsid; m.cflags = p_cflags;
+        m.normal = p_normal; m.length = p_length; m.area = p_area; m.ls_matrix = p_lsm; m.ls_weight = p_lsw;
+        m.ls_delta = p_lsd; m.disp = p_disp; m.disp_unit = p_dunit; m.disp_len = p_dlen; m.distance = p_dist;
+        BoundaryDev &b = s->bnd;
+        b.nseg = nseg; b.nslot = s->nslot; b.nown = s->nown;
+        int *p_scen_seg, *p_scen_own, *p_seg_off, *p_slot_face, *p_own_cell, *p_own_off, *p_own_slot;
+        TRY(s->upload(&p_scen_seg, s->seg_offset.data(), nscen + 1));
+        TRY(s->upload(&p_scen_own, scen_own.data(), nscen + 1));
+        std::vector<int> seg_off(nseg + 1, 0);
+        if (nseg) seg_off.assign(boundary_offset, boundary_offset + nseg + 1);
+        TRY(s->upload(&p_seg_off, seg_off.data(), nseg + 1));
+        std::vector<int> slot_face(s->nslot);
+        for (int k = 0; k < s->nslot; ++k) slot_face[k] = boundary_faces[k];
+        s->h_slot_face = slot_face;
+        TRY(s->upload(&p_slot_face, slot_face.data(), s->nslot));
+        TRY(s->upload(&p_own_cell, own_cell.data(), own_cell.size()));
+        TRY(s->upload(&p_own_off, own_off.data(), own_off.size()));
+        TRY(s->upload(&p_own_slot, own_slot.data(), own_slot.size()));
+        b.scen_seg = p_scen_seg; b.scen_own = p_scen_own; b.seg_off = p_seg_off; b.slot_face = p_slot_face;
+        b.own_cell = p_own_cell; b.own_off = p_own_off; b.own_slot = p_own_slot;
+        TRY(s->alloc(&s->d_seg_mode_rw, nseg)); TRY(s->alloc(&s->d_stage_policy_rw, nseg));
+        TRY(s->alloc(&s->d_ext_bed_rw, s->nslot));
+        double *p_forcing, *p_terms, *p_trace, *p_flux, *p_sums;
+        TRY(s->alloc(&p_forcing, 2 * (size_t)nseg)); TRY(s->alloc(&p_terms, 3 * (size_t)s->nslot));
+        TRY(s->alloc(&p_trace, 3 * (size_t)s->nslot)); TRY(s->alloc(&p_flux, 3 * (size_t)s->nslot));
+        TRY(s->alloc(&p_sums, 3 * (size_t)nseg));
+        b.seg_mode = s->d_seg_mode_rw; b.stage_policy = s->d_stage_policy_rw; b.ext_bed = s->d_ext_bed_rw;
+        b.forcing = p_forcing; b.terms = p_terms; b.trace = p_trace; b.flux = p_flux; b.seg_sums = p_sums;
+        b.table_len = 0; b.table_time = nullptr; b.table_value = nullptr;
+        // state and work
+        TRY(s->alloc(&s->state.q[1], 3 * (size_t)nc)); TRY(s->alloc(&s->state.work, 3 * (size_t)nc));
+        TRY(s->alloc(&s->state.q1, 3 * (size_t)nc));
+        TRY(s->alloc(&s->work.rec, nc)); TRY(s->alloc(&s->work.ws, nf)); TRY(s->alloc(&s->work.gf, nf));
+        TRY(s->alloc(&s->work.lim, nf)); TRY(s->alloc(&s->work.rate, 3 * (size_t)nc));
+        TRY(s->alloc(&s->work.theta, nc));
+        TRY(s->alloc(&s->d_ctrl, nscen));
+        CK(cudaMallocHost(&s->h_ctrl, sizeof(Ctrl) * nscen));
+        memset(s->h_ctrl, 0, sizeof(Ctrl) * nscen);
+        s->hint.assign(nscen, 0.0);
+        s->active.assign(nscen, 1);
+        for (int i = 0; i < nscen; ++i) {
+            Ctrl &c = s->h_ctrl[i];
+            c.grav = 9.81; c.dry = 1e-6; c.cfl = 0.9; c.speed_limit = 50.0;
+            c.roughness_mode = 2; c.roughness_value = 0.03; c.max_substeps = 4096;
+        }
+        // persistent grids: a multiple of the SM count, no more blocks than the work needs
+        int occ128 = 0, occ256 = 0;
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ128, k_faces, 128, 0));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ256, k_gather, 256, 0));
+        occ128 = std::max(occ128, 1); occ256 = std::max(occ256, 1);
+        auto grid = [&](int n, int block, int occ) { return std::max(1, std::min((n + block - 1) / block, s->sms * occ)); };
+        s->grid_c = grid(nc, 128, occ128); s->grid_f = grid(nf, 128, occ128);
+        s->grid_c256 = grid(nc, 256, occ256); s->grid_f256 = grid(nf, 256, occ256);
+        return BRX_OK;
+    }();
+    if (rc) { brx_solver_destroy(s); return rc; }
+    *out = s;
+    return BRX_OK;
+}
+
+extern "C" int brx_solver_destroy(brx_solver *s)
+{
+    if (!s) return BRX_OK;
+    if (s->graph) cudaGraphExecDestroy(s->graph);
+    for (void *p : s->allocations) cudaFree(p);
+    if (s->h_ctrl) cudaFreeHost(s->h_ctrl);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+    return BRX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// set-up calls
+// ---------------------------------------------------------------------------
+extern "C" int brx_controls_set(brx_solver *s, int scen, double gravity, double dry, double cfl, double speed_limit,
+                                int roughness_mode, double roughness_value)
+{
+    if (!s) return fail(BRX_ERR_ARGUMENT, "null solver");
+    if (scen < -1 || scen >= s->nscen) return fail(BRX_ERR_ARGUMENT, "scenario out of range");
+    if (!(gravity > 0) || !(dry > 0) || !(cfl > 0 && cfl <= 1) || !(speed_limit > 0) || !std::isfinite(gravity) ||
+        !std::isfinite(dry) || !std::isfinite(speed_limit))
+        return fail(BRX_ERR_ARGUMENT, "controls must be finite and positive, CFL in (0, 1]");
+    if (roughness_mode < 1 || roughness_mode > 4 || !(roughness_value > 0) || !std::isfinite(roughness_value))
+        return fail(BRX_ERR_ARGUMENT, "roughness mode 1-4 with a positive finite coefficient");
+    for (int i = 0; i < s->nscen; ++i)
+        if (scen < 0 || scen == i) {
+            Ctrl &c = s->h_ctrl[i];
+            c.grav = gravity; c.dry = dry; c.cfl = cfl; c.speed_limit = speed_limit;
+            c.roughness_mode = roughness_mode; c.roughness_value = roughness_value;
+        }
+    return BRX_OK;
+}
+
+extern "C" int brx_boundary_set(brx_solver *s, const int *seg_mode, const int *stage_policy, const double *exterior_bed,
+                                const double *forcing)
+{
+    if (!s) return fail(BRX_ERR_ARGUMENT, "null solver");
+    const int nseg = s->nseg, nf = s->nf;
+    if (nseg == 0) { s->boundary_ready = true; return BRX_OK; }
+    if (!seg_mode || !stage_policy || !exterior_bed || !forcing) return fail(BRX_ERR_ARGUMENT, "null boundary array");
+    for (int sg = 0; sg < nseg; ++sg) {
+        const int md = seg_mode[sg];
+        if (md != 2 && md != 3 && md != 6 && md != 9)
+            return fail(BRX_ERR_UNSUPPORTED, "open-boundary mode must be 2, 3, 6 or 9");
+        if (stage_policy[sg] != 0 && stage_policy[sg] != 1) return fail(BRX_ERR_ARGUMENT, "stage policy must be 0 or 1");
+        if (!std::isfinite(forcing[sg]) || !std::isfinite(forcing[nseg + sg])) return fail(BRX_ERR_ARGUMENT, "nonfinite forcing");
+    }
+    std::vector<int> bmode(nf, 0);
+    std::vector<double> ext(std::max(s->nslot, 1));
+    for (int k = 0; k < s->nslot; ++k) {
+        const int f = s->h_slot_face[k];
+        bmode[f] = seg_mode[s->h_bid[f]];
+        ext[k] = exterior_bed[f];
+        if (!std::isfinite(ext[k])) return fail(BRX_ERR_ARGUMENT, "nonfinite exterior bed");
+    }
+    CK(cudaMemcpy(s->d_bmode_rw, bmode.data(), sizeof(int) * nf, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s->d_seg_mode_rw, seg_mode, sizeof(int) * nseg, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s->d_stage_policy_rw, stage_policy, sizeof(int) * nseg, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s->d_ext_bed_rw, ext.data(), sizeof(double) * s->nslot, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s->bnd.forcing, forcing, sizeof(double) * 2 * nseg, cudaMemcpyHostToDevice));
+    s->boundary_ready = true;
+    return BRX_OK;
+}
+
+extern "C" int brx_forcing_table_set(brx_solver *s, int len, const double *time, const double *value)
+{
+    if (!s) return fail(BRX_ERR_ARGUMENT, "null solver");
+    if (len < 0 || (len > 0 && (!time || !value))) return fail(BRX_ERR_ARGUMENT, "invalid forcing table");
+    for (int i = 1; i < len; ++i)
+        if (!(time[i] > time[i - 1])) return fail(BRX_ERR_ARGUMENT, "table times must increase");
+    s->bnd.table_len = 0;
+    if (len > 0) {
+        double *t, *v;
+        TRY(s->upload(&t, time, len));
+        TRY(s->upload(&v, value, 2 * (size_t)s->nseg * len));
+        s->bnd.table_time = t;
+        s->bnd.table_value = v;
+        s->bnd.table_len = len;
+    }
+    s->graph_dirty = true;
+    return BRX_OK;
+}
+
+extern "C" int brx_state_bind(brx_solver *s, double *q_device, double *z_device)
+{
+    if (!s || !q_device || !z_device) return fail(BRX_ERR_ARGUMENT, "null state pointer");
+    s->state.q[0] = q_device;
+    s->state.z = z_device;
+    s->bound = true;
+    s->graph_dirty = true;
+    return BRX_OK;
+}
+
+extern "C" int brx_scenarios_activate(brx_solver *s, const int *active)
+{
+    if (!s || !active) return fail(BRX_ERR_ARGUMENT, "null argument");
+    for (int i = 0; i < s->nscen; ++i) s->active[i] = active[i] != 0;
+    return BRX_OK;
+}
+
+extern "C" int brx_hint_get(brx_solver *s, double *hint)
+{
+    if (!s || !hint) return fail(BRX_ERR_ARGUMENT, "null argument");
+    for (int i = 0; i < s->nscen; ++i) hint[i] = s->hint[i];
+    return BRX_OK;
+}
+
+extern "C" int brx_hint_set(brx_solver *s, const double *hint)
+{
+    if (!s || !hint) return fail(BRX_ERR_ARGUMENT, "null argument");
+    for (int i = 0; i < s->nscen; ++i) s->hint[i] = hint[i];
+    return BRX_OK;
+}
+
+extern "C" int brx_graph_chunk_set(brx_solver *s, int substeps)
+{
+    if (!s || substeps < 1 || substeps > 256) return fail(BRX_ERR_ARGUMENT, "chunk must be 1..256 substeps");
+    s->graph_chunk = substeps;
+    s->graph_dirty = true;
+    return BRX_OK;
+}
+
+extern "C" long long brx_launch_count(const brx_solver *s) { return s ? s->launches : 0; }
+extern "C" void *brx_stream(brx_solver *s) { return s ? (void *)s->stream : nullptr; }
+
+// ---------------------------------------------------------------------------
+// launch sequences
+// ---------------------------------------------------------------------------
+static void enqueue_stage(brx_solver *s, int stage, double *rate_out)
+{
+    cudaStream_t st = s->stream;
+    if (s->nslot) {
+        k_boundary<<<s->nscen, 256, 0, st>>>(s->mesh, s->state, s->bnd, s->d_ctrl, stage);
+        s->launches++;
+    }
+    if (s->maxdeg <= 4) k_cells<4><<<s->grid_c, 128, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage);
+    else k_cells<MAX_CELL_FACES><<<s->grid_c, 128, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage);
+    k_faces<<<s->grid_f, 128, 0, st>>>(s->mesh, s->state, s->bnd, s->d_ctrl, s->work, stage);
+    k_gather<<<s->grid_c256, 256, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage);
+    k_limit<<<s->grid_f256, 256, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage);
+    k_update<<<s->grid_c256, 256, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage, rate_out);
+    s->launches += 5;
+}
+
+static void enqueue_substep(brx_solver *s)
+{
+    k_open_drag<<<s->grid_c256, 256, 0, s->stream>>>(s->mesh, s->state, s->d_ctrl);
+    s->launches++;
+    enqueue_stage(s, 1, nullptr);
+    enqueue_stage(s, 2, nullptr);
+    k_control<<<(s->nscen + 127) / 128, 128, 0, s->stream>>>(s->d_ctrl, s->nscen);
+    s->launches++;
+}
+
+static void host_set_trial(Ctrl &c)
+{
+    c.trial = std::fmin(c.hint, c.dt_outer - c.elapsed);
+    c.truncated = c.trial < c.hint * (1 - 1e-12);
+    c.status1 = c.status2 = 0;
+    c.peak1 = c.peak2 = 0ull;
+}
+
+static void begin_interval(brx_solver *s, double dt, double time, bool fixed)
+{
+    for (int i = 0; i < s->nscen; ++i) {
+        Ctrl &c = s->h_ctrl[i];
+        c.active = s->active[i];
+        c.dt_outer = dt; c.time0 = time; c.elapsed = 0.0;
+        c.hint = fixed ? dt : (s->hint[i] > 0 ? s->hint[i] : dt);
+        c.floor_ = std::ldexp(dt, -20);
+        c.substeps = c.rejections = c.done = c.failed = c.cur = 0;
+        c.min_dt = c.max_dt = c.cfl_max = 0.0;
+        c.done = !c.active;
+        host_set_trial(c);
+    }
+}
+
+static int ensure_ready(brx_solver *s)
+{
+    if (!s) return fail(BRX_ERR_ARGUMENT, "null solver");
+    if (!s->bound) return fail(BRX_ERR_STATE, "no state bound (brx_state_bind)");
+    if (!s->boundary_ready && s->nseg) return fail(BRX_ERR_STATE, "open boundaries not configured (brx_boundary_set)");
+    return BRX_OK;
+}
+
+static int build_graph(brx_solver *s)
+{
+    if (s->graph) { cudaGraphExecDestroy(s->graph); s->graph = nullptr; }
+    const long long before = s->launches;
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+    for (int i = 0; i < s->graph_chunk; ++i) enqueue_substep(s);
+    CK(cudaStreamEndCapture(s->stream, &g));
+    s->launches_per_substep = (int)((s->launches - before) / s->graph_chunk);
+    s->launches = before;            // capture enqueues nothing; replays are counted
+    cudaError_t e = cudaGraphInstantiate(&s->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(BRX_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    s->graph_dirty = false;
+    s->graph_built_chunk = s->graph_chunk;
+    return BRX_OK;
+}
+
+extern "C" int brx_advance(brx_solver *s, double dt, double time, brx_advance_stats *stats)
+{
+    TRY(ensure_ready(s));
+    if (!(dt > 0) || !std::isfinite(dt) || !std::isfinite(time)) return fail(BRX_ERR_ARGUMENT, "dt must be finite and positive");
+    if (s->graph_dirty || !s->graph) TRY(build_graph(s));
+    begin_interval(s, dt, time, false);
+    CK(cudaMemcpyAsync(s->d_ctrl, s->h_ctrl, sizeof(Ctrl) * s->nscen, cudaMemcpyHostToDevice, s->stream));
+    // every scenario ends within max_substeps accepted + 101 rejected trials
+    const int max_replays = (4096 + 102) / s->graph_chunk + 2;
+    bool all_done = false;
+    for (int r = 0; r < max_replays && !all_done; ++r) {
+        CK(cudaGraphLaunch(s->graph, s->stream));
+        s->launches += (long long)s->launches_per_substep * s->graph_chunk;
+        CK(cudaMemcpyAsync(s->h_ctrl, s->d_ctrl, sizeof(Ctrl) * s->nscen, cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        all_done = true;
+        for (int i = 0; i < s->nscen; ++i) all_done = all_done && s->h_ctrl[i].done;
+    }
+    k_commit<<<s->grid_c256, 256, 0, s->stream>>>(s->mesh, s->state, s->d_ctrl);
+    s->launches++;
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s->stream));
+    int rc = BRX_OK;
+    for (int i = 0; i < s->nscen; ++i) {
+        Ctrl &c = s->h_ctrl[i];
+        if (!c.active) continue;
+        if (c.failed || !c.done) rc = BRX_ERR_REJECTED;
+        else s->hint[i] = c.hint;
+        if (stats) {
+            stats[i].substeps = c.substeps; stats[i].rejections = c.rejections;
+            stats[i].failed = c.done ? c.failed : 3; stats[i].pad = 0;
+            stats[i].min_dt = c.min_dt; stats[i].max_dt = c.max_dt;
+            stats[i].accepted_cfl_max = c.cfl_max; stats[i].hint = c.hint;
+        }
+        c.cur = 0;
+    }
+    if (rc) return fail(rc, "a scenario could not complete the interval");
+    return BRX_OK;
+}
+
+extern "C" int brx_substep(brx_solver *s, double dt, double time, unsigned *status, double *peak)
+{
+    TRY(ensure_ready(s));
+    if (!(dt > 0) || !std::isfinite(dt)) return fail(BRX_ERR_ARGUMENT, "dt must be finite and positive");
+    begin_interval(s, dt, time, true);
+    for (int i = 0; i < s->nscen; ++i) s->h_ctrl[i].max_substeps = 4096;
+    CK(cudaMemcpyAsync(s->d_ctrl, s->h_ctrl, sizeof(Ctrl) * s->nscen, cudaMemcpyHostToDevice, s->stream));
+    // the trial without the controller: its statuses are read before control runs
+    k_open_drag<<<s->grid_c256, 256, 0, s->stream>>>(s->mesh, s->state, s->d_ctrl);
+    s->launches++;
+    enqueue_stage(s, 1, nullptr);
+    enqueue_stage(s, 2, nullptr);
+    CK(cudaMemcpyAsync(s->h_ctrl, s->d_ctrl, sizeof(Ctrl) * s->nscen, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    std::vector<Ctrl> trial(s->h_ctrl, s->h_ctrl + s->nscen);
+    k_control<<<(s->nscen + 127) / 128, 128, 0, s->stream>>>(s->d_ctrl, s->nscen);
+    k_commit<<<s->grid_c256, 256, 0, s->stream>>>(s->mesh, s->state, s->d_ctrl);
+    s->launches += 2;
+    CK(cudaMemcpyAsync(s->h_ctrl, s->d_ctrl, sizeof(Ctrl) * s->nscen, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s->stream));
+    for (int i = 0; i < s->nscen; ++i) {
+        const Ctrl &t = trial[i];
+        const double f1 = bits_to_double(t.peak1), f2 = bits_to_double(t.peak2);
+        unsigned st = t.status1 | t.status2;
+        if (!(t.status1 & ST_PRE) && t.trial * f1 > t.cfl * (1 + 1e-12)) st |= 32u;
+        else if (!(t.status1) && !(t.status2 & ST_PRE) && t.trial * f2 > t.cfl * (1 + 1e-12)) st |= 32u;
+        if (status) status[i] = st;
+        if (peak) peak[i] = (t.status1 & ST_PRE) ? 0.0 : ((t.status1 || (t.status2 & ST_PRE)) ? f1 : std::fmax(f1, f2));
+        s->h_ctrl[i].cur = 0;
+    }
+    return BRX_OK;
+}
+
+extern "C" int brx_rate(brx_solver *s, double dt, double time, double *rate_device, double *water_device,
+                        unsigned *status, double *freq)
+{
+    TRY(ensure_ready(s));
+    if (!rate_device || !water_device) return fail(BRX_ERR_ARGUMENT, "null output buffer");
+    begin_interval(s, dt, time, true);
+    CK(cudaMemcpyAsync(s->d_ctrl, s->h_ctrl, sizeof(Ctrl) * s->nscen, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemcpyAsync(s->state.work, s->state.q[0], sizeof(double) * 3 * s->nc, cudaMemcpyDeviceToDevice, s->stream));
+    enqueue_stage(s, 1, rate_device);
+    k_water_out<<<s->grid_f256, 256, 0, s->stream>>>(s->mesh, s->work, water_device);
+    s->launches++;
+    CK(cudaMemcpyAsync(s->h_ctrl, s->d_ctrl, sizeof(Ctrl) * s->nscen, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s->stream));
+    for (int i = 0; i < s->nscen; ++i) {
+        const Ctrl &t = s->h_ctrl[i];
+        const double f1 = bits_to_double(t.peak1);
+        unsigned st = t.status1;
+        if (!(st & ST_PRE) && dt * f1 > t.cfl * (1 + 1e-12)) st |= 32u;
+        if (status) status[i] = st;
+        if (freq) freq[i] = f1;
+    }
+    return BRX_OK;
+}
+
+extern "C" int brx_profile_substep(brx_solver *s, double dt, double time, int cap, double *ms, int *kind, int *count)
+{
+    TRY(ensure_ready(s));
+    if (!ms || !kind || !count || cap < 1) return fail(BRX_ERR_ARGUMENT, "null or empty profile buffers");
+    if (!(dt > 0) || !std::isfinite(dt)) return fail(BRX_ERR_ARGUMENT, "dt must be finite and positive");
+    begin_interval(s, dt, time, true);
+    CK(cudaMemcpyAsync(s->d_ctrl, s->h_ctrl, sizeof(Ctrl) * s->nscen, cudaMemcpyHostToDevice, s->stream));
+    std::vector<cudaEvent_t> ev;
+    std::vector<int> kinds;
+    auto mark = [&](int k) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        cudaEventRecord(e, s->stream);
+        ev.push_back(e);
+        if (k >= 0) kinds.push_back(k);
+    };
+    cudaStream_t st = s->stream;
+    mark(-1);
+    k_open_drag<<<s->grid_c256, 256, 0, st>>>(s->mesh, s->state, s->d_ctrl); mark(0);
+    for (int stage = 1; stage <= 2; ++stage) {
+        if (s->nslot) { k_boundary<<<s->nscen, 256, 0, st>>>(s->mesh, s->state, s->bnd, s->d_ctrl, stage); mark(1); }
+        if (s->maxdeg <= 4) k_cells<4><<<s->grid_c, 128, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage);
+        else k_cells<MAX_CELL_FACES><<<s->grid_c, 128, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage);
+        mark(2);
+        k_faces<<<s->grid_f, 128, 0, st>>>(s->mesh, s->state, s->bnd, s->d_ctrl, s->work, stage); mark(3);
+        k_gather<<<s->grid_c256, 256, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage); mark(4);
+        k_limit<<<s->grid_f256, 256, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage); mark(5);
+        k_update<<<s->grid_c256, 256, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage, nullptr); mark(6);
+    }
+    k_control<<<(s->nscen + 127) / 128, 128, 0, st>>>(s->d_ctrl, s->nscen); mark(7);
+    k_commit<<<s->grid_c256, 256, 0, st>>>(s->mesh, s->state, s->d_ctrl);
+    s->launches += (long long)kinds.size() + 1;
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(st));
+    const int n = std::min(cap, (int)kinds.size());
+    for (int i = 0; i < n; ++i) {
+        float t = 0.f;
+        cudaEventElapsedTime(&t, ev[i], ev[i + 1]);
+        ms[i] = t;
+        kind[i] = kinds[i];
+    }
+    *count = n;
+    for (auto e : ev) cudaEventDestroy(e);
+    for (int i = 0; i < s->nscen; ++i) s->h_ctrl[i].cur = 0;
+    return BRX_OK;
+}

@@ -1,0 +1,941 @@
+// Kernels of one SSPRK(2,2) substep of the augmented f-wave river step.
+//
+// One substep = drag(dt/2) -> 2 x [boundary -> cells -> faces -> gather ->
+// limit -> update] -> control. Every kernel is batch-aware: cells and faces
+// of many scenarios are packed into one index space, each element carries
+// its scenario id, and each scenario owns a Ctrl block on the device that
+// holds its clock (trial dt, elapsed time, hint) and its rejection status.
+// The plain form is a batch of one.
+//
+// Restated from (file:line in the reference):
+//   boundary     src/braids_core/sediment/river_exterior_bed.h:29-174,
+//                src/braids_core/hydraulics/outlet_feasibility.py:25-38
+//   cells        src/braids_support/gpu_fwave/reconstruction.cu:24-168 with the
+//                wall_bed_hydraulics transforms (wall velocity bounds, LS
+//                fallback, directional projection limiter)
+//   faces        reconstruction.cu:170-212, resident_update.cu:11-148 with the
+//                hydrostatic-reconstruction and reflecting-wall transforms,
+//                augmented_fwave.cu:264-334
+//   gather       src/braids_gpu/implicit_midpoint_fwave.cu:65-90,
+//                src/braids_core/sediment/river_midpoint.h:21-29 (inventory),
+//                river_explicit_boundary_budget.py:41-50 (reservation),
+//                river_explicit.h:13-26 (CFL frequency)
+//   limit        river_midpoint.h:30-41
+//   update       river_midpoint.h:42-49, river_explicit.py:94-117
+//   drag         river_hydraulic_drag.h:3-16, river_roughness.py:42-47
+//   control      river_explicit.py:121-154
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+#include "brx_fwave.cuh"
+
+namespace brx {
+
+constexpr double EPS = 2.2204460492503131e-16;
+constexpr double DBL_MIN_ = 2.2250738585072014e-308;
+
+// Status bits of one stage. PRE bits are raised before the reference computes
+// its CFL frequency, so a stage that raised one does not feed the step hint.
+enum : unsigned {
+    ST_SPATIAL = 1u,      // invalid state, boundary, reconstruction or face status
+    ST_BUDGET = 2u,       // prescribed boundary exceeds the owner's stock
+    ST_RATE = 4u,         // nonfinite rate
+    ST_ENDPOINT = 8u,     // negative / nonfinite stage result
+    ST_FREQ = 16u,        // nonfinite CFL frequency
+    ST_PRE = ST_SPATIAL | ST_BUDGET | ST_RATE | ST_FREQ,
+};
+
+// Per-scenario clock and controls, resident on the device.
+struct Ctrl {
+    // controls
+    double grav, dry, cfl, speed_limit, roughness_value;
+    int roughness_mode, active;       // active: scenario takes part in this interval
+    // interval
+    double dt_outer, time0, elapsed, hint, floor_, trial;
+    int truncated, substeps, rejections, done;
+    int failed, cur, max_substeps, pad0;
+    // this trial
+    unsigned status1, status2;
+    unsigned long long peak1, peak2;  // bit patterns of nonnegative doubles
+    // diagnostics
+    double min_dt, max_dt, cfl_max;
+    double accepted_water_time;       // sum of accepted trial lengths (== elapsed)
+};
+
+struct MeshDev {
+    int nc, nf, nadj, nscen;
+    const int *owner, *neighbour, *bid, *offset, *faces, *signs;
+    const int *bslot;        // per face: boundary slot (open faces) or -1
+    const int *bmode;        // per face: hydraulic mode of its open segment, else 0
+    const int *cell_sid, *face_sid;
+    const int *cflags;       // per cell: bit0 owns an open face
+    const double *normal, *length, *area;
+    const double *ls_matrix, *ls_weight, *ls_delta;
+    const double *disp, *disp_unit, *disp_len, *distance;
+};
+
+struct BoundaryDev {
+    int nseg, nslot, nown;
+    const int *scen_seg;     // (nscen+1) segment range per scenario
+    const int *scen_own;     // (nscen+1) unique-owner range per scenario
+    const int *seg_off;      // (nseg+1) slot range per segment
+    const int *slot_face;    // (nslot)
+    const int *seg_mode, *stage_policy;
+    const double *ext_bed;   // (nslot)
+    double *forcing;         // (2,nseg) sampled per stage
+    int table_len;
+    const double *table_time;   // (table_len)
+    const double *table_value;  // (2, nseg, table_len)
+    const int *own_cell, *own_off, *own_slot;  // unique owners, CSR into slots (boundary order)
+    double *terms;           // (3, nslot) scratch: stage terms and weights
+    double *trace, *flux;    // (3, nslot) each
+    double *seg_sums;        // (3, nseg): wetted stage sum, wetted width, weight total
+};
+
+// Accepted / stage state buffers.
+struct StateDev {
+    double *q[2];            // (3,nc) ping-pong: ctrl.cur holds the accepted state
+    double *work;            // (3,nc) base after the opening drag
+    double *q1;              // (3,nc) first-stage result
+    const double *z;         // (nc) bed
+};
+
+// 128-byte cell record written by the cell kernel, read by the face kernel.
+struct __align__(16) CellRec {
+    double h, eta, u, v, b;
+    double gx[4], gy[4];
+    int flags, pad;          // bit0 flatten (hydro_constant), bit1 active
+    double pad2;
+};
+static_assert(sizeof(CellRec) == 128, "cell record is one 128-byte line");
+
+struct Work {
+    CellRec *rec;            // (nc)
+    double2 *ws;             // (nf) water, CFL speed
+    double4_32a *gf;             // (nf) pressure-deviation momentum flux: left x,y, right x,y
+    double4_32a *lim;            // (nf) limited water, momentum correction x,y
+    double *rate;            // (3,nc)
+    double *theta;           // (nc)
+};
+
+__device__ __forceinline__ void atomic_max_nonneg(unsigned long long *addr, double v)
+{
+    // nonnegative doubles (including +inf) order like their bit patterns
+    atomicMax(addr, (unsigned long long)__double_as_longlong(v));
+}
+
+__host__ __device__ __forceinline__ double bits_to_double(unsigned long long b)
+{
+#ifdef __CUDA_ARCH__
+    return __longlong_as_double((long long)b);
+#else
+    double d;
+    memcpy(&d, &b, sizeof d);
+    return d;
+#endif
+}
+
+// Stage 2 and the trailing kernels skip a scenario whose first stage failed.
+__device__ __forceinline__ bool stage1_failed(const Ctrl &c)
+{
+    if (c.status1) return true;
+    const double f = bits_to_double(c.peak1);
+    return c.trial * f > c.cfl * (1 + 1e-12);
+}
+
+__device__ __forceinline__ bool skip_stage(const Ctrl &c, int stage)
+{
+    if (!c.active || c.done) return true;
+    return stage == 2 && stage1_failed(c);
+}
+
+__device__ __forceinline__ void raise_status(Ctrl &c, int stage, unsigned bits)
+{
+    atomicOr(stage == 1 ? &c.status1 : &c.status2, bits);
+}
+
+// ---------------------------------------------------------------------------
+// Drag: cell-local implicit Manning/Chezy friction over dt_scale * trial.
+// src/braids_core/sediment/river_hydraulic_drag.h:3-16
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double chezy(int method, double depth, double value)
+{
+    if (method == 1) return value;
+    if (method == 2) return pow(depth, 1. / 6.) / value;
+    if (method == 3) return sqrt(9.81) / .41 * log1p(30. * depth / (exp(1.) * value));
+    return 18. * log10(12. * fmax(.5, depth / value));
+}
+
+__device__ __forceinline__ void drag_cell(const Ctrl &ct, double dt, double &h, double &hu, double &hv)
+{
+    if (h <= ct.dry) { hu = 0.; hv = 0.; return; }
+    const double c = chezy(ct.roughness_mode, h, ct.roughness_value);
+    const double speed = sqrt(hu * hu + hv * hv) / h;
+    const double factor = 1. / (1. + dt * ct.grav * speed / (c * c * h));
+    hu *= factor;
+    hv *= factor;
+}
+
+// work = drag(accepted, trial/2)
+__global__ void k_open_drag(MeshDev m, StateDev s, Ctrl *ctrl)
+{
+    const int nc = m.nc;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        const Ctrl &ct = ctrl[m.cell_sid[c]];
+        if (!ct.active || ct.done) continue;
+        const double *q = s.q[ct.cur];
+        double h = q[c], hu = q[nc + c], hv = q[2 * nc + c];
+        drag_cell(ct, .5 * ct.trial, h, hu, hv);
+        s.work[c] = h; s.work[nc + c] = hu; s.work[2 * nc + c] = hv;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Boundary: one CTA per scenario evaluates its open segments (stage sums,
+// conveyance weights, exterior traces/fluxes) and caps outlet outflow by the
+// owners' stage-start stock. Sums use the reference's fixed tree: 64-face
+// tiles from each segment start, then the tiles in order.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double exterior_chezy(int mode, double h, double parameter, double floor_, double gravity,
+                                                  int waqua)
+{
+    const double d = fmax(h, floor_);
+    if (mode == 1) return parameter;
+    if (mode == 2) return pow(d, 1. / 6.) / parameter;
+    return waqua ? 18. * log10(12. * fmax(.5, d / parameter))
+                 : sqrt(gravity) / .41 * log1p(30. * d / (exp(1.) * parameter));
+}
+
+__device__ __forceinline__ void stage_wave(double h, double un, double target, double gravity, double &depth,
+                                           double &velocity)
+{
+    const double c = sqrt(gravity * h);
+    depth = h; velocity = un;
+    if (target > h) {
+        const double k = sqrt(.5 * gravity * (1. / target + 1. / h));
+        const double shock = un - target * k;
+        if (shock >= 0.) return;
+        depth = target; velocity = un - (target - h) * k;
+        return;
+    }
+    if (un - c >= 0.) return;
+    const double cb = sqrt(gravity * target), ub = un + 2. * (c - cb);
+    if (ub - cb > 0. || target == 0.) {
+        velocity = (un + 2. * c) / 3.; depth = velocity * velocity / gravity;
+        return;
+    }
+    depth = target; velocity = ub;
+}
+
+__device__ __forceinline__ bool is_outlet(int mode)
+{
+    return mode == 2 || mode == 3 || mode == 4 || mode == 5 || mode == 10 || mode == 11;
+}
+
+// Sums of field `row` of b.terms over each segment of the scenario, in the
+// 64-tile tree. Called by all threads of the CTA; result in b.seg_sums[out_row].
+__device__ void segment_sums(const BoundaryDev &b, int s0, int s1, int row, int out_row, double *tile_buf)
+{
+    // tile partials: one thread per (segment, tile)
+    int ntile_total = 0;
+    for (int s = s0; s < s1; ++s) ntile_total += max(1, (b.seg_off[s + 1] - b.seg_off[s] + 63) / 64);
+    for (int t = threadIdx.x; t < ntile_total; t += blockDim.x) {
+        int s = s0, rem = t;
+        while (rem >= max(1, (b.seg_off[s + 1] - b.seg_off[s] + 63) / 64)) {
+            rem -= max(1, (b.seg_off[s + 1] - b.seg_off[s] + 63) / 64);
+            ++s;
+        }
+        const int start = b.seg_off[s] + 64 * rem, end = min(b.seg_off[s + 1], start + 64);
+        double sum = 0.;
+        for (int k = start; k < end; ++k) sum += b.terms[(size_t)row * b.nslot + k];
+        tile_buf[t] = sum;
+    }
+    __syncthreads();
+    for (int s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
+        int first = 0;
+        for (int u = s0; u < s; ++u) first += max(1, (b.seg_off[u + 1] - b.seg_off[u] + 63) / 64);
+        const int nt = max(1, (b.seg_off[s + 1] - b.seg_off[s] + 63) / 64);
+        double total = 0.;
+        for (int t = 0; t < nt; ++t) total += tile_buf[first + t];
+        b.seg_sums[(size_t)out_row * b.nseg + s] = total;
+    }
+    __syncthreads();
+}
+
+constexpr int BOUNDARY_TILES = 1024;   // tile slots of 64 faces per scenario (checked at set-up)
+
+__global__ void k_boundary(MeshDev m, StateDev s, BoundaryDev b, Ctrl *ctrl, int stage)
+{
+    __shared__ double tile_buf[BOUNDARY_TILES];
+    const int sid = blockIdx.x;
+    Ctrl &ct = ctrl[sid];
+    if (skip_stage(ct, stage)) return;
+    const int s0 = b.scen_seg[sid], s1 = b.scen_seg[sid + 1];
+    if (s0 == s1) return;
+    const int nc = m.nc;
+    const double *q = stage == 1 ? s.work : s.q1;
+    const double *base = q;                       // stage-start stock of this stage
+    const double *z = s.z;
+    const double dry = ct.dry, grav = ct.grav;
+    const double t = ct.time0 + ct.elapsed + (stage == 2 ? ct.trial : 0.0);
+    // forcing at the stage clock (piecewise linear tables, else constant)
+    if (b.table_len > 0)
+        for (int sg = s0 + threadIdx.x; sg < s1; sg += blockDim.x)
+            for (int row = 0; row < 2; ++row) {
+                const int L = b.table_len;
+                const double *y = b.table_value + ((size_t)row * b.nseg + sg) * L;
+                double val;
+                if (t <= b.table_time[0]) val = y[0];
+                else if (t >= b.table_time[L - 1]) val = y[L - 1];
+                else {
+                    int i = 0;
+                    while (b.table_time[i + 1] < t) ++i;
+                    const double sfrac = (t - b.table_time[i]) / (b.table_time[i + 1] - b.table_time[i]);
+                    val = y[i] + (y[i + 1] - y[i]) * sfrac;
+                }
+                b.forcing[(size_t)row * b.nseg + sg] = val;
+            }
+    const int k0 = b.seg_off[s0], k1 = b.seg_off[s1];
+    for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+        const int f = b.slot_face[k], c = m.owner[f];
+        const double w = q[c] > dry ? m.length[f] : 0.;
+        b.terms[k] = (z[c] + q[c]) * w;
+        b.terms[(size_t)b.nslot + k] = w;
+    }
+    __syncthreads();
+    segment_sums(b, s0, s1, 0, 0, tile_buf);
+    segment_sums(b, s0, s1, 1, 1, tile_buf);
+    const int rmode = ct.roughness_mode < 3 ? ct.roughness_mode : 3;
+    const int waqua = ct.roughness_mode == 4;
+    const int nseg = b.nseg;
+    for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+        const int f = b.slot_face[k], c = m.owner[f], sg = m.bid[f];
+        double w = 0.;
+        const double bed = b.ext_bed[k];
+        const int mode = b.seg_mode[sg];
+        if (mode == 9) {
+            const double h = fmax(b.forcing[nseg + sg] - bed, 0.);
+            if (h > dry) w = h * m.length[f];
+        } else if (mode == 6 && b.seg_sums[nseg + sg] > 0.) {
+            const double h = fmax(q[c] + z[c] - bed, 0.);
+            const double section = fmax(b.seg_sums[sg] / b.seg_sums[nseg + sg] - bed, 0.);
+            if (h > dry && section > 0.)
+                w = pow(section, 1.5) * exterior_chezy(rmode, h, ct.roughness_value, dry, grav, waqua) * m.length[f];
+        }
+        b.terms[2 * (size_t)b.nslot + k] = w;
+    }
+    __syncthreads();
+    segment_sums(b, s0, s1, 2, 2, tile_buf);
+    unsigned bad = 0;
+    for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+        const int f = b.slot_face[k], c = m.owner[f], sg = m.bid[f], mode = b.seg_mode[sg];
+        double tr0 = 0., tr1 = 0., tr2 = 0., fl0 = 0., fl1 = 0., fl2 = 0.;
+        const double h0 = q[c], nx = m.normal[f], ny = m.normal[m.nf + f], bed = b.ext_bed[k];
+        const double total = b.seg_sums[2 * (size_t)nseg + sg];
+        const double Q = b.forcing[sg], stagev = b.forcing[nseg + sg];
+        int st = 0;
+        if (!(mode == 4 || mode == 5 || mode == 10 || mode == 11)) {
+            double h = fmax(h0 + z[c] - bed, 0.), geometric = h, ux = 0., uy = 0.;
+            if (h0 > dry) { ux = q[nc + c] / h0; uy = q[2 * nc + c] / h0; }
+            double un = ux * nx + uy * ny, tx = ux - un * nx, ty = uy - un * ny, normal_speed = 0.;
+            if (mode == 9) {
+                h = fmax(stagev - bed, 0.); tx = ty = 0.;
+                if (Q > 0. && total <= 0.) st = 1;
+                else if (h > dry && Q > 0.) normal_speed = -Q / total;
+            } else if (mode == 6) {
+                if (Q > 0. && total <= 0.) st = 1;
+                else if (h > dry && Q > 0.) normal_speed = -Q * b.terms[2 * (size_t)b.nslot + k] / (total * h * m.length[f]);
+            } else if (mode == 3) {
+                if (h0 <= dry) h = 0.;
+                else if (h > dry) {
+                    if (un < sqrt(grav * h)) st = 6;
+                    else normal_speed = un;
+                }
+            } else if (mode == 2) {
+                const double prescribed = fmax(stagev - bed, 0.);
+                const int policy = b.stage_policy[sg];
+                if (policy && (h0 <= dry || h <= dry) && prescribed > dry) st = 4;
+                else {
+                    if (h0 <= dry) h = 0.;
+                    if (h > dry) {
+                        const double wave = sqrt(grav * h);
+                        if (un <= -wave) {
+                            if (policy) st = 5;
+                            else { normal_speed = 0.; tx = ty = 0.; }
+                        } else {
+                            const double target = fmax(stagev - bed, 0.);
+                            double hb, ub;
+                            stage_wave(h, un, target, grav, hb, ub);
+                            if (ub < 0. && policy) {
+                                if (ub <= -sqrt(grav * hb)) st = 5;
+                                else { h = hb; normal_speed = ub; tx = ty = 0.; }
+                            } else if (ub < 0.) { normal_speed = 0.; tx = ty = 0.; }
+                            else { h = hb; normal_speed = ub; }
+                        }
+                    }
+                }
+            } else st = 2;
+            if (!st && (!isfinite(h) || !isfinite(normal_speed) || h < 0. ||
+                        sqrt(normal_speed * normal_speed + tx * tx + ty * ty) > ct.speed_limit)) st = 3;
+            if (!st) {
+                double water = 0., fx = 0., fy = 0.;
+                if (h > dry) {
+                    tr0 = h;
+                    tr1 = h * (normal_speed * nx + tx);
+                    tr2 = h * (normal_speed * ny + ty);
+                    water = tr1 * nx + tr2 * ny;
+                    fx = water * tr1 / h + .5 * grav * h * h * nx;
+                    fy = water * tr2 / h + .5 * grav * h * h * ny;
+                }
+                double pressure = h0 > dry ? .5 * grav * (h0 * h0 - geometric * geometric) : 0.;
+                if (mode == 9 && h <= dry) pressure = h0 > dry ? .5 * grav * h0 * h0 : 0.;
+                fl0 = water; fl1 = fx + pressure * nx; fl2 = fy + pressure * ny;
+            }
+        }
+        if (st) bad = 1;
+        b.trace[k] = tr0; b.trace[(size_t)b.nslot + k] = tr1; b.trace[2 * (size_t)b.nslot + k] = tr2;
+        b.flux[k] = fl0; b.flux[(size_t)b.nslot + k] = fl1; b.flux[2 * (size_t)b.nslot + k] = fl2;
+    }
+    if (bad) raise_status(ct, stage, ST_SPATIAL);
+    __syncthreads();
+    // outlet stock cap, one thread per unique owner, its faces in boundary order
+    const int u0 = b.scen_own[sid], u1 = b.scen_own[sid + 1];
+    for (int u = u0 + threadIdx.x; u < u1; u += blockDim.x) {
+        const int c = b.own_cell[u];
+        double total = 0., reserved = 0.;
+        for (int j = b.own_off[u]; j < b.own_off[u + 1]; ++j) {
+            const int k = b.own_slot[j], f = b.slot_face[k];
+            const double debit = fmax(b.flux[k], 0.) * m.length[f];
+            if (is_outlet(b.seg_mode[m.bid[f]])) total += debit; else reserved += debit;
+        }
+        const double available = fmax(0., base[c] * m.area[c] / ct.trial - reserved);
+        const double ratio = fmin(1., available / fmax(total, 1e-300)) * (1. - 32. * EPS);
+        const double factor = total > available ? ratio : 1.;
+        for (int j = b.own_off[u]; j < b.own_off[u + 1]; ++j) {
+            const int k = b.own_slot[j], f = b.slot_face[k];
+            const double water = b.flux[k];
+            const double scale = (is_outlet(b.seg_mode[m.bid[f]]) && water > 0.) ? factor : 1.;
+            const double depth = b.trace[k], denom = fmax(depth, 1e-300);
+            const double ux = depth > 0. ? b.trace[(size_t)b.nslot + k] / denom : 0.;
+            const double uy = depth > 0. ? b.trace[2 * (size_t)b.nslot + k] / denom : 0.;
+            b.flux[(size_t)b.nslot + k] += (scale * scale - 1.) * water * ux;
+            b.flux[2 * (size_t)b.nslot + k] += (scale * scale - 1.) * water * uy;
+            b.flux[k] = water * scale;
+            b.trace[(size_t)b.nslot + k] *= scale;
+            b.trace[2 * (size_t)b.nslot + k] *= scale;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Cells: primitive values, limited least-squares gradients, flattening flag.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool feasible(double x, double y, int count, const double *ax, const double *ay,
+                                         const double *bb)
+{
+    for (int i = 0; i < count; ++i)
+        if (ax[i] * x + ay[i] * y > bb[i] + 2.e-14) return false;
+    return true;
+}
+
+__device__ __noinline__ void project_pair(double &x, double &y, int count, const double *ax, const double *ay,
+                                          const double *bb)
+{
+    const double rx = x, ry = y;
+    if (feasible(rx, ry, count, ax, ay, bb)) return;
+    double bx = 0., by = 0., best = rx * rx + ry * ry;
+    for (int i = 0; i < count; ++i) {
+        const double dot = ax[i] * rx + ay[i] * ry - bb[i];
+        double cx = rx - dot * ax[i], cy = ry - dot * ay[i];
+        double d = (cx - rx) * (cx - rx) + (cy - ry) * (cy - ry);
+        if (d < best && feasible(cx, cy, count, ax, ay, bb)) { bx = cx; by = cy; best = d; }
+        for (int j = 0; j < i; ++j) {
+            const double det = ax[i] * ay[j] - ay[i] * ax[j];
+            if (fabs(det) < 1.e-12) continue;
+            cx = (bb[i] * ay[j] - ay[i] * bb[j]) / det;
+            cy = (ax[i] * bb[j] - bb[i] * ax[j]) / det;
+            d = (cx - rx) * (cx - rx) + (cy - ry) * (cy - ry);
+            if (d < best && feasible(cx, cy, count, ax, ay, bb)) { bx = cx; by = cy; best = d; }
+        }
+    }
+    x = bx; y = by;
+}
+
+constexpr int MAX_CELL_FACES = 32;
+
+// MAXF bounds the faces of one cell (4 for triangle/quad meshes, 32 in general).
+template <int MAXF>
+__global__ void __launch_bounds__(128) k_cells(MeshDev m, StateDev s, Ctrl *ctrl, Work w, int stage)
+{
+    const int nc = m.nc, nf = m.nf, nadj = m.nadj;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        Ctrl &ct = ctrl[m.cell_sid[c]];
+        if (skip_stage(ct, stage)) continue;
+        const double *q = stage == 1 ? s.work : s.q1;
+        const double *z = s.z;
+        const double dry = ct.dry, grav = ct.grav;
+        const double h = q[c], hu = q[nc + c], hv = q[2 * nc + c], zc = z[c];
+        if (h < 0.0 || !isfinite(h) || !isfinite(zc) || !isfinite(hu) || !isfinite(hv))
+            raise_status(ct, stage, ST_SPATIAL);
+        double centre[4] = {h + zc, 0., 0., zc};
+        if (h > dry) { centre[1] = hu / h; centre[2] = hv / h; }
+        double lo[4], hi[4], gx[4] = {0., 0., 0., 0.}, gy[4] = {0., 0., 0., 0.};
+#pragma unroll
+        for (int p = 0; p < 4; ++p) { lo[p] = centre[p]; hi[p] = centre[p]; }
+        const int k0 = m.offset[c], k1 = m.offset[c + 1];
+        // active: wet, or touching an open face or a wet neighbour
+        bool active = h > dry;
+        double bx[4] = {0., 0., 0., 0.}, by[4] = {0., 0., 0., 0.};
+        for (int k = k0; k < k1; ++k) {
+            const int f = m.faces[k];
+            const int n = m.signs[k] < 0 ? m.owner[f] : m.neighbour[f];
+            if (n < 0) { if (m.bid[f] >= 0) active = true; continue; }
+            const double hn = q[n], zn = z[n];
+            if (hn > dry) active = true;
+            double vn[4] = {hn + zn, 0., 0., zn};
+            if (hn > dry) { vn[1] = q[nc + n] / hn; vn[2] = q[2 * nc + n] / hn; }
+            const double rx = m.ls_delta[k], ry = m.ls_delta[nadj + k], wt = m.ls_weight[k];
+#pragma unroll
+            for (int p = 0; p < 4; ++p) {
+                double adj = vn[p];
+                if (p == 0 && centre[0] - centre[3] > dry && vn[0] - vn[3] <= dry && vn[3] >= centre[0]) adj = centre[0];
+                bx[p] += wt * rx * (adj - centre[p]);
+                by[p] += wt * ry * (adj - centre[p]);
+                lo[p] = fmin(lo[p], adj); hi[p] = fmax(hi[p], adj);
+            }
+        }
+        if (active) {
+            const double a11 = m.ls_matrix[c], a12 = m.ls_matrix[nc + c], a22 = m.ls_matrix[2 * nc + c],
+                         det = m.ls_matrix[3 * nc + c];
+            if (a11 + a22 > 0.0) {
+                if (h > dry)
+                    for (int k = k0; k < k1; ++k) {
+                        const int f = m.faces[k];
+                        if (m.neighbour[f] >= 0 || m.bid[f] >= 0) continue;
+                        const double nx = m.normal[f], ny = m.normal[nf + f];
+                        const double un = centre[1] * nx + centre[2] * ny;
+                        const double mx = centre[1] - 2. * un * nx, my = centre[2] - 2. * un * ny;
+                        lo[1] = fmin(lo[1], mx); hi[1] = fmax(hi[1], mx);
+                        lo[2] = fmin(lo[2], my); hi[2] = fmax(hi[2], my);
+                    }
+                const bool full = det > 1.e-12 * ((a11 + a22) * (a11 + a22));
+#pragma unroll
+                for (int p = 0; p < 4; ++p) {
+                    if (full) {
+                        gx[p] = (a22 * bx[p] - a12 * by[p]) / det;
+                        gy[p] = (a11 * by[p] - a12 * bx[p]) / det;
+                    } else {
+                        gx[p] = (a11 * bx[p] + a12 * by[p]) / ((a11 + a22) * (a11 + a22));
+                        gy[p] = (a12 * bx[p] + a22 * by[p]) / ((a11 + a22) * (a11 + a22));
+                    }
+                }
+                const double hh = centre[0] - centre[3];
+                const double sq = hh > dry ? sqrt(grav * hh) : 0.;
+                const double bedtol = 64.0 * EPS * fmax(1.0, fabs(centre[3]));
+                double theta1 = 1., theta2 = 1.;
+                double ax0[2 * MAXF], ay0[2 * MAXF], b0[2 * MAXF];
+                double ax3[2 * MAXF], ay3[2 * MAXF], b3[2 * MAXF];
+                int n0 = 0, n3 = 0;
+                for (int k = k0; k < k1; ++k) {
+                    const int f = m.faces[k];
+                    const int side = m.signs[k] < 0;
+                    const double rx = m.disp[side * nf + f], ry = m.disp[(2 + side) * nf + f];
+                    // an open stage outlet with a subcritical wet owner keeps its bed slope
+                    if (m.bmode[f] == 2 && m.neighbour[f] < 0 && hh > dry &&
+                        fabs(centre[1] * m.normal[f] + centre[2] * m.normal[nf + f]) < sq &&
+                        fabs(gx[3] * rx + gy[3] * ry) > bedtol) continue;
+#pragma unroll
+                    for (int p = 1; p < 3; ++p) {
+                        const double d = gx[p] * rx + gy[p] * ry;
+                        if (fabs(d) <= 64.0 * EPS * fmax(1.0, fmax(fabs(centre[p]), fmax(fabs(lo[p]), fabs(hi[p])))))
+                            continue;
+                        double &th = p == 1 ? theta1 : theta2;
+                        if (d > 0.) th = fmin(th, (hi[p] - centre[p]) / d);
+                        if (d < 0.) th = fmin(th, (lo[p] - centre[p]) / d);
+                    }
+                    const double len = m.disp_len[side * nf + f];
+                    if (len <= 0.) continue;
+                    const double ux = m.disp_unit[side * nf + f], uy = m.disp_unit[(2 + side) * nf + f];
+                    ax0[n0] = ux; ay0[n0] = uy; b0[n0++] = fmax(0., hi[0] - centre[0]) / len;
+                    ax0[n0] = -ux; ay0[n0] = -uy; b0[n0++] = fmax(0., centre[0] - lo[0]) / len;
+                    if (m.neighbour[f] < 0 && m.bid[f] < 0) continue;   // walls do not bound the bed
+                    ax3[n3] = ux; ay3[n3] = uy; b3[n3++] = fmax(0., hi[3] - centre[3]) / len;
+                    ax3[n3] = -ux; ay3[n3] = -uy; b3[n3++] = fmax(0., centre[3] - lo[3]) / len;
+                }
+                double px0 = gx[0], py0 = gy[0], px3 = gx[3], py3 = gy[3];
+                project_pair(px0, py0, n0, ax0, ay0, b0);
+                project_pair(px3, py3, n3, ax3, ay3, b3);
+                gx[1] *= fmax(0., theta1); gy[1] *= fmax(0., theta1);
+                gx[2] *= fmax(0., theta2); gy[2] *= fmax(0., theta2);
+                gx[0] = px0; gy[0] = py0; gx[3] = px3; gy[3] = py3;
+            }
+        }
+        bool flatten = h <= dry;
+        if (!flatten)
+            for (int k = k0; k < k1; ++k) {
+                const int f = m.faces[k];
+                const int side = (c == m.owner[f]) ? 0 : 1;
+                const double rx = m.disp[side * nf + f], ry = m.disp[(2 + side) * nf + f];
+                const double eta = (centre[0] + gx[0] * rx) + gy[0] * ry;
+                const double zb = (centre[3] + gx[3] * rx) + gy[3] * ry;
+                if (eta - zb <= dry || fabs(zb - centre[3]) >= h) { flatten = true; break; }
+            }
+        CellRec r;
+        r.h = h; r.eta = centre[0]; r.u = centre[1]; r.v = centre[2]; r.b = centre[3];
+#pragma unroll
+        for (int p = 0; p < 4; ++p) { r.gx[p] = gx[p]; r.gy[p] = gy[p]; }
+        r.flags = (flatten ? 1 : 0) | (active ? 2 : 0);
+        r.pad = 0; r.pad2 = 0.;
+        w.rec[c] = r;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Faces: traces, hydrostatic reconstruction, f-wave, flux assembly.
+// ---------------------------------------------------------------------------
+struct Side { double h, hu, hv, b, raw; };
+
+__device__ __forceinline__ Side face_side(const CellRec &r, double rx, double ry, double dry, bool dryface,
+                                          unsigned &bad)
+{
+    double val[4] = {(r.eta + r.gx[0] * rx) + r.gy[0] * ry, (r.u + r.gx[1] * rx) + r.gy[1] * ry,
+                     (r.v + r.gx[2] * rx) + r.gy[2] * ry, (r.b + r.gx[3] * rx) + r.gy[3] * ry};
+    const bool constant = r.flags & 1;
+    if (constant) {
+        val[0] = r.eta; val[1] = r.u; val[2] = r.v;
+        if (r.eta - r.b <= dry) val[3] = r.b;
+    }
+    if (!isfinite(val[0]) || !isfinite(val[1]) || !isfinite(val[2]) || !isfinite(val[3])) bad = 1;
+    Side o = {0., 0., 0., 0., 0.};
+    if (dryface) return o;
+    double depth = fmax(val[0] - val[3], 0.);
+    o.raw = depth;
+    if (r.h <= dry || (constant && depth <= dry)) depth = 0.;
+    o.h = depth; o.hu = depth * val[1]; o.hv = depth * val[2]; o.b = val[3];
+    return o;
+}
+
+__global__ void __launch_bounds__(128) k_faces(MeshDev m, StateDev s, BoundaryDev b, Ctrl *ctrl, Work w, int stage)
+{
+    const int nf = m.nf, nc = m.nc;
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += gridDim.x * blockDim.x) {
+        Ctrl &ct = ctrl[m.face_sid[f]];
+        if (skip_stage(ct, stage)) continue;
+        const double dry = ct.dry, grav = ct.grav;
+        const int c = m.owner[f], n = m.neighbour[f];
+        const double nx = m.normal[f], ny = m.normal[nf + f];
+        const CellRec rc = w.rec[c];
+        const double pc = .5 * grav * rc.h * rc.h;
+        const int slot = m.bslot[f];
+        if (slot >= 0) {
+            // open face: the exterior owner's flux, owner/exterior CFL speed
+            const double *q = stage == 1 ? s.work : s.q1;
+            const double fl0 = b.flux[slot], fl1 = b.flux[(size_t)b.nslot + slot], fl2 = b.flux[2 * (size_t)b.nslot + slot];
+            const double hb = b.trace[slot];
+            const double hq = q[c];
+            const double a = hq > dry ? fabs((q[nc + c] * nx + q[2 * nc + c] * ny) / hq) + sqrt(grav * hq) : 0.;
+            const double bb = hb > dry ? fabs((b.trace[(size_t)b.nslot + slot] * nx + b.trace[2 * (size_t)b.nslot + slot] * ny) / hb) +
+                                             sqrt(grav * hb) : 0.;
+            w.ws[f] = make_double2(fl0, fmax(a, bb));
+            w.gf[f] = make_double4_32a(fl1 - pc * nx, fl2 - pc * ny, 0., 0.);
+            continue;
+        }
+        CellRec rn;
+        if (n >= 0) rn = w.rec[n];
+        int kind = n >= 0 ? 1 : 2;
+        if (rc.h <= dry && (n < 0 || rn.h <= dry)) kind = 0;
+        unsigned bad = 0;
+        const Side L = face_side(rc, m.disp[f], m.disp[2 * nf + f], dry, kind == 0, bad);
+        Side R = {0., 0., 0., 0., 0.};
+        if (n >= 0) R = face_side(rn, m.disp[nf + f], m.disp[3 * nf + f], dry, kind == 0, bad);
+        double water = 0., speed = 0., l1 = 0., l2 = 0., r1 = 0., r2 = 0.;
+        if (kind != 0) {
+            double hL = L.h, xL = L.hu, yL = L.hv, bL = L.b;
+            double hR = R.h, xR = R.hu, yR = R.hv, bR = R.b;
+            double rawR = R.raw;
+            if (kind == 2) {
+                hR = hL; xR = xL; yR = yL; bR = bL; rawR = L.raw;   // mirrored trace
+            }
+            // rotation to the face frame (prepare)
+            double xRr = xR, yRr = yR;
+            if (kind == 2) {
+                const double dot = xL * nx + yL * ny;
+                xRr = xL - 2.0 * dot * nx; yRr = yL - 2.0 * dot * ny;
+            }
+            const double unL = xL * nx + yL * ny, utL = xL * (-ny) + yL * nx;
+            const double unR = xRr * nx + yRr * ny, utR = xRr * (-ny) + yRr * nx;
+            double loc[8] = {hL, unL, utL, bL, hR, unR, utR, bR};
+            if (kind == 1) {
+                const double top = fmax(bL, bR);
+                const double tol = 16. * EPS * fmax(dry, fmax(fabs(top), fmax(fabs(hL + bL), fabs(hR + bR))));
+                double hl = fmax(0., hL + bL - top), hr = fmax(0., hR + bR - top);
+                if (hl <= dry + tol) hl = 0.;
+                if (hr <= dry + tol) hr = 0.;
+                loc[0] = hl; loc[3] = top; loc[4] = hr; loc[7] = top;
+                loc[1] = hL > dry ? unL * (hl / hL) : 0.;
+                loc[2] = hL > dry ? utL * (hl / hL) : 0.;
+                loc[5] = hR > dry ? unR * (hr / hR) : 0.;
+                loc[6] = hR > dry ? utR * (hr / hR) : 0.;
+            }
+            bool closed = false;
+            if (kind == 1 && !(fmin(rc.h, rn.h) > dry)) {
+                const double dc = m.distance[f], dn = m.distance[nf + f];
+                double shared;
+                if (dc + dn > DBL_MIN_)
+                    shared = (dn * (rc.b + rc.h) + dc * (rn.b + rn.h)) / (dc + dn) - fmax(rc.b, rn.b);
+                else
+                    shared = 0.5 * ((rc.b + rc.h) + (rn.b + rn.h)) - fmax(rc.b, rn.b);
+                closed = shared <= dry;
+                if (closed) {
+                    bool opens = false;
+                    if (hL > dry && hR <= dry && unL / hL > 0.0) {
+                        const RType<double> t = riemann_type<double>(hL, hL, unL / hL, -unL / hL, dry, grav);
+                        opens = t.hm > hL + dry && t.hm + bL > bR + dry;
+                    } else if (hR > dry && hL <= dry && -unR / hR > 0.0) {
+                        const RType<double> t = riemann_type<double>(hR, hR, -unR / hR, unR / hR, dry, grav);
+                        opens = t.hm > hR + dry && t.hm + bR > bL + dry;
+                    }
+                    closed = !opens;
+                }
+            }
+            double l[3] = {0., 0., 0.}, r[3] = {0., 0., 0.};
+            FWaveOut<double> fwo;
+            const int fst = fwave<double>(loc, grav, dry, fwo);
+            if (fst) bad = 1;
+            if (closed) {
+                l[1] = 0.5 * grav * (hL * hL) * nx; l[2] = 0.5 * grav * (hL * hL) * ny;
+                r[1] = 0.5 * grav * (hR * hR) * nx; r[2] = 0.5 * grav * (hR * hR) * ny;
+                if (hL > dry) speed = fmax(speed, fabs(loc[1] / hL) + sqrt(grav * hL));
+                if (hR > dry) speed = fmax(speed, fabs(loc[5] / hR) + sqrt(grav * hR));
+            } else {
+                const double starL = loc[0], starR = loc[4];
+                double pl[3] = {0., 0., 0.}, pr[3] = {0., 0., 0.};
+                if (starL > dry) {
+                    const double hu = loc[1], hv = loc[2];
+                    pl[0] = hu; pl[1] = (hu * hu) / starL + 0.5 * grav * (starL * starL); pl[2] = hu * hv / starL;
+                }
+                if (starR > dry) {
+                    const double hu = loc[5], hv = loc[6];
+                    pr[0] = hu; pr[1] = (hu * hu) / starR + 0.5 * grav * (starR * starR); pr[2] = hu * hv / starR;
+                }
+#pragma unroll
+                for (int j = 0; j < 3; ++j) { pl[j] += fwo.amdq[j]; pr[j] -= fwo.apdq[j]; }
+                l[0] = pl[0]; l[1] = pl[1] * nx + pl[2] * (-ny); l[2] = pl[1] * ny + pl[2] * nx;
+                r[0] = pr[0]; r[1] = pr[1] * nx + pr[2] * (-ny); r[2] = pr[1] * ny + pr[2] * nx;
+                if (fabs(l[0] - r[0]) > 1.e-10 * fmax(1.0, fmax(fabs(l[0]), fabs(r[0])))) bad = 1;
+                l[0] = 0.5 * (l[0] + r[0]); r[0] = l[0];
+                speed = fmax(fabs(fwo.s[0]), fmax(fabs(fwo.s[1]), fabs(fwo.s[2])));
+                if (kind == 1) {
+                    const double cl = .5 * grav * (hL * hL - starL * starL), cr = .5 * grav * (hR * hR - starR * starR);
+                    l[1] += cl * nx; l[2] += cl * ny; r[1] += cr * nx; r[2] += cr * ny;
+                }
+                if (kind == 2) {
+                    l[0] = 0.0;
+                    const double pressure = wall_pressure<double>(hL, loc[1], grav, dry);
+                    l[1] = pressure * nx; l[2] = pressure * ny;
+                    r[0] = l[0]; r[1] = l[1]; r[2] = l[2];
+                }
+            }
+            if (rc.h > dry) {
+                const double corr = (rc.flags & 1) ? 0.5 * grav * (rc.h * rc.h - hL * hL)
+                                                   : 0.5 * grav * (rc.h + L.raw) * (bL - rc.b);
+                l[1] += corr * nx; l[2] += corr * ny;
+            }
+            if (n >= 0) {
+                if (rn.h > dry) {
+                    const double corr = (rn.flags & 1) ? 0.5 * grav * (rn.h * rn.h - hR * hR)
+                                                       : 0.5 * grav * (rn.h + rawR) * (bR - rn.b);
+                    r[1] += corr * nx; r[2] += corr * ny;
+                }
+            } else { r[0] = l[0]; r[1] = l[1]; r[2] = l[2]; }
+            if (!isfinite(l[0]) || !isfinite(l[1]) || !isfinite(l[2]) || !isfinite(r[0]) || !isfinite(r[1]) ||
+                !isfinite(r[2])) bad = 1;
+            water = l[0]; l1 = l[1]; l2 = l[2]; r1 = r[1]; r2 = r[2];
+        }
+        if (bad) raise_status(ct, stage, ST_SPATIAL);
+        w.ws[f] = make_double2(water, speed);
+        const double pn = n >= 0 ? .5 * grav * rn.h * rn.h : 0.;
+        w.gf[f] = make_double4_32a(l1 - pc * nx, l2 - pc * ny, r1 - pn * nx, r2 - pn * ny);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Gather: rate, donor inventory / boundary reservation, CFL frequency.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_gather(MeshDev m, StateDev s, Ctrl *ctrl, Work w, int stage)
+{
+    const int nc = m.nc;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        Ctrl &ct = ctrl[m.cell_sid[c]];
+        if (skip_stage(ct, stage)) continue;
+        const double *base = stage == 1 ? s.work : s.q1;
+        const double dt = ct.trial, area = m.area[c];
+        const bool active = w.rec[c].flags & 2;
+        double sum0 = 0., sum1 = 0., sum2 = 0., out = 0., freq = 0., ext = 0., interior = 0.;
+        const bool owns_open = m.cflags[c] & 1;
+        for (int k = m.offset[c]; k < m.offset[c + 1]; ++k) {
+            const int f = m.faces[k];
+            const double len = m.length[f];
+            const double wt = len / area;
+            const double2 ws = w.ws[f];
+            const double4_32a gf = w.gf[f];
+            if (m.signs[k] > 0) { sum0 += wt * ws.x; sum1 += wt * gf.x; sum2 += wt * gf.y; }
+            else { sum0 -= wt * ws.x; sum1 -= wt * gf.z; sum2 -= wt * gf.w; }
+            const double debit = fmax(m.signs[k] * ws.x, 0.) * len;
+            out += debit;
+            if (owns_open) { if (m.bslot[f] >= 0) ext += debit; else interior += debit; }
+            freq += len * ws.y;
+        }
+        double r0 = 0., r1 = 0., r2 = 0.;
+        if (active) { r0 = -sum0; r1 = -sum1; r2 = -sum2; }
+        w.rate[c] = r0; w.rate[nc + c] = r1; w.rate[2 * nc + c] = r2;
+        double theta = 1.;
+        if (out > 0. && dt * out >= base[c] * area)
+            theta = fmin(1., base[c] * area / (dt * out)) * (1. - 32. * 2.2204460492503131e-16);
+        if (owns_open) {
+            const double available = base[c] * area / dt;
+            if (ext > available) raise_status(ct, stage, ST_BUDGET);
+            const double factor = fmin(1., (available - ext) / fmax(interior, 1e-300)) * (1. - 32. * EPS);
+            theta = (interior > 0. && interior >= available - ext) ? factor : 1.;
+        }
+        w.theta[c] = theta;
+        const double fr = freq / area;
+        if (isnan(fr)) raise_status(ct, stage, ST_FREQ);
+        else atomic_max_nonneg(stage == 1 ? &ct.peak1 : &ct.peak2, fr);
+    }
+}
+
+// midpoint_faces: limit donor outflow, carry the removed advective momentum.
+__global__ void __launch_bounds__(256) k_limit(MeshDev m, StateDev s, Ctrl *ctrl, Work w, int stage)
+{
+    const int nf = m.nf, nc = m.nc;
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += gridDim.x * blockDim.x) {
+        const Ctrl &ct = ctrl[m.face_sid[f]];
+        if (skip_stage(ct, stage)) continue;
+        const double *q = stage == 1 ? s.work : s.q1;
+        double water = w.ws[f].x, cx = 0., cy = 0.;
+        if (water != 0. && m.bslot[f] < 0) {
+            const int donor = water < 0. ? m.neighbour[f] : m.owner[f];
+            if (donor >= 0) {
+                const double th = w.theta[donor];
+                if (th != 1.) {
+                    const double delta = (th - 1.) * water;
+                    water *= th;
+                    const double hd = q[donor];
+                    if (hd > ct.dry) { cx = delta * q[nc + donor] / hd; cy = delta * q[2 * nc + donor] / hd; }
+                }
+            }
+        }
+        w.lim[f] = make_double4_32a(water, cx, cy, 0.);
+    }
+}
+
+// midpoint_gather + stage combination (+ closing drag on the second stage).
+// With rate_out set, the final rate is stored there and no state is written.
+__global__ void __launch_bounds__(256) k_update(MeshDev m, StateDev s, Ctrl *ctrl, Work w, int stage,
+                                                double *rate_out)
+{
+    const int nc = m.nc;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        Ctrl &ct = ctrl[m.cell_sid[c]];
+        if (skip_stage(ct, stage)) continue;
+        const double area = m.area[c];
+        double mass = 0., mx = 0., my = 0.;
+        for (int k = m.offset[c]; k < m.offset[c + 1]; ++k) {
+            const int f = m.faces[k];
+            const double wt = m.signs[k] * m.length[f] / area;
+            const double4_32a L = w.lim[f];
+            mass -= wt * L.x; mx -= wt * L.y; my -= wt * L.z;
+        }
+        const double r0 = mass, r1 = w.rate[nc + c] + mx, r2 = w.rate[2 * nc + c] + my;
+        if (!isfinite(r0) || !isfinite(r1) || !isfinite(r2)) raise_status(ct, stage, ST_RATE);
+        if (rate_out) { rate_out[c] = r0; rate_out[nc + c] = r1; rate_out[2 * nc + c] = r2; continue; }
+        const double dt = ct.trial, dry = ct.dry;
+        if (stage == 1) {
+            const double h = s.work[c] + dt * r0;
+            double hu = s.work[nc + c] + dt * r1, hv = s.work[2 * nc + c] + dt * r2;
+            if (h < 0) raise_status(ct, 1, ST_ENDPOINT);
+            if (h <= dry) { hu = 0.; hv = 0.; }
+            s.q1[c] = h; s.q1[nc + c] = hu; s.q1[2 * nc + c] = hv;
+        } else {
+            double h = .5 * s.work[c] + .5 * (s.q1[c] + dt * r0);
+            double hu = .5 * s.work[nc + c] + .5 * (s.q1[nc + c] + dt * r1);
+            double hv = .5 * s.work[2 * nc + c] + .5 * (s.q1[2 * nc + c] + dt * r2);
+            if (!isfinite(h) || !isfinite(hu) || !isfinite(hv) || h < 0) raise_status(ct, 2, ST_ENDPOINT);
+            if (h <= dry) { hu = 0.; hv = 0.; }
+            drag_cell(ct, .5 * dt, h, hu, hv);
+            double *qn = s.q[ct.cur ^ 1];
+            qn[c] = h; qn[nc + c] = hu; qn[2 * nc + c] = hv;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Control: accept/reject the trial and set the next one (RiverExplicit.advance).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void set_trial(Ctrl &c)
+{
+    c.trial = fmin(c.hint, c.dt_outer - c.elapsed);
+    c.truncated = c.trial < c.hint * (1 - 1e-12);
+    c.status1 = 0; c.status2 = 0; c.peak1 = 0ull; c.peak2 = 0ull;
+}
+
+__global__ void k_control(Ctrl *ctrl, int nscen)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nscen) return;
+    Ctrl &c = ctrl[i];
+    if (!c.active || c.done) return;
+    const double f1 = bits_to_double(c.peak1), f2 = bits_to_double(c.peak2);
+    // the reference's frequency peak only sees stages that reached the CFL evaluation
+    double peak = 0.;
+    bool reject = false;
+    if (c.status1 & ST_PRE) reject = true;
+    else {
+        peak = f1;
+        if (c.trial * f1 > c.cfl * (1 + 1e-12) || (c.status1 & ST_ENDPOINT)) reject = true;
+        else if (c.status2 & ST_PRE) reject = true;
+        else {
+            peak = fmax(peak, f2);
+            if (c.trial * f2 > c.cfl * (1 + 1e-12) || (c.status2 & ST_ENDPOINT)) reject = true;
+        }
+    }
+    if (reject) {
+        c.rejections++;
+        c.hint = peak > 0 ? fmin(.5 * c.trial, .98 * c.cfl / peak) : .5 * c.trial;
+        if (c.hint < c.floor_ || c.rejections > 100) { c.failed = 1; c.done = 1; return; }
+    } else {
+        c.cur ^= 1;
+        c.elapsed += c.trial;
+        c.substeps++;
+        if (c.substeps == 1 || c.trial < c.min_dt) c.min_dt = c.trial;
+        if (c.trial > c.max_dt) c.max_dt = c.trial;
+        if (c.trial * peak > c.cfl_max) c.cfl_max = c.trial * peak;
+        const double growth = c.truncated ? c.hint : 2 * c.trial;
+        c.hint = peak > 0 ? fmin(growth, .98 * c.cfl / peak) : growth;
+        if (c.substeps > c.max_substeps) { c.failed = 2; c.done = 1; return; }
+        if (!(c.elapsed < c.dt_outer - 1e-13 * fmax(1., c.dt_outer))) { c.done = 1; return; }
+    }
+    set_trial(c);
+}
+
+// Limited water flux of the last stage into a caller buffer.
+__global__ void k_water_out(MeshDev m, Work w, double *water)
+{
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < m.nf; f += gridDim.x * blockDim.x) water[f] = w.lim[f].x;
+}
+
+// Make the caller-bound buffer q[0] hold every scenario's accepted state.
+__global__ void k_commit(MeshDev m, StateDev s, Ctrl *ctrl)
+{
+    const int nc = m.nc;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        if (!ctrl[m.cell_sid[c]].cur) continue;
+        s.q[0][c] = s.q[1][c];
+        s.q[0][nc + c] = s.q[1][nc + c];
+        s.q[0][2 * nc + c] = s.q[1][2 * nc + c];
+    }
+}
+
+}  // namespace brx

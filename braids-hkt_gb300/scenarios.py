@@ -148,3 +148,33 @@ def perturbed_state(case, seed, amplitude=0.3, velocity=0.6, dry_fraction=0.0):
     u = velocity * rng.uniform(-1, 1, h.shape)
     v = velocity * rng.uniform(-1, 1, h.shape)
     return np.ascontiguousarray(np.stack((h, h * u, h * v)))
+
+
+# ---------------------------------------------------------------------------
+# (De)serialisation: a case as flat arrays, so fixtures do not depend on the
+# Delaunay implementation of the machine that reads them.
+# ---------------------------------------------------------------------------
+_MESH_FIELDS = ("points", "tri", "owner", "neighbour", "bid", "normal", "length", "mid", "area", "xy",
+                "offset", "faces", "signs", "boundary_offset", "boundary_faces")
+
+
+def case_arrays(case):
+    m = case["mesh"]
+    out = {f"mesh_{k}": getattr(m, k) for k in _MESH_FIELDS}
+    out.update({f"rec_{k}": v for k, v in m.records.items()})
+    for k in ("z", "q", "seg_mode", "stage_policy", "forcing", "exterior_bed"):
+        out[k] = np.asarray(case[k])
+    for k, v in case["controls"].items():
+        out[f"ctl_{k}"] = np.asarray(v)
+    return out
+
+
+def case_from_arrays(arrs):
+    mesh = M.Mesh(**{k: np.asarray(arrs[f"mesh_{k}"]) for k in _MESH_FIELDS})
+    mesh.records = {k[4:]: np.asarray(v) for k, v in arrs.items() if k.startswith("rec_")}
+    ctl = {k[4:]: arrs[k].item() for k in arrs if k.startswith("ctl_")}
+    ctl["roughness_mode"] = int(ctl["roughness_mode"])
+    case = dict(mesh=mesh, controls=ctl, name="fixture")
+    for k in ("z", "q", "seg_mode", "stage_policy", "forcing", "exterior_bed"):
+        case[k] = np.asarray(arrs[k])
+    return case

@@ -1,0 +1,276 @@
+"""Host-side owner of resident river scenarios on one GB300.
+
+``RiverSolver`` mirrors the reference's solver owner and explicit controller:
+
+  reference                                               here
+  ShorelineSolver(deck, data, backend='gpu', ...)          RiverSolver(case(s), precision=...)
+    src/braids_core/sediment/shoreline_solver.py:244
+  ShorelineSolver.step(dt) -> dict(q, z, ..., diagnostics) RiverSolver.step(dt)
+    shoreline_solver.py:345-372
+  RiverExplicit.advance(base, dt, time)                   RiverSolver.advance(dt, time)
+    -> (q, water/dt, diagnostics)                           -> diagnostics (state updated in place)
+    src/braids_core/sediment/river_explicit.py:121-154
+  RiverExplicit._single(base, dt, time)                   RiverSolver.substep(dt, time)
+    river_explicit.py:94-119
+  RiverExplicit.rate(q, dt, time) -> (rate, water)        RiverSolver.rate(dt, time)
+    river_explicit.py:63-92
+
+Device memory for the resident state is owned by PyTorch tensors (``q`` and
+``z``); all arithmetic runs in the CUDA library through its C ABI. Several
+scenarios passed together are packed into one index space and advanced by the
+same launches, each on its own clock.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import numpy as np
+
+from . import _lib
+from ._lib import AdvanceStats, check
+
+PRECISIONS = {"fp64": 0, "mixed": 1}
+METHOD = "explicit_fwave_ssprk22_river_v1"
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _ptr(a):
+    return C.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def pack(cases):
+    """Concatenate scenario meshes into one global index space."""
+    out = {k: [] for k in ("owner", "neighbour", "bid", "offset", "faces", "signs", "normal", "length", "area",
+                           "ls_matrix", "ls_weight", "ls_delta", "disp", "distance", "boundary_offset",
+                           "boundary_faces", "seg_mode", "stage_policy", "exterior_bed", "forcing", "q", "z")}
+    cell_off, face_off, seg_off = [0], [0], [0]
+    nadj_total = 0
+    nslot_total = 0
+    for case in cases:
+        m = case["mesh"]
+        r = m.records
+        C0, F0, S0 = cell_off[-1], face_off[-1], seg_off[-1]
+        out["owner"].append(m.owner + C0)
+        out["neighbour"].append(np.where(m.neighbour >= 0, m.neighbour + C0, -1))
+        out["bid"].append(np.where(m.bid >= 0, m.bid + S0, -1))
+        out["offset"].append(m.offset[:-1] + nadj_total)
+        out["faces"].append(m.faces + F0)
+        out["signs"].append(m.signs)
+        out["normal"].append(m.normal)
+        out["length"].append(m.length)
+        out["area"].append(m.area)
+        out["ls_matrix"].append(r["ls_matrix"])
+        out["ls_weight"].append(r["ls_weight"])
+        out["ls_delta"].append(r["ls_delta"])
+        out["disp"].append(r["disp"])
+        out["distance"].append(r["distance"])
+        nb = m.nb
+        out["boundary_offset"].append(m.boundary_offset[:-1] + nslot_total)
+        out["boundary_faces"].append(m.boundary_faces + F0)
+        if nb:
+            out["seg_mode"].append(np.asarray(case["seg_mode"], np.int32))
+            out["stage_policy"].append(np.asarray(case.get("stage_policy", np.zeros(nb)), np.int32))
+            out["forcing"].append(np.asarray(case["forcing"], np.float64)[:, :nb])
+        out["exterior_bed"].append(np.asarray(case.get("exterior_bed", np.zeros(m.nf)), np.float64))
+        out["q"].append(np.asarray(case["q"], np.float64))
+        out["z"].append(np.asarray(case["z"], np.float64))
+        nadj_total += m.nadj
+        nslot_total += len(m.boundary_faces)
+        cell_off.append(C0 + m.nc)
+        face_off.append(F0 + m.nf)
+        seg_off.append(S0 + nb)
+    p = {}
+    for k in ("owner", "neighbour", "bid", "faces", "signs", "boundary_faces", "seg_mode", "stage_policy"):
+        p[k] = _i32(np.concatenate(out[k]) if out[k] else np.zeros(0))
+    p["offset"] = _i32(np.concatenate(out["offset"] + [np.array([nadj_total])]))
+    p["boundary_offset"] = _i32(np.concatenate(out["boundary_offset"] + [np.array([nslot_total])]))
+    for k in ("length", "area", "ls_weight", "exterior_bed", "z"):
+        p[k] = _f64(np.concatenate(out[k]))
+    for k in ("normal", "ls_matrix", "ls_delta", "distance", "q"):
+        p[k] = _f64(np.concatenate(out[k], axis=-1))
+    p["disp"] = _f64(np.concatenate(out["disp"], axis=-1))
+    p["forcing"] = _f64(np.concatenate(out["forcing"], axis=1)) if out["forcing"] else np.zeros((2, 0))
+    p["cell_offset"] = _i32(cell_off)
+    p["face_offset"] = _i32(face_off)
+    p["seg_offset"] = _i32(seg_off)
+    p["nc"], p["nf"], p["nadj"], p["nseg"] = cell_off[-1], face_off[-1], nadj_total, seg_off[-1]
+    return p
+
+
+class RiverSolver:
+    """Resident GB300 river scenarios advanced by the CUDA step (see module docstring)."""
+
+    def __init__(self, cases, precision="fp64", graph_chunk=8):
+        import torch
+        if not torch.cuda.is_available():
+            raise RuntimeError("RiverSolver needs a CUDA device; the step has no CPU implementation")
+        self.torch = torch
+        self.single = isinstance(cases, dict)
+        self.cases = [cases] if self.single else list(cases)
+        self.precision = precision
+        self.lib = _lib.load()
+        p = self.packed = pack(self.cases)
+        self.nscen = len(self.cases)
+        self.nc, self.nf = p["nc"], p["nf"]
+        handle = C.c_void_p()
+        check(self.lib.brx_solver_create(
+            self.nscen, _ptr(p["cell_offset"]), _ptr(p["face_offset"]), p["nc"], p["nf"], p["nadj"],
+            _ptr(p["owner"]), _ptr(p["neighbour"]), _ptr(p["bid"]), _ptr(p["offset"]), _ptr(p["faces"]),
+            _ptr(p["signs"]), _ptr(p["normal"]), _ptr(p["length"]), _ptr(p["area"]), _ptr(p["ls_matrix"]),
+            _ptr(p["ls_weight"]), _ptr(p["ls_delta"]), _ptr(p["disp"]), _ptr(p["distance"]), p["nseg"],
+            _ptr(p["seg_offset"]), _ptr(p["boundary_offset"]), _ptr(p["boundary_faces"]),
+            PRECISIONS[precision], C.byref(handle)))
+        self.h = handle
+        for i, case in enumerate(self.cases):
+            c = case["controls"]
+            check(self.lib.brx_controls_set(self.h, i, c["grav"], c["dry"], c["cfl"], c["speed_limit"],
+                                            int(c["roughness_mode"]), c["roughness_value"]))
+        if p["nseg"]:
+            check(self.lib.brx_boundary_set(self.h, _ptr(p["seg_mode"]), _ptr(p["stage_policy"]),
+                                            _ptr(p["exterior_bed"]), _ptr(p["forcing"])))
+        else:
+            check(self.lib.brx_boundary_set(self.h, None, None, None, None))
+        dev = torch.device("cuda", torch.cuda.current_device())
+        self.q = torch.from_numpy(p["q"]).to(dev).contiguous()
+        self.z = torch.from_numpy(p["z"]).to(dev).contiguous()
+        check(self.lib.brx_state_bind(self.h, C.c_void_p(self.q.data_ptr()), C.c_void_p(self.z.data_ptr())))
+        check(self.lib.brx_graph_chunk_set(self.h, int(graph_chunk)))
+        self.time = np.zeros(self.nscen)
+        self.steps = 0
+
+    # ------------------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.brx_solver_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self):
+        return self.torch.cuda.ExternalStream(self.lib.brx_stream(self.h))
+
+    def launches(self):
+        return int(self.lib.brx_launch_count(self.h))
+
+    def set_forcing_table(self, time, value):
+        """value (2, nseg, len): discharge and stage tables for every segment."""
+        t = _f64(time)
+        v = _f64(value)
+        check(self.lib.brx_forcing_table_set(self.h, len(t), _ptr(t), _ptr(v)))
+
+    def activate(self, mask):
+        m = _i32(mask)
+        check(self.lib.brx_scenarios_activate(self.h, _ptr(m)))
+
+    def hints(self):
+        out = np.zeros(self.nscen)
+        check(self.lib.brx_hint_get(self.h, _ptr(out)))
+        return out
+
+    def set_hints(self, hints):
+        h = _f64(hints)
+        check(self.lib.brx_hint_set(self.h, _ptr(h)))
+
+    # ------------------------------------------------------------------
+    def advance(self, dt, time=None, raise_on_failure=True):
+        """Advance all active scenarios over [time, time+dt]; per-scenario diagnostics."""
+        self.torch.cuda.current_stream().synchronize()
+        t = float(self.time[0] if time is None else time)
+        stats = (AdvanceStats * self.nscen)()
+        code = self.lib.brx_advance(self.h, float(dt), t, stats)
+        if code and (raise_on_failure or code != 4):
+            check(code)
+        out = []
+        for s in stats:
+            out.append(dict(integrator=METHOD, hydraulic_substeps=s.substeps, hydraulic_rejections=s.rejections,
+                            hydraulic_minimum_dt=s.min_dt, hydraulic_maximum_dt=s.max_dt,
+                            accepted_cfl_max=s.accepted_cfl_max, hydraulic_next_substep_hint_s=s.hint,
+                            failed=s.failed))
+        return out[0] if self.single else out
+
+    def step(self, dt):
+        """Advance by dt from the owner clock (ShorelineSolver.step)."""
+        diag = self.advance(dt, self.time[0])
+        self.time += dt
+        self.steps += 1
+        return dict(q=self.q, z=self.z, diagnostics=diag)
+
+    def substep(self, dt, time=0.0):
+        """One SSPRK(2,2) trial of exactly dt: (status bits, stage-peak CFL frequency) per scenario."""
+        self.torch.cuda.current_stream().synchronize()
+        status = np.zeros(self.nscen, np.uint32)
+        peak = np.zeros(self.nscen)
+        check(self.lib.brx_substep(self.h, float(dt), float(time), _ptr(status), _ptr(peak)))
+        return (status[0], peak[0]) if self.single else (status, peak)
+
+    def rate(self, dt, time=0.0):
+        """One spatial residual of the current state: (rate (3,nc), water (nf), status, frequency)."""
+        torch = self.torch
+        torch.cuda.current_stream().synchronize()
+        rate = torch.zeros((3, self.nc), dtype=torch.float64, device=self.q.device)
+        water = torch.zeros(self.nf, dtype=torch.float64, device=self.q.device)
+        status = np.zeros(self.nscen, np.uint32)
+        freq = np.zeros(self.nscen)
+        check(self.lib.brx_rate(self.h, float(dt), float(time), C.c_void_p(rate.data_ptr()),
+                                C.c_void_p(water.data_ptr()), _ptr(status), _ptr(freq)))
+        if self.single:
+            return rate, water, status[0], freq[0]
+        return rate, water, status, freq
+
+    # ------------------------------------------------------------------
+    def set_state(self, q):
+        self.q.copy_(self.torch.from_numpy(_f64(q)))
+
+    def state(self, scenario=None):
+        q = self.q.cpu().numpy()
+        if scenario is None:
+            return q
+        a, b = self.packed["cell_offset"][scenario], self.packed["cell_offset"][scenario + 1]
+        return q[:, a:b]
+
+    def mass(self):
+        """Water volume per scenario (Kahan-compensated FP64 sum on the host)."""
+        q = self.q[0].cpu().numpy()
+        area = self.packed["area"]
+        out = []
+        for i in range(self.nscen):
+            a, b = self.packed["cell_offset"][i], self.packed["cell_offset"][i + 1]
+            out.append(kahan_sum(q[a:b] * area[a:b]))
+        return out[0] if self.single else np.array(out)
+
+
+def kahan_sum(values):
+    s = 0.0
+    c = 0.0
+    for v in np.asarray(values, dtype=np.float64).tolist():
+        y = v - c
+        t = s + y
+        c = (t - s) - y
+        s = t
+    return s
+
+
+def _profile(self, dt, time=0.0):
+    """Per-kernel durations (ms) of one trial launched without a graph: [(kernel name, ms), ...]."""
+    names = ["drag", "boundary", "cells", "faces", "gather", "limit", "update", "control"]
+    self.torch.cuda.current_stream().synchronize()
+    cap = 64
+    ms = np.zeros(cap)
+    kind = np.zeros(cap, np.int32)
+    count = C.c_int()
+    check(self.lib.brx_profile_substep(self.h, float(dt), float(time), cap, _ptr(ms), _ptr(kind), C.byref(count)))
+    return [(names[kind[i]], float(ms[i])) for i in range(count.value)]
+
+
+RiverSolver.profile_substep = _profile

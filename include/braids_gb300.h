@@ -1,0 +1,152 @@
+/*
+ * braids_gb300.h - C ABI of the GB300 river solver step (BRAIDS-HKT
+ * augmented f-wave path).
+ *
+ * Plain C types only: host pointers for set-up arrays, device pointers for
+ * the resident state, sizes as int. Every call returns BRX_OK (0) or a
+ * positive error code; brx_last_error() describes the last failure of the
+ * calling thread. No call traps or aborts.
+ *
+ * Layouts follow the reference's component-major (C-contiguous SoA) records:
+ * q is (3,nc) rows h, hu, hv; normal (2,nf); displacement (2,2,nf)
+ * [component][side][face]; distance (2,nf); ls_matrix (4,nc); ls_delta
+ * (2,nadj). Indices are zero-based int32 with -1 for "none".
+ *
+ * Batching: nscen scenarios are packed into one index space. cell_offset and
+ * face_offset (nscen+1) give each scenario's cell and face range; all
+ * indices (owner, neighbour, faces, boundary_faces) are global. bid[f] of an
+ * open face is its global segment number; seg_offset (nscen+1) gives each
+ * scenario's segment range. One scenario is the plain form.
+ */
+#ifndef BRAIDS_GB300_H
+#define BRAIDS_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BRX_OK 0
+#define BRX_ERR_ARGUMENT 1      /* invalid size, index or pointer */
+#define BRX_ERR_CUDA 2          /* CUDA runtime failure */
+#define BRX_ERR_STATE 3         /* call out of order (e.g. no state bound) */
+#define BRX_ERR_REJECTED 4      /* trial rejected / interval could not be completed */
+#define BRX_ERR_UNSUPPORTED 5   /* mesh or mode outside the supported scope */
+
+/* Arithmetic forms. */
+#define BRX_FP64 0    /* FP64 everywhere, reference operation order, no FMA */
+#define BRX_MIXED 1   /* FP32 fluxes and updates; FP64 stage, bed source, mass */
+
+/* Rejection causes reported per scenario (bit set). */
+#define BRX_ST_SPATIAL 1u
+#define BRX_ST_BUDGET 2u
+#define BRX_ST_RATE 4u
+#define BRX_ST_ENDPOINT 8u
+#define BRX_ST_FREQ 16u
+#define BRX_ST_CFL 32u      /* dt * max frequency above the CFL target */
+
+typedef struct brx_solver brx_solver;
+
+/* Per-scenario outcome of one brx_advance call
+ * (mirrors the diagnostics of RiverExplicit.advance,
+ *  src/braids_core/sediment/river_explicit.py:150-154). */
+typedef struct {
+    int substeps;        /* accepted SSPRK(2,2) substeps */
+    int rejections;      /* rejected trials */
+    int failed;          /* 0 ok, 1 dt floor / rejection limit, 2 substep limit */
+    int pad;
+    double min_dt, max_dt, accepted_cfl_max, hint;
+} brx_advance_stats;
+
+const char *brx_last_error(void);
+int brx_version(void);
+
+/* Create a solver resident on the current CUDA device. Replaces the records
+ * dict of the reference's physics owner (river_mesh_records.initialize,
+ * src/braids_core/sediment/adaptive_river_worker.py:228) and the geometry
+ * upload of ResidentReconstruction / ResidentFlux
+ * (src/braids_support/gpu_fwave/reconstruction.py:91-118). All arrays are
+ * host memory and are copied. */
+int brx_solver_create(int nscen, const int *cell_offset, const int *face_offset,
+                      int nc, int nf, int nadj,
+                      const int *owner, const int *neighbour, const int *bid,
+                      const int *offset, const int *faces, const int *signs,
+                      const double *normal, const double *length, const double *area,
+                      const double *ls_matrix, const double *ls_weight, const double *ls_delta,
+                      const double *displacement, const double *distance,
+                      int nseg, const int *seg_offset, const int *boundary_offset,
+                      const int *boundary_faces, int precision, brx_solver **out);
+
+int brx_solver_destroy(brx_solver *s);
+
+/* Physical and numerical controls of one scenario (scen = -1: all).
+ * Replaces the reference's Parameters / CurrentRiverControls
+ * (src/braids_core/sediment/bend_methods_v1.py:64-83, current_river_solver.py:17-32)
+ * and river_roughness.selected (river_roughness.py:23-38): roughness_mode 1
+ * Chezy, 2 Manning, 3 White-Colebrook log layer, 4 classical. */
+int brx_controls_set(brx_solver *s, int scen, double gravity, double dry, double cfl,
+                     double speed_limit, int roughness_mode, double roughness_value);
+
+/* Open-boundary set-up for all segments: hydraulic mode (2 stage, 3 free
+ * outflow, 6 total discharge, 9 discharge + water line), stage reversal
+ * policy, exterior bed per face (nf, read on open faces) and forcing (2,nseg)
+ * rows discharge, stage. Replaces ExteriorBed construction
+ * (src/braids_core/sediment/river_exterior_bed.py:47-93). */
+int brx_boundary_set(brx_solver *s, const int *seg_mode, const int *stage_policy,
+                     const double *exterior_bed, const double *forcing);
+
+/* Piecewise-linear forcing tables: time (len), value (2,nseg,len). len = 0
+ * returns to constant forcing. Replaces HydraulicForcing.sample
+ * (src/braids_core/river_hydraulic_schedule.py). */
+int brx_forcing_table_set(brx_solver *s, int len, const double *time, const double *value);
+
+/* Bind caller-owned DEVICE buffers: q (3,nc) accepted state, updated in place;
+ * z (nc) bed. The reference keeps q and z in its owner
+ * (ShorelineSolver.q / .z, src/braids_core/sediment/shoreline_solver.py:275). */
+int brx_state_bind(brx_solver *s, double *q_device, double *z_device);
+
+/* Advance every active scenario over [time, time+dt] with the adaptive
+ * SSPRK(2,2) controller. Replaces RiverExplicit.advance
+ * (src/braids_core/sediment/river_explicit.py:121-154). stats: nscen entries
+ * (host), may be NULL. Returns BRX_ERR_REJECTED if any scenario failed. */
+int brx_advance(brx_solver *s, double dt, double time, brx_advance_stats *stats);
+
+/* One SSPRK(2,2) trial of exactly dt on every active scenario
+ * (RiverExplicit._single, river_explicit.py:94-119). On acceptance the bound
+ * state is replaced; status (nscen, host) gets the rejection bits (0 =
+ * accepted) and peak (nscen, host) the larger stage CFL frequency. */
+int brx_substep(brx_solver *s, double dt, double time, unsigned *status, double *peak);
+
+/* One spatial residual of the bound state (RiverExplicit.rate with
+ * interval base = state, river_explicit.py:63-92): rate (3,nc) and limited
+ * water flux (nf) into caller DEVICE buffers; status/freq per scenario (host). */
+int brx_rate(brx_solver *s, double dt, double time, double *rate_device, double *water_device,
+             unsigned *status, double *freq);
+
+/* Scenario mask for brx_advance / brx_substep / brx_rate (nscen ints, host;
+ * nonzero = active). All scenarios are active after creation. */
+int brx_scenarios_activate(brx_solver *s, const int *active);
+
+/* Step hint carried between brx_advance calls (nscen, host; <= 0 = none). */
+int brx_hint_get(brx_solver *s, double *hint);
+int brx_hint_set(brx_solver *s, const double *hint);
+
+/* Number of substeps captured per CUDA graph replay inside brx_advance. */
+int brx_graph_chunk_set(brx_solver *s, int substeps);
+
+/* Time one SSPRK(2,2) trial of exactly dt kernel by kernel with CUDA events
+ * on the solver stream (no graph). ms (cap entries) gets each launch's
+ * duration and kind (cap entries) its kernel: 0 drag, 1 boundary, 2 cells,
+ * 3 faces, 4 gather, 5 limit, 6 update, 7 control. *count gets the number
+ * of launches. The bound state is advanced as by brx_substep. */
+int brx_profile_substep(brx_solver *s, double dt, double time, int cap, double *ms, int *kind, int *count);
+
+/* Kernel launches issued by this solver since creation (own kernels only). */
+long long brx_launch_count(const brx_solver *s);
+
+/* Stream the solver launches on (cudaStream_t as void*). */
+void *brx_stream(brx_solver *s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

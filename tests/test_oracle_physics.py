@@ -1,0 +1,75 @@
+"""Known-answer checks of the oracle (the reference's runtime invariants and
+analytic solutions), the same cases later run through the CUDA path.
+
+  lake at rest with emerged islands        reconstruction_oracle.py:30-31 ("cutcell_lake")
+  water budget per step                    shoreline_solver.py:29-39, 354-360
+  dry-bed dam break (Ritter)               reconstruction_oracle.py:30-31 ("dry_dam_break")
+"""
+import numpy as np
+
+import braids_hkt_gb300.scenarios as S
+from oracle import Oracle
+
+
+def test_lake_at_rest_round_off():
+    case = S.lake_at_rest()
+    o = Oracle(case, threads=2)
+    q = case["q"].copy()
+    st, _, stats = o.advance(q, 5.0, 0.0)
+    assert st == 0 and stats["substeps"] > 20
+    assert np.abs(q[0] - case["q"][0]).max() < 1e-12
+    assert np.abs(q[1:]).max() < 1e-11
+
+
+def test_closed_basin_mass_conserved():
+    case = S.lake_at_rest()
+    q = S.perturbed_state(case, 9, 0.4, 0.6, 0.05)
+    o = Oracle(case, threads=2)
+    area = case["mesh"].area
+    v0 = float(np.sum(q[0] * area))
+    st, _, stats = o.advance(q, 3.0, 0.0)
+    assert st == 0
+    v1 = float(np.sum(q[0] * area))
+    assert abs(v1 - v0) <= max(1e-10, 64 * np.finfo(float).eps * v0)
+    assert q[0].min() >= 0
+
+
+def test_open_channel_budget():
+    """Volume change equals the integrated boundary water flux (stage outlet, Q inlet)."""
+    case = S.small_channel()
+    m = case["mesh"]
+    o = Oracle(case, threads=2)
+    q = case["q"].copy()
+    v0 = float(np.sum(q[0] * m.area))
+    dt = 2.0
+    st, water_mean, _ = o.advance(q, dt, 0.0)
+    assert st == 0
+    openf = (m.neighbour < 0) & (m.bid >= 0)
+    outflow = float(np.sum(water_mean[openf] * m.length[openf])) * dt
+    v1 = float(np.sum(q[0] * m.area))
+    assert abs((v1 - v0) + outflow) <= 1e-9 * max(1.0, v0)
+    inflow = -float(np.sum((water_mean * m.length)[openf & (m.bid == 0)])) * dt
+    assert 0.9 * 20.0 * dt < inflow < 1.1 * 20.0 * dt       # Q = 20 m3/s imposed
+
+
+def ritter_depth(x, t, h0, x0, g=9.81):
+    c0 = np.sqrt(g * h0)
+    xi = (x - x0) / t
+    h = np.where(xi <= -c0, h0, np.where(xi >= 2 * c0, 0.0, (2 * c0 - xi) ** 2 / (9 * g)))
+    return h
+
+
+def test_dry_dam_break_matches_ritter():
+    case = S.dam_break()
+    o = Oracle(case, threads=2)
+    q = case["q"].copy()
+    t = 4.0
+    st, _, _ = o.advance(q, t, 0.0)
+    assert st == 0
+    x = case["mesh"].xy[0]
+    exact = ritter_depth(x, t, 2.0, 100.0)
+    inner = (x > 60) & (x < 140)
+    err = np.abs(q[0] - exact)[inner]
+    assert err.mean() < 0.03          # first-order-limited scheme on a 2 m mesh
+    front = x[(q[0] > 1e-3)].max()
+    assert abs(front - (100.0 + 2 * np.sqrt(9.81 * 2.0) * t)) < 12.0
