@@ -18,7 +18,7 @@ D = C.c_double
 SIGNATURES = {
     "brx_last_error": (C.c_char_p, []),
     "brx_version": (I, []),
-    "brx_solver_create": (I, [I, P, P, I, I, I, P, P, P, P, P, P, P, P, P, P, P, P, P, P, I, P, P, P, I,
+    "brx_solver_create": (I, [I, P, P, I, I, I, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P, I, P, P, P, I,
                               C.POINTER(P)]),
     "brx_solver_destroy": (I, [P]),
     "brx_controls_set": (I, [P, I, D, D, D, D, I, D]),

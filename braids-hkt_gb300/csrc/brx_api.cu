@@ -161,8 +161,8 @@ extern "C" int brx_solver_create(int nscen, const int *cell_offset, const int *f
                                  const int *owner, const int *neighbour, const int *bid, const int *offset,
                                  const int *faces, const int *signs, const double *normal, const double *length,
                                  const double *area, const double *ls_matrix, const double *ls_weight,
-                                 const double *ls_delta, const double *displacement, const double *distance,
-                                 int nseg, const int *seg_offset, const int *boundary_offset,
+                                 const double *ls_delta, const double *displacement,
+                                 const double *displacement_length, const double *distance, int nseg, const int *seg_offset, const int *boundary_offset,
                                  const int *boundary_faces, int precision, brx_solver **out)
 {
     if (!out) return fail(BRX_ERR_ARGUMENT, "null output handle");
@@ -199,12 +199,13 @@ extern "C" int brx_solver_create(int nscen, const int *cell_offset, const int *f
             cflags[owner[boundary_faces[k]]] |= 1;
         }
         for (int c = 0; c < nc; ++c) s->maxdeg = std::max(s->maxdeg, offset[c + 1] - offset[c]);
-        // per-face-side displacement length and unit vector (glibc hypot, as the host oracle)
+        // per-face-side displacement length (given, or the C library's hypot) and unit vector
         std::vector<double> dlen(2 * (size_t)nf), dunit(4 * (size_t)nf);
         for (int side = 0; side < 2; ++side)
             for (int f = 0; f < nf; ++f) {
                 const double rx = displacement[side * (size_t)nf + f], ry = displacement[(2 + side) * (size_t)nf + f];
-                const double len = std::hypot(rx, ry);
+                const double len = displacement_length ? displacement_length[side * (size_t)nf + f]
+                                                       : std::hypot(rx, ry);
                 dlen[side * (size_t)nf + f] = len;
                 dunit[side * (size_t)nf + f] = len > 0 ? rx / len : 0.0;
                 dunit[(2 + side) * (size_t)nf + f] = len > 0 ? ry / len : 0.0;

@@ -47,7 +47,7 @@ def _ptr(a):
 def pack(cases):
     """Concatenate scenario meshes into one global index space."""
     out = {k: [] for k in ("owner", "neighbour", "bid", "offset", "faces", "signs", "normal", "length", "area",
-                           "ls_matrix", "ls_weight", "ls_delta", "disp", "distance", "boundary_offset",
+                           "ls_matrix", "ls_weight", "ls_delta", "disp", "disp_len", "distance", "boundary_offset",
                            "boundary_faces", "seg_mode", "stage_policy", "exterior_bed", "forcing", "q", "z")}
     cell_off, face_off, seg_off = [0], [0], [0]
     nadj_total = 0
@@ -69,6 +69,7 @@ def pack(cases):
         out["ls_weight"].append(r["ls_weight"])
         out["ls_delta"].append(r["ls_delta"])
         out["disp"].append(r["disp"])
+        out["disp_len"].append(r["disp_len"])
         out["distance"].append(r["distance"])
         nb = m.nb
         out["boundary_offset"].append(m.boundary_offset[:-1] + nslot_total)
@@ -92,7 +93,7 @@ def pack(cases):
     p["boundary_offset"] = _i32(np.concatenate(out["boundary_offset"] + [np.array([nslot_total])]))
     for k in ("length", "area", "ls_weight", "exterior_bed", "z"):
         p[k] = _f64(np.concatenate(out[k]))
-    for k in ("normal", "ls_matrix", "ls_delta", "distance", "q"):
+    for k in ("normal", "ls_matrix", "ls_delta", "disp_len", "distance", "q"):
         p[k] = _f64(np.concatenate(out[k], axis=-1))
     p["disp"] = _f64(np.concatenate(out["disp"], axis=-1))
     p["forcing"] = _f64(np.concatenate(out["forcing"], axis=1)) if out["forcing"] else np.zeros((2, 0))
@@ -123,7 +124,8 @@ class RiverSolver:
             self.nscen, _ptr(p["cell_offset"]), _ptr(p["face_offset"]), p["nc"], p["nf"], p["nadj"],
             _ptr(p["owner"]), _ptr(p["neighbour"]), _ptr(p["bid"]), _ptr(p["offset"]), _ptr(p["faces"]),
             _ptr(p["signs"]), _ptr(p["normal"]), _ptr(p["length"]), _ptr(p["area"]), _ptr(p["ls_matrix"]),
-            _ptr(p["ls_weight"]), _ptr(p["ls_delta"]), _ptr(p["disp"]), _ptr(p["distance"]), p["nseg"],
+            _ptr(p["ls_weight"]), _ptr(p["ls_delta"]), _ptr(p["disp"]), _ptr(p["disp_len"]), _ptr(p["distance"]),
+            p["nseg"],
             _ptr(p["seg_offset"]), _ptr(p["boundary_offset"]), _ptr(p["boundary_faces"]),
             PRECISIONS[precision], C.byref(handle)))
         self.h = handle

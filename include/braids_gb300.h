@@ -65,15 +65,18 @@ int brx_version(void);
  * src/braids_core/sediment/adaptive_river_worker.py:228) and the geometry
  * upload of ResidentReconstruction / ResidentFlux
  * (src/braids_support/gpu_fwave/reconstruction.py:91-118). All arrays are
- * host memory and are copied. */
+ * host memory and are copied. displacement_length (2,nf) is |displacement| per
+ * face side; pass NULL to have it computed here with the C library's hypot
+ * (pass the caller's own values when they must match another machine's
+ * geometry records bit for bit). */
 int brx_solver_create(int nscen, const int *cell_offset, const int *face_offset,
                       int nc, int nf, int nadj,
                       const int *owner, const int *neighbour, const int *bid,
                       const int *offset, const int *faces, const int *signs,
                       const double *normal, const double *length, const double *area,
                       const double *ls_matrix, const double *ls_weight, const double *ls_delta,
-                      const double *displacement, const double *distance,
-                      int nseg, const int *seg_offset, const int *boundary_offset,
+                      const double *displacement, const double *displacement_length,
+                      const double *distance, int nseg, const int *seg_offset, const int *boundary_offset,
                       const int *boundary_faces, int precision, brx_solver **out);
 
 int brx_solver_destroy(brx_solver *s);

@@ -47,10 +47,10 @@ def test_create_rejects_bad_topology_without_cuda():
     p = lambda a: C.c_void_p(a.ctypes.data)
     rc = lib.brx_solver_create(1, p(one), p(one), 1, 1, 1, p(bad_owner), p(np.array([-1], np.int32)),
                                p(np.array([-1], np.int32)), p(one), p(np.array([0], np.int32)),
-                               p(np.array([1], np.int32)), p(z), p(z), p(z), p(z), p(z), p(z), p(z), p(z),
+                               p(np.array([1], np.int32)), p(z), p(z), p(z), p(z), p(z), p(z), p(z), None, p(z),
                                0, None, None, None, 0, C.byref(h))
     assert rc == 1 and b"out of range" in lib.brx_last_error()
     rc = lib.brx_solver_create(1, p(one), p(one), 1, 1, 1, p(i), p(i), p(i), p(one), p(i), p(i),
-                               p(z), p(z), p(z), p(z), p(z), p(z), p(z), p(z), 0, None, None, None, 7, C.byref(h))
+                               p(z), p(z), p(z), p(z), p(z), p(z), p(z), None, p(z), 0, None, None, None, 7, C.byref(h))
     assert rc == 1 and b"precision" in lib.brx_last_error()
     assert not h.value
