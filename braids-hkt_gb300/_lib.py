@@ -33,6 +33,8 @@ SIGNATURES = {
     "brx_hint_set": (I, [P, P]),
     "brx_graph_chunk_set": (I, [P, I]),
     "brx_profile_substep": (I, [P, D, D, I, P, P, P]),
+    "brx_rate_noalloc": (I, [I, I, I, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P, D, D, D, D, P, P, P, P,
+                             P]),
     "brx_launch_count": (C.c_longlong, [P]),
     "brx_stream": (P, [P]),
 }

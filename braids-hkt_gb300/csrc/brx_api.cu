@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -656,5 +657,169 @@ extern "C" int brx_profile_substep(brx_solver *s, double dt, double time, int ca
     *count = n;
     for (auto e : ev) cudaEventDestroy(e);
     for (int i = 0; i < s->nscen; ++i) s->h_ctrl[i].cur = 0;
+    return BRX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free residual: brx_rate_noalloc
+//
+// For callers that may not allocate device memory once they are running:
+// hosts that own a fixed device-memory budget handed out at start-up (an
+// embedding simulation framework, a plugin inside another runtime's memory
+// pool), and real-time loops where a cudaMalloc would synchronise the device
+// and stall every other stream. They pass their own device buffers for the
+// mesh, the state and the outputs; the stage scratch (cell records, face
+// fluxes, donor factors, the control block and the derived per-face tables)
+// lives in the one static device array below, which every GPU that loads
+// this library holds until the process exits.
+// ---------------------------------------------------------------------------
+constexpr int NOALLOC_MAX_CELLS = 16384;
+constexpr int NOALLOC_MAX_FACES = 32768;
+
+constexpr size_t noalloc_align(size_t x) { return (x + 255) & ~size_t(255); }
+constexpr size_t NA_REC = 0;
+constexpr size_t NA_WS = NA_REC + noalloc_align(sizeof(CellRec) * NOALLOC_MAX_CELLS);
+constexpr size_t NA_GF = NA_WS + noalloc_align(sizeof(double2) * NOALLOC_MAX_FACES);
+constexpr size_t NA_LIM = NA_GF + noalloc_align(sizeof(double4_32a) * NOALLOC_MAX_FACES);
+constexpr size_t NA_RATE = NA_LIM + noalloc_align(sizeof(double4_32a) * NOALLOC_MAX_FACES);
+constexpr size_t NA_THETA = NA_RATE + noalloc_align(sizeof(double) * 3 * NOALLOC_MAX_CELLS);
+constexpr size_t NA_CSID = NA_THETA + noalloc_align(sizeof(double) * NOALLOC_MAX_CELLS);
+constexpr size_t NA_CFLAGS = NA_CSID + noalloc_align(sizeof(int) * NOALLOC_MAX_CELLS);
+constexpr size_t NA_FSID = NA_CFLAGS + noalloc_align(sizeof(int) * NOALLOC_MAX_CELLS);
+constexpr size_t NA_BSLOT = NA_FSID + noalloc_align(sizeof(int) * NOALLOC_MAX_FACES);
+constexpr size_t NA_BMODE = NA_BSLOT + noalloc_align(sizeof(int) * NOALLOC_MAX_FACES);
+constexpr size_t NA_DUNIT = NA_BMODE + noalloc_align(sizeof(int) * NOALLOC_MAX_FACES);
+constexpr size_t NA_CTRL = NA_DUNIT + noalloc_align(sizeof(double) * 4 * NOALLOC_MAX_FACES);
+constexpr size_t NOALLOC_BYTES = NA_CTRL + noalloc_align(sizeof(Ctrl));   // about 7.4 MB
+
+static __device__ __align__(256) unsigned char brx_noalloc_scratch[NOALLOC_BYTES];
+
+// Device address of the static scratch, looked up once per device.
+static std::mutex g_noalloc_mutex;
+static std::map<int, unsigned char *> g_noalloc_address;
+
+static int noalloc_address(unsigned char **out)
+{
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    auto it = g_noalloc_address.find(dev);
+    if (it != g_noalloc_address.end()) { *out = it->second; return BRX_OK; }
+    void *ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, brx_noalloc_scratch);
+    if (e != cudaSuccess || !ptr)
+        return fail(BRX_ERR_CUDA, std::string("cudaGetSymbolAddress(brx_noalloc_scratch): ") + cudaGetErrorString(e));
+    g_noalloc_address[dev] = (unsigned char *)ptr;
+    *out = (unsigned char *)ptr;
+    return BRX_OK;
+}
+
+__global__ void k_noalloc_ctrl(Ctrl *ctrl, Ctrl init) { *ctrl = init; }
+
+// Derived per-cell/per-face tables of a closed single-scenario mesh, and a
+// bounds check of the caller's topology: any index out of range or a cell
+// with more than MAX_CELL_FACES faces deactivates the call (no kernel of the
+// residual then touches the mesh) and raises the spatial status bit.
+__global__ void k_noalloc_tables(MeshDev m, Ctrl *ctrl, int *cell_sid, int *cflags, int *face_sid, int *bslot,
+                                 int *bmode, double *disp_unit)
+{
+    const int nc = m.nc, nf = m.nf, nadj = m.nadj;
+    const int n = nc > nf ? nc : nf;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        bool bad = false;
+        if (i < nc) {
+            cell_sid[i] = 0;
+            cflags[i] = 0;
+            const int k0 = m.offset[i], k1 = m.offset[i + 1];
+            if (k0 < 0 || k1 < k0 || k1 > nadj || k1 - k0 > MAX_CELL_FACES) bad = true;
+            else
+                for (int k = k0; k < k1; ++k) {
+                    const int f = m.faces[k];
+                    if (f < 0 || f >= nf || (m.signs[k] != 1 && m.signs[k] != -1)) { bad = true; break; }
+                }
+        }
+        if (i < nf) {
+            face_sid[i] = 0;
+            bslot[i] = -1;
+            bmode[i] = 0;
+            if (m.owner[i] < 0 || m.owner[i] >= nc || m.neighbour[i] < -1 || m.neighbour[i] >= nc) bad = true;
+            for (int side = 0; side < 2; ++side) {
+                const double len = m.disp_len[side * nf + i];
+                disp_unit[side * nf + i] = len > 0 ? m.disp[side * nf + i] / len : 0.0;
+                disp_unit[(2 + side) * nf + i] = len > 0 ? m.disp[(2 + side) * nf + i] / len : 0.0;
+            }
+        }
+        if (bad) { ctrl->active = 0; atomicOr(&ctrl->status1, ST_SPATIAL); }
+    }
+}
+
+extern "C" int brx_rate_noalloc(int nc, int nf, int nadj, const int *owner, const int *neighbour, const int *offset,
+                                const int *faces, const int *signs, const double *normal, const double *length,
+                                const double *area, const double *ls_matrix, const double *ls_weight,
+                                const double *ls_delta, const double *displacement, const double *displacement_length,
+                                const double *distance, const double *q, const double *z, double gravity, double dry,
+                                double cfl, double dt, double *rate, double *water, unsigned *status, double *freq,
+                                void *stream)
+{
+    if (nc < 1 || nf < 1 || nadj < 1) return fail(BRX_ERR_ARGUMENT, "empty mesh");
+    if (nc > NOALLOC_MAX_CELLS || nf > NOALLOC_MAX_FACES)
+        return fail(BRX_ERR_UNSUPPORTED, "brx_rate_noalloc takes at most 16384 cells and 32768 faces");
+    if (!owner || !neighbour || !offset || !faces || !signs || !normal || !length || !area || !ls_matrix ||
+        !ls_weight || !ls_delta || !displacement || !displacement_length || !distance || !q || !z || !rate || !water)
+        return fail(BRX_ERR_ARGUMENT, "null device pointer");
+    if (!(gravity > 0) || !(dry > 0) || !(cfl > 0 && cfl <= 1) || !(dt > 0) || !std::isfinite(dt))
+        return fail(BRX_ERR_ARGUMENT, "gravity, dry, dt positive and CFL in (0, 1]");
+    unsigned char *base = nullptr;
+    TRY(noalloc_address(&base));
+    cudaStream_t st = (cudaStream_t)stream;
+    int *cell_sid = (int *)(base + NA_CSID), *cflags = (int *)(base + NA_CFLAGS);
+    int *face_sid = (int *)(base + NA_FSID), *bslot = (int *)(base + NA_BSLOT), *bmode = (int *)(base + NA_BMODE);
+    double *disp_unit = (double *)(base + NA_DUNIT);
+    Ctrl *ctrl = (Ctrl *)(base + NA_CTRL);
+    MeshDev m{};
+    m.nc = nc; m.nf = nf; m.nadj = nadj; m.nscen = 1;
+    m.owner = owner; m.neighbour = neighbour; m.bid = bslot;   // closed domain: every bid is -1
+    m.offset = offset; m.faces = faces; m.signs = signs;
+    m.bslot = bslot; m.bmode = bmode; m.cell_sid = cell_sid; m.face_sid = face_sid; m.cflags = cflags;
+    m.normal = normal; m.length = length; m.area = area; m.ls_matrix = ls_matrix; m.ls_weight = ls_weight;
+    m.ls_delta = ls_delta; m.disp = displacement; m.disp_unit = disp_unit; m.disp_len = displacement_length;
+    m.distance = distance;
+    StateDev sd{};
+    sd.q[0] = const_cast<double *>(q);
+    sd.work = const_cast<double *>(q);    // the residual reads its stage state here and never writes it
+    sd.z = z;
+    Work w{};
+    w.rec = (CellRec *)(base + NA_REC);
+    w.ws = (double2 *)(base + NA_WS);
+    w.gf = (double4_32a *)(base + NA_GF);
+    w.lim = (double4_32a *)(base + NA_LIM);
+    w.rate = (double *)(base + NA_RATE);
+    w.theta = (double *)(base + NA_THETA);
+    BoundaryDev b{};
+    Ctrl init{};
+    init.grav = gravity; init.dry = dry; init.cfl = cfl; init.speed_limit = 50.0;
+    init.roughness_mode = 1; init.roughness_value = 1.0; init.active = 1;
+    init.dt_outer = dt; init.hint = dt; init.trial = dt; init.max_substeps = 1;
+    // Every field the residual reads is rewritten here: the array keeps the
+    // previous call's contents, and calls that overlap on the GPU race on it.
+    k_noalloc_ctrl<<<1, 1, 0, st>>>(ctrl, init);
+    const int n = nc > nf ? nc : nf;
+    k_noalloc_tables<<<(n + 255) / 256, 256, 0, st>>>(m, ctrl, cell_sid, cflags, face_sid, bslot, bmode, disp_unit);
+    k_cells<MAX_CELL_FACES><<<(nc + 127) / 128, 128, 0, st>>>(m, sd, ctrl, w, 1);
+    k_faces<<<(nf + 127) / 128, 128, 0, st>>>(m, sd, b, ctrl, w, 1);
+    k_gather<<<(nc + 255) / 256, 256, 0, st>>>(m, sd, ctrl, w, 1);
+    k_limit<<<(nf + 255) / 256, 256, 0, st>>>(m, sd, ctrl, w, 1);
+    k_update<<<(nc + 255) / 256, 256, 0, st>>>(m, sd, ctrl, w, 1, rate);
+    k_water_out<<<(nf + 255) / 256, 256, 0, st>>>(m, w, water);
+    CK(cudaGetLastError());
+    Ctrl out{};
+    CK(cudaMemcpyAsync(&out, ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    const double f1 = bits_to_double(out.peak1);
+    unsigned bits = out.status1;
+    if (!(bits & ST_PRE) && dt * f1 > cfl * (1 + 1e-12)) bits |= 32u;
+    if (status) *status = bits;
+    if (freq) *freq = f1;
+    if (!out.active) return fail(BRX_ERR_ARGUMENT, "mesh topology out of range or a cell with more than 32 faces");
     return BRX_OK;
 }

@@ -143,6 +143,35 @@ int brx_graph_chunk_set(brx_solver *s, int substeps);
  * of launches. The bound state is advanced as by brx_substep. */
 int brx_profile_substep(brx_solver *s, double dt, double time, int cap, double *ms, int *kind, int *count);
 
+/* Allocation-free spatial residual of one closed scenario (walls only, no
+ * open boundaries). It has no counterpart in the reference: it exists for
+ * callers that may not allocate device memory once running - hosts that hand
+ * out a fixed device-memory budget at start-up, or real-time loops where a
+ * cudaMalloc would synchronise the device - and computes what brx_rate
+ * computes (rate (3,nc), limited water flux (nf), status bits and CFL
+ * frequency) without a solver handle and without allocating.
+ *
+ * Every mesh, state and output pointer is the caller's DEVICE memory, laid
+ * out as for brx_solver_create and brx_rate; status and freq are host
+ * pointers (may be NULL). At most 16384 cells and 32768 faces: larger meshes
+ * get BRX_ERR_UNSUPPORTED. The stage scratch is one static device array of
+ * about 7.4 MB that every GPU loading this library holds until process exit.
+ * The first call on each device looks up that array's device address
+ * (cudaGetSymbolAddress) with the device current; make that first call
+ * before any stream capture. Calls share the array and rewrite what they
+ * read, so consecutive calls are independent, but calls that overlap on the
+ * GPU (other streams, other host threads) race on it. The call runs on
+ * `stream` (cudaStream_t as void*, NULL for the default stream) and returns
+ * after it has finished. Invalid device topology (index out of range, a
+ * cell with more than 32 faces) is detected on the device and reported as
+ * BRX_ERR_ARGUMENT without touching the mesh further. */
+int brx_rate_noalloc(int nc, int nf, int nadj, const int *owner, const int *neighbour, const int *offset,
+                     const int *faces, const int *signs, const double *normal, const double *length,
+                     const double *area, const double *ls_matrix, const double *ls_weight, const double *ls_delta,
+                     const double *displacement, const double *displacement_length, const double *distance,
+                     const double *q, const double *z, double gravity, double dry, double cfl, double dt,
+                     double *rate, double *water, unsigned *status, double *freq, void *stream);
+
 /* Kernel launches issued by this solver since creation (own kernels only). */
 long long brx_launch_count(const brx_solver *s);
 
