@@ -45,11 +45,21 @@ def peaks():
 
 
 def build_workload(name, rank=0, world=1):
+    """(cases, precision, outer dt [s], config dict). Built before CUDA starts (spawn pool)."""
     import braids_hkt_gb300.scenarios as S
     if name == "config1":
         return [S.config1()], "fp64", 1.0, dict(workload="config1: straight channel 2000x200 m, 4 m jittered "
                                                "Delaunay, 50k triangles, Q=400 m3/s, stage 3.0 m, Manning 0.03, "
                                                "CFL 0.9, FP64 plain form")
+    if name == "config4":
+        params = S.config4_params(64, seed=4 + rank)
+        workers = max(1, (os.cpu_count() or 1) // max(world, 1))
+        cases = S.build_cases(params, workers)
+        return cases, "mixed", 0.5, dict(
+            workload="config4: 64 channel scenarios in one batch, cells logU(1e4,5e5), width U(100,400) m, "
+                     "Q U(100,1500) m3/s, length 10 widths, jittered Delaunay, Manning 0.03, CFL 0.9, "
+                     "mixed FP32/FP64 form, no turbines",
+            scenarios=len(cases))
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -156,6 +166,8 @@ def reference_arm(args):
     if rank != 0:
         return
     cases, precision, outer, cfg = build_workload(args.workload)
+    cases = sorted(cases, key=lambda c: c["mesh"].nc)[len(cases) // 2:len(cases) // 2 + 1]   # a median scenario
+    cfg = dict(cfg, cpu_sample="one median-size scenario of the workload")
     threads = os.cpu_count() or 1
     per_step = []
     for _ in range(args.warmup):
@@ -178,16 +190,18 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
-    ap.add_argument("--workload", default="config1")
+    ap.add_argument("--workload", default="config4")
+    ap.add_argument("--plain", type=int, default=3, help="scenarios re-run one by one in plain FP64")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
 
-    import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    cases, precision, outer, cfg = build_workload(args.workload, rank, world)   # before any CUDA use
+    import torch
     torch.cuda.set_device(local)
     dist = None
     if world > 1:
@@ -195,7 +209,6 @@ def main():
         dist.init_process_group("nccl")
     from braids_hkt_gb300.solver import RiverSolver
 
-    cases, precision, outer, cfg = build_workload(args.workload, rank, world)
     solver = RiverSolver(cases, precision=precision)
     nc, nf = solver.nc, solver.nf
     nadj = int(solver.packed["nadj"])
@@ -209,8 +222,11 @@ def main():
             dist.barrier()
 
     sim_time = 0.0
+    failed = set()
     for _ in range(args.warmup):
-        solver.advance(outer, sim_time)
+        diags = solver.advance(outer, sim_time, raise_on_failure=False)
+        diags = diags if isinstance(diags, list) else [diags]
+        failed |= {i for i, d in enumerate(diags) if d["failed"]}
         sim_time += outer
     # timed region: K outer steps, device time by events on the solver stream
     clocks = ClockSampler(local)
@@ -218,6 +234,7 @@ def main():
     launches0 = solver.launches()
     updates = 0
     device_ms = 0.0
+    step_ms = []
     barrier()
     wall0 = time.perf_counter()
     for _ in range(args.steps):
@@ -226,12 +243,14 @@ def main():
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        diags = solver.advance(outer, sim_time)
+        diags = solver.advance(outer, sim_time, raise_on_failure=False)
         e1.record(stream)
         e1.synchronize()
-        device_ms += e0.elapsed_time(e1)
+        step_ms.append(e0.elapsed_time(e1))
+        device_ms += step_ms[-1]
         sim_time += outer
         diags = diags if isinstance(diags, list) else [diags]
+        failed |= {i for i, d in enumerate(diags) if d["failed"]}
         updates += sum(d["hydraulic_substeps"] * (solver.packed["cell_offset"][i + 1] - solver.packed["cell_offset"][i])
                        for i, d in enumerate(diags))
     barrier()
@@ -289,19 +308,62 @@ def main():
                 "algorithmic_bytes_per_launch": dom_bytes,
                 "step_bytes_per_cell_update": BYTES_PER_CELL_UPDATE[precision],
                 "step_achieved_gbs": value * BYTES_PER_CELL_UPDATE[precision] / 1e9}
+    # the same scenarios one by one in the plain FP64 form, from the same initial state over the same
+    # intervals: FP64 throughput and the mixed form's depth error against it
+    plain = None
+    if precision == "mixed" and args.plain > 0:
+        order = np.argsort([c["mesh"].nc for c in cases])
+        pick = [int(order[0]), int(order[len(order) // 2]), int(order[-1])][:args.plain]
+        p_updates, p_ms, errs = 0, 0.0, []
+        batch_state = solver.q.cpu().numpy()
+        off = solver.packed["cell_offset"]
+        nsteps = args.warmup + args.steps
+        for i in pick:
+            one = RiverSolver(cases[i], precision="fp64")
+            t_sim = 0.0
+            for k in range(nsteps):
+                torch.cuda.synchronize()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(one.stream)
+                d = one.advance(outer, t_sim)
+                e1.record(one.stream)
+                e1.synchronize()
+                t_sim += outer
+                if k >= args.warmup:
+                    p_ms += e0.elapsed_time(e1)
+                    p_updates += d["hydraulic_substeps"] * one.nc
+            h64 = one.q[0].cpu().numpy()
+            hmx = batch_state[0, off[i]:off[i + 1]]
+            rel = np.abs(hmx - h64) / np.maximum(h64, 1e-3)
+            errs.append((float(rel.max()), float(np.percentile(rel, 99))))
+            one.close()
+        plain = {"value": p_updates / (p_ms / 1e3), "unit": METRIC, "scenarios": pick,
+                 "cells": [int(cases[i]["mesh"].nc) for i in pick],
+                 "note": "each scenario alone in the FP64 form over the same intervals"}
+        cfg["accuracy_vs_fp64"] = {"depth_rel_max": max(e[0] for e in errs), "depth_rel_p99": max(e[1] for e in errs),
+                                   "scenarios": pick, "after_sim_s": nsteps * outer,
+                                   "stated_tolerance": 1e-4}
     if rank != 0:
         return
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": device_ms / max(args.steps, 1), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if precision == "fp64" else "f32+f64",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if precision == "fp64" else "f32/f64 mixed",
             "data": "synthetic", "config": dict(cfg, cells=nc, faces=nf, outer_dt_s=outer,
+                                                failed_scenarios=sorted(failed),
                                                 l2="flushed between steps (256 MiB write)",
                                                 wall_s=wall),
             "roofline": roofline, "clocks": clock_info, "gpu_launches": int(gpu_launches),
+            "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99)),
+                           "what": "device time of one outer interval of the whole batch"},
             "e2e": {"value": e2e_updates / e2e_s, "unit": METRIC, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": h2d}}
+    if plain is not None:
+        line["plain_fp64"] = plain
+        line["batched_vs_plain_fp64"] = value / plain["value"]
     if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(cases, outer)
+        median = sorted(cases, key=lambda c: c["mesh"].nc)[len(cases) // 2]
+        line["cpu_baseline"] = cpu_baseline([median], outer)
     print(json.dumps(line), flush=True)
 
 

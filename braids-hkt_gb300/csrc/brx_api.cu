@@ -19,7 +19,9 @@
 #include <vector>
 
 #include "../../include/braids_gb300.h"
+#define BRX_NS brx
 #include "brx_kernels.cuh"
+#include "brx_launch.h"
 
 using namespace brx;
 
@@ -43,6 +45,8 @@ struct brx_solver {
     int nscen = 0, nc = 0, nf = 0, nadj = 0, nseg = 0, nslot = 0, nown = 0, maxdeg = 0;
     int device = 0, sms = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;       // boundary CTAs run here, concurrent with the cell sweep
+    cudaEvent_t fork = nullptr, join = nullptr;
     std::vector<void *> allocations;
     MeshDev mesh{};
     BoundaryDev bnd{};
@@ -169,7 +173,6 @@ extern "C" int brx_solver_create(int nscen, const int *cell_offset, const int *f
     if (!out) return fail(BRX_ERR_ARGUMENT, "null output handle");
     *out = nullptr;
     if (precision != BRX_FP64 && precision != BRX_MIXED) return fail(BRX_ERR_ARGUMENT, "unknown precision");
-    if (precision == BRX_MIXED) return fail(BRX_ERR_UNSUPPORTED, "mixed precision form is not built in this library");
     if (!normal || !length || !area || !ls_matrix || !ls_weight || !ls_delta || !displacement || !distance)
         return fail(BRX_ERR_ARGUMENT, "null geometry array");
     TRY(validate(nscen, cell_offset, face_offset, nc, nf, nadj, owner, neighbour, bid, offset, faces, signs, nseg,
@@ -181,6 +184,9 @@ extern "C" int brx_solver_create(int nscen, const int *cell_offset, const int *f
         CK(cudaGetDevice(&s->device));
         CK(cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, s->device));
         CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+        CK(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&s->join, cudaEventDisableTiming));
         s->cell_offset.assign(cell_offset, cell_offset + nscen + 1);
         s->face_offset.assign(face_offset, face_offset + nscen + 1);
         s->seg_offset.assign(nscen + 1, 0);
@@ -298,7 +304,7 @@ extern "C" int brx_solver_create(int nscen, const int *cell_offset, const int *f
         }
         // persistent grids: a multiple of the SM count, no more blocks than the work needs
         int occ128 = 0, occ256 = 0;
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ128, k_faces, 128, 0));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ128, k_faces<double>, 128, 0));
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ256, k_gather, 256, 0));
         occ128 = std::max(occ128, 1); occ256 = std::max(occ256, 1);
         auto grid = [&](int n, int block, int occ) { return std::max(1, std::min((n + block - 1) / block, s->sms * occ)); };
@@ -317,6 +323,9 @@ extern "C" int brx_solver_destroy(brx_solver *s)
     if (s->graph) cudaGraphExecDestroy(s->graph);
     for (void *p : s->allocations) cudaFree(p);
     if (s->h_ctrl) cudaFreeHost(s->h_ctrl);
+    if (s->fork) cudaEventDestroy(s->fork);
+    if (s->join) cudaEventDestroy(s->join);
+    if (s->side) cudaStreamDestroy(s->side);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return BRX_OK;
@@ -439,26 +448,70 @@ extern "C" void *brx_stream(brx_solver *s) { return s ? (void *)s->stream : null
 // ---------------------------------------------------------------------------
 // launch sequences
 // ---------------------------------------------------------------------------
+static Launch make_launch(brx_solver *s, cudaStream_t st)
+{
+    Launch L;
+    L.mesh = s->mesh; L.state = s->state; L.bnd = s->bnd; L.work = s->work; L.ctrl = s->d_ctrl;
+    L.nscen = s->nscen; L.nslot = s->nslot; L.maxdeg = s->maxdeg;
+    L.grid_c = s->grid_c; L.grid_f = s->grid_f; L.grid_c256 = s->grid_c256; L.grid_f256 = s->grid_f256;
+    L.stream = st;
+    return L;
+}
+
+// Launch one kernel of the solver's arithmetic form on stream st (default:
+// the solver stream); returns launches issued.
+static int launch_kernel(brx_solver *s, int kind, int stage, double *rate_out, cudaStream_t st = nullptr)
+{
+    if (!st) st = s->stream;
+    if (s->precision == BRX_MIXED) return mixed_kernel(make_launch(s, st), kind, stage, rate_out);
+    switch (kind) {
+    case K_DRAG:
+        k_open_drag<double><<<s->grid_c256, 256, 0, st>>>(s->mesh, s->state, s->d_ctrl);
+        return 1;
+    case K_BOUNDARY:
+        if (!s->nslot) return 0;
+        k_boundary<double><<<s->nscen, 256, 0, st>>>(s->mesh, s->state, s->bnd, s->d_ctrl, stage);
+        return 1;
+    case K_CELLS:
+        if (s->maxdeg <= 4) k_cells<double, 4><<<s->grid_c, 128, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage);
+        else k_cells<double, MAX_CELL_FACES><<<s->grid_c, 128, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage);
+        return 1;
+    case K_FACES:
+        k_faces<double><<<s->grid_f, 128, 0, st>>>(s->mesh, s->state, s->bnd, s->d_ctrl, s->work, stage);
+        return 1;
+    case K_GATHER:
+        k_gather<<<s->grid_c256, 256, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage);
+        return 1;
+    case K_LIMIT:
+        k_limit<<<s->grid_f256, 256, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage);
+        return 1;
+    case K_UPDATE:
+        k_update<double><<<s->grid_c256, 256, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage, rate_out);
+        return 1;
+    }
+    return 0;
+}
+
+// One stage: the boundary CTAs fork onto the side stream and overlap the cell
+// sweep (they are independent); the face sweep joins both.
 static void enqueue_stage(brx_solver *s, int stage, double *rate_out)
 {
-    cudaStream_t st = s->stream;
-    if (s->nslot) {
-        k_boundary<<<s->nscen, 256, 0, st>>>(s->mesh, s->state, s->bnd, s->d_ctrl, stage);
-        s->launches++;
+    const bool fork = s->nslot > 0;
+    if (fork) {
+        cudaEventRecord(s->fork, s->stream);
+        cudaStreamWaitEvent(s->side, s->fork, 0);
+        s->launches += launch_kernel(s, K_BOUNDARY, stage, nullptr, s->side);
+        cudaEventRecord(s->join, s->side);
     }
-    if (s->maxdeg <= 4) k_cells<4><<<s->grid_c, 128, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage);
-    else k_cells<MAX_CELL_FACES><<<s->grid_c, 128, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage);
-    k_faces<<<s->grid_f, 128, 0, st>>>(s->mesh, s->state, s->bnd, s->d_ctrl, s->work, stage);
-    k_gather<<<s->grid_c256, 256, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage);
-    k_limit<<<s->grid_f256, 256, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage);
-    k_update<<<s->grid_c256, 256, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage, rate_out);
-    s->launches += 5;
+    s->launches += launch_kernel(s, K_CELLS, stage, nullptr);
+    if (fork) cudaStreamWaitEvent(s->stream, s->join, 0);
+    for (int kind = K_FACES; kind <= K_UPDATE; ++kind)
+        s->launches += launch_kernel(s, kind, stage, kind == K_UPDATE ? rate_out : nullptr);
 }
 
 static void enqueue_substep(brx_solver *s)
 {
-    k_open_drag<<<s->grid_c256, 256, 0, s->stream>>>(s->mesh, s->state, s->d_ctrl);
-    s->launches++;
+    s->launches += launch_kernel(s, K_DRAG, 0, nullptr);
     enqueue_stage(s, 1, nullptr);
     enqueue_stage(s, 2, nullptr);
     k_control<<<(s->nscen + 127) / 128, 128, 0, s->stream>>>(s->d_ctrl, s->nscen);
@@ -473,11 +526,13 @@ static void host_set_trial(Ctrl &c)
     c.peak1 = c.peak2 = 0ull;
 }
 
-static void begin_interval(brx_solver *s, double dt, double time, bool fixed)
+// Per-scenario interval [time[i], time[i] + dt[i]]; dt[i] <= 0 leaves scenario i idle.
+static void begin_interval_each(brx_solver *s, const double *dt_each, const double *time_each, bool fixed)
 {
     for (int i = 0; i < s->nscen; ++i) {
         Ctrl &c = s->h_ctrl[i];
-        c.active = s->active[i];
+        const double dt = dt_each[i], time = time_each[i];
+        c.active = s->active[i] && dt > 0;
         c.dt_outer = dt; c.time0 = time; c.elapsed = 0.0;
         c.hint = fixed ? dt : (s->hint[i] > 0 ? s->hint[i] : dt);
         c.floor_ = std::ldexp(dt, -20);
@@ -486,6 +541,12 @@ static void begin_interval(brx_solver *s, double dt, double time, bool fixed)
         c.done = !c.active;
         host_set_trial(c);
     }
+}
+
+static void begin_interval(brx_solver *s, double dt, double time, bool fixed)
+{
+    std::vector<double> d(s->nscen, dt), t(s->nscen, time);
+    begin_interval_each(s, d.data(), t.data(), fixed);
 }
 
 static int ensure_ready(brx_solver *s)
@@ -514,12 +575,29 @@ static int build_graph(brx_solver *s)
     return BRX_OK;
 }
 
+static int advance_impl(brx_solver *s, const double *dt, const double *time, brx_advance_stats *stats);
+
 extern "C" int brx_advance(brx_solver *s, double dt, double time, brx_advance_stats *stats)
 {
     TRY(ensure_ready(s));
     if (!(dt > 0) || !std::isfinite(dt) || !std::isfinite(time)) return fail(BRX_ERR_ARGUMENT, "dt must be finite and positive");
+    std::vector<double> d(s->nscen, dt), t(s->nscen, time);
+    return advance_impl(s, d.data(), t.data(), stats);
+}
+
+extern "C" int brx_advance_batch(brx_solver *s, const double *dt, const double *time, brx_advance_stats *stats)
+{
+    TRY(ensure_ready(s));
+    if (!dt || !time) return fail(BRX_ERR_ARGUMENT, "null interval arrays");
+    for (int i = 0; i < s->nscen; ++i)
+        if (!std::isfinite(dt[i]) || !std::isfinite(time[i])) return fail(BRX_ERR_ARGUMENT, "nonfinite interval");
+    return advance_impl(s, dt, time, stats);
+}
+
+static int advance_impl(brx_solver *s, const double *dt, const double *time, brx_advance_stats *stats)
+{
     if (s->graph_dirty || !s->graph) TRY(build_graph(s));
-    begin_interval(s, dt, time, false);
+    begin_interval_each(s, dt, time, false);
     CK(cudaMemcpyAsync(s->d_ctrl, s->h_ctrl, sizeof(Ctrl) * s->nscen, cudaMemcpyHostToDevice, s->stream));
     // every scenario ends within max_substeps accepted + 101 rejected trials
     const int max_replays = (4096 + 102) / s->graph_chunk + 2;
@@ -562,8 +640,7 @@ extern "C" int brx_substep(brx_solver *s, double dt, double time, unsigned *stat
     for (int i = 0; i < s->nscen; ++i) s->h_ctrl[i].max_substeps = 4096;
     CK(cudaMemcpyAsync(s->d_ctrl, s->h_ctrl, sizeof(Ctrl) * s->nscen, cudaMemcpyHostToDevice, s->stream));
     // the trial without the controller: its statuses are read before control runs
-    k_open_drag<<<s->grid_c256, 256, 0, s->stream>>>(s->mesh, s->state, s->d_ctrl);
-    s->launches++;
+    s->launches += launch_kernel(s, K_DRAG, 0, nullptr);
     enqueue_stage(s, 1, nullptr);
     enqueue_stage(s, 2, nullptr);
     CK(cudaMemcpyAsync(s->h_ctrl, s->d_ctrl, sizeof(Ctrl) * s->nscen, cudaMemcpyDeviceToHost, s->stream));
@@ -631,17 +708,10 @@ extern "C" int brx_profile_substep(brx_solver *s, double dt, double time, int ca
     };
     cudaStream_t st = s->stream;
     mark(-1);
-    k_open_drag<<<s->grid_c256, 256, 0, st>>>(s->mesh, s->state, s->d_ctrl); mark(0);
-    for (int stage = 1; stage <= 2; ++stage) {
-        if (s->nslot) { k_boundary<<<s->nscen, 256, 0, st>>>(s->mesh, s->state, s->bnd, s->d_ctrl, stage); mark(1); }
-        if (s->maxdeg <= 4) k_cells<4><<<s->grid_c, 128, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage);
-        else k_cells<MAX_CELL_FACES><<<s->grid_c, 128, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage);
-        mark(2);
-        k_faces<<<s->grid_f, 128, 0, st>>>(s->mesh, s->state, s->bnd, s->d_ctrl, s->work, stage); mark(3);
-        k_gather<<<s->grid_c256, 256, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage); mark(4);
-        k_limit<<<s->grid_f256, 256, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage); mark(5);
-        k_update<<<s->grid_c256, 256, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage, nullptr); mark(6);
-    }
+    if (launch_kernel(s, K_DRAG, 0, nullptr)) mark(K_DRAG);
+    for (int stage = 1; stage <= 2; ++stage)
+        for (int kind = K_BOUNDARY; kind <= K_UPDATE; ++kind)
+            if (launch_kernel(s, kind, stage, nullptr)) mark(kind);
     k_control<<<(s->nscen + 127) / 128, 128, 0, st>>>(s->d_ctrl, s->nscen); mark(7);
     k_commit<<<s->grid_c256, 256, 0, st>>>(s->mesh, s->state, s->d_ctrl);
     s->launches += (long long)kinds.size() + 1;
@@ -805,11 +875,11 @@ extern "C" int brx_rate_noalloc(int nc, int nf, int nadj, const int *owner, cons
     k_noalloc_ctrl<<<1, 1, 0, st>>>(ctrl, init);
     const int n = nc > nf ? nc : nf;
     k_noalloc_tables<<<(n + 255) / 256, 256, 0, st>>>(m, ctrl, cell_sid, cflags, face_sid, bslot, bmode, disp_unit);
-    k_cells<MAX_CELL_FACES><<<(nc + 127) / 128, 128, 0, st>>>(m, sd, ctrl, w, 1);
-    k_faces<<<(nf + 127) / 128, 128, 0, st>>>(m, sd, b, ctrl, w, 1);
+    k_cells<double, MAX_CELL_FACES><<<(nc + 127) / 128, 128, 0, st>>>(m, sd, ctrl, w, 1);
+    k_faces<double><<<(nf + 127) / 128, 128, 0, st>>>(m, sd, b, ctrl, w, 1);
     k_gather<<<(nc + 255) / 256, 256, 0, st>>>(m, sd, ctrl, w, 1);
     k_limit<<<(nf + 255) / 256, 256, 0, st>>>(m, sd, ctrl, w, 1);
-    k_update<<<(nc + 255) / 256, 256, 0, st>>>(m, sd, ctrl, w, 1, rate);
+    k_update<double><<<(nc + 255) / 256, 256, 0, st>>>(m, sd, ctrl, w, 1, rate);
     k_water_out<<<(nf + 255) / 256, 256, 0, st>>>(m, w, water);
     CK(cudaGetLastError());
     Ctrl out{};

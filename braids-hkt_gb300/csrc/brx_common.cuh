@@ -1,0 +1,180 @@
+// Types and device helpers shared by both arithmetic forms of the river step.
+//
+// One substep = drag(dt/2) -> 2 x [boundary -> cells -> faces -> gather ->
+// limit -> update] -> control. Every kernel is batch-aware: cells and faces
+// of many scenarios are packed into one index space, each element carries
+// its scenario id, and each scenario owns a Ctrl block on the device that
+// holds its clock (trial dt, elapsed time, hint) and its rejection status.
+// The plain form is a batch of one.
+//
+// Restated from (file:line in the reference):
+//   boundary     src/braids_core/sediment/river_exterior_bed.h:29-174,
+//                src/braids_core/hydraulics/outlet_feasibility.py:25-38
+//   cells        src/braids_support/gpu_fwave/reconstruction.cu:24-168 with the
+//                wall_bed_hydraulics transforms (wall velocity bounds, LS
+//                fallback, directional projection limiter)
+//   faces        reconstruction.cu:170-212, resident_update.cu:11-148 with the
+//                hydrostatic-reconstruction and reflecting-wall transforms,
+//                augmented_fwave.cu:264-334
+//   gather       src/braids_gpu/implicit_midpoint_fwave.cu:65-90,
+//                src/braids_core/sediment/river_midpoint.h:21-29 (inventory),
+//                river_explicit_boundary_budget.py:41-50 (reservation),
+//                river_explicit.h:13-26 (CFL frequency)
+//   limit        river_midpoint.h:30-41
+//   update       river_midpoint.h:42-49, river_explicit.py:94-117
+//   drag         river_hydraulic_drag.h:3-16, river_roughness.py:42-47
+//   control      river_explicit.py:121-154
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+#include "brx_fwave.cuh"
+
+namespace brx {
+
+constexpr double EPS = 2.2204460492503131e-16;
+constexpr double DBL_MIN_ = 2.2250738585072014e-308;
+
+// Status bits of one stage. PRE bits are raised before the reference computes
+// its CFL frequency, so a stage that raised one does not feed the step hint.
+enum : unsigned {
+    ST_SPATIAL = 1u,      // invalid state, boundary, reconstruction or face status
+    ST_BUDGET = 2u,       // prescribed boundary exceeds the owner's stock
+    ST_RATE = 4u,         // nonfinite rate
+    ST_ENDPOINT = 8u,     // negative / nonfinite stage result
+    ST_FREQ = 16u,        // nonfinite CFL frequency
+    ST_PRE = ST_SPATIAL | ST_BUDGET | ST_RATE | ST_FREQ,
+};
+
+// Per-scenario clock and controls, resident on the device.
+struct Ctrl {
+    // controls
+    double grav, dry, cfl, speed_limit, roughness_value;
+    int roughness_mode, active;       // active: scenario takes part in this interval
+    // interval
+    double dt_outer, time0, elapsed, hint, floor_, trial;
+    int truncated, substeps, rejections, done;
+    int failed, cur, max_substeps, pad0;
+    // this trial
+    unsigned status1, status2;
+    unsigned long long peak1, peak2;  // bit patterns of nonnegative doubles
+    // diagnostics
+    double min_dt, max_dt, cfl_max;
+    double accepted_water_time;       // sum of accepted trial lengths (== elapsed)
+};
+
+struct MeshDev {
+    int nc, nf, nadj, nscen;
+    const int *owner, *neighbour, *bid, *offset, *faces, *signs;
+    const int *bslot;        // per face: boundary slot (open faces) or -1
+    const int *bmode;        // per face: hydraulic mode of its open segment, else 0
+    const int *cell_sid, *face_sid;
+    const int *cflags;       // per cell: bit0 owns an open face
+    const double *normal, *length, *area;
+    const double *ls_matrix, *ls_weight, *ls_delta;
+    const double *disp, *disp_unit, *disp_len, *distance;
+};
+
+struct BoundaryDev {
+    int nseg, nslot, nown;
+    const int *scen_seg;     // (nscen+1) segment range per scenario
+    const int *scen_own;     // (nscen+1) unique-owner range per scenario
+    const int *seg_off;      // (nseg+1) slot range per segment
+    const int *slot_face;    // (nslot)
+    const int *seg_mode, *stage_policy;
+    const double *ext_bed;   // (nslot)
+    double *forcing;         // (2,nseg) sampled per stage
+    int table_len;
+    const double *table_time;   // (table_len)
+    const double *table_value;  // (2, nseg, table_len)
+    const int *own_cell, *own_off, *own_slot;  // unique owners, CSR into slots (boundary order)
+    double *terms;           // (3, nslot) scratch: stage terms and weights
+    double *trace, *flux;    // (3, nslot) each
+    double *seg_sums;        // (3, nseg): wetted stage sum, wetted width, weight total
+};
+
+// Accepted / stage state buffers.
+struct StateDev {
+    double *q[2];            // (3,nc) ping-pong: ctrl.cur holds the accepted state
+    double *work;            // (3,nc) base after the opening drag
+    double *q1;              // (3,nc) first-stage result
+    const double *z;         // (nc) bed
+};
+
+// 128-byte cell record written by the cell kernel, read by the face kernel.
+struct __align__(16) CellRec {
+    double h, eta, u, v, b;
+    double gx[4], gy[4];
+    int flags, pad;          // bit0 flatten (hydro_constant), bit1 active
+    double pad2;
+};
+static_assert(sizeof(CellRec) == 128, "cell record is one 128-byte line");
+
+struct Work {
+    CellRec *rec;            // (nc)
+    double2 *ws;             // (nf) water, CFL speed
+    double4_32a *gf;             // (nf) pressure-deviation momentum flux: left x,y, right x,y
+    double4_32a *lim;            // (nf) limited water, momentum correction x,y
+    double *rate;            // (3,nc)
+    double *theta;           // (nc)
+};
+
+__device__ __forceinline__ void atomic_max_nonneg(unsigned long long *addr, double v)
+{
+    // nonnegative doubles (including +inf) order like their bit patterns
+    atomicMax(addr, (unsigned long long)__double_as_longlong(v));
+}
+
+// Warp-aggregated max of nonnegative doubles into ctrl[sid].peak: lanes with
+// the same scenario reduce the high then the low 32 bits of their bit
+// patterns (nonnegative doubles order like their bits) and the first lane of
+// each group issues one atomic. Max is exact and order-free. Every lane of
+// the warp must call it; lanes without a value pass valid = false.
+__device__ __forceinline__ void warp_max_peak(unsigned long long *peak_of_sid0, size_t stride_bytes, int sid,
+                                              bool valid, double v)
+{
+    const unsigned long long bits = valid ? (unsigned long long)__double_as_longlong(v) : 0ull;
+    const unsigned same = __match_any_sync(0xffffffffu, valid ? sid : -1);
+    const unsigned hi = (unsigned)(bits >> 32), lo = (unsigned)(bits & 0xffffffffull);
+    const unsigned mhi = __reduce_max_sync(same, hi);
+    const unsigned mlo = __reduce_max_sync(same, hi == mhi ? lo : 0u);
+    if (valid && (int)(threadIdx.x & 31) == __ffs(same) - 1) {
+        unsigned long long *addr = (unsigned long long *)((char *)peak_of_sid0 + stride_bytes * (size_t)sid);
+        atomicMax(addr, ((unsigned long long)mhi << 32) | mlo);
+    }
+}
+
+__host__ __device__ __forceinline__ double bits_to_double(unsigned long long b)
+{
+#ifdef __CUDA_ARCH__
+    return __longlong_as_double((long long)b);
+#else
+    double d;
+    memcpy(&d, &b, sizeof d);
+    return d;
+#endif
+}
+
+// Stage 2 and the trailing kernels skip a scenario whose first stage failed.
+__device__ __forceinline__ bool stage1_failed(const Ctrl &c)
+{
+    if (c.status1) return true;
+    const double f = bits_to_double(c.peak1);
+    return c.trial * f > c.cfl * (1 + 1e-12);
+}
+
+__device__ __forceinline__ bool skip_stage(const Ctrl &c, int stage)
+{
+    if (!c.active || c.done) return true;
+    return stage == 2 && stage1_failed(c);
+}
+
+__device__ __forceinline__ void raise_status(Ctrl &c, int stage, unsigned bits)
+{
+    atomicOr(stage == 1 ? &c.status1 : &c.status2, bits);
+}
+
+constexpr int BOUNDARY_TILES = 1024;   // tile slots of 64 faces per scenario (checked at set-up)
+constexpr int MAX_CELL_FACES = 32;     // faces of one cell, checked at set-up
+
+}  // namespace brx

@@ -1,192 +1,57 @@
 // Kernels of one SSPRK(2,2) substep of the augmented f-wave river step.
 //
-// One substep = drag(dt/2) -> 2 x [boundary -> cells -> faces -> gather ->
-// limit -> update] -> control. Every kernel is batch-aware: cells and faces
-// of many scenarios are packed into one index space, each element carries
-// its scenario id, and each scenario owns a Ctrl block on the device that
-// holds its clock (trial dt, elapsed time, hint) and its rejection status.
-// The plain form is a batch of one.
-//
-// Restated from (file:line in the reference):
-//   boundary     src/braids_core/sediment/river_exterior_bed.h:29-174,
-//                src/braids_core/hydraulics/outlet_feasibility.py:25-38
-//   cells        src/braids_support/gpu_fwave/reconstruction.cu:24-168 with the
-//                wall_bed_hydraulics transforms (wall velocity bounds, LS
-//                fallback, directional projection limiter)
-//   faces        reconstruction.cu:170-212, resident_update.cu:11-148 with the
-//                hydrostatic-reconstruction and reflecting-wall transforms,
-//                augmented_fwave.cu:264-334
-//   gather       src/braids_gpu/implicit_midpoint_fwave.cu:65-90,
-//                src/braids_core/sediment/river_midpoint.h:21-29 (inventory),
-//                river_explicit_boundary_budget.py:41-50 (reservation),
-//                river_explicit.h:13-26 (CFL frequency)
-//   limit        river_midpoint.h:30-41
-//   update       river_midpoint.h:42-49, river_explicit.py:94-117
-//   drag         river_hydraulic_drag.h:3-16, river_roughness.py:42-47
-//   control      river_explicit.py:121-154
+// Included by one translation unit per arithmetic form. Each includer
+// defines BRX_NS (the namespace its kernel copies live in) so the FP64
+// unit (-fmad=false, reference operation order) and the mixed unit (FP32
+// fluxes, FMA on) never share a symbol. Kernels whose arithmetic differs
+// between the forms are templates on the flux type F; with F = double they
+// evaluate exactly the FP64 expressions of the reference.
 #pragma once
-#include <cuda_runtime.h>
-#include <stdint.h>
-#include <string.h>
-#include "brx_fwave.cuh"
+#include "brx_common.cuh"
 
-namespace brx {
-
-constexpr double EPS = 2.2204460492503131e-16;
-constexpr double DBL_MIN_ = 2.2250738585072014e-308;
-
-// Status bits of one stage. PRE bits are raised before the reference computes
-// its CFL frequency, so a stage that raised one does not feed the step hint.
-enum : unsigned {
-    ST_SPATIAL = 1u,      // invalid state, boundary, reconstruction or face status
-    ST_BUDGET = 2u,       // prescribed boundary exceeds the owner's stock
-    ST_RATE = 4u,         // nonfinite rate
-    ST_ENDPOINT = 8u,     // negative / nonfinite stage result
-    ST_FREQ = 16u,        // nonfinite CFL frequency
-    ST_PRE = ST_SPATIAL | ST_BUDGET | ST_RATE | ST_FREQ,
-};
-
-// Per-scenario clock and controls, resident on the device.
-struct Ctrl {
-    // controls
-    double grav, dry, cfl, speed_limit, roughness_value;
-    int roughness_mode, active;       // active: scenario takes part in this interval
-    // interval
-    double dt_outer, time0, elapsed, hint, floor_, trial;
-    int truncated, substeps, rejections, done;
-    int failed, cur, max_substeps, pad0;
-    // this trial
-    unsigned status1, status2;
-    unsigned long long peak1, peak2;  // bit patterns of nonnegative doubles
-    // diagnostics
-    double min_dt, max_dt, cfl_max;
-    double accepted_water_time;       // sum of accepted trial lengths (== elapsed)
-};
-
-struct MeshDev {
-    int nc, nf, nadj, nscen;
-    const int *owner, *neighbour, *bid, *offset, *faces, *signs;
-    const int *bslot;        // per face: boundary slot (open faces) or -1
-    const int *bmode;        // per face: hydraulic mode of its open segment, else 0
-    const int *cell_sid, *face_sid;
-    const int *cflags;       // per cell: bit0 owns an open face
-    const double *normal, *length, *area;
-    const double *ls_matrix, *ls_weight, *ls_delta;
-    const double *disp, *disp_unit, *disp_len, *distance;
-};
-
-struct BoundaryDev {
-    int nseg, nslot, nown;
-    const int *scen_seg;     // (nscen+1) segment range per scenario
-    const int *scen_own;     // (nscen+1) unique-owner range per scenario
-    const int *seg_off;      // (nseg+1) slot range per segment
-    const int *slot_face;    // (nslot)
-    const int *seg_mode, *stage_policy;
-    const double *ext_bed;   // (nslot)
-    double *forcing;         // (2,nseg) sampled per stage
-    int table_len;
-    const double *table_time;   // (table_len)
-    const double *table_value;  // (2, nseg, table_len)
-    const int *own_cell, *own_off, *own_slot;  // unique owners, CSR into slots (boundary order)
-    double *terms;           // (3, nslot) scratch: stage terms and weights
-    double *trace, *flux;    // (3, nslot) each
-    double *seg_sums;        // (3, nseg): wetted stage sum, wetted width, weight total
-};
-
-// Accepted / stage state buffers.
-struct StateDev {
-    double *q[2];            // (3,nc) ping-pong: ctrl.cur holds the accepted state
-    double *work;            // (3,nc) base after the opening drag
-    double *q1;              // (3,nc) first-stage result
-    const double *z;         // (nc) bed
-};
-
-// 128-byte cell record written by the cell kernel, read by the face kernel.
-struct __align__(16) CellRec {
-    double h, eta, u, v, b;
-    double gx[4], gy[4];
-    int flags, pad;          // bit0 flatten (hydro_constant), bit1 active
-    double pad2;
-};
-static_assert(sizeof(CellRec) == 128, "cell record is one 128-byte line");
-
-struct Work {
-    CellRec *rec;            // (nc)
-    double2 *ws;             // (nf) water, CFL speed
-    double4_32a *gf;             // (nf) pressure-deviation momentum flux: left x,y, right x,y
-    double4_32a *lim;            // (nf) limited water, momentum correction x,y
-    double *rate;            // (3,nc)
-    double *theta;           // (nc)
-};
-
-__device__ __forceinline__ void atomic_max_nonneg(unsigned long long *addr, double v)
-{
-    // nonnegative doubles (including +inf) order like their bit patterns
-    atomicMax(addr, (unsigned long long)__double_as_longlong(v));
-}
-
-__host__ __device__ __forceinline__ double bits_to_double(unsigned long long b)
-{
-#ifdef __CUDA_ARCH__
-    return __longlong_as_double((long long)b);
-#else
-    double d;
-    memcpy(&d, &b, sizeof d);
-    return d;
+#ifndef BRX_NS
+#error "define BRX_NS before including brx_kernels.cuh"
 #endif
-}
 
-// Stage 2 and the trailing kernels skip a scenario whose first stage failed.
-__device__ __forceinline__ bool stage1_failed(const Ctrl &c)
-{
-    if (c.status1) return true;
-    const double f = bits_to_double(c.peak1);
-    return c.trial * f > c.cfl * (1 + 1e-12);
-}
-
-__device__ __forceinline__ bool skip_stage(const Ctrl &c, int stage)
-{
-    if (!c.active || c.done) return true;
-    return stage == 2 && stage1_failed(c);
-}
-
-__device__ __forceinline__ void raise_status(Ctrl &c, int stage, unsigned bits)
-{
-    atomicOr(stage == 1 ? &c.status1 : &c.status2, bits);
-}
-
+namespace BRX_NS {
+using namespace brx;
 // ---------------------------------------------------------------------------
 // Drag: cell-local implicit Manning/Chezy friction over dt_scale * trial.
 // src/braids_core/sediment/river_hydraulic_drag.h:3-16
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double chezy(int method, double depth, double value)
+template <class F>
+__device__ __forceinline__ F chezy(int method, F depth, F value)
 {
     if (method == 1) return value;
-    if (method == 2) return pow(depth, 1. / 6.) / value;
-    if (method == 3) return sqrt(9.81) / .41 * log1p(30. * depth / (exp(1.) * value));
-    return 18. * log10(12. * fmax(.5, depth / value));
+    if (method == 2) return pow(depth, F(1.) / F(6.)) / value;
+    if (method == 3) return sqrt(F(9.81)) / F(.41) * log1p(F(30.) * depth / (exp(F(1.)) * value));
+    return F(18.) * log10(F(12.) * fmax(F(.5), depth / value));
 }
 
+// Depth stays FP64; the friction factor is evaluated in F.
+template <class F>
 __device__ __forceinline__ void drag_cell(const Ctrl &ct, double dt, double &h, double &hu, double &hv)
 {
     if (h <= ct.dry) { hu = 0.; hv = 0.; return; }
-    const double c = chezy(ct.roughness_mode, h, ct.roughness_value);
-    const double speed = sqrt(hu * hu + hv * hv) / h;
-    const double factor = 1. / (1. + dt * ct.grav * speed / (c * c * h));
+    const F hf = F(h), uf = F(hu), vf = F(hv);
+    const F c = chezy<F>(ct.roughness_mode, hf, F(ct.roughness_value));
+    const F speed = sqrt(uf * uf + vf * vf) / hf;
+    const F factor = F(1.) / (F(1.) + F(dt) * F(ct.grav) * speed / (c * c * hf));
     hu *= factor;
     hv *= factor;
 }
 
 // work = drag(accepted, trial/2)
+template <class F>
 __global__ void k_open_drag(MeshDev m, StateDev s, Ctrl *ctrl)
 {
     const int nc = m.nc;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
         const Ctrl &ct = ctrl[m.cell_sid[c]];
         if (!ct.active || ct.done) continue;
-        const double *q = s.q[ct.cur];
+        const double *q = ct.cur ? s.q[1] : s.q[0];
         double h = q[c], hu = q[nc + c], hv = q[2 * nc + c];
-        drag_cell(ct, .5 * ct.trial, h, hu, hv);
+        drag_cell<F>(ct, .5 * ct.trial, h, hu, hv);
         s.work[c] = h; s.work[nc + c] = hu; s.work[2 * nc + c] = hv;
     }
 }
@@ -197,14 +62,14 @@ __global__ void k_open_drag(MeshDev m, StateDev s, Ctrl *ctrl)
 // owners' stage-start stock. Sums use the reference's fixed tree: 64-face
 // tiles from each segment start, then the tiles in order.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double exterior_chezy(int mode, double h, double parameter, double floor_, double gravity,
-                                                  int waqua)
+template <class F>
+__device__ __forceinline__ F exterior_chezy(int mode, F h, F parameter, F floor_, F gravity, int waqua)
 {
-    const double d = fmax(h, floor_);
+    const F d = fmax(h, floor_);
     if (mode == 1) return parameter;
-    if (mode == 2) return pow(d, 1. / 6.) / parameter;
-    return waqua ? 18. * log10(12. * fmax(.5, d / parameter))
-                 : sqrt(gravity) / .41 * log1p(30. * d / (exp(1.) * parameter));
+    if (mode == 2) return pow(d, F(1.) / F(6.)) / parameter;
+    return waqua ? F(18.) * log10(F(12.) * fmax(F(.5), d / parameter))
+                 : sqrt(gravity) / F(.41) * log1p(F(30.) * d / (exp(F(1.)) * parameter));
 }
 
 __device__ __forceinline__ void stage_wave(double h, double un, double target, double gravity, double &depth,
@@ -263,8 +128,8 @@ __device__ void segment_sums(const BoundaryDev &b, int s0, int s1, int row, int 
     __syncthreads();
 }
 
-constexpr int BOUNDARY_TILES = 1024;   // tile slots of 64 faces per scenario (checked at set-up)
 
+template <class F>
 __global__ void k_boundary(MeshDev m, StateDev s, BoundaryDev b, Ctrl *ctrl, int stage)
 {
     __shared__ double tile_buf[BOUNDARY_TILES];
@@ -321,7 +186,8 @@ __global__ void k_boundary(MeshDev m, StateDev s, BoundaryDev b, Ctrl *ctrl, int
             const double h = fmax(q[c] + z[c] - bed, 0.);
             const double section = fmax(b.seg_sums[sg] / b.seg_sums[nseg + sg] - bed, 0.);
             if (h > dry && section > 0.)
-                w = pow(section, 1.5) * exterior_chezy(rmode, h, ct.roughness_value, dry, grav, waqua) * m.length[f];
+                w = double(pow(F(section), F(1.5)) *
+                           exterior_chezy<F>(rmode, F(h), F(ct.roughness_value), F(dry), F(grav), waqua)) * m.length[f];
         }
         b.terms[2 * (size_t)b.nslot + k] = w;
     }
@@ -430,42 +296,52 @@ __global__ void k_boundary(MeshDev m, StateDev s, BoundaryDev b, Ctrl *ctrl, int
 
 // ---------------------------------------------------------------------------
 // Cells: primitive values, limited least-squares gradients, flattening flag.
+// Depth, surface and bed stay FP64 (the stage reconstruction); gradients,
+// limiter factors and the projection run in F.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ bool feasible(double x, double y, int count, const double *ax, const double *ay,
-                                         const double *bb)
+// Roundoff scale of the arithmetic type: the reference's FP64 thresholds
+// (64 eps, 2e-14) are kept verbatim for F = double; in FP32 the same tests
+// are widened to FP32 rounding so that a projection vertex lying on its own
+// constraints is not rejected by rounding noise.
+template <class F> struct Eps { static constexpr double value = 2.2204460492503131e-16; };
+template <> struct Eps<float> { static constexpr double value = 1.1920928955078125e-07; };
+
+template <class F>
+__device__ __forceinline__ bool feasible(F x, F y, int count, const F *ax, const F *ay, const F *bb)
 {
-    for (int i = 0; i < count; ++i)
-        if (ax[i] * x + ay[i] * y > bb[i] + 2.e-14) return false;
+    for (int i = 0; i < count; ++i) {
+        F tol = F(2.e-14);
+        if (sizeof(F) != 8) tol += F(16. * Eps<F>::value) * (fabs(ax[i] * x) + fabs(ay[i] * y) + fabs(bb[i]));
+        if (ax[i] * x + ay[i] * y > bb[i] + tol) return false;
+    }
     return true;
 }
 
-__device__ __noinline__ void project_pair(double &x, double &y, int count, const double *ax, const double *ay,
-                                          const double *bb)
+template <class F>
+__device__ __noinline__ void project_pair(F &x, F &y, int count, const F *ax, const F *ay, const F *bb)
 {
-    const double rx = x, ry = y;
-    if (feasible(rx, ry, count, ax, ay, bb)) return;
-    double bx = 0., by = 0., best = rx * rx + ry * ry;
+    const F rx = x, ry = y;
+    if (feasible<F>(rx, ry, count, ax, ay, bb)) return;
+    F bx = F(0.), by = F(0.), best = rx * rx + ry * ry;
     for (int i = 0; i < count; ++i) {
-        const double dot = ax[i] * rx + ay[i] * ry - bb[i];
-        double cx = rx - dot * ax[i], cy = ry - dot * ay[i];
-        double d = (cx - rx) * (cx - rx) + (cy - ry) * (cy - ry);
-        if (d < best && feasible(cx, cy, count, ax, ay, bb)) { bx = cx; by = cy; best = d; }
+        const F dot = ax[i] * rx + ay[i] * ry - bb[i];
+        F cx = rx - dot * ax[i], cy = ry - dot * ay[i];
+        F d = (cx - rx) * (cx - rx) + (cy - ry) * (cy - ry);
+        if (d < best && feasible<F>(cx, cy, count, ax, ay, bb)) { bx = cx; by = cy; best = d; }
         for (int j = 0; j < i; ++j) {
-            const double det = ax[i] * ay[j] - ay[i] * ax[j];
-            if (fabs(det) < 1.e-12) continue;
+            const F det = ax[i] * ay[j] - ay[i] * ax[j];
+            if (fabs(det) < F(1.e-12)) continue;
             cx = (bb[i] * ay[j] - ay[i] * bb[j]) / det;
             cy = (ax[i] * bb[j] - bb[i] * ax[j]) / det;
             d = (cx - rx) * (cx - rx) + (cy - ry) * (cy - ry);
-            if (d < best && feasible(cx, cy, count, ax, ay, bb)) { bx = cx; by = cy; best = d; }
+            if (d < best && feasible<F>(cx, cy, count, ax, ay, bb)) { bx = cx; by = cy; best = d; }
         }
     }
     x = bx; y = by;
 }
 
-constexpr int MAX_CELL_FACES = 32;
-
 // MAXF bounds the faces of one cell (4 for triangle/quad meshes, 32 in general).
-template <int MAXF>
+template <class F, int MAXF>
 __global__ void __launch_bounds__(128) k_cells(MeshDev m, StateDev s, Ctrl *ctrl, Work w, int stage)
 {
     const int nc = m.nc, nf = m.nf, nadj = m.nadj;
@@ -479,14 +355,15 @@ __global__ void __launch_bounds__(128) k_cells(MeshDev m, StateDev s, Ctrl *ctrl
         if (h < 0.0 || !isfinite(h) || !isfinite(zc) || !isfinite(hu) || !isfinite(hv))
             raise_status(ct, stage, ST_SPATIAL);
         double centre[4] = {h + zc, 0., 0., zc};
-        if (h > dry) { centre[1] = hu / h; centre[2] = hv / h; }
-        double lo[4], hi[4], gx[4] = {0., 0., 0., 0.}, gy[4] = {0., 0., 0., 0.};
+        if (h > dry) { centre[1] = double(F(hu) / F(h)); centre[2] = double(F(hv) / F(h)); }
+        double lo[4], hi[4];
+        F gx[4] = {F(0.), F(0.), F(0.), F(0.)}, gy[4] = {F(0.), F(0.), F(0.), F(0.)};
 #pragma unroll
         for (int p = 0; p < 4; ++p) { lo[p] = centre[p]; hi[p] = centre[p]; }
         const int k0 = m.offset[c], k1 = m.offset[c + 1];
         // active: wet, or touching an open face or a wet neighbour
         bool active = h > dry;
-        double bx[4] = {0., 0., 0., 0.}, by[4] = {0., 0., 0., 0.};
+        F bx[4] = {F(0.), F(0.), F(0.), F(0.)}, by[4] = {F(0.), F(0.), F(0.), F(0.)};
         for (int k = k0; k < k1; ++k) {
             const int f = m.faces[k];
             const int n = m.signs[k] < 0 ? m.owner[f] : m.neighbour[f];
@@ -494,21 +371,22 @@ __global__ void __launch_bounds__(128) k_cells(MeshDev m, StateDev s, Ctrl *ctrl
             const double hn = q[n], zn = z[n];
             if (hn > dry) active = true;
             double vn[4] = {hn + zn, 0., 0., zn};
-            if (hn > dry) { vn[1] = q[nc + n] / hn; vn[2] = q[2 * nc + n] / hn; }
-            const double rx = m.ls_delta[k], ry = m.ls_delta[nadj + k], wt = m.ls_weight[k];
+            if (hn > dry) { vn[1] = double(F(q[nc + n]) / F(hn)); vn[2] = double(F(q[2 * nc + n]) / F(hn)); }
+            const F rx = F(m.ls_delta[k]), ry = F(m.ls_delta[nadj + k]), wt = F(m.ls_weight[k]);
 #pragma unroll
             for (int p = 0; p < 4; ++p) {
                 double adj = vn[p];
                 if (p == 0 && centre[0] - centre[3] > dry && vn[0] - vn[3] <= dry && vn[3] >= centre[0]) adj = centre[0];
-                bx[p] += wt * rx * (adj - centre[p]);
-                by[p] += wt * ry * (adj - centre[p]);
+                const F d = F(adj - centre[p]);
+                bx[p] += wt * rx * d;
+                by[p] += wt * ry * d;
                 lo[p] = fmin(lo[p], adj); hi[p] = fmax(hi[p], adj);
             }
         }
         if (active) {
-            const double a11 = m.ls_matrix[c], a12 = m.ls_matrix[nc + c], a22 = m.ls_matrix[2 * nc + c],
-                         det = m.ls_matrix[3 * nc + c];
-            if (a11 + a22 > 0.0) {
+            const F a11 = F(m.ls_matrix[c]), a12 = F(m.ls_matrix[nc + c]), a22 = F(m.ls_matrix[2 * nc + c]),
+                    det = F(m.ls_matrix[3 * nc + c]);
+            if (a11 + a22 > F(0.0)) {
                 if (h > dry)
                     for (int k = k0; k < k1; ++k) {
                         const int f = m.faces[k];
@@ -519,7 +397,7 @@ __global__ void __launch_bounds__(128) k_cells(MeshDev m, StateDev s, Ctrl *ctrl
                         lo[1] = fmin(lo[1], mx); hi[1] = fmax(hi[1], mx);
                         lo[2] = fmin(lo[2], my); hi[2] = fmax(hi[2], my);
                     }
-                const bool full = det > 1.e-12 * ((a11 + a22) * (a11 + a22));
+                const bool full = det > F(1.e-12) * ((a11 + a22) * (a11 + a22));
 #pragma unroll
                 for (int p = 0; p < 4; ++p) {
                     if (full) {
@@ -531,43 +409,43 @@ __global__ void __launch_bounds__(128) k_cells(MeshDev m, StateDev s, Ctrl *ctrl
                     }
                 }
                 const double hh = centre[0] - centre[3];
-                const double sq = hh > dry ? sqrt(grav * hh) : 0.;
-                const double bedtol = 64.0 * EPS * fmax(1.0, fabs(centre[3]));
-                double theta1 = 1., theta2 = 1.;
-                double ax0[2 * MAXF], ay0[2 * MAXF], b0[2 * MAXF];
-                double ax3[2 * MAXF], ay3[2 * MAXF], b3[2 * MAXF];
+                const F sq = hh > dry ? sqrt(F(grav) * F(hh)) : F(0.);
+                const F bedtol = F(64.0 * Eps<F>::value) * fmax(F(1.0), F(fabs(centre[3])));
+                F theta1 = F(1.), theta2 = F(1.);
+                F ax0[2 * MAXF], ay0[2 * MAXF], b0[2 * MAXF];
+                F ax3[2 * MAXF], ay3[2 * MAXF], b3[2 * MAXF];
                 int n0 = 0, n3 = 0;
                 for (int k = k0; k < k1; ++k) {
                     const int f = m.faces[k];
                     const int side = m.signs[k] < 0;
-                    const double rx = m.disp[side * nf + f], ry = m.disp[(2 + side) * nf + f];
+                    const F rx = F(m.disp[side * nf + f]), ry = F(m.disp[(2 + side) * nf + f]);
                     // an open stage outlet with a subcritical wet owner keeps its bed slope
                     if (m.bmode[f] == 2 && m.neighbour[f] < 0 && hh > dry &&
-                        fabs(centre[1] * m.normal[f] + centre[2] * m.normal[nf + f]) < sq &&
+                        fabs(F(centre[1]) * F(m.normal[f]) + F(centre[2]) * F(m.normal[nf + f])) < sq &&
                         fabs(gx[3] * rx + gy[3] * ry) > bedtol) continue;
 #pragma unroll
                     for (int p = 1; p < 3; ++p) {
-                        const double d = gx[p] * rx + gy[p] * ry;
-                        if (fabs(d) <= 64.0 * EPS * fmax(1.0, fmax(fabs(centre[p]), fmax(fabs(lo[p]), fabs(hi[p])))))
+                        const F d = gx[p] * rx + gy[p] * ry;
+                        if (fabs(d) <= F(64.0 * Eps<F>::value) * fmax(F(1.0), F(fmax(fabs(centre[p]), fmax(fabs(lo[p]), fabs(hi[p]))))))
                             continue;
-                        double &th = p == 1 ? theta1 : theta2;
-                        if (d > 0.) th = fmin(th, (hi[p] - centre[p]) / d);
-                        if (d < 0.) th = fmin(th, (lo[p] - centre[p]) / d);
+                        F &th = p == 1 ? theta1 : theta2;
+                        if (d > F(0.)) th = fmin(th, F(hi[p] - centre[p]) / d);
+                        if (d < F(0.)) th = fmin(th, F(lo[p] - centre[p]) / d);
                     }
-                    const double len = m.disp_len[side * nf + f];
-                    if (len <= 0.) continue;
-                    const double ux = m.disp_unit[side * nf + f], uy = m.disp_unit[(2 + side) * nf + f];
-                    ax0[n0] = ux; ay0[n0] = uy; b0[n0++] = fmax(0., hi[0] - centre[0]) / len;
-                    ax0[n0] = -ux; ay0[n0] = -uy; b0[n0++] = fmax(0., centre[0] - lo[0]) / len;
+                    const F len = F(m.disp_len[side * nf + f]);
+                    if (len <= F(0.)) continue;
+                    const F ux = F(m.disp_unit[side * nf + f]), uy = F(m.disp_unit[(2 + side) * nf + f]);
+                    ax0[n0] = ux; ay0[n0] = uy; b0[n0++] = fmax(F(0.), F(hi[0] - centre[0])) / len;
+                    ax0[n0] = -ux; ay0[n0] = -uy; b0[n0++] = fmax(F(0.), F(centre[0] - lo[0])) / len;
                     if (m.neighbour[f] < 0 && m.bid[f] < 0) continue;   // walls do not bound the bed
-                    ax3[n3] = ux; ay3[n3] = uy; b3[n3++] = fmax(0., hi[3] - centre[3]) / len;
-                    ax3[n3] = -ux; ay3[n3] = -uy; b3[n3++] = fmax(0., centre[3] - lo[3]) / len;
+                    ax3[n3] = ux; ay3[n3] = uy; b3[n3++] = fmax(F(0.), F(hi[3] - centre[3])) / len;
+                    ax3[n3] = -ux; ay3[n3] = -uy; b3[n3++] = fmax(F(0.), F(centre[3] - lo[3])) / len;
                 }
-                double px0 = gx[0], py0 = gy[0], px3 = gx[3], py3 = gy[3];
-                project_pair(px0, py0, n0, ax0, ay0, b0);
-                project_pair(px3, py3, n3, ax3, ay3, b3);
-                gx[1] *= fmax(0., theta1); gy[1] *= fmax(0., theta1);
-                gx[2] *= fmax(0., theta2); gy[2] *= fmax(0., theta2);
+                F px0 = gx[0], py0 = gy[0], px3 = gx[3], py3 = gy[3];
+                project_pair<F>(px0, py0, n0, ax0, ay0, b0);
+                project_pair<F>(px3, py3, n3, ax3, ay3, b3);
+                gx[1] *= fmax(F(0.), theta1); gy[1] *= fmax(F(0.), theta1);
+                gx[2] *= fmax(F(0.), theta2); gy[2] *= fmax(F(0.), theta2);
                 gx[0] = px0; gy[0] = py0; gx[3] = px3; gy[3] = py3;
             }
         }
@@ -576,15 +454,15 @@ __global__ void __launch_bounds__(128) k_cells(MeshDev m, StateDev s, Ctrl *ctrl
             for (int k = k0; k < k1; ++k) {
                 const int f = m.faces[k];
                 const int side = (c == m.owner[f]) ? 0 : 1;
-                const double rx = m.disp[side * nf + f], ry = m.disp[(2 + side) * nf + f];
-                const double eta = (centre[0] + gx[0] * rx) + gy[0] * ry;
-                const double zb = (centre[3] + gx[3] * rx) + gy[3] * ry;
+                const F rx = F(m.disp[side * nf + f]), ry = F(m.disp[(2 + side) * nf + f]);
+                const double eta = (centre[0] + double(gx[0] * rx)) + double(gy[0] * ry);
+                const double zb = (centre[3] + double(gx[3] * rx)) + double(gy[3] * ry);
                 if (eta - zb <= dry || fabs(zb - centre[3]) >= h) { flatten = true; break; }
             }
         CellRec r;
         r.h = h; r.eta = centre[0]; r.u = centre[1]; r.v = centre[2]; r.b = centre[3];
 #pragma unroll
-        for (int p = 0; p < 4; ++p) { r.gx[p] = gx[p]; r.gy[p] = gy[p]; }
+        for (int p = 0; p < 4; ++p) { r.gx[p] = double(gx[p]); r.gy[p] = double(gy[p]); }
         r.flags = (flatten ? 1 : 0) | (active ? 2 : 0);
         r.pad = 0; r.pad2 = 0.;
         w.rec[c] = r;
@@ -593,14 +471,20 @@ __global__ void __launch_bounds__(128) k_cells(MeshDev m, StateDev s, Ctrl *ctrl
 
 // ---------------------------------------------------------------------------
 // Faces: traces, hydrostatic reconstruction, f-wave, flux assembly.
+// Traces, the common-bed stage, pressures and the bed source are FP64; the
+// Riemann solve and the advective fluxes run in F.
 // ---------------------------------------------------------------------------
 struct Side { double h, hu, hv, b, raw; };
 
-__device__ __forceinline__ Side face_side(const CellRec &r, double rx, double ry, double dry, bool dryface,
+template <class F>
+__device__ __forceinline__ Side face_side(const CellRec &r, double rx_, double ry_, double dry, bool dryface,
                                           unsigned &bad)
 {
-    double val[4] = {(r.eta + r.gx[0] * rx) + r.gy[0] * ry, (r.u + r.gx[1] * rx) + r.gy[1] * ry,
-                     (r.v + r.gx[2] * rx) + r.gy[2] * ry, (r.b + r.gx[3] * rx) + r.gy[3] * ry};
+    const F rx = F(rx_), ry = F(ry_);
+    double val[4] = {(r.eta + double(F(r.gx[0]) * rx)) + double(F(r.gy[0]) * ry),
+                     double((F(r.u) + F(r.gx[1]) * rx) + F(r.gy[1]) * ry),
+                     double((F(r.v) + F(r.gx[2]) * rx) + F(r.gy[2]) * ry),
+                     (r.b + double(F(r.gx[3]) * rx)) + double(F(r.gy[3]) * ry)};
     const bool constant = r.flags & 1;
     if (constant) {
         val[0] = r.eta; val[1] = r.u; val[2] = r.v;
@@ -616,6 +500,7 @@ __device__ __forceinline__ Side face_side(const CellRec &r, double rx, double ry
     return o;
 }
 
+template <class F>
 __global__ void __launch_bounds__(128) k_faces(MeshDev m, StateDev s, BoundaryDev b, Ctrl *ctrl, Work w, int stage)
 {
     const int nf = m.nf, nc = m.nc;
@@ -646,9 +531,9 @@ __global__ void __launch_bounds__(128) k_faces(MeshDev m, StateDev s, BoundaryDe
         int kind = n >= 0 ? 1 : 2;
         if (rc.h <= dry && (n < 0 || rn.h <= dry)) kind = 0;
         unsigned bad = 0;
-        const Side L = face_side(rc, m.disp[f], m.disp[2 * nf + f], dry, kind == 0, bad);
+        const Side L = face_side<F>(rc, m.disp[f], m.disp[2 * nf + f], dry, kind == 0, bad);
         Side R = {0., 0., 0., 0., 0.};
-        if (n >= 0) R = face_side(rn, m.disp[nf + f], m.disp[3 * nf + f], dry, kind == 0, bad);
+        if (n >= 0) R = face_side<F>(rn, m.disp[nf + f], m.disp[3 * nf + f], dry, kind == 0, bad);
         double water = 0., speed = 0., l1 = 0., l2 = 0., r1 = 0., r2 = 0.;
         if (kind != 0) {
             double hL = L.h, xL = L.hu, yL = L.hv, bL = L.b;
@@ -690,18 +575,21 @@ __global__ void __launch_bounds__(128) k_faces(MeshDev m, StateDev s, BoundaryDe
                 if (closed) {
                     bool opens = false;
                     if (hL > dry && hR <= dry && unL / hL > 0.0) {
-                        const RType<double> t = riemann_type<double>(hL, hL, unL / hL, -unL / hL, dry, grav);
+                        const RType<F> t = riemann_type<F>(F(hL), F(hL), F(unL / hL), F(-unL / hL), F(dry), F(grav));
                         opens = t.hm > hL + dry && t.hm + bL > bR + dry;
                     } else if (hR > dry && hL <= dry && -unR / hR > 0.0) {
-                        const RType<double> t = riemann_type<double>(hR, hR, -unR / hR, unR / hR, dry, grav);
+                        const RType<F> t = riemann_type<F>(F(hR), F(hR), F(-unR / hR), F(unR / hR), F(dry), F(grav));
                         opens = t.hm > hR + dry && t.hm + bR > bL + dry;
                     }
                     closed = !opens;
                 }
             }
             double l[3] = {0., 0., 0.}, r[3] = {0., 0., 0.};
-            FWaveOut<double> fwo;
-            const int fst = fwave<double>(loc, grav, dry, fwo);
+            FWaveOut<F> fwo;
+            F locf[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) locf[j] = F(loc[j]);
+            const int fst = fwave<F>(locf, F(grav), F(dry), fwo);
             if (fst) bad = 1;
             if (closed) {
                 l[1] = 0.5 * grav * (hL * hL) * nx; l[2] = 0.5 * grav * (hL * hL) * ny;
@@ -713,19 +601,23 @@ __global__ void __launch_bounds__(128) k_faces(MeshDev m, StateDev s, BoundaryDe
                 double pl[3] = {0., 0., 0.}, pr[3] = {0., 0., 0.};
                 if (starL > dry) {
                     const double hu = loc[1], hv = loc[2];
-                    pl[0] = hu; pl[1] = (hu * hu) / starL + 0.5 * grav * (starL * starL); pl[2] = hu * hv / starL;
+                    pl[0] = hu; pl[1] = double(F(hu) * F(hu) / F(starL)) + 0.5 * grav * (starL * starL);
+                    pl[2] = double(F(hu) * F(hv) / F(starL));
                 }
                 if (starR > dry) {
                     const double hu = loc[5], hv = loc[6];
-                    pr[0] = hu; pr[1] = (hu * hu) / starR + 0.5 * grav * (starR * starR); pr[2] = hu * hv / starR;
+                    pr[0] = hu; pr[1] = double(F(hu) * F(hu) / F(starR)) + 0.5 * grav * (starR * starR);
+                    pr[2] = double(F(hu) * F(hv) / F(starR));
                 }
 #pragma unroll
-                for (int j = 0; j < 3; ++j) { pl[j] += fwo.amdq[j]; pr[j] -= fwo.apdq[j]; }
+                for (int j = 0; j < 3; ++j) { pl[j] += double(fwo.amdq[j]); pr[j] -= double(fwo.apdq[j]); }
                 l[0] = pl[0]; l[1] = pl[1] * nx + pl[2] * (-ny); l[2] = pl[1] * ny + pl[2] * nx;
                 r[0] = pr[0]; r[1] = pr[1] * nx + pr[2] * (-ny); r[2] = pr[1] * ny + pr[2] * nx;
-                if (fabs(l[0] - r[0]) > 1.e-10 * fmax(1.0, fmax(fabs(l[0]), fabs(r[0])))) bad = 1;
+                // left/right mass fluxes agree to the Riemann solve's precision (1e-10 in FP64)
+                const double consistency = sizeof(F) == 8 ? 1.e-10 : 2.e-5;
+                if (fabs(l[0] - r[0]) > consistency * fmax(1.0, fmax(fabs(l[0]), fabs(r[0])))) bad = 1;
                 l[0] = 0.5 * (l[0] + r[0]); r[0] = l[0];
-                speed = fmax(fabs(fwo.s[0]), fmax(fabs(fwo.s[1]), fabs(fwo.s[2])));
+                speed = double(fmax(fabs(fwo.s[0]), fmax(fabs(fwo.s[1]), fabs(fwo.s[2]))));
                 if (kind == 1) {
                     const double cl = .5 * grav * (hL * hL - starL * starL), cr = .5 * grav * (hR * hR - starR * starR);
                     l[1] += cl * nx; l[2] += cl * ny; r[1] += cr * nx; r[2] += cr * ny;
@@ -766,43 +658,55 @@ __global__ void __launch_bounds__(128) k_faces(MeshDev m, StateDev s, BoundaryDe
 __global__ void __launch_bounds__(256) k_gather(MeshDev m, StateDev s, Ctrl *ctrl, Work w, int stage)
 {
     const int nc = m.nc;
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
-        Ctrl &ct = ctrl[m.cell_sid[c]];
-        if (skip_stage(ct, stage)) continue;
-        const double *base = stage == 1 ? s.work : s.q1;
-        const double dt = ct.trial, area = m.area[c];
-        const bool active = w.rec[c].flags & 2;
-        double sum0 = 0., sum1 = 0., sum2 = 0., out = 0., freq = 0., ext = 0., interior = 0.;
-        const bool owns_open = m.cflags[c] & 1;
-        for (int k = m.offset[c]; k < m.offset[c + 1]; ++k) {
-            const int f = m.faces[k];
-            const double len = m.length[f];
-            const double wt = len / area;
-            const double2 ws = w.ws[f];
-            const double4_32a gf = w.gf[f];
-            if (m.signs[k] > 0) { sum0 += wt * ws.x; sum1 += wt * gf.x; sum2 += wt * gf.y; }
-            else { sum0 -= wt * ws.x; sum1 -= wt * gf.z; sum2 -= wt * gf.w; }
-            const double debit = fmax(m.signs[k] * ws.x, 0.) * len;
-            out += debit;
-            if (owns_open) { if (m.bslot[f] >= 0) ext += debit; else interior += debit; }
-            freq += len * ws.y;
+    const int stride = gridDim.x * blockDim.x;
+    // warp-uniform trip count: every lane reaches the warp reduction below
+    for (int first = blockIdx.x * blockDim.x; first < nc; first += stride) {
+        const int c = first + threadIdx.x;
+        bool have = false;
+        double fr = 0.;
+        int sid = 0;
+        if (c < nc) {
+            sid = m.cell_sid[c];
+            Ctrl &ct = ctrl[sid];
+            if (!skip_stage(ct, stage)) {
+                const double *base = stage == 1 ? s.work : s.q1;
+                const double dt = ct.trial, area = m.area[c];
+                const bool active = w.rec[c].flags & 2;
+                double sum0 = 0., sum1 = 0., sum2 = 0., out = 0., freq = 0., ext = 0., interior = 0.;
+                const bool owns_open = m.cflags[c] & 1;
+                for (int k = m.offset[c]; k < m.offset[c + 1]; ++k) {
+                    const int f = m.faces[k];
+                    const double len = m.length[f];
+                    const double wt = len / area;
+                    const double2 ws = w.ws[f];
+                    const double4_32a gf = w.gf[f];
+                    if (m.signs[k] > 0) { sum0 += wt * ws.x; sum1 += wt * gf.x; sum2 += wt * gf.y; }
+                    else { sum0 -= wt * ws.x; sum1 -= wt * gf.z; sum2 -= wt * gf.w; }
+                    const double debit = fmax(m.signs[k] * ws.x, 0.) * len;
+                    out += debit;
+                    if (owns_open) { if (m.bslot[f] >= 0) ext += debit; else interior += debit; }
+                    freq += len * ws.y;
+                }
+                double r0 = 0., r1 = 0., r2 = 0.;
+                if (active) { r0 = -sum0; r1 = -sum1; r2 = -sum2; }
+                w.rate[c] = r0; w.rate[nc + c] = r1; w.rate[2 * nc + c] = r2;
+                double theta = 1.;
+                if (out > 0. && dt * out >= base[c] * area)
+                    theta = fmin(1., base[c] * area / (dt * out)) * (1. - 32. * 2.2204460492503131e-16);
+                if (owns_open) {
+                    const double available = base[c] * area / dt;
+                    if (ext > available) raise_status(ct, stage, ST_BUDGET);
+                    const double factor = fmin(1., (available - ext) / fmax(interior, 1e-300)) * (1. - 32. * EPS);
+                    theta = (interior > 0. && interior >= available - ext) ? factor : 1.;
+                }
+                w.theta[c] = theta;
+                fr = freq / area;
+                if (isnan(fr)) raise_status(ct, stage, ST_FREQ);
+                else have = true;
+            }
         }
-        double r0 = 0., r1 = 0., r2 = 0.;
-        if (active) { r0 = -sum0; r1 = -sum1; r2 = -sum2; }
-        w.rate[c] = r0; w.rate[nc + c] = r1; w.rate[2 * nc + c] = r2;
-        double theta = 1.;
-        if (out > 0. && dt * out >= base[c] * area)
-            theta = fmin(1., base[c] * area / (dt * out)) * (1. - 32. * 2.2204460492503131e-16);
-        if (owns_open) {
-            const double available = base[c] * area / dt;
-            if (ext > available) raise_status(ct, stage, ST_BUDGET);
-            const double factor = fmin(1., (available - ext) / fmax(interior, 1e-300)) * (1. - 32. * EPS);
-            theta = (interior > 0. && interior >= available - ext) ? factor : 1.;
-        }
-        w.theta[c] = theta;
-        const double fr = freq / area;
-        if (isnan(fr)) raise_status(ct, stage, ST_FREQ);
-        else atomic_max_nonneg(stage == 1 ? &ct.peak1 : &ct.peak2, fr);
+        unsigned long long *peak0 = stage == 1 ? &ctrl[0].peak1 : &ctrl[0].peak2;
+        warp_max_peak(peak0, sizeof(Ctrl), sid, have, fr);
     }
 }
 
@@ -833,6 +737,7 @@ __global__ void __launch_bounds__(256) k_limit(MeshDev m, StateDev s, Ctrl *ctrl
 
 // midpoint_gather + stage combination (+ closing drag on the second stage).
 // With rate_out set, the final rate is stored there and no state is written.
+template <class F>
 __global__ void __launch_bounds__(256) k_update(MeshDev m, StateDev s, Ctrl *ctrl, Work w, int stage,
                                                 double *rate_out)
 {
@@ -864,8 +769,8 @@ __global__ void __launch_bounds__(256) k_update(MeshDev m, StateDev s, Ctrl *ctr
             double hv = .5 * s.work[2 * nc + c] + .5 * (s.q1[2 * nc + c] + dt * r2);
             if (!isfinite(h) || !isfinite(hu) || !isfinite(hv) || h < 0) raise_status(ct, 2, ST_ENDPOINT);
             if (h <= dry) { hu = 0.; hv = 0.; }
-            drag_cell(ct, .5 * dt, h, hu, hv);
-            double *qn = s.q[ct.cur ^ 1];
+            drag_cell<F>(ct, .5 * dt, h, hu, hv);
+            double *qn = ct.cur ? s.q[0] : s.q[1];
             qn[c] = h; qn[nc + c] = hu; qn[2 * nc + c] = hv;
         }
     }
@@ -938,4 +843,4 @@ __global__ void k_commit(MeshDev m, StateDev s, Ctrl *ctrl)
     }
 }
 
-}  // namespace brx
+}  // namespace BRX_NS

@@ -272,9 +272,10 @@ def gaussian_field(length, width, sigma, correlation, rng, resolution=1.0):
     every side so the periodic FFT does not correlate opposite edges. Returns
     ``(x0, y0, res, raster)`` for bilinear sampling.
     """
+    from scipy.fft import next_fast_len
     pad = 3.0 * correlation
-    nx = int(np.ceil((length + 2 * pad) / resolution)) + 1
-    ny = int(np.ceil((width + 2 * pad) / resolution)) + 1
+    nx = next_fast_len(int(np.ceil((length + 2 * pad) / resolution)) + 1, real=True)
+    ny = next_fast_len(int(np.ceil((width + 2 * pad) / resolution)) + 1, real=True)
     noise = rng.standard_normal((nx, ny))
     kx = 2 * np.pi * np.fft.fftfreq(nx, d=resolution)
     ky = 2 * np.pi * np.fft.rfftfreq(ny, d=resolution)

@@ -43,12 +43,20 @@ def _exterior_bed(mesh, z):
 
 def channel(length=2000.0, width=200.0, spacing=4.0, jitter=1.0, seed=1, sigma=0.2, corr=25.0,
             slope=1e-3, outlet_bed=-5.0, stage=3.0, discharge=400.0, manning=0.03, cfl=0.9,
-            refine=(), field_resolution=1.0):
+            refine=(), field_resolution=1.0, apron=3.0):
     """Straight channel of the 50k-cell class: jittered-grid Delaunay, sloped bed + Gaussian field.
 
     Lake at rest at ``stage``; inflow ``discharge`` (mode 6, conveyance
     weighted) at x=0, stage outlet (mode 2) at x=L. The bed datum puts the
     outlet bed at ``outlet_bed`` so a 5 m rotor is covered.
+
+    The last ``apron`` grid spacings before the outlet are a flat bed at
+    ``outlet_bed``. The reconstruction lets a subcritical stage outlet keep its
+    cell's bed slope towards the outlet face (the face is left out of the
+    limiter); on jittered triangles with a sloping bed that leaves an
+    odd-even transverse mode of the outlet cells undamped, which grows from
+    round-off within seconds even in a lake at rest. On a flat apron the bed
+    gradient there is zero and the outlet is stable.
     """
     mesh = M.channel_mesh(length, width, spacing, jitter, seed, refine)
     rng = np.random.default_rng(seed + 1000003)
@@ -57,6 +65,8 @@ def channel(length=2000.0, width=200.0, spacing=4.0, jitter=1.0, seed=1, sigma=0
     z = outlet_bed + slope * (length - x)
     if grid is not None:
         z = z + M.sample_field(grid, x, y)
+    if apron > 0:
+        z = np.where(x > length - apron * spacing, outlet_bed, z)
     z = np.ascontiguousarray(z)
     h = np.maximum(stage - z, 0.0)
     q = np.ascontiguousarray(np.stack((h, np.zeros_like(h), np.zeros_like(h))))
@@ -178,3 +188,56 @@ def case_from_arrays(arrs):
     for k in ("z", "q", "seg_mode", "stage_policy", "forcing", "exterior_bed"):
         case[k] = np.asarray(arrs[k])
     return case
+
+
+# ---------------------------------------------------------------------------
+# Batched scenarios (64 channels of mixed size)
+# ---------------------------------------------------------------------------
+
+def config4_params(count=64, seed=4):
+    """Per-scenario draws: cells ~ logU(1e4, 5e5), width ~ U(100, 400) m, Q ~ U(100, 1500) m3/s.
+
+    Channels keep the config-1 construction (jittered-grid Delaunay, 1e-3 slope
+    plus a Gaussian field, stage outlet at 3 m, conveyance inlet). The length
+    is ten widths and the grid spacing follows from the drawn cell count
+    (spacing = sqrt(2 L W / cells)), which keeps every Delaunay domain compact.
+    """
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        cells = float(np.exp(rng.uniform(np.log(1e4), np.log(5e5))))
+        width = float(rng.uniform(100.0, 400.0))
+        q = float(rng.uniform(100.0, 1500.0))
+        length = 10.0 * width
+        spacing = float(np.sqrt(2.0 * length * width / cells))
+        out.append(dict(index=i, cells=cells, width=width, length=length, spacing=spacing, discharge=q,
+                        seed=int(rng.integers(1, 2**31 - 1))))
+    return out
+
+
+def config4_case(p):
+    """One batch scenario, started in uniform flow (unit discharge Q/W along the channel).
+
+    Starting a 100 m channel from rest under its full discharge drives a
+    startup bore past 30 m/s; the batch configuration prescribes no initial
+    state, so each channel starts already carrying its discharge.
+    """
+    case = channel(length=p["length"], width=p["width"], spacing=p["spacing"], jitter=0.25 * p["spacing"],
+                   seed=p["seed"], discharge=p["discharge"], field_resolution=min(1.0, p["spacing"]))
+    q = case["q"]
+    q[1] = np.where(q[0] > 0.0, p["discharge"] / p["width"], 0.0)
+    case["name"] = f"batch_{p['index']:02d}"
+    return case
+
+
+def build_cases(params, workers=None):
+    """Build scenario cases in a spawn-context process pool (safe before any CUDA use)."""
+    import multiprocessing as mp
+    import os
+    workers = workers or min(len(params), os.cpu_count() or 1)
+    # A spawned child re-imports an unguarded __main__; never start a pool from
+    # inside a pool worker (it would respawn forever): build serially there.
+    if workers <= 1 or mp.parent_process() is not None:
+        return [config4_case(p) for p in params]
+    with mp.get_context("spawn").Pool(workers) as pool:
+        return pool.map(config4_case, params, chunksize=1)

@@ -186,11 +186,20 @@ class RiverSolver:
 
     # ------------------------------------------------------------------
     def advance(self, dt, time=None, raise_on_failure=True):
-        """Advance all active scenarios over [time, time+dt]; per-scenario diagnostics."""
+        """Advance over [time, time+dt]; per-scenario diagnostics.
+
+        dt and time may be scalars (all active scenarios) or arrays of one
+        interval per scenario (dt <= 0 leaves a scenario idle).
+        """
         self.torch.cuda.current_stream().synchronize()
-        t = float(self.time[0] if time is None else time)
         stats = (AdvanceStats * self.nscen)()
-        code = self.lib.brx_advance(self.h, float(dt), t, stats)
+        if np.ndim(dt) == 0 and (time is None or np.ndim(time) == 0):
+            t = float(self.time[0] if time is None else time)
+            code = self.lib.brx_advance(self.h, float(dt), t, stats)
+        else:
+            d = _f64(np.broadcast_to(dt, (self.nscen,)))
+            t = _f64(np.broadcast_to(self.time if time is None else time, (self.nscen,)))
+            code = self.lib.brx_advance_batch(self.h, _ptr(d), _ptr(t), stats)
         if code and (raise_on_failure or code != 4):
             check(code)
         out = []

@@ -113,6 +113,11 @@ int brx_state_bind(brx_solver *s, double *q_device, double *z_device);
  * (host), may be NULL. Returns BRX_ERR_REJECTED if any scenario failed. */
 int brx_advance(brx_solver *s, double dt, double time, brx_advance_stats *stats);
 
+/* As brx_advance with one interval per scenario: scenario i advances over
+ * [time[i], time[i] + dt[i]] (host arrays of nscen); dt[i] <= 0 leaves it
+ * idle. Scenarios keep independent clocks inside the same launches. */
+int brx_advance_batch(brx_solver *s, const double *dt, const double *time, brx_advance_stats *stats);
+
 /* One SSPRK(2,2) trial of exactly dt on every active scenario
  * (RiverExplicit._single, river_explicit.py:94-119). On acceptance the bound
  * state is replaced; status (nscen, host) gets the rejection bits (0 =
