@@ -121,9 +121,28 @@ def flush_l2(torch, buf):
     buf.fill_(1.0)            # 256 MiB write evicts the 129 MB L2
 
 
-def algorithmic_bytes(kernel, nc, nf, nadj, nslot):
-    """Compulsory unique bytes one launch of each kernel reads and writes (FP64 form)."""
+def algorithmic_bytes(kernel, nc, nf, nadj, nslot, precision="fp64"):
+    """Compulsory unique bytes one launch of each kernel reads and writes.
+
+    Every array a kernel touches counts once per element (neighbour gathers
+    that re-read a cell already counted are free), for the layout of the given
+    arithmetic form.
+    """
     i4, d8 = 4, 8
+    if precision == "mixed":
+        if kernel == "cells":    # state, bed, id, CSR, LS inverse, record out; per entry: index, geometry, weight
+            return nc * (3 * d8 + d8 + i4 + i4 + 16 + 64) + nadj * (8 + 16 + 4)
+        if kernel == "faces":    # two records (each cell once), face ids/geometry, water/speed + 4 momentum out
+            return nc * 64 + nf * (2 * i4 + i4 + i4 + 8 + 16 + 8) + nf * (8 + 16)
+        if kernel == "gather":   # id, CSR, record flags, stock, rate/theta out; per entry weight; face fluxes
+            return nc * (i4 + i4 + 4 + d8 + 3 * d8 + d8 + i4) + nadj * (i4 + d8) + nf * (8 + 16)
+        if kernel == "limit":
+            return nf * (8 + 2 * i4 + i4 + i4 + 16) + nc * (d8 + 3 * d8)
+        if kernel == "update":
+            return nc * (i4 + i4 + 3 * d8 + 6 * d8 + 3 * d8) + nadj * (i4 + d8) + nf * 16
+        if kernel == "drag":
+            return nc * (i4 + 6 * d8)
+        return 0
     if kernel == "faces":
         return nf * (2 * i4 + 2 * d8 + 4 * d8 + 2 * d8 + i4 + i4) + nc * 128 + nf * (16 + 32)
     if kernel == "cells":
@@ -266,6 +285,8 @@ def main():
         t_max, updates = float(tmax.item()), int(t[1].item())
     value = updates / t_max
 
+    state_after_timed = solver.q.cpu().numpy()       # for the accuracy check against FP64 below
+    sim_after_timed = sim_time
     # end to end through the public API with host buffers: H2D of the step's
     # input state from pinned memory, advance, D2H of the result
     q_host = torch.empty_like(solver.q, device="cpu").pin_memory()
@@ -287,13 +308,13 @@ def main():
     h2d = int(q_host.numel() * 8)
 
     # live per-kernel timing of one substep for the roofline of the dominant kernel
-    prof = solver.profile_substep(0.5 * diags[0]["hydraulic_next_substep_hint_s"], sim_time)
+    prof = solver.profile_substep(0.5 * min(d["hydraulic_next_substep_hint_s"] for d in diags), sim_time)
     per_kind = {}
     for name, ms in prof:
         per_kind.setdefault(name, []).append(ms)
     dom = max(per_kind, key=lambda k: sum(per_kind[k]))
     dom_ms = float(np.mean(per_kind[dom]))
-    dom_bytes = algorithmic_bytes(dom, nc, nf, nadj, nslot)
+    dom_bytes = algorithmic_bytes(dom, nc, nf, nadj, nslot, precision)
     peak, peak_kind = peaks()
     achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
     traffic = None
@@ -305,6 +326,7 @@ def main():
     roofline = {"bound": "hbm", "kernel": f"k_{dom}", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                 "kernel_ms": dom_ms, "kernel_share_of_substep": sum(per_kind[dom]) / total_ms,
+                "substep_kernels_ms": {k: [round(v, 4) for v in vs] for k, vs in per_kind.items()},
                 "algorithmic_bytes_per_launch": dom_bytes,
                 "step_bytes_per_cell_update": BYTES_PER_CELL_UPDATE[precision],
                 "step_achieved_gbs": value * BYTES_PER_CELL_UPDATE[precision] / 1e9}
@@ -315,7 +337,7 @@ def main():
         order = np.argsort([c["mesh"].nc for c in cases])
         pick = [int(order[0]), int(order[len(order) // 2]), int(order[-1])][:args.plain]
         p_updates, p_ms, errs = 0, 0.0, []
-        batch_state = solver.q.cpu().numpy()
+        batch_state = state_after_timed
         off = solver.packed["cell_offset"]
         nsteps = args.warmup + args.steps
         for i in pick:

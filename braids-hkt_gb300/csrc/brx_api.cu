@@ -69,6 +69,10 @@ struct brx_solver {
     int grid_c = 0, grid_f = 0;      // persistent grid sizes (cells / faces kernels)
     int grid_c256 = 0, grid_f256 = 0;
     int launches_per_substep = 0;
+    MixedGeo mx{};                   // FP32 geometry of the mixed form
+    std::vector<int2> h_cidx;        // host copy: stage-outlet flags follow brx_boundary_set
+    int2 *d_cidx = nullptr;
+    std::vector<int> h_faces_csr;
 
     template <class T> int alloc(T **p, size_t count)
     {
@@ -293,6 +297,59 @@ extern "C" int brx_solver_create(int nscen, const int *cell_offset, const int *f
         TRY(s->alloc(&s->work.lim, nf)); TRY(s->alloc(&s->work.rate, 3 * (size_t)nc));
         TRY(s->alloc(&s->work.theta, nc));
         TRY(s->alloc(&s->d_ctrl, nscen));
+        if (precision == BRX_MIXED) {
+            // FP32 geometry packed per cell, per CSR entry and per face; the LS
+            // inverse is formed in FP64 here so the sweep only multiplies.
+            std::vector<float4> cinv(nc);
+            for (int c = 0; c < nc; ++c) {
+                const double a11 = ls_matrix[c], a12 = ls_matrix[nc + c], a22 = ls_matrix[2 * (size_t)nc + c],
+                             det = ls_matrix[3 * (size_t)nc + c], tr = a11 + a22;
+                float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (tr > 0.0) {
+                    if (det > 1.e-12 * (tr * tr)) v = make_float4(float(a22 / det), float(-a12 / det), float(a11 / det), 0.f);
+                    else v = make_float4(float(a11 / (tr * tr)), float(a12 / (tr * tr)), float(a22 / (tr * tr)), 0.f);
+                }
+                cinv[c] = v;
+            }
+            std::vector<float4> cent(nadj);
+            std::vector<float> cwt(nadj);
+            std::vector<double> cw8(nadj);
+            s->h_cidx.assign(nadj, make_int2(-1, 0));
+            s->h_faces_csr.assign(faces, faces + nadj);
+            for (int c = 0; c < nc; ++c)
+                for (int k = offset[c]; k < offset[c + 1]; ++k) {
+                    const int f = faces[k];
+                    const int side = signs[k] < 0 ? 1 : 0;
+                    const int other = signs[k] < 0 ? owner[f] : neighbour[f];
+                    int flags = 0;
+                    if (bid[f] >= 0) flags |= 1;
+                    if (neighbour[f] < 0 && bid[f] < 0) flags |= 4;
+                    s->h_cidx[k] = make_int2(other, flags);
+                    cent[k] = make_float4(float(ls_delta[k]), float(ls_delta[nadj + k]),
+                                          float(displacement[side * (size_t)nf + f]),
+                                          float(displacement[(2 + side) * (size_t)nf + f]));
+                    cwt[k] = float(ls_weight[k]);
+                    cw8[k] = signs[k] * length[f] / area[c];
+                }
+            std::vector<float2> fnorm(nf), fdist(nf);
+            std::vector<float4> fdisp(nf);
+            for (int f = 0; f < nf; ++f) {
+                fnorm[f] = make_float2(float(normal[f]), float(normal[nf + f]));
+                fdist[f] = make_float2(float(distance[f]), float(distance[nf + f]));
+                fdisp[f] = make_float4(float(displacement[f]), float(displacement[2 * (size_t)nf + f]),
+                                       float(displacement[nf + f]), float(displacement[3 * (size_t)nf + f]));
+            }
+            float4 *p_cinv, *p_cent, *p_fdisp;
+            float *p_cwt;
+            double *p_cw8;
+            float2 *p_fnorm, *p_fdist;
+            TRY(s->upload(&p_cinv, cinv.data(), nc)); TRY(s->upload(&s->d_cidx, s->h_cidx.data(), nadj));
+            TRY(s->upload(&p_cent, cent.data(), nadj)); TRY(s->upload(&p_cwt, cwt.data(), nadj));
+            TRY(s->upload(&p_cw8, cw8.data(), nadj)); TRY(s->upload(&p_fnorm, fnorm.data(), nf));
+            TRY(s->upload(&p_fdisp, fdisp.data(), nf)); TRY(s->upload(&p_fdist, fdist.data(), nf));
+            s->mx.cinv = p_cinv; s->mx.cidx = s->d_cidx; s->mx.cent = p_cent; s->mx.cwt = p_cwt; s->mx.cw8 = p_cw8;
+            s->mx.fnorm = p_fnorm; s->mx.fdisp = p_fdisp; s->mx.fdist = p_fdist;
+        }
         CK(cudaMallocHost(&s->h_ctrl, sizeof(Ctrl) * nscen));
         memset(s->h_ctrl, 0, sizeof(Ctrl) * nscen);
         s->hint.assign(nscen, 0.0);
@@ -380,6 +437,15 @@ extern "C" int brx_boundary_set(brx_solver *s, const int *seg_mode, const int *s
     CK(cudaMemcpy(s->d_stage_policy_rw, stage_policy, sizeof(int) * nseg, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(s->d_ext_bed_rw, ext.data(), sizeof(double) * s->nslot, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(s->bnd.forcing, forcing, sizeof(double) * 2 * nseg, cudaMemcpyHostToDevice));
+    if (s->precision == BRX_MIXED) {
+        // entries on a stage outlet face (flag bit1) for the mixed cell sweep
+        for (size_t k = 0; k < s->h_cidx.size(); ++k) {
+            const int f = s->h_faces_csr[k];
+            s->h_cidx[k].y &= ~2;
+            if (s->h_neighbour[f] < 0 && bmode[f] == 2) s->h_cidx[k].y |= 2;
+        }
+        CK(cudaMemcpy(s->d_cidx, s->h_cidx.data(), sizeof(int2) * s->h_cidx.size(), cudaMemcpyHostToDevice));
+    }
     s->boundary_ready = true;
     return BRX_OK;
 }
@@ -455,6 +521,7 @@ static Launch make_launch(brx_solver *s, cudaStream_t st)
     L.nscen = s->nscen; L.nslot = s->nslot; L.maxdeg = s->maxdeg;
     L.grid_c = s->grid_c; L.grid_f = s->grid_f; L.grid_c256 = s->grid_c256; L.grid_f256 = s->grid_f256;
     L.stream = st;
+    L.mx = s->mx;
     return L;
 }
 
