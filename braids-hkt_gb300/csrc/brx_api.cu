@@ -359,14 +359,12 @@ extern "C" int brx_solver_create(int nscen, const int *cell_offset, const int *f
             c.grav = 9.81; c.dry = 1e-6; c.cfl = 0.9; c.speed_limit = 50.0;
             c.roughness_mode = 2; c.roughness_value = 0.03; c.max_substeps = 4096;
         }
-        // persistent grids: a multiple of the SM count, no more blocks than the work needs
-        int occ128 = 0, occ256 = 0;
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ128, k_faces<double>, 128, 0));
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ256, k_gather, 256, 0));
-        occ128 = std::max(occ128, 1); occ256 = std::max(occ256, 1);
-        auto grid = [&](int n, int block, int occ) { return std::max(1, std::min((n + block - 1) / block, s->sms * occ)); };
-        s->grid_c = grid(nc, 128, occ128); s->grid_f = grid(nf, 128, occ128);
-        s->grid_c256 = grid(nc, 256, occ256); s->grid_f256 = grid(nf, 256, occ256);
+        // grid-stride grids: up to 32 blocks per SM (more than any of these kernels keeps
+        // resident), so every kernel fills the SMs at its own occupancy and large meshes
+        // loop; small meshes get one thread per element
+        auto grid = [&](int n, int block) { return std::max(1, std::min((n + block - 1) / block, s->sms * 32)); };
+        s->grid_c = grid(nc, 128); s->grid_f = grid(nf, 128);
+        s->grid_c256 = grid(nc, 256); s->grid_f256 = grid(nf, 256);
         return BRX_OK;
     }();
     if (rc) { brx_solver_destroy(s); return rc; }

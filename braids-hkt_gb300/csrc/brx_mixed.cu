@@ -53,8 +53,11 @@ __device__ __forceinline__ bool feasible_f(float x, float y, int count, const fl
     return true;
 }
 
-// Nearest feasible point of the bound polygon (single-constraint projections
-// and pairwise vertices), as the directional projection limiter.
+// Nearest feasible point of the bound polygon, as the directional projection
+// limiter: the best feasible candidate among single-constraint projections and
+// pairwise vertices. The polygon contains the origin (all bounds are >= 0) and
+// is convex, so its nearest point is unique and lies on a constraint the
+// unlimited gradient violates: only violated constraints seed candidates.
 __device__ __noinline__ void project_f(float &x, float &y, int count, const float *ax, const float *ay,
                                        const float *bb)
 {
@@ -63,10 +66,12 @@ __device__ __noinline__ void project_f(float &x, float &y, int count, const floa
     float bx = 0.f, by = 0.f, best = rx * rx + ry * ry;
     for (int i = 0; i < count; ++i) {
         const float dot = ax[i] * rx + ay[i] * ry - bb[i];
+        if (dot <= 0.f) continue;                 // satisfied: cannot be the only active constraint
         float cx = rx - dot * ax[i], cy = ry - dot * ay[i];
         float d = (cx - rx) * (cx - rx) + (cy - ry) * (cy - ry);
         if (d < best && feasible_f(cx, cy, count, ax, ay, bb)) { bx = cx; by = cy; best = d; }
-        for (int j = 0; j < i; ++j) {
+        for (int j = 0; j < count; ++j) {
+            if (j == i) continue;
             const float det = ax[i] * ay[j] - ay[i] * ax[j];
             if (fabsf(det) < 1.e-12f) continue;
             cx = (bb[i] * ay[j] - ay[i] * bb[j]) / det;
@@ -148,9 +153,8 @@ __global__ void __launch_bounds__(128) km_cells(MeshDev m, StateDev s, Ctrl *ctr
             const float sq = wet ? sqrtf(grav * hf) : 0.f;
             const float bedtol = 64.f * FEPS * fmaxf(1.f, fabsf(float(zc)));
             float theta1 = 1.f, theta2 = 1.f;
-            float ax0[2 * MAXF], ay0[2 * MAXF], b0[2 * MAXF];
-            float ax3[2 * MAXF], ay3[2 * MAXF], b3[2 * MAXF];
-            int n0 = 0, n3 = 0;
+            // pass 1: Barth factors of u, v and feasibility of the eta / bed gradients
+            bool feas0 = true, feas3 = true;
             for (int k = k0; k < k1; ++k) {
                 const int2 id = g.cidx[k];
                 const float4 ge = g.cent[k];
@@ -173,15 +177,42 @@ __global__ void __launch_bounds__(128) km_cells(MeshDev m, StateDev s, Ctrl *ctr
                 const float len = sqrtf(rx * rx + ry * ry);
                 if (len <= 0.f) continue;
                 const float inv_len = 1.f / len, ux = rx * inv_len, uy = ry * inv_len;
-                ax0[n0] = ux; ay0[n0] = uy; b0[n0++] = fmaxf(0.f, hi[0]) * inv_len;
-                ax0[n0] = -ux; ay0[n0] = -uy; b0[n0++] = fmaxf(0.f, -lo[0]) * inv_len;
-                if (id.y & 4) continue;   // walls do not bound the bed
-                ax3[n3] = ux; ay3[n3] = uy; b3[n3++] = fmaxf(0.f, hi[3]) * inv_len;
-                ax3[n3] = -ux; ay3[n3] = -uy; b3[n3++] = fmaxf(0.f, -lo[3]) * inv_len;
+                const float e0 = ux * gx[0] + uy * gy[0];
+                const float t0 = 2.e-14f + 16.f * FEPS * (fabsf(ux * gx[0]) + fabsf(uy * gy[0]));
+                if (e0 > fmaxf(0.f, hi[0]) * inv_len + t0 + 16.f * FEPS * fmaxf(0.f, hi[0]) * inv_len ||
+                    -e0 > fmaxf(0.f, -lo[0]) * inv_len + t0 + 16.f * FEPS * fmaxf(0.f, -lo[0]) * inv_len) feas0 = false;
+                if (id.y & 4) continue;
+                const float e3 = ux * gx[3] + uy * gy[3];
+                const float t3 = 2.e-14f + 16.f * FEPS * (fabsf(ux * gx[3]) + fabsf(uy * gy[3]));
+                if (e3 > fmaxf(0.f, hi[3]) * inv_len + t3 + 16.f * FEPS * fmaxf(0.f, hi[3]) * inv_len ||
+                    -e3 > fmaxf(0.f, -lo[3]) * inv_len + t3 + 16.f * FEPS * fmaxf(0.f, -lo[3]) * inv_len) feas3 = false;
             }
             float px0 = gx[0], py0 = gy[0], px3 = gx[3], py3 = gy[3];
-            project_f(px0, py0, n0, ax0, ay0, b0);
-            project_f(px3, py3, n3, ax3, ay3, b3);
+            if (!feas0 || !feas3) {
+                // pass 2: the bound polygons, only for a gradient that leaves them
+                float ax0[2 * MAXF], ay0[2 * MAXF], b0[2 * MAXF];
+                float ax3[2 * MAXF], ay3[2 * MAXF], b3[2 * MAXF];
+                int n0 = 0, n3 = 0;
+                for (int k = k0; k < k1; ++k) {
+                    const int2 id = g.cidx[k];
+                    const float4 ge = g.cent[k];
+                    const float rx = ge.z, ry = ge.w;
+                    if ((id.y & 2) && wet) {
+                        const float2 nn = g.fnorm[m.faces[k]];
+                        if (fabsf(u * nn.x + v * nn.y) < sq && fabsf(gx[3] * rx + gy[3] * ry) > bedtol) continue;
+                    }
+                    const float len = sqrtf(rx * rx + ry * ry);
+                    if (len <= 0.f) continue;
+                    const float inv_len = 1.f / len, ux = rx * inv_len, uy = ry * inv_len;
+                    ax0[n0] = ux; ay0[n0] = uy; b0[n0++] = fmaxf(0.f, hi[0]) * inv_len;
+                    ax0[n0] = -ux; ay0[n0] = -uy; b0[n0++] = fmaxf(0.f, -lo[0]) * inv_len;
+                    if (id.y & 4) continue;   // walls do not bound the bed
+                    ax3[n3] = ux; ay3[n3] = uy; b3[n3++] = fmaxf(0.f, hi[3]) * inv_len;
+                    ax3[n3] = -ux; ay3[n3] = -uy; b3[n3++] = fmaxf(0.f, -lo[3]) * inv_len;
+                }
+                if (!feas0) project_f(px0, py0, n0, ax0, ay0, b0);
+                if (!feas3) project_f(px3, py3, n3, ax3, ay3, b3);
+            }
             gx[1] *= fmaxf(0.f, theta1); gy[1] *= fmaxf(0.f, theta1);
             gx[2] *= fmaxf(0.f, theta2); gy[2] *= fmaxf(0.f, theta2);
             gx[0] = px0; gy[0] = py0; gx[3] = px3; gy[3] = py3;
@@ -213,6 +244,7 @@ struct MxSide {
     float raw;         // raw reconstructed depth (>= 0)
     float db;          // face bed - cell bed
     float dh;          // trace depth - cell depth
+    float de;          // face surface - cell surface
 };
 
 __device__ __forceinline__ MxSide mx_side(const MxRec &r, float rx, float ry, float dry, bool dryface, unsigned &bad)
@@ -228,7 +260,7 @@ __device__ __forceinline__ MxSide mx_side(const MxRec &r, float rx, float ry, fl
         if (hf <= dry) db = 0.f;
     }
     if (!isfinite(de) || !isfinite(uu) || !isfinite(vv) || !isfinite(db)) bad = 1;
-    MxSide o = {0.f, 0.f, 0.f, 0.f, db, -hf};
+    MxSide o = {0.f, 0.f, 0.f, 0.f, db, -hf, de};
     if (dryface) return o;
     const float rel = de - db;
     const float raw = fmaxf(hf + rel, 0.f);
@@ -288,7 +320,7 @@ __global__ void __launch_bounds__(128) km_faces(MeshDev m, StateDev s, BoundaryD
         unsigned bad = 0;
         const float4 dsp = g.fdisp[f];
         const MxSide L = mx_side(rc, dsp.x, dsp.y, dry, kind == 0, bad);
-        MxSide R = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        MxSide R = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         const float hn = n >= 0 ? float(rn.h) : 0.f;
         if (n >= 0) R = mx_side(rn, dsp.z, dsp.w, dry, kind == 0, bad);
         float water = 0.f, speed = 0.f;
@@ -297,9 +329,14 @@ __global__ void __launch_bounds__(128) km_faces(MeshDev m, StateDev s, BoundaryD
             float hL = L.h, xL = L.hu, yL = L.hv;
             float hR = R.h, xR = R.hu, yR = R.hv;
             // beds relative to the owner's bed
+            // surfaces and beds relative to the owner's surface / bed; both sides
+            // share the owner's FP32 depth as base, so a surface at rest gives
+            // bit-identical hydrostatic depths on the two sides
             const float bLr = L.db;
             float bRr = n >= 0 ? float(rn.b - rc.b) + R.db : L.db;
-            if (kind == 2) { hR = hL; xR = xL; yR = yL; bRr = bLr; }
+            const float sL = hc + L.de;
+            float sR = n >= 0 ? hc + (float((rn.h + rn.b) - (rc.h + rc.b)) + R.de) : sL;
+            if (kind == 2) { hR = hL; xR = xL; yR = yL; bRr = bLr; sR = sL; }
             float xRr = xR, yRr = yR;
             if (kind == 2) {
                 const float dot = xL * nx + yL * ny;
@@ -312,7 +349,7 @@ __global__ void __launch_bounds__(128) km_faces(MeshDev m, StateDev s, BoundaryD
                 const float top = fmaxf(bLr, bRr);
                 const float bc = float(rc.b);
                 const float tol = 16.f * FEPS * fmaxf(dry, fmaxf(fabsf(bc + top), fmaxf(fabsf(bc + hL + bLr), fabsf(bc + hR + bRr))));
-                float hl = fmaxf(0.f, hL + (bLr - top)), hr = fmaxf(0.f, hR + (bRr - top));
+                float hl = hL > 0.f ? fmaxf(0.f, sL - top) : 0.f, hr = hR > 0.f ? fmaxf(0.f, sR - top) : 0.f;
                 if (hl <= dry + tol) hl = 0.f;
                 if (hr <= dry + tol) hr = 0.f;
                 loc[0] = hl; loc[4] = hr;
@@ -368,7 +405,10 @@ __global__ void __launch_bounds__(128) km_faces(MeshDev m, StateDev s, BoundaryD
                     // exact reflecting-wall pressure replaces the whole wall momentum flux
                     const float p = wall_pressure<float>(hL, loc[1], grav, dry);
                     dl0 = 0.f; dl1 = 0.f; dl2 = 0.f;
-                    wallx = p - half_g * hL * hL;
+                    // rounded separately: a wall at rest has p == (half_g hL) hL
+                    // bit for bit, so the difference is exactly zero (an FMA
+                    // would leave the rounding residual of p)
+                    wallx = __fsub_rn(p, __fmul_rn(__fmul_rn(half_g, hL), hL));
                     dr0 = dl0; dr1 = dl1; dr2 = dl2;
                 }
             }
