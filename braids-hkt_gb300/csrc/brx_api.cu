@@ -57,7 +57,7 @@ struct brx_solver {
     std::vector<double> hint;
     std::vector<int> active;
     std::vector<int> cell_offset, face_offset, seg_offset;
-    std::vector<int> h_bid, h_owner, h_neighbour, h_slot_face;
+    std::vector<int> h_bid, h_owner, h_neighbour, h_slot_face, h_offset;
     int *d_bmode_rw = nullptr;       // writable alias of mesh.bmode
     int *d_seg_mode_rw = nullptr, *d_stage_policy_rw = nullptr;
     double *d_ext_bed_rw = nullptr, *d_table_time = nullptr, *d_table_value = nullptr;
@@ -73,6 +73,8 @@ struct brx_solver {
     std::vector<int2> h_cidx;        // host copy: stage-outlet flags follow brx_boundary_set
     int2 *d_cidx = nullptr;
     std::vector<int> h_faces_csr;
+    std::vector<int> h_ccls;         // per cell: bit0 has a stage outlet face
+    int *d_ccls = nullptr;
 
     template <class T> int alloc(T **p, size_t count)
     {
@@ -198,6 +200,7 @@ extern "C" int brx_solver_create(int nscen, const int *cell_offset, const int *f
         s->h_bid.assign(bid, bid + nf);
         s->h_owner.assign(owner, owner + nf);
         s->h_neighbour.assign(neighbour, neighbour + nf);
+        s->h_offset.assign(offset, offset + nc + 1);
         // derived host tables
         std::vector<int> csid(nc), fsid(nf), bslot(nf, -1), cflags(nc, 0);
         for (int i = 0; i < nscen; ++i) {
@@ -312,7 +315,7 @@ extern "C" int brx_solver_create(int nscen, const int *cell_offset, const int *f
                 cinv[c] = v;
             }
             std::vector<float4> cent(nadj);
-            std::vector<float> cwt(nadj);
+            std::vector<float> cw4(nadj);
             std::vector<double> cw8(nadj);
             s->h_cidx.assign(nadj, make_int2(-1, 0));
             s->h_faces_csr.assign(faces, faces + nadj);
@@ -325,11 +328,13 @@ extern "C" int brx_solver_create(int nscen, const int *cell_offset, const int *f
                     if (bid[f] >= 0) flags |= 1;
                     if (neighbour[f] < 0 && bid[f] < 0) flags |= 4;
                     s->h_cidx[k] = make_int2(other, flags);
-                    cent[k] = make_float4(float(ls_delta[k]), float(ls_delta[nadj + k]),
+                    // LS weight times offset, rounded as the FP32 sweep would form it
+                    const float wt = float(ls_weight[k]);
+                    cent[k] = make_float4(wt * float(ls_delta[k]), wt * float(ls_delta[nadj + k]),
                                           float(displacement[side * (size_t)nf + f]),
                                           float(displacement[(2 + side) * (size_t)nf + f]));
-                    cwt[k] = float(ls_weight[k]);
                     cw8[k] = signs[k] * length[f] / area[c];
+                    cw4[k] = float(cw8[k]);
                 }
             std::vector<float2> fnorm(nf), fdist(nf);
             std::vector<float4> fdisp(nf);
@@ -340,15 +345,20 @@ extern "C" int brx_solver_create(int nscen, const int *cell_offset, const int *f
                                        float(displacement[nf + f]), float(displacement[3 * (size_t)nf + f]));
             }
             float4 *p_cinv, *p_cent, *p_fdisp;
-            float *p_cwt;
+            float *p_cw4;
             double *p_cw8;
             float2 *p_fnorm, *p_fdist;
             TRY(s->upload(&p_cinv, cinv.data(), nc)); TRY(s->upload(&s->d_cidx, s->h_cidx.data(), nadj));
-            TRY(s->upload(&p_cent, cent.data(), nadj)); TRY(s->upload(&p_cwt, cwt.data(), nadj));
+            TRY(s->upload(&p_cent, cent.data(), nadj)); TRY(s->upload(&p_cw4, cw4.data(), nadj));
             TRY(s->upload(&p_cw8, cw8.data(), nadj)); TRY(s->upload(&p_fnorm, fnorm.data(), nf));
             TRY(s->upload(&p_fdisp, fdisp.data(), nf)); TRY(s->upload(&p_fdist, fdist.data(), nf));
-            s->mx.cinv = p_cinv; s->mx.cidx = s->d_cidx; s->mx.cent = p_cent; s->mx.cwt = p_cwt; s->mx.cw8 = p_cw8;
+            s->h_ccls.assign(nc, 0);
+            TRY(s->upload(&s->d_ccls, s->h_ccls.data(), nc));
+            s->mx.cinv = p_cinv; s->mx.cidx = s->d_cidx; s->mx.cent = p_cent; s->mx.cw4 = p_cw4; s->mx.cw8 = p_cw8;
+            s->mx.ccls = s->d_ccls;
             s->mx.fnorm = p_fnorm; s->mx.fdisp = p_fdisp; s->mx.fdist = p_fdist;
+            TRY(s->alloc(&s->mx.cdb, nadj)); TRY(s->alloc(&s->mx.fdb, nf)); TRY(s->alloc(&s->mx.gbed, nc));
+            TRY(s->alloc(&s->mx.prim[0], 2 * (size_t)nc)); TRY(s->alloc(&s->mx.prim[1], 2 * (size_t)nc));
         }
         CK(cudaMallocHost(&s->h_ctrl, sizeof(Ctrl) * nscen));
         memset(s->h_ctrl, 0, sizeof(Ctrl) * nscen);
@@ -437,12 +447,15 @@ extern "C" int brx_boundary_set(brx_solver *s, const int *seg_mode, const int *s
     CK(cudaMemcpy(s->bnd.forcing, forcing, sizeof(double) * 2 * nseg, cudaMemcpyHostToDevice));
     if (s->precision == BRX_MIXED) {
         // entries on a stage outlet face (flag bit1) for the mixed cell sweep
-        for (size_t k = 0; k < s->h_cidx.size(); ++k) {
-            const int f = s->h_faces_csr[k];
-            s->h_cidx[k].y &= ~2;
-            if (s->h_neighbour[f] < 0 && bmode[f] == 2) s->h_cidx[k].y |= 2;
-        }
+        std::fill(s->h_ccls.begin(), s->h_ccls.end(), 0);
+        for (int c = 0; c < s->nc; ++c)
+            for (int k = s->h_offset[c]; k < s->h_offset[c + 1]; ++k) {
+                const int f = s->h_faces_csr[k];
+                s->h_cidx[k].y &= ~2;
+                if (s->h_neighbour[f] < 0 && bmode[f] == 2) { s->h_cidx[k].y |= 2; s->h_ccls[c] |= 1; }
+            }
         CK(cudaMemcpy(s->d_cidx, s->h_cidx.data(), sizeof(int2) * s->h_cidx.size(), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(s->d_ccls, s->h_ccls.data(), sizeof(int) * s->nc, cudaMemcpyHostToDevice));
     }
     s->boundary_ready = true;
     return BRX_OK;
@@ -589,6 +602,8 @@ static void host_set_trial(Ctrl &c)
     c.truncated = c.trial < c.hint * (1 - 1e-12);
     c.status1 = c.status2 = 0;
     c.peak1 = c.peak2 = 0ull;
+    c.gravf = float(c.grav); c.dryf = float(c.dry); c.trialf = float(c.trial);
+    c.roughf = float(c.roughness_value); c.cfl1 = 0;
 }
 
 // Per-scenario interval [time[i], time[i] + dt[i]]; dt[i] <= 0 leaves scenario i idle.
@@ -612,6 +627,13 @@ static void begin_interval(brx_solver *s, double dt, double time, bool fixed)
 {
     std::vector<double> d(s->nscen, dt), t(s->nscen, time);
     begin_interval_each(s, d.data(), t.data(), fixed);
+}
+
+// Mixed form: bed-derived tables from the bed as it is now (it may have
+// changed since the last call).
+static void refresh_bed(brx_solver *s)
+{
+    if (s->precision == BRX_MIXED) s->launches += mixed_kernel(make_launch(s, s->stream), K_BED, 0, nullptr);
 }
 
 static int ensure_ready(brx_solver *s)
@@ -663,6 +685,7 @@ static int advance_impl(brx_solver *s, const double *dt, const double *time, brx
 {
     if (s->graph_dirty || !s->graph) TRY(build_graph(s));
     begin_interval_each(s, dt, time, false);
+    refresh_bed(s);
     CK(cudaMemcpyAsync(s->d_ctrl, s->h_ctrl, sizeof(Ctrl) * s->nscen, cudaMemcpyHostToDevice, s->stream));
     // every scenario ends within max_substeps accepted + 101 rejected trials
     const int max_replays = (4096 + 102) / s->graph_chunk + 2;
@@ -702,6 +725,7 @@ extern "C" int brx_substep(brx_solver *s, double dt, double time, unsigned *stat
     TRY(ensure_ready(s));
     if (!(dt > 0) || !std::isfinite(dt)) return fail(BRX_ERR_ARGUMENT, "dt must be finite and positive");
     begin_interval(s, dt, time, true);
+    refresh_bed(s);
     for (int i = 0; i < s->nscen; ++i) s->h_ctrl[i].max_substeps = 4096;
     CK(cudaMemcpyAsync(s->d_ctrl, s->h_ctrl, sizeof(Ctrl) * s->nscen, cudaMemcpyHostToDevice, s->stream));
     // the trial without the controller: its statuses are read before control runs
@@ -738,9 +762,15 @@ extern "C" int brx_rate(brx_solver *s, double dt, double time, double *rate_devi
     begin_interval(s, dt, time, true);
     CK(cudaMemcpyAsync(s->d_ctrl, s->h_ctrl, sizeof(Ctrl) * s->nscen, cudaMemcpyHostToDevice, s->stream));
     CK(cudaMemcpyAsync(s->state.work, s->state.q[0], sizeof(double) * 3 * s->nc, cudaMemcpyDeviceToDevice, s->stream));
+    refresh_bed(s);
+    if (s->precision == BRX_MIXED) s->launches += launch_kernel(s, K_PRIM, 1, nullptr);
     enqueue_stage(s, 1, rate_device);
-    k_water_out<<<s->grid_f256, 256, 0, s->stream>>>(s->mesh, s->work, water_device);
-    s->launches++;
+    if (s->precision == BRX_MIXED) {
+        s->launches += launch_kernel(s, K_WATER, 1, water_device);
+    } else {
+        k_water_out<<<s->grid_f256, 256, 0, s->stream>>>(s->mesh, s->work, water_device);
+        s->launches++;
+    }
     CK(cudaMemcpyAsync(s->h_ctrl, s->d_ctrl, sizeof(Ctrl) * s->nscen, cudaMemcpyDeviceToHost, s->stream));
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(s->stream));
@@ -761,6 +791,7 @@ extern "C" int brx_profile_substep(brx_solver *s, double dt, double time, int ca
     if (!ms || !kind || !count || cap < 1) return fail(BRX_ERR_ARGUMENT, "null or empty profile buffers");
     if (!(dt > 0) || !std::isfinite(dt)) return fail(BRX_ERR_ARGUMENT, "dt must be finite and positive");
     begin_interval(s, dt, time, true);
+    refresh_bed(s);
     CK(cudaMemcpyAsync(s->d_ctrl, s->h_ctrl, sizeof(Ctrl) * s->nscen, cudaMemcpyHostToDevice, s->stream));
     std::vector<cudaEvent_t> ev;
     std::vector<int> kinds;

@@ -61,6 +61,9 @@ struct Ctrl {
     // diagnostics
     double min_dt, max_dt, cfl_max;
     double accepted_water_time;       // sum of accepted trial lengths (== elapsed)
+    // FP32 copies for the mixed form's sweeps, refreshed with every trial
+    float gravf, dryf, trialf, roughf;
+    int cfl1, pad1;                         // stage 1 exceeded the CFL limit (mixed form, set after its gather)
 };
 
 struct MeshDev {

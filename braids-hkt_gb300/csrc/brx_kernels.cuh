@@ -784,6 +784,8 @@ __device__ __forceinline__ void set_trial(Ctrl &c)
     c.trial = fmin(c.hint, c.dt_outer - c.elapsed);
     c.truncated = c.trial < c.hint * (1 - 1e-12);
     c.status1 = 0; c.status2 = 0; c.peak1 = 0ull; c.peak2 = 0ull;
+    c.gravf = float(c.grav); c.dryf = float(c.dry); c.trialf = float(c.trial);
+    c.roughf = float(c.roughness_value); c.cfl1 = 0;
 }
 
 __global__ void k_control(Ctrl *ctrl, int nscen)

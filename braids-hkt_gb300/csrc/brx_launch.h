@@ -6,16 +6,23 @@
 
 namespace brx {
 
-// FP32 geometry of the mixed form, packed for the sweep that reads it.
+// FP32 geometry and tables of the mixed form, packed for the sweep that reads them.
 struct MixedGeo {
     const float4 *cinv;      // (nc) inverse LS normal matrix (i11, i12, i22, 0); zero when no gradient
     const int2 *cidx;        // (nadj) other cell (-1 none), flags: bit0 open face, bit1 stage outlet, bit2 wall
-    const float4 *cent;      // (nadj) ls_delta x, y, this side's face displacement x, y
-    const float *cwt;        // (nadj) least-squares weight
-    const double *cw8;       // (nadj) signed length / area (mass bookkeeping)
+    const float4 *cent;      // (nadj) LS weight * ls_delta x, y; this side's face displacement x, y
+    const float *cw4;        // (nadj) signed length / area, FP32 (momentum, outflow and CFL sums)
+    const double *cw8;       // (nadj) signed length / area, FP64 (mass)
+    const int *ccls;         // (nc) bit0: the cell has a stage outlet face
     const float2 *fnorm;     // (nf) unit normal
     const float4 *fdisp;     // (nf) displacement owner side x, y, neighbour side x, y
     const float2 *fdist;     // (nf) |(mid - xy_owner).n|, |(xy_neighbour - mid).n|
+    // bed-derived tables, rebuilt from the FP64 bed by K_BED
+    float *cdb;              // (nadj) bed of the other cell - own bed (0 without one)
+    float *fdb;              // (nf) neighbour bed - owner bed
+    float2 *gbed;            // (nc) limited bed gradient
+    // FP32 primitives of the two stage inputs (32 bytes per cell each)
+    float4 *prim[2];
 };
 
 struct Launch {
@@ -32,10 +39,14 @@ struct Launch {
 
 // Kernel kinds of one substep, in launch order within a stage.
 enum KernelKind { K_DRAG = 0, K_BOUNDARY = 1, K_CELLS = 2, K_FACES = 3, K_GATHER = 4, K_LIMIT = 5, K_UPDATE = 6 };
+// Mixed form only: first-stage primitives of a state placed in work, the
+// bed-derived tables, the limited water flux into a caller buffer.
+enum MixedAux { K_PRIM = 8, K_BED = 9, K_WATER = 10 };
 
-// Mixed form (FP32 fluxes and updates, FP64 stage, pressure, bed source and
-// mass): launch one kernel of the given kind for the given stage. Returns the
-// number of kernels launched (0 for a boundary kernel without open faces).
-int mixed_kernel(const Launch &L, int kind, int stage, double *rate_out);
+// Mixed form (FP32 sweeps, FP64 stage pair, depth and mass): launch one kernel
+// of the given kind for the given stage; out is the rate buffer of K_UPDATE or
+// the water buffer of K_WATER. Returns the number of kernels launched (0 for a
+// boundary kernel without open faces).
+int mixed_kernel(const Launch &L, int kind, int stage, double *out);
 
 }  // namespace brx

@@ -2,22 +2,31 @@
 //
 // Same algorithm as the FP64 form (the reference's reconstruction, hydrostatic
 // reconstruction at the common face bed, augmented f-wave, flux assembly,
-// donor limiter and SSPRK(2,2) update), rearranged so that the face and cell
-// sweeps run in FP32:
+// donor limiter and SSPRK(2,2) update), rearranged for a GPU whose FP64 rate
+// is a small fraction of its FP32 rate: the cell, face and gather sweeps do
+// no FP64 arithmetic per neighbour or per face.
 //
-//   * the cell record keeps depth h and bed b in FP64 and everything else
-//     (velocities, limited gradients) in FP32, 64 bytes;
-//   * every reconstructed face value is an FP32 increment relative to its
-//     cell (surface d_eta, bed d_b, velocity); only differences of the FP64
-//     cell depths and beds are formed in FP64, once per neighbour;
-//   * the hydrostatic part of the momentum flux minus the gathering cell's
-//     own pressure is evaluated in perturbation form,
+//   * The kernels that produce a stage input (the drag half-step and the
+//     first-stage update) also write a 32-byte FP32 primitive record per cell:
+//     depth, velocities, a wet bit decided on the FP64 depth, and the FP64
+//     stage eta = h + b as an unevaluated pair of FP32 numbers (hi, lo).
+//     Differences (hi_n - hi_c) + (lo_n - lo_c) carry the FP64 stage to FP32
+//     accuracy of the difference and vanish exactly for equal stages, so the
+//     stage reconstruction keeps FP64 information at wet/dry faces.
+//   * Bed differences per CSR entry and per face, and the limited bed gradient
+//     (it depends on the bed alone, except beside a stage outlet), are tables
+//     rebuilt from the FP64 bed at the start of every call.
+//   * Every reconstructed face value is an FP32 increment relative to its
+//     cell. The hydrostatic part of the momentum flux minus the gathering
+//     cell's own pressure is evaluated in perturbation form,
 //        1/2 g [ (hL - h)(hL + h) + (h + raw) d_b ],
-//     which cancels exactly for a surface at rest in FP32 arithmetic, so the
-//     lake-at-rest balance does not rest on FP64;
-//   * the Riemann solve, limiter, projection and drag run in FP32;
-//   * mass bookkeeping (limited water flux, donor factors, the depth update)
-//     uses FP64 signed weights s*len/area, so mass telescopes exactly.
+//     with separately rounded products, which cancels exactly for a surface
+//     at rest.
+//   * The Riemann solve, limiter, projection, gather sums and drag run in
+//     FP32. The donor factor carries a margin that covers the FP32 outflow
+//     sum, so the FP64 depth update stays nonnegative.
+//   * Mass bookkeeping (limited water flux, the depth update) uses FP64
+//     signed weights s*len/area, so mass telescopes exactly.
 //
 // This unit is compiled with FMA contraction and fast FP32 division / sqrt.
 #include "brx_launch.h"
@@ -28,13 +37,23 @@ using namespace brx;
 
 constexpr float FEPS = 1.1920928955078125e-07f;
 
-// 64-byte cell record of the mixed form.
+// FP32 primitives of one stage input, one sector per cell.
+struct __align__(16) MxPrim {
+    float ehi, elo;   // eta = h + b (FP64) as ehi = fl32(eta), elo = fl32(eta - ehi)
+    float h, u, v;    // depth, velocities (0 when dry)
+    int wet;          // h > dry, decided on the FP64 depth
+    float pad0, pad1;
+};
+static_assert(sizeof(MxPrim) == 32, "primitive record is one sector");
+
+// Cell record of the face sweep, 64 bytes.
 struct __align__(16) MxRec {
-    double h, b;
+    float h;
+    int flags;                   // bit0 flatten, bit1 active, bit2 wet
+    float ehi, elo;
     float u, v;
     float gx[4], gy[4];          // eta, u, v, b
-    int flags;                   // bit0 flatten, bit1 active
-    float pad;
+    float pad0, pad1;
 };
 static_assert(sizeof(MxRec) == 64, "mixed record is half a line");
 
@@ -43,123 +62,253 @@ struct __align__(16) MxLim {
     float cx, cy;                // momentum correction
 };
 
-__device__ __forceinline__ bool feasible_f(float x, float y, int count, const float *ax, const float *ay,
-                                           const float *bb)
+__device__ __forceinline__ bool finite64(double x) { return (__double2hiint(x) & 0x7ff00000) != 0x7ff00000; }
+
+// Stage 2 skips a scenario whose first stage failed (status, or the CFL test
+// evaluated once per scenario after the first gather).
+__device__ __forceinline__ bool mx_skip(const Ctrl &c, int stage)
 {
-    for (int i = 0; i < count; ++i) {
-        const float tol = 2.e-14f + 16.f * FEPS * (fabsf(ax[i] * x) + fabsf(ay[i] * y) + fabsf(bb[i]));
-        if (ax[i] * x + ay[i] * y > bb[i] + tol) return false;
-    }
-    return true;
+    if (!c.active || c.done) return true;
+    return stage == 2 && (c.status1 != 0u || c.cfl1 != 0);
 }
 
-// Nearest feasible point of the bound polygon, as the directional projection
-// limiter: the best feasible candidate among single-constraint projections and
-// pairwise vertices. The polygon contains the origin (all bounds are >= 0) and
-// is convex, so its nearest point is unique and lies on a constraint the
-// unlimited gradient violates: only violated constraints seed candidates.
-__device__ __noinline__ void project_f(float &x, float &y, int count, const float *ax, const float *ay,
-                                       const float *bb)
+// FP32 primitives of a cell state; returns whether the state is a valid sweep input.
+__device__ __forceinline__ bool put_prim(MxPrim *P, int c, double h, double hu, double hv, double z, double dry)
+{
+    const double eta = h + z;
+    MxPrim p;
+    p.ehi = float(eta);
+    p.elo = float(eta - double(p.ehi));
+    p.h = float(h);
+    const bool wet = h > dry;
+    p.u = wet ? float(hu) / p.h : 0.f;
+    p.v = wet ? float(hv) / p.h : 0.f;
+    p.wet = wet;
+    p.pad0 = 0.f; p.pad1 = 0.f;
+    P[c] = p;
+    return !(h < 0.0) && finite64(h) && finite64(hu) && finite64(hv) && finite64(z);
+}
+
+// Per-scenario CFL peak: FP32 warp maximum, one atomic per scenario group.
+__device__ __forceinline__ void warp_max_peak_f(unsigned long long *peak_of_sid0, size_t stride_bytes, int sid,
+                                                bool valid, float v)
+{
+    const unsigned bits = valid ? __float_as_uint(v) : 0u;     // nonnegative floats order like their bits
+    const unsigned same = __match_any_sync(0xffffffffu, valid ? sid : -1);
+    const unsigned top = __reduce_max_sync(same, bits);
+    if (valid && (int)(threadIdx.x & 31) == __ffs(same) - 1) {
+        unsigned long long *addr = (unsigned long long *)((char *)peak_of_sid0 + stride_bytes * (size_t)sid);
+        atomicMax(addr, (unsigned long long)__double_as_longlong(double(__uint_as_float(top))));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Gradient bounds: the directional projection limiter on a set of slabs
+//     -bm[j] <= (ux[j], uy[j]) . g <= bp[j]      (entries j of one cell)
+// ---------------------------------------------------------------------------
+template <int N>
+struct Slabs {
+    float ux[N], uy[N], bp[N], bm[N];
+    unsigned mask;   // enabled entries
+};
+
+template <int N>
+__device__ __forceinline__ bool slabs_feasible(const Slabs<N> &S, float x, float y)
+{
+    bool ok = true;
+#pragma unroll (N <= 4 ? N : 1)
+    for (int j = 0; j < N; ++j)
+        if (S.mask >> j & 1u) {
+            const float t = S.ux[j] * x + S.uy[j] * y;
+            const float a = fabsf(S.ux[j] * x) + fabsf(S.uy[j] * y);
+            if (t > S.bp[j] + (2.e-14f + 16.f * FEPS * (a + S.bp[j]))) ok = false;
+            if (-t > S.bm[j] + (2.e-14f + 16.f * FEPS * (a + S.bm[j]))) ok = false;
+        }
+    return ok;
+}
+
+// Nearest feasible point: the best feasible candidate among single-side
+// projections and pairwise vertices. The polygon contains the origin (all
+// bounds >= 0) and is convex, so its nearest point is unique and lies on a
+// side the unlimited gradient violates: only violated sides seed candidates.
+template <int N>
+__device__ __forceinline__ void slabs_project(const Slabs<N> &S, float &x, float &y)
 {
     const float rx = x, ry = y;
-    if (feasible_f(rx, ry, count, ax, ay, bb)) return;
     float bx = 0.f, by = 0.f, best = rx * rx + ry * ry;
-    for (int i = 0; i < count; ++i) {
-        const float dot = ax[i] * rx + ay[i] * ry - bb[i];
-        if (dot <= 0.f) continue;                 // satisfied: cannot be the only active constraint
-        float cx = rx - dot * ax[i], cy = ry - dot * ay[i];
+#pragma unroll (N <= 4 ? N : 1)
+    for (int i = 0; i < N; ++i) {
+        if (!(S.mask >> i & 1u)) continue;
+        const float t = S.ux[i] * rx + S.uy[i] * ry;
+        float ax, ay, b;
+        if (t - S.bp[i] > 0.f) { ax = S.ux[i]; ay = S.uy[i]; b = S.bp[i]; }
+        else if (-t - S.bm[i] > 0.f) { ax = -S.ux[i]; ay = -S.uy[i]; b = S.bm[i]; }
+        else continue;
+        const float dot = ax * rx + ay * ry - b;
+        float cx = rx - dot * ax, cy = ry - dot * ay;
         float d = (cx - rx) * (cx - rx) + (cy - ry) * (cy - ry);
-        if (d < best && feasible_f(cx, cy, count, ax, ay, bb)) { bx = cx; by = cy; best = d; }
-        for (int j = 0; j < count; ++j) {
-            if (j == i) continue;
-            const float det = ax[i] * ay[j] - ay[i] * ax[j];
-            if (fabsf(det) < 1.e-12f) continue;
-            cx = (bb[i] * ay[j] - ay[i] * bb[j]) / det;
-            cy = (ax[i] * bb[j] - bb[i] * ax[j]) / det;
-            d = (cx - rx) * (cx - rx) + (cy - ry) * (cy - ry);
-            if (d < best && feasible_f(cx, cy, count, ax, ay, bb)) { bx = cx; by = cy; best = d; }
+        if (d < best && slabs_feasible(S, cx, cy)) { bx = cx; by = cy; best = d; }
+#pragma unroll (N <= 4 ? N : 1)
+        for (int j = 0; j < N; ++j) {
+            if (j == i || !(S.mask >> j & 1u)) continue;
+#pragma unroll
+            for (int side = 0; side < 2; ++side) {
+                const float jx = side ? -S.ux[j] : S.ux[j], jy = side ? -S.uy[j] : S.uy[j];
+                const float jb = side ? S.bm[j] : S.bp[j];
+                const float det = ax * jy - ay * jx;
+                if (fabsf(det) < 1.e-12f) continue;
+                cx = (b * jy - ay * jb) / det;
+                cy = (ax * jb - b * jx) / det;
+                d = (cx - rx) * (cx - rx) + (cy - ry) * (cy - ry);
+                if (d < best && slabs_feasible(S, cx, cy)) { bx = cx; by = cy; best = d; }
+            }
         }
     }
     x = bx; y = by;
 }
 
 // ---------------------------------------------------------------------------
-// Cells
+// Bed-derived tables (once per call: the bed may change between calls)
+// ---------------------------------------------------------------------------
+template <int MAXF>
+__global__ void __launch_bounds__(128) km_bed(MeshDev m, StateDev s, MixedGeo g)
+{
+    const int nc = m.nc, nf = m.nf, n = nc > nf ? nc : nf;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (i < nf) {
+            const int o = m.neighbour[i];
+            g.fdb[i] = o >= 0 ? float(s.z[o] - s.z[m.owner[i]]) : 0.f;
+        }
+        if (i >= nc) continue;
+        const int c = i, k0 = m.offset[c], deg = m.offset[c + 1] - k0;
+        const double zc = s.z[c];
+        float bx = 0.f, by = 0.f, lo = 0.f, hi = 0.f;
+        for (int k = k0; k < k0 + deg; ++k) {
+            const int o = g.cidx[k].x;
+            float d = 0.f;
+            if (o >= 0) {
+                d = float(s.z[o] - zc);
+                const float4 ge = g.cent[k];
+                bx += ge.x * d; by += ge.y * d;
+                lo = fminf(lo, d); hi = fmaxf(hi, d);
+            }
+            g.cdb[k] = d;
+        }
+        float2 gb = make_float2(0.f, 0.f);
+        const float4 inv = g.cinv[c];
+        if (inv.x != 0.f || inv.y != 0.f || inv.z != 0.f) {
+            float gx = inv.x * bx + inv.y * by, gy = inv.y * bx + inv.z * by;
+            Slabs<MAXF> S{};
+            const float bp = fmaxf(0.f, hi), bm = fmaxf(0.f, -lo);
+#pragma unroll (MAXF <= 4 ? MAXF : 1)
+            for (int j = 0; j < MAXF; ++j) {
+                if (j >= deg) continue;      // (a break would stop the unrolling)
+                if (g.cidx[k0 + j].y & 4) continue;          // walls do not bound the bed
+                const float4 ge = g.cent[k0 + j];
+                const float len = sqrtf(ge.z * ge.z + ge.w * ge.w);
+                if (len <= 0.f) continue;
+                const float il = 1.f / len;
+                S.ux[j] = ge.z * il; S.uy[j] = ge.w * il; S.bp[j] = bp * il; S.bm[j] = bm * il;
+                S.mask |= 1u << j;
+            }
+            if (!slabs_feasible(S, gx, gy)) slabs_project(S, gx, gy);
+            gb = make_float2(gx, gy);
+        }
+        g.gbed[c] = gb;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Cells: limited gradients and the cell record
 // ---------------------------------------------------------------------------
 template <int MAXF>
 __global__ void __launch_bounds__(128) km_cells(MeshDev m, StateDev s, Ctrl *ctrl, Work w, MixedGeo g, int stage)
 {
     const int nc = m.nc;
     MxRec *rec = reinterpret_cast<MxRec *>(w.rec);
+    const MxPrim *P = reinterpret_cast<const MxPrim *>((stage == 1 ? g.prim[0] : g.prim[1]));
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
-        Ctrl &ct = ctrl[m.cell_sid[c]];
-        if (skip_stage(ct, stage)) continue;
-        const double *q = stage == 1 ? s.work : s.q1;
-        const double dry = ct.dry;
-        const float grav = float(ct.grav);
-        const double h = q[c], hu = q[nc + c], hv = q[2 * nc + c], zc = s.z[c];
-        if (h < 0.0 || !isfinite(h) || !isfinite(zc) || !isfinite(hu) || !isfinite(hv))
-            raise_status(ct, stage, ST_SPATIAL);
-        const bool wet = h > dry;
-        const float u = wet ? float(hu) / float(h) : 0.f, v = wet ? float(hv) / float(h) : 0.f;
+        const Ctrl &ct = ctrl[m.cell_sid[c]];
+        if (mx_skip(ct, stage)) continue;
+        const float dry = ct.dryf;
+        const MxPrim pc = P[c];
+        const bool wet = pc.wet != 0;
+        const float hf = pc.h, u = pc.u, v = pc.v;
+        const bool outlet = g.ccls[c] & 1;   // a stage outlet face: the bed gradient is formed here
         // bounds of eta and b relative to the cell (centre = 0), of u and v absolute
         float lo[4] = {0.f, u, v, 0.f}, hi[4] = {0.f, u, v, 0.f};
         float bx[4] = {0.f, 0.f, 0.f, 0.f}, by[4] = {0.f, 0.f, 0.f, 0.f};
-        const int k0 = m.offset[c], k1 = m.offset[c + 1];
+        const int k0 = m.offset[c], deg = m.offset[c + 1] - k0;
         bool active = wet;
-        for (int k = k0; k < k1; ++k) {
+        for (int k = k0; k < k0 + deg; ++k) {
             const int2 id = g.cidx[k];
             const int n = id.x;
-            if (n < 0) { if (id.y & 1) active = true; continue; }
-            const double hn = q[n], zn = s.z[n];
-            const bool wetn = hn > dry;
-            if (wetn) active = true;
-            const double ddb = zn - zc;
-            float d[4];
-            d[0] = float((hn - h) + ddb);
-            d[1] = (wetn ? float(q[nc + n]) / float(hn) : 0.f) - u;
-            d[2] = (wetn ? float(q[2 * nc + n]) / float(hn) : 0.f) - v;
-            d[3] = float(ddb);
-            // a dry neighbour whose bed rises above the wet surface contributes the surface
-            if (wet && !wetn && ddb >= h) d[0] = 0.f;
-            const float4 ge = g.cent[k];
-            const float wt = g.cwt[k];
-#pragma unroll
-            for (int p = 0; p < 4; ++p) {
-                bx[p] += wt * ge.x * d[p];
-                by[p] += wt * ge.y * d[p];
-                const float val = (p == 1 || p == 2) ? d[p] + (p == 1 ? u : v) : d[p];
-                lo[p] = fminf(lo[p], val); hi[p] = fmaxf(hi[p], val);
-            }
-        }
-        float gx[4] = {0.f, 0.f, 0.f, 0.f}, gy[4] = {0.f, 0.f, 0.f, 0.f};
-        const float4 inv = g.cinv[c];
-        if (active && (inv.x != 0.f || inv.y != 0.f || inv.z != 0.f)) {
-            if (wet)
-                for (int k = k0; k < k1; ++k) {
-                    if (!(g.cidx[k].y & 4)) continue;
+            if (n < 0) {
+                if (id.y & 1) active = true;
+                else if ((id.y & 4) && wet) {
+                    // a wall bounds the velocities by the mirrored cell velocity
                     const float2 nn = g.fnorm[m.faces[k]];
                     const float un = u * nn.x + v * nn.y;
                     const float mx = u - 2.f * un * nn.x, my = v - 2.f * un * nn.y;
                     lo[1] = fminf(lo[1], mx); hi[1] = fmaxf(hi[1], mx);
                     lo[2] = fminf(lo[2], my); hi[2] = fmaxf(hi[2], my);
                 }
+                continue;
+            }
+            const MxPrim pn = P[n];
+            const bool wetn = pn.wet != 0;
+            if (wetn) active = true;
+            const float ddb = g.cdb[k];
+            float d[4];
+            d[0] = (pn.ehi - pc.ehi) + (pn.elo - pc.elo);
+            d[1] = pn.u - u;
+            d[2] = pn.v - v;
+            d[3] = ddb;
+            // a dry neighbour whose bed rises above the wet surface contributes the surface
+            if (wet && !wetn && ddb >= hf) d[0] = 0.f;
+            const float4 ge = g.cent[k];     // LS weight * (dx, dy), face displacement
 #pragma unroll
-            for (int p = 0; p < 4; ++p) {
+            for (int p = 0; p < 3; ++p) {
+                bx[p] += ge.x * d[p];
+                by[p] += ge.y * d[p];
+                const float val = (p == 1 || p == 2) ? d[p] + (p == 1 ? u : v) : d[p];
+                lo[p] = fminf(lo[p], val); hi[p] = fmaxf(hi[p], val);
+            }
+            if (outlet) {
+                bx[3] += ge.x * d[3]; by[3] += ge.y * d[3];
+                lo[3] = fminf(lo[3], d[3]); hi[3] = fmaxf(hi[3], d[3]);
+            }
+        }
+        float gx[4] = {0.f, 0.f, 0.f, 0.f}, gy[4] = {0.f, 0.f, 0.f, 0.f};
+        const float4 inv = g.cinv[c];
+        if (active && (inv.x != 0.f || inv.y != 0.f || inv.z != 0.f)) {
+#pragma unroll
+            for (int p = 0; p < 3; ++p) {
                 gx[p] = inv.x * bx[p] + inv.y * by[p];
                 gy[p] = inv.y * bx[p] + inv.z * by[p];
             }
-            const float hf = float(h);
-            const float sq = wet ? sqrtf(grav * hf) : 0.f;
-            const float bedtol = 64.f * FEPS * fmaxf(1.f, fabsf(float(zc)));
+            float bedtol = 0.f, sq = 0.f;
+            if (outlet) {
+                gx[3] = inv.x * bx[3] + inv.y * by[3];
+                gy[3] = inv.y * bx[3] + inv.z * by[3];
+                bedtol = 64.f * FEPS * fmaxf(1.f, fabsf(float(s.z[c])));
+                sq = wet ? sqrtf(ct.gravf * hf) : 0.f;
+            } else {
+                const float2 gb = g.gbed[c];
+                gx[3] = gb.x; gy[3] = gb.y;
+            }
             float theta1 = 1.f, theta2 = 1.f;
-            // pass 1: Barth factors of u, v and feasibility of the eta / bed gradients
-            bool feas0 = true, feas3 = true;
-            for (int k = k0; k < k1; ++k) {
-                const int2 id = g.cidx[k];
+            Slabs<MAXF> S0{}, S3{};
+            const float b0p = fmaxf(0.f, hi[0]), b0m = fmaxf(0.f, -lo[0]);
+            const float b3p = fmaxf(0.f, hi[3]), b3m = fmaxf(0.f, -lo[3]);
+#pragma unroll (MAXF <= 4 ? MAXF : 1)
+            for (int j = 0; j < MAXF; ++j) {
+                if (j >= deg) continue;      // (a break would stop the unrolling)
+                const int k = k0 + j;
+                const int fl = g.cidx[k].y;
                 const float4 ge = g.cent[k];
                 const float rx = ge.z, ry = ge.w;
-                if ((id.y & 2) && wet) {
+                if (outlet && (fl & 2) && wet) {
                     // an open stage outlet with a subcritical wet owner keeps its bed slope
                     const float2 nn = g.fnorm[m.faces[k]];
                     if (fabsf(u * nn.x + v * nn.y) < sq && fabsf(gx[3] * rx + gy[3] * ry) > bedtol) continue;
@@ -176,62 +325,34 @@ __global__ void __launch_bounds__(128) km_cells(MeshDev m, StateDev s, Ctrl *ctr
                 }
                 const float len = sqrtf(rx * rx + ry * ry);
                 if (len <= 0.f) continue;
-                const float inv_len = 1.f / len, ux = rx * inv_len, uy = ry * inv_len;
-                const float e0 = ux * gx[0] + uy * gy[0];
-                const float t0 = 2.e-14f + 16.f * FEPS * (fabsf(ux * gx[0]) + fabsf(uy * gy[0]));
-                if (e0 > fmaxf(0.f, hi[0]) * inv_len + t0 + 16.f * FEPS * fmaxf(0.f, hi[0]) * inv_len ||
-                    -e0 > fmaxf(0.f, -lo[0]) * inv_len + t0 + 16.f * FEPS * fmaxf(0.f, -lo[0]) * inv_len) feas0 = false;
-                if (id.y & 4) continue;
-                const float e3 = ux * gx[3] + uy * gy[3];
-                const float t3 = 2.e-14f + 16.f * FEPS * (fabsf(ux * gx[3]) + fabsf(uy * gy[3]));
-                if (e3 > fmaxf(0.f, hi[3]) * inv_len + t3 + 16.f * FEPS * fmaxf(0.f, hi[3]) * inv_len ||
-                    -e3 > fmaxf(0.f, -lo[3]) * inv_len + t3 + 16.f * FEPS * fmaxf(0.f, -lo[3]) * inv_len) feas3 = false;
-            }
-            float px0 = gx[0], py0 = gy[0], px3 = gx[3], py3 = gy[3];
-            if (!feas0 || !feas3) {
-                // pass 2: the bound polygons, only for a gradient that leaves them
-                float ax0[2 * MAXF], ay0[2 * MAXF], b0[2 * MAXF];
-                float ax3[2 * MAXF], ay3[2 * MAXF], b3[2 * MAXF];
-                int n0 = 0, n3 = 0;
-                for (int k = k0; k < k1; ++k) {
-                    const int2 id = g.cidx[k];
-                    const float4 ge = g.cent[k];
-                    const float rx = ge.z, ry = ge.w;
-                    if ((id.y & 2) && wet) {
-                        const float2 nn = g.fnorm[m.faces[k]];
-                        if (fabsf(u * nn.x + v * nn.y) < sq && fabsf(gx[3] * rx + gy[3] * ry) > bedtol) continue;
-                    }
-                    const float len = sqrtf(rx * rx + ry * ry);
-                    if (len <= 0.f) continue;
-                    const float inv_len = 1.f / len, ux = rx * inv_len, uy = ry * inv_len;
-                    ax0[n0] = ux; ay0[n0] = uy; b0[n0++] = fmaxf(0.f, hi[0]) * inv_len;
-                    ax0[n0] = -ux; ay0[n0] = -uy; b0[n0++] = fmaxf(0.f, -lo[0]) * inv_len;
-                    if (id.y & 4) continue;   // walls do not bound the bed
-                    ax3[n3] = ux; ay3[n3] = uy; b3[n3++] = fmaxf(0.f, hi[3]) * inv_len;
-                    ax3[n3] = -ux; ay3[n3] = -uy; b3[n3++] = fmaxf(0.f, -lo[3]) * inv_len;
+                const float il = 1.f / len, ux = rx * il, uy = ry * il;
+                S0.ux[j] = ux; S0.uy[j] = uy; S0.bp[j] = b0p * il; S0.bm[j] = b0m * il;
+                S0.mask |= 1u << j;
+                if (outlet && !(fl & 4)) {          // walls do not bound the bed
+                    S3.ux[j] = ux; S3.uy[j] = uy; S3.bp[j] = b3p * il; S3.bm[j] = b3m * il;
+                    S3.mask |= 1u << j;
                 }
-                if (!feas0) project_f(px0, py0, n0, ax0, ay0, b0);
-                if (!feas3) project_f(px3, py3, n3, ax3, ay3, b3);
             }
+            if (!slabs_feasible(S0, gx[0], gy[0])) slabs_project(S0, gx[0], gy[0]);
+            if (outlet && !slabs_feasible(S3, gx[3], gy[3])) slabs_project(S3, gx[3], gy[3]);
             gx[1] *= fmaxf(0.f, theta1); gy[1] *= fmaxf(0.f, theta1);
             gx[2] *= fmaxf(0.f, theta2); gy[2] *= fmaxf(0.f, theta2);
-            gx[0] = px0; gy[0] = py0; gx[3] = px3; gy[3] = py3;
         }
         bool flatten = !wet;
         if (!flatten) {
-            const float hf = float(h);
-            for (int k = k0; k < k1; ++k) {
+            for (int k = k0; k < k0 + deg; ++k) {
                 const float4 ge = g.cent[k];
                 const float de = gx[0] * ge.z + gy[0] * ge.w, db = gx[3] * ge.z + gy[3] * ge.w;
-                if (hf + (de - db) <= float(dry) || fabsf(db) >= hf) { flatten = true; break; }
+                if (hf + (de - db) <= dry || fabsf(db) >= hf) { flatten = true; break; }
             }
         }
         MxRec r;
-        r.h = h; r.b = zc; r.u = u; r.v = v;
+        r.h = hf;
+        r.flags = (flatten ? 1 : 0) | (active ? 2 : 0) | (wet ? 4 : 0);
+        r.ehi = pc.ehi; r.elo = pc.elo; r.u = u; r.v = v;
 #pragma unroll
         for (int p = 0; p < 4; ++p) { r.gx[p] = gx[p]; r.gy[p] = gy[p]; }
-        r.flags = (flatten ? 1 : 0) | (active ? 2 : 0);
-        r.pad = 0.f;
+        r.pad0 = 0.f; r.pad1 = 0.f;
         rec[c] = r;
     }
 }
@@ -253,8 +374,8 @@ __device__ __forceinline__ MxSide mx_side(const MxRec &r, float rx, float ry, fl
     float uu = r.u + (r.gx[1] * rx + r.gy[1] * ry);
     float vv = r.v + (r.gx[2] * rx + r.gy[2] * ry);
     float db = r.gx[3] * rx + r.gy[3] * ry;
-    const float hf = float(r.h);
-    const bool constant = r.flags & 1;
+    const float hf = r.h;
+    const bool constant = r.flags & 1, wet = r.flags & 4;
     if (constant) {
         de = 0.f; uu = r.u; vv = r.v;
         if (hf <= dry) db = 0.f;
@@ -266,7 +387,7 @@ __device__ __forceinline__ MxSide mx_side(const MxRec &r, float rx, float ry, fl
     const float raw = fmaxf(hf + rel, 0.f);
     o.raw = raw;
     float depth = raw;
-    if (r.h <= double(dry) || (constant && raw <= dry)) depth = 0.f;
+    if (!wet || (constant && raw <= dry)) depth = 0.f;
     o.h = depth; o.hu = depth * uu; o.hv = depth * vv;
     o.dh = (depth == hf + rel) ? rel : depth - hf;
     return o;
@@ -290,14 +411,14 @@ __global__ void __launch_bounds__(128) km_faces(MeshDev m, StateDev s, BoundaryD
     float4 *gf = reinterpret_cast<float4 *>(w.gf);
     for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += gridDim.x * blockDim.x) {
         Ctrl &ct = ctrl[m.face_sid[f]];
-        if (skip_stage(ct, stage)) continue;
-        const float dry = float(ct.dry), grav = float(ct.grav);
+        if (mx_skip(ct, stage)) continue;
+        const float dry = ct.dryf, grav = ct.gravf;
         const float half_g = 0.5f * grav;
         const int c = m.owner[f], n = m.neighbour[f];
         const float2 nn = g.fnorm[f];
         const float nx = nn.x, ny = nn.y;
         const MxRec rc = rec[c];
-        const float hc = float(rc.h);
+        const float hc = rc.h;
         const int slot = m.bslot[f];
         if (slot >= 0) {
             // open face: the exterior owner's flux and the owner/exterior CFL speed (FP64, few faces)
@@ -315,27 +436,27 @@ __global__ void __launch_bounds__(128) km_faces(MeshDev m, StateDev s, BoundaryD
         }
         MxRec rn;
         if (n >= 0) rn = rec[n];
+        const bool wc = rc.flags & 4, wn = n >= 0 && (rn.flags & 4);
         int kind = n >= 0 ? 1 : 2;
-        if (rc.h <= double(dry) && (n < 0 || rn.h <= double(dry))) kind = 0;
+        if (!wc && !wn) kind = 0;
         unsigned bad = 0;
         const float4 dsp = g.fdisp[f];
         const MxSide L = mx_side(rc, dsp.x, dsp.y, dry, kind == 0, bad);
         MxSide R = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        const float hn = n >= 0 ? float(rn.h) : 0.f;
+        const float hn = n >= 0 ? rn.h : 0.f;
         if (n >= 0) R = mx_side(rn, dsp.z, dsp.w, dry, kind == 0, bad);
         float water = 0.f, speed = 0.f;
         float gl1 = 0.f, gl2 = 0.f, gr1 = 0.f, gr2 = 0.f;
         if (kind != 0) {
             float hL = L.h, xL = L.hu, yL = L.hv;
             float hR = R.h, xR = R.hu, yR = R.hv;
-            // beds relative to the owner's bed
             // surfaces and beds relative to the owner's surface / bed; both sides
-            // share the owner's FP32 depth as base, so a surface at rest gives
+            // share the owner's depth as base, so a surface at rest gives
             // bit-identical hydrostatic depths on the two sides
             const float bLr = L.db;
-            float bRr = n >= 0 ? float(rn.b - rc.b) + R.db : L.db;
+            float bRr = n >= 0 ? g.fdb[f] + R.db : L.db;
             const float sL = hc + L.de;
-            float sR = n >= 0 ? hc + (float((rn.h + rn.b) - (rc.h + rc.b)) + R.de) : sL;
+            float sR = n >= 0 ? hc + (((rn.ehi - rc.ehi) + (rn.elo - rc.elo)) + R.de) : sL;
             if (kind == 2) { hR = hL; xR = xL; yR = yL; bRr = bLr; sR = sL; }
             float xRr = xR, yRr = yR;
             if (kind == 2) {
@@ -347,7 +468,7 @@ __global__ void __launch_bounds__(128) km_faces(MeshDev m, StateDev s, BoundaryD
             float loc[8] = {hL, unL, utL, 0.f, hR, unR, utR, 0.f};
             if (kind == 1) {
                 const float top = fmaxf(bLr, bRr);
-                const float bc = float(rc.b);
+                const float bc = rc.ehi - hc;      // the owner's bed, as a tolerance scale
                 const float tol = 16.f * FEPS * fmaxf(dry, fmaxf(fabsf(bc + top), fmaxf(fabsf(bc + hL + bLr), fabsf(bc + hR + bRr))));
                 float hl = hL > 0.f ? fmaxf(0.f, sL - top) : 0.f, hr = hR > 0.f ? fmaxf(0.f, sR - top) : 0.f;
                 if (hl <= dry + tol) hl = 0.f;
@@ -361,14 +482,16 @@ __global__ void __launch_bounds__(128) km_faces(MeshDev m, StateDev s, BoundaryD
             bool closed = false;
             if (kind == 1 && !(fminf(hc, hn) > dry)) {
                 // wet/dry face: the shared surface from distance-weighted cell stages (FP64, rare)
+                const double *q = stage == 1 ? s.work : s.q1;
+                const double zc = s.z[c], zn = s.z[n], hcd = q[c], hnd = q[n];
                 const float2 di = g.fdist[f];
                 const double dc = di.x, dn = di.y;
                 double shared;
                 if (dc + dn > 0.0)
-                    shared = (dn * (rc.b + rc.h) + dc * (rn.b + rn.h)) / (dc + dn) - fmax(rc.b, rn.b);
+                    shared = (dn * (zc + hcd) + dc * (zn + hnd)) / (dc + dn) - fmax(zc, zn);
                 else
-                    shared = 0.5 * ((rc.b + rc.h) + (rn.b + rn.h)) - fmax(rc.b, rn.b);
-                closed = shared <= double(dry);
+                    shared = 0.5 * ((zc + hcd) + (zn + hnd)) - fmax(zc, zn);
+                closed = shared <= ct.dry;
                 if (closed) {
                     bool opens = false;
                     if (hL > dry && hR <= dry && unL / hL > 0.f) {
@@ -439,93 +562,105 @@ __global__ void __launch_bounds__(128) km_faces(MeshDev m, StateDev s, BoundaryD
 }
 
 // ---------------------------------------------------------------------------
-// Gather: rate, donor factor, CFL frequency (rate form, FP64 mass)
+// Gather: momentum rate, donor factor, CFL frequency (FP32 sums)
 // ---------------------------------------------------------------------------
+// Margin of the donor factor over the FP32 outflow sum: a sum of m products
+// of rounded weights carries a relative error below (m + 2) eps32, and cells
+// have at most MAX_CELL_FACES faces.
+constexpr double DONOR_MARGIN = 64.0 * (double)FEPS;
+
 __global__ void __launch_bounds__(256) km_gather(MeshDev m, StateDev s, Ctrl *ctrl, Work w, MixedGeo g, int stage)
 {
     const int nc = m.nc;
     const float2 *ws = reinterpret_cast<const float2 *>(w.ws);
     const float4 *gf = reinterpret_cast<const float4 *>(w.gf);
     const MxRec *rec = reinterpret_cast<const MxRec *>(w.rec);
+    float *rate32 = reinterpret_cast<float *>(w.rate);      // (2, nc) momentum rates
+    float *theta32 = reinterpret_cast<float *>(w.theta);
     const int stride = gridDim.x * blockDim.x;
     for (int first = blockIdx.x * blockDim.x; first < nc; first += stride) {
         const int c = first + threadIdx.x;
         bool have = false;
-        double fr = 0.;
+        float fr = 0.f;
         int sid = 0;
         if (c < nc) {
             sid = m.cell_sid[c];
             Ctrl &ct = ctrl[sid];
-            if (!skip_stage(ct, stage)) {
-                const double *base = stage == 1 ? s.work : s.q1;
-                const double dt = ct.trial;
-                const bool active = rec[c].flags & 2;
+            if (!mx_skip(ct, stage)) {
+                const float2 hf = *reinterpret_cast<const float2 *>(&rec[c]);   // depth, flags
+                const bool active = __float_as_int(hf.y) & 2;
                 const bool owns_open = m.cflags[c] & 1;
-                double sum0 = 0., out = 0., ext = 0., interior = 0.;
-                float sum1 = 0.f, sum2 = 0.f, freq = 0.f;
+                float out = 0.f, ext = 0.f, interior = 0.f, sum1 = 0.f, sum2 = 0.f, freq = 0.f;
                 for (int k = m.offset[c]; k < m.offset[c + 1]; ++k) {
                     const int f = m.faces[k];
-                    const double wk = g.cw8[k];            // s * len / area
+                    const float wk = g.cw4[k];            // s * len / area
                     const float2 wsf = ws[f];
                     const float4 gff = gf[f];
-                    const double flow = wk * double(wsf.x);   // outward water rate of this cell
-                    sum0 += flow;
-                    if (wk > 0.) { sum1 += float(wk) * gff.x; sum2 += float(wk) * gff.y; }
-                    else { sum1 += float(wk) * gff.z; sum2 += float(wk) * gff.w; }
-                    const double debit = fmax(flow, 0.);
+                    const float debit = fmaxf(wk * wsf.x, 0.f);   // outward water rate of this cell
+                    if (wk > 0.f) { sum1 += wk * gff.x; sum2 += wk * gff.y; }
+                    else { sum1 += wk * gff.z; sum2 += wk * gff.w; }
                     out += debit;
                     if (owns_open) { if (m.bslot[f] >= 0) ext += debit; else interior += debit; }
-                    freq += fabsf(float(wk)) * wsf.y;
+                    freq += fabsf(wk) * wsf.y;
                 }
-                double r0 = 0.;
-                float r1 = 0.f, r2 = 0.f;
-                if (active) { r0 = -sum0; r1 = -sum1; r2 = -sum2; }
-                w.rate[c] = r0; w.rate[nc + c] = r1; w.rate[2 * nc + c] = r2;
-                const double hb = base[c];
-                double theta = 1.;
-                if (out > 0. && dt * out >= hb) theta = fmin(1., hb / (dt * out)) * (1. - 32. * EPS);
+                rate32[c] = active ? -sum1 : 0.f;
+                rate32[nc + c] = active ? -sum2 : 0.f;
+                float theta = 1.f;
+                // donor factor: an FP32 test that is conservative, the value in FP64
+                if (out > 0.f && ct.trialf * out >= 0.999f * hf.x) {
+                    const double hb = (stage == 1 ? s.work : s.q1)[c];
+                    const double cap = ct.trial * double(out) * (1. + DONOR_MARGIN);
+                    if (cap >= hb) theta = float(fmin(1., hb / cap) * (1. - 32. * EPS));
+                }
                 if (owns_open) {
-                    const double available = hb / dt;
-                    if (ext > available) raise_status(ct, stage, ST_BUDGET);
-                    const double factor = fmin(1., (available - ext) / fmax(interior, 1e-300)) * (1. - 32. * EPS);
-                    theta = (interior > 0. && interior >= available - ext) ? factor : 1.;
+                    const double hb = (stage == 1 ? s.work : s.q1)[c];
+                    const double available = hb / ct.trial;
+                    const double e = double(ext), e_hi = e * (1. + DONOR_MARGIN);
+                    const double in_hi = double(interior) * (1. + DONOR_MARGIN);
+                    if (e > available) raise_status(ct, stage, ST_BUDGET);
+                    const double factor = fmin(1., (available - e_hi) / fmax(in_hi, 1e-300)) * (1. - 32. * EPS);
+                    theta = (interior > 0.f && in_hi >= available - e_hi) ? float(fmax(factor, 0.)) : 1.f;
                 }
-                w.theta[c] = theta;
-                fr = double(freq);
+                theta32[c] = theta;
+                fr = freq;
                 if (isnan(fr)) raise_status(ct, stage, ST_FREQ);
                 else have = true;
             }
         }
         unsigned long long *peak0 = stage == 1 ? &ctrl[0].peak1 : &ctrl[0].peak2;
-        warp_max_peak(peak0, sizeof(Ctrl), sid, have, fr);
+        warp_max_peak_f(peak0, sizeof(Ctrl), sid, have, fr);
     }
 }
 
-// Donor-limited water flux (FP64) and the momentum it carries.
-__global__ void __launch_bounds__(256) km_limit(MeshDev m, StateDev s, Ctrl *ctrl, Work w, int stage)
+// Donor-limited water flux (FP64) and the momentum it carries. After the
+// first gather, block 0 also evaluates each scenario's first-stage CFL test.
+__global__ void __launch_bounds__(256) km_limit(MeshDev m, Ctrl *ctrl, Work w, MixedGeo g, int stage)
 {
-    const int nf = m.nf, nc = m.nc;
+    const int nf = m.nf;
+    if (stage == 1 && blockIdx.x == 0)
+        for (int i = threadIdx.x; i < m.nscen; i += blockDim.x) {
+            Ctrl &c = ctrl[i];
+            c.cfl1 = c.trial * bits_to_double(c.peak1) > c.cfl * (1 + 1e-12);
+        }
     const float2 *ws = reinterpret_cast<const float2 *>(w.ws);
+    const float *theta32 = reinterpret_cast<const float *>(w.theta);
+    const MxPrim *P = reinterpret_cast<const MxPrim *>((stage == 1 ? g.prim[0] : g.prim[1]));
     MxLim *lim = reinterpret_cast<MxLim *>(w.lim);
     for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += gridDim.x * blockDim.x) {
         const Ctrl &ct = ctrl[m.face_sid[f]];
-        if (skip_stage(ct, stage)) continue;
-        const double *q = stage == 1 ? s.work : s.q1;
-        double water = double(ws[f].x);
+        if (mx_skip(ct, stage)) continue;
+        const float wf = ws[f].x;
+        double water = double(wf);
         float cx = 0.f, cy = 0.f;
-        if (water != 0. && m.bslot[f] < 0) {
-            const int donor = water < 0. ? m.neighbour[f] : m.owner[f];
+        if (wf != 0.f && m.bslot[f] < 0) {
+            const int donor = wf < 0.f ? m.neighbour[f] : m.owner[f];
             if (donor >= 0) {
-                const double th = w.theta[donor];
-                if (th != 1.) {
-                    const double delta = (th - 1.) * water;
-                    water *= th;
-                    const double hd = q[donor];
-                    if (hd > ct.dry) {
-                        const float inv = 1.f / float(hd);
-                        cx = float(delta) * float(q[nc + donor]) * inv;
-                        cy = float(delta) * float(q[2 * nc + donor]) * inv;
-                    }
+                const float th = theta32[donor];
+                if (th != 1.f) {
+                    const float delta = (th - 1.f) * wf;
+                    water = double(wf) * double(th);          // exact product
+                    const MxPrim pd = P[donor];
+                    if (pd.wet) { cx = delta * pd.u; cy = delta * pd.v; }
                 }
             }
         }
@@ -535,18 +670,18 @@ __global__ void __launch_bounds__(256) km_limit(MeshDev m, StateDev s, Ctrl *ctr
     }
 }
 
-__device__ __forceinline__ void drag_f(const Ctrl &ct, double dt, double &h, double &hu, double &hv)
+__device__ __forceinline__ void drag_f(const Ctrl &ct, float dtf, double &h, double &hu, double &hv)
 {
     if (h <= ct.dry) { hu = 0.; hv = 0.; return; }
     const float hf = float(h), uf = float(hu), vf = float(hv);
     float c;
-    const float val = float(ct.roughness_value);
+    const float val = ct.roughf;
     if (ct.roughness_mode == 1) c = val;
     else if (ct.roughness_mode == 2) c = powf(hf, 1.f / 6.f) / val;
     else if (ct.roughness_mode == 3) c = sqrtf(9.81f) / .41f * log1pf(30.f * hf / (2.718281828459045f * val));
     else c = 18.f * log10f(12.f * fmaxf(.5f, hf / val));
     const float speed = sqrtf(uf * uf + vf * vf) / hf;
-    const float factor = 1.f / (1.f + float(dt) * float(ct.grav) * speed / (c * c * hf));
+    const float factor = 1.f / (1.f + dtf * ct.gravf * speed / (c * c * hf));
     hu *= factor;
     hv *= factor;
 }
@@ -556,52 +691,79 @@ __global__ void __launch_bounds__(256) km_update(MeshDev m, StateDev s, Ctrl *ct
 {
     const int nc = m.nc;
     const MxLim *lim = reinterpret_cast<const MxLim *>(w.lim);
+    const float *rate32 = reinterpret_cast<const float *>(w.rate);
+    MxPrim *P2 = reinterpret_cast<MxPrim *>(g.prim[1]);
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
         Ctrl &ct = ctrl[m.cell_sid[c]];
-        if (skip_stage(ct, stage)) continue;
+        if (mx_skip(ct, stage)) continue;
         double mass = 0.;
         float mx = 0.f, my = 0.f;
         for (int k = m.offset[c]; k < m.offset[c + 1]; ++k) {
             const MxLim L = lim[m.faces[k]];
-            const double wk = g.cw8[k];
-            mass -= wk * L.water;
-            mx -= float(wk) * L.cx;
-            my -= float(wk) * L.cy;
+            mass -= g.cw8[k] * L.water;
+            const float wk = g.cw4[k];
+            mx -= wk * L.cx;
+            my -= wk * L.cy;
         }
-        const double r0 = mass, r1 = w.rate[nc + c] + double(mx), r2 = w.rate[2 * nc + c] + double(my);
-        if (!isfinite(r0) || !isfinite(r1) || !isfinite(r2)) raise_status(ct, stage, ST_RATE);
-        if (rate_out) { rate_out[c] = r0; rate_out[nc + c] = r1; rate_out[2 * nc + c] = r2; continue; }
+        const float r1 = rate32[c] + mx, r2 = rate32[nc + c] + my;
+        if (!finite64(mass) || !isfinite(r1) || !isfinite(r2)) raise_status(ct, stage, ST_RATE);
+        if (rate_out) { rate_out[c] = mass; rate_out[nc + c] = double(r1); rate_out[2 * nc + c] = double(r2); continue; }
         const double dt = ct.trial, dry = ct.dry;
         if (stage == 1) {
-            const double h = s.work[c] + dt * r0;
-            double hu = s.work[nc + c] + dt * r1, hv = s.work[2 * nc + c] + dt * r2;
+            const double h = s.work[c] + dt * mass;
+            double hu = s.work[nc + c] + dt * double(r1), hv = s.work[2 * nc + c] + dt * double(r2);
             if (h < 0) raise_status(ct, 1, ST_ENDPOINT);
             if (h <= dry) { hu = 0.; hv = 0.; }
             s.q1[c] = h; s.q1[nc + c] = hu; s.q1[2 * nc + c] = hv;
+            // the second stage's input; an invalid one fails that stage
+            if (!put_prim(P2, c, h, hu, hv, s.z[c], dry) && !(h < 0)) raise_status(ct, 2, ST_SPATIAL);
         } else {
-            double h = .5 * s.work[c] + .5 * (s.q1[c] + dt * r0);
-            double hu = .5 * s.work[nc + c] + .5 * (s.q1[nc + c] + dt * r1);
-            double hv = .5 * s.work[2 * nc + c] + .5 * (s.q1[2 * nc + c] + dt * r2);
-            if (!isfinite(h) || !isfinite(hu) || !isfinite(hv) || h < 0) raise_status(ct, 2, ST_ENDPOINT);
+            double h = .5 * s.work[c] + .5 * (s.q1[c] + dt * mass);
+            double hu = .5 * s.work[nc + c] + .5 * (s.q1[nc + c] + dt * double(r1));
+            double hv = .5 * s.work[2 * nc + c] + .5 * (s.q1[2 * nc + c] + dt * double(r2));
+            if (!finite64(h) || !finite64(hu) || !finite64(hv) || h < 0) raise_status(ct, 2, ST_ENDPOINT);
             if (h <= dry) { hu = 0.; hv = 0.; }
-            drag_f(ct, .5 * dt, h, hu, hv);
+            drag_f(ct, .5f * ct.trialf, h, hu, hv);
             double *qn = ct.cur ? s.q[0] : s.q[1];
             qn[c] = h; qn[nc + c] = hu; qn[2 * nc + c] = hv;
         }
     }
 }
 
-__global__ void km_open_drag(MeshDev m, StateDev s, Ctrl *ctrl)
+// First drag half-step: work = drag(accepted, trial/2), and the first stage's primitives.
+__global__ void __launch_bounds__(256) km_open_drag(MeshDev m, StateDev s, Ctrl *ctrl, MixedGeo g)
 {
     const int nc = m.nc;
+    MxPrim *P1 = reinterpret_cast<MxPrim *>(g.prim[0]);
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
-        const Ctrl &ct = ctrl[m.cell_sid[c]];
+        Ctrl &ct = ctrl[m.cell_sid[c]];
         if (!ct.active || ct.done) continue;
         const double *q = ct.cur ? s.q[1] : s.q[0];
         double h = q[c], hu = q[nc + c], hv = q[2 * nc + c];
-        drag_f(ct, .5 * ct.trial, h, hu, hv);
+        drag_f(ct, .5f * ct.trialf, h, hu, hv);
         s.work[c] = h; s.work[nc + c] = hu; s.work[2 * nc + c] = hv;
+        if (!put_prim(P1, c, h, hu, hv, s.z[c], ct.dry)) raise_status(ct, 1, ST_SPATIAL);
     }
+}
+
+// First stage's primitives of a state placed in work directly (single residual).
+__global__ void __launch_bounds__(256) km_prim(MeshDev m, StateDev s, Ctrl *ctrl, MixedGeo g)
+{
+    const int nc = m.nc;
+    MxPrim *P1 = reinterpret_cast<MxPrim *>(g.prim[0]);
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        Ctrl &ct = ctrl[m.cell_sid[c]];
+        if (!ct.active || ct.done) continue;
+        if (!put_prim(P1, c, s.work[c], s.work[nc + c], s.work[2 * nc + c], s.z[c], ct.dry))
+            raise_status(ct, 1, ST_SPATIAL);
+    }
+}
+
+// Limited water flux of the last stage into a caller buffer.
+__global__ void km_water_out(MeshDev m, Work w, double *water)
+{
+    const MxLim *lim = reinterpret_cast<const MxLim *>(w.lim);
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < m.nf; f += gridDim.x * blockDim.x) water[f] = lim[f].water;
 }
 
 }  // namespace brx_mx
@@ -612,22 +774,21 @@ __global__ void km_open_drag(MeshDev m, StateDev s, Ctrl *ctrl)
 
 namespace brx {
 
-int mixed_kernel(const Launch &L, int kind, int stage, double *rate_out)
+int mixed_kernel(const Launch &L, int kind, int stage, double *out)
 {
     cudaStream_t st = L.stream;
+    const bool small = L.maxdeg <= 4;
     switch (kind) {
     case K_DRAG:
-        brx_mx::km_open_drag<<<L.grid_c256, 256, 0, st>>>(L.mesh, L.state, L.ctrl);
+        brx_mx::km_open_drag<<<L.grid_c256, 256, 0, st>>>(L.mesh, L.state, L.ctrl, L.mx);
         return 1;
     case K_BOUNDARY:
         if (!L.nslot) return 0;
         brx_mixb::k_boundary<float><<<L.nscen, 256, 0, st>>>(L.mesh, L.state, L.bnd, L.ctrl, stage);
         return 1;
     case K_CELLS:
-        if (L.maxdeg <= 4)
-            brx_mx::km_cells<4><<<L.grid_c, 128, 0, st>>>(L.mesh, L.state, L.ctrl, L.work, L.mx, stage);
-        else
-            brx_mx::km_cells<MAX_CELL_FACES><<<L.grid_c, 128, 0, st>>>(L.mesh, L.state, L.ctrl, L.work, L.mx, stage);
+        if (small) brx_mx::km_cells<4><<<L.grid_c, 128, 0, st>>>(L.mesh, L.state, L.ctrl, L.work, L.mx, stage);
+        else brx_mx::km_cells<MAX_CELL_FACES><<<L.grid_c, 128, 0, st>>>(L.mesh, L.state, L.ctrl, L.work, L.mx, stage);
         return 1;
     case K_FACES:
         brx_mx::km_faces<<<L.grid_f, 128, 0, st>>>(L.mesh, L.state, L.bnd, L.ctrl, L.work, L.mx, stage);
@@ -636,10 +797,22 @@ int mixed_kernel(const Launch &L, int kind, int stage, double *rate_out)
         brx_mx::km_gather<<<L.grid_c256, 256, 0, st>>>(L.mesh, L.state, L.ctrl, L.work, L.mx, stage);
         return 1;
     case K_LIMIT:
-        brx_mx::km_limit<<<L.grid_f256, 256, 0, st>>>(L.mesh, L.state, L.ctrl, L.work, stage);
+        brx_mx::km_limit<<<L.grid_f256, 256, 0, st>>>(L.mesh, L.ctrl, L.work, L.mx, stage);
         return 1;
     case K_UPDATE:
-        brx_mx::km_update<<<L.grid_c256, 256, 0, st>>>(L.mesh, L.state, L.ctrl, L.work, L.mx, stage, rate_out);
+        brx_mx::km_update<<<L.grid_c256, 256, 0, st>>>(L.mesh, L.state, L.ctrl, L.work, L.mx, stage, out);
+        return 1;
+    case K_PRIM:
+        brx_mx::km_prim<<<L.grid_c256, 256, 0, st>>>(L.mesh, L.state, L.ctrl, L.mx);
+        return 1;
+    case K_BED: {
+        const int grid = L.grid_c > L.grid_f ? L.grid_c : L.grid_f;
+        if (small) brx_mx::km_bed<4><<<grid, 128, 0, st>>>(L.mesh, L.state, L.mx);
+        else brx_mx::km_bed<MAX_CELL_FACES><<<grid, 128, 0, st>>>(L.mesh, L.state, L.mx);
+        return 1;
+    }
+    case K_WATER:
+        brx_mx::km_water_out<<<L.grid_f256, 256, 0, st>>>(L.mesh, L.work, out);
         return 1;
     }
     return 0;
