@@ -83,23 +83,52 @@ def config1(seed=1):
     return channel(seed=seed)
 
 
-def rotors_on_centreline(length, width, count, spacing, first_x, diameter=5.0, ct=0.8):
+def rotor_rows(case, centres, diameter=5.0, control=None, bed_clearance=0.5, surface_clearance=0.5, nu=0.0):
+    """Rotor dicts at the given centres with the hub fixed D/2 + bed_clearance
+    above the highest bed in each footprint (the reference's explicit fixed
+    hub elevation and clearance limits, river_turbine_flow.py:46-52)."""
+    from . import turbines as TB
+    mesh, z = case["mesh"], case["z"]
+    control = control or {"mode": "constant_ct", "thrust_coefficient": 0.8, "power_coefficient": None}
     rows = []
-    for i in range(count):
-        rows.append(dict(turbine_id=i, x=first_x + i * spacing, y=0.5 * width, D=diameter,
-                         thrust_coefficient=ct))
+    for k, (x, y) in enumerate(centres):
+        cells, _ = TB.bump_integrals(mesh, x, y, diameter)
+        hub = float(np.max(z[cells])) + bed_clearance + 0.5 * diameter + 0.25
+        rows.append(dict(name=f"T{k + 1}", X=float(x), Y=float(y), D=float(diameter), hub_elevation_m=round(hub, 3),
+                         minimum_bed_clearance_m=0.2, minimum_surface_clearance_m=float(surface_clearance),
+                         control=control, nu=float(nu)))
     return rows
 
 
-def config2(seed=2, refine_spacing=1.0):
-    """Config-1 channel with 3 tandem rotors on the centreline 150 m apart, refined wakes (about 120k cells)."""
+def config2(seed=2, refine_spacing=1.0, control=None):
+    """Config-1 channel with 3 tandem rotors on the centreline 150 m apart, refined wakes (about 120k cells).
+
+    Rotors: D = 5 m, Ct = 0.8 with Cp(U) = min(0.4, 500 kW / (1/2 rho A U^3))
+    referenced to the incident speed (rated near 5.0 m/s), hub 0.75 m above
+    D/2 over the highest bed in the footprint.
+    """
+    from . import turbines as TB
     length, width = 2000.0, 200.0
-    first = 700.0
-    rotors = rotors_on_centreline(length, width, 3, 150.0, first)
-    boxes = [(r["x"] - 10.0, r["x"] + 60.0, r["y"] - 15.0, r["y"] + 15.0, refine_spacing) for r in rotors]
+    xs = [700.0, 850.0, 1000.0]
+    boxes = [(x - 10.0, x + 60.0, 0.5 * width - 15.0, 0.5 * width + 15.0, refine_spacing) for x in xs]
     case = channel(length, width, seed=seed, refine=boxes)
-    case["turbines"] = rotors
+    control = control or TB.rated_power_curve(5.0, 0.8, 0.4, 500e3)
+    case["turbines"] = rotor_rows(case, [(x, 0.5 * width) for x in xs], control=control)
     case["name"] = "channel_3_rotors"
+    return case
+
+
+def small_rotor_channel(length=150.0, width=30.0, spacing=1.5, seed=21, discharge=150.0, rotors=2, control=None,
+                        nu=0.0, sigma=0.1, corr=6.0):
+    """A 150 m x 30 m channel resolved for 5 m rotors (about 4k cells) with
+    ``rotors`` rotors on the centreline, 40 m apart, starting in uniform flow."""
+    case = channel(length=length, width=width, spacing=spacing, jitter=0.25 * spacing, seed=seed, sigma=sigma,
+                   corr=corr, discharge=discharge, field_resolution=min(1.0, spacing))
+    q = case["q"]
+    q[1] = np.where(q[0] > 0.0, discharge / width, 0.0)
+    xs = [50.0 + 40.0 * k for k in range(rotors)]
+    case["turbines"] = rotor_rows(case, [(x, 0.5 * width) for x in xs], control=control, nu=nu)
+    case["name"] = "small_rotor_channel"
     return case
 
 

@@ -32,6 +32,12 @@
  *   CFL frequency     src/braids_core/sediment/river_explicit.h:13-26
  *   Manning drag      src/braids_core/sediment/river_hydraulic_drag.h:3-16,
  *                     river_roughness.py:42-47
+ *   turbines          src/braids_core/sediment/river_turbine_flow.py:230-239 (momentum order),
+ *                     river_turbine_flow.h:13-82 (wet gradients, surface pack, pressure),
+ *                     river_hydrokinetic_stress.h:13-35 (ambient stress),
+ *                     river_turbine_thetis.py:182-216,263-297 (cell terms, sample),
+ *                     river_turbine_flow.py:82-120 (coverage gate),
+ *                     flow2dh_fixed_bed_kernels.h:54-60 (face momentum gather)
  *
  * Scope: meshes without WENO stencils or virtual-wall triangles (the
  * generated Delaunay meshes), outlet_extension = 0, cells with at most 32
@@ -48,6 +54,7 @@
 #endif
 
 #define OM_EPS 2.2204460492503131e-16
+#define OM_PI 3.14159265358979323846
 #define OM_DBL_MIN 2.2250738585072014e-308
 
 /* Rejection kinds, mirroring the reference's BendTrialRejected reasons. */
@@ -74,6 +81,7 @@ typedef struct {
     const double *table_time;                      /* (table_len) */
     const double *table_value;                     /* (2, nb, table_len) */
     int threads;
+    const struct om_turbines *turb;                /* rotors (NULL: none) */
 } om_ctx;
 
 /* ------------------------------------------------------------------ */
@@ -1081,6 +1089,302 @@ void om_drag(const om_ctx *m, double dt, double *q)
 /* ------------------------------------------------------------------ */
 
 /* Scratch for one spatial evaluation. */
+/* ------------------------------------------------------------------ */
+/* Turbines: Thetis actuator sink, coverage gate, balanced pressure    */
+/* ------------------------------------------------------------------ */
+enum { OM_TURB_FIELDS = 16 };
+/* per-rotor parameter record (doubles): D, hub elevation, minimum bed and
+ * surface clearances, tolerance, mode, Ct, Cp (constant mode, Cp resolved) */
+enum { OM_TP_D = 0, OM_TP_HUB, OM_TP_BEDCLEAR, OM_TP_SURFCLEAR, OM_TP_TOL, OM_TP_MODE, OM_TP_CT, OM_TP_CP, OM_TP_N };
+/* control modes */
+enum { OM_CONSTANT = 0, OM_SPEED_TABLE = 1, OM_INCIDENT_TABLE = 2, OM_INCIDENT_CURVES = 3 };
+/* diagnostic record fields */
+enum { OM_TD_ACTIVE = 0, OM_TD_REASON, OM_TD_MARGIN, OM_TD_CLEARANCE, OM_TD_U1, OM_TD_U0, OM_TD_DEPTH,
+       OM_TD_CT, OM_TD_CP, OM_TD_FORCE, OM_TD_POWER, OM_TD_REMOVED, OM_TD_LOW, OM_TD_HIGH, OM_TD_ERROR };
+/* inactive reasons, in the order the gate tests them */
+enum { OM_R_COVERED = 0, OM_R_DEPTH, OM_R_BED, OM_R_SURFCLEAR, OM_R_BEDCLEAR, OM_R_DRY, OM_R_REVERSE,
+       OM_R_NOFLOW, OM_R_CUTIN };
+
+typedef struct om_turbines {
+    int nr;
+    const int *support_offset, *support_cell;          /* (nr+1), (ns) */
+    const double *support_weight, *support_density;    /* normalized bump weight, density integral */
+    const int *plane_offset, *plane_cell;              /* (nr+1), (np) */
+    const double *plane_delta;                         /* (2, np) */
+    const double *param;                               /* (nr, OM_TP_N) */
+    const int *curve;                                  /* (nr, 4): thrust first, count; power first, count */
+    const double *curve_x, *curve_y;
+    const double *nu;                                  /* (nc) ambient viscosity, NULL: none */
+    int pressure;                                      /* balanced-pressure correction on */
+    const double *dxdy, *inverse, *xy, *mdisp;         /* (2,nadj) (3,nc) (2,nc) (4,nf) */
+    double *diag;                                      /* (nr, OM_TURB_FIELDS) last evaluation */
+    double *grad, *raw, *face, *work, *trace, *kcell;  /* scratch (10,nc) (3,nc) (2,nf) (3,nc) (10,nf) (ns) */
+    int *fstatus;                                      /* (nf) */
+} om_turbines;
+
+/* Wet-only least-squares gradients of u, v, eta and the bed (river_turbine_flow.h:13-37). */
+void om_hkt_gradients(const om_ctx *m, const om_turbines *T, const double *q, const double *z, double *out)
+{
+    const int n = m->nc, na = m->nadj;
+    const double dry = m->dry;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; ++i) {
+        for (int k = 0; k < 10; ++k) out[k * n + i] = 0.;
+        double xx = 0., xy = 0., yy = 0., bx[3] = {0., 0., 0.}, by[3] = {0., 0., 0.}, bz[2] = {0., 0.};
+        const int wet = q[i] > dry;
+        for (int s = m->offset[i]; s < m->offset[i + 1]; ++s) {
+            const int j = om_other(m, s);
+            if (j < 0) continue;
+            const double dx = T->dxdy[s], dy = T->dxdy[na + s], w = 1. / (dx * dx + dy * dy), dz = z[j] - z[i];
+            bz[0] += w * dx * dz; bz[1] += w * dy * dz;
+            if (!wet || q[j] <= dry) continue;
+            xx += w * dx * dx; xy += w * dx * dy; yy += w * dy * dy;
+            const double d[3] = {q[n + j] / q[j] - q[n + i] / q[i], q[2 * n + j] / q[j] - q[2 * n + i] / q[i],
+                                 (q[j] + z[j]) - (q[i] + z[i])};
+            for (int k = 0; k < 3; ++k) { bx[k] += w * dx * d[k]; by[k] += w * dy * d[k]; }
+        }
+        out[6 * n + i] = T->inverse[i] * bz[0] + T->inverse[n + i] * bz[1];
+        out[7 * n + i] = T->inverse[n + i] * bz[0] + T->inverse[2 * n + i] * bz[1];
+        const double det = xx * yy - xy * xy;
+        if (det > 1e-12 * fmax(1., xx * yy))
+            for (int k = 0; k < 3; ++k) {
+                out[2 * k * n + i] = (yy * bx[k] - xy * by[k]) / det;
+                out[(2 * k + 1) * n + i] = (xx * by[k] - xy * bx[k]) / det;
+            }
+    }
+}
+
+/* numpy.interp on one table, zero outside [x0, xlast) (river_turbine_thetis.py:158-172) */
+static double om_lookup(const double *x, const double *y, int count, double v)
+{
+    if (!(v >= x[0]) || v >= x[count - 1]) return 0.;
+    int j = 0;
+    while (j + 1 < count - 1 && x[j + 1] <= v) ++j;
+    if (v == x[j]) return y[j];
+    const double slope = (y[j + 1] - y[j]) / (x[j + 1] - x[j]);
+    return slope * (v - x[j]) + y[j];
+}
+
+/* Per-cell Thetis terms K, P, U, Ct, Cp (river_turbine_thetis.py:175-216). Returns 0 or an error. */
+static int om_cell_terms(const om_turbines *T, int r, double depth, double u, double v, double out[5])
+{
+    const double *p = T->param + (size_t)r * OM_TP_N;
+    const double D = p[OM_TP_D];
+    const int mode = (int)p[OM_TP_MODE];
+    const int *cv = T->curve + 4 * r;
+    const double *tx = T->curve_x + cv[0], *ty = T->curve_y + cv[0], *px = T->curve_x + cv[2], *py = T->curve_y + cv[2];
+    const double speed = hypot(u, v);
+    const double area = OM_PI * (D * D) / 4;
+    if (mode == OM_INCIDENT_TABLE || mode == OM_INCIDENT_CURVES) {
+        if (depth < D * (1 - 1e-10)) return 2;
+        const double c = OM_PI * D / (4 * depth);
+        double low = tx[0], high = tx[cv[1] - 1];
+        const double smin = low * .5 * (1 + sqrt(1 - c * ty[0]));
+        const double smax = high * .5 * (1 + sqrt(1 - c * ty[cv[1] - 1]));
+        const int active = speed >= smin && speed < smax;
+        for (int it = 0; it < 44; ++it) {
+            const double mid = .5 * (low + high);
+            const double ct = om_lookup(tx, ty, cv[1], mid);
+            const double local = mid * .5 * (1 + sqrt(1 - c * ct));
+            if (local < speed) low = mid; else high = mid;
+        }
+        const double incident = active ? .5 * (low + high) : speed;
+        const double ct = active ? om_lookup(tx, ty, cv[1], incident) : 0.;
+        const double cp = active ? om_lookup(px, py, cv[3], incident) : 0.;
+        const double alpha = .5 * (1 + sqrt(1 - c * ct));
+        out[0] = area * ct / (2 * (alpha * alpha));
+        out[1] = .5 * area * cp * (incident * incident * incident);
+        out[2] = incident; out[3] = ct; out[4] = cp;
+        return 0;
+    }
+    double ct, cp;
+    if (mode == OM_CONSTANT) ct = p[OM_TP_CT];
+    else ct = om_lookup(tx, ty, cv[1], speed);
+    const double radicand = 1 - area * ct / (D * depth);
+    if (radicand < 0) return 1;
+    const double alpha = .5 * (1 + sqrt(radicand));
+    const double incident = speed / alpha;
+    if (mode == OM_CONSTANT) cp = p[OM_TP_CP];
+    else cp = om_lookup(px, py, cv[3], incident);
+    out[0] = area * ct / (2 * (alpha * alpha));
+    out[1] = .5 * area * cp * (incident * incident * incident);
+    out[2] = incident; out[3] = ct; out[4] = cp;
+    return 0;
+}
+
+/* One rotor's sample (ThetisRotor.sample with the CoveredRotor gate) and its
+ * sink coefficient per support cell. Returns 0 or an error code. */
+static int om_turbine_sample(const om_ctx *m, const om_turbines *T, int r, const double *q, const double *z,
+                             const double *grad, double *kcell, double *diag)
+{
+    const int n = m->nc, np_ = T->plane_offset[T->nr];
+    const double dry = m->dry;
+    const double *p = T->param + (size_t)r * OM_TP_N;
+    const double D = p[OM_TP_D], tol = p[OM_TP_TOL];
+    const double top = p[OM_TP_HUB] + D / 2, bottom = p[OM_TP_HUB] - D / 2;
+    const int mode = (int)p[OM_TP_MODE];
+    double low = INFINITY, high = -INFINITY;
+    for (int j = T->plane_offset[r]; j < T->plane_offset[r + 1]; ++j) {
+        const int c = T->plane_cell[j];
+        const double eta = q[c] + z[c];
+        const double surface = eta + grad[4 * n + c] * T->plane_delta[j] + grad[5 * n + c] * T->plane_delta[np_ + j];
+        const double bed = z[c] + grad[6 * n + c] * T->plane_delta[j] + grad[7 * n + c] * T->plane_delta[np_ + j];
+        low = fmin(low, fmin(surface, eta)); high = fmax(high, fmax(bed, z[c]));
+    }
+    int support_dry = 0, below = 0;
+    double u1 = 0., depth = 0.;
+    const int *cv = T->curve + 4 * r;
+    for (int e = T->support_offset[r]; e < T->support_offset[r + 1]; ++e) {
+        const int c = T->support_cell[e];
+        const double h = q[c], u = q[n + c] / fmax(h, dry), v = q[2 * n + c] / fmax(h, dry);
+        const double speed = hypot(u, v), w = T->support_weight[e];
+        if (h <= dry) support_dry = 1;
+        u1 += w * speed; depth += w * h;
+        kcell[e] = 0.;
+        if (mode != OM_CONSTANT) {
+            double minimum = T->curve_x[cv[0]];
+            if (mode != OM_SPEED_TABLE)
+                minimum = minimum * .5 * (1 + sqrt(1 - OM_PI * D * T->curve_y[cv[0]] / (4 * h)));
+            if (speed < minimum) below = 1;
+        }
+    }
+    const double margin = low - top, clearance = bottom - high;
+    int reason = OM_R_COVERED;
+    if (margin < tol) reason = OM_R_DEPTH;
+    else if (clearance < tol) reason = OM_R_BED;
+    else if (margin + tol < p[OM_TP_SURFCLEAR]) reason = OM_R_SURFCLEAR;
+    else if (clearance + tol < p[OM_TP_BEDCLEAR]) reason = OM_R_BEDCLEAR;
+    else if (support_dry) reason = OM_R_DRY;
+    int active = reason == OM_R_COVERED;
+    if (active && u1 <= 1e-10) { active = 0; reason = u1 < 0 ? OM_R_REVERSE : OM_R_NOFLOW; }
+    if (active && mode != OM_CONSTANT && below) { active = 0; reason = OM_R_CUTIN; }
+    for (int k = 0; k < OM_TURB_FIELDS; ++k) diag[k] = 0.;
+    diag[OM_TD_ACTIVE] = active; diag[OM_TD_REASON] = reason;
+    diag[OM_TD_MARGIN] = margin; diag[OM_TD_CLEARANCE] = clearance;
+    diag[OM_TD_U1] = u1; diag[OM_TD_U0] = u1; diag[OM_TD_DEPTH] = depth;
+    diag[OM_TD_LOW] = low; diag[OM_TD_HIGH] = high;
+    if (!active) return 0;
+    double F = 0., work = 0., P = 0., incoming = 0., ctm = 0., cpm = 0.;
+    for (int e = T->support_offset[r]; e < T->support_offset[r + 1]; ++e) {
+        const int c = T->support_cell[e];
+        const double h = q[c], u = q[n + c] / fmax(h, dry), v = q[2 * n + c] / fmax(h, dry);
+        const double speed = hypot(u, v), w = T->support_weight[e], density = T->support_density[e];
+        double t[5];
+        const int err = om_cell_terms(T, r, h, u, v, t);
+        if (err) { diag[OM_TD_ERROR] = err; return err; }
+        kcell[e] = t[0] * density / m->area[c];
+        F += t[0] * density * (speed * speed);
+        work += t[0] * density * (speed * speed * speed);
+        P += t[1] * density;
+        incoming += w * t[2]; ctm += w * t[3]; cpm += w * t[4];
+    }
+    diag[OM_TD_FORCE] = F; diag[OM_TD_REMOVED] = work; diag[OM_TD_POWER] = P;
+    diag[OM_TD_U0] = incoming; diag[OM_TD_CT] = ctm; diag[OM_TD_CP] = cpm;
+    return 0;
+}
+
+/* Face traces of the hydrostatically reconstructed states (river_turbine_flow.h:39-52). */
+static void om_hkt_surface_pack(const om_ctx *m, const double *local, const int *constant, double *out)
+{
+    const int nf = m->nf;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < nf; ++i) {
+        for (int k = 0; k < 10; ++k) out[k * nf + i] = 0.;
+        if (m->neighbour[i] < 0) continue;
+        const double hl = local[i], hr = local[4 * nf + i];
+        out[i] = hl + local[3 * nf + i]; out[nf + i] = hr + local[7 * nf + i];
+        out[2 * nf + i] = hl > 0. ? local[nf + i] / hl : 0.; out[3 * nf + i] = hr > 0. ? local[5 * nf + i] / hr : 0.;
+        out[4 * nf + i] = hl > 0. ? hypot(local[nf + i], local[2 * nf + i]) / hl : 0.;
+        out[5 * nf + i] = hr > 0. ? hypot(local[5 * nf + i], local[6 * nf + i]) / hr : 0.;
+        out[6 * nf + i] = local[3 * nf + i]; out[7 * nf + i] = local[7 * nf + i];
+        out[8 * nf + i] = constant[m->owner[i]]; out[9 * nf + i] = constant[m->neighbour[i]];
+    }
+}
+
+/* Balanced face pressure correction (river_turbine_flow.h:54-82). */
+void om_hkt_pressure(const om_ctx *m, const om_turbines *T, const double *q, const double *z, const double *trace,
+                     const double *grad, const double *source, double *out, int *status)
+{
+    const int nf = m->nf, n = m->nc;
+    const double gravity = m->grav, dry = m->dry;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < nf; ++i) {
+        out[i] = 0.; out[nf + i] = 0.; status[i] = 0;
+        const int a = m->owner[i], b = m->neighbour[i];
+        if (b < 0) continue;
+        if (q[a] <= dry || q[b] <= dry) { status[i] = 1; continue; }
+        const double bed = fmax(fmax(z[a], z[b]), fmax(trace[6 * nf + i], trace[7 * nf + i]));
+        const double ha = fmax(0., q[a] + z[a] - bed), hb = fmax(0., q[b] + z[b] - bed);
+        const double hl = fmax(0., trace[i] - bed), hr = fmax(0., trace[nf + i] - bed);
+        if (fmin(fmin(ha, hb), fmin(hl, hr)) <= dry) { status[i] = 1; continue; }
+        const double h = .5 * (hl + hr);
+        if (fabs(hr - hl) > .005 * h) { status[i] = 2; continue; }
+        const double old = .25 * gravity * (hl * hl + hr * hr);
+        double po = old, pn = old;
+        if (trace[8 * nf + i] != 0.) po += .5 * gravity * (ha * ha - hl * hl);
+        if (trace[9 * nf + i] != 0.) pn += .5 * gravity * (hb * hb - hr * hr);
+        if (fabs(po - pn) > 128. * OM_EPS * fmax(1., fmax(fabs(po), fabs(pn)))) { status[i] = 3; continue; }
+        const double da = m->distance[i], db = m->distance[nf + i], d = da + db, wa = db / d, wb = da / d;
+        const double sx = wa * T->mdisp[i] + wb * T->mdisp[2 * nf + i];
+        const double sy = wa * T->mdisp[nf + i] + wb * T->mdisp[3 * nf + i];
+        double pressure = .5 * gravity * (wa * ha * ha + wb * hb * hb);
+        pressure += gravity * sx * (wa * ha * grad[4 * n + a] + wb * hb * grad[4 * n + b]);
+        pressure += gravity * sy * (wa * ha * grad[5 * n + a] + wb * hb * grad[5 * n + b]);
+        const double nx = m->normal[i], ny = m->normal[nf + i];
+        pressure += da * db / d * ((source[n + a] - source[n + b]) * nx + (source[2 * n + a] - source[2 * n + b]) * ny);
+        double delta = .5 * (po + pn) - pressure;
+        const double speed = sqrt(gravity * h), theta = fmin(1., fmax(trace[4 * nf + i], trace[5 * nf + i]) / speed);
+        delta -= .5 * (1. - theta) * speed * (2. * hl * hr / (hl + hr)) * (trace[3 * nf + i] - trace[2 * nf + i]);
+        out[i] = delta * nx; out[nf + i] = delta * ny;
+    }
+}
+
+/* Symmetric-strain ambient stress (river_hydrokinetic_stress.h:13-35). */
+void om_hkt_stress(const om_ctx *m, const om_turbines *T, const double *q, const double *z, const double *grad,
+                   double *out)
+{
+    const int nf = m->nf, n = m->nc;
+    const double dry = m->dry;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < nf; ++i) {
+        out[i] = 0.; out[nf + i] = 0.;
+        const int o = m->owner[i], j = m->neighbour[i];
+        if (j < 0 || q[o] <= dry || q[j] <= dry) continue;
+        double h = fmin(q[o], q[j]);
+        h = fmin(h, fmax(0., .5 * (q[o] + z[o] + q[j] + z[j]) - fmax(z[o], z[j])));
+        const double d = m->distance[i] + m->distance[nf + i], wo = m->distance[nf + i] / d, wj = m->distance[i] / d;
+        const double visc = wo * T->nu[o] + wj * T->nu[j];
+        const double nx = m->normal[i], ny = m->normal[nf + i];
+        const double dx = T->xy[j] - T->xy[o], dy = T->xy[n + j] - T->xy[n + o];
+        const double dn = dx * nx + dy * ny;
+        const double du = q[n + j] / q[j] - q[n + o] / q[o], dv = q[2 * n + j] / q[j] - q[2 * n + o] / q[o];
+        double ux = wo * grad[o] + wj * grad[j], uy = wo * grad[n + o] + wj * grad[n + j];
+        double vx = wo * grad[2 * n + o] + wj * grad[2 * n + j], vy = wo * grad[3 * n + o] + wj * grad[3 * n + j];
+        const double cu = (du - ux * dx - uy * dy) / dn, cv = (dv - vx * dx - vy * dy) / dn;
+        ux += cu * nx; uy += cu * ny; vx += cv * nx; vy += cv * ny;
+        out[i] = visc * h * (2. * ux * nx + (uy + vx) * ny);
+        out[nf + i] = visc * h * ((uy + vx) * nx + 2. * vy * ny);
+    }
+}
+
+/* work(1:2) = sum_k s len flux / area, then rate(1:2) += work(1:2)
+ * (flow2dh_fixed_bed_kernels.h:54-60 with unit depth weights). */
+static void om_face_momentum_add(const om_ctx *m, const double *flux, double *rate)
+{
+    const int n = m->nc, nf = m->nf;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; ++i) {
+        double x = 0., y = 0.;
+        for (int k = m->offset[i]; k < m->offset[i + 1]; ++k) {
+            const int f = m->faces[k];
+            x += m->signs[k] * m->length[f] * flux[f];
+            y += m->signs[k] * m->length[f] * flux[nf + f];
+        }
+        rate[n + i] += (1. * x / m->area[i]);
+        rate[2 * n + i] += (1. * y / m->area[i]);
+    }
+}
+
 typedef struct {
     double *v, *grad, *trace, *local, *riemann, *fl, *fr, *speed, *ext_trace, *ext_flux, *work,
            *theta, *correction, *freq, *stage, *total;
@@ -1113,6 +1417,54 @@ void om_scratch_destroy(om_scratch *s)
                    s->pstatus, s->constant, s->kind, s->rstatus, s->closed, s->astatus, s->fstatus, s->estatus};
     for (size_t i = 0; i < sizeof(all) / sizeof(all[0]); ++i) free(all[i]);
     free(s);
+}
+
+/* Momentum sources of an installed rotor array, in the order of the
+ * reference's add_momentum: ambient stress, actuator sinks, balanced
+ * pressure (river_turbine_flow.py:230-239). Returns 0 or an error code. */
+int om_turbine_momentum(const om_ctx *m, om_scratch *s, const double *q, const double *z, double *rate)
+{
+    om_turbines *T = (om_turbines *)m->turb;
+    const int n = m->nc;
+    om_hkt_gradients(m, T, q, z, T->grad);
+    if (T->nu) {
+        om_hkt_stress(m, T, q, z, T->grad, T->face);
+        om_face_momentum_add(m, T->face, rate);
+    }
+    memset(T->raw, 0, sizeof(double) * 3 * (size_t)n);
+    int err = 0;
+    for (int r = 0; r < T->nr; ++r) {
+        const int e = om_turbine_sample(m, T, r, q, z, T->grad, T->kcell, T->diag + (size_t)r * OM_TURB_FIELDS);
+        if (e && !err) err = e;
+        for (int k = T->support_offset[r]; k < T->support_offset[r + 1]; ++k) {
+            const int c = T->support_cell[k];
+            const double h = q[c], u = q[n + c] / fmax(h, m->dry), v = q[2 * n + c] / fmax(h, m->dry);
+            const double speed = hypot(u, v);
+            T->raw[n + c] -= T->kcell[k] * speed * u;
+            T->raw[2 * n + c] -= T->kcell[k] * speed * v;
+        }
+    }
+    if (err) return err;
+    for (int i = 0; i < n; ++i) { rate[n + i] += T->raw[n + i]; rate[2 * n + i] += T->raw[2 * n + i]; }
+    if (T->pressure) {
+        om_hkt_surface_pack(m, s->local, s->constant, T->trace);
+        om_hkt_pressure(m, T, q, z, T->trace, T->grad, T->raw, T->face, T->fstatus);
+        om_face_momentum_add(m, T->face, rate);
+    }
+    return 0;
+}
+
+/* Rotor diagnostics of a state (the reference's hkt_diagnose): gradients, then every rotor's sample. */
+int om_turbine_diagnose(const om_ctx *m, const double *q, const double *z)
+{
+    om_turbines *T = (om_turbines *)m->turb;
+    om_hkt_gradients(m, T, q, z, T->grad);
+    int err = 0;
+    for (int r = 0; r < T->nr; ++r) {
+        const int e = om_turbine_sample(m, T, r, q, z, T->grad, T->kcell, T->diag + (size_t)r * OM_TURB_FIELDS);
+        if (e && !err) err = e;
+    }
+    return err;
 }
 
 /* One spatial residual (RiverMidpoint.rate + RiverExplicit.rate).
@@ -1155,6 +1507,7 @@ int om_rate(om_ctx *m, om_scratch *s, const double *q, const double *z, const do
     if (m->nb > 0 && om_reserve(m, dt, base, water, s->theta)) return OM_REJECT_BUDGET;
     om_limit_faces(m, q, s->theta, water, s->correction);
     om_limit_gather(m, water, s->correction, rate);
+    if (m->turb && om_turbine_momentum(m, s, q, z, rate)) return OM_FAIL;
     for (int i = 0; i < 3 * nc; ++i) if (!isfinite(rate[i])) return OM_REJECT_SPATIAL;
     const double freq = om_frequency(m, q, s->speed, s->ext_trace, s->freq);
     *freq_out = freq;
@@ -1255,3 +1608,4 @@ void om_set_threads(int n)
 
 size_t om_ctx_size(void) { return sizeof(om_ctx); }
 size_t om_stats_size(void) { return sizeof(om_stats); }
+size_t om_turbines_size(void) { return sizeof(om_turbines); }

@@ -59,7 +59,16 @@ class Ctx(C.Structure):
                 ("grav", D), ("dry", D), ("cfl", D), ("speed_limit", D),
                 ("roughness_mode", I), ("roughness_value", D),
                 ("seg_mode", P), ("stage_policy", P), ("exterior_bed", P), ("forcing", P),
-                ("table_len", I), ("table_time", P), ("table_value", P), ("threads", I)]
+                ("table_len", I), ("table_time", P), ("table_value", P), ("threads", I),
+                ("turb", P)]
+
+
+class Turbines(C.Structure):
+    _fields_ = [("nr", I), ("support_offset", P), ("support_cell", P), ("support_weight", P),
+                ("support_density", P), ("plane_offset", P), ("plane_cell", P), ("plane_delta", P),
+                ("param", P), ("curve", P), ("curve_x", P), ("curve_y", P), ("nu", P), ("pressure", I),
+                ("dxdy", P), ("inverse", P), ("xy", P), ("mdisp", P), ("diag", P),
+                ("grad", P), ("raw", P), ("face", P), ("work", P), ("trace", P), ("kcell", P), ("fstatus", P)]
 
 
 class Stats(C.Structure):
@@ -95,6 +104,12 @@ def _setup(L):
     L.om_advance.argtypes = [P, P, P, D, D, P, P, P]
     L.om_advance.restype = I
     L.om_set_threads.argtypes = [I]
+    L.om_turbines_size.restype = C.c_size_t
+    assert L.om_turbines_size() == C.sizeof(Turbines), "oracle turbine layout differs"
+    L.om_turbine_diagnose.argtypes = [P, P, P]
+    L.om_turbine_diagnose.restype = I
+    L.om_hkt_gradients.argtypes = [P, P, P, P, P]
+    L.om_hkt_gradients.restype = None
 
 
 def _p(a):
@@ -165,6 +180,10 @@ class Oracle:
             ctx.table_time = k("table_time", _f64(tt))
             ctx.table_value = k("table_value", _f64(case["table_value"]))
         ctx.threads = threads or 0
+        self.turbines = None
+        if case.get("turbines"):
+            self._bind_turbines(case, k)
+            ctx.turb = C.cast(C.pointer(self._turb), P)
         self.ctx = ctx
         self.cp = C.byref(ctx)
         self.m = m
@@ -172,6 +191,50 @@ class Oracle:
         self.L.om_set_threads(threads or os.cpu_count() or 1)
         self._scratch = self.L.om_scratch_create(self.cp)
         self.hint = C.c_double(0.0)
+
+    def _bind_turbines(self, case, k):
+        """Rotor array of the case (the product's host-side geometry packing)."""
+        from braids_hkt_gb300 import turbines as TB
+        pk = TB.pack([case], [0])
+        self.turbines = pk
+        m = case["mesh"]
+        nr, ns = pk["nrotor"], len(pk["support_cell"])
+        t = Turbines()
+        t.nr = nr
+        for name in ("support_offset", "support_cell", "plane_offset", "plane_cell", "curve"):
+            setattr(t, name, k("t_" + name, _i32(pk[name])))
+        for name in ("support_weight", "support_density", "plane_delta", "param", "curve_x", "curve_y",
+                     "dxdy", "inverse", "xy"):
+            setattr(t, name, k("t_" + name, _f64(pk[name])))
+        t.mdisp = k("t_mdisp", _f64(pk["mid_disp"]))
+        t.nu = k("t_nu", _f64(pk["nu"])) if pk["nu"].any() else None
+        t.pressure = 1
+        self.diag = np.zeros((nr, TB.NDIAG))
+        t.diag = k("t_diag", self.diag)
+        t.grad = k("t_grad", np.zeros((10, m.nc)))
+        t.raw = k("t_raw", np.zeros((3, m.nc)))
+        t.face = k("t_face", np.zeros((2, m.nf)))
+        t.work = k("t_work", np.zeros((3, m.nc)))
+        t.trace = k("t_trace", np.zeros((10, m.nf)))
+        t.kcell = k("t_kcell", np.zeros(max(ns, 1)))
+        t.fstatus = k("t_fstatus", np.zeros(m.nf, np.int32))
+        self._turb = t
+
+    def turbine_pressure(self, on):
+        """Switch the balanced-pressure correction (on by default with rotors)."""
+        self._turb.pressure = int(bool(on))
+
+    def diagnose(self, q):
+        """Rotor diagnostics of state q: (error code, (nrotor, NDIAG) record)."""
+        q = _f64(q)
+        err = self.L.om_turbine_diagnose(self.cp, _p(q), _p(self.z))
+        return err, self.diag.copy()
+
+    def hkt_gradients(self, q):
+        q = _f64(q)
+        out = np.zeros((10, self.m.nc))
+        self.L.om_hkt_gradients(self.cp, C.cast(C.pointer(self._turb), P), _p(q), _p(self.z), _p(out))
+        return out
 
     def __del__(self):
         try:

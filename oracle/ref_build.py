@@ -19,7 +19,8 @@ built-ins and a loop over the launch grid):
   implicit_midpoint_fwave.cu (src/braids_gpu/implicit_midpoint_fwave.cu)
 Dual-compiled OpenMP headers (their ENTRY/LOOP macros select the host form):
   river_midpoint.h, river_explicit.h, river_exterior_bed.h,
-  river_hydraulic_drag.source() (src/braids_core/sediment/river_hydraulic_drag.py:11-15)
+  river_hydraulic_drag.source() (src/braids_core/sediment/river_hydraulic_drag.py:11-15),
+  river_turbine_flow.h, river_hydrokinetic_stress.h (turbine momentum terms)
 
 Usage: python oracle/ref_build.py   (exits non-zero when the reference is absent)
 """
@@ -95,6 +96,10 @@ def generate():
         "ref_explicit": (src / "braids_core/sediment/river_explicit.h").read_text(),
         "ref_exterior": (src / "braids_core/sediment/river_exterior_bed.h").read_text(),
         "ref_drag": river_hydraulic_drag.source(False),
+        # turbine momentum terms (river_turbine_flow.h, river_hydrokinetic_stress.h)
+        "ref_hkt": (src / "braids_core/sediment/river_turbine_flow.h").read_text(),
+        "ref_stress": (src / "braids_core/sediment/river_hydrokinetic_stress.h").read_text(),
+        "ref_flow": (src / "braids_core/sediment/flow2dh_fixed_bed_kernels.h").read_text(),
     }
     for name, code in headers.items():
         (OUT / f"{name}.h").write_text(code)

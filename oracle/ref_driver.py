@@ -8,6 +8,9 @@ the reference's Python owners line by line:
   RiverMidpoint.rate, GPU branch       src/braids_core/sediment/river_midpoint.py:100-176
   RiverExplicit.rate/_single/advance   src/braids_core/sediment/river_explicit.py:63-154
   ExteriorBed.evaluate/apply_*         src/braids_core/sediment/river_exterior_bed.py:183-233
+  turbine momentum (install.add)       src/braids_core/sediment/river_turbine_flow.py:222-239,
+                                       with the reference's ThetisRotor.sample / cell_terms
+                                       (river_turbine_thetis.py) run on numpy
 
 The stock-budget steps run the reference's own Python classes
 (``OutletFeasibility`` and ``ExplicitBoundaryBudget``) on a minimal stand-in
@@ -104,6 +107,130 @@ class Ref:
         self.frequency_peak = 0.0
         if nb:
             self._budget = self._make_budget()
+        self.rotors = None
+        if case.get("turbines"):
+            self._install_turbines(case)
+
+    # -- rotor array: the reference's Thetis rotors on this mesh ----------------
+    @staticmethod
+    def _stub_shapely():
+        """The turbine modules import shapely at module level for geometry set-up
+        that is not exercised here (the footprint integrals come in packed)."""
+        import types
+        for name in ("shapely", "shapely.geometry", "shapely.strtree", "shapely.ops"):
+            sys.modules.setdefault(name, types.ModuleType(name))
+        g = sys.modules["shapely.geometry"]
+        for attr in ("Polygon", "LineString", "box", "Point"):
+            setattr(g, attr, getattr(g, attr, object))
+        sys.modules["shapely"].constrained_delaunay_triangles = None
+        sys.modules["shapely.strtree"].STRtree = object
+        sys.modules["shapely.ops"].unary_union = None
+
+    def _install_turbines(self, case):
+        self._stub_shapely()
+        from braids_core.sediment import river_turbine_thetis as T
+        from braids_core.sediment.bend_methods_v1 import prepared_geometry
+        from braids_hkt_gb300 import turbines as TB
+        m = self.m
+        data = dict(xy=m.xy, area=m.area, owner=m.owner, neighbour=m.neighbour, normal=m.normal,
+                    length=m.length, mid=m.mid, offset=m.offset, faces=m.faces, signs=m.signs,
+                    distance=m.records["distance"], bid=m.bid)
+        self.pg = prepared_geometry(data)
+        for n in ("hkt", "stress", "flow"):
+            self.libs[n] = C.CDLL(str(REF / f"libref_{n}.so"))
+        self.libs["hkt"].hkt_stress_threads(C.c_int(1))
+        self.libs["stress"].hkt_stress_threads(C.c_int(1))
+        self.libs["flow"].flow_threads(C.c_int(1))
+        ra = TB.RotorArray(m, case["turbines"])
+        rotors = []
+        for k, row in enumerate(case["turbines"]):
+            r = object.__new__(T.ThetisRotor)
+            D = float(row["D"])
+            r.xp, r.dry = np, self.dry
+            r.c = dict(row, normal_xy=[1., 0.], ct=0., cp=0., control={"mode": "constant_ct"})
+            r.minimum_bed_clearance = row["minimum_bed_clearance_m"]
+            r.minimum_surface_clearance = row["minimum_surface_clearance_m"]
+            r.top, r.bottom = row["hub_elevation_m"] + D / 2, row["hub_elevation_m"] - D / 2
+            cells, weight, density = ra.support[k]
+            r.weights = np.zeros(m.nc)
+            r.weights[cells] = density * ((D / 2) ** 2 * 1.45661)
+            r.normalized = np.zeros(m.nc)
+            r.normalized[cells] = weight
+            r.area = np.asarray(m.area, dtype=np.float64)
+            r.ids = np.asarray(cells)
+            r.normal = np.array([1., 0.])
+            rows, disp = ra.plane[k]
+            r.plane, r.delta = np.asarray(rows, dtype=np.int32), np.ascontiguousarray(disp)
+            r.tolerance = max(1e-9, 64 * np.finfo(float).eps * max(1., abs(r.top), abs(r.bottom)))
+            r.control = T.validate_control(row["control"])
+            r.original = dict(row)
+            r.density_integrals = np.zeros(m.nc)
+            r.density_integrals[cells] = density
+            rotors.append(r)
+        self.rotors = rotors
+        self.rotor_nu = float(case["turbines"][0].get("nu", 0.0))
+        self.last_turbines = None
+        self.hkt_pressure = True
+
+    @staticmethod
+    def _invoke(fn, *args):
+        """Call a host kernel; the argument tuple (and any temporary arrays in
+        it) stays referenced until the call returns."""
+        fn.restype = None
+        fn(*[_arg(a) for a in args])
+
+    def hkt_gradients(self, q, z=None):
+        m = self.m
+        z = self.z if z is None else np.ascontiguousarray(z)
+        grad = np.zeros((10, m.nc))
+        self._invoke(self.libs["hkt"].hkt_wet_gradients, *(m.nc, self.dry, np.ascontiguousarray(q), z, self.pg["offset"], self.pg["faces"],
+                       self.pg["owner"], self.pg["neighbour"], np.ascontiguousarray(self.pg["dxdy"]),
+                       np.ascontiguousarray(self.pg["inverse"]), grad))
+        return grad
+
+    def turbine_sample(self, q, grad=None):
+        """Every rotor's reference sample: list of (diagnostic dict, k, u, v)."""
+        grad = self.hkt_gradients(q) if grad is None else grad
+        return [r.sample(np.ascontiguousarray(q), self.z, grad) for r in self.rotors]
+
+    def _momentum_gather(self, face, rate):
+        m, g = self.m, self.g
+        work = np.zeros((3, m.nc))
+        self._invoke(self.libs["flow"].flow_momentum_gather, *(m.nc, m.nf, np.ones(m.nc), face, g["offset"], g["faces"], g["signs"], g["length"],
+                       g["area"], work))
+        rate[1:] += work[1:]
+
+    def turbine_momentum(self, q, o, rate):
+        """The reference's add_momentum with a rotor array (river_turbine_flow.py:230-239)."""
+        m, g = self.m, self.g
+        q = np.ascontiguousarray(q)
+        grad = self.hkt_gradients(q)
+        face = np.zeros((2, m.nf))
+        if self.rotor_nu > 0.:
+            self._invoke(self.libs["stress"].hkt_full_strain_faces, *(m.nf, m.nc, self.dry, q, self.z, grad, np.full(m.nc, self.rotor_nu), g["owner"],
+                           g["neighbour"], g["normal"], np.ascontiguousarray(m.records["distance"]),
+                           np.ascontiguousarray(m.xy), face))
+            self._momentum_gather(face, rate)
+        raw = np.zeros((3, m.nc))
+        samples = []
+        for r in self.rotors:
+            d, k, u, v = r.sample(q, self.z, grad)
+            speed = np.hypot(u, v)
+            raw[1, r.ids] -= k * speed * u
+            raw[2, r.ids] -= k * speed * v
+            samples.append((d, k))
+        rate[1:] += raw[1:]
+        self.last_turbines = dict(samples=samples, grad=grad, raw=raw)
+        if self.hkt_pressure:
+            trace = np.zeros((10, m.nf))
+            self._invoke(self.libs["hkt"].hkt_surface_pack, *(m.nf, m.nc, np.ascontiguousarray(o["local"]), g["owner"], g["neighbour"],
+                           np.ascontiguousarray(o["constant"], dtype=np.int32), trace))
+            status = np.zeros(m.nf, np.int32)
+            self._invoke(self.libs["hkt"].hkt_balanced_pressure, *(m.nf, m.nc, self.grav, self.dry, q, self.z, trace, grad, raw, g["owner"],
+                           g["neighbour"], g["normal"], np.ascontiguousarray(m.records["distance"]),
+                           np.ascontiguousarray(self.pg["displacement"]), face, status))
+            self._momentum_gather(face, rate)
+            self.last_turbines.update(trace=trace, pressure=face.copy(), pressure_status=status)
 
     # -- the reference's own stock-budget classes on a stand-in owner --------
     def _make_budget(self):
@@ -261,6 +388,8 @@ class Ref:
             raise Rejected("budget")
         self.call("midpoint", "midpoint_gather", 0, n, nf, g["area"], g["length"], g["offset"], g["faces"],
                   g["signs"], water, correction, rate)
+        if self.rotors:
+            self.turbine_momentum(q, o, rate)
         if not np.all(np.isfinite(rate)):
             raise Rejected("spatial")
         freq = np.zeros(n)
