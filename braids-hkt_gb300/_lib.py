@@ -30,6 +30,9 @@ SIGNATURES = {
     "brx_substep": (I, [P, D, D, P, P]),
     "brx_rate": (I, [P, D, D, P, P, P, P]),
     "brx_scenarios_activate": (I, [P, P]),
+    "brx_turbines_set": (I, [P, I, P, P, P, I, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P]),
+    "brx_turbines_diagnose": (I, [P, P]),
+    "brx_turbines_last": (I, [P, P]),
     "brx_hint_get": (I, [P, P]),
     "brx_hint_set": (I, [P, P]),
     "brx_graph_chunk_set": (I, [P, I]),

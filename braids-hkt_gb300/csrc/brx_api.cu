@@ -22,6 +22,7 @@
 #define BRX_NS brx
 #include "brx_kernels.cuh"
 #include "brx_launch.h"
+#include "brx_turbine.cuh"
 
 using namespace brx;
 
@@ -75,6 +76,10 @@ struct brx_solver {
     std::vector<int> h_faces_csr;
     std::vector<int> h_ccls;         // per cell: bit0 has a stage outlet face
     int *d_ccls = nullptr;
+    TurbDev turb{};                  // rotor arrays
+    bool has_turb = false;
+    int nrotor = 0;
+    double *d_tdiag_out = nullptr;   // (nrotor, 16) diagnostics of brx_turbines_diagnose
 
     template <class T> int alloc(T **p, size_t count)
     {
@@ -497,6 +502,132 @@ extern "C" int brx_scenarios_activate(brx_solver *s, const int *active)
     return BRX_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Rotor arrays
+// ---------------------------------------------------------------------------
+static int ensure_ready(brx_solver *s);
+extern "C" int brx_turbines_set(brx_solver *s, int nrotor, const int *rotor_scenario, const double *param,
+                                const int *curve, int ncurve, const double *curve_x, const double *curve_y,
+                                const int *support_offset, const int *support_cell, const double *support_weight,
+                                const double *support_density, const int *plane_offset, const int *plane_cell,
+                                const double *plane_delta, const double *dxdy, const double *inverse,
+                                const double *xy, const double *mid_disp, const double *nu, const int *hkt)
+{
+    if (!s) return fail(BRX_ERR_ARGUMENT, "null solver");
+    if (s->has_turb) return fail(BRX_ERR_STATE, "rotor arrays are already installed");
+    if (nrotor < 1 || !rotor_scenario || !param || !curve || ncurve < 1 || !curve_x || !curve_y || !support_offset ||
+        !support_cell || !support_weight || !support_density || !plane_offset || !plane_cell || !plane_delta ||
+        !dxdy || !inverse || !xy || !mid_disp || !nu || !hkt)
+        return fail(BRX_ERR_ARGUMENT, "missing rotor array input");
+    const int nc = s->nc, nf = s->nf, nadj = s->nadj;
+    if (support_offset[0] != 0 || plane_offset[0] != 0) return fail(BRX_ERR_ARGUMENT, "offsets must start at 0");
+    for (int r = 0; r < nrotor; ++r) {
+        if (rotor_scenario[r] < 0 || rotor_scenario[r] >= s->nscen || !hkt[rotor_scenario[r]])
+            return fail(BRX_ERR_ARGUMENT, "rotor scenario out of range or without a rotor array");
+        if (support_offset[r + 1] <= support_offset[r] || plane_offset[r + 1] <= plane_offset[r])
+            return fail(BRX_ERR_ARGUMENT, "every rotor needs support cells and rotor-plane rows");
+        const int mode = (int)param[r * TP_N + TP_MODE];
+        if (mode < TM_CONSTANT || mode > TM_INCIDENT_CURVES) return fail(BRX_ERR_ARGUMENT, "unknown rotor control mode");
+        const int *cv = curve + 4 * r;
+        if (mode != TM_CONSTANT && (cv[0] < 0 || cv[1] < 2 || cv[0] + cv[1] > ncurve || cv[2] < 0 || cv[3] < 2 ||
+                                    cv[2] + cv[3] > ncurve))
+            return fail(BRX_ERR_ARGUMENT, "rotor curve out of range");
+        const int first = s->cell_offset[rotor_scenario[r]], last = s->cell_offset[rotor_scenario[r] + 1];
+        for (int e = support_offset[r]; e < support_offset[r + 1]; ++e)
+            if (support_cell[e] < first || support_cell[e] >= last) return fail(BRX_ERR_ARGUMENT, "support cell outside its scenario");
+        for (int j = plane_offset[r]; j < plane_offset[r + 1]; ++j)
+            if (plane_cell[j] < first || plane_cell[j] >= last) return fail(BRX_ERR_ARGUMENT, "rotor-plane cell outside its scenario");
+    }
+    const int ns = support_offset[nrotor], np_ = plane_offset[nrotor];
+    // unique support cells, each with its entries in rotor order
+    std::vector<std::pair<int, int>> pairs(ns);
+    for (int e = 0; e < ns; ++e) pairs[e] = {support_cell[e], e};
+    std::sort(pairs.begin(), pairs.end());
+    std::vector<int> ucell, uoff{0}, uent;
+    for (int e = 0; e < ns; ++e) {
+        if (e == 0 || pairs[e].first != pairs[e - 1].first) {
+            if (e) uoff.push_back(e);
+            ucell.push_back(pairs[e].first);
+        }
+        uent.push_back(pairs[e].second);
+    }
+    uoff.push_back(ns);
+    std::vector<int> stress(s->nscen, 0), sid(nrotor);
+    for (int i = 0; i < s->nscen; ++i)
+        for (int c = s->cell_offset[i]; c < s->cell_offset[i + 1]; ++c)
+            if (hkt[i] && nu[c] > 0) { stress[i] = 1; break; }
+    TurbDev t{};
+    t.nr = nrotor; t.np = np_; t.nucell = (int)ucell.size();
+    int *p_hkt, *p_stress, *p_sid, *p_soff, *p_scell, *p_poff, *p_pcell, *p_curve, *p_ucell, *p_uoff, *p_uent;
+    double *p_sw, *p_sd, *p_pdel, *p_param, *p_cx, *p_cy, *p_dxdy, *p_inv, *p_xy, *p_md, *p_nu;
+    TRY(s->upload(&p_hkt, hkt, s->nscen)); TRY(s->upload(&p_stress, stress.data(), s->nscen));
+    TRY(s->upload(&p_sid, rotor_scenario, nrotor));
+    TRY(s->upload(&p_soff, support_offset, nrotor + 1)); TRY(s->upload(&p_scell, support_cell, ns));
+    TRY(s->upload(&p_sw, support_weight, ns)); TRY(s->upload(&p_sd, support_density, ns));
+    TRY(s->upload(&p_poff, plane_offset, nrotor + 1)); TRY(s->upload(&p_pcell, plane_cell, np_));
+    TRY(s->upload(&p_pdel, plane_delta, 2 * (size_t)np_));
+    TRY(s->upload(&p_param, param, (size_t)nrotor * TP_N)); TRY(s->upload(&p_curve, curve, 4 * (size_t)nrotor));
+    TRY(s->upload(&p_cx, curve_x, ncurve)); TRY(s->upload(&p_cy, curve_y, ncurve));
+    TRY(s->upload(&p_ucell, ucell.data(), ucell.size())); TRY(s->upload(&p_uoff, uoff.data(), uoff.size()));
+    TRY(s->upload(&p_uent, uent.data(), uent.size()));
+    TRY(s->upload(&p_dxdy, dxdy, 2 * (size_t)nadj)); TRY(s->upload(&p_inv, inverse, 3 * (size_t)nc));
+    TRY(s->upload(&p_xy, xy, 2 * (size_t)nc)); TRY(s->upload(&p_md, mid_disp, 4 * (size_t)nf));
+    TRY(s->upload(&p_nu, nu, nc));
+    t.hkt = p_hkt; t.stress = p_stress; t.rotor_sid = p_sid;
+    t.support_offset = p_soff; t.support_cell = p_scell; t.support_weight = p_sw; t.support_density = p_sd;
+    t.plane_offset = p_poff; t.plane_cell = p_pcell; t.plane_delta = p_pdel;
+    t.param = p_param; t.curve = p_curve; t.curve_x = p_cx; t.curve_y = p_cy;
+    t.ucell = p_ucell; t.uoff = p_uoff; t.uent = p_uent;
+    t.dxdy = p_dxdy; t.inverse = p_inv; t.xy = p_xy; t.mdisp = p_md; t.nu = p_nu;
+    TRY(s->alloc(&t.grad, 8 * (size_t)nc)); TRY(s->alloc(&t.kcell, ns)); TRY(s->alloc(&t.raw, 2 * (size_t)nc));
+    TRY(s->alloc(&t.trace, 10 * (size_t)nf)); TRY(s->alloc(&t.pface, 2 * (size_t)nf));
+    TRY(s->alloc(&t.sface, 2 * (size_t)nf)); TRY(s->alloc(&t.diag, (size_t)nrotor * TD_N));
+    TRY(s->alloc(&s->d_tdiag_out, (size_t)nrotor * TD_N));
+    CK(cudaMemset(t.raw, 0, sizeof(double) * 2 * (size_t)nc));
+    CK(cudaMemset(t.grad, 0, sizeof(double) * 8 * (size_t)nc));
+    CK(cudaMemset(t.trace, 0, sizeof(double) * 10 * (size_t)nf));
+    CK(cudaMemset(t.pface, 0, sizeof(double) * 2 * (size_t)nf));
+    CK(cudaMemset(t.sface, 0, sizeof(double) * 2 * (size_t)nf));
+    CK(cudaMemset(t.diag, 0, sizeof(double) * (size_t)nrotor * TD_N));
+    s->turb = t;
+    s->has_turb = true;
+    s->nrotor = nrotor;
+    s->graph_dirty = true;
+    return BRX_OK;
+}
+
+// Rotor diagnostics of the bound state (the reference's hkt_diagnose):
+// out (nrotor, 16) in the rotor-record layout.
+extern "C" int brx_turbines_diagnose(brx_solver *s, double *out)
+{
+    TRY(ensure_ready(s));
+    if (!s->has_turb) return fail(BRX_ERR_STATE, "no rotor arrays installed");
+    if (!out) return fail(BRX_ERR_ARGUMENT, "null output");
+    const TurbDev &t = s->turb;
+    CK(cudaMemcpyAsync(s->d_ctrl, s->h_ctrl, sizeof(Ctrl) * s->nscen, cudaMemcpyHostToDevice, s->stream));
+    k_hkt_gradients<<<s->grid_c256, 256, 0, s->stream>>>(s->mesh, t, s->state.q[0], s->state.z, s->d_ctrl, 0);
+    k_turbine_sample<<<t.nr, TURB_THREADS, 0, s->stream>>>(s->mesh, t, s->state.q[0], s->state.z, s->d_ctrl, 0,
+                                                           s->d_tdiag_out);
+    s->launches += 2;
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, s->d_tdiag_out, sizeof(double) * (size_t)s->nrotor * TD_N, cudaMemcpyDeviceToHost,
+                       s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return BRX_OK;
+}
+
+// Rotor diagnostics of the last evaluated stage (the reference's turbine_diagnostics).
+extern "C" int brx_turbines_last(brx_solver *s, double *out)
+{
+    if (!s) return fail(BRX_ERR_ARGUMENT, "null solver");
+    if (!s->has_turb) return fail(BRX_ERR_STATE, "no rotor arrays installed");
+    if (!out) return fail(BRX_ERR_ARGUMENT, "null output");
+    CK(cudaMemcpyAsync(out, s->turb.diag, sizeof(double) * (size_t)s->nrotor * TD_N, cudaMemcpyDeviceToHost,
+                       s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return BRX_OK;
+}
+
 extern "C" int brx_hint_get(brx_solver *s, double *hint)
 {
     if (!s || !hint) return fail(BRX_ERR_ARGUMENT, "null argument");
@@ -533,14 +664,31 @@ static Launch make_launch(brx_solver *s, cudaStream_t st)
     L.grid_c = s->grid_c; L.grid_f = s->grid_f; L.grid_c256 = s->grid_c256; L.grid_f256 = s->grid_f256;
     L.stream = st;
     L.mx = s->mx;
+    L.turb = s->turb;
+    L.has_turb = s->has_turb;
     return L;
 }
 
 // Launch one kernel of the solver's arithmetic form on stream st (default:
 // the solver stream); returns launches issued.
+// The rotor-array terms of one stage (scenarios with rotors only): wet
+// gradients, one CTA per rotor, the sink per support cell, face terms.
+static int launch_turbines(brx_solver *s, int stage, cudaStream_t st)
+{
+    if (!s->has_turb) return 0;
+    const double *q = stage == 1 ? s->state.work : s->state.q1;
+    const TurbDev &t = s->turb;
+    k_hkt_gradients<<<s->grid_c256, 256, 0, st>>>(s->mesh, t, q, s->state.z, s->d_ctrl, stage);
+    k_turbine_sample<<<t.nr, TURB_THREADS, 0, st>>>(s->mesh, t, q, s->state.z, s->d_ctrl, stage, t.diag);
+    k_turbine_raw<<<std::max(1, std::min((t.nucell + 255) / 256, s->sms * 8)), 256, 0, st>>>(s->mesh, t, q, s->d_ctrl, stage);
+    k_hkt_faces<<<s->grid_f, 128, 0, st>>>(s->mesh, t, q, s->state.z, s->d_ctrl, stage);
+    return 4;
+}
+
 static int launch_kernel(brx_solver *s, int kind, int stage, double *rate_out, cudaStream_t st = nullptr)
 {
     if (!st) st = s->stream;
+    if (kind == K_TURB) return launch_turbines(s, stage, st);
     if (s->precision == BRX_MIXED) return mixed_kernel(make_launch(s, st), kind, stage, rate_out);
     switch (kind) {
     case K_DRAG:
@@ -555,7 +703,8 @@ static int launch_kernel(brx_solver *s, int kind, int stage, double *rate_out, c
         else k_cells<double, MAX_CELL_FACES><<<s->grid_c, 128, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage);
         return 1;
     case K_FACES:
-        k_faces<double><<<s->grid_f, 128, 0, st>>>(s->mesh, s->state, s->bnd, s->d_ctrl, s->work, stage);
+        k_faces<double><<<s->grid_f, 128, 0, st>>>(s->mesh, s->state, s->bnd, s->d_ctrl, s->work, stage,
+                                                    s->has_turb ? s->turb.trace : nullptr, s->turb.hkt);
         return 1;
     case K_GATHER:
         k_gather<<<s->grid_c256, 256, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage);
@@ -564,7 +713,8 @@ static int launch_kernel(brx_solver *s, int kind, int stage, double *rate_out, c
         k_limit<<<s->grid_f256, 256, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage);
         return 1;
     case K_UPDATE:
-        k_update<double><<<s->grid_c256, 256, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage, rate_out);
+        k_update<double><<<s->grid_c256, 256, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage, rate_out,
+                                                        s->turb, s->has_turb);
         return 1;
     }
     return 0;
@@ -583,7 +733,7 @@ static void enqueue_stage(brx_solver *s, int stage, double *rate_out)
     }
     s->launches += launch_kernel(s, K_CELLS, stage, nullptr);
     if (fork) cudaStreamWaitEvent(s->stream, s->join, 0);
-    for (int kind = K_FACES; kind <= K_UPDATE; ++kind)
+    for (int kind : {(int)K_FACES, (int)K_GATHER, (int)K_LIMIT, (int)K_TURB, (int)K_UPDATE})
         s->launches += launch_kernel(s, kind, stage, kind == K_UPDATE ? rate_out : nullptr);
 }
 
@@ -803,14 +953,16 @@ extern "C" int brx_profile_substep(brx_solver *s, double dt, double time, int ca
         if (k >= 0) kinds.push_back(k);
     };
     cudaStream_t st = s->stream;
+    int extra = 0;                   // kernels beyond one per timed kind
     mark(-1);
     if (launch_kernel(s, K_DRAG, 0, nullptr)) mark(K_DRAG);
     for (int stage = 1; stage <= 2; ++stage)
-        for (int kind = K_BOUNDARY; kind <= K_UPDATE; ++kind)
-            if (launch_kernel(s, kind, stage, nullptr)) mark(kind);
+        for (int kind : {(int)K_BOUNDARY, (int)K_CELLS, (int)K_FACES, (int)K_GATHER, (int)K_LIMIT, (int)K_TURB,
+                         (int)K_UPDATE})
+            if (const int nl = launch_kernel(s, kind, stage, nullptr)) { mark(kind); extra += nl - 1; }
     k_control<<<(s->nscen + 127) / 128, 128, 0, st>>>(s->d_ctrl, s->nscen); mark(7);
     k_commit<<<s->grid_c256, 256, 0, st>>>(s->mesh, s->state, s->d_ctrl);
-    s->launches += (long long)kinds.size() + 1;
+    s->launches += (long long)kinds.size() + 1 + extra;
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(st));
     const int n = std::min(cap, (int)kinds.size());
@@ -972,10 +1124,10 @@ extern "C" int brx_rate_noalloc(int nc, int nf, int nadj, const int *owner, cons
     const int n = nc > nf ? nc : nf;
     k_noalloc_tables<<<(n + 255) / 256, 256, 0, st>>>(m, ctrl, cell_sid, cflags, face_sid, bslot, bmode, disp_unit);
     k_cells<double, MAX_CELL_FACES><<<(nc + 127) / 128, 128, 0, st>>>(m, sd, ctrl, w, 1);
-    k_faces<double><<<(nf + 127) / 128, 128, 0, st>>>(m, sd, b, ctrl, w, 1);
+    k_faces<double><<<(nf + 127) / 128, 128, 0, st>>>(m, sd, b, ctrl, w, 1, nullptr, nullptr);
     k_gather<<<(nc + 255) / 256, 256, 0, st>>>(m, sd, ctrl, w, 1);
     k_limit<<<(nf + 255) / 256, 256, 0, st>>>(m, sd, ctrl, w, 1);
-    k_update<double><<<(nc + 255) / 256, 256, 0, st>>>(m, sd, ctrl, w, 1, rate);
+    k_update<double><<<(nc + 255) / 256, 256, 0, st>>>(m, sd, ctrl, w, 1, rate, TurbDev{}, 0);
     k_water_out<<<(nf + 255) / 256, 256, 0, st>>>(m, w, water);
     CK(cudaGetLastError());
     Ctrl out{};

@@ -43,7 +43,8 @@ enum : unsigned {
     ST_RATE = 4u,         // nonfinite rate
     ST_ENDPOINT = 8u,     // negative / nonfinite stage result
     ST_FREQ = 16u,        // nonfinite CFL frequency
-    ST_PRE = ST_SPATIAL | ST_BUDGET | ST_RATE | ST_FREQ,
+    ST_TURBINE = 64u,     // rotor model outside its domain (the reference raises): the scenario fails
+    ST_PRE = ST_SPATIAL | ST_BUDGET | ST_RATE | ST_FREQ | ST_TURBINE,
 };
 
 // Per-scenario clock and controls, resident on the device.
@@ -76,6 +77,30 @@ struct MeshDev {
     const double *normal, *length, *area;
     const double *ls_matrix, *ls_weight, *ls_delta;
     const double *disp, *disp_unit, *disp_len, *distance;
+};
+
+// Rotor arrays on the device: the actuator sink and its diagnostics, and the
+// balanced-pressure / ambient-stress face terms of scenarios that have rotors.
+struct TurbDev {
+    int nr, np, nucell;
+    const int *hkt;             // (nscen) 1: the scenario has a rotor array
+    const int *stress;          // (nscen) 1: its ambient viscosity is positive
+    const int *rotor_sid;       // (nr)
+    const int *support_offset, *support_cell;       // (nr+1), (ns)
+    const double *support_weight, *support_density; // (ns)
+    const int *plane_offset, *plane_cell;           // (nr+1), (np)
+    const double *plane_delta;                      // (2, np)
+    const double *param;                            // (nr, 8)
+    const int *curve;                               // (nr, 4): thrust first, count; power first, count
+    const double *curve_x, *curve_y;
+    const int *ucell, *uoff, *uent;                 // unique support cells -> their entries, rotor order
+    const double *dxdy, *inverse, *xy, *mdisp, *nu; // (2,nadj) (3,nc) (2,nc) (4,nf) (nc)
+    double *grad;               // (8, nc) wet gradients: u, v, eta, b (x, y)
+    double *kcell;              // (ns) sink coefficient
+    double *raw;                // (2, nc) actuator momentum sink
+    double *trace;              // (10, nf) hydrostatically reconstructed face traces
+    double *pface, *sface;      // (2, nf) pressure correction, ambient stress
+    double *diag;               // (nr, 16) rotor diagnostics of the last sampled state
 };
 
 struct BoundaryDev {
@@ -175,6 +200,47 @@ __device__ __forceinline__ bool skip_stage(const Ctrl &c, int stage)
 __device__ __forceinline__ void raise_status(Ctrl &c, int stage, unsigned bits)
 {
     atomicOr(stage == 1 ? &c.status1 : &c.status2, bits);
+}
+
+// Face traces of the hydrostatically reconstructed states for the rotor
+// pressure correction (river_turbine_flow.h:39-52): surfaces, normal
+// velocities and speeds of both sides, the common bed, constant flags.
+__device__ __forceinline__ void put_trace(double *tr, int nf, int f, const double loc[8], bool cl, bool cr)
+{
+    const double hl = loc[0], hr = loc[4];
+    tr[f] = hl + loc[3]; tr[nf + f] = hr + loc[7];
+    tr[2 * nf + f] = hl > 0. ? loc[1] / hl : 0.; tr[3 * nf + f] = hr > 0. ? loc[5] / hr : 0.;
+    tr[4 * nf + f] = hl > 0. ? hypot(loc[1], loc[2]) / hl : 0.;
+    tr[5 * nf + f] = hr > 0. ? hypot(loc[5], loc[6]) / hr : 0.;
+    tr[6 * nf + f] = loc[3]; tr[7 * nf + f] = loc[7];
+    tr[8 * nf + f] = cl ? 1. : 0.; tr[9 * nf + f] = cr ? 1. : 0.;
+}
+
+// Momentum terms of a rotor array, in the reference's add_momentum order
+// (river_turbine_flow.py:230-239): ambient stress, actuator sink, balanced
+// pressure; face terms gathered as sum(s len flux) / area
+// (flow2dh_fixed_bed_kernels.h:54-60 with unit depth weights).
+__device__ __forceinline__ void add_rotor_momentum(const MeshDev &m, const TurbDev &t, int sid, int c, double area,
+                                                   double &r1, double &r2)
+{
+    const int nc = m.nc, nf = m.nf;
+    if (t.stress[sid]) {
+        double x = 0., y = 0.;
+        for (int k = m.offset[c]; k < m.offset[c + 1]; ++k) {
+            const int f = m.faces[k];
+            x += m.signs[k] * m.length[f] * t.sface[f];
+            y += m.signs[k] * m.length[f] * t.sface[nf + f];
+        }
+        r1 += 1. * x / area; r2 += 1. * y / area;
+    }
+    r1 += t.raw[c]; r2 += t.raw[nc + c];
+    double x = 0., y = 0.;
+    for (int k = m.offset[c]; k < m.offset[c + 1]; ++k) {
+        const int f = m.faces[k];
+        x += m.signs[k] * m.length[f] * t.pface[f];
+        y += m.signs[k] * m.length[f] * t.pface[nf + f];
+    }
+    r1 += 1. * x / area; r2 += 1. * y / area;
 }
 
 constexpr int BOUNDARY_TILES = 1024;   // tile slots of 64 faces per scenario (checked at set-up)

@@ -501,7 +501,8 @@ __device__ __forceinline__ Side face_side(const CellRec &r, double rx_, double r
 }
 
 template <class F>
-__global__ void __launch_bounds__(128) k_faces(MeshDev m, StateDev s, BoundaryDev b, Ctrl *ctrl, Work w, int stage)
+__global__ void __launch_bounds__(128) k_faces(MeshDev m, StateDev s, BoundaryDev b, Ctrl *ctrl, Work w, int stage,
+                                               double *trace, const int *hkt)
 {
     const int nf = m.nf, nc = m.nc;
     for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += gridDim.x * blockDim.x) {
@@ -563,6 +564,7 @@ __global__ void __launch_bounds__(128) k_faces(MeshDev m, StateDev s, BoundaryDe
                 loc[5] = hR > dry ? unR * (hr / hR) : 0.;
                 loc[6] = hR > dry ? utR * (hr / hR) : 0.;
             }
+            if (trace && n >= 0 && hkt[m.face_sid[f]]) put_trace(trace, nf, f, loc, rc.flags & 1, rn.flags & 1);
             bool closed = false;
             if (kind == 1 && !(fmin(rc.h, rn.h) > dry)) {
                 const double dc = m.distance[f], dn = m.distance[nf + f];
@@ -644,6 +646,10 @@ __global__ void __launch_bounds__(128) k_faces(MeshDev m, StateDev s, BoundaryDe
             if (!isfinite(l[0]) || !isfinite(l[1]) || !isfinite(l[2]) || !isfinite(r[0]) || !isfinite(r[1]) ||
                 !isfinite(r[2])) bad = 1;
             water = l[0]; l1 = l[1]; l2 = l[2]; r1 = r[1]; r2 = r[2];
+        }
+        if (kind == 0 && trace && n >= 0 && hkt[m.face_sid[f]]) {
+            const double zero[8] = {0., 0., 0., 0., 0., 0., 0., 0.};
+            put_trace(trace, nf, f, zero, rc.flags & 1, rn.flags & 1);
         }
         if (bad) raise_status(ct, stage, ST_SPATIAL);
         w.ws[f] = make_double2(water, speed);
@@ -739,11 +745,12 @@ __global__ void __launch_bounds__(256) k_limit(MeshDev m, StateDev s, Ctrl *ctrl
 // With rate_out set, the final rate is stored there and no state is written.
 template <class F>
 __global__ void __launch_bounds__(256) k_update(MeshDev m, StateDev s, Ctrl *ctrl, Work w, int stage,
-                                                double *rate_out)
+                                                double *rate_out, TurbDev t, int turb)
 {
     const int nc = m.nc;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
-        Ctrl &ct = ctrl[m.cell_sid[c]];
+        const int sid = m.cell_sid[c];
+        Ctrl &ct = ctrl[sid];
         if (skip_stage(ct, stage)) continue;
         const double area = m.area[c];
         double mass = 0., mx = 0., my = 0.;
@@ -753,7 +760,9 @@ __global__ void __launch_bounds__(256) k_update(MeshDev m, StateDev s, Ctrl *ctr
             const double4_32a L = w.lim[f];
             mass -= wt * L.x; mx -= wt * L.y; my -= wt * L.z;
         }
-        const double r0 = mass, r1 = w.rate[nc + c] + mx, r2 = w.rate[2 * nc + c] + my;
+        const double r0 = mass;
+        double r1 = w.rate[nc + c] + mx, r2 = w.rate[2 * nc + c] + my;
+        if (turb && t.hkt[sid]) add_rotor_momentum(m, t, sid, c, area, r1, r2);
         if (!isfinite(r0) || !isfinite(r1) || !isfinite(r2)) raise_status(ct, stage, ST_RATE);
         if (rate_out) { rate_out[c] = r0; rate_out[nc + c] = r1; rate_out[2 * nc + c] = r2; continue; }
         const double dt = ct.trial, dry = ct.dry;
@@ -794,6 +803,8 @@ __global__ void k_control(Ctrl *ctrl, int nscen)
     if (i >= nscen) return;
     Ctrl &c = ctrl[i];
     if (!c.active || c.done) return;
+    // a rotor outside its model's domain ends the scenario (the reference raises)
+    if ((c.status1 | c.status2) & ST_TURBINE) { c.failed = 4; c.done = 1; return; }
     const double f1 = bits_to_double(c.peak1), f2 = bits_to_double(c.peak2);
     // the reference's frequency peak only sees stages that reached the CFL evaluation
     double peak = 0.;

@@ -35,6 +35,8 @@ struct Launch {
     int grid_c, grid_f, grid_c256, grid_f256;
     cudaStream_t stream;
     MixedGeo mx;
+    TurbDev turb;            // rotor arrays (valid when has_turb)
+    int has_turb;
 };
 
 // Kernel kinds of one substep, in launch order within a stage.
@@ -42,6 +44,8 @@ enum KernelKind { K_DRAG = 0, K_BOUNDARY = 1, K_CELLS = 2, K_FACES = 3, K_GATHER
 // Mixed form only: first-stage primitives of a state placed in work, the
 // bed-derived tables, the limited water flux into a caller buffer.
 enum MixedAux { K_PRIM = 8, K_BED = 9, K_WATER = 10 };
+// Rotor-array terms of one stage (both forms; FP64 kernels of the FP64 unit).
+enum { K_TURB = 11 };
 
 // Mixed form (FP32 sweeps, FP64 stage pair, depth and mass): launch one kernel
 // of the given kind for the given stage; out is the rate buffer of K_UPDATE or

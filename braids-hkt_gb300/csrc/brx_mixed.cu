@@ -403,7 +403,7 @@ __device__ __forceinline__ float hydro_perturbation(float dh, float hL, float h,
 }
 
 __global__ void __launch_bounds__(128) km_faces(MeshDev m, StateDev s, BoundaryDev b, Ctrl *ctrl, Work w,
-                                                MixedGeo g, int stage)
+                                                MixedGeo g, int stage, TurbDev t, int turb)
 {
     const int nf = m.nf, nc = m.nc;
     const MxRec *rec = reinterpret_cast<const MxRec *>(w.rec);
@@ -478,6 +478,12 @@ __global__ void __launch_bounds__(128) km_faces(MeshDev m, StateDev s, BoundaryD
                 loc[2] = hL > dry ? utL * (hl / hL) : 0.f;
                 loc[5] = hR > dry ? unR * (hr / hR) : 0.f;
                 loc[6] = hR > dry ? utR * (hr / hR) : 0.f;
+                if (turb && t.hkt[m.face_sid[f]]) {
+                    // traces for the rotor pressure correction, beds made absolute in FP64
+                    const double zt = s.z[c] + double(top);
+                    const double l8[8] = {loc[0], loc[1], loc[2], zt, loc[4], loc[5], loc[6], zt};
+                    put_trace(t.trace, nf, f, l8, rc.flags & 1, rn.flags & 1);
+                }
             }
             bool closed = false;
             if (kind == 1 && !(fminf(hc, hn) > dry)) {
@@ -551,6 +557,10 @@ __global__ void __launch_bounds__(128) km_faces(MeshDev m, StateDev s, BoundaryD
             water = dl0;
             if (!isfinite(water) || !isfinite(gl1) || !isfinite(gl2) || !isfinite(gr1) || !isfinite(gr2)) bad = 1;
         } else {
+            if (turb && n >= 0 && t.hkt[m.face_sid[f]]) {
+                const double zero[8] = {0., 0., 0., 0., 0., 0., 0., 0.};
+                put_trace(t.trace, nf, f, zero, rc.flags & 1, rn.flags & 1);
+            }
             // dry face: zero flux, the cells' own pressure still enters the gather
             gl1 = -half_g * hc * hc * nx; gl2 = -half_g * hc * hc * ny;
             gr1 = -half_g * hn * hn * nx; gr2 = -half_g * hn * hn * ny;
@@ -687,14 +697,15 @@ __device__ __forceinline__ void drag_f(const Ctrl &ct, float dtf, double &h, dou
 }
 
 __global__ void __launch_bounds__(256) km_update(MeshDev m, StateDev s, Ctrl *ctrl, Work w, MixedGeo g, int stage,
-                                                 double *rate_out)
+                                                 double *rate_out, TurbDev t, int turb)
 {
     const int nc = m.nc;
     const MxLim *lim = reinterpret_cast<const MxLim *>(w.lim);
     const float *rate32 = reinterpret_cast<const float *>(w.rate);
     MxPrim *P2 = reinterpret_cast<MxPrim *>(g.prim[1]);
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
-        Ctrl &ct = ctrl[m.cell_sid[c]];
+        const int sid = m.cell_sid[c];
+        Ctrl &ct = ctrl[sid];
         if (mx_skip(ct, stage)) continue;
         double mass = 0.;
         float mx = 0.f, my = 0.f;
@@ -705,13 +716,14 @@ __global__ void __launch_bounds__(256) km_update(MeshDev m, StateDev s, Ctrl *ct
             mx -= wk * L.cx;
             my -= wk * L.cy;
         }
-        const float r1 = rate32[c] + mx, r2 = rate32[nc + c] + my;
-        if (!finite64(mass) || !isfinite(r1) || !isfinite(r2)) raise_status(ct, stage, ST_RATE);
-        if (rate_out) { rate_out[c] = mass; rate_out[nc + c] = double(r1); rate_out[2 * nc + c] = double(r2); continue; }
+        double r1 = double(rate32[c] + mx), r2 = double(rate32[nc + c] + my);
+        if (turb && t.hkt[sid]) add_rotor_momentum(m, t, sid, c, m.area[c], r1, r2);
+        if (!finite64(mass) || !finite64(r1) || !finite64(r2)) raise_status(ct, stage, ST_RATE);
+        if (rate_out) { rate_out[c] = mass; rate_out[nc + c] = r1; rate_out[2 * nc + c] = r2; continue; }
         const double dt = ct.trial, dry = ct.dry;
         if (stage == 1) {
             const double h = s.work[c] + dt * mass;
-            double hu = s.work[nc + c] + dt * double(r1), hv = s.work[2 * nc + c] + dt * double(r2);
+            double hu = s.work[nc + c] + dt * r1, hv = s.work[2 * nc + c] + dt * r2;
             if (h < 0) raise_status(ct, 1, ST_ENDPOINT);
             if (h <= dry) { hu = 0.; hv = 0.; }
             s.q1[c] = h; s.q1[nc + c] = hu; s.q1[2 * nc + c] = hv;
@@ -719,8 +731,8 @@ __global__ void __launch_bounds__(256) km_update(MeshDev m, StateDev s, Ctrl *ct
             if (!put_prim(P2, c, h, hu, hv, s.z[c], dry) && !(h < 0)) raise_status(ct, 2, ST_SPATIAL);
         } else {
             double h = .5 * s.work[c] + .5 * (s.q1[c] + dt * mass);
-            double hu = .5 * s.work[nc + c] + .5 * (s.q1[nc + c] + dt * double(r1));
-            double hv = .5 * s.work[2 * nc + c] + .5 * (s.q1[2 * nc + c] + dt * double(r2));
+            double hu = .5 * s.work[nc + c] + .5 * (s.q1[nc + c] + dt * r1);
+            double hv = .5 * s.work[2 * nc + c] + .5 * (s.q1[2 * nc + c] + dt * r2);
             if (!finite64(h) || !finite64(hu) || !finite64(hv) || h < 0) raise_status(ct, 2, ST_ENDPOINT);
             if (h <= dry) { hu = 0.; hv = 0.; }
             drag_f(ct, .5f * ct.trialf, h, hu, hv);
@@ -791,7 +803,8 @@ int mixed_kernel(const Launch &L, int kind, int stage, double *out)
         else brx_mx::km_cells<MAX_CELL_FACES><<<L.grid_c, 128, 0, st>>>(L.mesh, L.state, L.ctrl, L.work, L.mx, stage);
         return 1;
     case K_FACES:
-        brx_mx::km_faces<<<L.grid_f, 128, 0, st>>>(L.mesh, L.state, L.bnd, L.ctrl, L.work, L.mx, stage);
+        brx_mx::km_faces<<<L.grid_f, 128, 0, st>>>(L.mesh, L.state, L.bnd, L.ctrl, L.work, L.mx, stage, L.turb,
+                                                    L.has_turb);
         return 1;
     case K_GATHER:
         brx_mx::km_gather<<<L.grid_c256, 256, 0, st>>>(L.mesh, L.state, L.ctrl, L.work, L.mx, stage);
@@ -800,7 +813,8 @@ int mixed_kernel(const Launch &L, int kind, int stage, double *out)
         brx_mx::km_limit<<<L.grid_f256, 256, 0, st>>>(L.mesh, L.ctrl, L.work, L.mx, stage);
         return 1;
     case K_UPDATE:
-        brx_mx::km_update<<<L.grid_c256, 256, 0, st>>>(L.mesh, L.state, L.ctrl, L.work, L.mx, stage, out);
+        brx_mx::km_update<<<L.grid_c256, 256, 0, st>>>(L.mesh, L.state, L.ctrl, L.work, L.mx, stage, out, L.turb,
+                                                     L.has_turb);
         return 1;
     case K_PRIM:
         brx_mx::km_prim<<<L.grid_c256, 256, 0, st>>>(L.mesh, L.state, L.ctrl, L.mx);

@@ -143,6 +143,17 @@ class RiverSolver:
         self.z = torch.from_numpy(p["z"]).to(dev).contiguous()
         check(self.lib.brx_state_bind(self.h, C.c_void_p(self.q.data_ptr()), C.c_void_p(self.z.data_ptr())))
         check(self.lib.brx_graph_chunk_set(self.h, int(graph_chunk)))
+        self.rotors = None
+        from . import turbines as TB
+        tp = TB.pack(self.cases, p["cell_offset"])
+        if tp is not None:
+            self.rotors = tp
+            check(self.lib.brx_turbines_set(
+                self.h, tp["nrotor"], _ptr(tp["scenario"]), _ptr(tp["param"]), _ptr(tp["curve"]),
+                len(tp["curve_x"]), _ptr(tp["curve_x"]), _ptr(tp["curve_y"]), _ptr(tp["support_offset"]),
+                _ptr(tp["support_cell"]), _ptr(tp["support_weight"]), _ptr(tp["support_density"]),
+                _ptr(tp["plane_offset"]), _ptr(tp["plane_cell"]), _ptr(tp["plane_delta"]), _ptr(tp["dxdy"]),
+                _ptr(tp["inverse"]), _ptr(tp["xy"]), _ptr(tp["mid_disp"]), _ptr(tp["nu"]), _ptr(tp["hkt"])))
         self.time = np.zeros(self.nscen)
         self.steps = 0
 
@@ -164,6 +175,33 @@ class RiverSolver:
 
     def launches(self):
         return int(self.lib.brx_launch_count(self.h))
+
+    # --- rotor arrays ---------------------------------------------------
+    def turbine_record(self, last=False):
+        """(nrotor, 16) rotor record of the current state (or of the last evaluated stage)."""
+        from . import turbines as TB
+        if self.rotors is None:
+            raise ValueError("no rotor arrays")
+        self.torch.cuda.current_stream().synchronize()
+        out = np.zeros((self.rotors["nrotor"], TB.NDIAG))
+        fn = self.lib.brx_turbines_last if last else self.lib.brx_turbines_diagnose
+        check(fn(self.h, _ptr(out)))
+        return out
+
+    def turbines(self, scenario=None):
+        """Per-rotor diagnostics of the current state (the reference's hkt_diagnose),
+        with thrust [N] and power [W] at water density 1000 kg/m3."""
+        from . import turbines as TB
+        rec = self.turbine_record()
+        rows = TB.diagnostics_rows(rec, self.rotors["names"])
+        for row, sid in zip(rows, self.rotors["scenario"]):
+            row["scenario"] = int(sid)
+            err = int(row["error"])
+            if err:
+                raise ValueError(f"rotor {row['turbine_id']}: {TB.ERRORS.get(err, 'model error')}")
+        if scenario is not None:
+            rows = [r for r in rows if r["scenario"] == scenario]
+        return rows
 
     def set_forcing_table(self, time, value):
         """value (2, nseg, len): discharge and stage tables for every segment."""
@@ -274,7 +312,8 @@ def kahan_sum(values):
 
 def _profile(self, dt, time=0.0):
     """Per-kernel durations (ms) of one trial launched without a graph: [(kernel name, ms), ...]."""
-    names = ["drag", "boundary", "cells", "faces", "gather", "limit", "update", "control"]
+    names = {0: "drag", 1: "boundary", 2: "cells", 3: "faces", 4: "gather", 5: "limit", 6: "update",
+             7: "control", 11: "rotors"}
     self.torch.cuda.current_stream().synchronize()
     cap = 64
     ms = np.zeros(cap)

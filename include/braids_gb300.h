@@ -43,6 +43,7 @@ extern "C" {
 #define BRX_ST_ENDPOINT 8u
 #define BRX_ST_FREQ 16u
 #define BRX_ST_CFL 32u      /* dt * max frequency above the CFL target */
+#define BRX_ST_TURBINE 64u  /* rotor model outside its domain: the scenario fails (failed = 4) */
 
 typedef struct brx_solver brx_solver;
 
@@ -52,7 +53,7 @@ typedef struct brx_solver brx_solver;
 typedef struct {
     int substeps;        /* accepted SSPRK(2,2) substeps */
     int rejections;      /* rejected trials */
-    int failed;          /* 0 ok, 1 dt floor / rejection limit, 2 substep limit */
+    int failed;          /* 0 ok, 1 dt floor / rejection limit, 2 substep limit, 4 rotor model error */
     int pad;
     double min_dt, max_dt, accepted_cfl_max, hint;
 } brx_advance_stats;
@@ -134,6 +135,45 @@ int brx_rate(brx_solver *s, double dt, double time, double *rate_device, double 
  * nonzero = active). All scenarios are active after creation. */
 int brx_scenarios_activate(brx_solver *s, const int *active);
 
+/* Rotor arrays (replaces the reference's river_turbine_flow.install with a
+ * ThetisArray, src/braids_core/sediment/river_turbine_flow.py:222-252 and
+ * river_turbine_thetis.py:300-318). Called once, after brx_solver_create.
+ *   rotor_scenario (nrotor)      owning scenario of each rotor
+ *   param (nrotor, 8)            D, hub elevation, minimum bed clearance,
+ *                                minimum surface clearance, gate tolerance,
+ *                                control mode (0 constant Ct, 1 speed table,
+ *                                2 incident-speed table, 3 incident-speed
+ *                                curves), Ct and Cp of the constant mode
+ *   curve (nrotor, 4)            first index and count of the thrust (Ct) and
+ *                                power (Cp) tables in curve_x / curve_y
+ *   support_offset (nrotor+1), support_cell, support_weight, support_density
+ *                                footprint cells (global ids), normalized bump
+ *                                weights, bump density integrals
+ *   plane_offset (nrotor+1), plane_cell, plane_delta (2, np)
+ *                                rotor-plane crossings and their displacement
+ *                                from the cell centroid
+ *   dxdy (2, nadj), inverse (3, nc), xy (2, nc), mid_disp (4, nf)
+ *                                the flow engines' least-squares metric
+ *                                (bend_methods_v1.py:100-128)
+ *   nu (nc)                      ambient eddy viscosity
+ *   hkt (nscen)                  1 where the scenario has a rotor array
+ * All arrays are host memory, copied. */
+int brx_turbines_set(brx_solver *s, int nrotor, const int *rotor_scenario, const double *param,
+                     const int *curve, int ncurve, const double *curve_x, const double *curve_y,
+                     const int *support_offset, const int *support_cell, const double *support_weight,
+                     const double *support_density, const int *plane_offset, const int *plane_cell,
+                     const double *plane_delta, const double *dxdy, const double *inverse, const double *xy,
+                     const double *mid_disp, const double *nu, const int *hkt);
+
+/* Rotor diagnostics (nrotor, 16 doubles, host) of the bound state
+ * (hkt_diagnose: river_turbine_flow.py:240-241): active, inactive reason,
+ * coverage margin, bed clearance, local speed, upstream speed, mean depth,
+ * Ct, Cp, force/rho [m4/s2], useful power/rho [m5/s3], removed power/rho,
+ * lowest rotor-plane surface, highest bed, error code, reserved. */
+int brx_turbines_diagnose(brx_solver *s, double *out);
+/* The same record for the state of the last evaluated stage. */
+int brx_turbines_last(brx_solver *s, double *out);
+
 /* Step hint carried between brx_advance calls (nscen, host; <= 0 = none). */
 int brx_hint_get(brx_solver *s, double *hint);
 int brx_hint_set(brx_solver *s, const double *hint);
@@ -144,7 +184,8 @@ int brx_graph_chunk_set(brx_solver *s, int substeps);
 /* Time one SSPRK(2,2) trial of exactly dt kernel by kernel with CUDA events
  * on the solver stream (no graph). ms (cap entries) gets each launch's
  * duration and kind (cap entries) its kernel: 0 drag, 1 boundary, 2 cells,
- * 3 faces, 4 gather, 5 limit, 6 update, 7 control. *count gets the number
+ * 3 faces, 4 gather, 5 limit, 6 update, 7 control, 11 rotor terms (four
+ * kernels timed together). *count gets the number
  * of launches. The bound state is advanced as by brx_substep. */
 int brx_profile_substep(brx_solver *s, double dt, double time, int cap, double *ms, int *kind, int *count);
 
