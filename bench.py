@@ -55,11 +55,13 @@ def build_workload(name, rank=0, world=1):
         params = S.config4_params(64, seed=4 + rank)
         workers = max(1, (os.cpu_count() or 1) // max(world, 1))
         cases = S.build_cases(params, workers)
+        rotors = sum(len(c.get("turbines", [])) for c in cases)
         return cases, "mixed", 0.5, dict(
             workload="config4: 64 channel scenarios in one batch, cells logU(1e4,5e5), width U(100,400) m, "
                      "Q U(100,1500) m3/s, length 10 widths, jittered Delaunay, Manning 0.03, CFL 0.9, "
-                     "mixed FP32/FP64 form, no turbines",
-            scenarios=len(cases))
+                     "0-8 rotors each (D 5 m, Ct 0.8, rated 500 kW incident-speed curves, >= 5 D apart, "
+                     "1.5 m refined footprints), mixed FP32/FP64 form",
+            scenarios=len(cases), rotors=rotors)
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -286,6 +288,7 @@ def main():
     value = updates / t_max
 
     state_after_timed = solver.q.cpu().numpy()       # for the accuracy check against FP64 below
+    rotors_after_timed = solver.turbine_record() if solver.rotors is not None else None
     sim_after_timed = sim_time
     # end to end through the public API with host buffers: H2D of the step's
     # input state from pinned memory, advance, D2H of the result
@@ -334,9 +337,15 @@ def main():
     # intervals: FP64 throughput and the mixed form's depth error against it
     plain = None
     if precision == "mixed" and args.plain > 0:
-        order = np.argsort([c["mesh"].nc for c in cases])
+        # smallest / median / largest scenario among those with rotors (all, without rotors)
+        pool = [i for i, c in enumerate(cases) if c.get("turbines")] or list(range(len(cases)))
+        order = sorted(pool, key=lambda i: cases[i]["mesh"].nc)
         pick = [int(order[0]), int(order[len(order) // 2]), int(order[-1])][:args.plain]
-        p_updates, p_ms, errs = 0, 0.0, []
+        p_updates, p_ms, errs, perr = 0, 0.0, [], []
+        rotor_first = {}
+        if solver.rotors is not None:
+            for k, sid in enumerate(solver.rotors["scenario"]):
+                rotor_first.setdefault(int(sid), []).append(k)
         batch_state = state_after_timed
         off = solver.packed["cell_offset"]
         nsteps = args.warmup + args.steps
@@ -359,13 +368,21 @@ def main():
             hmx = batch_state[0, off[i]:off[i + 1]]
             rel = np.abs(hmx - h64) / np.maximum(h64, 1e-3)
             errs.append((float(rel.max()), float(np.percentile(rel, 99))))
+            if one.rotors is not None and i in rotor_first:
+                import braids_hkt_gb300.turbines as TB
+                col = TB.DIAG_FIELDS.index("useful_power_per_density_m5_s3")
+                p64 = one.turbine_record()[:, col]
+                pmx = rotors_after_timed[rotor_first[i], col]
+                perr += [float(abs(a - b) / max(abs(b), 1e-30)) for a, b in zip(pmx, p64) if b != 0]
             one.close()
         plain = {"value": p_updates / (p_ms / 1e3), "unit": METRIC, "scenarios": pick,
                  "cells": [int(cases[i]["mesh"].nc) for i in pick],
                  "note": "each scenario alone in the FP64 form over the same intervals"}
         cfg["accuracy_vs_fp64"] = {"depth_rel_max": max(e[0] for e in errs), "depth_rel_p99": max(e[1] for e in errs),
                                    "scenarios": pick, "after_sim_s": nsteps * outer,
-                                   "stated_tolerance": 1e-4}
+                                   "stated_tolerance": 1e-4,
+                                   "rotor_power_rel_max": max(perr) if perr else None,
+                                   "rotors_compared": len(perr)}
     if rank != 0:
         return
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,

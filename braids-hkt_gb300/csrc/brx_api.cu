@@ -579,16 +579,39 @@ extern "C" int brx_turbines_set(brx_solver *s, int nrotor, const int *rotor_scen
     t.param = p_param; t.curve = p_curve; t.curve_x = p_cx; t.curve_y = p_cy;
     t.ucell = p_ucell; t.uoff = p_uoff; t.uent = p_uent;
     t.dxdy = p_dxdy; t.inverse = p_inv; t.xy = p_xy; t.mdisp = p_md; t.nu = p_nu;
-    TRY(s->alloc(&t.grad, 8 * (size_t)nc)); TRY(s->alloc(&t.kcell, ns)); TRY(s->alloc(&t.raw, 2 * (size_t)nc));
-    TRY(s->alloc(&t.trace, 10 * (size_t)nf)); TRY(s->alloc(&t.pface, 2 * (size_t)nf));
-    TRY(s->alloc(&t.sface, 2 * (size_t)nf)); TRY(s->alloc(&t.diag, (size_t)nrotor * TD_N));
-    TRY(s->alloc(&s->d_tdiag_out, (size_t)nrotor * TD_N));
+    TRY(s->alloc(&t.kcell, ns)); TRY(s->alloc(&t.raw, 2 * (size_t)nc));
+    TRY(s->alloc(&t.diag, (size_t)nrotor * TD_N)); TRY(s->alloc(&s->d_tdiag_out, (size_t)nrotor * TD_N));
     CK(cudaMemset(t.raw, 0, sizeof(double) * 2 * (size_t)nc));
-    CK(cudaMemset(t.grad, 0, sizeof(double) * 8 * (size_t)nc));
-    CK(cudaMemset(t.trace, 0, sizeof(double) * 10 * (size_t)nf));
-    CK(cudaMemset(t.pface, 0, sizeof(double) * 2 * (size_t)nf));
-    CK(cudaMemset(t.sface, 0, sizeof(double) * 2 * (size_t)nf));
     CK(cudaMemset(t.diag, 0, sizeof(double) * (size_t)nrotor * TD_N));
+    if (s->precision == BRX_MIXED) {
+        // FP32 flow metric and face-term buffers of the mixed form
+        std::vector<float2> hdxy(nadj), hcc(nf);
+        std::vector<float4> hmd(nf);
+        for (int k = 0; k < nadj; ++k) hdxy[k] = make_float2(float(dxdy[k]), float(dxdy[nadj + k]));
+        for (int f = 0; f < nf; ++f) {
+            hmd[f] = make_float4(float(mid_disp[f]), float(mid_disp[nf + f]), float(mid_disp[2 * (size_t)nf + f]),
+                                 float(mid_disp[3 * (size_t)nf + f]));
+            const int a = s->h_owner[f], b = s->h_neighbour[f];
+            hcc[f] = b >= 0 ? make_float2(float(xy[b] - xy[a]), float(xy[nc + b] - xy[nc + a])) : make_float2(0.f, 0.f);
+        }
+        float2 *p_hdxy, *p_hcc;
+        float4 *p_hmd;
+        TRY(s->upload(&p_hdxy, hdxy.data(), nadj)); TRY(s->upload(&p_hcc, hcc.data(), nf));
+        TRY(s->upload(&p_hmd, hmd.data(), nf));
+        s->mx.hdxy = p_hdxy; s->mx.hcc = p_hcc; s->mx.hmd = p_hmd;
+        TRY(s->alloc(&s->mx.htr, 2 * (size_t)nf)); TRY(s->alloc(&s->mx.hgrad, 6 * (size_t)nc));
+        TRY(s->alloc(&s->mx.hp, nf)); TRY(s->alloc(&s->mx.hs, nf));
+        CK(cudaMemset(s->mx.htr, 0, sizeof(float4) * 2 * (size_t)nf));
+        CK(cudaMemset(s->mx.hgrad, 0, sizeof(float) * 6 * (size_t)nc));
+        CK(cudaMemset(s->mx.hp, 0, sizeof(float2) * nf)); CK(cudaMemset(s->mx.hs, 0, sizeof(float2) * nf));
+    } else {
+        TRY(s->alloc(&t.grad, 8 * (size_t)nc)); TRY(s->alloc(&t.trace, 10 * (size_t)nf));
+        TRY(s->alloc(&t.pface, 2 * (size_t)nf)); TRY(s->alloc(&t.sface, 2 * (size_t)nf));
+        CK(cudaMemset(t.grad, 0, sizeof(double) * 8 * (size_t)nc));
+        CK(cudaMemset(t.trace, 0, sizeof(double) * 10 * (size_t)nf));
+        CK(cudaMemset(t.pface, 0, sizeof(double) * 2 * (size_t)nf));
+        CK(cudaMemset(t.sface, 0, sizeof(double) * 2 * (size_t)nf));
+    }
     s->turb = t;
     s->has_turb = true;
     s->nrotor = nrotor;
@@ -605,10 +628,10 @@ extern "C" int brx_turbines_diagnose(brx_solver *s, double *out)
     if (!out) return fail(BRX_ERR_ARGUMENT, "null output");
     const TurbDev &t = s->turb;
     CK(cudaMemcpyAsync(s->d_ctrl, s->h_ctrl, sizeof(Ctrl) * s->nscen, cudaMemcpyHostToDevice, s->stream));
-    k_hkt_gradients<<<s->grid_c256, 256, 0, s->stream>>>(s->mesh, t, s->state.q[0], s->state.z, s->d_ctrl, 0);
+    // the sample forms its rotor-plane gradients itself (FP64, both forms)
     k_turbine_sample<<<t.nr, TURB_THREADS, 0, s->stream>>>(s->mesh, t, s->state.q[0], s->state.z, s->d_ctrl, 0,
                                                            s->d_tdiag_out);
-    s->launches += 2;
+    s->launches += 1;
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(out, s->d_tdiag_out, sizeof(double) * (size_t)s->nrotor * TD_N, cudaMemcpyDeviceToHost,
                        s->stream));
@@ -678,10 +701,13 @@ static int launch_turbines(brx_solver *s, int stage, cudaStream_t st)
     if (!s->has_turb) return 0;
     const double *q = stage == 1 ? s->state.work : s->state.q1;
     const TurbDev &t = s->turb;
-    k_hkt_gradients<<<s->grid_c256, 256, 0, st>>>(s->mesh, t, q, s->state.z, s->d_ctrl, stage);
+    const bool mixed = s->precision == BRX_MIXED;
+    if (mixed) mixed_kernel(make_launch(s, st), K_HKT_GRAD, stage, nullptr);
+    else k_hkt_gradients<<<s->grid_c256, 256, 0, st>>>(s->mesh, t, q, s->state.z, s->d_ctrl, stage);
     k_turbine_sample<<<t.nr, TURB_THREADS, 0, st>>>(s->mesh, t, q, s->state.z, s->d_ctrl, stage, t.diag);
     k_turbine_raw<<<std::max(1, std::min((t.nucell + 255) / 256, s->sms * 8)), 256, 0, st>>>(s->mesh, t, q, s->d_ctrl, stage);
-    k_hkt_faces<<<s->grid_f, 128, 0, st>>>(s->mesh, t, q, s->state.z, s->d_ctrl, stage);
+    if (mixed) mixed_kernel(make_launch(s, st), K_HKT_FACES, stage, nullptr);
+    else k_hkt_faces<<<s->grid_f, 128, 0, st>>>(s->mesh, t, q, s->state.z, s->d_ctrl, stage);
     return 4;
 }
 

@@ -23,6 +23,13 @@ struct MixedGeo {
     float2 *gbed;            // (nc) limited bed gradient
     // FP32 primitives of the two stage inputs (32 bytes per cell each)
     float4 *prim[2];
+    // rotor arrays: FP32 flow metric and face terms
+    const float2 *hdxy;      // (nadj) centre offsets of the flow least-squares metric
+    const float4 *hmd;       // (nf) face-midpoint displacement: owner x, y; neighbour x, y
+    const float2 *hcc;       // (nf) neighbour centroid - owner centroid
+    float4 *htr;             // (2 nf) face traces: (hl, hr, common bed, constant flags), (un_l, un_r, |u|_l, |u|_r)
+    float *hgrad;            // (6, nc) wet gradients of u, v, eta
+    float2 *hp, *hs;         // (nf) balanced-pressure correction, ambient stress
 };
 
 struct Launch {
@@ -43,7 +50,7 @@ struct Launch {
 enum KernelKind { K_DRAG = 0, K_BOUNDARY = 1, K_CELLS = 2, K_FACES = 3, K_GATHER = 4, K_LIMIT = 5, K_UPDATE = 6 };
 // Mixed form only: first-stage primitives of a state placed in work, the
 // bed-derived tables, the limited water flux into a caller buffer.
-enum MixedAux { K_PRIM = 8, K_BED = 9, K_WATER = 10 };
+enum MixedAux { K_PRIM = 8, K_BED = 9, K_WATER = 10, K_HKT_GRAD = 12, K_HKT_FACES = 13 };
 // Rotor-array terms of one stage (both forms; FP64 kernels of the FP64 unit).
 enum { K_TURB = 11 };
 

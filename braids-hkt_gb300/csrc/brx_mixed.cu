@@ -479,10 +479,12 @@ __global__ void __launch_bounds__(128) km_faces(MeshDev m, StateDev s, BoundaryD
                 loc[5] = hR > dry ? unR * (hr / hR) : 0.f;
                 loc[6] = hR > dry ? utR * (hr / hR) : 0.f;
                 if (turb && t.hkt[m.face_sid[f]]) {
-                    // traces for the rotor pressure correction, beds made absolute in FP64
-                    const double zt = s.z[c] + double(top);
-                    const double l8[8] = {loc[0], loc[1], loc[2], zt, loc[4], loc[5], loc[6], zt};
-                    put_trace(t.trace, nf, f, l8, rc.flags & 1, rn.flags & 1);
+                    // traces for the rotor pressure correction (beds relative to the owner's)
+                    const int fl = (rc.flags & 1) | ((rn.flags & 1) << 1);
+                    g.htr[f] = make_float4(hl, hr, top, __int_as_float(fl));
+                    g.htr[nf + f] = make_float4(hl > 0.f ? loc[1] / hl : 0.f, hr > 0.f ? loc[5] / hr : 0.f,
+                                                hl > 0.f ? hypotf(loc[1], loc[2]) / hl : 0.f,
+                                                hr > 0.f ? hypotf(loc[5], loc[6]) / hr : 0.f);
                 }
             }
             bool closed = false;
@@ -558,8 +560,9 @@ __global__ void __launch_bounds__(128) km_faces(MeshDev m, StateDev s, BoundaryD
             if (!isfinite(water) || !isfinite(gl1) || !isfinite(gl2) || !isfinite(gr1) || !isfinite(gr2)) bad = 1;
         } else {
             if (turb && n >= 0 && t.hkt[m.face_sid[f]]) {
-                const double zero[8] = {0., 0., 0., 0., 0., 0., 0., 0.};
-                put_trace(t.trace, nf, f, zero, rc.flags & 1, rn.flags & 1);
+                const int fl = (rc.flags & 1) | ((rn.flags & 1) << 1);
+                g.htr[f] = make_float4(0.f, 0.f, 0.f, __int_as_float(fl));
+                g.htr[nf + f] = make_float4(0.f, 0.f, 0.f, 0.f);
             }
             // dry face: zero flux, the cells' own pressure still enters the gather
             gl1 = -half_g * hc * hc * nx; gl2 = -half_g * hc * hc * ny;
@@ -717,7 +720,19 @@ __global__ void __launch_bounds__(256) km_update(MeshDev m, StateDev s, Ctrl *ct
             my -= wk * L.cy;
         }
         double r1 = double(rate32[c] + mx), r2 = double(rate32[nc + c] + my);
-        if (turb && t.hkt[sid]) add_rotor_momentum(m, t, sid, c, m.area[c], r1, r2);
+        if (turb && t.hkt[sid]) {
+            // ambient stress, actuator sink, balanced pressure (the reference's add_momentum order)
+            const int k0 = m.offset[c], k1 = m.offset[c + 1];
+            if (t.stress[sid]) {
+                float x = 0.f, y = 0.f;
+                for (int k = k0; k < k1; ++k) { const float2 v = g.hs[m.faces[k]]; x += g.cw4[k] * v.x; y += g.cw4[k] * v.y; }
+                r1 += double(x); r2 += double(y);
+            }
+            r1 += t.raw[c]; r2 += t.raw[nc + c];
+            float x = 0.f, y = 0.f;
+            for (int k = k0; k < k1; ++k) { const float2 v = g.hp[m.faces[k]]; x += g.cw4[k] * v.x; y += g.cw4[k] * v.y; }
+            r1 += double(x); r2 += double(y);
+        }
         if (!finite64(mass) || !finite64(r1) || !finite64(r2)) raise_status(ct, stage, ST_RATE);
         if (rate_out) { rate_out[c] = mass; rate_out[nc + c] = r1; rate_out[2 * nc + c] = r2; continue; }
         const double dt = ct.trial, dry = ct.dry;
@@ -778,6 +793,115 @@ __global__ void km_water_out(MeshDev m, Work w, double *water)
     for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < m.nf; f += gridDim.x * blockDim.x) water[f] = lim[f].water;
 }
 
+// ---------------------------------------------------------------------------
+// Rotor arrays in the mixed form: FP32 wet gradients and face terms
+// (river_turbine_flow.h:13-82, river_hydrokinetic_stress.h:13-35)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) km_hkt_gradients(MeshDev m, Ctrl *ctrl, MixedGeo g, TurbDev t, int stage)
+{
+    const int nc = m.nc;
+    const MxPrim *P = reinterpret_cast<const MxPrim *>(stage == 1 ? g.prim[0] : g.prim[1]);
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        const int sid = m.cell_sid[c];
+        if (!t.hkt[sid]) continue;
+        const Ctrl &ct = ctrl[sid];
+        if (mx_skip(ct, stage)) continue;
+        const MxPrim pc = P[c];
+        float xx = 0.f, xy = 0.f, yy = 0.f, bx[3] = {0.f, 0.f, 0.f}, by[3] = {0.f, 0.f, 0.f};
+        if (pc.wet)
+            for (int k = m.offset[c]; k < m.offset[c + 1]; ++k) {
+                const int n = g.cidx[k].x;
+                if (n < 0) continue;
+                const MxPrim pn = P[n];
+                if (!pn.wet) continue;
+                const float2 d = g.hdxy[k];
+                const float w = 1.f / (d.x * d.x + d.y * d.y);
+                xx += w * d.x * d.x; xy += w * d.x * d.y; yy += w * d.y * d.y;
+                const float dv[3] = {pn.u - pc.u, pn.v - pc.v, (pn.ehi - pc.ehi) + (pn.elo - pc.elo)};
+#pragma unroll
+                for (int p = 0; p < 3; ++p) { bx[p] += w * d.x * dv[p]; by[p] += w * d.y * dv[p]; }
+            }
+        const float det = xx * yy - xy * xy;
+        const bool solve = det > 1e-6f * fmaxf(1.f, xx * yy);
+#pragma unroll
+        for (int p = 0; p < 3; ++p) {
+            g.hgrad[(2 * p) * nc + c] = solve ? (yy * bx[p] - xy * by[p]) / det : 0.f;
+            g.hgrad[(2 * p + 1) * nc + c] = solve ? (xx * by[p] - xy * bx[p]) / det : 0.f;
+        }
+    }
+}
+
+// Heights relative to the owner's bed. The hydrostatic part of the pressure
+// correction is written in difference form,
+//   1/4 g [(hl-ha)(hl+ha) + (hr-hb)(hr+hb)] + 1/4 g (da-db)/d (ha-hb)(ha+hb)
+//   + 1/4 g [ca (ha-hl)(ha+hl) + cb (hb-hr)(hb+hr)]
+// (algebraically the reference's 1/2 (po + pn) - 1/2 g (wa ha^2 + wb hb^2)),
+// so a surface at rest gives exactly zero and FP32 carries only the small
+// differences.
+__global__ void __launch_bounds__(128) km_hkt_faces(MeshDev m, Ctrl *ctrl, MixedGeo g, TurbDev t, int stage)
+{
+    const int nf = m.nf, nc = m.nc;
+    const MxPrim *P = reinterpret_cast<const MxPrim *>(stage == 1 ? g.prim[0] : g.prim[1]);
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += gridDim.x * blockDim.x) {
+        const int sid = m.face_sid[f];
+        if (!t.hkt[sid]) continue;
+        const Ctrl &ct = ctrl[sid];
+        if (mx_skip(ct, stage)) continue;
+        const float gravity = ct.gravf, dry = ct.dryf;
+        const int a = m.owner[f], b = m.neighbour[f];
+        float2 pr = make_float2(0.f, 0.f), st = make_float2(0.f, 0.f);
+        if (b >= 0) {
+            const MxPrim pa = P[a], pb = P[b];
+            if (pa.wet && pb.wet) {
+                const float2 nn = g.fnorm[f], di = g.fdist[f];
+                const float nx = nn.x, ny = nn.y, da = di.x, db = di.y, d = da + db, wa = db / d, wb = da / d;
+                const float zb = g.fdb[f];
+                const float ea = pa.h, eb = pa.h + ((pb.ehi - pa.ehi) + (pb.elo - pa.elo));
+                if (t.stress[sid]) {
+                    float h = fminf(pa.h, pb.h);
+                    h = fminf(h, fmaxf(0.f, .5f * (ea + eb) - fmaxf(0.f, zb)));
+                    const float visc = wa * float(t.nu[a]) + wb * float(t.nu[b]);
+                    const float2 dd = g.hcc[f];
+                    const float dn = dd.x * nx + dd.y * ny;
+                    const float du = pb.u - pa.u, dv = pb.v - pa.v;
+                    const float *G = g.hgrad;
+                    float ux = wa * G[a] + wb * G[b], uy = wa * G[nc + a] + wb * G[nc + b];
+                    float vx = wa * G[2 * nc + a] + wb * G[2 * nc + b], vy = wa * G[3 * nc + a] + wb * G[3 * nc + b];
+                    const float cu = (du - ux * dd.x - uy * dd.y) / dn, cv = (dv - vx * dd.x - vy * dd.y) / dn;
+                    ux += cu * nx; uy += cu * ny; vx += cv * nx; vy += cv * ny;
+                    st = make_float2(visc * h * (2.f * ux * nx + (uy + vx) * ny), visc * h * ((uy + vx) * nx + 2.f * vy * ny));
+                }
+                const float4 t0 = g.htr[f], t1 = g.htr[nf + f];
+                const int cf = __float_as_int(t0.w);
+                const float top = t0.z, bed = fmaxf(fmaxf(0.f, zb), top);
+                const float ha = fmaxf(0.f, ea - bed), hb = fmaxf(0.f, eb - bed);
+                const float hl = fmaxf(0.f, (top + t0.x) - bed), hr = fmaxf(0.f, (top + t0.y) - bed);
+                const float h = .5f * (hl + hr);
+                const float qg = .25f * gravity;
+                const float ca = (cf & 1) ? qg * __fmul_rn(ha - hl, ha + hl) : 0.f;
+                const float cb = (cf & 2) ? qg * __fmul_rn(hb - hr, hb + hr) : 0.f;
+                const float scale = qg * (hl * hl + hr * hr);                       // |po|, |pn| to first order
+                if (!(fminf(fminf(ha, hb), fminf(hl, hr)) <= dry) && !(fabsf(hr - hl) > .005f * h) &&
+                    !(fabsf(2.f * (ca - cb)) > 128.f * FEPS * fmaxf(1.f, scale))) {
+                    const float4 md = g.hmd[f];
+                    const float sx = wa * md.x + wb * md.z, sy = wa * md.y + wb * md.w;
+                    const float *G = g.hgrad;
+                    float delta = qg * (__fmul_rn(hl - ha, hl + ha) + __fmul_rn(hr - hb, hr + hb)) +
+                                  qg * ((da - db) / d) * __fmul_rn(ha - hb, ha + hb) + (ca + cb);
+                    delta -= gravity * sx * (wa * ha * G[4 * nc + a] + wb * hb * G[4 * nc + b]);
+                    delta -= gravity * sy * (wa * ha * G[5 * nc + a] + wb * hb * G[5 * nc + b]);
+                    delta -= da * db / d * (float(t.raw[a] - t.raw[b]) * nx + float(t.raw[nc + a] - t.raw[nc + b]) * ny);
+                    const float speed = sqrtf(gravity * h), theta = fminf(1.f, fmaxf(t1.z, t1.w) / speed);
+                    delta -= .5f * (1.f - theta) * speed * (2.f * hl * hr / (hl + hr)) * (t1.y - t1.x);
+                    pr = make_float2(delta * nx, delta * ny);
+                }
+            }
+        }
+        g.hp[f] = pr;
+        if (t.stress[sid]) g.hs[f] = st;
+    }
+}
+
 }  // namespace brx_mx
 
 // The boundary CTA of the mixed form is the FP64 kernel (few faces, FP64 sums).
@@ -827,6 +951,12 @@ int mixed_kernel(const Launch &L, int kind, int stage, double *out)
     }
     case K_WATER:
         brx_mx::km_water_out<<<L.grid_f256, 256, 0, st>>>(L.mesh, L.work, out);
+        return 1;
+    case K_HKT_GRAD:
+        brx_mx::km_hkt_gradients<<<L.grid_c, 128, 0, st>>>(L.mesh, L.ctrl, L.mx, L.turb, stage);
+        return 1;
+    case K_HKT_FACES:
+        brx_mx::km_hkt_faces<<<L.grid_f, 128, 0, st>>>(L.mesh, L.ctrl, L.mx, L.turb, stage);
         return 1;
     }
     return 0;

@@ -30,17 +30,13 @@ constexpr double PI_D = 3.14159265358979323846;
 constexpr int TURB_THREADS = 128;
 
 // Wet-only least-squares gradients of u, v, eta (fully wet pairs) and of the
-// bed (all neighbours, unweighted metric): rows u_x u_y v_x v_y eta_x eta_y b_x b_y.
-__global__ void __launch_bounds__(256) k_hkt_gradients(MeshDev m, TurbDev t, const double *q, const double *z,
-                                                       Ctrl *ctrl, int stage)
+// bed (all neighbours, unweighted metric) of one cell:
+// g = u_x u_y v_x v_y eta_x eta_y b_x b_y.
+__device__ __forceinline__ void hkt_cell_gradient(const MeshDev &m, const TurbDev &t, const double *q,
+                                                  const double *z, double dry, int i, double g[8])
 {
     const int n = m.nc, na = m.nadj;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const int sid = m.cell_sid[i];
-        if (!t.hkt[sid]) continue;
-        const Ctrl &ct = ctrl[sid];
-        if (stage && skip_stage(ct, stage)) continue;
-        const double dry = ct.dry;
+    {
         double xx = 0., xy = 0., yy = 0., bx[3] = {0., 0., 0.}, by[3] = {0., 0., 0.}, bz[2] = {0., 0.};
         const bool wet = q[i] > dry;
         for (int s = m.offset[i]; s < m.offset[i + 1]; ++s) {
@@ -56,7 +52,8 @@ __global__ void __launch_bounds__(256) k_hkt_gradients(MeshDev m, TurbDev t, con
 #pragma unroll
             for (int k = 0; k < 3; ++k) { bx[k] += w * dx * d[k]; by[k] += w * dy * d[k]; }
         }
-        double g[8] = {0., 0., 0., 0., 0., 0., 0., 0.};
+#pragma unroll
+        for (int k = 0; k < 8; ++k) g[k] = 0.;
         g[6] = t.inverse[i] * bz[0] + t.inverse[n + i] * bz[1];
         g[7] = t.inverse[n + i] * bz[0] + t.inverse[2 * n + i] * bz[1];
         const double det = xx * yy - xy * xy;
@@ -66,6 +63,20 @@ __global__ void __launch_bounds__(256) k_hkt_gradients(MeshDev m, TurbDev t, con
                 g[2 * k] = (yy * bx[k] - xy * by[k]) / det;
                 g[2 * k + 1] = (xx * by[k] - xy * bx[k]) / det;
             }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_hkt_gradients(MeshDev m, TurbDev t, const double *q, const double *z,
+                                                       Ctrl *ctrl, int stage)
+{
+    const int n = m.nc;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int sid = m.cell_sid[i];
+        if (!t.hkt[sid]) continue;
+        const Ctrl &ct = ctrl[sid];
+        if (stage && skip_stage(ct, stage)) continue;
+        double g[8];
+        hkt_cell_gradient(m, t, q, z, ct.dry, i, g);
 #pragma unroll
         for (int k = 0; k < 8; ++k) t.grad[k * n + i] = g[k];
     }
@@ -173,9 +184,11 @@ __global__ void __launch_bounds__(TURB_THREADS) k_turbine_sample(MeshDev m, Turb
     double low = INFINITY, high = -INFINITY;
     for (int j = t.plane_offset[r] + tid; j < t.plane_offset[r + 1]; j += TURB_THREADS) {
         const int c = t.plane_cell[j];
+        double g[8];
+        hkt_cell_gradient(m, t, q, z, dry, c, g);          // the plane cell's own gradients, FP64
         const double eta = q[c] + z[c];
-        const double surface = eta + t.grad[4 * n + c] * t.plane_delta[j] + t.grad[5 * n + c] * t.plane_delta[np_ + j];
-        const double bed = z[c] + t.grad[6 * n + c] * t.plane_delta[j] + t.grad[7 * n + c] * t.plane_delta[np_ + j];
+        const double surface = eta + g[4] * t.plane_delta[j] + g[5] * t.plane_delta[np_ + j];
+        const double bed = z[c] + g[6] * t.plane_delta[j] + g[7] * t.plane_delta[np_ + j];
         low = fmin(low, fmin(surface, eta)); high = fmax(high, fmax(bed, z[c]));
     }
     red[0][tid] = low; red[1][tid] = high;

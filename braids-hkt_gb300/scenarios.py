@@ -241,20 +241,48 @@ def config4_params(count=64, seed=4):
         spacing = float(np.sqrt(2.0 * length * width / cells))
         out.append(dict(index=i, cells=cells, width=width, length=length, spacing=spacing, discharge=q,
                         seed=int(rng.integers(1, 2**31 - 1))))
+    for p in out:
+        p["rotors"] = rotor_layout(p["length"], p["width"], p["seed"])
     return out
 
 
-def config4_case(p):
-    """One batch scenario, started in uniform flow (unit discharge Q/W along the channel).
+def rotor_layout(length, width, seed, diameter=5.0, most=8, spacing_d=5.0):
+    """0..most rotor centres, uniform over the downstream channel reach
+    (x in [0.4, 0.85] L, y in [0.3, 0.7] W), at least spacing_d diameters apart.
+    Drawn from a stream derived from the scenario seed, so the hydraulic draws
+    of a scenario do not depend on its rotors."""
+    rng = np.random.default_rng([seed, 0x7E57])
+    count = int(rng.integers(0, most + 1))
+    centres = []
+    for _ in range(200 * max(count, 1)):
+        if len(centres) == count:
+            break
+        x = float(rng.uniform(0.4 * length, 0.85 * length))
+        y = float(rng.uniform(0.3 * width, 0.7 * width))
+        if all(np.hypot(x - a, y - b) >= spacing_d * diameter for a, b in centres):
+            centres.append((x, y))
+    return centres
+
+
+def config4_case(p, rotors=True):
+    """One batch scenario, started in uniform flow (unit discharge Q/W along the channel),
+    with its rotors (rated 500 kW, Ct 0.8) in 16 m boxes refined to 1.5 m.
 
     Starting a 100 m channel from rest under its full discharge drives a
     startup bore past 30 m/s; the batch configuration prescribes no initial
     state, so each channel starts already carrying its discharge.
     """
+    from . import turbines as TB
+    centres = p.get("rotors", []) if rotors else []
+    fine = min(p["spacing"], 1.5)
+    boxes = [(x - 8.0, x + 8.0, y - 8.0, y + 8.0, fine) for x, y in centres]
     case = channel(length=p["length"], width=p["width"], spacing=p["spacing"], jitter=0.25 * p["spacing"],
-                   seed=p["seed"], discharge=p["discharge"], field_resolution=min(1.0, p["spacing"]))
+                   seed=p["seed"], discharge=p["discharge"], field_resolution=min(1.0, p["spacing"]), refine=boxes)
     q = case["q"]
     q[1] = np.where(q[0] > 0.0, p["discharge"] / p["width"], 0.0)
+    if centres:
+        case["turbines"] = rotor_rows(case, centres, control=TB.rated_power_curve(5.0, 0.8, 0.4, 500e3))
+        TB.RotorArray(case["mesh"], case["turbines"])        # validate the layout while building
     case["name"] = f"batch_{p['index']:02d}"
     return case
 
