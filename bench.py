@@ -161,6 +161,42 @@ def algorithmic_bytes(kernel, nc, nf, nadj, nslot, precision="fp64"):
     return 0
 
 
+def serving_session(cases, precision, rate=20.0, window=4.0, duration=5.0, interval=2.5, budget=150e9, seed=5):
+    """Config 5, scaled: Poisson arrivals of requests drawn from the config-4
+    scenario pool (mesh and rotor layout from the pool, discharge U(100, 1500)),
+    each asking for ``duration`` simulated seconds, served with continuous
+    batching under an HBM budget; latency is arrival to result on the host
+    clock. A few finished requests are re-run alone in FP64 for the depth error."""
+    import braids_hkt_gb300.serving as SV
+    from braids_hkt_gb300.solver import RiverSolver
+    rng = np.random.default_rng(seed)
+    times = SV.poisson_arrivals(rate, window, seed)
+    reqs = []
+    for k, t in enumerate(times):
+        base = cases[int(rng.integers(len(cases)))]
+        reqs.append(SV.Request(rid=k, case=SV.request_case(base, float(rng.uniform(100.0, 1500.0))),
+                               duration=duration, arrival=t))
+    eng = SV.ServingEngine(budget_bytes=budget, precision=precision, interval=interval, max_cohort_cells=4_000_000)
+    done = eng.run(reqs, max_wall=240.0)
+    rep = eng.report()
+    errs = []
+    for r in sorted(done, key=lambda r: r.case["mesh"].nc)[::max(1, len(done) // 3)][:3]:
+        one = RiverSolver(r.case, precision="fp64")
+        t = 0.0
+        while t < r.duration - 1e-9:
+            dt = min(interval, r.duration - t)
+            one.advance(dt, t)
+            t += dt
+        h64 = one.state()[0]
+        errs.append(float((np.abs(r.state[0] - h64) / np.maximum(h64, 1e-3)).max()))
+        one.close()
+    rep.update(arrival_rate_per_s=rate, arrival_window_s=window, simulated_s_per_request=duration,
+               interval_s=interval, depth_rel_vs_fp64_max=max(errs) if errs else None,
+               note=f"config 5 scaled: Poisson {rate:g}/s over {window:g} s (not 300 s), {duration:g} s simulated "
+                    "per request (not 600 s), requests from the config-4 pool with their own discharge")
+    return rep
+
+
 def cpu_baseline(cases, outer, seconds=10.0, threads=None):
     """The oracle port on the host cores over a bounded sample of the workload."""
     from oracle import Oracle
@@ -214,6 +250,7 @@ def main():
     ap.add_argument("--workload", default="config4")
     ap.add_argument("--plain", type=int, default=3, help="scenarios re-run one by one in plain FP64")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serving", action="store_true", help="skip the scaled config-5 serving session")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
@@ -400,6 +437,14 @@ def main():
     if plain is not None:
         line["plain_fp64"] = plain
         line["batched_vs_plain_fp64"] = value / plain["value"]
+    if precision == "mixed" and not args.no_serving:
+        solver.close()
+        try:
+            line["serving"] = serving_session(cases, precision)
+            line["latency_ms"]["serving_p50_s"] = line["serving"]["latency_s"]["p50"]
+            line["latency_ms"]["serving_p99_s"] = line["serving"]["latency_s"]["p99"]
+        except TimeoutError as exc:
+            line["serving"] = {"error": str(exc)}
     if not args.no_cpu_baseline:
         median = sorted(cases, key=lambda c: c["mesh"].nc)[len(cases) // 2]
         line["cpu_baseline"] = cpu_baseline([median], outer)

@@ -33,6 +33,9 @@ SIGNATURES = {
     "brx_turbines_set": (I, [P, I, P, P, P, I, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P]),
     "brx_turbines_diagnose": (I, [P, P]),
     "brx_turbines_last": (I, [P, P]),
+    "brx_advance_start": (I, [P, P, P]),
+    "brx_advance_poll": (I, [P, P, P]),
+    "brx_solver_bytes": (C.c_longlong, [P]),
     "brx_hint_get": (I, [P, P]),
     "brx_hint_set": (I, [P, P]),
     "brx_graph_chunk_set": (I, [P, I]),

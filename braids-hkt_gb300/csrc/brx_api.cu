@@ -49,6 +49,10 @@ struct brx_solver {
     cudaStream_t side = nullptr;       // boundary CTAs run here, concurrent with the cell sweep
     cudaEvent_t fork = nullptr, join = nullptr;
     std::vector<void *> allocations;
+    size_t bytes = 0;                // device bytes held (sum of allocations)
+    cudaEvent_t polled = nullptr;    // asynchronous advance: control mirror copied back
+    bool pending = false;            // an asynchronous interval is in flight
+    int replays = 0;
     MeshDev mesh{};
     BoundaryDev bnd{};
     StateDev state{};
@@ -88,6 +92,7 @@ struct brx_solver {
         cudaError_t e = cudaMalloc(&ptr, count * sizeof(T));
         if (e != cudaSuccess) return fail(BRX_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
         allocations.push_back(ptr);
+        bytes += count * sizeof(T);
         *p = (T *)ptr;
         return BRX_OK;
     }
@@ -198,6 +203,7 @@ extern "C" int brx_solver_create(int nscen, const int *cell_offset, const int *f
         CK(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
         CK(cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&s->join, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&s->polled, cudaEventDisableTiming));
         s->cell_offset.assign(cell_offset, cell_offset + nscen + 1);
         s->face_offset.assign(face_offset, face_offset + nscen + 1);
         s->seg_offset.assign(nscen + 1, 0);
@@ -394,6 +400,7 @@ extern "C" int brx_solver_destroy(brx_solver *s)
     for (void *p : s->allocations) cudaFree(p);
     if (s->h_ctrl) cudaFreeHost(s->h_ctrl);
     if (s->fork) cudaEventDestroy(s->fork);
+    if (s->polled) cudaEventDestroy(s->polled);
     if (s->join) cudaEventDestroy(s->join);
     if (s->side) cudaStreamDestroy(s->side);
     if (s->stream) cudaStreamDestroy(s->stream);
@@ -839,6 +846,7 @@ static int build_graph(brx_solver *s)
 }
 
 static int advance_impl(brx_solver *s, const double *dt, const double *time, brx_advance_stats *stats);
+static int finish_interval(brx_solver *s, brx_advance_stats *stats);
 
 extern "C" int brx_advance(brx_solver *s, double dt, double time, brx_advance_stats *stats)
 {
@@ -847,6 +855,56 @@ extern "C" int brx_advance(brx_solver *s, double dt, double time, brx_advance_st
     std::vector<double> d(s->nscen, dt), t(s->nscen, time);
     return advance_impl(s, d.data(), t.data(), stats);
 }
+
+// Asynchronous interval: launch the first graph chunk and return. Each poll
+// checks (without blocking) whether the control mirror has come back; if a
+// scenario is still running it launches the next chunk, otherwise it commits
+// and reports like brx_advance_batch.
+static int launch_chunk(brx_solver *s)
+{
+    CK(cudaGraphLaunch(s->graph, s->stream));
+    s->launches += (long long)s->launches_per_substep * s->graph_chunk;
+    CK(cudaMemcpyAsync(s->h_ctrl, s->d_ctrl, sizeof(Ctrl) * s->nscen, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaEventRecord(s->polled, s->stream));
+    s->replays++;
+    return BRX_OK;
+}
+
+extern "C" int brx_advance_start(brx_solver *s, const double *dt, const double *time)
+{
+    TRY(ensure_ready(s));
+    if (!dt || !time) return fail(BRX_ERR_ARGUMENT, "null interval arrays");
+    if (s->pending) return fail(BRX_ERR_STATE, "an asynchronous interval is already in flight");
+    for (int i = 0; i < s->nscen; ++i)
+        if (!std::isfinite(dt[i]) || !std::isfinite(time[i])) return fail(BRX_ERR_ARGUMENT, "nonfinite interval");
+    if (s->graph_dirty || !s->graph) TRY(build_graph(s));
+    begin_interval_each(s, dt, time, false);
+    CK(cudaMemcpyAsync(s->d_ctrl, s->h_ctrl, sizeof(Ctrl) * s->nscen, cudaMemcpyHostToDevice, s->stream));
+    refresh_bed(s);
+    s->replays = 0;
+    s->pending = true;
+    return launch_chunk(s);
+}
+
+extern "C" int brx_advance_poll(brx_solver *s, int *done, brx_advance_stats *stats)
+{
+    if (!s || !done) return fail(BRX_ERR_ARGUMENT, "null argument");
+    if (!s->pending) return fail(BRX_ERR_STATE, "no asynchronous interval in flight");
+    *done = 0;
+    const cudaError_t e = cudaEventQuery(s->polled);
+    if (e == cudaErrorNotReady) return BRX_OK;
+    CK(e);
+    bool all_done = true;
+    for (int i = 0; i < s->nscen; ++i) all_done = all_done && s->h_ctrl[i].done;
+    const int max_replays = (4096 + 102) / s->graph_chunk + 2;
+    if (!all_done && s->replays < max_replays) return launch_chunk(s);
+    s->pending = false;
+    *done = 1;
+    return finish_interval(s, stats);
+}
+
+// Device bytes held by the solver (its allocations).
+extern "C" long long brx_solver_bytes(const brx_solver *s) { return s ? (long long)s->bytes : 0; }
 
 extern "C" int brx_advance_batch(brx_solver *s, const double *dt, const double *time, brx_advance_stats *stats)
 {
@@ -874,6 +932,12 @@ static int advance_impl(brx_solver *s, const double *dt, const double *time, brx
         all_done = true;
         for (int i = 0; i < s->nscen; ++i) all_done = all_done && s->h_ctrl[i].done;
     }
+    return finish_interval(s, stats);
+}
+
+// Commit every scenario's accepted state into the bound buffer and report.
+static int finish_interval(brx_solver *s, brx_advance_stats *stats)
+{
     k_commit<<<s->grid_c256, 256, 0, s->stream>>>(s->mesh, s->state, s->d_ctrl);
     s->launches++;
     CK(cudaGetLastError());

@@ -248,6 +248,32 @@ class RiverSolver:
                             failed=s.failed))
         return out[0] if self.single else out
 
+    # --- asynchronous intervals (serving loops) ---------------------------
+    def advance_start(self, dt, time):
+        """Launch one interval per scenario (arrays; dt <= 0 idles a scenario) and return at once."""
+        self.torch.cuda.current_stream().synchronize()
+        d = _f64(np.broadcast_to(dt, (self.nscen,)))
+        t = _f64(np.broadcast_to(time, (self.nscen,)))
+        check(self.lib.brx_advance_start(self.h, _ptr(d), _ptr(t)))
+        self._async_stats = (AdvanceStats * self.nscen)()
+
+    def advance_poll(self):
+        """None while the interval runs; per-scenario diagnostics once it has finished."""
+        done = C.c_int(0)
+        code = self.lib.brx_advance_poll(self.h, C.byref(done), self._async_stats)
+        if code and code != 4:
+            check(code)
+        if not done.value:
+            return None
+        return [dict(integrator=METHOD, hydraulic_substeps=s.substeps, hydraulic_rejections=s.rejections,
+                     hydraulic_minimum_dt=s.min_dt, hydraulic_maximum_dt=s.max_dt,
+                     accepted_cfl_max=s.accepted_cfl_max, hydraulic_next_substep_hint_s=s.hint,
+                     failed=s.failed) for s in self._async_stats]
+
+    def device_bytes(self):
+        """Device memory the solver holds (its allocations plus the bound state)."""
+        return int(self.lib.brx_solver_bytes(self.h)) + self.q.numel() * 8 + self.z.numel() * 8
+
     def step(self, dt):
         """Advance by dt from the owner clock (ShorelineSolver.step)."""
         diag = self.advance(dt, self.time[0])

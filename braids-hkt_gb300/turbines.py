@@ -403,7 +403,9 @@ def pack(cases, cell_offsets):
             dxdy.append(np.zeros((2, m.nadj))); inverse.append(np.zeros((3, m.nc)))
             mdisp.append(np.zeros((4, m.nf))); xy.append(m.xy); nu.append(np.zeros(m.nc)); hkt.append(0)
             continue
-        d, inv, disp = flow_geometry(m)
+        if getattr(ra, "flow", None) is None:
+            ra.flow = flow_geometry(m)              # once per mesh (the rotor array travels with the case)
+        d, inv, disp = ra.flow
         dxdy.append(d); inverse.append(inv); mdisp.append(disp); xy.append(m.xy)
         nu.append(np.full(m.nc, ra.nu)); hkt.append(1)
         shift = len(cx)

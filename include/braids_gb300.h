@@ -174,6 +174,18 @@ int brx_turbines_diagnose(brx_solver *s, double *out);
 /* The same record for the state of the last evaluated stage. */
 int brx_turbines_last(brx_solver *s, double *out);
 
+/* Asynchronous form of brx_advance_batch for serving loops: start launches
+ * the interval's first CUDA-graph chunk and returns; poll never blocks. It
+ * sets *done = 0 while the interval runs (launching the next chunk when the
+ * last one has finished) and *done = 1 once every scenario has completed,
+ * with stats (nscen) filled and the return code of brx_advance_batch. One
+ * interval per solver at a time; solvers on their own streams overlap. */
+int brx_advance_start(brx_solver *s, const double *dt, const double *time);
+int brx_advance_poll(brx_solver *s, int *done, brx_advance_stats *stats);
+
+/* Device bytes the solver holds (for admission against a memory budget). */
+long long brx_solver_bytes(const brx_solver *s);
+
 /* Step hint carried between brx_advance calls (nscen, host; <= 0 = none). */
 int brx_hint_get(brx_solver *s, double *hint);
 int brx_hint_set(brx_solver *s, const double *hint);
