@@ -132,6 +132,25 @@ def small_rotor_channel(length=150.0, width=30.0, spacing=1.5, seed=21, discharg
     return case
 
 
+def exner_params(case, diameter=0.002, porosity=0.4, chezy=44.0, morfac=1.0, sediment_depth=0.001,
+                 erodible=2.0, inlet_bc=3, outlet_bc=2, feed=0.0):
+    """Bed-update parameters of one scenario: a single grain size, porosity,
+    Chezy coefficient of the transport formula, morphological factor, the
+    sediment working depth, a non-erodible layer ``erodible`` metres below the
+    bed, and per-face bed boundaries (0 wall, 1 prescribed feed, 2 open
+    outflow, 3 transport capacity) on the inlet and outlet segments."""
+    m = case["mesh"]
+    bedbc = np.zeros(m.nf, np.int32)
+    feeds = np.zeros(m.nf)
+    openf = (m.neighbour < 0) & (m.bid >= 0)
+    bedbc[openf & (m.bid == 0)] = inlet_bc
+    bedbc[openf & (m.bid == 1)] = outlet_bc
+    feeds[openf & (m.bid == 0)] = feed
+    return dict(diameter=float(diameter), porosity=float(porosity), chezy=float(chezy), morfac=float(morfac),
+                sediment_depth=float(sediment_depth), bedbc=bedbc, feed=feeds,
+                rock=np.ascontiguousarray(case["z"] - erodible))
+
+
 def small_channel(length=120.0, width=24.0, spacing=4.0, seed=7, sigma=0.15, corr=8.0,
                   discharge=20.0, stage=3.0, outlet_bed=-1.0, slope=2e-3, cfl=0.9):
     """A few hundred cells with the same physics as config 1 (for parity tests)."""

@@ -32,6 +32,10 @@
  *   CFL frequency     src/braids_core/sediment/river_explicit.h:13-26
  *   Manning drag      src/braids_core/sediment/river_hydraulic_drag.h:3-16,
  *                     river_roughness.py:42-47
+ *   Exner / MPM       src/braids_core/sediment/shoreline_solver.py:209-240 (finish, bed_faces),
+ *                     flow2dh_mobile_bed.py:101-109, river_mpm.h:12-46 (mixture, mpm),
+ *                     flow2dh_mobile_kernels.h:13-53, bend_methods_v1_kernels.h:23-39,389-405,
+ *                     src/braids_gpu/flow_bed_slope_runtime.cu:13-144 (Koch-Flokstra, mode 3)
  *   turbines          src/braids_core/sediment/river_turbine_flow.py:230-239 (momentum order),
  *                     river_turbine_flow.h:13-82 (wet gradients, surface pack, pressure),
  *                     river_hydrokinetic_stress.h:13-35 (ambient stress),
@@ -1467,6 +1471,181 @@ int om_turbine_diagnose(const om_ctx *m, const double *q, const double *z)
     return err;
 }
 
+/* ------------------------------------------------------------------ */
+/* Exner bed update with MPM transport (one grain size)                */
+/* ------------------------------------------------------------------ */
+typedef struct {
+    double diameter, porosity, chezy, morfac, sediment_depth;
+    const int *bedbc;                                  /* (nf) 0 wall, 1 feed, 2 outflow, 3 capacity */
+    const double *feed, *rock;                         /* (nf) (nc) */
+    const double *dxdy, *inverse, *xy;                 /* (2,nadj) (3,nc) (2,nc) */
+} om_exner_params;
+
+typedef struct { int ok; double residual, boundary, donor, change; } om_exner_stats;
+
+/* Koch--Flokstra slope correction, FLOW ISlope = 3 with alfabs = alfabn = 0,
+ * ashld .85, bshld .5, cshld = dshld = 0 (flow_bed_slope_runtime.cu:13-144). */
+static int om_slope3(double qx, double qy, double down_x, double down_y, double stress, double *cx, double *cy)
+{
+    *cx = qx; *cy = qy;
+    if (!isfinite(qx) || !isfinite(qy) || !isfinite(down_x) || !isfinite(down_y) || !isfinite(stress) || stress < 0.0)
+        return 2;
+    double magnitude = sqrt(qx * qx + qy * qy);
+    if (!isfinite(magnitude)) return 2;
+    if (magnitude <= 1.0e-6) return 0;
+    const double alfabs = 0., ashld = .85, bshld = .5;
+    double dzds = down_x * qx / magnitude + down_y * qy / magnitude;
+    const double tan_phi = tan((double)(30.0f / 180.0f) * acos(-1.0));
+    dzds = fmin((double)0.9f * tan_phi, dzds);
+    double ftheta = 0.0;
+    if (stress != 0.0) ftheta = ashld * pow(stress, bshld) * pow(1.0, 0.0) * pow(1.0, 0.0);
+    double dirx, diry;
+    if (down_x != 0.0 || down_y != 0.0) { dirx = ftheta * qx / magnitude + down_x; diry = ftheta * qy / magnitude + down_y; }
+    else { dirx = qx / magnitude; diry = qy / magnitude; }
+    const double norm = sqrt(dirx * dirx + diry * diry);
+    if (!isfinite(norm) || norm <= 2.2250738585072014e-308) return 3;
+    magnitude = magnitude * (1.0 + alfabs * dzds);
+    *cx = magnitude * dirx / norm; *cy = magnitude * diry / norm;
+    if (!isfinite(*cx) || !isfinite(*cy)) { *cx = qx; *cy = qy; return 4; }
+    return 0;
+}
+
+/* One bed update over dt (seconds of hydraulics; morfac applied here).
+ * q is the accepted state, z0 the bed; writes ztrial (nc). */
+int om_exner(const om_ctx *m, const om_exner_params *ex, const double *q, const double *z0, double dt,
+             double *ztrial, om_exner_stats *st)
+{
+    const int n = m->nc, nf = m->nf, na = m->nadj;
+    const double d = ex->diameter, phi = 1.0 - ex->porosity, dtm = dt * ex->morfac;
+    double *safe = om_alloc(sizeof(double) * 3 * (size_t)n), *gz = om_alloc(sizeof(double) * 2 * (size_t)n);
+    double *cell = om_alloc(sizeof(double) * 6 * (size_t)n), *flux = om_alloc(sizeof(double) * nf);
+    double *fac = om_alloc(sizeof(double) * n);
+    int *wet = om_alloc(sizeof(int) * n), bad = 0;
+    /* single-grain mixture: D90 by the log-linear bisection, hiding factor */
+    double hiding, d90;
+    {
+        const double logd = log(d), lo = logd + 1.25 * log(.75), hi = logd + 1.25 * log(1.5);
+        const double mean = d * 1. / 1., r = d / fmax(mean, 1.e-4), v = 1.27875360095283;
+        hiding = pow(v / (v + log10(r)), 2.);
+        double low = lo, high = hi;
+        for (int it = 0; it < 60; ++it) {
+            const double mid = .5 * (low + high);
+            double f = 0.;
+            if (mid >= hi) f = 1.;
+            else if (mid > logd) f = .5 + .5 * (mid - logd) / (hi - logd);
+            else if (mid > lo) f = .5 * (mid - lo) / (logd - lo);
+            const double cdf = 1. / 1. * f;
+            if (cdf < .9) low = mid; else high = mid;
+        }
+        d90 = exp(.5 * (low + high));
+    }
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; ++i) {
+        wet[i] = q[i] > ex->sediment_depth;
+        safe[i] = wet[i] ? q[i] : .001001;
+        safe[n + i] = wet[i] ? q[n + i] : 0.;
+        safe[2 * n + i] = wet[i] ? q[2 * n + i] : 0.;
+    }
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; ++i) {
+        /* bed gradient of the flow engines' LS metric (bend_methods_v1_kernels.h:23-39, z row) */
+        double bx = 0., by = 0.;
+        for (int s = m->offset[i]; s < m->offset[i + 1]; ++s) {
+            const int j = om_other(m, s);
+            if (j < 0) continue;
+            const double dx = ex->dxdy[s], dy = ex->dxdy[na + s], wt = 1. / (dx * dx + dy * dy);
+            bx += wt * dx * (z0[j] - z0[i]); by += wt * dy * (z0[j] - z0[i]);
+        }
+        gz[i] = ex->inverse[i] * bx + ex->inverse[n + i] * by;
+        gz[n + i] = ex->inverse[n + i] * bx + ex->inverse[2 * n + i] * by;
+        /* MPM (river_mpm.h:32-46) with hI = 0 */
+        const double h = safe[i], u = safe[n + i] / h, vv = safe[2 * n + i] / h;
+        const double ue = safe[n + i] / safe[i], ve = safe[2 * n + i] / safe[i], c = ex->chezy;
+        const double speed = hypot(ue, ve), theta = speed * speed / (c * c * 1.65 * d);
+        const double grain = 18. * log10(12. * fmax(fmax(.01, safe[i]) / d90, 1.)), mu = fmin(1., pow(c / grain, 1.5));
+        const double excess = fmax(0., mu * theta - .047 * hiding);
+        const double mag = 2650. * 8. * sqrt(9.81 * 1.65 * d * excess) * d * excess;
+        const double x = speed > 0. ? mag * ue / speed : 0., y = speed > 0. ? mag * ve / speed : 0.;
+        const double us = hypot(u, vv), alpha = us > 0. && mag > 0. ? 12.5 * (1. - sqrt(9.81) / (.4 * c)) * (0. / h) / us : 0.;
+        const double bxr = u + alpha * vv, byr = vv - alpha * u, bs = hypot(bxr, byr);
+        cell[i] = x; cell[n + i] = y; cell[2 * n + i] = theta;
+        cell[3 * n + i] = bs > 0. ? mag * bxr / bs : 0.; cell[4 * n + i] = bs > 0. ? mag * byr / bs : 0.;
+        cell[5 * n + i] = alpha;
+    }
+#pragma omp parallel for schedule(static) reduction(| : bad)
+    for (int f = 0; f < nf; ++f) {
+        /* face inputs (flow2dh_mobile_kernels.h:13-38) */
+        const int o = m->owner[f], j = m->neighbour[f];
+        const double nx = m->normal[f], ny = m->normal[nf + f];
+        double x = cell[3 * n + o], y = cell[4 * n + o], gx = gz[o], gy = gz[n + o];
+        double stress = cell[2 * n + o] * sqrt(1. + cell[5 * n + o] * cell[5 * n + o]);
+        if (j >= 0) {
+            const double dd = m->distance[f] + m->distance[nf + f], wo = m->distance[nf + f] / dd, wj = m->distance[f] / dd;
+            const double a = x * nx + y * ny, b = cell[3 * n + j] * nx + cell[4 * n + j] * ny;
+            const double un = (a > 0. && b > 0.) ? a : ((a < 0. && b < 0.) ? b : .5 * (a + b));
+            const double ut = wo * (-x * ny + y * nx) + wj * (-cell[3 * n + j] * ny + cell[4 * n + j] * nx);
+            x = un * nx - ut * ny; y = un * ny + ut * nx;
+            gx = wo * gx + wj * gz[j]; gy = wo * gy + wj * gz[n + j];
+            const double dx = ex->xy[j] - ex->xy[o], dy = ex->xy[n + j] - ex->xy[n + o], dn = dx * nx + dy * ny;
+            const double correction = (z0[j] - z0[o] - gx * dx - gy * dy) / dn;
+            gx += correction * nx; gy += correction * ny;
+            stress = wo * stress + wj * cell[2 * n + j] * sqrt(1. + cell[5 * n + j] * cell[5 * n + j]);
+        } else {
+            const double normal_slope = gx * nx + gy * ny;
+            gx -= normal_slope * nx; gy -= normal_slope * ny;
+        }
+        double cx, cy;
+        if (om_slope3(x, y, -gx, -gy, stress, &cx, &cy)) bad |= 1;
+        /* bed flux and its boundaries (flow2dh_mobile_kernels.h:41-53) */
+        double fl = (cx * nx + cy * ny) / 2650.;
+        if (j < 0) {
+            const int bc = ex->bedbc[f];
+            if (bc == 1) fl = -ex->feed[f];
+            else if (bc == 2) fl = fmax(0., fl);
+            else if (bc == 3) {}
+            else fl = 0.;
+        }
+        /* no bed flux across a face with a dry side (shoreline_solver.py:214-215) */
+        const int active = wet[o] && (j >= 0 ? wet[j] : 1);
+        flux[f] = fl * active;
+    }
+    /* donor limiter of the solid stock (bend_methods_v1_kernels.h:396-405) */
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; ++i) {
+        double outgoing = 0.;
+        for (int k = m->offset[i]; k < m->offset[i + 1]; ++k) {
+            const int f = m->faces[k];
+            outgoing += fmax(0., m->signs[k] * flux[f]) * m->length[f];
+        }
+        const double available = phi * (z0[i] - ex->rock[i]);
+        fac[i] = outgoing > 0. ? fmin(1., fmax(0., available) * m->area[i] / (dtm * outgoing)) : 1.;
+    }
+    for (int f = 0; f < nf; ++f) {
+        const int j = flux[f] >= 0. ? m->owner[f] : m->neighbour[f];
+        if (j >= 0) flux[f] *= fac[j];
+    }
+    double donor = 1., change = 0., residual = 0., boundary = 0.;
+    int finite = 1, above = 1;
+    for (int i = 0; i < n; ++i) {
+        double r = 0.;
+        for (int k = m->offset[i]; k < m->offset[i + 1]; ++k) r -= m->signs[k] * m->length[m->faces[k]] * flux[m->faces[k]];
+        r = r / m->area[i];
+        ztrial[i] = z0[i] + (dtm / phi) * r;
+        donor = fmin(donor, fac[i]);
+        if (!isfinite(ztrial[i])) finite = 0;
+        if (ztrial[i] < ex->rock[i] - 1e-13) above = 0;
+        change = fmax(change, fabs(ztrial[i] - z0[i]) / fmax(q[i], ex->sediment_depth));
+        residual += phi * (ztrial[i] - z0[i]) * m->area[i];
+    }
+    for (int f = 0; f < nf; ++f)
+        if (m->neighbour[f] < 0 && m->bid[f] >= 0) boundary -= dtm * flux[f] * m->length[f];
+    residual -= boundary;
+    st->ok = !bad && finite && above && fabs(residual) <= 1e-10 && change <= .05;
+    st->residual = residual; st->boundary = boundary; st->donor = donor; st->change = change;
+    free(safe); free(gz); free(cell); free(flux); free(fac); free(wet);
+    return bad ? OM_REJECT_SPATIAL : (st->ok ? OM_OK : OM_REJECT_BUDGET);
+}
+
 /* One spatial residual (RiverMidpoint.rate + RiverExplicit.rate).
  * q is the stage state, base the interval-start stock. Writes rate (3,nc)
  * and the limited water flux (nf); *freq_out gets the max CFL frequency. */
@@ -1609,3 +1788,4 @@ void om_set_threads(int n)
 size_t om_ctx_size(void) { return sizeof(om_ctx); }
 size_t om_stats_size(void) { return sizeof(om_stats); }
 size_t om_turbines_size(void) { return sizeof(om_turbines); }
+size_t om_exner_size(void) { return sizeof(om_exner_params); }

@@ -71,6 +71,15 @@ class Turbines(C.Structure):
                 ("grad", P), ("raw", P), ("face", P), ("work", P), ("trace", P), ("kcell", P), ("fstatus", P)]
 
 
+class ExnerParams(C.Structure):
+    _fields_ = [("diameter", D), ("porosity", D), ("chezy", D), ("morfac", D), ("sediment_depth", D),
+                ("bedbc", P), ("feed", P), ("rock", P), ("dxdy", P), ("inverse", P), ("xy", P)]
+
+
+class ExnerStats(C.Structure):
+    _fields_ = [("ok", I), ("residual", D), ("boundary", D), ("donor", D), ("change", D)]
+
+
 class Stats(C.Structure):
     _fields_ = [("substeps", I), ("rejections", I), ("status", I),
                 ("min_dt", D), ("max_dt", D), ("accepted_cfl_max", D), ("hint", D)]
@@ -106,6 +115,10 @@ def _setup(L):
     L.om_set_threads.argtypes = [I]
     L.om_turbines_size.restype = C.c_size_t
     assert L.om_turbines_size() == C.sizeof(Turbines), "oracle turbine layout differs"
+    L.om_exner_size.restype = C.c_size_t
+    assert L.om_exner_size() == C.sizeof(ExnerParams), "oracle bed-update layout differs"
+    L.om_exner.argtypes = [P, P, P, P, D, P, P]
+    L.om_exner.restype = I
     L.om_turbine_diagnose.argtypes = [P, P, P]
     L.om_turbine_diagnose.restype = I
     L.om_hkt_gradients.argtypes = [P, P, P, P, P]
@@ -181,6 +194,7 @@ class Oracle:
             ctx.table_value = k("table_value", _f64(case["table_value"]))
         ctx.threads = threads or 0
         self.turbines = None
+        self.case_exner = case.get("exner")
         if case.get("turbines"):
             self._bind_turbines(case, k)
             ctx.turb = C.cast(C.pointer(self._turb), P)
@@ -219,6 +233,26 @@ class Oracle:
         t.kcell = k("t_kcell", np.zeros(max(ns, 1)))
         t.fstatus = k("t_fstatus", np.zeros(m.nf, np.int32))
         self._turb = t
+
+    def exner(self, q, dt, z0=None):
+        """One bed update of the accepted state q over dt: (status, z_trial, stats dict)."""
+        from braids_hkt_gb300 import turbines as TB
+        ex = self.case_exner
+        if not hasattr(self, "_exner"):
+            d, inv, _ = TB.flow_geometry(self.m)
+            keep = self._keep
+            keep.update(ex_bedbc=_i32(ex["bedbc"]), ex_feed=_f64(ex["feed"]), ex_rock=_f64(ex["rock"]),
+                        ex_dxdy=_f64(d), ex_inv=_f64(inv), ex_xy=_f64(self.m.xy))
+            p = ExnerParams(ex["diameter"], ex["porosity"], ex["chezy"], ex.get("morfac", 1.0), ex["sediment_depth"],
+                            _p(keep["ex_bedbc"]), _p(keep["ex_feed"]), _p(keep["ex_rock"]), _p(keep["ex_dxdy"]),
+                            _p(keep["ex_inv"]), _p(keep["ex_xy"]))
+            self._exner = p
+        q = _f64(q)
+        z0 = self.z if z0 is None else _f64(z0)
+        zt = np.zeros(self.m.nc)
+        st = ExnerStats()
+        code = self.L.om_exner(self.cp, C.byref(self._exner), _p(q), _p(z0), float(dt), _p(zt), C.byref(st))
+        return code, zt, {f: getattr(st, f) for f, _ in ExnerStats._fields_}
 
     def turbine_pressure(self, on):
         """Switch the balanced-pressure correction (on by default with rotors)."""

@@ -20,7 +20,9 @@ built-ins and a loop over the launch grid):
 Dual-compiled OpenMP headers (their ENTRY/LOOP macros select the host form):
   river_midpoint.h, river_explicit.h, river_exterior_bed.h,
   river_hydraulic_drag.source() (src/braids_core/sediment/river_hydraulic_drag.py:11-15),
-  river_turbine_flow.h, river_hydrokinetic_stress.h (turbine momentum terms)
+  river_turbine_flow.h, river_hydrokinetic_stress.h (turbine momentum terms),
+  river_mpm.h, flow2dh_mobile_kernels.h, bend_methods_v1_kernels.h (Exner / MPM)
+Generated CUDA C also: flow_bed_slope_runtime.cu (src/braids_gpu, Koch-Flokstra slope)
 
 Usage: python oracle/ref_build.py   (exits non-zero when the reference is absent)
 """
@@ -88,7 +90,9 @@ def generate():
         face_activity.cuda_transform((gpu / "resident_update.cu").read_text())
     gather = (src / "braids_gpu/implicit_midpoint_fwave.cu").read_text()
     OUT.mkdir(exist_ok=True)
-    units = {"ref_reconstruction": reconstruction, "ref_update": update, "ref_gather": gather}
+    slope = (src / "braids_gpu/flow_bed_slope_runtime.cu").read_text()
+    units = {"ref_reconstruction": reconstruction, "ref_update": update, "ref_gather": gather,
+             "ref_slope": slope}
     for name, code in units.items():
         (OUT / f"{name}.cpp").write_text(SHIM + "\n" + code + "\n" + _kernel_wrappers(code) + "\n")
     headers = {
@@ -100,6 +104,10 @@ def generate():
         "ref_hkt": (src / "braids_core/sediment/river_turbine_flow.h").read_text(),
         "ref_stress": (src / "braids_core/sediment/river_hydrokinetic_stress.h").read_text(),
         "ref_flow": (src / "braids_core/sediment/flow2dh_fixed_bed_kernels.h").read_text(),
+        # Exner bed update with MPM transport
+        "ref_mpm": (src / "braids_core/sediment/river_mpm.h").read_text(),
+        "ref_mobile": (src / "braids_core/sediment/flow2dh_mobile_kernels.h").read_text(),
+        "ref_bend": (src / "braids_core/sediment/bend_methods_v1_kernels.h").read_text(),
     }
     for name, code in headers.items():
         (OUT / f"{name}.h").write_text(code)

@@ -8,6 +8,9 @@ the reference's Python owners line by line:
   RiverMidpoint.rate, GPU branch       src/braids_core/sediment/river_midpoint.py:100-176
   RiverExplicit.rate/_single/advance   src/braids_core/sediment/river_explicit.py:63-154
   ExteriorBed.evaluate/apply_*         src/braids_core/sediment/river_exterior_bed.py:183-233
+  Exner bed update (finish + bed_faces) src/braids_core/sediment/shoreline_solver.py:209-240,
+                                       flow2dh_mobile_bed.py:101-129, bend_methods_v1.py:415-463,
+                                       river_mpm.py:21-33, flow2dh_eh_operator.py:111-120
   turbine momentum (install.add)       src/braids_core/sediment/river_turbine_flow.py:222-239,
                                        with the reference's ThetisRotor.sample / cell_terms
                                        (river_turbine_thetis.py) run on numpy
@@ -178,6 +181,83 @@ class Ref:
         it) stays referenced until the call returns."""
         fn.restype = None
         fn(*[_arg(a) for a in args])
+
+    # -- Exner bed update with MPM transport, the reference's kernels -----------
+    def exner(self, q, z0, dt):
+        """One bed update over dt (ShorelinePhysics.finish with morphology):
+        (z_trial, stats dict). Parameters come from case["exner"]."""
+        from braids_core.sediment.bend_methods_v1 import prepared_geometry
+        ex = self.case["exner"]
+        m, g = self.m, self.g
+        n, nf = m.nc, m.nf
+        for name in ("mpm", "mobile", "bend", "slope"):
+            if name not in self.libs:
+                self.libs[name] = C.CDLL(str(REF / f"libref_{name}.so"))
+        for name, fn in (("mpm", "mobile_threads"), ("mobile", "mobile_threads"), ("bend", "bend_threads")):
+            getattr(self.libs[name], fn)(C.c_int(1))
+        if not hasattr(self, "pg"):
+            data = dict(xy=m.xy, area=m.area, owner=m.owner, neighbour=m.neighbour, normal=m.normal,
+                        length=m.length, mid=m.mid, offset=m.offset, faces=m.faces, signs=m.signs,
+                        distance=m.records["distance"], bid=m.bid)
+            self.pg = prepared_geometry(data)
+        pg = self.pg
+        f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+        i32 = lambda a: np.ascontiguousarray(a, dtype=np.int32)
+        d, phi = float(ex["diameter"]), 1.0 - float(ex["porosity"])
+        dtm = float(dt) * float(ex.get("morfac", 1.0))
+        z0 = f64(z0)
+        rock = f64(ex["rock"])
+        # division-safe state (secondary_vector_ops.safe) at the sediment depth
+        q = f64(q)
+        wet = q[0] > ex["sediment_depth"]
+        safe = q.copy()
+        safe[0] = np.where(wet, q[0], .001001)
+        safe[1:] = np.where(wet, q[1:], 0.)
+        hi = np.zeros(n)
+        # single-grain mixture: D90 and hiding (river_mpm.h mixture)
+        hiding, d90, mean = np.zeros(n), np.zeros(n), np.zeros(n)
+        self._invoke(self.libs["mpm"].mixture, n, 1, 1, np.ones(n), np.array([d]), hiding, d90, mean)
+        grad = np.zeros((10, n))
+        self._invoke(self.libs["bend"].gradients, n, safe, z0, hi, np.zeros(n), pg["offset"], pg["faces"],
+                     pg["owner"], pg["neighbour"], f64(pg["dxdy"]), f64(pg["inverse"]), grad)
+        cell = np.zeros((6, n))
+        self._invoke(self.libs["mpm"].mpm, n, d, safe, safe, np.full(n, float(ex["chezy"])), hi, d90, hiding, cell)
+        face = np.zeros((10, nf))
+        self._invoke(self.libs["mobile"].flow_bed_face_inputs, nf, n, d, safe, z0, cell, grad, g["owner"],
+                     g["neighbour"], g["normal"], f64(m.records["distance"]), f64(m.xy), face)
+        corrected = np.zeros((2, nf))
+        status = np.zeros(nf, np.int32)
+        self._invoke(self.libs["slope"].L_flow_bed_slope_direction, LL(nf), LL(nf), 3,
+                     *[np.ascontiguousarray(face[k]) for k in range(10)],
+                     0., 0., .85, .5, 0., 0., 1., .05, corrected[0], corrected[1], status)
+        corrected = np.ascontiguousarray(corrected)
+        if np.any(status):
+            raise ValueError("Koch--Flokstra rejected face input")
+        aux = np.zeros((3, nf))
+        self._invoke(self.libs["mobile"].flow_bed_flux, nf, 2650., corrected, g["neighbour"], i32(ex["bedbc"]),
+                     g["normal"], f64(ex["feed"]), aux)
+        o, j = m.owner, m.neighbour
+        active = wet[o] & np.where(j >= 0, wet[np.maximum(j, 0)], True)
+        aux[2] *= active
+        available = phi * (z0 - rock)
+        factors = np.zeros(n)
+        self._invoke(self.libs["bend"].donor_factors, n, nf, 2, dtm, available, aux, g["length"], g["area"],
+                     g["offset"], g["faces"], g["signs"], factors)
+        self._invoke(self.libs["bend"].limit_flux, nf, 2, g["owner"], g["neighbour"], factors, aux)
+        donor = float(np.min(factors))
+        integral = dtm * aux[2]
+        rate = np.zeros(n)
+        self._invoke(self.libs["bend"].divergence, n, nf, 2, aux, g["length"], g["area"], g["offset"], g["faces"],
+                     g["signs"], rate)
+        ztrial = z0 + (dtm / phi) * rate
+        outside = (j < 0) & (m.bid >= 0)
+        boundary = -np.sum(integral * m.length * outside)
+        residual = np.sum(phi * (ztrial - z0) * m.area) - boundary
+        change = float(np.max(np.abs(ztrial - z0) / np.maximum(q[0], ex["sediment_depth"])))
+        ok = (np.all(np.isfinite(ztrial)) and not np.any(ztrial < rock - 1e-13) and abs(float(residual)) <= 1e-10
+              and change <= .05)
+        return ztrial, dict(ok=bool(ok), residual=float(residual), boundary=float(boundary), donor=donor,
+                            change=change, flux=aux[2].copy(), cell=cell, face=face, corrected=corrected)
 
     def hkt_gradients(self, q, z=None):
         m = self.m
