@@ -33,6 +33,8 @@ SIGNATURES = {
     "brx_turbines_set": (I, [P, I, P, P, P, I, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P]),
     "brx_turbines_diagnose": (I, [P, P]),
     "brx_turbines_last": (I, [P, P]),
+    "brx_exner_set": (I, [P, P, P, P, P, P, P, P, P]),
+    "brx_exner": (I, [P, P, P]),
     "brx_advance_start": (I, [P, P, P]),
     "brx_advance_poll": (I, [P, P, P]),
     "brx_solver_bytes": (C.c_longlong, [P]),

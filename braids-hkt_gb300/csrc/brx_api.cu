@@ -23,6 +23,7 @@
 #include "brx_kernels.cuh"
 #include "brx_launch.h"
 #include "brx_turbine.cuh"
+#include "brx_exner.cuh"
 
 using namespace brx;
 
@@ -84,6 +85,10 @@ struct brx_solver {
     bool has_turb = false;
     int nrotor = 0;
     double *d_tdiag_out = nullptr;   // (nrotor, 16) diagnostics of brx_turbines_diagnose
+    ExnerDev exner{};                // bed model (valid when has_exner)
+    bool has_exner = false;
+    int *d_cell_off = nullptr, *d_face_off = nullptr;
+    double *d_exdt = nullptr;
 
     template <class T> int alloc(T **p, size_t count)
     {
@@ -623,6 +628,98 @@ extern "C" int brx_turbines_set(brx_solver *s, int nrotor, const int *rotor_scen
     s->has_turb = true;
     s->nrotor = nrotor;
     s->graph_dirty = true;
+    return BRX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Exner bed update
+// ---------------------------------------------------------------------------
+extern "C" int brx_exner_set(brx_solver *s, const int *enabled, const double *param, const int *bedbc,
+                             const double *feed, const double *rock, const double *dxdy, const double *inverse,
+                             const double *xy)
+{
+    if (!s) return fail(BRX_ERR_ARGUMENT, "null solver");
+    if (s->has_exner) return fail(BRX_ERR_STATE, "a bed model is already installed");
+    if (!enabled || !param || !bedbc || !feed || !rock || !dxdy || !inverse || !xy)
+        return fail(BRX_ERR_ARGUMENT, "missing bed-model input");
+    const int nc = s->nc, nf = s->nf, nadj = s->nadj, ns = s->nscen;
+    std::vector<double> par((size_t)ns * EP_N, 0.);
+    for (int i = 0; i < ns; ++i) {
+        if (!enabled[i]) continue;
+        const double *p = param + 5 * (size_t)i;
+        const double d = p[0], porosity = p[1], chezy = p[2], morfac = p[3], sd = p[4];
+        if (!(d > 0) || !(porosity >= 0 && porosity < 1) || !(chezy >= 20) || !(morfac > 0) || !(sd >= .001))
+            return fail(BRX_ERR_ARGUMENT, "bed model: diameter > 0, 0 <= porosity < 1, Chezy >= 20, morfac > 0, "
+                                          "sediment depth >= 1 mm required");
+        // one-grain mixture: D90 of the log-linear grain distribution and the
+        // Egiazaroff hiding factor (river_mpm.h:12-30)
+        const double logd = std::log(d), lo = logd + 1.25 * std::log(.75), hi = logd + 1.25 * std::log(1.5);
+        const double mean = d * 1. / 1., r = d / std::fmax(mean, 1.e-4), v = 1.27875360095283;
+        const double hiding = std::pow(v / (v + std::log10(r)), 2.);
+        double low = lo, high = hi;
+        for (int it = 0; it < 60; ++it) {
+            const double mid = .5 * (low + high);
+            double f = 0.;
+            if (mid >= hi) f = 1.;
+            else if (mid > logd) f = .5 + .5 * (mid - logd) / (hi - logd);
+            else if (mid > lo) f = .5 * (mid - lo) / (logd - lo);
+            if (1. / 1. * f < .9) low = mid; else high = mid;
+        }
+        double *q = par.data() + (size_t)i * EP_N;
+        q[EP_D] = d; q[EP_POROSITY] = porosity; q[EP_CHEZY] = chezy; q[EP_MORFAC] = morfac; q[EP_SEDDEPTH] = sd;
+        q[EP_D90] = std::exp(.5 * (low + high)); q[EP_HIDING] = hiding;
+    }
+    ExnerDev e{};
+    int *p_en, *p_bc;
+    double *p_par, *p_feed, *p_rock, *p_dxdy, *p_inv, *p_xy;
+    TRY(s->upload(&p_en, enabled, ns)); TRY(s->upload(&p_par, par.data(), par.size()));
+    TRY(s->upload(&p_bc, bedbc, nf)); TRY(s->upload(&p_feed, feed, nf)); TRY(s->upload(&p_rock, rock, nc));
+    TRY(s->upload(&p_dxdy, dxdy, 2 * (size_t)nadj)); TRY(s->upload(&p_inv, inverse, 3 * (size_t)nc));
+    TRY(s->upload(&p_xy, xy, 2 * (size_t)nc));
+    e.enabled = p_en; e.param = p_par; e.bedbc = p_bc; e.feed = p_feed; e.rock = p_rock;
+    e.dxdy = p_dxdy; e.inverse = p_inv; e.xy = p_xy;
+    TRY(s->alloc(&e.cell, 6 * (size_t)nc)); TRY(s->alloc(&e.gz, 2 * (size_t)nc)); TRY(s->alloc(&e.flux, nf));
+    TRY(s->alloc(&e.fac, nc)); TRY(s->alloc(&e.ztrial, nc)); TRY(s->alloc(&e.stats, (size_t)ns * ES_N));
+    TRY(s->alloc(&e.wet, nc)); TRY(s->alloc(&e.bad, ns));
+    TRY(s->alloc(&s->d_exdt, ns));
+    e.dt = s->d_exdt;
+    TRY(s->upload(&s->d_cell_off, s->cell_offset.data(), s->cell_offset.size()));
+    TRY(s->upload(&s->d_face_off, s->face_offset.data(), s->face_offset.size()));
+    s->exner = e;
+    s->has_exner = true;
+    return BRX_OK;
+}
+
+// One bed update of every scenario with a bed model, from the accepted state
+// over its interval dt[i] (x morfac); a scenario's bed is replaced only where
+// its checks pass. stats (nscen, 8): ok, solid-volume residual [m3], boundary
+// solid volume [m3], donor minimum, maximum relative change, slope-operator
+// failure.
+extern "C" int brx_exner(brx_solver *s, const double *dt, double *stats)
+{
+    TRY(ensure_ready(s));
+    if (!s->has_exner) return fail(BRX_ERR_STATE, "no bed model installed");
+    if (!dt || !stats) return fail(BRX_ERR_ARGUMENT, "null argument");
+    for (int i = 0; i < s->nscen; ++i)
+        if (!(dt[i] >= 0) || !std::isfinite(dt[i])) return fail(BRX_ERR_ARGUMENT, "dt must be finite and >= 0");
+    const ExnerDev &e = s->exner;
+    cudaStream_t st = s->stream;
+    CK(cudaMemcpyAsync(s->d_exdt, dt, sizeof(double) * s->nscen, cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(e.bad, 0, sizeof(int) * s->nscen, st));
+    CK(cudaMemsetAsync(e.stats, 0, sizeof(double) * s->nscen * ES_N, st));
+    const double *q = s->state.q[0];
+    double *z = const_cast<double *>(s->state.z);     // the caller's bound bed, updated in place
+    k_ex_cells<<<s->grid_c256, 256, 0, st>>>(s->mesh, e, q, z);
+    k_ex_faces<<<s->grid_f, 128, 0, st>>>(s->mesh, e, z);
+    k_ex_donor<<<s->grid_c256, 256, 0, st>>>(s->mesh, e, z);
+    k_ex_limit<<<s->grid_f256, 256, 0, st>>>(s->mesh, e);
+    k_ex_trial<<<s->grid_c256, 256, 0, st>>>(s->mesh, e, z);
+    k_ex_reduce<<<s->nscen, 256, 0, st>>>(s->mesh, e, q, z, s->d_cell_off, s->d_face_off);
+    k_ex_commit<<<s->grid_c256, 256, 0, st>>>(s->mesh, e, z);
+    s->launches += 7;
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(stats, e.stats, sizeof(double) * s->nscen * ES_N, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
     return BRX_OK;
 }
 

@@ -154,10 +154,12 @@ __global__ void k_boundary(MeshDev m, StateDev s, BoundaryDev b, Ctrl *ctrl, int
                 if (t <= b.table_time[0]) val = y[0];
                 else if (t >= b.table_time[L - 1]) val = y[L - 1];
                 else {
+                    // last knot at or before t, capped at L - 2; (1 - w) y_i + w y_{i+1}
+                    // (RiverHydraulicSchedule.sample, river_hydraulic_schedule.py:57-65)
                     int i = 0;
-                    while (b.table_time[i + 1] < t) ++i;
-                    const double sfrac = (t - b.table_time[i]) / (b.table_time[i + 1] - b.table_time[i]);
-                    val = y[i] + (y[i + 1] - y[i]) * sfrac;
+                    while (i < L - 2 && b.table_time[i + 1] <= t) ++i;
+                    const double w = (t - b.table_time[i]) / (b.table_time[i + 1] - b.table_time[i]);
+                    val = (1. - w) * y[i] + w * y[i + 1];
                 }
                 b.forcing[(size_t)row * b.nseg + sg] = val;
             }

@@ -132,6 +132,80 @@ def small_rotor_channel(length=150.0, width=30.0, spacing=1.5, seed=21, discharg
     return case
 
 
+def config3(length=10000.0, width=1500.0, spacing=3.87, channels=5, seed=3, amplitude=200.0,
+            channel_depth=(2.0, 4.0), sigma=0.5, corr=50.0, slope=1e-3, rotors=12, rotor_d=2.0,
+            q_low=200.0, q_high=2000.0, rise_s=3600.0, stage_above=0.5, grain=0.02):
+    """Braided river (config 3): ``channels`` seeded sinuous channels
+    (amplitude ``amplitude`` m, depth U(channel_depth)) cut into a floodplain
+    of slope ``slope`` carrying a Gaussian field (sigma, corr), stage outlet
+    ``stage_above`` m over the floodplain at the outlet (extensive wet/dry),
+    inlet hydrograph q_low -> q_high m3/s over rise_s seconds (forcing
+    table), MPM bed update (d50 = grain, porosity 0.4) and ``rotors``
+    staggered rotors of diameter rotor_d on the deepest channels, their
+    footprints refined. The full size (10 km x 1.5 km, 3.87 m) is about 2M
+    triangles; tests use a scaled-down copy."""
+    rng = np.random.default_rng(seed)
+    ys = (np.arange(channels) + 1.0) / (channels + 1.0) * width
+    wl = rng.uniform(0.8, 1.6, channels) * 10.0 * width / 1.5 / channels * 1.5   # meander wavelengths
+    phase = rng.uniform(0.0, 2 * np.pi, channels)
+    half = rng.uniform(0.02, 0.04, channels) * width
+    depth = rng.uniform(channel_depth[0], channel_depth[1], channels)
+    amp = amplitude * width / 1500.0
+
+    def centre(k, x):
+        return ys[k] + amp * np.sin(2 * np.pi * x / wl[k] + phase[k])
+
+    # rotors: staggered along the deepest channels, away from the ends
+    order = np.argsort(-depth)
+    centres = []
+    for j in range(rotors):
+        k = int(order[j % max(1, min(channels, 3))])
+        x = length * (0.3 + 0.5 * (j + 0.5) / rotors)
+        centres.append((float(x), float(centre(k, x))))
+    fine = min(spacing, 0.35 * rotor_d)
+    boxes = [(x - 3 * rotor_d, x + 3 * rotor_d, y - 3 * rotor_d, y + 3 * rotor_d, fine) for x, y in centres]
+    mesh = M.channel_mesh(length, width, spacing, 0.25 * spacing, seed, refine=boxes)
+    grid = M.gaussian_field(length, width, sigma, corr, rng, min(spacing, 5.0))
+    x, y = mesh.xy
+    floodplain = slope * (length - x) + M.sample_field(grid, x, y)
+    cut = np.zeros_like(x)
+    for k in range(channels):
+        d = np.abs(y - centre(k, x))
+        cut = np.maximum(cut, depth[k] * np.clip(1.0 - (d / half[k]) ** 2, 0.0, None))
+    z = floodplain - cut
+    apron = x > length - 3 * spacing
+    z = np.where(apron, np.minimum(z, -max(channel_depth)), z)
+    # inlet forebay: a flat pool across the inlet, filled to the floodplain
+    # level there, so the total-discharge inlet sees a wet cross-section
+    level = float(slope * length)
+    forebay = x < 4 * spacing
+    z = np.where(forebay, level - max(channel_depth), z)
+    z = np.ascontiguousarray(z)
+    stage = stage_above
+    h = np.maximum(np.maximum(stage - z, 0.0), np.where(cut > 0, floodplain - z, 0.0))
+    h = np.where(forebay, level - z, h)
+    q = np.ascontiguousarray(np.stack((h, np.zeros_like(h), np.zeros_like(h))))
+    case = dict(mesh=mesh, z=z, q=q, seg_mode=np.array([M.MODE_TOTAL_Q, M.MODE_STAGE], np.int32),
+                stage_policy=np.zeros(2, np.int32), forcing=np.array([[q_low, 0.0], [0.0, stage]]),
+                exterior_bed=_exterior_bed(mesh, z), controls=controls(0.9, 0.03),
+                name=f"braided_{length:g}x{width:g}")
+    times = np.array([0.0, rise_s, 10 * rise_s])
+    value = np.zeros((2, 2, 3))
+    value[0, 0] = [q_low, q_high, q_high]
+    value[1, 1] = stage
+    case["table_time"], case["table_value"] = times, value
+    case["exner"] = exner_params(case, diameter=grain, chezy=40.0, erodible=2.0)
+    control = {"mode": "constant_ct", "thrust_coefficient": 0.8, "power_coefficient": None}
+    rows = []
+    for k, (cx, cy) in enumerate(centres):
+        cells, _ = __import__("braids_hkt_gb300.turbines", fromlist=["x"]).bump_integrals(mesh, cx, cy, rotor_d)
+        hub = float(np.max(z[cells])) + 0.3 + 0.5 * rotor_d
+        rows.append(dict(name=f"R{k + 1}", X=cx, Y=cy, D=float(rotor_d), hub_elevation_m=round(hub, 3),
+                         minimum_bed_clearance_m=0.1, minimum_surface_clearance_m=0.2, control=control, nu=0.0))
+    case["turbines"] = rows
+    return case
+
+
 def exner_params(case, diameter=0.002, porosity=0.4, chezy=44.0, morfac=1.0, sediment_depth=0.001,
                  erodible=2.0, inlet_bc=3, outlet_bc=2, feed=0.0):
     """Bed-update parameters of one scenario: a single grain size, porosity,

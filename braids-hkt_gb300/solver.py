@@ -154,6 +154,9 @@ class RiverSolver:
                 _ptr(tp["support_cell"]), _ptr(tp["support_weight"]), _ptr(tp["support_density"]),
                 _ptr(tp["plane_offset"]), _ptr(tp["plane_cell"]), _ptr(tp["plane_delta"]), _ptr(tp["dxdy"]),
                 _ptr(tp["inverse"]), _ptr(tp["xy"]), _ptr(tp["mid_disp"]), _ptr(tp["nu"]), _ptr(tp["hkt"])))
+        self.bed_model = None
+        if any(c.get("exner") for c in self.cases):
+            self._set_exner()
         self.time = np.zeros(self.nscen)
         self.steps = 0
 
@@ -175,6 +178,51 @@ class RiverSolver:
 
     def launches(self):
         return int(self.lib.brx_launch_count(self.h))
+
+    # --- Exner bed model -------------------------------------------------
+    def _set_exner(self):
+        from . import turbines as TB
+        p = self.packed
+        en = np.zeros(self.nscen, np.int32)
+        par = np.zeros((self.nscen, 5))
+        bedbc = np.zeros(self.nf, np.int32)
+        feed = np.zeros(self.nf)
+        rock = np.full(self.nc, -1e30)
+        dxdy, inv, xy = [], [], []
+        for i, case in enumerate(self.cases):
+            m = case["mesh"]
+            c0, c1 = p["cell_offset"][i], p["cell_offset"][i + 1]
+            f0, f1 = p["face_offset"][i], p["face_offset"][i + 1]
+            ex = case.get("exner")
+            flow = case.get("_flow") or TB.flow_geometry(m)
+            case["_flow"] = flow
+            dxdy.append(flow[0]); inv.append(flow[1]); xy.append(m.xy)
+            if not ex:
+                continue
+            en[i] = 1
+            par[i] = (ex["diameter"], ex["porosity"], ex["chezy"], ex.get("morfac", 1.0), ex["sediment_depth"])
+            bedbc[f0:f1] = ex["bedbc"]
+            feed[f0:f1] = ex["feed"]
+            rock[c0:c1] = ex["rock"]
+        self.bed_model = en
+        cat = lambda a: np.ascontiguousarray(np.concatenate(a, axis=1))
+        self._ex_keep = (cat(dxdy), cat(inv), cat(xy))
+        check(self.lib.brx_exner_set(self.h, _ptr(en), _ptr(_f64(par)), _ptr(bedbc), _ptr(feed), _ptr(rock),
+                                     _ptr(self._ex_keep[0]), _ptr(self._ex_keep[1]), _ptr(self._ex_keep[2])))
+
+    def morphology(self, dt):
+        """One Exner bed update of the current state over dt (scalar or per scenario);
+        per-scenario dicts: ok, solid-volume residual and boundary [m3], donor
+        minimum, maximum relative change. The bed is replaced where ok."""
+        if self.bed_model is None:
+            raise ValueError("no bed model")
+        self.torch.cuda.current_stream().synchronize()
+        d = _f64(np.broadcast_to(dt, (self.nscen,)) * (self.bed_model > 0))
+        stats = np.zeros((self.nscen, 8))
+        check(self.lib.brx_exner(self.h, _ptr(d), _ptr(stats)))
+        out = [dict(ok=bool(r[0]), residual=r[1], boundary=r[2], donor=r[3], change=r[4], slope_failure=bool(r[5]))
+               for r in stats]
+        return out[0] if self.single else out
 
     # --- rotor arrays ---------------------------------------------------
     def turbine_record(self, last=False):

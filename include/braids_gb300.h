@@ -98,9 +98,12 @@ int brx_controls_set(brx_solver *s, int scen, double gravity, double dry, double
 int brx_boundary_set(brx_solver *s, const int *seg_mode, const int *stage_policy,
                      const double *exterior_bed, const double *forcing);
 
-/* Piecewise-linear forcing tables: time (len), value (2,nseg,len). len = 0
- * returns to constant forcing. Replaces HydraulicForcing.sample
- * (src/braids_core/river_hydraulic_schedule.py). */
+/* Piecewise-linear forcing tables: time (len >= 2, increasing), value
+ * (2,nseg,len) rows discharge and stage. len = 0 returns to constant forcing.
+ * Replaces RiverHydraulicSchedule.sample
+ * (src/braids_core/river_hydraulic_schedule.py:57-65): the same knot choice
+ * and (1 - w) y_i + w y_{i+1}. Outside the table the end values hold (the
+ * reference raises instead; keep evaluation times inside the table). */
 int brx_forcing_table_set(brx_solver *s, int len, const double *time, const double *value);
 
 /* Bind caller-owned DEVICE buffers: q (3,nc) accepted state, updated in place;
@@ -173,6 +176,30 @@ int brx_turbines_set(brx_solver *s, int nrotor, const int *rotor_scenario, const
 int brx_turbines_diagnose(brx_solver *s, double *out);
 /* The same record for the state of the last evaluated stage. */
 int brx_turbines_last(brx_solver *s, double *out);
+
+/* Exner bed model (replaces ShorelinePhysics.finish with morphology:
+ * src/braids_core/sediment/shoreline_solver.py:218-240 with the MPM
+ * capacity of river_mpm.py:21-33, one grain size, no secondary-flow spiral).
+ *   enabled (nscen)          1 where a scenario has a bed model
+ *   param (nscen, 5)         grain diameter [m], porosity, Chezy coefficient,
+ *                            morphological factor, sediment working depth [m]
+ *   bedbc (nf)               boundary faces: 0 wall, 1 prescribed feed, 2 open
+ *                            outflow, 3 transport capacity
+ *   feed (nf), rock (nc)     prescribed solid volume inflow per length [m2/s],
+ *                            non-erodible elevation
+ *   dxdy, inverse, xy        the flow engines' least-squares metric (as for
+ *                            brx_turbines_set) and the cell centroids
+ * Host arrays, copied. */
+int brx_exner_set(brx_solver *s, const int *enabled, const double *param, const int *bedbc, const double *feed,
+                  const double *rock, const double *dxdy, const double *inverse, const double *xy);
+
+/* One bed update of the bound accepted state over dt (nscen, host; 0 skips a
+ * scenario) times each scenario's morphological factor. The bound bed is
+ * replaced where the scenario's checks pass (finite, above the non-erodible
+ * layer, solid-volume residual <= 1e-10 m3, change <= 5% of the depth);
+ * stats (nscen, 8 doubles, host): ok, residual, boundary solid volume, donor
+ * minimum, maximum relative change, slope-operator failure. */
+int brx_exner(brx_solver *s, const double *dt, double *stats);
 
 /* Asynchronous form of brx_advance_batch for serving loops: start launches
  * the interval's first CUDA-graph chunk and returns; poll never blocks. It

@@ -787,10 +787,11 @@ void om_sample_forcing(om_ctx *m, double t)
             if (t <= m->table_time[0]) val = y[0];
             else if (t >= m->table_time[L - 1]) val = y[L - 1];
             else {
+                /* river_hydraulic_schedule.py:57-65 (inside the table) */
                 int i = 0;
-                while (m->table_time[i + 1] < t) ++i;
-                const double s = (t - m->table_time[i]) / (m->table_time[i + 1] - m->table_time[i]);
-                val = y[i] + (y[i + 1] - y[i]) * s;
+                while (i < L - 2 && m->table_time[i + 1] <= t) ++i;
+                const double w = (t - m->table_time[i]) / (m->table_time[i + 1] - m->table_time[i]);
+                val = (1. - w) * y[i] + w * y[i + 1];
             }
             m->forcing[row * nb + b] = val;
         }

@@ -113,6 +113,8 @@ def _setup(L):
     L.om_advance.argtypes = [P, P, P, D, D, P, P, P]
     L.om_advance.restype = I
     L.om_set_threads.argtypes = [I]
+    L.om_sample_forcing.argtypes = [P, D]
+    L.om_sample_forcing.restype = None
     L.om_turbines_size.restype = C.c_size_t
     assert L.om_turbines_size() == C.sizeof(Turbines), "oracle turbine layout differs"
     L.om_exner_size.restype = C.c_size_t
@@ -233,6 +235,11 @@ class Oracle:
         t.kcell = k("t_kcell", np.zeros(max(ns, 1)))
         t.fstatus = k("t_fstatus", np.zeros(m.nf, np.int32))
         self._turb = t
+
+    def sample_forcing(self, t):
+        """Forcing (2, nb) at time t from the case's tables."""
+        self.L.om_sample_forcing(self.cp, float(t))
+        return self.forcing.copy()
 
     def exner(self, q, dt, z0=None):
         """One bed update of the accepted state q over dt: (status, z_trial, stats dict)."""
