@@ -580,6 +580,25 @@ extern "C" int brx_turbines_set(brx_solver *s, int nrotor, const int *rotor_scen
     TRY(s->upload(&p_pdel, plane_delta, 2 * (size_t)np_));
     TRY(s->upload(&p_param, param, (size_t)nrotor * TP_N)); TRY(s->upload(&p_curve, curve, 4 * (size_t)nrotor));
     TRY(s->upload(&p_cx, curve_x, ncurve)); TRY(s->upload(&p_cy, curve_y, ncurve));
+    // knot slopes, formed once (the same IEEE division the lookup would do),
+    // and which thrust tables are constant
+    std::vector<double> slope(ncurve, 0.);
+    std::vector<int> flat(nrotor, 0);
+    for (int r = 0; r < nrotor; ++r) {
+        const int *cv = curve + 4 * r;
+        if ((int)param[r * TP_N + TP_MODE] == TM_CONSTANT) continue;
+        for (int pair = 0; pair < 2; ++pair) {
+            const int first = cv[2 * pair], count = cv[2 * pair + 1];
+            for (int k = first; k + 1 < first + count; ++k)
+                slope[k] = (curve_y[k + 1] - curve_y[k]) / (curve_x[k + 1] - curve_x[k]);
+        }
+        bool same = true;
+        for (int k = cv[0] + 1; k < cv[0] + cv[1]; ++k) same = same && curve_y[k] == curve_y[cv[0]];
+        flat[r] = same;
+    }
+    double *p_slope;
+    int *p_flat;
+    TRY(s->upload(&p_slope, slope.data(), ncurve)); TRY(s->upload(&p_flat, flat.data(), nrotor));
     TRY(s->upload(&p_ucell, ucell.data(), ucell.size())); TRY(s->upload(&p_uoff, uoff.data(), uoff.size()));
     TRY(s->upload(&p_uent, uent.data(), uent.size()));
     TRY(s->upload(&p_dxdy, dxdy, 2 * (size_t)nadj)); TRY(s->upload(&p_inv, inverse, 3 * (size_t)nc));
@@ -589,6 +608,7 @@ extern "C" int brx_turbines_set(brx_solver *s, int nrotor, const int *rotor_scen
     t.support_offset = p_soff; t.support_cell = p_scell; t.support_weight = p_sw; t.support_density = p_sd;
     t.plane_offset = p_poff; t.plane_cell = p_pcell; t.plane_delta = p_pdel;
     t.param = p_param; t.curve = p_curve; t.curve_x = p_cx; t.curve_y = p_cy;
+    t.curve_slope = p_slope; t.flat_thrust = p_flat;
     t.ucell = p_ucell; t.uoff = p_uoff; t.uent = p_uent;
     t.dxdy = p_dxdy; t.inverse = p_inv; t.xy = p_xy; t.mdisp = p_md; t.nu = p_nu;
     TRY(s->alloc(&t.kcell, ns)); TRY(s->alloc(&t.raw, 2 * (size_t)nc));

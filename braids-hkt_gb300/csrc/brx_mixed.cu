@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(128) km_bed(MeshDev m, StateDev s, MixedGeo g)
 // Cells: limited gradients and the cell record
 // ---------------------------------------------------------------------------
 template <int MAXF>
-__global__ void __launch_bounds__(128) km_cells(MeshDev m, StateDev s, Ctrl *ctrl, Work w, MixedGeo g, int stage)
+__global__ void __launch_bounds__(128, 8) km_cells(MeshDev m, StateDev s, Ctrl *ctrl, Work w, MixedGeo g, int stage)
 {
     const int nc = m.nc;
     MxRec *rec = reinterpret_cast<MxRec *>(w.rec);
@@ -402,7 +402,7 @@ __device__ __forceinline__ float hydro_perturbation(float dh, float hL, float h,
     return __fadd_rn(__fmul_rn(dh, hL + h), __fmul_rn(h + raw, db));
 }
 
-__global__ void __launch_bounds__(128) km_faces(MeshDev m, StateDev s, BoundaryDev b, Ctrl *ctrl, Work w,
+__global__ void __launch_bounds__(128, 8) km_faces(MeshDev m, StateDev s, BoundaryDev b, Ctrl *ctrl, Work w,
                                                 MixedGeo g, int stage, TurbDev t, int turb)
 {
     const int nf = m.nf, nc = m.nc;

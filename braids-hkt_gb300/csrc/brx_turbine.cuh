@@ -82,8 +82,10 @@ __global__ void __launch_bounds__(256) k_hkt_gradients(MeshDev m, TurbDev t, con
     }
 }
 
-// numpy.interp on one table, zero outside [x0, xlast)
-__device__ __forceinline__ double table_lookup(const double *x, const double *y, int count, double v)
+// numpy.interp on one table, zero outside [x0, xlast); the knot slopes
+// (y[k+1]-y[k])/(x[k+1]-x[k]) are precomputed with the same division
+__device__ __forceinline__ double table_lookup(const double *x, const double *y, const double *slope, int count,
+                                               double v)
 {
     if (!(v >= x[0]) || v >= x[count - 1]) return 0.;
     int lo = 0, hi = count - 1;           // x[lo] <= v < x[hi]
@@ -92,8 +94,7 @@ __device__ __forceinline__ double table_lookup(const double *x, const double *y,
         if (x[mid] <= v) lo = mid; else hi = mid;
     }
     if (v == x[lo]) return y[lo];
-    const double slope = (y[lo + 1] - y[lo]) / (x[lo + 1] - x[lo]);
-    return slope * (v - x[lo]) + y[lo];
+    return slope[lo] * (v - x[lo]) + y[lo];
 }
 
 // Thetis terms of one cell: K, P, incident speed U, Ct, Cp. Returns 0 or an error code.
@@ -103,8 +104,8 @@ __device__ int rotor_cell_terms(const TurbDev &t, int r, double depth, double u,
     const double D = p[TP_D];
     const int mode = (int)p[TP_MODE];
     const int *cv = t.curve + 4 * r;
-    const double *tx = t.curve_x + cv[0], *ty = t.curve_y + cv[0];
-    const double *px = t.curve_x + cv[2], *py = t.curve_y + cv[2];
+    const double *tx = t.curve_x + cv[0], *ty = t.curve_y + cv[0], *ts = t.curve_slope + cv[0];
+    const double *px = t.curve_x + cv[2], *py = t.curve_y + cv[2], *ps = t.curve_slope + cv[2];
     const double speed = hypot(u, v);
     const double area = PI_D * (D * D) / 4;
     if (mode == TM_INCIDENT_TABLE || mode == TM_INCIDENT_CURVES) {
@@ -115,27 +116,38 @@ __device__ int rotor_cell_terms(const TurbDev &t, int r, double depth, double u,
         const double smax = high * .5 * (1 + sqrt(1 - c * ty[cv[1] - 1]));
         const bool active = speed >= smin && speed < smax;
         // induction-corrected operating point: bisection on the incident speed
-        for (int it = 0; it < 44; ++it) {
-            const double mid = .5 * (low + high);
-            const double ct = table_lookup(tx, ty, cv[1], mid);
-            const double local = mid * .5 * (1 + sqrt(1 - c * ct));
-            if (local < speed) low = mid; else high = mid;
+        if (t.flat_thrust[r]) {
+            // constant Ct: every lookup inside the table returns ty[0] (slope 0),
+            // and 0 at or above the last knot; the square root is hoisted
+            const double in_table = .5 * (1 + sqrt(1 - c * ty[0])), beyond = .5 * (1 + sqrt(1 - c * 0.));
+            for (int it = 0; it < 44; ++it) {
+                const double mid = .5 * (low + high);
+                const double local = mid * ((mid >= tx[0] && mid < tx[cv[1] - 1]) ? in_table : beyond);
+                if (local < speed) low = mid; else high = mid;
+            }
+        } else {
+            for (int it = 0; it < 44; ++it) {
+                const double mid = .5 * (low + high);
+                const double ct = table_lookup(tx, ty, ts, cv[1], mid);
+                const double local = mid * .5 * (1 + sqrt(1 - c * ct));
+                if (local < speed) low = mid; else high = mid;
+            }
         }
         const double incident = active ? .5 * (low + high) : speed;
-        const double ct = active ? table_lookup(tx, ty, cv[1], incident) : 0.;
-        const double cp = active ? table_lookup(px, py, cv[3], incident) : 0.;
+        const double ct = active ? table_lookup(tx, ty, ts, cv[1], incident) : 0.;
+        const double cp = active ? table_lookup(px, py, ps, cv[3], incident) : 0.;
         const double alpha = .5 * (1 + sqrt(1 - c * ct));
         out[0] = area * ct / (2 * (alpha * alpha));
         out[1] = .5 * area * cp * (incident * incident * incident);
         out[2] = incident; out[3] = ct; out[4] = cp;
         return 0;
     }
-    const double ct = mode == TM_CONSTANT ? p[TP_CT] : table_lookup(tx, ty, cv[1], speed);
+    const double ct = mode == TM_CONSTANT ? p[TP_CT] : table_lookup(tx, ty, ts, cv[1], speed);
     const double radicand = 1 - area * ct / (D * depth);
     if (radicand < 0) return 1;
     const double alpha = .5 * (1 + sqrt(radicand));
     const double incident = speed / alpha;
-    const double cp = mode == TM_CONSTANT ? p[TP_CP] : table_lookup(px, py, cv[3], incident);
+    const double cp = mode == TM_CONSTANT ? p[TP_CP] : table_lookup(px, py, ps, cv[3], incident);
     out[0] = area * ct / (2 * (alpha * alpha));
     out[1] = .5 * area * cp * (incident * incident * incident);
     out[2] = incident; out[3] = ct; out[4] = cp;
