@@ -44,7 +44,7 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def build_workload(name, rank=0, world=1):
+def build_workload(name, rank=0, world=1, subset=None):
     """(cases, precision, outer dt [s], config dict). Built before CUDA starts (spawn pool)."""
     import braids_hkt_gb300.scenarios as S
     if name == "config1":
@@ -53,6 +53,9 @@ def build_workload(name, rank=0, world=1):
                                                "CFL 0.9, FP64 plain form")
     if name == "config4":
         params = S.config4_params(64, seed=4 + rank)
+        if subset:
+            a, b = (int(v) for v in subset.split(":"))
+            params = sorted(params, key=lambda p: p["cells"])[a:b]
         workers = max(1, (os.cpu_count() or 1) // max(world, 1))
         cases = S.build_cases(params, workers)
         rotors = sum(len(c.get("turbines", [])) for c in cases)
@@ -251,6 +254,10 @@ def main():
     ap.add_argument("--plain", type=int, default=3, help="scenarios re-run one by one in plain FP64")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true", help="skip the scaled config-5 serving session")
+    ap.add_argument("--subset", default=None,
+                    help="START:STOP slice of the config-4 scenarios sorted by size (profiling a smaller case)")
+    ap.add_argument("--profile-only", type=int, default=0,
+                    help="only time N substeps kernel by kernel (brx_profile_substep) and exit")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
@@ -258,9 +265,16 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    cases, precision, outer, cfg = build_workload(args.workload, rank, world)   # before any CUDA use
+    cases, precision, outer, cfg = build_workload(args.workload, rank, world, args.subset)   # before any CUDA use
     import torch
     torch.cuda.set_device(local)
+    if args.profile_only:
+        from braids_hkt_gb300.solver import RiverSolver
+        solver = RiverSolver(cases, precision=precision)
+        dt = 1e-3                   # one trial of every kernel from the initial state, no interval before it
+        for _ in range(args.profile_only):
+            print(json.dumps({"cells": solver.nc, "substep_kernels_ms": solver.profile_substep(dt, 0.0)}))
+        return
     dist = None
     if world > 1:
         import torch.distributed as dist
