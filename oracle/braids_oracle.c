@@ -1777,6 +1777,448 @@ int om_advance(om_ctx *m, double *q, const double *z, double dt, double time, do
     return status;
 }
 
+/* ------------------------------------------------------------------ */
+/* HLLC / MUSCL-Hancock option                                          */
+/*   orchestration  src/braids_core/hydraulics/hllc.py:76-149           */
+/*   kernels        src/braids_core/hydraulics/hllc.h:15-155            */
+/*   rotor pressure src/braids_core/hydraulics/hllc_turbines.h:13-31    */
+/*   rotor momentum src/braids_core/hydraulics/river_turbines.py:27-36  */
+/* ------------------------------------------------------------------ */
+
+/* Cell incidence in the HLLC operator's own order (each cell's faces in
+ * ascending face number, hllc.py:29-34), its least-squares inverse (walls
+ * mirrored, open faces left out, hllc.py:35-43) and the open-face flags. */
+typedef struct {
+    const int *off, *faces, *signs;
+    const double *xy, *mid, *inverse;   /* (2,nc) (2,nf) (3,nc) */
+    const int *selected;                /* (nf) */
+} om_hllc_geo;
+
+/* Limited MUSCL gradients of (eta, u, v, b) and the half-step predictor
+ * (hllc.h:15-50). dt is the predictor's full interval (2 * 0.5 * dt). */
+void om_hllc_reconstruct(const om_ctx *m, const om_hllc_geo *G, double dt, const double *q, const double *z,
+                         double *grad, double *half, double *qhalf, int *status)
+{
+    const int n = m->nc, nf = m->nf;
+    const double dry = m->dry, g = m->grav;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; ++i) {
+        const double h0 = q[i];
+        double c[4] = {h0 + z[i], h0 > dry ? q[n + i] / h0 : 0., h0 > dry ? q[2 * n + i] / h0 : 0., z[i]};
+        double bx[4] = {0., 0., 0., 0.}, by[4] = {0., 0., 0., 0.}, lo[4], hi[4], gr[8];
+        for (int k = 0; k < 4; ++k) lo[k] = hi[k] = c[k];
+        for (int e = G->off[i]; e < G->off[i + 1]; ++e) {
+            const int f = G->faces[e], j = m->owner[f] == i ? m->neighbour[f] : m->owner[f];
+            double dx, dy, o[4];
+            if (j >= 0) {
+                const double hj = q[j];
+                dx = G->xy[j] - G->xy[i];
+                dy = G->xy[n + j] - G->xy[n + i];
+                o[0] = hj + z[j]; o[1] = hj > dry ? q[n + j] / hj : 0.; o[2] = hj > dry ? q[2 * n + j] / hj : 0.;
+                o[3] = z[j];
+                if (o[0] - o[3] <= dry && o[3] >= c[0]) o[0] = c[0];     /* dry bank above the water line */
+            } else {
+                if (G->selected[f]) continue;
+                const double nx = m->normal[f], ny = m->normal[nf + f];
+                const double dist = (G->mid[f] - G->xy[i]) * nx + (G->mid[nf + f] - G->xy[n + i]) * ny;
+                dx = 2. * dist * nx; dy = 2. * dist * ny;
+                for (int k = 0; k < 4; ++k) o[k] = c[k];
+                const double un = c[1] * nx + c[2] * ny;           /* mirrored wall ghost */
+                o[1] -= 2. * un * nx; o[2] -= 2. * un * ny;
+            }
+            const double d2 = dx * dx + dy * dy;
+            if (d2 <= 0.) continue;
+            for (int k = 0; k < 4; ++k) {
+                const double d = o[k] - c[k];
+                bx[k] += d * dx / d2; by[k] += d * dy / d2;
+                lo[k] = fmin(lo[k], o[k]); hi[k] = fmax(hi[k], o[k]);
+            }
+        }
+        const double i0 = G->inverse[i], i1 = G->inverse[n + i], i2 = G->inverse[2 * n + i];
+        for (int k = 0; k < 4; ++k) {
+            const double gx = i0 * bx[k] + i1 * by[k], gy = i1 * bx[k] + i2 * by[k];
+            double lim = 1.;
+            for (int e = G->off[i]; e < G->off[i + 1]; ++e) {
+                const int f = G->faces[e];
+                const double d = gx * (G->mid[f] - G->xy[i]) + gy * (G->mid[nf + f] - G->xy[n + i]);
+                if (d > 0.) lim = fmin(lim, (hi[k] - c[k]) / d);
+                else if (d < 0.) lim = fmin(lim, (lo[k] - c[k]) / d);
+            }
+            gr[2 * k] = lim * gx; gr[2 * k + 1] = lim * gy;
+        }
+        const double h = c[0] - c[3];
+        if (h <= dry) for (int k = 0; k < 6; ++k) gr[k] = 0.;
+        for (int k = 0; k < 8; ++k) grad[(size_t)k * n + i] = gr[k];
+        const double u = c[1], w = c[2];
+        double eta = c[0] - .5 * dt * (u * (gr[0] - gr[6]) + w * (gr[1] - gr[7]) + h * (gr[2] + gr[5]));
+        double uh = u - .5 * dt * (u * gr[2] + w * gr[3] + g * gr[0]);
+        double wh = w - .5 * dt * (u * gr[4] + w * gr[5] + g * gr[1]);
+        if (eta < c[3]) { eta = c[0]; uh = u; wh = w; }
+        if (h <= dry) { eta = c[0]; uh = 0.; wh = 0.; }
+        half[i] = eta; half[n + i] = uh; half[2 * n + i] = wh; half[3 * n + i] = c[3];
+        const double hh = fmax(0., eta - c[3]);
+        qhalf[i] = hh; qhalf[n + i] = hh * uh; qhalf[2 * n + i] = hh * wh;
+        status[i] = !isfinite(eta) || !isfinite(uh) || !isfinite(wh);
+    }
+}
+
+/* HLLC flux of one rotated face, HLLE where a side is dry or the contact
+ * state is inadmissible (hllc.h:52-78). */
+static void om_hllc_flux(double hl, double ul, double vl, double hr, double ur, double vr, double g, double dry,
+                         double out[3], double *speed)
+{
+    const double cl = sqrt(g * hl), cr = sqrt(g * hr);
+    double sl = fmin(ul - cl, ur - cr), sr = fmax(ul + cl, ur + cr);
+    if (hl <= dry) sl = ur - 2. * cr;
+    if (hr <= dry) sr = ul + 2. * cl;
+    *speed = fmax(fabs(sl), fabs(sr));
+    const double fL[3] = {hl * ul, hl * ul * ul + .5 * g * hl * hl, hl * ul * vl};
+    const double fR[3] = {hr * ur, hr * ur * ur + .5 * g * hr * hr, hr * ur * vr};
+    if (hl <= dry && hr <= dry) { out[0] = out[1] = out[2] = 0.; *speed = 0.; return; }
+    if (sl >= 0.) { for (int k = 0; k < 3; ++k) out[k] = fL[k]; return; }
+    if (sr <= 0.) { for (int k = 0; k < 3; ++k) out[k] = fR[k]; return; }
+    const double a = hl * (sl - ul), b = hr * (sr - ur), den = a - b;
+    const double sm = fabs(den) > 1e-30 ? (.5 * g * (hr * hr - hl * hl) + a * ul - b * ur) / den : 0.;
+    if (hl > dry && hr > dry && sl < sm && sm < sr) {
+        const double hs = sm >= 0. ? a / (sl - sm) : b / (sr - sm);
+        if (hs >= 0. && isfinite(hs)) {
+            if (sm >= 0.) {
+                out[0] = fL[0] + sl * (hs - hl); out[1] = fL[1] + sl * (hs * sm - hl * ul);
+                out[2] = fL[2] + sl * (hs * vl - hl * vl);
+            } else {
+                out[0] = fR[0] + sr * (hs - hr); out[1] = fR[1] + sr * (hs * sm - hr * ur);
+                out[2] = fR[2] + sr * (hs * vr - hr * vr);
+            }
+            return;
+        }
+    }
+    const double uL[3] = {hl, hl * ul, hl * vl}, uR[3] = {hr, hr * ur, hr * vr};
+    for (int k = 0; k < 3; ++k) out[k] = (sr * fL[k] - sl * fR[k] + sl * sr * (uR[k] - uL[k])) / (sr - sl);
+}
+
+/* Half-step momentum source on the predicted state (hllc.h:74-77). */
+void om_hllc_predict_source(int n, double dry, double dt, const double *rate, double *half, double *qhalf)
+{
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; ++i) {
+        const double h = qhalf[i];
+        qhalf[n + i] += .5 * dt * rate[n + i];
+        qhalf[2 * n + i] += .5 * dt * rate[2 * n + i];
+        half[n + i] = h > dry ? qhalf[n + i] / h : 0.;
+        half[2 * n + i] = h > dry ? qhalf[2 * n + i] / h : 0.;
+    }
+}
+
+/* Face extrapolation of the predicted primitive m of cell c to face f. */
+static inline double om_hllc_face_value(const om_ctx *m, const om_hllc_geo *G, const double *half,
+                                        const double *grad, int k, int c, int f)
+{
+    const int n = m->nc, nf = m->nf;
+    return half[(size_t)k * n + c] + grad[(size_t)2 * k * n + c] * (G->mid[f] - G->xy[c]) +
+           grad[(size_t)(2 * k + 1) * n + c] * (G->mid[nf + f] - G->xy[n + c]);
+}
+
+/* Face fluxes (hllc.h:80-114): open faces take the exterior flux with the
+ * cell-reference pressure removed; others the hydrostatically reconstructed
+ * HLLC flux with the cell-reference pressure quadrature. */
+void om_hllc_faces(const om_ctx *m, const om_hllc_geo *G, const double *half, const double *grad,
+                   const double *external, const double *ext_trace, double *fl, double *fr, double *speed)
+{
+    const int n = m->nc, nf = m->nf;
+    const double g = m->grav, dry = m->dry;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < nf; ++i) {
+        const int l = m->owner[i], r = m->neighbour[i];
+        const double nx = m->normal[i], ny = m->normal[nf + i];
+        if (G->selected[i]) {
+            const double h = fmax(0., half[l] - half[3 * n + l]);
+            fl[i] = fr[i] = external[i];
+            fl[nf + i] = fr[nf + i] = external[nf + i] - .5 * g * h * h * nx;
+            fl[2 * nf + i] = fr[2 * nf + i] = external[2 * nf + i] - .5 * g * h * h * ny;
+            const double hb = ext_trace[i];
+            const double ub = hb > dry ? (ext_trace[nf + i] * nx + ext_trace[2 * nf + i] * ny) / hb : 0.;
+            speed[i] = fmax(fabs(half[n + l] * nx + half[2 * n + l] * ny) + sqrt(g * h),
+                            fabs(ub) + sqrt(g * fmax(hb, 0.)));
+            continue;
+        }
+        double L[4], R[4];
+        for (int k = 0; k < 4; ++k) {
+            L[k] = om_hllc_face_value(m, G, half, grad, k, l, i);
+            R[k] = r < 0 ? L[k] : om_hllc_face_value(m, G, half, grad, k, r, i);
+        }
+        const int ldry = half[l] - half[3 * n + l] <= dry, rdry = r >= 0 && half[r] - half[3 * n + r] <= dry;
+        if (ldry || rdry) { L[3] = half[3 * n + l]; R[3] = r < 0 ? L[3] : half[3 * n + r]; }
+        if (ldry) { L[0] = L[3]; L[1] = L[2] = 0.; }
+        if (rdry) { R[0] = R[3]; R[1] = R[2] = 0.; }
+        if (r < 0) { const double un = R[1] * nx + R[2] * ny; R[1] -= 2. * un * nx; R[2] -= 2. * un * ny; }
+        const double top = fmax(L[3], R[3]), hl = fmax(0., L[0] - L[3]), hr = fmax(0., R[0] - R[3]);
+        const double hls = fmax(0., L[0] - top), hrs = fmax(0., R[0] - top);
+        double out[3], s;
+        om_hllc_flux(hls, L[1] * nx + L[2] * ny, -L[1] * ny + L[2] * nx,
+                     hrs, R[1] * nx + R[2] * ny, -R[1] * ny + R[2] * nx, g, dry, out, &s);
+        const double el = fmax(0., half[l] - L[3]), er = r < 0 ? el : fmax(0., half[r] - R[3]);
+        const double pl = .5 * g * (hl * hl - hls * hls - el * el), pr = .5 * g * (hr * hr - hrs * hrs - er * er);
+        fl[i] = fr[i] = r < 0 ? 0. : out[0];
+        fl[nf + i] = (out[1] + pl) * nx - out[2] * ny; fl[2 * nf + i] = (out[1] + pl) * ny + out[2] * nx;
+        fr[nf + i] = (out[1] + pr) * nx - out[2] * ny; fr[2 * nf + i] = (out[1] + pr) * ny + out[2] * nx;
+        speed[i] = s;
+    }
+}
+
+/* Low-Froude acoustic correction on fully wet, small-jump interior faces
+ * of a rotor array's mesh (hllc_turbines.h:13-31). */
+void om_hllc_turbine_pressure(const om_ctx *m, const om_hllc_geo *G, const double *half, const double *grad,
+                              double *fl, double *fr)
+{
+    const int n = m->nc, nf = m->nf;
+    const double g = m->grav, dry = m->dry;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < nf; ++i) {
+        const int a = m->owner[i], b = m->neighbour[i];
+        if (b < 0) continue;
+        if (half[a] - half[3 * n + a] <= dry || half[b] - half[3 * n + b] <= dry) continue;
+        double L[4], R[4];
+        for (int k = 0; k < 4; ++k) {
+            L[k] = om_hllc_face_value(m, G, half, grad, k, a, i);
+            R[k] = om_hllc_face_value(m, G, half, grad, k, b, i);
+        }
+        const double bed = fmax(L[3], R[3]), hl = L[0] - bed, hr = R[0] - bed, h = .5 * (hl + hr);
+        if (fmin(hl, hr) <= dry || fabs(hr - hl) > .005 * h) continue;
+        const double c = sqrt(g * h), theta = fmin(1., fmax(hypot(L[1], L[2]), hypot(R[1], R[2])) / c);
+        const double nx = m->normal[i], ny = m->normal[nf + i];
+        const double du = (R[1] - L[1]) * nx + (R[2] - L[2]) * ny;
+        const double delta = .5 * (1. - theta) * c * (2. * hl * hr / (hl + hr)) * du;
+        fl[nf + i] += delta * nx; fr[nf + i] += delta * nx;
+        fl[2 * nf + i] += delta * ny; fr[2 * nf + i] += delta * ny;
+    }
+}
+
+/* Donor budget and CFL frequency per cell (hllc.h:116-132): prescribed
+ * exterior debits are reserved first; theta = -1 marks an unfunded one. */
+void om_hllc_budget(const om_ctx *m, const om_hllc_geo *G, double dt, const double *q, const double *fl,
+                    const double *speed, const int *pstatus, double *theta, double *freq)
+{
+    const int n = m->nc;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; ++i) {
+        double outgoing = 0., prescribed = 0., sum = 0.;
+        for (int e = G->off[i]; e < G->off[i + 1]; ++e) {
+            const int f = G->faces[e];
+            const double debit = fmax(0., G->signs[e] * fl[f]) * m->length[f];
+            if (G->selected[f]) prescribed += debit; else outgoing += debit;
+            sum += speed[f] * m->length[f];
+        }
+        freq[i] = pstatus[i] ? INFINITY : sum / m->area[i];
+        theta[i] = 1.;
+        const double available = q[i] * m->area[i] / dt;
+        if (prescribed > available) theta[i] = -1.;
+        else if (outgoing > 0. && outgoing >= available - prescribed)
+            theta[i] = fmin(1., (available - prescribed) / outgoing) * (1. - 32. * OM_EPS);
+    }
+}
+
+/* Donor limiting of interior faces; unfunded exterior debits flag their face (hllc.h:134-143). */
+void om_hllc_limit(const om_ctx *m, const om_hllc_geo *G, const double *q, const double *theta,
+                   double *fl, double *fr, int *fstatus)
+{
+    const int n = m->nc, nf = m->nf;
+    const double dry = m->dry;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < nf; ++i) {
+        fstatus[i] = 0;
+        const double water = fl[i];
+        const int donor = water < 0. ? m->neighbour[i] : m->owner[i];
+        if (donor < 0 || water == 0.) continue;
+        if (G->selected[i]) { fstatus[i] = theta[donor] < 0. ? 1 : 0; continue; }
+        if (theta[donor] >= 1.) continue;
+        const double factor = fmax(0., theta[donor]), delta = (factor - 1.) * water;
+        fl[i] = fr[i] = water * factor;
+        if (q[donor] > dry)
+            for (int k = 1; k < 3; ++k) {
+                const double d = delta * q[(size_t)k * n + donor] / q[donor];
+                fl[(size_t)k * nf + i] += d; fr[(size_t)k * nf + i] += d;
+            }
+    }
+}
+
+/* Conservative update from the limited fluxes (hllc.h:145-155). */
+void om_hllc_update(const om_ctx *m, const om_hllc_geo *G, double dt, const double *q, const double *fl,
+                    const double *fr, const int *fstatus, double *next, int *status)
+{
+    const int n = m->nc, nf = m->nf;
+    const double dry = m->dry;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; ++i) {
+        double v[3] = {q[i], q[n + i], q[2 * n + i]};
+        int bad = 0;
+        for (int e = G->off[i]; e < G->off[i + 1]; ++e) {
+            const int f = G->faces[e], s = G->signs[e];
+            const double a = dt * s * m->length[f] / m->area[i];
+            const double *src = s > 0 ? fl : fr;
+            for (int k = 0; k < 3; ++k) v[k] -= a * src[(size_t)k * nf + f];
+            bad = bad || fstatus[f];
+        }
+        if (v[0] <= dry) v[1] = v[2] = 0.;
+        for (int k = 0; k < 3; ++k) { next[(size_t)k * n + i] = v[k]; bad = bad || !isfinite(v[k]); }
+        status[i] = bad || v[0] < 0.;
+    }
+}
+
+typedef struct {
+    double *grad, *half, *qhalf, *fl, *fr, *speed, *theta, *freq, *next, *rate, *work;
+    int *pstatus, *fstatus, *status;
+} om_hllc_scratch;
+
+static om_hllc_scratch *om_hllc_scratch_create(const om_ctx *m)
+{
+    const size_t nc = m->nc, nf = m->nf;
+    om_hllc_scratch *S = (om_hllc_scratch *)om_alloc(sizeof(*S));
+    S->grad = om_alloc(8 * nc * 8); S->half = om_alloc(4 * nc * 8); S->qhalf = om_alloc(3 * nc * 8);
+    S->fl = om_alloc(3 * nf * 8); S->fr = om_alloc(3 * nf * 8); S->speed = om_alloc(nf * 8);
+    S->theta = om_alloc(nc * 8); S->freq = om_alloc(nc * 8); S->next = om_alloc(3 * nc * 8);
+    S->rate = om_alloc(3 * nc * 8); S->work = om_alloc(3 * nc * 8);
+    S->pstatus = om_alloc(nc * 4); S->fstatus = om_alloc(nf * 4); S->status = om_alloc(nc * 4);
+    return S;
+}
+
+static void om_hllc_scratch_destroy(om_hllc_scratch *S)
+{
+    void *all[] = {S->grad, S->half, S->qhalf, S->fl, S->fr, S->speed, S->theta, S->freq, S->next, S->rate,
+                   S->work, S->pstatus, S->fstatus, S->status};
+    for (size_t i = 0; i < sizeof(all) / sizeof(all[0]); ++i) free(all[i]);
+    free(S);
+}
+
+/* One Hancock substep (HLLCHydraulics._spatial_step with predictor 0.5):
+ * Strang drag, predictor, half-time rotor source, exterior at t + dt/2
+ * with the outlet stock cap, faces, budget, CFL check, limiter, update,
+ * rotor source at the half state, drag. *peak is the reference's
+ * frequency_peak (0 before the budget; possibly inf or NaN). */
+int om_hllc_single(om_ctx *m, const om_hllc_geo *G, om_scratch *s, om_hllc_scratch *S, const double *q,
+                   const double *z, double dt, double time, double *out, double *water, double *peak)
+{
+    const int n = m->nc, nf = m->nf;
+    *peak = 0.;
+    memcpy(S->work, q, sizeof(double) * 3 * n);
+    om_drag(m, .5 * dt, S->work);
+    om_hllc_reconstruct(m, G, dt, S->work, z, S->grad, S->half, S->qhalf, S->pstatus);
+    if (m->turb) {
+        memset(S->rate, 0, sizeof(double) * 3 * n);
+        if (om_turbine_momentum(m, s, S->work, z, S->rate)) return OM_FAIL;
+        om_hllc_predict_source(n, m->dry, dt, S->rate, S->half, S->qhalf);
+    }
+    const double *ext = s->ext_flux, *ext_trace = s->ext_trace;
+    if (m->nb > 0) {
+        if (om_exterior(m, S->qhalf, z, time + .5 * dt, s->ext_trace, s->ext_flux, s->estatus, s->work, s->stage,
+                        s->total))
+            return OM_REJECT_SPATIAL;
+        om_outlet_feasibility(m, S->work, dt, s->ext_flux, s->ext_trace, s->work);
+    }
+    om_hllc_faces(m, G, S->half, S->grad, ext, ext_trace, S->fl, S->fr, S->speed);
+    if (m->turb) om_hllc_turbine_pressure(m, G, S->half, S->grad, S->fl, S->fr);
+    om_hllc_budget(m, G, dt, S->work, S->fl, S->speed, S->pstatus, S->theta, S->freq);
+    double f = -INFINITY;
+    int nan = 0;
+    for (int i = 0; i < n; ++i) { if (isnan(S->freq[i])) nan = 1; else if (S->freq[i] > f) f = S->freq[i]; }
+    if (nan) f = NAN;                           /* numpy max propagates NaN */
+    *peak = f;
+    if (!isfinite(f) || dt * f > m->cfl * (1 + 1e-12)) return OM_REJECT_CFL;
+    om_hllc_limit(m, G, S->work, S->theta, S->fl, S->fr, S->fstatus);
+    om_hllc_update(m, G, dt, S->work, S->fl, S->fr, S->fstatus, S->next, S->status);
+    for (int i = 0; i < n; ++i) if (S->status[i]) return OM_REJECT_BUDGET;
+    memcpy(out, S->next, sizeof(double) * 3 * n);
+    if (m->turb) {
+        memset(S->rate, 0, sizeof(double) * 3 * n);
+        if (om_turbine_momentum(m, s, S->qhalf, z, S->rate)) return OM_FAIL;
+        for (int i = 0; i < 3 * n; ++i) out[i] += dt * S->rate[i];
+        for (int i = 0; i < 3 * n; ++i) if (!isfinite(out[i])) return OM_REJECT_SPATIAL;
+    }
+    om_drag(m, .5 * dt, out);
+    memcpy(water, S->fl, sizeof(double) * nf);
+    return OM_OK;
+}
+
+/* Adaptive Hancock substeps over one outer interval (HLLCHydraulics.advance,
+ * hllc.py:131-149): no substep cap; a rejection halves the trial (bounded by
+ * the CFL estimate of the frequency seen); more than 100 rejections or a
+ * hint below dt / 2^20 fail the interval. */
+int om_hllc_advance(om_ctx *m, const om_hllc_geo *G, double *q, const double *z, double dt, double time,
+                    double *hint, double *water_mean, om_stats *stats)
+{
+    const int n = m->nc, nf = m->nf;
+    om_scratch *s = om_scratch_create(m);
+    om_hllc_scratch *S = om_hllc_scratch_create(m);
+    double *next = om_alloc(sizeof(double) * 3 * (size_t)n), *w = om_alloc(sizeof(double) * nf);
+    double elapsed = 0., h = *hint > 0 ? *hint : dt;
+    memset(stats, 0, sizeof(*stats));
+    memset(water_mean, 0, sizeof(double) * nf);
+    /* the HLLC owner's rotor momentum has no balanced-pressure term
+     * (hydrostatic HLLC pressure; river_turbines.py:27-36) */
+    om_turbines *T = (om_turbines *)m->turb;
+    const int pressure = T ? T->pressure : 0;
+    if (T) T->pressure = 0;
+    int status = OM_OK;
+    while (stats->substeps == 0 || elapsed < dt - 1e-13 * fmax(1., dt)) {
+        const double trial = fmin(h, dt - elapsed);
+        const int truncated = trial < h * (1 - 1e-12);
+        double peak = 0.;
+        const int st = om_hllc_single(m, G, s, S, q, z, trial, time + elapsed, next, w, &peak);
+        if (st == OM_FAIL) { status = st; break; }
+        if (st) {
+            stats->rejections++;
+            h = peak > 0 ? fmin(.5 * trial, .98 * m->cfl / peak) : .5 * trial;
+            if (stats->rejections > 100 || h < dt * ldexp(1., -20)) { status = st; break; }
+            continue;
+        }
+        memcpy(q, next, sizeof(double) * 3 * n);
+        for (int f = 0; f < nf; ++f) water_mean[f] += trial * w[f];
+        elapsed += trial;
+        stats->substeps++;
+        if (stats->substeps == 1 || trial < stats->min_dt) stats->min_dt = trial;
+        if (trial > stats->max_dt) stats->max_dt = trial;
+        if (trial * peak > stats->accepted_cfl_max) stats->accepted_cfl_max = trial * peak;
+        const double growth = truncated ? h : 2 * trial;
+        h = peak > 0 ? fmin(growth, .98 * m->cfl / peak) : growth;
+    }
+    if (T) T->pressure = pressure;
+    for (int f = 0; f < nf; ++f) water_mean[f] /= dt;
+    *hint = h;
+    stats->hint = h;
+    stats->status = status;
+    free(next); free(w);
+    om_hllc_scratch_destroy(S);
+    om_scratch_destroy(s);
+    return status;
+}
+
+/* One Hancock step from q with its internals copied out (any output may be NULL). */
+int om_hllc_step(om_ctx *m, const om_hllc_geo *G, const double *q, const double *z, double dt, double time,
+                 double *out, double *water, double *peak, double *grad, double *half, double *qhalf,
+                 double *fl, double *fr, double *speed, double *theta, double *freq, double *next)
+{
+    const size_t n = m->nc, nf = m->nf;
+    om_scratch *s = om_scratch_create(m);
+    om_hllc_scratch *S = om_hllc_scratch_create(m);
+    double *res = om_alloc(sizeof(double) * 3 * n), *w = om_alloc(sizeof(double) * nf);
+    om_turbines *T = (om_turbines *)m->turb;
+    const int pressure = T ? T->pressure : 0;
+    if (T) T->pressure = 0;
+    const int st = om_hllc_single(m, G, s, S, q, z, dt, time, res, w, peak);
+    if (T) T->pressure = pressure;
+#define OM_COPY(dst, src, count) if (dst) memcpy(dst, src, sizeof(double) * (count))
+    OM_COPY(out, res, 3 * n); OM_COPY(water, w, nf); OM_COPY(grad, S->grad, 8 * n);
+    OM_COPY(half, S->half, 4 * n); OM_COPY(qhalf, S->qhalf, 3 * n); OM_COPY(fl, S->fl, 3 * nf);
+    OM_COPY(fr, S->fr, 3 * nf); OM_COPY(speed, S->speed, nf); OM_COPY(theta, S->theta, n);
+    OM_COPY(freq, S->freq, n); OM_COPY(next, S->next, 3 * n);
+#undef OM_COPY
+    free(res); free(w);
+    om_hllc_scratch_destroy(S);
+    om_scratch_destroy(s);
+    return st;
+}
+
+size_t om_hllc_geo_size(void) { return sizeof(om_hllc_geo); }
+
 void om_set_threads(int n)
 {
 #ifdef _OPENMP

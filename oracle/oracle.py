@@ -80,6 +80,10 @@ class ExnerStats(C.Structure):
     _fields_ = [("ok", I), ("residual", D), ("boundary", D), ("donor", D), ("change", D)]
 
 
+class HllcGeo(C.Structure):
+    _fields_ = [("off", P), ("faces", P), ("signs", P), ("xy", P), ("mid", P), ("inverse", P), ("selected", P)]
+
+
 class Stats(C.Structure):
     _fields_ = [("substeps", I), ("rejections", I), ("status", I),
                 ("min_dt", D), ("max_dt", D), ("accepted_cfl_max", D), ("hint", D)]
@@ -125,6 +129,22 @@ def _setup(L):
     L.om_turbine_diagnose.restype = I
     L.om_hkt_gradients.argtypes = [P, P, P, P, P]
     L.om_hkt_gradients.restype = None
+    L.om_hllc_geo_size.restype = C.c_size_t
+    assert L.om_hllc_geo_size() == C.sizeof(HllcGeo), "oracle HLLC geometry layout differs"
+    L.om_hllc_advance.argtypes = [P, P, P, P, D, D, P, P, P]
+    L.om_hllc_advance.restype = I
+    L.om_hllc_step.argtypes = [P, P, P, P, D, D] + [P] * 12
+    L.om_hllc_step.restype = I
+    L.om_hllc_reconstruct.argtypes = [P, P, D, P, P, P, P, P, P]
+    L.om_hllc_faces.argtypes = [P, P, P, P, P, P, P, P, P]
+    L.om_hllc_budget.argtypes = [P, P, D, P, P, P, P, P, P]
+    L.om_hllc_limit.argtypes = [P, P, P, P, P, P, P]
+    L.om_hllc_update.argtypes = [P, P, D, P, P, P, P, P, P]
+    L.om_hllc_turbine_pressure.argtypes = [P, P, P, P, P, P]
+    L.om_hllc_predict_source.argtypes = [I, D, D, P, P, P]
+    for name in ("om_hllc_reconstruct", "om_hllc_faces", "om_hllc_budget", "om_hllc_limit", "om_hllc_update",
+                 "om_hllc_turbine_pressure", "om_hllc_predict_source"):
+        getattr(L, name).restype = None
 
 
 def _p(a):
@@ -312,6 +332,70 @@ class Oracle:
         stats = Stats()
         st = self.L.om_advance(self.cp, _p(q), _p(self.z), dt, time, C.byref(self.hint), _p(water), C.byref(stats))
         return st, water, {f: getattr(stats, f) for f, _ in Stats._fields_}
+
+    # --- HLLC / MUSCL-Hancock option ----------------------------------------
+    def _hllc(self):
+        if not hasattr(self, "_hgeo"):
+            from braids_hkt_gb300.hllc import hllc_geometry
+            g = hllc_geometry(self.m)
+            keep = self._keep
+            keep.update(h_off=_i32(g["offset"]), h_faces=_i32(g["faces"]), h_signs=_i32(g["signs"]),
+                        h_xy=_f64(self.m.xy), h_mid=_f64(self.m.mid), h_inv=_f64(g["inverse"]),
+                        h_sel=_i32(g["selected"]))
+            self._hgeo = HllcGeo(*(_p(keep[k]) for k in ("h_off", "h_faces", "h_signs", "h_xy", "h_mid",
+                                                           "h_inv", "h_sel")))
+            self.hllc_hint = C.c_double(0.0)
+        return C.byref(self._hgeo)
+
+    def hllc_advance(self, q, dt, time=0.0):
+        """HLLC (MUSCL-Hancock) interval: q (3,nc) advanced in place; (status, water_mean, stats)."""
+        assert q.dtype == np.float64 and q.flags.c_contiguous
+        G = self._hllc()
+        water = np.zeros(self.m.nf)
+        stats = Stats()
+        st = self.L.om_hllc_advance(self.cp, G, _p(q), _p(self.z), dt, time, C.byref(self.hllc_hint), _p(water),
+                                    C.byref(stats))
+        return st, water, {f: getattr(stats, f) for f, _ in Stats._fields_}
+
+    def hllc_step(self, q, dt, time=0.0):
+        """One Hancock step from q: (status, result, water, frequency peak, internals dict)."""
+        G = self._hllc()
+        q = _f64(q)
+        nc, nf = self.m.nc, self.m.nf
+        o = dict(out=np.zeros((3, nc)), water=np.zeros(nf), grad=np.zeros((8, nc)), half=np.zeros((4, nc)),
+                 qhalf=np.zeros((3, nc)), fl=np.zeros((3, nf)), fr=np.zeros((3, nf)), speed=np.zeros(nf),
+                 theta=np.zeros(nc), freq=np.zeros(nc), next=np.zeros((3, nc)))
+        peak = C.c_double()
+        st = self.L.om_hllc_step(self.cp, G, _p(q), _p(self.z), dt, time, _p(o["out"]), _p(o["water"]),
+                                 C.byref(peak), *(_p(o[k]) for k in ("grad", "half", "qhalf", "fl", "fr", "speed",
+                                                                     "theta", "freq", "next")))
+        return st, o["out"], o["water"], peak.value, o
+
+    def hllc_kernels(self, q, dt, external=None, ext_trace=None, rotors=False):
+        """reconstruct -> faces [-> rotor pressure] -> budget -> limit -> update on q (no exterior call)."""
+        G = self._hllc()
+        L, cp, m = self.L, self.cp, self.m
+        q = _f64(q)
+        nc, nf = m.nc, m.nf
+        o = dict(grad=np.zeros((8, nc)), half=np.zeros((4, nc)), qhalf=np.zeros((3, nc)),
+                 pstatus=np.zeros(nc, np.int32), fl=np.zeros((3, nf)), fr=np.zeros((3, nf)), speed=np.zeros(nf),
+                 theta=np.zeros(nc), freq=np.zeros(nc), fstatus=np.zeros(nf, np.int32), next=np.zeros((3, nc)),
+                 status=np.zeros(nc, np.int32))
+        external = np.zeros((3, nf)) if external is None else _f64(external)
+        ext_trace = np.zeros((3, nf)) if ext_trace is None else _f64(ext_trace)
+        L.om_hllc_reconstruct(cp, G, dt, _p(q), _p(self.z), _p(o["grad"]), _p(o["half"]), _p(o["qhalf"]),
+                              _p(o["pstatus"]))
+        L.om_hllc_faces(cp, G, _p(o["half"]), _p(o["grad"]), _p(external), _p(ext_trace), _p(o["fl"]),
+                        _p(o["fr"]), _p(o["speed"]))
+        if rotors:
+            L.om_hllc_turbine_pressure(cp, G, _p(o["half"]), _p(o["grad"]), _p(o["fl"]), _p(o["fr"]))
+        o["fl_raw"], o["fr_raw"] = o["fl"].copy(), o["fr"].copy()
+        L.om_hllc_budget(cp, G, dt, _p(q), _p(o["fl"]), _p(o["speed"]), _p(o["pstatus"]), _p(o["theta"]),
+                         _p(o["freq"]))
+        L.om_hllc_limit(cp, G, _p(q), _p(o["theta"]), _p(o["fl"]), _p(o["fr"]), _p(o["fstatus"]))
+        L.om_hllc_update(cp, G, dt, _p(q), _p(o["fl"]), _p(o["fr"]), _p(o["fstatus"]), _p(o["next"]),
+                         _p(o["status"]))
+        return o
 
     # --- single kernels (for pinning against the reference kernels) -------
     def kernels(self, q, z=None):

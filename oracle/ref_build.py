@@ -21,7 +21,8 @@ Dual-compiled OpenMP headers (their ENTRY/LOOP macros select the host form):
   river_midpoint.h, river_explicit.h, river_exterior_bed.h,
   river_hydraulic_drag.source() (src/braids_core/sediment/river_hydraulic_drag.py:11-15),
   river_turbine_flow.h, river_hydrokinetic_stress.h (turbine momentum terms),
-  river_mpm.h, flow2dh_mobile_kernels.h, bend_methods_v1_kernels.h (Exner / MPM)
+  river_mpm.h, flow2dh_mobile_kernels.h, bend_methods_v1_kernels.h (Exner / MPM),
+  hllc.h, hllc_turbines.h (src/braids_core/hydraulics, the HLLC option)
 Generated CUDA C also: flow_bed_slope_runtime.cu (src/braids_gpu, Koch-Flokstra slope)
 
 Usage: python oracle/ref_build.py   (exits non-zero when the reference is absent)
@@ -108,6 +109,9 @@ def generate():
         "ref_mpm": (src / "braids_core/sediment/river_mpm.h").read_text(),
         "ref_mobile": (src / "braids_core/sediment/flow2dh_mobile_kernels.h").read_text(),
         "ref_bend": (src / "braids_core/sediment/bend_methods_v1_kernels.h").read_text(),
+        # HLLC / MUSCL-Hancock option and its rotor pressure correction
+        "ref_hllc": (src / "braids_core/hydraulics/hllc.h").read_text(),
+        "ref_hllc_turbines": (src / "braids_core/hydraulics/hllc_turbines.h").read_text(),
     }
     for name, code in headers.items():
         (OUT / f"{name}.h").write_text(code)

@@ -15,6 +15,13 @@ the reference's Python owners line by line:
                                        with the reference's ThetisRotor.sample / cell_terms
                                        (river_turbine_thetis.py) run on numpy
 
+The HLLC option runs the reference's own ``HLLCHydraulics`` class
+(src/braids_core/hydraulics/hllc.py) unchanged; only its kernel engine is
+pointed at the host build of the reference's hllc.h in oracle/_ref, and its
+exterior, friction, rotor-momentum and rotor-pressure hooks are the ones its
+river owner installs (river_hllc.py:14-55, river_turbines.py:27-51) over the
+kernels above.
+
 The stock-budget steps run the reference's own Python classes
 (``OutletFeasibility`` and ``ExplicitBoundaryBudget``) on a minimal stand-in
 owner that carries only the attributes they read.
@@ -482,6 +489,73 @@ class Ref:
         if not np.isfinite(frequency) or dt * frequency > self.cfl * (1 + 1e-12):
             raise Rejected("cfl")
         return rate, water, frequency
+
+    # -- HLLC / MUSCL-Hancock option: the reference's own operator ---------------
+    def _hllc_engine(self, source, names):
+        """A WaveEngine (sediment_wave.py:22-56) bound to the host build of ``source``."""
+        from braids_support.sediment.river_morphodynamics.sediment_wave import WaveEngine
+        lib = C.CDLL(str(REF / ("libref_hllc_turbines.so" if Path(source).name == "hllc_turbines.h"
+                                else "libref_hllc.so")))
+        e = WaveEngine.__new__(WaveEngine)
+        e.backend, e.threads = "cpu", os.cpu_count() or 1
+        e.lib, e.fn = lib, {name: getattr(lib, name) for name in names}
+        for fn in e.fn.values():
+            fn.restype = None
+        e.identity = dict(backend="cpu", source=str(source))
+        return e
+
+    def hllc_operator(self, cfl=None):
+        """The reference's HLLCHydraulics on this mesh, hooked as RiverHLLC / the
+        HLLC rotor install hook it (river_hllc.py:14-55, river_turbines.py:27-51)."""
+        from braids_core.hydraulics import hllc as H
+        from braids_core.hydraulics.outlet_feasibility import OutletFeasibility
+        from braids_core.sediment.bend_methods_v1 import BendTrialRejected
+        m, g = self.m, self.g
+        H.WaveEngine = lambda backend, threads, source=None, names=None: self._hllc_engine(source, names)
+        inlet = {6, 9}
+        cells = [SimpleNamespace(centroid_xy=(float(m.xy[0, i]), float(m.xy[1, i])), area_m2=float(m.area[i]))
+                 for i in range(m.nc)]
+        faces = []
+        for f in range(m.nf):
+            mid = (float(m.mid[0, f]), float(m.mid[1, f]))   # (mid + mid) / 2 == mid exactly
+            kind = "interior" if m.neighbour[f] >= 0 else "wall"
+            if self.openf[f]:
+                kind = "inlet" if int(self.seg_mode[m.bid[f]]) in inlet else "outlet"
+            faces.append(SimpleNamespace(start_xy=np.array(mid), end_xy=np.array(mid),
+                                         outward_normal=(float(m.normal[0, f]), float(m.normal[1, f])),
+                                         owner=int(m.owner[f]), neighbour=int(m.neighbour[f]),
+                                         length_m=float(m.length[f]), kind=kind))
+        mesh = SimpleNamespace(cells=cells, faces=faces)
+
+        def exterior(q, z, time):
+            trace, flux, status = self.exterior(np.ascontiguousarray(q))
+            if np.any(status):
+                raise BendTrialRejected("Exterior hydraulic boundary rejected")
+            return flux, trace
+        feasibility = OutletFeasibility(self._ext_stub) if self.nb else None
+
+        def boundary_correction(q, dt, flux, trace):
+            feasibility(q, dt, flux, trace)
+
+        momentum = correct = None
+        if self.rotors:
+            def momentum(q, water, rate):
+                saved, self.hkt_pressure = self.hkt_pressure, False
+                try:
+                    self.turbine_momentum(q, None, rate)
+                finally:
+                    self.hkt_pressure = saved
+            pressure = self._hllc_engine("hllc_turbines.h", ("hllc_turbine_pressure",))
+
+            def correct(op):
+                k = op.g
+                pressure.launch("hllc_turbine_pressure", op.nf, op.n, op.nf, op.gravity, op.dry, op.half, op.grad,
+                                k["xy"], k["mid"], k["normal"], k["owner"], k["neighbour"], op.fl, op.fr)
+        return H.HLLCHydraulics(mesh, backend="cpu", threads=os.cpu_count() or 1, gravity=self.grav, dry=self.dry,
+                                cfl=self.cfl if cfl is None else cfl, exterior=exterior if self.nb else None,
+                                friction=self.friction, check=None, integration="hancock", momentum=momentum,
+                                boundary_correction=boundary_correction if self.nb else None,
+                                face_correction=correct)
 
     def friction(self, q, dt):
         chezy = np.zeros(self.m.nc)
