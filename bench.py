@@ -256,6 +256,8 @@ def main():
     ap.add_argument("--no-serving", action="store_true", help="skip the scaled config-5 serving session")
     ap.add_argument("--subset", default=None,
                     help="START:STOP slice of the config-4 scenarios sorted by size (profiling a smaller case)")
+    ap.add_argument("--no-hllc", dest="hllc", action="store_false",
+                    help="skip the HLLC MUSCL-Hancock legs (per-scenario and whole batch, FP64 form)")
     ap.add_argument("--profile-only", type=int, default=0,
                     help="only time N substeps kernel by kernel (brx_profile_substep) and exit")
     args = ap.parse_args()
@@ -400,7 +402,26 @@ def main():
         batch_state = state_after_timed
         off = solver.packed["cell_offset"]
         nsteps = args.warmup + args.steps
+        h_updates, h_ms, h_failed = 0, 0.0, False
         for i in pick:
+            if args.hllc:
+                # the HLLC MUSCL-Hancock method on the same scenario, intervals and CFL (FP64 form)
+                hs = RiverSolver(cases[i], precision="fp64", method="hllc")
+                t_sim = 0.0
+                for k in range(nsteps):
+                    torch.cuda.synchronize()
+                    e0 = torch.cuda.Event(enable_timing=True)
+                    e1 = torch.cuda.Event(enable_timing=True)
+                    e0.record(hs.stream)
+                    d = hs.advance(outer, t_sim, raise_on_failure=False)
+                    e1.record(hs.stream)
+                    e1.synchronize()
+                    t_sim += outer
+                    h_failed = h_failed or bool(d["failed"])
+                    if k >= args.warmup:
+                        h_ms += e0.elapsed_time(e1)
+                        h_updates += d["hydraulic_substeps"] * hs.nc
+                hs.close()
             one = RiverSolver(cases[i], precision="fp64")
             t_sim = 0.0
             for k in range(nsteps):
@@ -429,11 +450,44 @@ def main():
         plain = {"value": p_updates / (p_ms / 1e3), "unit": METRIC, "scenarios": pick,
                  "cells": [int(cases[i]["mesh"].nc) for i in pick],
                  "note": "each scenario alone in the FP64 form over the same intervals"}
+        if args.hllc:
+            plain["hllc"] = {"value": h_updates / (h_ms / 1e3), "unit": METRIC,
+                             "speedup_vs_fwave_fp64_same_intervals": p_ms / h_ms, "any_failed": h_failed,
+                             "note": "the same scenarios alone with the HLLC MUSCL-Hancock method (FP64 form, one "
+                                     "spatial evaluation per substep), the same intervals and CFL; speed-up = "
+                                     "f-wave FP64 device time / HLLC device time for the same simulated time"}
         cfg["accuracy_vs_fp64"] = {"depth_rel_max": max(e[0] for e in errs), "depth_rel_p99": max(e[1] for e in errs),
                                    "scenarios": pick, "after_sim_s": nsteps * outer,
                                    "stated_tolerance": 1e-4,
                                    "rotor_power_rel_max": max(perr) if perr else None,
                                    "rotors_compared": len(perr)}
+    hllc_batch = None
+    if args.hllc and precision == "mixed":
+        # the whole batch with the HLLC method (FP64 form): one warm-up and up to two timed intervals
+        hs = RiverSolver(cases, precision="fp64", method="hllc")
+        t_sim, ms, ups, hfail = 0.0, 0.0, 0, set()
+        for k in range(1 + max(1, min(args.steps, 2))):
+            flush_l2(torch, flush)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(hs.stream)
+            ds = hs.advance(outer, t_sim, raise_on_failure=False)
+            e1.record(hs.stream)
+            e1.synchronize()
+            t_sim += outer
+            hfail |= {i for i, d in enumerate(ds) if d["failed"]}
+            if k >= 1:
+                ms += e0.elapsed_time(e1)
+                ups += sum(d["hydraulic_substeps"] * (hs.packed["cell_offset"][i + 1] - hs.packed["cell_offset"][i])
+                           for i, d in enumerate(ds))
+        hprof = hs.profile_substep(0.5 * min(d["hydraulic_next_substep_hint_s"] for d in ds), t_sim)
+        hllc_batch = {"value": ups / (ms / 1e3), "unit": METRIC, "ms_per_interval": ms / max(1, min(args.steps, 2)),
+                      "failed_scenarios": sorted(hfail),
+                      "substep_kernels_ms": [(n, round(v, 4)) for n, v in hprof],
+                      "note": "the whole batch (rotors included) with the HLLC MUSCL-Hancock method, FP64 form; "
+                              "one cell-update = one cell advanced by one accepted Hancock substep"}
+        hs.close()
     if rank != 0:
         return
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
@@ -451,6 +505,8 @@ def main():
     if plain is not None:
         line["plain_fp64"] = plain
         line["batched_vs_plain_fp64"] = value / plain["value"]
+    if hllc_batch is not None:
+        line["hllc_fp64_batch"] = hllc_batch
     if precision == "mixed" and not args.no_serving:
         solver.close()
         try:

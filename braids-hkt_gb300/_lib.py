@@ -38,6 +38,8 @@ SIGNATURES = {
     "brx_advance_start": (I, [P, P, P]),
     "brx_advance_poll": (I, [P, P, P]),
     "brx_solver_bytes": (C.c_longlong, [P]),
+    "brx_hllc_set": (I, [P, P, P, P, P]),
+    "brx_method_set": (I, [P, I]),
     "brx_hint_get": (I, [P, P]),
     "brx_hint_set": (I, [P, P]),
     "brx_graph_chunk_set": (I, [P, I]),

@@ -24,6 +24,7 @@
 #include "brx_launch.h"
 #include "brx_turbine.cuh"
 #include "brx_exner.cuh"
+#include "brx_hllc.cuh"
 
 using namespace brx;
 
@@ -89,6 +90,10 @@ struct brx_solver {
     bool has_exner = false;
     int *d_cell_off = nullptr, *d_face_off = nullptr;
     double *d_exdt = nullptr;
+    int method = BRX_METHOD_FWAVE;   // hydraulic method of the substep graph
+    HllcDev hllc{};                  // HLLC stencil (valid when hllc_ready)
+    bool hllc_ready = false;
+    std::vector<int> h_seg_mode;     // host copy of the segment modes
 
     template <class T> int alloc(T **p, size_t count)
     {
@@ -449,6 +454,10 @@ extern "C" int brx_boundary_set(brx_solver *s, const int *seg_mode, const int *s
         if (stage_policy[sg] != 0 && stage_policy[sg] != 1) return fail(BRX_ERR_ARGUMENT, "stage policy must be 0 or 1");
         if (!std::isfinite(forcing[sg]) || !std::isfinite(forcing[nseg + sg])) return fail(BRX_ERR_ARGUMENT, "nonfinite forcing");
     }
+    if (s->method == BRX_METHOD_HLLC)
+        for (int sg = 0; sg < nseg; ++sg)
+            if (seg_mode[sg] == 9) return fail(BRX_ERR_UNSUPPORTED, "the HLLC method has no stage-discharge inlet (mode 9)");
+    s->h_seg_mode.assign(seg_mode, seg_mode + nseg);
     std::vector<int> bmode(nf, 0);
     std::vector<double> ext(std::max(s->nslot, 1));
     for (int k = 0; k < s->nslot; ++k) {
@@ -644,9 +653,69 @@ extern "C" int brx_turbines_set(brx_solver *s, int nrotor, const int *rotor_scen
         CK(cudaMemset(t.pface, 0, sizeof(double) * 2 * (size_t)nf));
         CK(cudaMemset(t.sface, 0, sizeof(double) * 2 * (size_t)nf));
     }
+    t.balanced = s->method == BRX_METHOD_FWAVE;
     s->turb = t;
     s->has_turb = true;
     s->nrotor = nrotor;
+    s->graph_dirty = true;
+    return BRX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// HLLC / MUSCL-Hancock method
+// ---------------------------------------------------------------------------
+extern "C" int brx_hllc_set(brx_solver *s, const int *entry_face, const int *entry_other, const double *entry_geo,
+                            const double *inverse)
+{
+    if (!s) return fail(BRX_ERR_ARGUMENT, "null solver");
+    if (!entry_face || !entry_other || !entry_geo || !inverse) return fail(BRX_ERR_ARGUMENT, "null HLLC stencil array");
+    if (s->hllc_ready) return fail(BRX_ERR_STATE, "the HLLC stencil is already installed");
+    const int nc = s->nc, nf = s->nf, nadj = s->nadj;
+    std::vector<int2> ent(nadj);
+    std::vector<double4_32a> geo(nadj);
+    std::vector<int> seen(nf, 0);
+    for (int c = 0; c < nc; ++c)
+        for (int k = s->h_offset[c]; k < s->h_offset[c + 1]; ++k) {
+            const int x = entry_face[k], f = x >= 0 ? x : ~x, o = entry_other[k];
+            if (f < 0 || f >= nf) return fail(BRX_ERR_ARGUMENT, "HLLC entry face out of range");
+            const int owner = s->h_owner[f], nb = s->h_neighbour[f];
+            const bool mine = x >= 0 ? owner == c : nb == c;
+            if (!mine) return fail(BRX_ERR_ARGUMENT, "HLLC entry face does not border its cell");
+            const int expect = x >= 0 ? (nb >= 0 ? nb : (s->h_bid[f] >= 0 ? HE_OPEN : HE_WALL)) : owner;
+            if (o != expect) return fail(BRX_ERR_ARGUMENT, "HLLC entry neighbour code inconsistent with the mesh");
+            if (k > s->h_offset[c] && f <= (entry_face[k - 1] >= 0 ? entry_face[k - 1] : ~entry_face[k - 1]))
+                return fail(BRX_ERR_ARGUMENT, "HLLC entries must list each cell's faces in ascending order");
+            seen[f] += 1;
+            ent[k] = make_int2(x, o);
+            geo[k] = make_double4_32a(entry_geo[k], entry_geo[(size_t)nadj + k], entry_geo[2 * (size_t)nadj + k],
+                                      entry_geo[3 * (size_t)nadj + k]);
+        }
+    for (int f = 0; f < nf; ++f)
+        if (seen[f] != (s->h_neighbour[f] >= 0 ? 2 : 1)) return fail(BRX_ERR_ARGUMENT, "HLLC entries must cover every face side once");
+    int2 *p_ent;
+    double4_32a *p_geo;
+    double *p_inv;
+    TRY(s->upload(&p_ent, ent.data(), nadj)); TRY(s->upload(&p_geo, geo.data(), nadj));
+    TRY(s->upload(&p_inv, inverse, 3 * (size_t)nc));
+    s->hllc.ent = p_ent; s->hllc.geo = p_geo; s->hllc.inverse = p_inv;
+    s->hllc_ready = true;
+    return BRX_OK;
+}
+
+extern "C" int brx_method_set(brx_solver *s, int method)
+{
+    if (!s) return fail(BRX_ERR_ARGUMENT, "null solver");
+    if (s->pending) return fail(BRX_ERR_STATE, "an asynchronous interval is in flight");
+    if (method != BRX_METHOD_FWAVE && method != BRX_METHOD_HLLC) return fail(BRX_ERR_ARGUMENT, "unknown method");
+    if (method == BRX_METHOD_HLLC) {
+        if (s->precision != BRX_FP64) return fail(BRX_ERR_UNSUPPORTED, "the HLLC method runs in the FP64 form");
+        if (!s->hllc_ready) return fail(BRX_ERR_STATE, "HLLC stencil not installed (brx_hllc_set)");
+        if (s->maxdeg > MAX_CELL_FACES) return fail(BRX_ERR_UNSUPPORTED, "cell with too many faces");
+        for (int md : s->h_seg_mode)
+            if (md == 9) return fail(BRX_ERR_UNSUPPORTED, "the HLLC method has no stage-discharge inlet (mode 9)");
+    }
+    s->method = method;
+    s->turb.balanced = method == BRX_METHOD_FWAVE;
     s->graph_dirty = true;
     return BRX_OK;
 }
@@ -887,11 +956,63 @@ static void enqueue_stage(brx_solver *s, int stage, double *rate_out)
         s->launches += launch_kernel(s, kind, stage, kind == K_UPDATE ? rate_out : nullptr);
 }
 
-static void enqueue_substep(brx_solver *s)
+// HLLC / MUSCL-Hancock kernels of one substep (kinds of the profile), on st.
+enum HllcKind { KH_CELLS = 20, KH_PREDICT = 21, KH_BOUNDARY = 22, KH_FACES = 23, KH_BUDGET = 24, KH_TURB = 25,
+                KH_UPDATE = 26, KH_TURB0 = 27 };
+
+static int launch_hllc(brx_solver *s, int kind, cudaStream_t st = nullptr)
+{
+    if (!st) st = s->stream;
+    HCell *rec = reinterpret_cast<HCell *>(s->work.rec);      // 96 of the 128 bytes per cell
+    switch (kind) {
+    case KH_CELLS:
+        if (s->maxdeg <= 4) k_hllc_cells<4><<<s->grid_c, 128, 0, st>>>(s->mesh, s->state, s->hllc, rec, s->d_ctrl);
+        else k_hllc_cells<MAX_CELL_FACES><<<s->grid_c, 128, 0, st>>>(s->mesh, s->state, s->hllc, rec, s->d_ctrl);
+        return 1;
+    case KH_TURB0:        // rotor terms on the start state (stage 1 reads work)
+        return s->has_turb ? launch_turbines(s, 1, st) : 0;
+    case KH_PREDICT:
+        if (!s->has_turb) return 0;
+        k_hllc_predict<<<s->grid_c256, 256, 0, st>>>(s->mesh, s->state, s->turb, rec, s->d_ctrl);
+        return 1;
+    case KH_BOUNDARY:
+        if (!s->nslot) return 0;
+        k_boundary<double><<<s->nscen, 256, 0, st>>>(s->mesh, s->state, s->bnd, s->d_ctrl, STAGE_HANCOCK);
+        return 1;
+    case KH_FACES:
+        k_hllc_faces<<<s->grid_f, 128, 0, st>>>(s->mesh, s->bnd, rec, s->work, s->turb, s->has_turb, s->d_ctrl);
+        return 1;
+    case KH_BUDGET:
+        k_hllc_budget<<<s->grid_c256, 256, 0, st>>>(s->mesh, s->state, s->hllc, s->work, s->d_ctrl);
+        return 1;
+    case KH_TURB:         // rotor terms on the predicted state (stage 2 reads q1)
+        return s->has_turb ? launch_turbines(s, 2, st) : 0;
+    case KH_UPDATE:
+        k_hllc_update<<<s->grid_c256, 256, 0, st>>>(s->mesh, s->state, s->hllc, s->work, s->turb, s->has_turb,
+                                                    s->d_ctrl);
+        return 1;
+    }
+    return 0;
+}
+
+static const int HLLC_SEQUENCE[] = {KH_CELLS, KH_TURB0, KH_PREDICT, KH_BOUNDARY, KH_FACES, KH_BUDGET, KH_TURB,
+                                    KH_UPDATE};
+
+// One trial of the selected method without the controller.
+static void enqueue_trial(brx_solver *s)
 {
     s->launches += launch_kernel(s, K_DRAG, 0, nullptr);
+    if (s->method == BRX_METHOD_HLLC) {
+        for (int kind : HLLC_SEQUENCE) s->launches += launch_hllc(s, kind);
+        return;
+    }
     enqueue_stage(s, 1, nullptr);
     enqueue_stage(s, 2, nullptr);
+}
+
+static void enqueue_substep(brx_solver *s)
+{
+    enqueue_trial(s);
     k_control<<<(s->nscen + 127) / 128, 128, 0, s->stream>>>(s->d_ctrl, s->nscen);
     s->launches++;
 }
@@ -1086,9 +1207,7 @@ extern "C" int brx_substep(brx_solver *s, double dt, double time, unsigned *stat
     for (int i = 0; i < s->nscen; ++i) s->h_ctrl[i].max_substeps = 4096;
     CK(cudaMemcpyAsync(s->d_ctrl, s->h_ctrl, sizeof(Ctrl) * s->nscen, cudaMemcpyHostToDevice, s->stream));
     // the trial without the controller: its statuses are read before control runs
-    s->launches += launch_kernel(s, K_DRAG, 0, nullptr);
-    enqueue_stage(s, 1, nullptr);
-    enqueue_stage(s, 2, nullptr);
+    enqueue_trial(s);
     CK(cudaMemcpyAsync(s->h_ctrl, s->d_ctrl, sizeof(Ctrl) * s->nscen, cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     std::vector<Ctrl> trial(s->h_ctrl, s->h_ctrl + s->nscen);
@@ -1116,6 +1235,7 @@ extern "C" int brx_rate(brx_solver *s, double dt, double time, double *rate_devi
 {
     TRY(ensure_ready(s));
     if (!rate_device || !water_device) return fail(BRX_ERR_ARGUMENT, "null output buffer");
+    if (s->method != BRX_METHOD_FWAVE) return fail(BRX_ERR_UNSUPPORTED, "brx_rate is the f-wave spatial residual");
     begin_interval(s, dt, time, true);
     CK(cudaMemcpyAsync(s->d_ctrl, s->h_ctrl, sizeof(Ctrl) * s->nscen, cudaMemcpyHostToDevice, s->stream));
     CK(cudaMemcpyAsync(s->state.work, s->state.q[0], sizeof(double) * 3 * s->nc, cudaMemcpyDeviceToDevice, s->stream));
@@ -1163,10 +1283,15 @@ extern "C" int brx_profile_substep(brx_solver *s, double dt, double time, int ca
     int extra = 0;                   // kernels beyond one per timed kind
     mark(-1);
     if (launch_kernel(s, K_DRAG, 0, nullptr)) mark(K_DRAG);
-    for (int stage = 1; stage <= 2; ++stage)
-        for (int kind : {(int)K_BOUNDARY, (int)K_CELLS, (int)K_FACES, (int)K_GATHER, (int)K_LIMIT, (int)K_TURB,
-                         (int)K_UPDATE})
-            if (const int nl = launch_kernel(s, kind, stage, nullptr)) { mark(kind); extra += nl - 1; }
+    if (s->method == BRX_METHOD_HLLC) {
+        for (int kind : HLLC_SEQUENCE)
+            if (const int nl = launch_hllc(s, kind)) { mark(kind); extra += nl - 1; }
+    } else {
+        for (int stage = 1; stage <= 2; ++stage)
+            for (int kind : {(int)K_BOUNDARY, (int)K_CELLS, (int)K_FACES, (int)K_GATHER, (int)K_LIMIT, (int)K_TURB,
+                             (int)K_UPDATE})
+                if (const int nl = launch_kernel(s, kind, stage, nullptr)) { mark(kind); extra += nl - 1; }
+    }
     k_control<<<(s->nscen + 127) / 128, 128, 0, st>>>(s->d_ctrl, s->nscen); mark(7);
     k_commit<<<s->grid_c256, 256, 0, st>>>(s->mesh, s->state, s->d_ctrl);
     s->launches += (long long)kinds.size() + 1 + extra;

@@ -103,6 +103,7 @@ struct TurbDev {
     double *trace;              // (10, nf) hydrostatically reconstructed face traces
     double *pface, *sface;      // (2, nf) pressure correction, ambient stress
     double *diag;               // (nr, 16) rotor diagnostics of the last sampled state
+    int balanced;               // 1: balanced-pressure face term (f-wave owner); 0: HLLC owner
 };
 
 struct BoundaryDev {
@@ -221,9 +222,11 @@ __device__ __forceinline__ void put_trace(double *tr, int nf, int f, const doubl
 // Momentum terms of a rotor array, in the reference's add_momentum order
 // (river_turbine_flow.py:230-239): ambient stress, actuator sink, balanced
 // pressure; face terms gathered as sum(s len flux) / area
-// (flow2dh_fixed_bed_kernels.h:54-60 with unit depth weights).
+// (flow2dh_fixed_bed_kernels.h:54-60 with unit depth weights). The HLLC
+// owner's rotor hook has no balanced pressure (river_turbines.py:27-36):
+// balanced = false.
 __device__ __forceinline__ void add_rotor_momentum(const MeshDev &m, const TurbDev &t, int sid, int c, double area,
-                                                   double &r1, double &r2)
+                                                   double &r1, double &r2, bool balanced = true)
 {
     const int nc = m.nc, nf = m.nf;
     if (t.stress[sid]) {
@@ -236,6 +239,7 @@ __device__ __forceinline__ void add_rotor_momentum(const MeshDev &m, const TurbD
         r1 += 1. * x / area; r2 += 1. * y / area;
     }
     r1 += t.raw[c]; r2 += t.raw[nc + c];
+    if (!balanced) return;
     double x = 0., y = 0.;
     for (int k = m.offset[c]; k < m.offset[c + 1]; ++k) {
         const int f = m.faces[k];

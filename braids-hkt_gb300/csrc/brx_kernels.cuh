@@ -129,21 +129,28 @@ __device__ void segment_sums(const BoundaryDev &b, int s0, int s1, int row, int 
 }
 
 
+// stage 1 / 2: the SSPRK stages (state work / q1, its own stock, clock t or
+// t + dt); STAGE_HANCOCK: the HLLC predicted state q1 at t + dt/2, outlet
+// stock of the substep's start state work (hllc.py:91-97), status of stage 1.
+constexpr int STAGE_HANCOCK = 3;
+
 template <class F>
-__global__ void k_boundary(MeshDev m, StateDev s, BoundaryDev b, Ctrl *ctrl, int stage)
+__global__ void k_boundary(MeshDev m, StateDev s, BoundaryDev b, Ctrl *ctrl, int stage_in)
 {
     __shared__ double tile_buf[BOUNDARY_TILES];
     const int sid = blockIdx.x;
     Ctrl &ct = ctrl[sid];
+    const bool hancock = stage_in == STAGE_HANCOCK;
+    const int stage = hancock ? 1 : stage_in;
     if (skip_stage(ct, stage)) return;
     const int s0 = b.scen_seg[sid], s1 = b.scen_seg[sid + 1];
     if (s0 == s1) return;
     const int nc = m.nc;
-    const double *q = stage == 1 ? s.work : s.q1;
-    const double *base = q;                       // stage-start stock of this stage
+    const double *q = stage == 1 && !hancock ? s.work : s.q1;
+    const double *base = hancock ? s.work : q;    // stock of the stage start (the substep start for Hancock)
     const double *z = s.z;
     const double dry = ct.dry, grav = ct.grav;
-    const double t = ct.time0 + ct.elapsed + (stage == 2 ? ct.trial : 0.0);
+    const double t = ct.time0 + ct.elapsed + (stage == 2 ? ct.trial : hancock ? .5 * ct.trial : 0.0);
     // forcing at the stage clock (piecewise linear tables, else constant)
     if (b.table_len > 0)
         for (int sg = s0 + threadIdx.x; sg < s1; sg += blockDim.x)

@@ -331,6 +331,7 @@ __global__ void __launch_bounds__(128) k_hkt_faces(MeshDev m, TurbDev t, const d
             }
             t.sface[i] = ox; t.sface[nf + i] = oy;
         }
+        if (!t.balanced) continue;
         double px = 0., py = 0.;
         if (b >= 0 && q[a] > dry && q[b] > dry) {
             const double *tr = t.trace;

@@ -64,3 +64,55 @@ def hllc_geometry(mesh):
                inverse=inverse, selected=selected)
     mesh.records["hllc"] = rec
     return rec
+
+
+def entry_records(mesh):
+    """Per CSR entry of the HLLC incidence: encoded face, other-cell code and
+    stencil geometry (4, nadj), as brx_hllc_set takes them (local indices).
+
+    Offsets follow the kernel's expressions exactly (IEEE subtraction and
+    products, no contraction): xy[j] - xy[i] to a neighbour; for a wall
+    2 * ((mid - xy) . n) * n with the dot product as (mid_x - x) n_x +
+    (mid_y - y) n_y (hllc.h:25-28); mid - xy for the limiter (hllc.h:33).
+    """
+    g = hllc_geometry(mesh)
+    nc = mesh.nc
+    faces, signs = g["faces"], g["signs"]
+    cell = np.repeat(np.arange(nc), np.diff(g["offset"]))
+    owner, neighbour = mesh.owner, mesh.neighbour
+    other = np.where(signs > 0, neighbour[faces], owner[faces]).astype(np.int32)
+    wall = other < 0
+    is_open = wall & (g["selected"][faces] != 0)
+    other = np.where(is_open, -2, other).astype(np.int32)
+    code = np.where(signs > 0, faces, ~faces).astype(np.int32)
+    xy, mid, normal = mesh.xy, mesh.mid, mesh.normal
+    jj = np.where(other >= 0, other, 0)
+    geo = np.zeros((4, len(faces)))
+    geo[0] = np.where(other >= 0, xy[0, jj] - xy[0, cell], 0.0)
+    geo[1] = np.where(other >= 0, xy[1, jj] - xy[1, cell], 0.0)
+    nx, ny = normal[0, faces], normal[1, faces]
+    mdx, mdy = mid[0, faces] - xy[0, cell], mid[1, faces] - xy[1, cell]
+    dist = mdx * nx + mdy * ny
+    wl = other == -1
+    geo[0, wl] = (2. * dist[wl]) * nx[wl]
+    geo[1, wl] = (2. * dist[wl]) * ny[wl]
+    geo[2], geo[3] = mdx, mdy
+    return code, other, np.ascontiguousarray(geo), g["inverse"]
+
+
+def pack(cases, cell_offset, face_offset):
+    """Concatenated HLLC stencil of a scenario batch (global indices)."""
+    codes, others, geos, invs = [], [], [], []
+    for i, case in enumerate(cases):
+        if np.any(np.asarray(case.get("seg_mode", []), dtype=int) == 9):
+            raise ValueError("the HLLC method has no stage-discharge inlet (mode 9)")
+        code, other, geo, inv = entry_records(case["mesh"])
+        F0, C0 = int(face_offset[i]), int(cell_offset[i])
+        codes.append(np.where(code >= 0, code + F0, ~(~code + F0)).astype(np.int32))
+        others.append(np.where(other >= 0, other + C0, other).astype(np.int32))
+        geos.append(geo)
+        invs.append(inv)
+    return dict(entry_face=np.ascontiguousarray(np.concatenate(codes), dtype=np.int32),
+                entry_other=np.ascontiguousarray(np.concatenate(others), dtype=np.int32),
+                entry_geo=np.ascontiguousarray(np.concatenate(geos, axis=1)),
+                inverse=np.ascontiguousarray(np.concatenate(invs, axis=1)))

@@ -29,7 +29,9 @@ from . import _lib
 from ._lib import AdvanceStats, check
 
 PRECISIONS = {"fp64": 0, "mixed": 1}
+METHODS = {"fwave": 0, "hllc": 1}
 METHOD = "explicit_fwave_ssprk22_river_v1"
+METHOD_NAMES = {"fwave": METHOD, "hllc": "explicit_hllc_muscl_hancock_river_v1"}
 
 
 def _i32(a):
@@ -107,7 +109,7 @@ def pack(cases):
 class RiverSolver:
     """Resident GB300 river scenarios advanced by the CUDA step (see module docstring)."""
 
-    def __init__(self, cases, precision="fp64", graph_chunk=8):
+    def __init__(self, cases, precision="fp64", graph_chunk=8, method="fwave"):
         import torch
         if not torch.cuda.is_available():
             raise RuntimeError("RiverSolver needs a CUDA device; the step has no CPU implementation")
@@ -154,6 +156,16 @@ class RiverSolver:
                 _ptr(tp["support_cell"]), _ptr(tp["support_weight"]), _ptr(tp["support_density"]),
                 _ptr(tp["plane_offset"]), _ptr(tp["plane_cell"]), _ptr(tp["plane_delta"]), _ptr(tp["dxdy"]),
                 _ptr(tp["inverse"]), _ptr(tp["xy"]), _ptr(tp["mid_disp"]), _ptr(tp["nu"]), _ptr(tp["hkt"])))
+        self.method = method
+        if method not in METHODS:
+            raise ValueError(f"unknown hydraulic method {method!r}")
+        if method == "hllc":
+            # the HLLC owner (river_hllc.install, river_hllc.py:95-101): its own stencil, then the switch
+            from . import hllc as HL
+            hp = HL.pack(self.cases, p["cell_offset"], p["face_offset"])
+            check(self.lib.brx_hllc_set(self.h, _ptr(hp["entry_face"]), _ptr(hp["entry_other"]),
+                                        _ptr(hp["entry_geo"]), _ptr(hp["inverse"])))
+            check(self.lib.brx_method_set(self.h, METHODS[method]))
         self.bed_model = None
         if any(c.get("exner") for c in self.cases):
             self._set_exner()
@@ -290,7 +302,7 @@ class RiverSolver:
             check(code)
         out = []
         for s in stats:
-            out.append(dict(integrator=METHOD, hydraulic_substeps=s.substeps, hydraulic_rejections=s.rejections,
+            out.append(dict(integrator=METHOD_NAMES[self.method], hydraulic_substeps=s.substeps, hydraulic_rejections=s.rejections,
                             hydraulic_minimum_dt=s.min_dt, hydraulic_maximum_dt=s.max_dt,
                             accepted_cfl_max=s.accepted_cfl_max, hydraulic_next_substep_hint_s=s.hint,
                             failed=s.failed))
@@ -313,7 +325,7 @@ class RiverSolver:
             check(code)
         if not done.value:
             return None
-        return [dict(integrator=METHOD, hydraulic_substeps=s.substeps, hydraulic_rejections=s.rejections,
+        return [dict(integrator=METHOD_NAMES[self.method], hydraulic_substeps=s.substeps, hydraulic_rejections=s.rejections,
                      hydraulic_minimum_dt=s.min_dt, hydraulic_maximum_dt=s.max_dt,
                      accepted_cfl_max=s.accepted_cfl_max, hydraulic_next_substep_hint_s=s.hint,
                      failed=s.failed) for s in self._async_stats]
@@ -387,7 +399,9 @@ def kahan_sum(values):
 def _profile(self, dt, time=0.0):
     """Per-kernel durations (ms) of one trial launched without a graph: [(kernel name, ms), ...]."""
     names = {0: "drag", 1: "boundary", 2: "cells", 3: "faces", 4: "gather", 5: "limit", 6: "update",
-             7: "control", 11: "rotors"}
+             7: "control", 11: "rotors",
+             20: "hllc_cells", 21: "hllc_predict", 22: "boundary", 23: "hllc_faces", 24: "hllc_budget",
+             25: "rotors", 26: "hllc_update", 27: "rotors_start"}
     self.torch.cuda.current_stream().synchronize()
     cap = 64
     ms = np.zeros(cap)

@@ -213,6 +213,33 @@ int brx_advance_poll(brx_solver *s, int *done, brx_advance_stats *stats);
 /* Device bytes the solver holds (for admission against a memory budget). */
 long long brx_solver_bytes(const brx_solver *s);
 
+/* Hydraulic methods. */
+#define BRX_METHOD_FWAVE 0   /* augmented f-wave, SSPRK(2,2) (RiverExplicit) */
+#define BRX_METHOD_HLLC 1    /* HLLC / HLLE MUSCL-Hancock (RiverHLLC, FP64 form only) */
+
+/* The HLLC operator's own stencil (replaces HLLCHydraulics.__init__,
+ * src/braids_core/hydraulics/hllc.py:16-61). Per CSR entry k of the cell
+ * incidence (the offsets of brx_solver_create; each cell's faces in
+ * ascending face number, hllc.py:29-34):
+ *   entry_face (nadj)    face id, or its bitwise NOT where the cell is the
+ *                        face's neighbour
+ *   entry_other (nadj)   the other cell, -1 for a wall, -2 for an open face
+ *   entry_geo (4, nadj)  offset to the other centroid (wall: the mirror
+ *                        2 ((mid - xy) . n) n) x, y; face midpoint minus the
+ *                        cell centroid x, y
+ *   inverse (3, nc)      pinv of sum d d^T / |d|^2 over neighbours and walls
+ *                        (open faces excluded): i11, i12, i22
+ * Host arrays, copied. Stage-discharge inlets (mode 9) are not supported by
+ * this method (the reference pairs them with its inlet-feasibility owner). */
+int brx_hllc_set(brx_solver *s, const int *entry_face, const int *entry_other, const double *entry_geo,
+                 const double *inverse);
+
+/* Select the hydraulic method advanced by brx_advance / brx_advance_batch /
+ * brx_advance_start / brx_substep (replaces the reference's river_hllc.install,
+ * src/braids_core/hydraulics/river_hllc.py:95-101). BRX_METHOD_HLLC needs
+ * the FP64 form and brx_hllc_set; brx_rate stays an f-wave residual. */
+int brx_method_set(brx_solver *s, int method);
+
 /* Step hint carried between brx_advance calls (nscen, host; <= 0 = none). */
 int brx_hint_get(brx_solver *s, double *hint);
 int brx_hint_set(brx_solver *s, const double *hint);
@@ -224,7 +251,9 @@ int brx_graph_chunk_set(brx_solver *s, int substeps);
  * on the solver stream (no graph). ms (cap entries) gets each launch's
  * duration and kind (cap entries) its kernel: 0 drag, 1 boundary, 2 cells,
  * 3 faces, 4 gather, 5 limit, 6 update, 7 control, 11 rotor terms (four
- * kernels timed together). *count gets the number
+ * kernels timed together); for BRX_METHOD_HLLC 20 cells, 21 predictor
+ * source, 22 boundary, 23 faces, 24 budget, 25 rotor terms at the predicted
+ * state, 26 update, 27 rotor terms at the start state. *count gets the number
  * of launches. The bound state is advanced as by brx_substep. */
 int brx_profile_substep(brx_solver *s, double dt, double time, int cap, double *ms, int *kind, int *count);
 
