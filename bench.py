@@ -260,6 +260,8 @@ def main():
                     help="skip the HLLC MUSCL-Hancock legs (per-scenario and whole batch, FP64 form)")
     ap.add_argument("--profile-only", type=int, default=0,
                     help="only time N substeps kernel by kernel (brx_profile_substep) and exit")
+    ap.add_argument("--profile-method", default="fwave", choices=("fwave", "hllc"),
+                    help="hydraulic method of --profile-only (hllc runs the FP64 form)")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
@@ -272,7 +274,10 @@ def main():
     torch.cuda.set_device(local)
     if args.profile_only:
         from braids_hkt_gb300.solver import RiverSolver
-        solver = RiverSolver(cases, precision=precision)
+        if args.profile_method == "hllc":
+            solver = RiverSolver(cases, precision="fp64", method="hllc")
+        else:
+            solver = RiverSolver(cases, precision=precision)
         dt = 1e-3                   # one trial of every kernel from the initial state, no interval before it
         for _ in range(args.profile_only):
             print(json.dumps({"cells": solver.nc, "substep_kernels_ms": solver.profile_substep(dt, 0.0)}))
@@ -325,7 +330,7 @@ def main():
         sim_time += outer
         diags = diags if isinstance(diags, list) else [diags]
         failed |= {i for i, d in enumerate(diags) if d["failed"]}
-        updates += sum(d["hydraulic_substeps"] * (solver.packed["cell_offset"][i + 1] - solver.packed["cell_offset"][i])
+        updates += sum(int(d["hydraulic_substeps"]) * int(solver.packed["cell_offset"][i + 1] - solver.packed["cell_offset"][i])
                        for i, d in enumerate(diags))
     barrier()
     wall = time.perf_counter() - wall0
@@ -358,7 +363,7 @@ def main():
         torch.cuda.synchronize()
         sim_time += outer
         diags = diags if isinstance(diags, list) else [diags]
-        e2e_updates += sum(d["hydraulic_substeps"] * (solver.packed["cell_offset"][i + 1] - solver.packed["cell_offset"][i])
+        e2e_updates += sum(int(d["hydraulic_substeps"]) * int(solver.packed["cell_offset"][i + 1] - solver.packed["cell_offset"][i])
                            for i, d in enumerate(diags))
     e2e_s = time.perf_counter() - t0
     h2d = int(q_host.numel() * 8)
@@ -420,7 +425,7 @@ def main():
                     h_failed = h_failed or bool(d["failed"])
                     if k >= args.warmup:
                         h_ms += e0.elapsed_time(e1)
-                        h_updates += d["hydraulic_substeps"] * hs.nc
+                        h_updates += int(d["hydraulic_substeps"]) * int(hs.nc)
                 hs.close()
             one = RiverSolver(cases[i], precision="fp64")
             t_sim = 0.0
@@ -435,7 +440,7 @@ def main():
                 t_sim += outer
                 if k >= args.warmup:
                     p_ms += e0.elapsed_time(e1)
-                    p_updates += d["hydraulic_substeps"] * one.nc
+                    p_updates += int(d["hydraulic_substeps"]) * int(one.nc)
             h64 = one.q[0].cpu().numpy()
             hmx = batch_state[0, off[i]:off[i + 1]]
             rel = np.abs(hmx - h64) / np.maximum(h64, 1e-3)
@@ -479,7 +484,7 @@ def main():
             hfail |= {i for i, d in enumerate(ds) if d["failed"]}
             if k >= 1:
                 ms += e0.elapsed_time(e1)
-                ups += sum(d["hydraulic_substeps"] * (hs.packed["cell_offset"][i + 1] - hs.packed["cell_offset"][i])
+                ups += sum(int(d["hydraulic_substeps"]) * int(hs.packed["cell_offset"][i + 1] - hs.packed["cell_offset"][i])
                            for i, d in enumerate(ds))
         hprof = hs.profile_substep(0.5 * min(d["hydraulic_next_substep_hint_s"] for d in ds), t_sim)
         hllc_batch = {"value": ups / (ms / 1e3), "unit": METRIC, "ms_per_interval": ms / max(1, min(args.steps, 2)),

@@ -40,6 +40,8 @@ SIGNATURES = {
     "brx_solver_bytes": (C.c_longlong, [P]),
     "brx_hllc_set": (I, [P, P, P, P, P]),
     "brx_method_set": (I, [P, I]),
+    "brx_launch_shape_set": (I, [P, I, I, I]),
+    "brx_launch_shape_get": (I, [P, I, P, P, P]),
     "brx_hint_get": (I, [P, P]),
     "brx_hint_set": (I, [P, P]),
     "brx_graph_chunk_set": (I, [P, I]),

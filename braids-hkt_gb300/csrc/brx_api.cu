@@ -28,6 +28,9 @@
 
 using namespace brx;
 
+// Launch-shape slots of the HLLC kernels (their profile kinds).
+enum { KH_CELLS_SHAPE = 20, KH_PREDICT_SHAPE = 21, KH_FACES_SHAPE = 23, KH_BUDGET_SHAPE = 24, KH_UPDATE_SHAPE = 26 };
+
 static thread_local std::string g_error;
 
 static int fail(int code, const std::string &msg)
@@ -75,6 +78,7 @@ struct brx_solver {
     long long launches = 0;
     int grid_c = 0, grid_f = 0;      // persistent grid sizes (cells / faces kernels)
     int grid_c256 = 0, grid_f256 = 0;
+    LaunchShape shape[NSHAPE];       // tunable launch shape per kernel kind (brx_launch_shape_set)
     int launches_per_substep = 0;
     MixedGeo mx{};                   // FP32 geometry of the mixed form
     std::vector<int2> h_cidx;        // host copy: stage-outlet flags follow brx_boundary_set
@@ -84,6 +88,7 @@ struct brx_solver {
     int *d_ccls = nullptr;
     TurbDev turb{};                  // rotor arrays
     bool has_turb = false;
+    bool any_stress = false;         // some rotor scenario has a positive ambient viscosity
     int nrotor = 0;
     double *d_tdiag_out = nullptr;   // (nrotor, 16) diagnostics of brx_turbines_diagnose
     ExnerDev exner{};                // bed model (valid when has_exner)
@@ -396,6 +401,11 @@ extern "C" int brx_solver_create(int nscen, const int *cell_offset, const int *f
         auto grid = [&](int n, int block) { return std::max(1, std::min((n + block - 1) / block, s->sms * 32)); };
         s->grid_c = grid(nc, 128); s->grid_f = grid(nf, 128);
         s->grid_c256 = grid(nc, 256); s->grid_f256 = grid(nf, 256);
+        // default launch shapes: the blocks the kernels were written for, up to 32 blocks per SM
+        for (int k = 0; k < NSHAPE; ++k) s->shape[k] = {256, 32};
+        for (int k : {(int)K_CELLS, (int)K_FACES, (int)KH_CELLS_SHAPE, (int)KH_FACES_SHAPE, (int)K_HKT_FACES})
+            s->shape[k].block = 128;
+        if (precision == BRX_MIXED) s->shape[K_HKT_GRAD].block = 128;
         return BRX_OK;
     }();
     if (rc) { brx_solver_destroy(s); return rc; }
@@ -654,6 +664,7 @@ extern "C" int brx_turbines_set(brx_solver *s, int nrotor, const int *rotor_scen
         CK(cudaMemset(t.sface, 0, sizeof(double) * 2 * (size_t)nf));
     }
     t.balanced = s->method == BRX_METHOD_FWAVE;
+    s->any_stress = std::any_of(stress.begin(), stress.end(), [](int v) { return v != 0; });
     s->turb = t;
     s->has_turb = true;
     s->nrotor = nrotor;
@@ -717,6 +728,62 @@ extern "C" int brx_method_set(brx_solver *s, int method)
     s->method = method;
     s->turb.balanced = method == BRX_METHOD_FWAVE;
     s->graph_dirty = true;
+    return BRX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Launch shapes (the autotuner's knobs)
+// ---------------------------------------------------------------------------
+// Largest block a kind's kernel accepts in this solver's form (its launch
+// bounds and register use), 0 when the kind has no tunable kernel.
+static int max_block(const brx_solver *s, int kind)
+{
+    if (kind < 0 || kind >= NSHAPE) return 0;
+    if (s->precision == BRX_MIXED) return kind >= 20 ? 0 : mixed_max_block(kind, s->maxdeg);
+    const bool small = s->maxdeg <= 4;
+    const void *fn = nullptr;
+    switch (kind) {
+    case K_DRAG: fn = (const void *)k_open_drag<double>; break;
+    case K_CELLS: fn = small ? (const void *)k_cells<double, 4> : (const void *)k_cells<double, MAX_CELL_FACES>; break;
+    case K_FACES: fn = (const void *)k_faces<double>; break;
+    case K_GATHER: fn = (const void *)k_gather; break;
+    case K_LIMIT: fn = (const void *)k_limit; break;
+    case K_UPDATE: fn = (const void *)k_update<double>; break;
+    case K_HKT_GRAD: fn = (const void *)k_hkt_gradients; break;
+    case K_HKT_FACES: fn = (const void *)k_hkt_faces; break;
+    case KH_CELLS_SHAPE:
+        fn = small ? (const void *)k_hllc_cells<4> : (const void *)k_hllc_cells<MAX_CELL_FACES>;
+        break;
+    case KH_PREDICT_SHAPE: fn = (const void *)k_hllc_predict; break;
+    case KH_FACES_SHAPE: fn = (const void *)k_hllc_faces; break;
+    case KH_BUDGET_SHAPE: fn = (const void *)k_hllc_budget; break;
+    case KH_UPDATE_SHAPE: fn = (const void *)k_hllc_update; break;
+    default: return 0;
+    }
+    cudaFuncAttributes a;
+    if (cudaFuncGetAttributes(&a, fn) != cudaSuccess) return 0;
+    return a.maxThreadsPerBlock;
+}
+
+extern "C" int brx_launch_shape_set(brx_solver *s, int kind, int block, int blocks_per_sm)
+{
+    if (!s) return fail(BRX_ERR_ARGUMENT, "null solver");
+    if (s->pending) return fail(BRX_ERR_STATE, "an asynchronous interval is in flight");
+    const int mb = max_block(s, kind);
+    if (mb <= 0) return fail(BRX_ERR_ARGUMENT, "kernel kind has no tunable launch shape");
+    if (block < 32 || block % 32 || block > mb) return fail(BRX_ERR_ARGUMENT, "block must be a multiple of 32 within the kernel's limit");
+    if (blocks_per_sm < 1 || blocks_per_sm > 64) return fail(BRX_ERR_ARGUMENT, "blocks per SM must be in 1..64");
+    s->shape[kind] = {block, blocks_per_sm};
+    s->graph_dirty = true;
+    return BRX_OK;
+}
+
+extern "C" int brx_launch_shape_get(brx_solver *s, int kind, int *block, int *blocks_per_sm, int *max_threads)
+{
+    if (!s || !block || !blocks_per_sm || !max_threads) return fail(BRX_ERR_ARGUMENT, "null argument");
+    const int mb = max_block(s, kind);
+    if (mb <= 0) return fail(BRX_ERR_ARGUMENT, "kernel kind has no tunable launch shape");
+    *block = s->shape[kind].block; *blocks_per_sm = s->shape[kind].per_sm; *max_threads = mb;
     return BRX_OK;
 }
 
@@ -878,6 +945,8 @@ static Launch make_launch(brx_solver *s, cudaStream_t st)
     L.mesh = s->mesh; L.state = s->state; L.bnd = s->bnd; L.work = s->work; L.ctrl = s->d_ctrl;
     L.nscen = s->nscen; L.nslot = s->nslot; L.maxdeg = s->maxdeg;
     L.grid_c = s->grid_c; L.grid_f = s->grid_f; L.grid_c256 = s->grid_c256; L.grid_f256 = s->grid_f256;
+    L.sms = s->sms;
+    for (int k = 0; k < NSHAPE; ++k) L.shape[k] = s->shape[k];
     L.stream = st;
     L.mx = s->mx;
     L.turb = s->turb;
@@ -889,19 +958,31 @@ static Launch make_launch(brx_solver *s, cudaStream_t st)
 // the solver stream); returns launches issued.
 // The rotor-array terms of one stage (scenarios with rotors only): wet
 // gradients, one CTA per rotor, the sink per support cell, face terms.
+// Grid and block of a kernel kind from its launch shape.
+static inline int sgrid(const brx_solver *s, int kind, int n)
+{
+    const LaunchShape &sh = s->shape[kind];
+    const int g = (n + sh.block - 1) / sh.block, cap = sh.per_sm * s->sms;
+    return std::max(1, std::min(g, cap));
+}
+#define SSHAPE(kind_, n_) sgrid(s, kind_, n_), s->shape[kind_].block
+
 static int launch_turbines(brx_solver *s, int stage, cudaStream_t st)
 {
     if (!s->has_turb) return 0;
     const double *q = stage == 1 ? s->state.work : s->state.q1;
     const TurbDev &t = s->turb;
     const bool mixed = s->precision == BRX_MIXED;
+    // the wet gradients feed only the face terms (balanced pressure, ambient
+    // stress); the HLLC owner without ambient stress has neither
+    const bool faces = t.balanced || s->any_stress;
     if (mixed) mixed_kernel(make_launch(s, st), K_HKT_GRAD, stage, nullptr);
-    else k_hkt_gradients<<<s->grid_c256, 256, 0, st>>>(s->mesh, t, q, s->state.z, s->d_ctrl, stage);
+    else if (faces) k_hkt_gradients<<<SSHAPE(K_HKT_GRAD, s->nc), 0, st>>>(s->mesh, t, q, s->state.z, s->d_ctrl, stage);
     k_turbine_sample<<<t.nr, TURB_THREADS, 0, st>>>(s->mesh, t, q, s->state.z, s->d_ctrl, stage, t.diag);
     k_turbine_raw<<<std::max(1, std::min((t.nucell + 255) / 256, s->sms * 8)), 256, 0, st>>>(s->mesh, t, q, s->d_ctrl, stage);
     if (mixed) mixed_kernel(make_launch(s, st), K_HKT_FACES, stage, nullptr);
-    else k_hkt_faces<<<s->grid_f, 128, 0, st>>>(s->mesh, t, q, s->state.z, s->d_ctrl, stage);
-    return 4;
+    else if (faces) k_hkt_faces<<<SSHAPE(K_HKT_FACES, s->nf), 0, st>>>(s->mesh, t, q, s->state.z, s->d_ctrl, stage);
+    return mixed || faces ? 4 : 2;
 }
 
 static int launch_kernel(brx_solver *s, int kind, int stage, double *rate_out, cudaStream_t st = nullptr)
@@ -911,28 +992,28 @@ static int launch_kernel(brx_solver *s, int kind, int stage, double *rate_out, c
     if (s->precision == BRX_MIXED) return mixed_kernel(make_launch(s, st), kind, stage, rate_out);
     switch (kind) {
     case K_DRAG:
-        k_open_drag<double><<<s->grid_c256, 256, 0, st>>>(s->mesh, s->state, s->d_ctrl);
+        k_open_drag<double><<<SSHAPE(K_DRAG, s->nc), 0, st>>>(s->mesh, s->state, s->d_ctrl);
         return 1;
     case K_BOUNDARY:
         if (!s->nslot) return 0;
         k_boundary<double><<<s->nscen, 256, 0, st>>>(s->mesh, s->state, s->bnd, s->d_ctrl, stage);
         return 1;
     case K_CELLS:
-        if (s->maxdeg <= 4) k_cells<double, 4><<<s->grid_c, 128, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage);
-        else k_cells<double, MAX_CELL_FACES><<<s->grid_c, 128, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage);
+        if (s->maxdeg <= 4) k_cells<double, 4><<<SSHAPE(K_CELLS, s->nc), 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage);
+        else k_cells<double, MAX_CELL_FACES><<<SSHAPE(K_CELLS, s->nc), 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage);
         return 1;
     case K_FACES:
-        k_faces<double><<<s->grid_f, 128, 0, st>>>(s->mesh, s->state, s->bnd, s->d_ctrl, s->work, stage,
+        k_faces<double><<<SSHAPE(K_FACES, s->nf), 0, st>>>(s->mesh, s->state, s->bnd, s->d_ctrl, s->work, stage,
                                                     s->has_turb ? s->turb.trace : nullptr, s->turb.hkt);
         return 1;
     case K_GATHER:
-        k_gather<<<s->grid_c256, 256, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage);
+        k_gather<<<SSHAPE(K_GATHER, s->nc), 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage);
         return 1;
     case K_LIMIT:
-        k_limit<<<s->grid_f256, 256, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage);
+        k_limit<<<SSHAPE(K_LIMIT, s->nf), 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage);
         return 1;
     case K_UPDATE:
-        k_update<double><<<s->grid_c256, 256, 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage, rate_out,
+        k_update<double><<<SSHAPE(K_UPDATE, s->nc), 0, st>>>(s->mesh, s->state, s->d_ctrl, s->work, stage, rate_out,
                                                         s->turb, s->has_turb);
         return 1;
     }
@@ -966,29 +1047,29 @@ static int launch_hllc(brx_solver *s, int kind, cudaStream_t st = nullptr)
     HCell *rec = reinterpret_cast<HCell *>(s->work.rec);      // 96 of the 128 bytes per cell
     switch (kind) {
     case KH_CELLS:
-        if (s->maxdeg <= 4) k_hllc_cells<4><<<s->grid_c, 128, 0, st>>>(s->mesh, s->state, s->hllc, rec, s->d_ctrl);
-        else k_hllc_cells<MAX_CELL_FACES><<<s->grid_c, 128, 0, st>>>(s->mesh, s->state, s->hllc, rec, s->d_ctrl);
+        if (s->maxdeg <= 4) k_hllc_cells<4><<<SSHAPE(KH_CELLS_SHAPE, s->nc), 0, st>>>(s->mesh, s->state, s->hllc, rec, s->d_ctrl);
+        else k_hllc_cells<MAX_CELL_FACES><<<SSHAPE(KH_CELLS_SHAPE, s->nc), 0, st>>>(s->mesh, s->state, s->hllc, rec, s->d_ctrl);
         return 1;
     case KH_TURB0:        // rotor terms on the start state (stage 1 reads work)
         return s->has_turb ? launch_turbines(s, 1, st) : 0;
     case KH_PREDICT:
         if (!s->has_turb) return 0;
-        k_hllc_predict<<<s->grid_c256, 256, 0, st>>>(s->mesh, s->state, s->turb, rec, s->d_ctrl);
+        k_hllc_predict<<<SSHAPE(KH_PREDICT_SHAPE, s->nc), 0, st>>>(s->mesh, s->state, s->turb, rec, s->d_ctrl);
         return 1;
     case KH_BOUNDARY:
         if (!s->nslot) return 0;
         k_boundary<double><<<s->nscen, 256, 0, st>>>(s->mesh, s->state, s->bnd, s->d_ctrl, STAGE_HANCOCK);
         return 1;
     case KH_FACES:
-        k_hllc_faces<<<s->grid_f, 128, 0, st>>>(s->mesh, s->bnd, rec, s->work, s->turb, s->has_turb, s->d_ctrl);
+        k_hllc_faces<<<SSHAPE(KH_FACES_SHAPE, s->nf), 0, st>>>(s->mesh, s->bnd, rec, s->work, s->turb, s->has_turb, s->d_ctrl);
         return 1;
     case KH_BUDGET:
-        k_hllc_budget<<<s->grid_c256, 256, 0, st>>>(s->mesh, s->state, s->hllc, s->work, s->d_ctrl);
+        k_hllc_budget<<<SSHAPE(KH_BUDGET_SHAPE, s->nc), 0, st>>>(s->mesh, s->state, s->hllc, s->work, s->d_ctrl);
         return 1;
     case KH_TURB:         // rotor terms on the predicted state (stage 2 reads q1)
         return s->has_turb ? launch_turbines(s, 2, st) : 0;
     case KH_UPDATE:
-        k_hllc_update<<<s->grid_c256, 256, 0, st>>>(s->mesh, s->state, s->hllc, s->work, s->turb, s->has_turb,
+        k_hllc_update<<<SSHAPE(KH_UPDATE_SHAPE, s->nc), 0, st>>>(s->mesh, s->state, s->hllc, s->work, s->turb, s->has_turb,
                                                     s->d_ctrl);
         return 1;
     }

@@ -32,6 +32,14 @@ struct MixedGeo {
     float2 *hp, *hs;         // (nf) balanced-pressure correction, ambient stress
 };
 
+// Launch shape of one kernel kind: threads per block and the grid cap in
+// resident blocks per SM (grid = min(ceil(n / block), per_sm * SMs); the
+// sweeps are grid-stride loops, so any shape covers every element).
+constexpr int NSHAPE = 32;
+struct LaunchShape {
+    int block, per_sm;
+};
+
 struct Launch {
     MeshDev mesh;
     StateDev state;
@@ -44,7 +52,16 @@ struct Launch {
     MixedGeo mx;
     TurbDev turb;            // rotor arrays (valid when has_turb)
     int has_turb;
+    int sms;
+    LaunchShape shape[NSHAPE];
 };
+
+inline int shape_grid(const Launch &L, int kind, int n)
+{
+    const LaunchShape &sh = L.shape[kind];
+    const int g = (n + sh.block - 1) / sh.block, cap = sh.per_sm * L.sms;
+    return g < 1 ? 1 : (g < cap ? g : cap);
+}
 
 // Kernel kinds of one substep, in launch order within a stage.
 enum KernelKind { K_DRAG = 0, K_BOUNDARY = 1, K_CELLS = 2, K_FACES = 3, K_GATHER = 4, K_LIMIT = 5, K_UPDATE = 6 };
@@ -59,5 +76,9 @@ enum { K_TURB = 11 };
 // the water buffer of K_WATER. Returns the number of kernels launched (0 for a
 // boundary kernel without open faces).
 int mixed_kernel(const Launch &L, int kind, int stage, double *out);
+
+// Largest block the mixed form's kernel of this kind accepts (its launch
+// bounds and registers), 0 for a kind without a tunable kernel.
+int mixed_max_block(int kind, int maxdeg);
 
 }  // namespace brx

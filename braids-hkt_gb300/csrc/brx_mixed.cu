@@ -910,34 +910,56 @@ __global__ void __launch_bounds__(128) km_hkt_faces(MeshDev m, Ctrl *ctrl, Mixed
 
 namespace brx {
 
+int mixed_max_block(int kind, int maxdeg)
+{
+    const bool small = maxdeg <= 4;
+    const void *fn = nullptr;
+    switch (kind) {
+    case K_DRAG: fn = (const void *)brx_mx::km_open_drag; break;
+    case K_CELLS: fn = small ? (const void *)brx_mx::km_cells<4> : (const void *)brx_mx::km_cells<MAX_CELL_FACES>; break;
+    case K_FACES: fn = (const void *)brx_mx::km_faces; break;
+    case K_GATHER: fn = (const void *)brx_mx::km_gather; break;
+    case K_LIMIT: fn = (const void *)brx_mx::km_limit; break;
+    case K_UPDATE: fn = (const void *)brx_mx::km_update; break;
+    case K_HKT_GRAD: fn = (const void *)brx_mx::km_hkt_gradients; break;
+    case K_HKT_FACES: fn = (const void *)brx_mx::km_hkt_faces; break;
+    default: return 0;
+    }
+    cudaFuncAttributes a;
+    if (cudaFuncGetAttributes(&a, fn) != cudaSuccess) return 0;
+    return a.maxThreadsPerBlock;
+}
+
 int mixed_kernel(const Launch &L, int kind, int stage, double *out)
 {
     cudaStream_t st = L.stream;
     const bool small = L.maxdeg <= 4;
+    const int nc = L.mesh.nc, nf = L.mesh.nf;
+#define SHAPE(kind_, n_) shape_grid(L, kind_, n_), L.shape[kind_].block
     switch (kind) {
     case K_DRAG:
-        brx_mx::km_open_drag<<<L.grid_c256, 256, 0, st>>>(L.mesh, L.state, L.ctrl, L.mx);
+        brx_mx::km_open_drag<<<SHAPE(K_DRAG, nc), 0, st>>>(L.mesh, L.state, L.ctrl, L.mx);
         return 1;
     case K_BOUNDARY:
         if (!L.nslot) return 0;
         brx_mixb::k_boundary<float><<<L.nscen, 256, 0, st>>>(L.mesh, L.state, L.bnd, L.ctrl, stage);
         return 1;
     case K_CELLS:
-        if (small) brx_mx::km_cells<4><<<L.grid_c, 128, 0, st>>>(L.mesh, L.state, L.ctrl, L.work, L.mx, stage);
-        else brx_mx::km_cells<MAX_CELL_FACES><<<L.grid_c, 128, 0, st>>>(L.mesh, L.state, L.ctrl, L.work, L.mx, stage);
+        if (small) brx_mx::km_cells<4><<<SHAPE(K_CELLS, nc), 0, st>>>(L.mesh, L.state, L.ctrl, L.work, L.mx, stage);
+        else brx_mx::km_cells<MAX_CELL_FACES><<<SHAPE(K_CELLS, nc), 0, st>>>(L.mesh, L.state, L.ctrl, L.work, L.mx, stage);
         return 1;
     case K_FACES:
-        brx_mx::km_faces<<<L.grid_f, 128, 0, st>>>(L.mesh, L.state, L.bnd, L.ctrl, L.work, L.mx, stage, L.turb,
+        brx_mx::km_faces<<<SHAPE(K_FACES, nf), 0, st>>>(L.mesh, L.state, L.bnd, L.ctrl, L.work, L.mx, stage, L.turb,
                                                     L.has_turb);
         return 1;
     case K_GATHER:
-        brx_mx::km_gather<<<L.grid_c256, 256, 0, st>>>(L.mesh, L.state, L.ctrl, L.work, L.mx, stage);
+        brx_mx::km_gather<<<SHAPE(K_GATHER, nc), 0, st>>>(L.mesh, L.state, L.ctrl, L.work, L.mx, stage);
         return 1;
     case K_LIMIT:
-        brx_mx::km_limit<<<L.grid_f256, 256, 0, st>>>(L.mesh, L.ctrl, L.work, L.mx, stage);
+        brx_mx::km_limit<<<SHAPE(K_LIMIT, nf), 0, st>>>(L.mesh, L.ctrl, L.work, L.mx, stage);
         return 1;
     case K_UPDATE:
-        brx_mx::km_update<<<L.grid_c256, 256, 0, st>>>(L.mesh, L.state, L.ctrl, L.work, L.mx, stage, out, L.turb,
+        brx_mx::km_update<<<SHAPE(K_UPDATE, nc), 0, st>>>(L.mesh, L.state, L.ctrl, L.work, L.mx, stage, out, L.turb,
                                                      L.has_turb);
         return 1;
     case K_PRIM:
@@ -953,12 +975,13 @@ int mixed_kernel(const Launch &L, int kind, int stage, double *out)
         brx_mx::km_water_out<<<L.grid_f256, 256, 0, st>>>(L.mesh, L.work, out);
         return 1;
     case K_HKT_GRAD:
-        brx_mx::km_hkt_gradients<<<L.grid_c, 128, 0, st>>>(L.mesh, L.ctrl, L.mx, L.turb, stage);
+        brx_mx::km_hkt_gradients<<<SHAPE(K_HKT_GRAD, nc), 0, st>>>(L.mesh, L.ctrl, L.mx, L.turb, stage);
         return 1;
     case K_HKT_FACES:
-        brx_mx::km_hkt_faces<<<L.grid_f, 128, 0, st>>>(L.mesh, L.ctrl, L.mx, L.turb, stage);
+        brx_mx::km_hkt_faces<<<SHAPE(K_HKT_FACES, nf), 0, st>>>(L.mesh, L.ctrl, L.mx, L.turb, stage);
         return 1;
     }
+#undef SHAPE
     return 0;
 }
 

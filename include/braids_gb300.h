@@ -247,6 +247,16 @@ int brx_hint_set(brx_solver *s, const double *hint);
 /* Number of substeps captured per CUDA graph replay inside brx_advance. */
 int brx_graph_chunk_set(brx_solver *s, int substeps);
 
+/* Launch shape of one kernel kind (the kinds of brx_profile_substep: 0 drag,
+ * 2 cells, 3 faces, 4 gather, 5 limit, 6 update, 12 / 13 rotor gradients /
+ * face terms; HLLC 20 cells, 21 predictor, 23 faces, 24 budget, 26 update):
+ * threads per block (a multiple of 32 up to the kernel's limit) and the grid
+ * cap in blocks per SM. Every sweep is a grid-stride loop, so results do not
+ * depend on the shape. The autotuner (braids_hkt_gb300.autotune) sets these;
+ * no counterpart in the reference. get also returns the kernel's limit. */
+int brx_launch_shape_set(brx_solver *s, int kind, int block, int blocks_per_sm);
+int brx_launch_shape_get(brx_solver *s, int kind, int *block, int *blocks_per_sm, int *max_threads);
+
 /* Time one SSPRK(2,2) trial of exactly dt kernel by kernel with CUDA events
  * on the solver stream (no graph). ms (cap entries) gets each launch's
  * duration and kind (cap entries) its kernel: 0 drag, 1 boundary, 2 cells,
