@@ -307,6 +307,12 @@ def main():
         diags = diags if isinstance(diags, list) else [diags]
         failed |= {i for i, d in enumerate(diags) if d["failed"]}
         sim_time += outer
+    # launch schedule picked by the autotuner on this batch (outside the timed region)
+    from braids_hkt_gb300 import autotune
+    tuned = autotune.tune(solver, dt=0.25 * min(d["hydraulic_next_substep_hint_s"] for d in diags), time0=sim_time,
+                          cache=False)
+    cfg["autotune"] = {k: tuned[k] for k in ("kernels", "chunk", "chunk_ms", "substep_ms_default",
+                                             "substep_ms_tuned", "tuning_s")}
     # timed region: K outer steps, device time by events on the solver stream
     clocks = ClockSampler(local)
     clocks.start()
@@ -335,6 +341,12 @@ def main():
     barrier()
     wall = time.perf_counter() - wall0
     gpu_launches = solver.launches() - launches0
+    # substeps of the last timed interval per scenario: the batch runs as many
+    # graph substeps as its slowest scenario needs
+    subs = np.array([int(d["hydraulic_substeps"]) for d in diags])
+    cells = np.diff(solver.packed["cell_offset"]).astype(np.int64)
+    cfg["substeps_per_interval"] = {"min": int(subs.min()), "median": float(np.median(subs)), "max": int(subs.max()),
+                                    "cell_weighted_mean": float((subs * cells).sum() / cells.sum())}
     clock_info = clocks.stop()
     t_max = device_ms / 1e3
     if dist is not None:
@@ -470,6 +482,8 @@ def main():
     if args.hllc and precision == "mixed":
         # the whole batch with the HLLC method (FP64 form): one warm-up and up to two timed intervals
         hs = RiverSolver(cases, precision="fp64", method="hllc")
+        from braids_hkt_gb300 import autotune
+        htuned = autotune.tune(hs, cache=False)
         t_sim, ms, ups, hfail = 0.0, 0.0, 0, set()
         for k in range(1 + max(1, min(args.steps, 2))):
             flush_l2(torch, flush)
@@ -490,6 +504,7 @@ def main():
         hllc_batch = {"value": ups / (ms / 1e3), "unit": METRIC, "ms_per_interval": ms / max(1, min(args.steps, 2)),
                       "failed_scenarios": sorted(hfail),
                       "substep_kernels_ms": [(n, round(v, 4)) for n, v in hprof],
+                      "autotune": {k: htuned[k] for k in ("kernels", "chunk", "substep_ms_default", "substep_ms_tuned")},
                       "note": "the whole batch (rotors included) with the HLLC MUSCL-Hancock method, FP64 form; "
                               "one cell-update = one cell advanced by one accepted Hancock substep"}
         hs.close()

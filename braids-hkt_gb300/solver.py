@@ -145,6 +145,7 @@ class RiverSolver:
         self.z = torch.from_numpy(p["z"]).to(dev).contiguous()
         check(self.lib.brx_state_bind(self.h, C.c_void_p(self.q.data_ptr()), C.c_void_p(self.z.data_ptr())))
         check(self.lib.brx_graph_chunk_set(self.h, int(graph_chunk)))
+        self.graph_chunk = int(graph_chunk)
         self.rotors = None
         from . import turbines as TB
         tp = TB.pack(self.cases, p["cell_offset"])
@@ -396,8 +397,9 @@ def kahan_sum(values):
     return s
 
 
-def _profile(self, dt, time=0.0):
-    """Per-kernel durations (ms) of one trial launched without a graph: [(kernel name, ms), ...]."""
+def _profile(self, dt, time=0.0, kinds=False):
+    """Per-kernel durations (ms) of one trial launched without a graph: [(kernel name, ms), ...]
+    (kernel kind ids instead of names with kinds=True)."""
     names = {0: "drag", 1: "boundary", 2: "cells", 3: "faces", 4: "gather", 5: "limit", 6: "update",
              7: "control", 11: "rotors",
              20: "hllc_cells", 21: "hllc_predict", 22: "boundary", 23: "hllc_faces", 24: "hllc_budget",
@@ -408,7 +410,28 @@ def _profile(self, dt, time=0.0):
     kind = np.zeros(cap, np.int32)
     count = C.c_int()
     check(self.lib.brx_profile_substep(self.h, float(dt), float(time), cap, _ptr(ms), _ptr(kind), C.byref(count)))
+    if kinds:
+        return [(int(kind[i]), float(ms[i])) for i in range(count.value)]
     return [(names[kind[i]], float(ms[i])) for i in range(count.value)]
 
 
+def _shape(self, kind):
+    """(block, blocks per SM, the kernel's largest block) of a kernel kind."""
+    b, p, m = C.c_int(), C.c_int(), C.c_int()
+    check(self.lib.brx_launch_shape_get(self.h, int(kind), C.byref(b), C.byref(p), C.byref(m)))
+    return b.value, p.value, m.value
+
+
+def _set_shape(self, kind, block, per_sm):
+    check(self.lib.brx_launch_shape_set(self.h, int(kind), int(block), int(per_sm)))
+
+
+def _set_chunk(self, substeps):
+    check(self.lib.brx_graph_chunk_set(self.h, int(substeps)))
+    self.graph_chunk = int(substeps)
+
+
 RiverSolver.profile_substep = _profile
+RiverSolver.launch_shape = _shape
+RiverSolver.set_launch_shape = _set_shape
+RiverSolver.set_graph_chunk = _set_chunk
