@@ -326,6 +326,14 @@ extern "C" int brx_solver_create(int nscen, const int *cell_offset, const int *f
         TRY(s->alloc(&s->work.lim, nf)); TRY(s->alloc(&s->work.rate, 3 * (size_t)nc));
         TRY(s->alloc(&s->work.theta, nc));
         TRY(s->alloc(&s->d_ctrl, nscen));
+        // active set of the current trial (rebuilt on the device by k_control)
+        TRY(s->upload(&s->d_cell_off, s->cell_offset.data(), s->cell_offset.size()));
+        TRY(s->upload(&s->d_face_off, s->face_offset.data(), s->face_offset.size()));
+        ActiveDev &a = s->mesh.act;
+        TRY(s->alloc(&a.count, 3)); TRY(s->alloc(&a.sid, nscen));
+        TRY(s->alloc(&a.cstart, nscen + 1)); TRY(s->alloc(&a.fstart, nscen + 1));
+        CK(cudaMemset(a.count, 0, sizeof(int) * 3));
+        a.cell_off = s->d_cell_off; a.face_off = s->d_face_off;
         if (precision == BRX_MIXED) {
             // FP32 geometry packed per cell, per CSR entry and per face; the LS
             // inverse is formed in FP64 here so the sweep only multiplies.
@@ -839,8 +847,6 @@ extern "C" int brx_exner_set(brx_solver *s, const int *enabled, const double *pa
     TRY(s->alloc(&e.wet, nc)); TRY(s->alloc(&e.bad, ns));
     TRY(s->alloc(&s->d_exdt, ns));
     e.dt = s->d_exdt;
-    TRY(s->upload(&s->d_cell_off, s->cell_offset.data(), s->cell_offset.size()));
-    TRY(s->upload(&s->d_face_off, s->face_offset.data(), s->face_offset.size()));
     s->exner = e;
     s->has_exner = true;
     return BRX_OK;
@@ -1094,7 +1100,15 @@ static void enqueue_trial(brx_solver *s)
 static void enqueue_substep(brx_solver *s)
 {
     enqueue_trial(s);
-    k_control<<<(s->nscen + 127) / 128, 128, 0, s->stream>>>(s->d_ctrl, s->nscen);
+    k_control<<<1, 256, 0, s->stream>>>(s->d_ctrl, s->nscen, s->mesh.act);
+    s->launches++;
+}
+
+// Control blocks to the device and the first trial's active set from them.
+static void upload_ctrl(brx_solver *s)
+{
+    cudaMemcpyAsync(s->d_ctrl, s->h_ctrl, sizeof(Ctrl) * s->nscen, cudaMemcpyHostToDevice, s->stream);
+    k_active_init<<<1, 32, 0, s->stream>>>(s->d_ctrl, s->nscen, s->mesh.act);
     s->launches++;
 }
 
@@ -1198,7 +1212,7 @@ extern "C" int brx_advance_start(brx_solver *s, const double *dt, const double *
         if (!std::isfinite(dt[i]) || !std::isfinite(time[i])) return fail(BRX_ERR_ARGUMENT, "nonfinite interval");
     if (s->graph_dirty || !s->graph) TRY(build_graph(s));
     begin_interval_each(s, dt, time, false);
-    CK(cudaMemcpyAsync(s->d_ctrl, s->h_ctrl, sizeof(Ctrl) * s->nscen, cudaMemcpyHostToDevice, s->stream));
+    upload_ctrl(s);
     refresh_bed(s);
     s->replays = 0;
     s->pending = true;
@@ -1239,7 +1253,7 @@ static int advance_impl(brx_solver *s, const double *dt, const double *time, brx
     if (s->graph_dirty || !s->graph) TRY(build_graph(s));
     begin_interval_each(s, dt, time, false);
     refresh_bed(s);
-    CK(cudaMemcpyAsync(s->d_ctrl, s->h_ctrl, sizeof(Ctrl) * s->nscen, cudaMemcpyHostToDevice, s->stream));
+    upload_ctrl(s);
     // every scenario ends within max_substeps accepted + 101 rejected trials
     const int max_replays = (4096 + 102) / s->graph_chunk + 2;
     bool all_done = false;
@@ -1286,13 +1300,13 @@ extern "C" int brx_substep(brx_solver *s, double dt, double time, unsigned *stat
     begin_interval(s, dt, time, true);
     refresh_bed(s);
     for (int i = 0; i < s->nscen; ++i) s->h_ctrl[i].max_substeps = 4096;
-    CK(cudaMemcpyAsync(s->d_ctrl, s->h_ctrl, sizeof(Ctrl) * s->nscen, cudaMemcpyHostToDevice, s->stream));
+    upload_ctrl(s);
     // the trial without the controller: its statuses are read before control runs
     enqueue_trial(s);
     CK(cudaMemcpyAsync(s->h_ctrl, s->d_ctrl, sizeof(Ctrl) * s->nscen, cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     std::vector<Ctrl> trial(s->h_ctrl, s->h_ctrl + s->nscen);
-    k_control<<<(s->nscen + 127) / 128, 128, 0, s->stream>>>(s->d_ctrl, s->nscen);
+    k_control<<<1, 256, 0, s->stream>>>(s->d_ctrl, s->nscen, s->mesh.act);
     k_commit<<<s->grid_c256, 256, 0, s->stream>>>(s->mesh, s->state, s->d_ctrl);
     s->launches += 2;
     CK(cudaMemcpyAsync(s->h_ctrl, s->d_ctrl, sizeof(Ctrl) * s->nscen, cudaMemcpyDeviceToHost, s->stream));
@@ -1318,7 +1332,7 @@ extern "C" int brx_rate(brx_solver *s, double dt, double time, double *rate_devi
     if (!rate_device || !water_device) return fail(BRX_ERR_ARGUMENT, "null output buffer");
     if (s->method != BRX_METHOD_FWAVE) return fail(BRX_ERR_UNSUPPORTED, "brx_rate is the f-wave spatial residual");
     begin_interval(s, dt, time, true);
-    CK(cudaMemcpyAsync(s->d_ctrl, s->h_ctrl, sizeof(Ctrl) * s->nscen, cudaMemcpyHostToDevice, s->stream));
+    upload_ctrl(s);
     CK(cudaMemcpyAsync(s->state.work, s->state.q[0], sizeof(double) * 3 * s->nc, cudaMemcpyDeviceToDevice, s->stream));
     refresh_bed(s);
     if (s->precision == BRX_MIXED) s->launches += launch_kernel(s, K_PRIM, 1, nullptr);
@@ -1350,7 +1364,7 @@ extern "C" int brx_profile_substep(brx_solver *s, double dt, double time, int ca
     if (!(dt > 0) || !std::isfinite(dt)) return fail(BRX_ERR_ARGUMENT, "dt must be finite and positive");
     begin_interval(s, dt, time, true);
     refresh_bed(s);
-    CK(cudaMemcpyAsync(s->d_ctrl, s->h_ctrl, sizeof(Ctrl) * s->nscen, cudaMemcpyHostToDevice, s->stream));
+    upload_ctrl(s);
     std::vector<cudaEvent_t> ev;
     std::vector<int> kinds;
     auto mark = [&](int k) {
@@ -1373,7 +1387,7 @@ extern "C" int brx_profile_substep(brx_solver *s, double dt, double time, int ca
                              (int)K_UPDATE})
                 if (const int nl = launch_kernel(s, kind, stage, nullptr)) { mark(kind); extra += nl - 1; }
     }
-    k_control<<<(s->nscen + 127) / 128, 128, 0, st>>>(s->d_ctrl, s->nscen); mark(7);
+    k_control<<<1, 256, 0, st>>>(s->d_ctrl, s->nscen, s->mesh.act); mark(7);
     k_commit<<<s->grid_c256, 256, 0, st>>>(s->mesh, s->state, s->d_ctrl);
     s->launches += (long long)kinds.size() + 1 + extra;
     CK(cudaGetLastError());
@@ -1421,7 +1435,8 @@ constexpr size_t NA_BSLOT = NA_FSID + noalloc_align(sizeof(int) * NOALLOC_MAX_FA
 constexpr size_t NA_BMODE = NA_BSLOT + noalloc_align(sizeof(int) * NOALLOC_MAX_FACES);
 constexpr size_t NA_DUNIT = NA_BMODE + noalloc_align(sizeof(int) * NOALLOC_MAX_FACES);
 constexpr size_t NA_CTRL = NA_DUNIT + noalloc_align(sizeof(double) * 4 * NOALLOC_MAX_FACES);
-constexpr size_t NOALLOC_BYTES = NA_CTRL + noalloc_align(sizeof(Ctrl));   // about 7.4 MB
+constexpr size_t NA_ACT = NA_CTRL + noalloc_align(sizeof(Ctrl));
+constexpr size_t NOALLOC_BYTES = NA_ACT + noalloc_align(sizeof(int) * 16);   // about 7.4 MB
 
 static __device__ __align__(256) unsigned char brx_noalloc_scratch[NOALLOC_BYTES];
 
@@ -1445,7 +1460,15 @@ static int noalloc_address(unsigned char **out)
     return BRX_OK;
 }
 
-__global__ void k_noalloc_ctrl(Ctrl *ctrl, Ctrl init) { *ctrl = init; }
+// The control block and the one-scenario active set: count {1, nc, nf}, sid
+// {0}, cell / face prefixes {0, nc} / {0, nf}, packed ranges the same.
+__global__ void k_noalloc_ctrl(Ctrl *ctrl, Ctrl init, int *act, int nc, int nf)
+{
+    *ctrl = init;
+    const int v[11] = {1, nc, nf, 0, 0, nc, 0, nf, 0, nc, 0};
+    for (int i = 0; i < 11; ++i) act[i] = v[i];
+    act[11] = nf;
+}
 
 // Derived per-cell/per-face tables of a closed single-scenario mesh, and a
 // bounds check of the caller's topology: any index out of range or a cell
@@ -1515,6 +1538,9 @@ extern "C" int brx_rate_noalloc(int nc, int nf, int nadj, const int *owner, cons
     m.normal = normal; m.length = length; m.area = area; m.ls_matrix = ls_matrix; m.ls_weight = ls_weight;
     m.ls_delta = ls_delta; m.disp = displacement; m.disp_unit = disp_unit; m.disp_len = displacement_length;
     m.distance = distance;
+    int *act = (int *)(base + NA_ACT);   // count[3] sid[1] cstart[2] fstart[2] cell_off[2] face_off[2]
+    m.act.count = act; m.act.sid = act + 3; m.act.cstart = act + 4; m.act.fstart = act + 6;
+    m.act.cell_off = act + 8; m.act.face_off = act + 10;
     StateDev sd{};
     sd.q[0] = const_cast<double *>(q);
     sd.work = const_cast<double *>(q);    // the residual reads its stage state here and never writes it
@@ -1533,7 +1559,7 @@ extern "C" int brx_rate_noalloc(int nc, int nf, int nadj, const int *owner, cons
     init.dt_outer = dt; init.hint = dt; init.trial = dt; init.max_substeps = 1;
     // Every field the residual reads is rewritten here: the array keeps the
     // previous call's contents, and calls that overlap on the GPU race on it.
-    k_noalloc_ctrl<<<1, 1, 0, st>>>(ctrl, init);
+    k_noalloc_ctrl<<<1, 1, 0, st>>>(ctrl, init, act, nc, nf);
     const int n = nc > nf ? nc : nf;
     k_noalloc_tables<<<(n + 255) / 256, 256, 0, st>>>(m, ctrl, cell_sid, cflags, face_sid, bslot, bmode, disp_unit);
     k_cells<double, MAX_CELL_FACES><<<(nc + 127) / 128, 128, 0, st>>>(m, sd, ctrl, w, 1);

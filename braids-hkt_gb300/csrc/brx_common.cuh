@@ -67,6 +67,50 @@ struct Ctrl {
     int cfl1, pad1;                         // stage 1 exceeded the CFL limit (mixed form, set after its gather)
 };
 
+// Scenarios taking part in the current trial, packed: every sweep visits only
+// their cells and faces, so a batch whose scenarios need different substep
+// counts pays nothing for the ones that have finished their interval. The
+// host sets it at the start of an interval; k_control rebuilds it after every
+// trial (ascending scenario order).
+struct ActiveDev {
+    int *count;              // [0] scenarios, [1] cells, [2] faces
+    int *sid;                // (nscen) active scenario ids
+    int *cstart, *fstart;    // (nscen+1) prefix sums of their cell and face counts
+    const int *cell_off, *face_off;   // (nscen+1) packed ranges of every scenario
+};
+
+// Position of packed index i in a prefix array: the largest j < n with start[j] <= i.
+__device__ __forceinline__ int active_slot(const int *start, int n, int i)
+{
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (start[mid] <= i) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ int active_cell(const ActiveDev &a, int i)
+{
+    const int j = active_slot(a.cstart, a.count[0], i);
+    return a.cell_off[a.sid[j]] + (i - a.cstart[j]);
+}
+
+__device__ __forceinline__ int active_face(const ActiveDev &a, int i)
+{
+    const int j = active_slot(a.fstart, a.count[0], i);
+    return a.face_off[a.sid[j]] + (i - a.fstart[j]);
+}
+
+// Grid-stride sweep over the cells (faces) of the active scenarios; the body
+// sees the packed id as `c` (`f`) and may `continue`.
+#define FOR_ACTIVE_CELLS(A, c)                                                                              \
+    for (int i_ = blockIdx.x * blockDim.x + threadIdx.x, n_ = (A).count[1]; i_ < n_; i_ += gridDim.x * blockDim.x) \
+        if (const int c = active_cell((A), i_); true)
+#define FOR_ACTIVE_FACES(A, f)                                                                              \
+    for (int i_ = blockIdx.x * blockDim.x + threadIdx.x, n_ = (A).count[2]; i_ < n_; i_ += gridDim.x * blockDim.x) \
+        if (const int f = active_face((A), i_); true)
+
 struct MeshDev {
     int nc, nf, nadj, nscen;
     const int *owner, *neighbour, *bid, *offset, *faces, *signs;
@@ -77,6 +121,7 @@ struct MeshDev {
     const double *normal, *length, *area;
     const double *ls_matrix, *ls_weight, *ls_delta;
     const double *disp, *disp_unit, *disp_len, *distance;
+    ActiveDev act;           // scenarios of the current trial
 };
 
 // Rotor arrays on the device: the actuator sink and its diagnostics, and the

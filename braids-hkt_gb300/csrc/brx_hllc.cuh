@@ -89,7 +89,7 @@ template <int MAXF>
 __global__ void __launch_bounds__(128) k_hllc_cells(MeshDev m, StateDev s, HllcDev h, HCell *rec, Ctrl *ctrl)
 {
     const int nc = m.nc, nf = m.nf;
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+    FOR_ACTIVE_CELLS(m.act, c) {
         const int sid = m.cell_sid[c];
         Ctrl &ct = ctrl[sid];
         if (!ct.active || ct.done) continue;
@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(128) k_hllc_cells(MeshDev m, StateDev s, HllcD
 __global__ void __launch_bounds__(256) k_hllc_predict(MeshDev m, StateDev s, TurbDev t, HCell *rec, Ctrl *ctrl)
 {
     const int nc = m.nc;
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+    FOR_ACTIVE_CELLS(m.act, c) {
         const int sid = m.cell_sid[c];
         if (!t.hkt[sid]) continue;
         const Ctrl &ct = ctrl[sid];
@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(128) k_hllc_faces(MeshDev m, BoundaryDev b, co
                                                     int turb, Ctrl *ctrl)
 {
     const int nf = m.nf;
-    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += gridDim.x * blockDim.x) {
+    FOR_ACTIVE_FACES(m.act, f) {
         const int sid = m.face_sid[f];
         const Ctrl &ct = ctrl[sid];
         if (!ct.active || ct.done || (ct.status1 & ST_PRE)) continue;
@@ -279,8 +279,9 @@ __global__ void __launch_bounds__(256) k_hllc_budget(MeshDev m, StateDev s, Hllc
 {
     const int nc = m.nc;
     const int stride = gridDim.x * blockDim.x;
-    for (int first = blockIdx.x * blockDim.x; first < nc; first += stride) {   // warp-uniform trip count
-        const int c = first + threadIdx.x;
+    const int na = m.act.count[1];
+    for (int first = blockIdx.x * blockDim.x; first < na; first += stride) {   // warp-uniform trip count
+        const int c = first + threadIdx.x < na ? active_cell(m.act, first + threadIdx.x) : nc;
         bool have = false;
         double fr = 0.;
         int sid = 0;
@@ -323,7 +324,7 @@ __global__ void __launch_bounds__(256) k_hllc_update(MeshDev m, StateDev s, Hllc
                                                      Ctrl *ctrl)
 {
     const int nc = m.nc;
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+    FOR_ACTIVE_CELLS(m.act, c) {
         const int sid = m.cell_sid[c];
         Ctrl &ct = ctrl[sid];
         if (!ct.active || ct.done || stage1_failed(ct)) continue;

@@ -46,7 +46,7 @@ template <class F>
 __global__ void k_open_drag(MeshDev m, StateDev s, Ctrl *ctrl)
 {
     const int nc = m.nc;
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+    FOR_ACTIVE_CELLS(m.act, c) {
         const Ctrl &ct = ctrl[m.cell_sid[c]];
         if (!ct.active || ct.done) continue;
         const double *q = ct.cur ? s.q[1] : s.q[0];
@@ -354,7 +354,7 @@ template <class F, int MAXF>
 __global__ void __launch_bounds__(128) k_cells(MeshDev m, StateDev s, Ctrl *ctrl, Work w, int stage)
 {
     const int nc = m.nc, nf = m.nf, nadj = m.nadj;
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+    FOR_ACTIVE_CELLS(m.act, c) {
         Ctrl &ct = ctrl[m.cell_sid[c]];
         if (skip_stage(ct, stage)) continue;
         const double *q = stage == 1 ? s.work : s.q1;
@@ -514,7 +514,7 @@ __global__ void __launch_bounds__(128) k_faces(MeshDev m, StateDev s, BoundaryDe
                                                double *trace, const int *hkt)
 {
     const int nf = m.nf, nc = m.nc;
-    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += gridDim.x * blockDim.x) {
+    FOR_ACTIVE_FACES(m.act, f) {
         Ctrl &ct = ctrl[m.face_sid[f]];
         if (skip_stage(ct, stage)) continue;
         const double dry = ct.dry, grav = ct.grav;
@@ -675,8 +675,9 @@ __global__ void __launch_bounds__(256) k_gather(MeshDev m, StateDev s, Ctrl *ctr
     const int nc = m.nc;
     const int stride = gridDim.x * blockDim.x;
     // warp-uniform trip count: every lane reaches the warp reduction below
-    for (int first = blockIdx.x * blockDim.x; first < nc; first += stride) {
-        const int c = first + threadIdx.x;
+    const int na = m.act.count[1];
+    for (int first = blockIdx.x * blockDim.x; first < na; first += stride) {   // warp-uniform trip count
+        const int c = first + threadIdx.x < na ? active_cell(m.act, first + threadIdx.x) : nc;
         bool have = false;
         double fr = 0.;
         int sid = 0;
@@ -729,7 +730,7 @@ __global__ void __launch_bounds__(256) k_gather(MeshDev m, StateDev s, Ctrl *ctr
 __global__ void __launch_bounds__(256) k_limit(MeshDev m, StateDev s, Ctrl *ctrl, Work w, int stage)
 {
     const int nf = m.nf, nc = m.nc;
-    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += gridDim.x * blockDim.x) {
+    FOR_ACTIVE_FACES(m.act, f) {
         const Ctrl &ct = ctrl[m.face_sid[f]];
         if (skip_stage(ct, stage)) continue;
         const double *q = stage == 1 ? s.work : s.q1;
@@ -757,7 +758,7 @@ __global__ void __launch_bounds__(256) k_update(MeshDev m, StateDev s, Ctrl *ctr
                                                 double *rate_out, TurbDev t, int turb)
 {
     const int nc = m.nc;
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+    FOR_ACTIVE_CELLS(m.act, c) {
         const int sid = m.cell_sid[c];
         Ctrl &ct = ctrl[sid];
         if (skip_stage(ct, stage)) continue;
@@ -806,11 +807,57 @@ __device__ __forceinline__ void set_trial(Ctrl &c)
     c.roughf = float(c.roughness_value); c.cfl1 = 0;
 }
 
-__global__ void k_control(Ctrl *ctrl, int nscen)
+// The active set of the next trial from the control blocks: warp 0 scans the
+// scenarios 32 at a time (ballot for the ranks, shuffle scans for the cell
+// and face prefixes), ascending scenario order.
+__device__ void active_rebuild(const Ctrl *ctrl, int nscen, const ActiveDev &a)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nscen) return;
-    Ctrl &c = ctrl[i];
+    if (threadIdx.x >= 32) return;
+    const int lane = threadIdx.x;
+    int ns = 0, ncell = 0, nface = 0;
+    for (int base = 0; base < nscen; base += 32) {
+        const int i = base + lane;
+        const bool on = i < nscen && ctrl[i].active && !ctrl[i].done;
+        const int cells = on ? a.cell_off[i + 1] - a.cell_off[i] : 0;
+        const int faces = on ? a.face_off[i + 1] - a.face_off[i] : 0;
+        const unsigned mask = __ballot_sync(0xffffffffu, on);
+        int cs = cells, fs = faces;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int x = __shfl_up_sync(0xffffffffu, cs, d), y = __shfl_up_sync(0xffffffffu, fs, d);
+            if (lane >= d) { cs += x; fs += y; }
+        }
+        if (on) {
+            const int r = ns + __popc(mask & ((1u << lane) - 1u));
+            a.sid[r] = i;
+            a.cstart[r] = ncell + cs - cells;
+            a.fstart[r] = nface + fs - faces;
+        }
+        ns += __popc(mask);
+        ncell += __shfl_sync(0xffffffffu, cs, 31);
+        nface += __shfl_sync(0xffffffffu, fs, 31);
+    }
+    if (lane == 0) {
+        a.cstart[ns] = ncell; a.fstart[ns] = nface;
+        a.count[0] = ns; a.count[1] = ncell; a.count[2] = nface;
+    }
+}
+
+// Active set of the first trial of an interval (after the host's control upload).
+__global__ void k_active_init(const Ctrl *ctrl, int nscen, ActiveDev a) { active_rebuild(ctrl, nscen, a); }
+
+__device__ void control_one(Ctrl &c);
+
+// Substep control of every scenario (one block), then the next trial's active set.
+__global__ void k_control(Ctrl *ctrl, int nscen, ActiveDev a)
+{
+    for (int i = threadIdx.x; i < nscen; i += blockDim.x) control_one(ctrl[i]);
+    __syncthreads();
+    active_rebuild(ctrl, nscen, a);
+}
+
+__device__ void control_one(Ctrl &c)
+{
     if (!c.active || c.done) return;
     // a rotor outside its model's domain ends the scenario (the reference raises)
     if ((c.status1 | c.status2) & ST_TURBINE) { c.failed = 4; c.done = 1; return; }

@@ -227,7 +227,7 @@ __global__ void __launch_bounds__(128, 8) km_cells(MeshDev m, StateDev s, Ctrl *
     const int nc = m.nc;
     MxRec *rec = reinterpret_cast<MxRec *>(w.rec);
     const MxPrim *P = reinterpret_cast<const MxPrim *>((stage == 1 ? g.prim[0] : g.prim[1]));
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+    FOR_ACTIVE_CELLS(m.act, c) {
         const Ctrl &ct = ctrl[m.cell_sid[c]];
         if (mx_skip(ct, stage)) continue;
         const float dry = ct.dryf;
@@ -409,7 +409,7 @@ __global__ void __launch_bounds__(128, 8) km_faces(MeshDev m, StateDev s, Bounda
     const MxRec *rec = reinterpret_cast<const MxRec *>(w.rec);
     float2 *ws = reinterpret_cast<float2 *>(w.ws);
     float4 *gf = reinterpret_cast<float4 *>(w.gf);
-    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += gridDim.x * blockDim.x) {
+    FOR_ACTIVE_FACES(m.act, f) {
         Ctrl &ct = ctrl[m.face_sid[f]];
         if (mx_skip(ct, stage)) continue;
         const float dry = ct.dryf, grav = ct.gravf;
@@ -591,8 +591,9 @@ __global__ void __launch_bounds__(256) km_gather(MeshDev m, StateDev s, Ctrl *ct
     float *rate32 = reinterpret_cast<float *>(w.rate);      // (2, nc) momentum rates
     float *theta32 = reinterpret_cast<float *>(w.theta);
     const int stride = gridDim.x * blockDim.x;
-    for (int first = blockIdx.x * blockDim.x; first < nc; first += stride) {
-        const int c = first + threadIdx.x;
+    const int na = m.act.count[1];
+    for (int first = blockIdx.x * blockDim.x; first < na; first += stride) {   // warp-uniform trip count
+        const int c = first + threadIdx.x < na ? active_cell(m.act, first + threadIdx.x) : nc;
         bool have = false;
         float fr = 0.f;
         int sid = 0;
@@ -659,7 +660,7 @@ __global__ void __launch_bounds__(256) km_limit(MeshDev m, Ctrl *ctrl, Work w, M
     const float *theta32 = reinterpret_cast<const float *>(w.theta);
     const MxPrim *P = reinterpret_cast<const MxPrim *>((stage == 1 ? g.prim[0] : g.prim[1]));
     MxLim *lim = reinterpret_cast<MxLim *>(w.lim);
-    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += gridDim.x * blockDim.x) {
+    FOR_ACTIVE_FACES(m.act, f) {
         const Ctrl &ct = ctrl[m.face_sid[f]];
         if (mx_skip(ct, stage)) continue;
         const float wf = ws[f].x;
@@ -706,7 +707,7 @@ __global__ void __launch_bounds__(256) km_update(MeshDev m, StateDev s, Ctrl *ct
     const MxLim *lim = reinterpret_cast<const MxLim *>(w.lim);
     const float *rate32 = reinterpret_cast<const float *>(w.rate);
     MxPrim *P2 = reinterpret_cast<MxPrim *>(g.prim[1]);
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+    FOR_ACTIVE_CELLS(m.act, c) {
         const int sid = m.cell_sid[c];
         Ctrl &ct = ctrl[sid];
         if (mx_skip(ct, stage)) continue;
@@ -762,7 +763,7 @@ __global__ void __launch_bounds__(256) km_open_drag(MeshDev m, StateDev s, Ctrl 
 {
     const int nc = m.nc;
     MxPrim *P1 = reinterpret_cast<MxPrim *>(g.prim[0]);
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+    FOR_ACTIVE_CELLS(m.act, c) {
         Ctrl &ct = ctrl[m.cell_sid[c]];
         if (!ct.active || ct.done) continue;
         const double *q = ct.cur ? s.q[1] : s.q[0];
@@ -778,7 +779,7 @@ __global__ void __launch_bounds__(256) km_prim(MeshDev m, StateDev s, Ctrl *ctrl
 {
     const int nc = m.nc;
     MxPrim *P1 = reinterpret_cast<MxPrim *>(g.prim[0]);
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+    FOR_ACTIVE_CELLS(m.act, c) {
         Ctrl &ct = ctrl[m.cell_sid[c]];
         if (!ct.active || ct.done) continue;
         if (!put_prim(P1, c, s.work[c], s.work[nc + c], s.work[2 * nc + c], s.z[c], ct.dry))
@@ -801,7 +802,7 @@ __global__ void __launch_bounds__(128) km_hkt_gradients(MeshDev m, Ctrl *ctrl, M
 {
     const int nc = m.nc;
     const MxPrim *P = reinterpret_cast<const MxPrim *>(stage == 1 ? g.prim[0] : g.prim[1]);
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+    FOR_ACTIVE_CELLS(m.act, c) {
         const int sid = m.cell_sid[c];
         if (!t.hkt[sid]) continue;
         const Ctrl &ct = ctrl[sid];
@@ -842,7 +843,7 @@ __global__ void __launch_bounds__(128) km_hkt_faces(MeshDev m, Ctrl *ctrl, Mixed
 {
     const int nf = m.nf, nc = m.nc;
     const MxPrim *P = reinterpret_cast<const MxPrim *>(stage == 1 ? g.prim[0] : g.prim[1]);
-    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += gridDim.x * blockDim.x) {
+    FOR_ACTIVE_FACES(m.act, f) {
         const int sid = m.face_sid[f];
         if (!t.hkt[sid]) continue;
         const Ctrl &ct = ctrl[sid];

@@ -70,7 +70,7 @@ __global__ void __launch_bounds__(256) k_hkt_gradients(MeshDev m, TurbDev t, con
                                                        Ctrl *ctrl, int stage)
 {
     const int n = m.nc;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    FOR_ACTIVE_CELLS(m.act, i) {
         const int sid = m.cell_sid[i];
         if (!t.hkt[sid]) continue;
         const Ctrl &ct = ctrl[sid];
@@ -303,7 +303,7 @@ __global__ void __launch_bounds__(128) k_hkt_faces(MeshDev m, TurbDev t, const d
                                                    Ctrl *ctrl, int stage)
 {
     const int nf = m.nf, n = m.nc;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nf; i += gridDim.x * blockDim.x) {
+    FOR_ACTIVE_FACES(m.act, i) {
         const int sid = m.face_sid[i];
         if (!t.hkt[sid]) continue;
         const Ctrl &ct = ctrl[sid];
