@@ -411,7 +411,7 @@ def main():
         pool = [i for i, c in enumerate(cases) if c.get("turbines")] or list(range(len(cases)))
         order = sorted(pool, key=lambda i: cases[i]["mesh"].nc)
         pick = [int(order[0]), int(order[len(order) // 2]), int(order[-1])][:args.plain]
-        p_updates, p_ms, errs, perr = 0, 0.0, [], []
+        p_updates, p_ms, errs, perr, qerrs, merrs = 0, 0.0, [], [], [], []
         rotor_first = {}
         if solver.rotors is not None:
             for k, sid in enumerate(solver.rotors["scenario"]):
@@ -453,10 +453,17 @@ def main():
                 if k >= args.warmup:
                     p_ms += e0.elapsed_time(e1)
                     p_updates += int(d["hydraulic_substeps"]) * int(one.nc)
-            h64 = one.q[0].cpu().numpy()
-            hmx = batch_state[0, off[i]:off[i + 1]]
+            q64 = one.q.cpu().numpy()
+            h64 = q64[0]
+            qmx = batch_state[:, off[i]:off[i + 1]]
+            hmx = qmx[0]
             rel = np.abs(hmx - h64) / np.maximum(h64, 1e-3)
             errs.append((float(rel.max()), float(np.percentile(rel, 99))))
+            # unit discharge (hu, hv) against the scenario's largest unit discharge
+            qscale = max(float(np.abs(q64[1:]).max()), 1e-12)
+            qerrs.append(float(np.abs(qmx[1:] - q64[1:]).max() / qscale))
+            m64, mmx = float(np.sum(h64 * cases[i]["mesh"].area)), float(np.sum(hmx * cases[i]["mesh"].area))
+            merrs.append(abs(mmx - m64) / m64)
             if one.rotors is not None and i in rotor_first:
                 import braids_hkt_gb300.turbines as TB
                 col = TB.DIAG_FIELDS.index("useful_power_per_density_m5_s3")
@@ -474,6 +481,8 @@ def main():
                                      "spatial evaluation per substep), the same intervals and CFL; speed-up = "
                                      "f-wave FP64 device time / HLLC device time for the same simulated time"}
         cfg["accuracy_vs_fp64"] = {"depth_rel_max": max(e[0] for e in errs), "depth_rel_p99": max(e[1] for e in errs),
+                                   "unit_discharge_rel_max": max(qerrs),
+                                   "volume_rel_max": max(merrs),
                                    "scenarios": pick, "after_sim_s": nsteps * outer,
                                    "stated_tolerance": 1e-4,
                                    "rotor_power_rel_max": max(perr) if perr else None,

@@ -95,6 +95,7 @@ struct brx_solver {
     bool has_exner = false;
     int *d_cell_off = nullptr, *d_face_off = nullptr;
     double *d_exdt = nullptr;
+    double *d_totals = nullptr;      // (nscen, 2) brx_totals output
     int method = BRX_METHOD_FWAVE;   // hydraulic method of the substep graph
     HllcDev hllc{};                  // HLLC stencil (valid when hllc_ready)
     bool hllc_ready = false;
@@ -1234,6 +1235,21 @@ extern "C" int brx_advance_poll(brx_solver *s, int *done, brx_advance_stats *sta
     s->pending = false;
     *done = 1;
     return finish_interval(s, stats);
+}
+
+extern "C" int brx_totals(brx_solver *s, double *out)
+{
+    TRY(ensure_ready(s));
+    if (!out) return fail(BRX_ERR_ARGUMENT, "null output");
+    double *d = nullptr;
+    if (!s->d_totals) TRY(s->alloc(&s->d_totals, 2 * (size_t)s->nscen));
+    d = s->d_totals;
+    k_totals<<<s->nscen, 256, 0, s->stream>>>(s->mesh, s->state.q[0], s->state.z, s->d_ctrl, d);
+    s->launches++;
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, d, sizeof(double) * 2 * s->nscen, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return BRX_OK;
 }
 
 // Device bytes held by the solver (its allocations).

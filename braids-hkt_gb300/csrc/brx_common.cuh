@@ -96,20 +96,34 @@ __device__ __forceinline__ int active_cell(const ActiveDev &a, int i)
     return a.cell_off[a.sid[j]] + (i - a.cstart[j]);
 }
 
-__device__ __forceinline__ int active_face(const ActiveDev &a, int i)
+// Warp-cooperative form for sweeps whose 32 lanes take 32 consecutive packed
+// indices w .. w+31 (w warp-uniform): lane 0 searches the prefix once and
+// every lane steps past at most the few scenario starts inside the warp's
+// span. Every lane of the warp must call it. -1 for an index at or past n.
+__device__ __forceinline__ int active_index_warp(const int *start, const int *sid, const int *off, int ns, int w,
+                                                 int n)
 {
-    const int j = active_slot(a.fstart, a.count[0], i);
-    return a.face_off[a.sid[j]] + (i - a.fstart[j]);
+    const int lane = threadIdx.x & 31;
+    int j = lane == 0 ? active_slot(start, ns, w) : 0;
+    j = __shfl_sync(0xffffffffu, j, 0);
+    const int i = w + lane;
+    if (i >= n) return -1;
+    while (j + 1 < ns && start[j + 1] <= i) ++j;
+    return off[sid[j]] + (i - start[j]);
 }
 
 // Grid-stride sweep over the cells (faces) of the active scenarios; the body
-// sees the packed id as `c` (`f`) and may `continue`.
+// sees the packed id as `c` (`f`) and may `continue` (never `break` or
+// `return`: the trip count is warp-uniform and the index search is a warp
+// collective). Blocks are multiples of 32 threads.
 #define FOR_ACTIVE_CELLS(A, c)                                                                              \
-    for (int i_ = blockIdx.x * blockDim.x + threadIdx.x, n_ = (A).count[1]; i_ < n_; i_ += gridDim.x * blockDim.x) \
-        if (const int c = active_cell((A), i_); true)
+    for (int w_ = blockIdx.x * blockDim.x + (threadIdx.x & ~31), n_ = (A).count[1]; w_ < n_;                \
+         w_ += gridDim.x * blockDim.x)                                                                      \
+        if (const int c = active_index_warp((A).cstart, (A).sid, (A).cell_off, (A).count[0], w_, n_); c >= 0)
 #define FOR_ACTIVE_FACES(A, f)                                                                              \
-    for (int i_ = blockIdx.x * blockDim.x + threadIdx.x, n_ = (A).count[2]; i_ < n_; i_ += gridDim.x * blockDim.x) \
-        if (const int f = active_face((A), i_); true)
+    for (int w_ = blockIdx.x * blockDim.x + (threadIdx.x & ~31), n_ = (A).count[2]; w_ < n_;                \
+         w_ += gridDim.x * blockDim.x)                                                                      \
+        if (const int f = active_index_warp((A).fstart, (A).sid, (A).face_off, (A).count[0], w_, n_); f >= 0)
 
 struct MeshDev {
     int nc, nf, nadj, nscen;

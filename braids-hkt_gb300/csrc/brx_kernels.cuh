@@ -677,7 +677,9 @@ __global__ void __launch_bounds__(256) k_gather(MeshDev m, StateDev s, Ctrl *ctr
     // warp-uniform trip count: every lane reaches the warp reduction below
     const int na = m.act.count[1];
     for (int first = blockIdx.x * blockDim.x; first < na; first += stride) {   // warp-uniform trip count
-        const int c = first + threadIdx.x < na ? active_cell(m.act, first + threadIdx.x) : nc;
+        const int ci_ = active_index_warp(m.act.cstart, m.act.sid, m.act.cell_off, m.act.count[0],
+                                          first + (int)(threadIdx.x & ~31u), na);
+        const int c = ci_ >= 0 ? ci_ : nc;
         bool have = false;
         double fr = 0.;
         int sid = 0;
@@ -901,6 +903,48 @@ __global__ void k_water_out(MeshDev m, Work w, double *water)
 }
 
 // Make the caller-bound buffer q[0] hold every scenario's accepted state.
+// Compensated per-scenario totals of a state: water volume sum(A h) and
+// mechanical energy per unit density sum(A (|hu|^2 / (2h) + g h^2 / 2 + g h z))
+// (kinetic only where h > dry). Neumaier summation: each thread a strided
+// slice, then thread 0 combines the 256 partial pairs in thread order, so the
+// result is the same on every run.
+__device__ __forceinline__ void neumaier_add(double &sum, double &comp, double v)
+{
+    const double t = sum + v;
+    if (fabs(sum) >= fabs(v)) comp += (sum - t) + v;
+    else comp += (v - t) + sum;
+    sum = t;
+}
+
+__global__ void __launch_bounds__(256) k_totals(MeshDev m, const double *q, const double *z, const Ctrl *ctrl,
+                                                double *out)
+{
+    __shared__ double part[256][4];
+    const int sid = blockIdx.x, nc = m.nc;
+    const int c0 = m.act.cell_off[sid], c1 = m.act.cell_off[sid + 1];
+    const double g = ctrl[sid].grav, dry = ctrl[sid].dry;
+    double ms = 0., mc = 0., es = 0., ec = 0.;
+    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
+        const double h = q[c], a = m.area[c];
+        neumaier_add(ms, mc, a * h);
+        double e = .5 * g * h * h + g * h * z[c];
+        if (h > dry) e += .5 * (q[nc + c] * q[nc + c] + q[2 * nc + c] * q[2 * nc + c]) / h;
+        neumaier_add(es, ec, a * e);
+    }
+    part[threadIdx.x][0] = ms; part[threadIdx.x][1] = mc;
+    part[threadIdx.x][2] = es; part[threadIdx.x][3] = ec;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s0 = 0., c0s = 0., s1 = 0., c1s = 0.;
+        for (int t = 0; t < (int)blockDim.x; ++t) {
+            neumaier_add(s0, c0s, part[t][0]); c0s += part[t][1];
+            neumaier_add(s1, c1s, part[t][2]); c1s += part[t][3];
+        }
+        out[2 * sid] = s0 + c0s;
+        out[2 * sid + 1] = s1 + c1s;
+    }
+}
+
 __global__ void k_commit(MeshDev m, StateDev s, Ctrl *ctrl)
 {
     const int nc = m.nc;

@@ -375,6 +375,14 @@ class RiverSolver:
         a, b = self.packed["cell_offset"][scenario], self.packed["cell_offset"][scenario + 1]
         return q[:, a:b]
 
+    def totals(self):
+        """(nscen, 2) compensated water volume [m3] and mechanical energy per unit density
+        [m5/s2] of the current state, summed on the device in a fixed order."""
+        self.torch.cuda.current_stream().synchronize()
+        out = np.zeros((self.nscen, 2))
+        check(self.lib.brx_totals(self.h, _ptr(out)))
+        return out[0] if self.single else out
+
     def mass(self):
         """Water volume per scenario (Kahan-compensated FP64 sum on the host)."""
         q = self.q[0].cpu().numpy()

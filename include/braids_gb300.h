@@ -210,6 +210,14 @@ int brx_exner(brx_solver *s, const double *dt, double *stats);
 int brx_advance_start(brx_solver *s, const double *dt, const double *time);
 int brx_advance_poll(brx_solver *s, int *done, brx_advance_stats *stats);
 
+/* Compensated totals of the bound state per scenario (out: nscen x 2, host):
+ * water volume sum(A h) [m3] and mechanical energy per unit density
+ * sum(A (|hu|^2 / 2h + g h^2 / 2 + g h z)) [m5/s2], Neumaier-summed in a fixed
+ * order (the same value on every run). The reference checks its water budget
+ * on the host (shoreline_solver.py:345-372); this gives the device-resident
+ * batch the same totals without copying the state. */
+int brx_totals(brx_solver *s, double *out);
+
 /* Device bytes the solver holds (for admission against a memory budget). */
 long long brx_solver_bytes(const brx_solver *s);
 
