@@ -1241,10 +1241,13 @@ extern "C" int brx_totals(brx_solver *s, double *out)
 {
     TRY(ensure_ready(s));
     if (!out) return fail(BRX_ERR_ARGUMENT, "null output");
-    double *d = nullptr;
-    if (!s->d_totals) TRY(s->alloc(&s->d_totals, 2 * (size_t)s->nscen));
-    d = s->d_totals;
-    k_totals<<<s->nscen, 256, 0, s->stream>>>(s->mesh, s->state.q[0], s->state.z, s->d_ctrl, d);
+    if (s->pending) return fail(BRX_ERR_STATE, "an asynchronous interval is in flight");
+    if (!s->d_totals) TRY(s->alloc(&s->d_totals, 4 * (size_t)s->nscen));
+    double *d = s->d_totals, *gd = s->d_totals + 2 * (size_t)s->nscen;
+    std::vector<double> h_gd(2 * (size_t)s->nscen);
+    for (int i = 0; i < s->nscen; ++i) { h_gd[2 * i] = s->h_ctrl[i].grav; h_gd[2 * i + 1] = s->h_ctrl[i].dry; }
+    CK(cudaMemcpyAsync(gd, h_gd.data(), sizeof(double) * h_gd.size(), cudaMemcpyHostToDevice, s->stream));
+    k_totals<<<s->nscen, 256, 0, s->stream>>>(s->mesh, s->state.q[0], s->state.z, gd, d);
     s->launches++;
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(out, d, sizeof(double) * 2 * s->nscen, cudaMemcpyDeviceToHost, s->stream));

@@ -916,13 +916,13 @@ __device__ __forceinline__ void neumaier_add(double &sum, double &comp, double v
     sum = t;
 }
 
-__global__ void __launch_bounds__(256) k_totals(MeshDev m, const double *q, const double *z, const Ctrl *ctrl,
+__global__ void __launch_bounds__(256) k_totals(MeshDev m, const double *q, const double *z, const double *gd,
                                                 double *out)
 {
     __shared__ double part[256][4];
     const int sid = blockIdx.x, nc = m.nc;
     const int c0 = m.act.cell_off[sid], c1 = m.act.cell_off[sid + 1];
-    const double g = ctrl[sid].grav, dry = ctrl[sid].dry;
+    const double g = gd[2 * sid], dry = gd[2 * sid + 1];     // the scenario's gravity and dry depth
     double ms = 0., mc = 0., es = 0., ec = 0.;
     for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
         const double h = q[c], a = m.area[c];

@@ -251,6 +251,32 @@ def lake_at_rest(length=80.0, width=40.0, spacing=4.0, seed=11, islands=True):
                 controls=controls(0.9, 0.03), name="lake_at_rest")
 
 
+def hydraulic_jump(length=60.0, width=3.0, spacing=0.5, seed=17, froude=2.5, h1=0.4, cfl=0.9):
+    """A stationary hydraulic jump on a flat frictionless channel.
+
+    Supercritical inflow of depth h1 at Froude number `froude` through a
+    mode-9 inlet (prescribed water line, uniform normal speed Q / (h W)); the
+    outlet stage at the conjugate depth h2 = h1 (sqrt(1 + 8 Fr^2) - 1) / 2
+    (Belanger); the initial state is the two conjugate states either side of
+    mid-channel with the unit discharge q = h1 u1 throughout.
+    """
+    mesh = M.channel_mesh(length, width, spacing, 0.2, seed)
+    g = 9.81
+    u1 = froude * np.sqrt(g * h1)
+    qx = h1 * u1
+    h2 = 0.5 * h1 * (np.sqrt(1.0 + 8.0 * froude ** 2) - 1.0)
+    x = mesh.xy[0]
+    h = np.where(x < 0.5 * length, h1, h2)
+    q = np.ascontiguousarray(np.stack((h, np.full_like(h, qx), np.zeros_like(h))))
+    ctl = controls(cfl, 0.03)
+    ctl["roughness_mode"] = 1
+    ctl["roughness_value"] = 1e12          # Chezy -> infinity: frictionless
+    forcing = np.array([[qx * width, 0.0], [h1, h2]])
+    return dict(mesh=mesh, z=np.zeros(mesh.nc), q=q, seg_mode=np.array([9, 2], np.int32),
+                stage_policy=np.zeros(2, np.int32), forcing=forcing, exterior_bed=np.zeros(mesh.nf),
+                controls=ctl, name="hydraulic_jump", jump=dict(h1=h1, h2=h2, q=qx, froude=froude))
+
+
 def dam_break(length=200.0, width=8.0, spacing=2.0, seed=13, h_left=2.0, h_right=0.0):
     """Dam break on a flat frictionless bed; h_right = 0 gives the dry-bed (Ritter) case."""
     mesh = M.channel_mesh(length, width, spacing, 0.4, seed)

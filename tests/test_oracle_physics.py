@@ -4,6 +4,7 @@ analytic solutions), the same cases later run through the CUDA path.
   lake at rest with emerged islands        reconstruction_oracle.py:30-31 ("cutcell_lake")
   water budget per step                    shoreline_solver.py:29-39, 354-360
   dry-bed dam break (Ritter)               reconstruction_oracle.py:30-31 ("dry_dam_break")
+  stationary hydraulic jump (Belanger)     reconstruction_oracle.py:30-31 ("hydraulic_jump")
 """
 import numpy as np
 
@@ -73,3 +74,29 @@ def test_dry_dam_break_matches_ritter():
     assert err.mean() < 0.03          # first-order-limited scheme on a 2 m mesh
     front = x[(q[0] > 1e-3)].max()
     assert abs(front - (100.0 + 2 * np.sqrt(9.81 * 2.0) * t)) < 12.0
+
+
+def test_hydraulic_jump_holds_conjugate_depths():
+    """Supercritical inflow (Fr 2.5, 0.4 m) against the conjugate outlet stage: after 20 s
+    the jump stays near mid-channel, the depths either side are Belanger's conjugate pair,
+    the unit discharge is uniform and the momentum function q^2/h + g h^2/2 is continuous."""
+    case = S.hydraulic_jump()
+    j = case["jump"]
+    o = Oracle(case, threads=2)
+    q = case["q"].copy()
+    for k in range(4):
+        st, _, _ = o.advance(q, 5.0, 5.0 * k)
+        assert st == 0
+    x, y = case["mesh"].xy
+    up, dn = (x > 5) & (x < 20), (x > 40) & (x < 55)
+    h_up, h_dn = q[0][up].mean(), q[0][dn].mean()
+    assert abs(h_up - j["h1"]) <= 0.01 * j["h1"]
+    assert abs(h_dn - j["h2"]) <= 0.02 * j["h2"]
+    for region in (up, dn):
+        assert abs(q[1][region].mean() - j["q"]) <= 0.01 * j["q"]
+    momentum = lambda h, qq: qq * qq / h + 9.81 * h * h / 2
+    m_up, m_dn = momentum(h_up, q[1][up].mean()), momentum(h_dn, q[1][dn].mean())
+    assert abs(m_up - m_dn) <= 0.02 * m_up
+    band = np.abs(y - 1.5) < 1.0
+    x_jump = x[band & (q[0] > 0.5 * (j["h1"] + j["h2"]))].min()
+    assert 25.0 < x_jump < 35.0
