@@ -331,7 +331,7 @@ extern "C" int brx_solver_create(int nscen, const int *cell_offset, const int *f
         TRY(s->upload(&s->d_cell_off, s->cell_offset.data(), s->cell_offset.size()));
         TRY(s->upload(&s->d_face_off, s->face_offset.data(), s->face_offset.size()));
         ActiveDev &a = s->mesh.act;
-        TRY(s->alloc(&a.count, 3)); TRY(s->alloc(&a.sid, nscen));
+        TRY(s->alloc(&a.count, 3)); TRY(s->alloc(&a.cdelta, nscen)); TRY(s->alloc(&a.fdelta, nscen));
         TRY(s->alloc(&a.cstart, nscen + 1)); TRY(s->alloc(&a.fstart, nscen + 1));
         CK(cudaMemset(a.count, 0, sizeof(int) * 3));
         a.cell_off = s->d_cell_off; a.face_off = s->d_face_off;
@@ -1479,14 +1479,14 @@ static int noalloc_address(unsigned char **out)
     return BRX_OK;
 }
 
-// The control block and the one-scenario active set: count {1, nc, nf}, sid
-// {0}, cell / face prefixes {0, nc} / {0, nf}, packed ranges the same.
+// The control block and the one-scenario active set: one run {count 1, nc,
+// nf}, cell run {start 0, nc; delta 0}, face run {0, nf; 0}, packed ranges
+// {0, nc} and {0, nf}.
 __global__ void k_noalloc_ctrl(Ctrl *ctrl, Ctrl init, int *act, int nc, int nf)
 {
     *ctrl = init;
-    const int v[11] = {1, nc, nf, 0, 0, nc, 0, nf, 0, nc, 0};
-    for (int i = 0; i < 11; ++i) act[i] = v[i];
-    act[11] = nf;
+    const int v[13] = {1, nc, nf, 0, nc, 0, 0, nf, 0, 0, nc, 0, nf};
+    for (int i = 0; i < 13; ++i) act[i] = v[i];
 }
 
 // Derived per-cell/per-face tables of a closed single-scenario mesh, and a
@@ -1557,9 +1557,9 @@ extern "C" int brx_rate_noalloc(int nc, int nf, int nadj, const int *owner, cons
     m.normal = normal; m.length = length; m.area = area; m.ls_matrix = ls_matrix; m.ls_weight = ls_weight;
     m.ls_delta = ls_delta; m.disp = displacement; m.disp_unit = disp_unit; m.disp_len = displacement_length;
     m.distance = distance;
-    int *act = (int *)(base + NA_ACT);   // count[3] sid[1] cstart[2] fstart[2] cell_off[2] face_off[2]
-    m.act.count = act; m.act.sid = act + 3; m.act.cstart = act + 4; m.act.fstart = act + 6;
-    m.act.cell_off = act + 8; m.act.face_off = act + 10;
+    int *act = (int *)(base + NA_ACT);   // count[3] cstart[2] cdelta[1] fstart[2] fdelta[1] cell_off[2] face_off[2]
+    m.act.count = act; m.act.cstart = act + 3; m.act.cdelta = act + 5; m.act.fstart = act + 6;
+    m.act.fdelta = act + 8; m.act.cell_off = act + 9; m.act.face_off = act + 11;
     StateDev sd{};
     sd.q[0] = const_cast<double *>(q);
     sd.work = const_cast<double *>(q);    // the residual reads its stage state here and never writes it

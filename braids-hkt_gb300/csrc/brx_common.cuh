@@ -73,9 +73,9 @@ struct Ctrl {
 // host sets it at the start of an interval; k_control rebuilds it after every
 // trial (ascending scenario order).
 struct ActiveDev {
-    int *count;              // [0] scenarios, [1] cells, [2] faces
-    int *sid;                // (nscen) active scenario ids
-    int *cstart, *fstart;    // (nscen+1) prefix sums of their cell and face counts
+    int *count;              // [0] runs, [1] cells, [2] faces
+    int *cstart, *cdelta;    // (nscen+1), (nscen): per run, its first packed active cell index, and cell id - index
+    int *fstart, *fdelta;    // the same for faces
     const int *cell_off, *face_off;   // (nscen+1) packed ranges of every scenario
 };
 
@@ -90,40 +90,27 @@ __device__ __forceinline__ int active_slot(const int *start, int n, int i)
     return lo;
 }
 
+// Cell (face) id of the i-th active cell (face): runs of consecutive active
+// scenarios are contiguous id ranges, so the map is i + delta of i's run (a
+// fully active batch is one run: the identity).
 __device__ __forceinline__ int active_cell(const ActiveDev &a, int i)
 {
-    const int j = active_slot(a.cstart, a.count[0], i);
-    return a.cell_off[a.sid[j]] + (i - a.cstart[j]);
+    return i + a.cdelta[active_slot(a.cstart, a.count[0], i)];
 }
 
-// Warp-cooperative form for sweeps whose 32 lanes take 32 consecutive packed
-// indices w .. w+31 (w warp-uniform): lane 0 searches the prefix once and
-// every lane steps past at most the few scenario starts inside the warp's
-// span. Every lane of the warp must call it. -1 for an index at or past n.
-__device__ __forceinline__ int active_index_warp(const int *start, const int *sid, const int *off, int ns, int w,
-                                                 int n)
+__device__ __forceinline__ int active_face(const ActiveDev &a, int i)
 {
-    const int lane = threadIdx.x & 31;
-    int j = lane == 0 ? active_slot(start, ns, w) : 0;
-    j = __shfl_sync(0xffffffffu, j, 0);
-    const int i = w + lane;
-    if (i >= n) return -1;
-    while (j + 1 < ns && start[j + 1] <= i) ++j;
-    return off[sid[j]] + (i - start[j]);
+    return i + a.fdelta[active_slot(a.fstart, a.count[0], i)];
 }
 
 // Grid-stride sweep over the cells (faces) of the active scenarios; the body
-// sees the packed id as `c` (`f`) and may `continue` (never `break` or
-// `return`: the trip count is warp-uniform and the index search is a warp
-// collective). Blocks are multiples of 32 threads.
+// sees the packed id as `c` (`f`) and may `continue`.
 #define FOR_ACTIVE_CELLS(A, c)                                                                              \
-    for (int w_ = blockIdx.x * blockDim.x + (threadIdx.x & ~31), n_ = (A).count[1]; w_ < n_;                \
-         w_ += gridDim.x * blockDim.x)                                                                      \
-        if (const int c = active_index_warp((A).cstart, (A).sid, (A).cell_off, (A).count[0], w_, n_); c >= 0)
+    for (int i_ = blockIdx.x * blockDim.x + threadIdx.x, n_ = (A).count[1]; i_ < n_; i_ += gridDim.x * blockDim.x) \
+        if (const int c = active_cell((A), i_); true)
 #define FOR_ACTIVE_FACES(A, f)                                                                              \
-    for (int w_ = blockIdx.x * blockDim.x + (threadIdx.x & ~31), n_ = (A).count[2]; w_ < n_;                \
-         w_ += gridDim.x * blockDim.x)                                                                      \
-        if (const int f = active_index_warp((A).fstart, (A).sid, (A).face_off, (A).count[0], w_, n_); f >= 0)
+    for (int i_ = blockIdx.x * blockDim.x + threadIdx.x, n_ = (A).count[2]; i_ < n_; i_ += gridDim.x * blockDim.x) \
+        if (const int f = active_face((A), i_); true)
 
 struct MeshDev {
     int nc, nf, nadj, nscen;

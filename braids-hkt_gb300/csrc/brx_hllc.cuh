@@ -281,9 +281,7 @@ __global__ void __launch_bounds__(256) k_hllc_budget(MeshDev m, StateDev s, Hllc
     const int stride = gridDim.x * blockDim.x;
     const int na = m.act.count[1];
     for (int first = blockIdx.x * blockDim.x; first < na; first += stride) {   // warp-uniform trip count
-        const int ci_ = active_index_warp(m.act.cstart, m.act.sid, m.act.cell_off, m.act.count[0],
-                                          first + (int)(threadIdx.x & ~31u), na);
-        const int c = ci_ >= 0 ? ci_ : nc;
+        const int c = first + (int)threadIdx.x < na ? active_cell(m.act, first + threadIdx.x) : nc;
         bool have = false;
         double fr = 0.;
         int sid = 0;

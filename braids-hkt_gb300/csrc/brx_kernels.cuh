@@ -677,9 +677,7 @@ __global__ void __launch_bounds__(256) k_gather(MeshDev m, StateDev s, Ctrl *ctr
     // warp-uniform trip count: every lane reaches the warp reduction below
     const int na = m.act.count[1];
     for (int first = blockIdx.x * blockDim.x; first < na; first += stride) {   // warp-uniform trip count
-        const int ci_ = active_index_warp(m.act.cstart, m.act.sid, m.act.cell_off, m.act.count[0],
-                                          first + (int)(threadIdx.x & ~31u), na);
-        const int c = ci_ >= 0 ? ci_ : nc;
+        const int c = first + (int)threadIdx.x < na ? active_cell(m.act, first + threadIdx.x) : nc;
         bool have = false;
         double fr = 0.;
         int sid = 0;
@@ -809,39 +807,45 @@ __device__ __forceinline__ void set_trial(Ctrl &c)
     c.roughf = float(c.roughness_value); c.cfl1 = 0;
 }
 
-// The active set of the next trial from the control blocks: warp 0 scans the
-// scenarios 32 at a time (ballot for the ranks, shuffle scans for the cell
-// and face prefixes), ascending scenario order.
+// The active set of the next trial from the control blocks, as runs of
+// consecutive active scenarios: warp 0 scans the scenarios 32 at a time
+// (ballots for run starts, shuffle scans for the cell and face prefixes).
 __device__ void active_rebuild(const Ctrl *ctrl, int nscen, const ActiveDev &a)
 {
     if (threadIdx.x >= 32) return;
+    const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x;
-    int ns = 0, ncell = 0, nface = 0;
+    int nrun = 0, ncell = 0, nface = 0;
+    bool carry = false;                       // the previous chunk's last scenario was active
     for (int base = 0; base < nscen; base += 32) {
         const int i = base + lane;
         const bool on = i < nscen && ctrl[i].active && !ctrl[i].done;
+        bool prev = __shfl_up_sync(full, on, 1);
+        if (lane == 0) prev = carry;
+        const bool first = on && !prev;
         const int cells = on ? a.cell_off[i + 1] - a.cell_off[i] : 0;
         const int faces = on ? a.face_off[i + 1] - a.face_off[i] : 0;
-        const unsigned mask = __ballot_sync(0xffffffffu, on);
+        const unsigned starts = __ballot_sync(full, first);
         int cs = cells, fs = faces;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
-            const int x = __shfl_up_sync(0xffffffffu, cs, d), y = __shfl_up_sync(0xffffffffu, fs, d);
+            const int x = __shfl_up_sync(full, cs, d), y = __shfl_up_sync(full, fs, d);
             if (lane >= d) { cs += x; fs += y; }
         }
-        if (on) {
-            const int r = ns + __popc(mask & ((1u << lane) - 1u));
-            a.sid[r] = i;
-            a.cstart[r] = ncell + cs - cells;
-            a.fstart[r] = nface + fs - faces;
+        if (first) {
+            const int r = nrun + __popc(starts & ((1u << lane) - 1u));
+            const int c0 = ncell + cs - cells, f0 = nface + fs - faces;
+            a.cstart[r] = c0; a.cdelta[r] = a.cell_off[i] - c0;
+            a.fstart[r] = f0; a.fdelta[r] = a.face_off[i] - f0;
         }
-        ns += __popc(mask);
-        ncell += __shfl_sync(0xffffffffu, cs, 31);
-        nface += __shfl_sync(0xffffffffu, fs, 31);
+        nrun += __popc(starts);
+        ncell += __shfl_sync(full, cs, 31);
+        nface += __shfl_sync(full, fs, 31);
+        carry = __shfl_sync(full, on, 31);
     }
     if (lane == 0) {
-        a.cstart[ns] = ncell; a.fstart[ns] = nface;
-        a.count[0] = ns; a.count[1] = ncell; a.count[2] = nface;
+        a.cstart[nrun] = ncell; a.fstart[nrun] = nface;
+        a.count[0] = nrun; a.count[1] = ncell; a.count[2] = nface;
     }
 }
 

@@ -593,9 +593,7 @@ __global__ void __launch_bounds__(256) km_gather(MeshDev m, StateDev s, Ctrl *ct
     const int stride = gridDim.x * blockDim.x;
     const int na = m.act.count[1];
     for (int first = blockIdx.x * blockDim.x; first < na; first += stride) {   // warp-uniform trip count
-        const int ci_ = active_index_warp(m.act.cstart, m.act.sid, m.act.cell_off, m.act.count[0],
-                                          first + (int)(threadIdx.x & ~31u), na);
-        const int c = ci_ >= 0 ? ci_ : nc;
+        const int c = first + (int)threadIdx.x < na ? active_cell(m.act, first + threadIdx.x) : nc;
         bool have = false;
         float fr = 0.f;
         int sid = 0;
