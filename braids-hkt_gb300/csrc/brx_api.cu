@@ -1041,7 +1041,7 @@ static void enqueue_stage(brx_solver *s, int stage, double *rate_out)
     s->launches += launch_kernel(s, K_CELLS, stage, nullptr);
     if (fork) cudaStreamWaitEvent(s->stream, s->join, 0);
     for (int kind : {(int)K_FACES, (int)K_GATHER, (int)K_LIMIT, (int)K_TURB, (int)K_UPDATE})
-        s->launches += launch_kernel(s, kind, stage, kind == K_UPDATE ? rate_out : nullptr);
+        s->launches += launch_kernel(s, kind, stage, kind == K_UPDATE || kind == K_LIMIT ? rate_out : nullptr);
 }
 
 // HLLC / MUSCL-Hancock kernels of one substep (kinds of the profile), on st.
