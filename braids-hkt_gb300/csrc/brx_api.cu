@@ -52,7 +52,7 @@ struct brx_solver {
     int device = 0, sms = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t side = nullptr;       // boundary CTAs run here, concurrent with the cell sweep
-    cudaEvent_t fork = nullptr, join = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr, join2 = nullptr;   // side-stream fork / joins of a stage
     std::vector<void *> allocations;
     size_t bytes = 0;                // device bytes held (sum of allocations)
     cudaEvent_t polled = nullptr;    // asynchronous advance: control mirror copied back
@@ -219,6 +219,7 @@ extern "C" int brx_solver_create(int nscen, const int *cell_offset, const int *f
         CK(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
         CK(cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&s->join, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&s->join2, cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&s->polled, cudaEventDisableTiming));
         s->cell_offset.assign(cell_offset, cell_offset + nscen + 1);
         s->face_offset.assign(face_offset, face_offset + nscen + 1);
@@ -431,6 +432,7 @@ extern "C" int brx_solver_destroy(brx_solver *s)
     if (s->fork) cudaEventDestroy(s->fork);
     if (s->polled) cudaEventDestroy(s->polled);
     if (s->join) cudaEventDestroy(s->join);
+    if (s->join2) cudaEventDestroy(s->join2);
     if (s->side) cudaStreamDestroy(s->side);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
@@ -974,7 +976,11 @@ static inline int sgrid(const brx_solver *s, int kind, int n)
 }
 #define SSHAPE(kind_, n_) sgrid(s, kind_, n_), s->shape[kind_].block
 
-static int launch_turbines(brx_solver *s, int stage, cudaStream_t st)
+// part: 1 the cell terms (wet gradients, rotor sample, actuator sink), which
+// need only the stage state; 2 the face terms (balanced pressure, ambient
+// stress), which also need the face sweep's traces; 3 both, in order.
+enum { TURB_CELLS = 1, TURB_FACES = 2, TURB_ALL = 3 };
+static int launch_turbines(brx_solver *s, int stage, cudaStream_t st, int part = TURB_ALL)
 {
     if (!s->has_turb) return 0;
     const double *q = stage == 1 ? s->state.work : s->state.q1;
@@ -983,13 +989,26 @@ static int launch_turbines(brx_solver *s, int stage, cudaStream_t st)
     // the wet gradients feed only the face terms (balanced pressure, ambient
     // stress); the HLLC owner without ambient stress has neither
     const bool faces = t.balanced || s->any_stress;
-    if (mixed) mixed_kernel(make_launch(s, st), K_HKT_GRAD, stage, nullptr);
-    else if (faces) k_hkt_gradients<<<SSHAPE(K_HKT_GRAD, s->nc), 0, st>>>(s->mesh, t, q, s->state.z, s->d_ctrl, stage);
-    k_turbine_sample<<<t.nr, TURB_THREADS, 0, st>>>(s->mesh, t, q, s->state.z, s->d_ctrl, stage, t.diag);
-    k_turbine_raw<<<std::max(1, std::min((t.nucell + 255) / 256, s->sms * 8)), 256, 0, st>>>(s->mesh, t, q, s->d_ctrl, stage);
-    if (mixed) mixed_kernel(make_launch(s, st), K_HKT_FACES, stage, nullptr);
-    else if (faces) k_hkt_faces<<<SSHAPE(K_HKT_FACES, s->nf), 0, st>>>(s->mesh, t, q, s->state.z, s->d_ctrl, stage);
-    return mixed || faces ? 4 : 2;
+    int n = 0;
+    if (part & TURB_CELLS) {
+        if (mixed) n += mixed_kernel(make_launch(s, st), K_HKT_GRAD, stage, nullptr);
+        else if (faces) {
+            k_hkt_gradients<<<SSHAPE(K_HKT_GRAD, s->nc), 0, st>>>(s->mesh, t, q, s->state.z, s->d_ctrl, stage);
+            ++n;
+        }
+        k_turbine_sample<<<t.nr, TURB_THREADS, 0, st>>>(s->mesh, t, q, s->state.z, s->d_ctrl, stage, t.diag);
+        k_turbine_raw<<<std::max(1, std::min((t.nucell + 255) / 256, s->sms * 8)), 256, 0, st>>>(s->mesh, t, q,
+                                                                                               s->d_ctrl, stage);
+        n += 2;
+    }
+    if (part & TURB_FACES) {
+        if (mixed) n += mixed_kernel(make_launch(s, st), K_HKT_FACES, stage, nullptr);
+        else if (faces) {
+            k_hkt_faces<<<SSHAPE(K_HKT_FACES, s->nf), 0, st>>>(s->mesh, t, q, s->state.z, s->d_ctrl, stage);
+            ++n;
+        }
+    }
+    return n;
 }
 
 static int launch_kernel(brx_solver *s, int kind, int stage, double *rate_out, cudaStream_t st = nullptr)
@@ -1029,19 +1048,28 @@ static int launch_kernel(brx_solver *s, int kind, int stage, double *rate_out, c
 
 // One stage: the boundary CTAs fork onto the side stream and overlap the cell
 // sweep (they are independent); the face sweep joins both.
+// One stage. The side stream takes the work that needs only the stage
+// state: the boundary CTAs (joined before the face sweep) and the rotor cell
+// terms (joined before the rotor face terms), overlapping the cell, face and
+// gather sweeps on the main stream.
 static void enqueue_stage(brx_solver *s, int stage, double *rate_out)
 {
-    const bool fork = s->nslot > 0;
+    const bool fork = s->nslot > 0 || s->has_turb;
     if (fork) {
         cudaEventRecord(s->fork, s->stream);
         cudaStreamWaitEvent(s->side, s->fork, 0);
         s->launches += launch_kernel(s, K_BOUNDARY, stage, nullptr, s->side);
         cudaEventRecord(s->join, s->side);
+        s->launches += launch_turbines(s, stage, s->side, TURB_CELLS);
+        cudaEventRecord(s->join2, s->side);
     }
     s->launches += launch_kernel(s, K_CELLS, stage, nullptr);
     if (fork) cudaStreamWaitEvent(s->stream, s->join, 0);
-    for (int kind : {(int)K_FACES, (int)K_GATHER, (int)K_LIMIT, (int)K_TURB, (int)K_UPDATE})
-        s->launches += launch_kernel(s, kind, stage, kind == K_UPDATE || kind == K_LIMIT ? rate_out : nullptr);
+    for (int kind : {(int)K_FACES, (int)K_GATHER, (int)K_LIMIT})
+        s->launches += launch_kernel(s, kind, stage, kind == K_LIMIT ? rate_out : nullptr);
+    if (fork) cudaStreamWaitEvent(s->stream, s->join2, 0);
+    s->launches += launch_turbines(s, stage, s->stream, TURB_FACES);
+    s->launches += launch_kernel(s, K_UPDATE, stage, rate_out);
 }
 
 // HLLC / MUSCL-Hancock kernels of one substep (kinds of the profile), on st.

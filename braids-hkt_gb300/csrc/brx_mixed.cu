@@ -704,14 +704,7 @@ __global__ void __launch_bounds__(256) km_update(MeshDev m, StateDev s, Ctrl *ct
                                                  double *rate_out, TurbDev t, int turb)
 {
     const int nc = m.nc;
-    if (stage == 1 && blockIdx.x == 0)          // the first stage's CFL test, for the second stage's skip
-        for (int i = threadIdx.x; i < m.nscen; i += blockDim.x) {
-            Ctrl &cc = ctrl[i];
-            cc.cfl1 = cc.trial * bits_to_double(cc.peak1) > cc.cfl * (1 + 1e-12);
-        }
-    const float2 *ws = reinterpret_cast<const float2 *>(w.ws);
-    const float *theta32 = reinterpret_cast<const float *>(w.theta);
-    const MxPrim *P = reinterpret_cast<const MxPrim *>(stage == 1 ? g.prim[0] : g.prim[1]);
+    const MxLim *lim = reinterpret_cast<const MxLim *>(w.lim);
     const float *rate32 = reinterpret_cast<const float *>(w.rate);
     MxPrim *P2 = reinterpret_cast<MxPrim *>(g.prim[1]);
     FOR_ACTIVE_CELLS(m.act, c) {
@@ -721,31 +714,11 @@ __global__ void __launch_bounds__(256) km_update(MeshDev m, StateDev s, Ctrl *ct
         double mass = 0.;
         float mx = 0.f, my = 0.f;
         for (int k = m.offset[c]; k < m.offset[c + 1]; ++k) {
-            // the face's donor-limited flux (river_midpoint.h:30-41), formed
-            // identically by both of its cells
-            const int f = m.faces[k];
-            const double w8 = g.cw8[k];
-            const float wf = ws[f].x;
-            double water = double(wf);
-            float cx = 0.f, cy = 0.f;
-            const int2 ci = g.cidx[k];
-            if (wf != 0.f && !(ci.y & 1)) {
-                const bool own = w8 > 0.;                       // this cell is the face's owner
-                const int donor = ((wf < 0.f) == own) ? ci.x : c;
-                if (donor >= 0) {
-                    const float th = theta32[donor];
-                    if (th != 1.f) {
-                        const float delta = (th - 1.f) * wf;
-                        water = double(wf) * double(th);      // exact product
-                        const MxPrim pd = P[donor];
-                        if (pd.wet) { cx = delta * pd.u; cy = delta * pd.v; }
-                    }
-                }
-            }
-            mass -= w8 * water;
+            const MxLim L = lim[m.faces[k]];
+            mass -= g.cw8[k] * L.water;
             const float wk = g.cw4[k];
-            mx -= wk * cx;
-            my -= wk * cy;
+            mx -= wk * L.cx;
+            my -= wk * L.cy;
         }
         double r1 = double(rate32[c] + mx), r2 = double(rate32[nc + c] + my);
         if (turb && t.hkt[sid]) {
@@ -984,9 +957,6 @@ int mixed_kernel(const Launch &L, int kind, int stage, double *out)
         brx_mx::km_gather<<<SHAPE(K_GATHER, nc), 0, st>>>(L.mesh, L.state, L.ctrl, L.work, L.mx, stage);
         return 1;
     case K_LIMIT:
-        // the substep's update forms the limited fluxes itself; the residual
-        // entry (out = its rate buffer) also exports them (K_WATER)
-        if (!out) return 0;
         brx_mx::km_limit<<<SHAPE(K_LIMIT, nf), 0, st>>>(L.mesh, L.ctrl, L.work, L.mx, stage);
         return 1;
     case K_UPDATE:
