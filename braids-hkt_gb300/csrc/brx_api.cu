@@ -99,6 +99,8 @@ struct brx_solver {
     int method = BRX_METHOD_FWAVE;   // hydraulic method of the substep graph
     HllcDev hllc{};                  // HLLC stencil (valid when hllc_ready)
     bool hllc_ready = false;
+    bool rating_ready = false;       // Q-H curves installed (brx_rating_set)
+    std::vector<int> h_rating_off;
     std::vector<int> h_seg_mode;     // host copy of the segment modes
 
     template <class T> int alloc(T **p, size_t count)
@@ -470,8 +472,10 @@ extern "C" int brx_boundary_set(brx_solver *s, const int *seg_mode, const int *s
     if (!seg_mode || !stage_policy || !exterior_bed || !forcing) return fail(BRX_ERR_ARGUMENT, "null boundary array");
     for (int sg = 0; sg < nseg; ++sg) {
         const int md = seg_mode[sg];
-        if (md != 2 && md != 3 && md != 6 && md != 9)
-            return fail(BRX_ERR_UNSUPPORTED, "open-boundary mode must be 2, 3, 6 or 9");
+        if (md != 2 && md != 3 && md != 6 && md != 9 && md != 11)
+            return fail(BRX_ERR_UNSUPPORTED, "open-boundary mode must be 2, 3, 6, 9 or 11");
+        if (md == 11 && (!s->rating_ready || s->h_rating_off[sg + 1] - s->h_rating_off[sg] < 2))
+            return fail(BRX_ERR_STATE, "a rating-curve outlet (mode 11) needs its curve first (brx_rating_set)");
         if (stage_policy[sg] != 0 && stage_policy[sg] != 1) return fail(BRX_ERR_ARGUMENT, "stage policy must be 0 or 1");
         if (!std::isfinite(forcing[sg]) || !std::isfinite(forcing[nseg + sg])) return fail(BRX_ERR_ARGUMENT, "nonfinite forcing");
     }
@@ -505,6 +509,34 @@ extern "C" int brx_boundary_set(brx_solver *s, const int *seg_mode, const int *s
         CK(cudaMemcpy(s->d_ccls, s->h_ccls.data(), sizeof(int) * s->nc, cudaMemcpyHostToDevice));
     }
     s->boundary_ready = true;
+    return BRX_OK;
+}
+
+extern "C" int brx_rating_set(brx_solver *s, const int *offset, const double *discharge, const double *elevation)
+{
+    if (!s) return fail(BRX_ERR_ARGUMENT, "null solver");
+    if (!offset || !discharge || !elevation) return fail(BRX_ERR_ARGUMENT, "null rating array");
+    if (s->rating_ready) return fail(BRX_ERR_STATE, "rating curves are already installed");
+    const int nseg = s->nseg;
+    if (nseg == 0 || offset[0] != 0) return fail(BRX_ERR_ARGUMENT, "rating offsets must start at 0");
+    for (int sg = 0; sg < nseg; ++sg) {
+        if (offset[sg + 1] < offset[sg]) return fail(BRX_ERR_ARGUMENT, "rating offsets must not decrease");
+        for (int k = offset[sg]; k < offset[sg + 1]; ++k) {
+            if (!std::isfinite(discharge[k]) || !std::isfinite(elevation[k]) || discharge[k] < 0)
+                return fail(BRX_ERR_ARGUMENT, "rating knots must be finite with nonnegative discharge");
+            if (k > offset[sg] && !(elevation[k] > elevation[k - 1]))
+                return fail(BRX_ERR_ARGUMENT, "rating elevations must increase");
+        }
+    }
+    const int n = std::max(offset[nseg], 1);
+    int *p_off;
+    double *p_q, *p_e;
+    TRY(s->upload(&p_off, offset, nseg + 1));
+    TRY(s->upload(&p_q, discharge, n)); TRY(s->upload(&p_e, elevation, n));
+    s->bnd.rt_off = p_off; s->bnd.rt_q = p_q; s->bnd.rt_eta = p_e;
+    s->h_rating_off.assign(offset, offset + nseg + 1);
+    s->rating_ready = true;
+    s->graph_dirty = true;
     return BRX_OK;
 }
 

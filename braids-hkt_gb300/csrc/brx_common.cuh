@@ -44,7 +44,8 @@ enum : unsigned {
     ST_ENDPOINT = 8u,     // negative / nonfinite stage result
     ST_FREQ = 16u,        // nonfinite CFL frequency
     ST_TURBINE = 64u,     // rotor model outside its domain (the reference raises): the scenario fails
-    ST_PRE = ST_SPATIAL | ST_BUDGET | ST_RATE | ST_FREQ | ST_TURBINE,
+    ST_FATAL = 128u,      // an outlet section without an admissible solution (the reference raises ValueError)
+    ST_PRE = ST_SPATIAL | ST_BUDGET | ST_RATE | ST_FREQ | ST_TURBINE | ST_FATAL,
 };
 
 // Per-scenario clock and controls, resident on the device.
@@ -168,6 +169,8 @@ struct BoundaryDev {
     double *terms;           // (3, nslot) scratch: stage terms and weights
     double *trace, *flux;    // (3, nslot) each
     double *seg_sums;        // (3, nseg): wetted stage sum, wetted width, weight total
+    const int *rt_off;       // (nseg+1) Q-H rating knots per mode-11 segment
+    const double *rt_q, *rt_eta;
 };
 
 // Accepted / stage state buffers.

@@ -129,6 +129,132 @@ __device__ void segment_sums(const BoundaryDev &b, int s0, int s1, int row, int 
 }
 
 
+// ---------------------------------------------------------------------------
+// Q-H rating outlet (mode 11): the common water elevation at which the
+// outgoing characteristic discharge of the opening equals the rating curve,
+// then each face's trace (river_rating_outlet.h:15-102). One thread per
+// segment, faces in boundary order.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double rating_velocity(double h, double hi, double u, double g)
+{
+    return h > hi ? u - (h - hi) * sqrt(.5 * g * (1. / h + 1. / hi)) : u + 2. * (sqrt(g * hi) - sqrt(g * h));
+}
+
+__device__ double rating_q(const BoundaryDev &b, int sg, double eta)
+{
+    const int a = b.rt_off[sg], end = b.rt_off[sg + 1];
+    if (eta <= b.rt_eta[a]) return b.rt_q[a];
+    if (eta >= b.rt_eta[end - 1]) return b.rt_q[end - 1];
+    int lo = a, hi = end - 1;
+    while (hi - lo > 1) { const int mid = (lo + hi) / 2; if (b.rt_eta[mid] <= eta) lo = mid; else hi = mid; }
+    const double w = (eta - b.rt_eta[lo]) / (b.rt_eta[hi] - b.rt_eta[lo]);
+    return (1. - w) * b.rt_q[lo] + w * b.rt_q[hi];
+}
+
+__device__ double rating_residual(const MeshDev &m, const BoundaryDev &b, int sg, double eta, double g, double dry,
+                                  const double *q, const double *z, double &actual)
+{
+    const int nc = m.nc, nf = m.nf;
+    double Q = 0.;
+    for (int k = b.seg_off[sg]; k < b.seg_off[sg + 1]; ++k) {
+        const int f = b.slot_face[k], c = m.owner[f];
+        const double bed = b.ext_bed[k], hc = q[c], hi = fmax(hc + z[c] - bed, 0.);
+        if (hc <= dry || hi <= dry) continue;
+        const double u = (q[nc + c] * m.normal[f] + q[2 * nc + c] * m.normal[nf + f]) / hc;
+        if (u >= sqrt(g * hi)) { Q += hi * u * m.length[f]; continue; }
+        const double h = fmax(eta - bed, 0.);
+        if (h > dry) Q += h * fmax(rating_velocity(h, hi, u, g), 0.) * m.length[f];
+    }
+    actual = Q;
+    return Q - rating_q(b, sg, eta);
+}
+
+// 0, or the section failure: 1 no bracket, 2 residual, 3 a fictitious zero-flow root.
+__device__ int rating_section(const MeshDev &m, const BoundaryDev &b, int sg, double g, double dry, double speed,
+                              const double *q, const double *z, bool &bad)
+{
+    const int nc = m.nc, nf = m.nf;
+    double lo = b.rt_eta[b.rt_off[sg]], hi = b.rt_eta[b.rt_off[sg + 1] - 1];
+    int wet = 0;
+    for (int k = b.seg_off[sg]; k < b.seg_off[sg + 1]; ++k) {
+        const int f = b.slot_face[k], c = m.owner[f];
+        const double h0 = q[c], h = fmax(h0 + z[c] - b.ext_bed[k], 0.);
+        if (h0 <= dry || h <= dry) continue;
+        const double u = (q[nc + c] * m.normal[f] + q[2 * nc + c] * m.normal[nf + f]) / h0;
+        if (u >= sqrt(g * h)) continue;
+        double left = dry, right = fmax(h, 1.);
+        for (int it = 0; it < 60 && rating_velocity(right, h, u, g) > sqrt(g * right); ++it) right *= 2.;
+        for (int it = 0; it < 60; ++it) {
+            const double mid = .5 * (left + right);
+            if (rating_velocity(mid, h, u, g) > sqrt(g * mid)) left = mid; else right = mid;
+        }
+        lo = fmax(lo, b.ext_bed[k] + right);
+        ++wet;
+    }
+    double level = 0., actual = 0.;
+    if (wet) {
+        if (!(lo <= hi)) return 1;
+        const double rlo = rating_residual(m, b, sg, lo, g, dry, q, z, actual);
+        const double rhi = rating_residual(m, b, sg, hi, g, dry, q, z, actual);
+        if (!isfinite(rlo) || !isfinite(rhi) || rlo < 0. || rhi > 0.) return 1;
+        for (int it = 0; it < 90; ++it) {
+            const double mid = .5 * (lo + hi);
+            if (mid == lo || mid == hi) break;
+            if (rating_residual(m, b, sg, mid, g, dry, q, z, actual) > 0.) lo = mid; else hi = mid;
+        }
+        level = .5 * (lo + hi);
+        const double r = rating_residual(m, b, sg, level, g, dry, q, z, actual);
+        if (!isfinite(r) || fabs(r) > 1e-10 * fmax(1., fabs(actual))) return 2;
+        if (actual <= 1e-14)
+            for (int k = b.seg_off[sg]; k < b.seg_off[sg + 1]; ++k) {
+                const int f = b.slot_face[k], c = m.owner[f];
+                const double hc = q[c], hh = fmax(hc + z[c] - b.ext_bed[k], 0.);
+                if (hc <= dry || hh <= dry) continue;
+                const double ui = (q[nc + c] * m.normal[f] + q[2 * nc + c] * m.normal[nf + f]) / hc;
+                const double h = fmax(level - b.ext_bed[k], 0.);
+                if (h > dry && ui < sqrt(g * hh) && rating_velocity(h, hh, ui, g) < -1e-12) return 3;
+            }
+    }
+    const size_t ns = b.nslot;
+    for (int k = b.seg_off[sg]; k < b.seg_off[sg + 1]; ++k) {
+        const int f = b.slot_face[k], c = m.owner[f];
+        const double bed = b.ext_bed[k], h0 = q[c], geom = fmax(h0 + z[c] - bed, 0.);
+        const double nx = m.normal[f], ny = m.normal[nf + f];
+        double ux = 0., uy = 0.;
+        if (h0 > dry) { ux = q[nc + c] / h0; uy = q[2 * nc + c] / h0; }
+        double un = ux * nx + uy * ny, h = geom;
+        const double tx = ux - un * nx, ty = uy - un * ny;
+        if (h0 <= dry || geom <= dry) { h = 0.; un = 0.; }
+        else if (!(un >= sqrt(g * geom))) {     // subcritical: the common level; supercritical keeps its own
+            const double incoming = un;
+            h = fmax(level - bed, 0.);
+            un = h > dry ? rating_velocity(h, geom, incoming, g) : 0.;
+            if (un <= 0.) {                      // reflected: the stagnation depth of the incoming stream
+                double left = dry, right = fmax(geom, 1.);
+                for (int it = 0; it < 60 && rating_velocity(right, geom, incoming, g) > 0.; ++it) right *= 2.;
+                for (int it = 0; it < 80; ++it) {
+                    const double mid = .5 * (left + right);
+                    if (rating_velocity(mid, geom, incoming, g) > 0.) left = mid; else right = mid;
+                }
+                h = .5 * (left + right);
+                un = 0.;
+            }
+        }
+        if (!isfinite(h) || !isfinite(un) || sqrt(un * un + tx * tx + ty * ty) > speed) { bad = true; continue; }
+        double water = 0., fx = 0., fy = 0., t0 = 0., t1 = 0., t2 = 0.;
+        if (h > dry) {
+            t0 = h; t1 = h * (un * nx + tx); t2 = h * (un * ny + ty);
+            water = h * un;
+            fx = water * (un * nx + tx) + .5 * g * h * h * nx;
+            fy = water * (un * ny + ty) + .5 * g * h * h * ny;
+        }
+        const double pressure = h0 > dry ? .5 * g * (h0 * h0 - geom * geom) : 0.;
+        b.trace[k] = t0; b.trace[ns + k] = t1; b.trace[2 * ns + k] = t2;
+        b.flux[k] = water; b.flux[ns + k] = fx + pressure * nx; b.flux[2 * ns + k] = fy + pressure * ny;
+    }
+    return 0;
+}
+
 // stage 1 / 2: the SSPRK stages (state work / q1, its own stock, clock t or
 // t + dt); STAGE_HANCOCK: the HLLC predicted state q1 at t + dt/2, outlet
 // stock of the substep's start state work (hllc.py:91-97), status of stage 1.
@@ -272,6 +398,15 @@ __global__ void k_boundary(MeshDev m, StateDev s, BoundaryDev b, Ctrl *ctrl, int
         b.trace[k] = tr0; b.trace[(size_t)b.nslot + k] = tr1; b.trace[2 * (size_t)b.nslot + k] = tr2;
         b.flux[k] = fl0; b.flux[(size_t)b.nslot + k] = fl1; b.flux[2 * (size_t)b.nslot + k] = fl2;
     }
+    __syncthreads();
+    // section owners of the remaining outlet modes, after the face loop
+    // (river_exterior_bed.py:213-217); a section without a solution fails the scenario
+    for (int sg = s0 + threadIdx.x; sg < s1; sg += blockDim.x)
+        if (b.seg_mode[sg] == 11) {
+            bool sbad = false;
+            if (rating_section(m, b, sg, grav, dry, ct.speed_limit, q, z, sbad)) raise_status(ct, stage, ST_FATAL);
+            if (sbad) bad = 1;
+        }
     if (bad) raise_status(ct, stage, ST_SPATIAL);
     __syncthreads();
     // outlet stock cap, one thread per unique owner, its faces in boundary order
@@ -867,6 +1002,7 @@ __device__ void control_one(Ctrl &c)
     if (!c.active || c.done) return;
     // a rotor outside its model's domain ends the scenario (the reference raises)
     if ((c.status1 | c.status2) & ST_TURBINE) { c.failed = 4; c.done = 1; return; }
+    if ((c.status1 | c.status2) & ST_FATAL) { c.failed = 5; c.done = 1; return; }
     const double f1 = bits_to_double(c.peak1), f2 = bits_to_double(c.peak2);
     // the reference's frequency peak only sees stages that reached the CFL evaluation
     double peak = 0.;

@@ -232,6 +232,19 @@ def small_channel(length=120.0, width=24.0, spacing=4.0, seed=7, sigma=0.15, cor
                    discharge, 0.03, cfl, field_resolution=0.5)
 
 
+def rating_channel(discharge=20.0, knots=((0.0, 2.0), (10.0, 2.6), (20.0, 3.0), (40.0, 3.6), (80.0, 4.5)),
+                   **kw):
+    """The small channel with its outlet controlled by a Q-H rating curve
+    (mode 11) instead of a fixed stage: `knots` are (Q [m3/s], water
+    elevation [m]); the default passes through the inflow at the initial
+    stage of 3.0 m."""
+    case = small_channel(discharge=discharge, **kw)
+    case["seg_mode"] = np.array([M.MODE_TOTAL_Q, 11], np.int32)
+    case["rating"] = {1: [tuple(map(float, k)) for k in knots]}
+    case["name"] = "rating_channel"
+    return case
+
+
 def lake_at_rest(length=80.0, width=40.0, spacing=4.0, seed=11, islands=True):
     """Variable bed with emerged islands, flat surface at 1.0 m, closed walls (no open segments)."""
     mesh = M.channel_mesh(length, width, spacing, 1.0, seed)
@@ -324,6 +337,8 @@ def case_arrays(case):
         out[k] = np.asarray(case[k])
     for k, v in case["controls"].items():
         out[f"ctl_{k}"] = np.asarray(v)
+    for b, knots in (case.get("rating") or {}).items():
+        out[f"rating_{int(b)}"] = np.asarray(knots, dtype=np.float64)
     return out
 
 
@@ -335,6 +350,9 @@ def case_from_arrays(arrs):
     case = dict(mesh=mesh, controls=ctl, name="fixture")
     for k in ("z", "q", "seg_mode", "stage_policy", "forcing", "exterior_bed"):
         case[k] = np.asarray(arrs[k])
+    rating = {int(k[7:]): [tuple(r) for r in np.asarray(v)] for k, v in arrs.items() if k.startswith("rating_")}
+    if rating:
+        case["rating"] = rating
     return case
 
 

@@ -46,6 +46,32 @@ def _ptr(a):
     return C.c_void_p(a.ctypes.data) if a is not None else None
 
 
+def rating_tables(cases):
+    """Q-H rating curves of the mode-11 outlets of a batch: (offset (nseg+1),
+    discharge, elevation) over the packed segments; case["rating"] maps a
+    segment to its knots [(Q [m3/s], water elevation [m]), ...], elevation
+    increasing (the reference's rating_curve rows, river_rating_outlet.py:12-16)."""
+    off, rq, re_ = [0], [], []
+    for case in cases:
+        nb = case["mesh"].nb
+        curves = case.get("rating") or {}
+        modes = np.asarray(case.get("seg_mode", np.zeros(0)), dtype=int)
+        for b in range(nb):
+            knots = curves.get(b)
+            if modes[b] == 11:
+                if knots is None or len(knots) < 2:
+                    raise ValueError(f"rating outlet segment {b} needs a curve of at least two knots")
+                eta = np.array([float(e) for _, e in knots])
+                if not np.all(np.diff(eta) > 0):
+                    raise ValueError("rating curve elevations must increase")
+                for qv, e in knots:
+                    rq.append(float(qv))
+                    re_.append(float(e))
+            off.append(len(rq))
+    return (np.asarray(off, np.int32), np.asarray(rq if rq else [0.0], np.float64),
+            np.asarray(re_ if re_ else [0.0], np.float64))
+
+
 def pack(cases):
     """Concatenate scenario meshes into one global index space."""
     out = {k: [] for k in ("owner", "neighbour", "bid", "offset", "faces", "signs", "normal", "length", "area",
@@ -136,6 +162,9 @@ class RiverSolver:
             check(self.lib.brx_controls_set(self.h, i, c["grav"], c["dry"], c["cfl"], c["speed_limit"],
                                             int(c["roughness_mode"]), c["roughness_value"]))
         if p["nseg"]:
+            if np.any(p["seg_mode"] == 11):
+                off, rq, re_ = rating_tables(self.cases)
+                check(self.lib.brx_rating_set(self.h, _ptr(off), _ptr(rq), _ptr(re_)))
             check(self.lib.brx_boundary_set(self.h, _ptr(p["seg_mode"]), _ptr(p["stage_policy"]),
                                             _ptr(p["exterior_bed"]), _ptr(p["forcing"])))
         else:

@@ -90,8 +90,17 @@ int brx_solver_destroy(brx_solver *s);
 int brx_controls_set(brx_solver *s, int scen, double gravity, double dry, double cfl,
                      double speed_limit, int roughness_mode, double roughness_value);
 
+/* Q-H rating curves of the mode-11 outlets (replaces RatingOutlet's tables,
+ * src/braids_core/sediment/river_rating_outlet.py:10-18): segment s's knots
+ * are offset[s] .. offset[s+1]-1 of discharge [m3/s] / elevation [m], the
+ * elevations increasing; offset (nseg+1), host arrays, copied. Call before
+ * brx_boundary_set when any segment has mode 11. */
+int brx_rating_set(brx_solver *s, const int *offset, const double *discharge, const double *elevation);
+
 /* Open-boundary set-up for all segments: hydraulic mode (2 stage, 3 free
- * outflow, 6 total discharge, 9 discharge + water line), stage reversal
+ * outflow, 6 total discharge, 9 discharge + water line, 11 Q-H rating
+ * curve: one common water elevation at which the outgoing characteristic
+ * discharge equals the curve, river_rating_outlet.h), stage reversal
  * policy, exterior bed per face (nf, read on open faces) and forcing (2,nseg)
  * rows discharge, stage. Replaces ExteriorBed construction
  * (src/braids_core/sediment/river_exterior_bed.py:47-93). */

@@ -86,6 +86,10 @@ typedef struct {
     const double *table_value;                     /* (2, nb, table_len) */
     int threads;
     const struct om_turbines *turb;                /* rotors (NULL: none) */
+    /* Q-H rating curves of mode-11 outlets: segment b's knots are
+     * rating_offset[b] .. rating_offset[b+1]-1 (elevation increasing) */
+    const int *rating_offset;                      /* (nb+1) or NULL */
+    const double *rating_q, *rating_eta;
 } om_ctx;
 
 /* ------------------------------------------------------------------ */
@@ -800,6 +804,137 @@ void om_sample_forcing(om_ctx *m, double t)
 /* Exterior traces and fluxes on open faces (ExteriorBed.evaluate).
  * work needs 3*nf doubles; stage_out (2,nb), total_out (nb). Returns 0 or
  * the first nonzero face status. */
+/* ------------------------------------------------------------------ */
+/* Q-H rating outlet (mode 11): one common water elevation across the   */
+/* opening at which the outgoing characteristic discharge equals the    */
+/* rating curve (src/braids_core/sediment/river_rating_outlet.h:15-102). */
+/* ------------------------------------------------------------------ */
+enum { OM_EXTERIOR_FATAL = 100 };
+
+static double om_rating_velocity(double h, double hi, double u, double g)
+{
+    return h > hi ? u - (h - hi) * sqrt(.5 * g * (1. / h + 1. / hi)) : u + 2. * (sqrt(g * hi) - sqrt(g * h));
+}
+
+static double om_rating_q(const om_ctx *m, int b, double eta)
+{
+    const int a = m->rating_offset[b], end = m->rating_offset[b + 1];
+    const double *tq = m->rating_q, *te = m->rating_eta;
+    if (eta <= te[a]) return tq[a];
+    if (eta >= te[end - 1]) return tq[end - 1];
+    int lo = a, hi = end - 1;
+    while (hi - lo > 1) { const int mid = (lo + hi) / 2; if (te[mid] <= eta) lo = mid; else hi = mid; }
+    const double w = (eta - te[lo]) / (te[hi] - te[lo]);
+    return (1. - w) * tq[lo] + w * tq[hi];
+}
+
+static double om_rating_residual(const om_ctx *m, int b, double eta, const double *q, const double *z, double *actual)
+{
+    const int nc = m->nc, nf = m->nf;
+    const double g = m->grav, dry = m->dry;
+    double Q = 0.;
+    for (int k = m->boundary_offset[b]; k < m->boundary_offset[b + 1]; ++k) {
+        const int f = m->boundary_faces[k], c = m->owner[f];
+        const double bed = m->exterior_bed[f], hc = q[c], hi = fmax(hc + z[c] - bed, 0.);
+        if (hc <= dry || hi <= dry) continue;
+        const double u = (q[nc + c] * m->normal[f] + q[2 * nc + c] * m->normal[nf + f]) / hc;
+        if (u >= sqrt(g * hi)) { Q += hi * u * m->length[f]; continue; }
+        const double h = fmax(eta - bed, 0.);
+        if (h > dry) Q += h * fmax(om_rating_velocity(h, hi, u, g), 0.) * m->length[f];
+    }
+    *actual = Q;
+    return Q - om_rating_q(m, b, eta);
+}
+
+/* Returns 0, or the section's failure (1 no bracket, 2 residual, 3 a
+ * fictitious zero-flow root), on which the reference raises ValueError. */
+static int om_rating_outlet(const om_ctx *m, int b, const double *q, const double *z, double *trace, double *flux,
+                            int *status)
+{
+    const int nc = m->nc, nf = m->nf;
+    const double g = m->grav, dry = m->dry, speed = m->speed_limit;
+    const int first = m->rating_offset[b], last = m->rating_offset[b + 1] - 1;
+    double lo = m->rating_eta[first], hi = m->rating_eta[last];
+    int wet = 0;
+    for (int k = m->boundary_offset[b]; k < m->boundary_offset[b + 1]; ++k) {
+        const int f = m->boundary_faces[k], c = m->owner[f];
+        const double h0 = q[c], h = fmax(h0 + z[c] - m->exterior_bed[f], 0.);
+        if (h0 <= dry || h <= dry) continue;
+        const double u = (q[nc + c] * m->normal[f] + q[2 * nc + c] * m->normal[nf + f]) / h0;
+        if (u >= sqrt(g * h)) continue;
+        /* the subcritical branch: the lowest admissible level of this face */
+        double left = dry, right = fmax(h, 1.);
+        for (int it = 0; it < 60 && om_rating_velocity(right, h, u, g) > sqrt(g * right); ++it) right *= 2.;
+        for (int it = 0; it < 60; ++it) {
+            const double mid = .5 * (left + right);
+            if (om_rating_velocity(mid, h, u, g) > sqrt(g * mid)) left = mid; else right = mid;
+        }
+        lo = fmax(lo, m->exterior_bed[f] + right);
+        ++wet;
+    }
+    double level = 0., actual = 0.;
+    if (wet) {
+        if (!(lo <= hi)) return 1;
+        const double rlo = om_rating_residual(m, b, lo, q, z, &actual);
+        const double rhi = om_rating_residual(m, b, hi, q, z, &actual);
+        if (!isfinite(rlo) || !isfinite(rhi) || rlo < 0. || rhi > 0.) return 1;
+        for (int it = 0; it < 90; ++it) {
+            const double mid = .5 * (lo + hi);
+            if (mid == lo || mid == hi) break;
+            if (om_rating_residual(m, b, mid, q, z, &actual) > 0.) lo = mid; else hi = mid;
+        }
+        level = .5 * (lo + hi);
+        const double r = om_rating_residual(m, b, level, q, z, &actual);
+        if (!isfinite(r) || fabs(r) > 1e-10 * fmax(1., fabs(actual))) return 2;
+        if (actual <= 1e-14)
+            for (int k = m->boundary_offset[b]; k < m->boundary_offset[b + 1]; ++k) {
+                const int f = m->boundary_faces[k], c = m->owner[f];
+                const double hc = q[c], hh = fmax(hc + z[c] - m->exterior_bed[f], 0.);
+                if (hc <= dry || hh <= dry) continue;
+                const double ui = (q[nc + c] * m->normal[f] + q[2 * nc + c] * m->normal[nf + f]) / hc;
+                const double h = fmax(level - m->exterior_bed[f], 0.);
+                if (h > dry && ui < sqrt(g * hh) && om_rating_velocity(h, hh, ui, g) < -1e-12) return 3;
+            }
+    }
+    for (int k = m->boundary_offset[b]; k < m->boundary_offset[b + 1]; ++k) {
+        const int f = m->boundary_faces[k], c = m->owner[f];
+        const double bed = m->exterior_bed[f], h0 = q[c], geom = fmax(h0 + z[c] - bed, 0.);
+        const double nx = m->normal[f], ny = m->normal[nf + f];
+        double ux = 0., uy = 0.;
+        if (h0 > dry) { ux = q[nc + c] / h0; uy = q[2 * nc + c] / h0; }
+        double un = ux * nx + uy * ny, h = geom;
+        const double tx = ux - un * nx, ty = uy - un * ny;
+        if (h0 <= dry || geom <= dry) { h = 0.; un = 0.; }
+        else if (un >= sqrt(g * geom)) { /* supercritical outflow: no downstream control */ }
+        else {
+            const double incoming = un;
+            h = fmax(level - bed, 0.);
+            un = h > dry ? om_rating_velocity(h, geom, incoming, g) : 0.;
+            if (un <= 0.) {             /* reflected: the stagnation depth of the incoming stream */
+                double left = dry, right = fmax(geom, 1.);
+                for (int it = 0; it < 60 && om_rating_velocity(right, geom, incoming, g) > 0.; ++it) right *= 2.;
+                for (int it = 0; it < 80; ++it) {
+                    const double mid = .5 * (left + right);
+                    if (om_rating_velocity(mid, geom, incoming, g) > 0.) left = mid; else right = mid;
+                }
+                h = .5 * (left + right);
+                un = 0.;
+            }
+        }
+        if (!isfinite(h) || !isfinite(un) || sqrt(un * un + tx * tx + ty * ty) > speed) { status[f] = 3; continue; }
+        double water = 0., fx = 0., fy = 0.;
+        if (h > dry) {
+            trace[f] = h; trace[nf + f] = h * (un * nx + tx); trace[2 * nf + f] = h * (un * ny + ty);
+            water = h * un;
+            fx = water * (un * nx + tx) + .5 * g * h * h * nx;
+            fy = water * (un * ny + ty) + .5 * g * h * h * ny;
+        } else trace[f] = trace[nf + f] = trace[2 * nf + f] = 0.;
+        const double pressure = h0 > dry ? .5 * g * (h0 * h0 - geom * geom) : 0.;
+        flux[f] = water; flux[nf + f] = fx + pressure * nx; flux[2 * nf + f] = fy + pressure * ny;
+    }
+    return 0;
+}
+
 int om_exterior(om_ctx *m, const double *q, const double *z, double time,
                 double *trace, double *flux, int *status, double *work,
                 double *stage_out, double *total_out)
@@ -901,6 +1036,12 @@ int om_exterior(om_ctx *m, const double *q, const double *z, double time,
         if (mode == 9 && h <= dry) pressure = h0 > dry ? .5 * gravity * h0 * h0 : 0.;
         flux[i] = water; flux[nf + i] = fx + pressure * nx; flux[2 * nf + i] = fy + pressure * ny;
     }
+    /* section owners of the remaining outlet modes (river_exterior_bed.py:213-217) */
+    for (int b = 0; b < nb; ++b)
+        if (m->seg_mode[b] == 11 && om_rating_outlet(m, b, q, z, trace, flux, status)) return OM_EXTERIOR_FATAL;
+    if (!first)
+        for (int i = 0; i < nf; ++i)
+            if (status[i]) { first = status[i]; break; }
     return first;
 }
 
@@ -1660,8 +1801,9 @@ int om_rate(om_ctx *m, om_scratch *s, const double *q, const double *z, const do
     for (int i = 0; i < nc; ++i)
         if (q[i] < 0) return OM_REJECT_SPATIAL;
     if (m->nb > 0) {
-        if (om_exterior(m, q, z, time, s->ext_trace, s->ext_flux, s->estatus, s->work, s->stage, s->total))
-            return OM_REJECT_SPATIAL;
+        const int ex = om_exterior(m, q, z, time, s->ext_trace, s->ext_flux, s->estatus, s->work, s->stage, s->total);
+        if (ex == OM_EXTERIOR_FATAL) return OM_FAIL;
+        if (ex) return OM_REJECT_SPATIAL;
         om_outlet_feasibility(m, base, dt, s->ext_flux, s->ext_trace, s->work);
     }
     om_primitive(m, q, z, s->v, s->active, s->pstatus);
@@ -2109,9 +2251,10 @@ int om_hllc_single(om_ctx *m, const om_hllc_geo *G, om_scratch *s, om_hllc_scrat
     }
     const double *ext = s->ext_flux, *ext_trace = s->ext_trace;
     if (m->nb > 0) {
-        if (om_exterior(m, S->qhalf, z, time + .5 * dt, s->ext_trace, s->ext_flux, s->estatus, s->work, s->stage,
-                        s->total))
-            return OM_REJECT_SPATIAL;
+        const int ex = om_exterior(m, S->qhalf, z, time + .5 * dt, s->ext_trace, s->ext_flux, s->estatus, s->work,
+                                   s->stage, s->total);
+        if (ex == OM_EXTERIOR_FATAL) return OM_FAIL;
+        if (ex) return OM_REJECT_SPATIAL;
         om_outlet_feasibility(m, S->work, dt, s->ext_flux, s->ext_trace, s->work);
     }
     om_hllc_faces(m, G, S->half, S->grad, ext, ext_trace, S->fl, S->fr, S->speed);

@@ -60,7 +60,7 @@ class Ctx(C.Structure):
                 ("roughness_mode", I), ("roughness_value", D),
                 ("seg_mode", P), ("stage_policy", P), ("exterior_bed", P), ("forcing", P),
                 ("table_len", I), ("table_time", P), ("table_value", P), ("threads", I),
-                ("turb", P)]
+                ("turb", P), ("rating_offset", P), ("rating_q", P), ("rating_eta", P)]
 
 
 class Turbines(C.Structure):
@@ -215,6 +215,12 @@ class Oracle:
             ctx.table_time = k("table_time", _f64(tt))
             ctx.table_value = k("table_value", _f64(case["table_value"]))
         ctx.threads = threads or 0
+        if case.get("rating"):
+            from braids_hkt_gb300.solver import rating_tables
+            off, rq, re_ = rating_tables([case])
+            ctx.rating_offset = k("rating_offset", _i32(off))
+            ctx.rating_q = k("rating_q", _f64(rq))
+            ctx.rating_eta = k("rating_eta", _f64(re_))
         self.turbines = None
         self.case_exner = case.get("exner")
         if case.get("turbines"):

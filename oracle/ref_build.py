@@ -22,7 +22,8 @@ Dual-compiled OpenMP headers (their ENTRY/LOOP macros select the host form):
   river_hydraulic_drag.source() (src/braids_core/sediment/river_hydraulic_drag.py:11-15),
   river_turbine_flow.h, river_hydrokinetic_stress.h (turbine momentum terms),
   river_mpm.h, flow2dh_mobile_kernels.h, bend_methods_v1_kernels.h (Exner / MPM),
-  hllc.h, hllc_turbines.h (src/braids_core/hydraulics, the HLLC option)
+  hllc.h, hllc_turbines.h (src/braids_core/hydraulics, the HLLC option),
+  river_rating_outlet.h (Q-H rating outlet)
 Generated CUDA C also: flow_bed_slope_runtime.cu (src/braids_gpu, Koch-Flokstra slope)
 
 Usage: python oracle/ref_build.py   (exits non-zero when the reference is absent)
@@ -112,6 +113,8 @@ def generate():
         # HLLC / MUSCL-Hancock option and its rotor pressure correction
         "ref_hllc": (src / "braids_core/hydraulics/hllc.h").read_text(),
         "ref_hllc_turbines": (src / "braids_core/hydraulics/hllc_turbines.h").read_text(),
+        # section owners of the remaining outlet modes
+        "ref_rating": (src / "braids_core/sediment/river_rating_outlet.h").read_text(),
     }
     for name, code in headers.items():
         (OUT / f"{name}.h").write_text(code)

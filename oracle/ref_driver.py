@@ -45,6 +45,10 @@ class Rejected(Exception):
     pass
 
 
+class Fatal(Exception):
+    """A failure the reference raises as an error, not a trial rejection."""
+
+
 def _ptr(a):
     return C.c_void_p(a.ctypes.data)
 
@@ -422,6 +426,20 @@ class Ref:
         self.call("exterior", "exterior_flux", 0, nf, n, nb, self.grav, self.dry, self.speed_limit,
                   g["owner"], g["bid"], g["selected"], self.seg_mode, self.stage_policy, q, self.z,
                   self.exterior_bed, g["normal"], g["length"], self.forcing, weights, total, trace, flux, status)
+        # section owners after exterior_flux (ExteriorBed.evaluate, river_exterior_bed.py:213-217)
+        if np.any(self.seg_mode[:nb] == 11):
+            from braids_hkt_gb300.solver import rating_tables
+            if "ref_rating" not in self.libs:
+                self.libs["ref_rating"] = C.CDLL(str(REF / "libref_rating.so"))
+                self.libs["ref_rating"].mobile_threads(C.c_int(os.cpu_count() or 1))
+            off, rq, re_ = rating_tables([self.case])
+            control = np.ascontiguousarray((self.seg_mode[:nb] == 11).astype(np.int32))
+            sec = np.zeros(nb, np.int32)
+            self.call("ref_rating", "rating_outlet", 0, nf, n, nb, self.grav, self.dry, self.speed_limit, control,
+                      g["boffset"], g["bfaces"], g["owner"], q, self.z, self.exterior_bed, g["normal"], g["length"],
+                      off, rq, re_, np.zeros(nb), np.zeros(nb), trace, flux, status, sec)
+            if np.any(sec):
+                raise Fatal("Q-H outlet has no admissible subcritical solution within the supplied curve")
         return trace, flux, status
 
     # -- one spatial residual --------------------------------------------------

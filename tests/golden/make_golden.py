@@ -25,17 +25,22 @@ from ref_driver import Ref  # noqa: E402
 
 OUT = Path(__file__).resolve().parent
 
+ONLY = sys.argv[1:]          # case names to (re)generate; all when empty
+
 CASES = {
     "channel_wet": (S.small_channel, lambda c: S.perturbed_state(c, 3, 0.3, 0.6, 0.0), 0.01, 1.0),
     "channel_wetdry": (S.small_channel, lambda c: S.perturbed_state(c, 4, 1.5, 0.8, 0.2), 0.01, 1.0),
     "lake_islands": (S.lake_at_rest, lambda c: c["q"], 0.05, 2.0),
     "lake_perturbed": (S.lake_at_rest, lambda c: S.perturbed_state(c, 5, 0.5, 0.5, 0.1), 0.01, 1.0),
     "dam_break_dry": (S.dam_break, lambda c: c["q"], 0.02, 1.0),
+    "rating_outlet": (S.rating_channel, lambda c: S.perturbed_state(c, 6, 0.2, 0.4, 0.0), 0.01, 1.0),
 }
 
 
 def main():
     for name, (make, state, dt, interval) in CASES.items():
+        if ONLY and name not in ONLY:
+            continue
         case = make()
         q = np.ascontiguousarray(state(case))
         ref = Ref(case, threads=1)

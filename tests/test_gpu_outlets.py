@@ -1,0 +1,37 @@
+"""Outlet section owners on the GPU: the Q-H rating outlet (mode 11) against
+the oracle (FP64 to 1e-10 with identical substep counts; mixed against FP64
+to 1e-4 in depth) and its failure without a bracket (the scenario fails,
+failed = 5). The reference fixture is checked in test_gpu_parity."""
+import numpy as np
+import pytest
+
+import braids_hkt_gb300.scenarios as S
+
+pytestmark = pytest.mark.gpu
+
+
+def test_rating_outlet_fp64_oracle_and_mixed():
+    from braids_hkt_gb300.solver import RiverSolver
+    from oracle import Oracle
+    case = S.rating_channel()
+    a, b = RiverSolver(case, precision="fp64"), RiverSolver(case, precision="mixed")
+    o = Oracle(case, threads=4)
+    q = case["q"].copy()
+    for k in range(4):
+        da, db = a.advance(2.0, 2.0 * k), b.advance(2.0, 2.0 * k)
+        st, _, stats = o.advance(q, 2.0, 2.0 * k)
+        assert st == 0 and da["failed"] == 0 and db["failed"] == 0
+        assert da["hydraulic_substeps"] == stats["substeps"]
+    scale = np.abs(q).max(axis=1, keepdims=True)
+    assert (np.abs(a.state() - q) / scale).max() <= 1e-10
+    ha, hb = a.state()[0], b.state()[0]
+    assert (np.abs(hb - ha) / np.maximum(ha, 1e-3)).max() <= 1e-4
+
+
+def test_rating_outlet_without_a_bracket_fails_the_scenario():
+    from braids_hkt_gb300.solver import RiverSolver
+    bad = S.rating_channel(knots=((0.0, -5.0), (1.0, -4.0)))
+    good = S.rating_channel()
+    s = RiverSolver([good, bad], precision="fp64")
+    d = s.advance(1.0, 0.0, raise_on_failure=False)
+    assert d[0]["failed"] == 0 and d[1]["failed"] == 5

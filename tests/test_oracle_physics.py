@@ -100,3 +100,40 @@ def test_hydraulic_jump_holds_conjugate_depths():
     band = np.abs(y - 1.5) < 1.0
     x_jump = x[band & (q[0] > 0.5 * (j["h1"] + j["h2"]))].min()
     assert 25.0 < x_jump < 35.0
+
+
+def _rating_q(knots, eta):
+    e = np.array([k[1] for k in knots])
+    qv = np.array([k[0] for k in knots])
+    return float(np.interp(eta, e, qv))
+
+
+def test_rating_outlet_follows_its_curve():
+    """Q-H outlet (mode 11): the discharge through the opening is the rating
+    curve at the opening's water level (within 3% of it, the face level
+    differing from the owner cells' mean), through a seiche of the channel."""
+    case = S.rating_channel()
+    o = Oracle(case, threads=2)
+    q = case["q"].copy()
+    m = case["mesh"]
+    outlet = (m.neighbour < 0) & (m.bid == 1)
+    owners = m.owner[outlet]
+    t = 0.0
+    for k in range(6):
+        st, _, _ = o.advance(q, 5.0, t)
+        t += 5.0
+        stage = float(np.mean(q[0][owners] + case["z"][owners]))
+        st2, water, _ = o.advance(q, 0.1, t)      # the discharge over a short window at that level
+        t += 0.1
+        assert st == 0 and st2 == 0
+        out = float(np.sum(water[outlet] * m.length[outlet]))
+        assert abs(out - _rating_q(case["rating"][1], stage)) <= 0.03 * max(out, 1.0)
+
+
+def test_rating_outlet_without_a_bracket_fails():
+    """A curve whose elevations lie below any admissible level: the reference
+    raises (no retry); the oracle's interval fails."""
+    case = S.rating_channel(knots=((0.0, -5.0), (1.0, -4.0)))
+    o = Oracle(case, threads=2)
+    st, _, _ = o.advance(case["q"].copy(), 1.0, 0.0)
+    assert st == 4
