@@ -100,6 +100,7 @@ struct brx_solver {
     HllcDev hllc{};                  // HLLC stencil (valid when hllc_ready)
     bool hllc_ready = false;
     bool rating_ready = false;       // Q-H curves installed (brx_rating_set)
+    bool chains_ready = false;       // normal-depth outlet chains installed (brx_outlet_chains_set)
     std::vector<int> h_rating_off;
     std::vector<int> h_seg_mode;     // host copy of the segment modes
 
@@ -472,8 +473,10 @@ extern "C" int brx_boundary_set(brx_solver *s, const int *seg_mode, const int *s
     if (!seg_mode || !stage_policy || !exterior_bed || !forcing) return fail(BRX_ERR_ARGUMENT, "null boundary array");
     for (int sg = 0; sg < nseg; ++sg) {
         const int md = seg_mode[sg];
-        if (md != 2 && md != 3 && md != 6 && md != 9 && md != 11)
-            return fail(BRX_ERR_UNSUPPORTED, "open-boundary mode must be 2, 3, 6, 9 or 11");
+        if (md != 2 && md != 3 && md != 6 && md != 9 && md != 10 && md != 11)
+            return fail(BRX_ERR_UNSUPPORTED, "open-boundary mode must be 2, 3, 6, 9, 10 or 11");
+        if (md == 10 && !s->chains_ready)
+            return fail(BRX_ERR_STATE, "a normal-depth outlet (mode 10) needs its face chains first (brx_outlet_chains_set)");
         if (md == 11 && (!s->rating_ready || s->h_rating_off[sg + 1] - s->h_rating_off[sg] < 2))
             return fail(BRX_ERR_STATE, "a rating-curve outlet (mode 11) needs its curve first (brx_rating_set)");
         if (stage_policy[sg] != 0 && stage_policy[sg] != 1) return fail(BRX_ERR_ARGUMENT, "stage policy must be 0 or 1");
@@ -536,6 +539,45 @@ extern "C" int brx_rating_set(brx_solver *s, const int *offset, const double *di
     s->bnd.rt_off = p_off; s->bnd.rt_q = p_q; s->bnd.rt_eta = p_e;
     s->h_rating_off.assign(offset, offset + nseg + 1);
     s->rating_ready = true;
+    s->graph_dirty = true;
+    return BRX_OK;
+}
+
+extern "C" int brx_outlet_chains_set(brx_solver *s, int nchain, const int *offset, const int *faces,
+                                     const double *slope)
+{
+    if (!s) return fail(BRX_ERR_ARGUMENT, "null solver");
+    if (s->chains_ready) return fail(BRX_ERR_STATE, "outlet chains are already installed");
+    if (nchain < 1 || !offset || !faces || !slope) return fail(BRX_ERR_ARGUMENT, "missing chain arrays");
+    if (offset[0] != 0) return fail(BRX_ERR_ARGUMENT, "chain offsets must start at 0");
+    std::vector<int> slot(offset[nchain]), scen(s->nscen + 1, 0), fsid(s->nf, -1);
+    for (int i = 0; i < s->nscen; ++i)
+        for (int f = s->face_offset[i]; f < s->face_offset[i + 1]; ++f) fsid[f] = i;
+    std::vector<int> bslot(s->nf, -1);
+    for (int k = 0; k < s->nslot; ++k) bslot[s->h_slot_face[k]] = k;
+    int prev_sid = -1;
+    for (int c = 0; c < nchain; ++c) {
+        if (offset[c + 1] <= offset[c]) return fail(BRX_ERR_ARGUMENT, "every chain needs faces");
+        if (!(slope[c] > 0) || !std::isfinite(slope[c])) return fail(BRX_ERR_ARGUMENT, "chain bed slopes must be positive");
+        int sid = -1;
+        for (int k = offset[c]; k < offset[c + 1]; ++k) {
+            const int f = faces[k];
+            if (f < 0 || f >= s->nf || bslot[f] < 0) return fail(BRX_ERR_ARGUMENT, "chain face is not an open face");
+            if (sid < 0) sid = fsid[f];
+            else if (fsid[f] != sid) return fail(BRX_ERR_ARGUMENT, "a chain crosses scenarios");
+            slot[k] = bslot[f];
+        }
+        if (sid < prev_sid) return fail(BRX_ERR_ARGUMENT, "chains must come in scenario order");
+        prev_sid = sid;
+        scen[sid + 1] = c + 1;
+    }
+    for (int i = 1; i <= s->nscen; ++i) scen[i] = std::max(scen[i], scen[i - 1]);
+    int *p_scen, *p_off, *p_slot;
+    double *p_slope;
+    TRY(s->upload(&p_scen, scen.data(), scen.size())); TRY(s->upload(&p_off, offset, nchain + 1));
+    TRY(s->upload(&p_slot, slot.data(), slot.size())); TRY(s->upload(&p_slope, slope, nchain));
+    s->bnd.scen_chain = p_scen; s->bnd.chain_off = p_off; s->bnd.chain_slot = p_slot; s->bnd.chain_slope = p_slope;
+    s->chains_ready = true;
     s->graph_dirty = true;
     return BRX_OK;
 }

@@ -171,6 +171,9 @@ struct BoundaryDev {
     double *seg_sums;        // (3, nseg): wetted stage sum, wetted width, weight total
     const int *rt_off;       // (nseg+1) Q-H rating knots per mode-11 segment
     const double *rt_q, *rt_eta;
+    const int *scen_chain;   // (nscen+1) normal-depth outlet chains per scenario
+    const int *chain_off, *chain_slot;   // (nchain+1), slots in section order
+    const double *chain_slope;           // (nchain)
 };
 
 // Accepted / stage state buffers.

@@ -255,6 +255,172 @@ __device__ int rating_section(const MeshDev &m, const BoundaryDev &b, int sg, do
     return 0;
 }
 
+// ---------------------------------------------------------------------------
+// Normal-depth outlet (mode 10): per connected face chain, the level at which
+// the outgoing characteristic discharge equals the uniform-flow conveyance
+// at the chain's bed slope (river_normal_outlet.h:17-134). One thread per
+// chain; dry faces close with their owner's pressure.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double nout_chezy(int law, double r, double value, double g)
+{
+    if (law == 1) return value;
+    if (law == 2) return pow(r, 1. / 6.) / value;
+    if (law == 3) return sqrt(g) / .41 * log1p(30. * r / (exp(1.) * value));
+    return 18. * log10(12. * fmax(.5, r / value));
+}
+
+__device__ double nout_residual(const MeshDev &m, const BoundaryDev &b, const int *slots, int start, int end,
+                                double eta, double slope, double g, double dry, int law, double rough,
+                                const double *q, const double *z, double &area_out, double &q_out)
+{
+    const int nc = m.nc, nf = m.nf;
+    double area = 0., perimeter = 0., rate = 0., drag = 0., prev = 0.;
+    for (int k = start; k < end; ++k) {
+        const int sl = slots[k], f = b.slot_face[sl];
+        const double h = fmax(eta - b.ext_bed[sl], 0.);
+        area += h * m.length[f];
+        perimeter += h > dry ? m.length[f] : 0.;
+        if (k == start) perimeter += h; else perimeter += fabs(h - prev);
+        prev = h;
+    }
+    perimeter += prev;
+    if (area <= 0. || perimeter <= 0.) { area_out = 0.; q_out = 0.; return 0.; }
+    const double radius = area / perimeter;
+    const double manning_radius = law == 2 ? pow(radius, 1. / 6.) : 0.;
+    for (int k = start; k < end; ++k) {
+        const int sl = slots[k], f = b.slot_face[sl], c = m.owner[f];
+        const double bed = b.ext_bed[sl], h0 = q[c], hi = fmax(h0 + z[c] - bed, 0.), h = fmax(eta - bed, 0.);
+        double face_rate = 0.;
+        if (h0 > dry && hi > dry) {
+            const double ui = (q[nc + c] * m.normal[f] + q[2 * nc + c] * m.normal[nf + f]) / h0;
+            if (ui >= sqrt(g * hi)) face_rate = ui * hi;
+            else {
+                const double invariant = fmax(ui + 2. * sqrt(g * hi), 0.), sonic = invariant * invariant / (9. * g);
+                if (h < sonic) face_rate = sonic * sqrt(g * sonic);
+                else if (h > dry) face_rate = h * fmax(rating_velocity(h, hi, ui, g), 0.);
+            }
+        }
+        rate += face_rate * m.length[f];
+        if (h <= dry) continue;
+        const double left = k == start ? 0. : fmax(eta - b.ext_bed[slots[k - 1]], 0.);
+        const double right = k + 1 == end ? 0. : fmax(eta - b.ext_bed[slots[k + 1]], 0.);
+        const double p = m.length[f] + fmax(h - left, 0.) + fmax(h - right, 0.);
+        const double C = law == 2 ? manning_radius / rough : nout_chezy(law, radius, rough, g);
+        drag += p / (C * C);
+    }
+    area_out = area; q_out = rate;
+    return rate - (drag > 0. ? area * sqrt(area * slope / drag) : 0.);
+}
+
+// 0, or the chain's failure (a trial rejection in the reference).
+__device__ int normal_chain(const MeshDev &m, const BoundaryDev &b, int ch, double g, double dry, double speed,
+                            int law, double rough, const double *q, const double *z, bool &bad)
+{
+    const int nc = m.nc, nf = m.nf;
+    const size_t ns = b.nslot;
+    const int *slots = b.chain_slot;
+    const double slope = b.chain_slope[ch];
+    int cursor = b.chain_off[ch];
+    const int stop = b.chain_off[ch + 1];
+    while (cursor < stop) {
+        const int fsl = slots[cursor], ff = b.slot_face[fsl], fc = m.owner[ff];
+        const double fh = q[fc], fgeom = fmax(fh + z[fc] - b.ext_bed[fsl], 0.);
+        if (fh <= dry || fgeom <= dry) {
+            const double pressure = fh > dry ? .5 * g * fh * fh : 0.;
+            b.trace[fsl] = 0.; b.trace[ns + fsl] = 0.; b.trace[2 * ns + fsl] = 0.;
+            b.flux[fsl] = 0.; b.flux[ns + fsl] = pressure * m.normal[ff]; b.flux[2 * ns + fsl] = pressure * m.normal[nf + ff];
+            ++cursor;
+            continue;
+        }
+        const int start = cursor;
+        while (cursor < stop) {
+            const int sl = slots[cursor], f = b.slot_face[sl], c = m.owner[f];
+            const double hh = q[c];
+            if (hh <= dry || hh + z[c] - b.ext_bed[sl] <= dry) break;
+            ++cursor;
+        }
+        const int end = cursor;
+        int wet = 0;
+        double lo = 1e300, hi = -1e300, area = 0., rate = 0.;
+        for (int k = start; k < end; ++k) {
+            const int sl = slots[k], f = b.slot_face[sl], c = m.owner[f];
+            const double h0 = q[c], hf = fmax(h0 + z[c] - b.ext_bed[sl], 0.);
+            if (h0 <= dry || hf <= dry) continue;
+            const double u = (q[nc + c] * m.normal[f] + q[2 * nc + c] * m.normal[nf + f]) / h0;
+            if (u >= sqrt(g * hf)) continue;
+            lo = fmin(lo, b.ext_bed[sl] + 2. * dry);
+            hi = fmax(hi, z[c] + h0);
+            ++wet;
+        }
+        double level = 0.;
+        bool fallback = false;
+        if (wet) {
+            hi = fmax(hi, lo + 1.);
+            double r = nout_residual(m, b, slots, start, end, lo, slope, g, dry, law, rough, q, z, area, rate);
+            if (!isfinite(r)) return 1;
+            if (r < 0.) fallback = true;           // supercritical normal flow: keep the outgoing trace
+            else {
+                double rh = nout_residual(m, b, slots, start, end, hi, slope, g, dry, law, rough, q, z, area, rate);
+                for (int it = 0; it < 60 && rh > 0.; ++it) {
+                    hi = lo + 2. * (hi - lo);
+                    rh = nout_residual(m, b, slots, start, end, hi, slope, g, dry, law, rough, q, z, area, rate);
+                }
+                if (!isfinite(rh) || rh > 0.) return 2;
+                for (int it = 0; it < 90; ++it) {
+                    const double mid = .5 * (lo + hi);
+                    if (mid == lo || mid == hi) break;
+                    r = nout_residual(m, b, slots, start, end, mid, slope, g, dry, law, rough, q, z, area, rate);
+                    if (r > 0.) lo = mid; else hi = mid;
+                }
+                level = .5 * (lo + hi);
+                r = nout_residual(m, b, slots, start, end, level, slope, g, dry, law, rough, q, z, area, rate);
+                if (!isfinite(r) || fabs(r) > 1e-10 * fmax(1., fabs(rate))) return 3;
+            }
+        }
+        for (int k = start; k < end; ++k) {
+            const int sl = slots[k], f = b.slot_face[sl], c = m.owner[f];
+            const double bed = b.ext_bed[sl], h0 = q[c], geom = fmax(h0 + z[c] - bed, 0.);
+            const double nx = m.normal[f], ny = m.normal[nf + f];
+            double ux = 0., uy = 0.;
+            if (h0 > dry) { ux = q[nc + c] / h0; uy = q[2 * nc + c] / h0; }
+            double un = ux * nx + uy * ny, h = geom;
+            const double tx = ux - un * nx, ty = uy - un * ny;
+            if (h0 <= dry || geom <= dry) { h = 0.; un = 0.; }
+            else if (fallback) { }
+            else if (un >= sqrt(g * geom)) { }
+            else {
+                const double incoming = un;
+                h = fmax(level - bed, 0.);
+                const double invariant = fmax(incoming + 2. * sqrt(g * geom), 0.), sonic = invariant * invariant / (9. * g);
+                if (h < sonic) { h = sonic; un = sqrt(g * sonic); }
+                else un = h > dry ? rating_velocity(h, geom, incoming, g) : 0.;
+                if (un <= 0.) {
+                    double left = dry, right = fmax(geom, 1.);
+                    for (int it = 0; it < 60 && rating_velocity(right, geom, incoming, g) > 0.; ++it) right *= 2.;
+                    for (int it = 0; it < 80; ++it) {
+                        const double mid = .5 * (left + right);
+                        if (rating_velocity(mid, geom, incoming, g) > 0.) left = mid; else right = mid;
+                    }
+                    h = .5 * (left + right);
+                    un = 0.;
+                }
+            }
+            if (!isfinite(h) || !isfinite(un) || sqrt(un * un + tx * tx + ty * ty) > speed) { bad = true; continue; }
+            double water = 0., fx = 0., fy = 0., t0 = 0., t1 = 0., t2 = 0.;
+            if (h > dry) {
+                t0 = h; t1 = h * (un * nx + tx); t2 = h * (un * ny + ty);
+                water = h * un;
+                fx = water * (un * nx + tx) + .5 * g * h * h * nx;
+                fy = water * (un * ny + ty) + .5 * g * h * h * ny;
+            }
+            const double pressure = h0 > dry ? .5 * g * (h0 * h0 - geom * geom) : 0.;
+            b.trace[sl] = t0; b.trace[ns + sl] = t1; b.trace[2 * ns + sl] = t2;
+            b.flux[sl] = water; b.flux[ns + sl] = fx + pressure * nx; b.flux[2 * ns + sl] = fy + pressure * ny;
+        }
+    }
+    return 0;
+}
+
 // stage 1 / 2: the SSPRK stages (state work / q1, its own stock, clock t or
 // t + dt); STAGE_HANCOCK: the HLLC predicted state q1 at t + dt/2, outlet
 // stock of the substep's start state work (hllc.py:91-97), status of stage 1.
@@ -399,14 +565,31 @@ __global__ void k_boundary(MeshDev m, StateDev s, BoundaryDev b, Ctrl *ctrl, int
         b.flux[k] = fl0; b.flux[(size_t)b.nslot + k] = fl1; b.flux[2 * (size_t)b.nslot + k] = fl2;
     }
     __syncthreads();
-    // section owners of the remaining outlet modes, after the face loop
-    // (river_exterior_bed.py:213-217); a section without a solution fails the scenario
-    for (int sg = s0 + threadIdx.x; sg < s1; sg += blockDim.x)
-        if (b.seg_mode[sg] == 11) {
+    // section owners of the remaining outlet modes, after the face loop, in
+    // the reference's order (river_exterior_bed.py:213-217): a normal-depth
+    // chain without a root rejects the trial before the rating owner runs; a
+    // rating section without a solution fails the scenario
+    __shared__ int section_reject;
+    if (threadIdx.x == 0) section_reject = 0;
+    __syncthreads();
+    if (b.scen_chain) {
+        const int law = ct.roughness_mode;
+        for (int ch = b.scen_chain[sid] + threadIdx.x; ch < b.scen_chain[sid + 1]; ch += blockDim.x) {
             bool sbad = false;
-            if (rating_section(m, b, sg, grav, dry, ct.speed_limit, q, z, sbad)) raise_status(ct, stage, ST_FATAL);
+            if (normal_chain(m, b, ch, grav, dry, ct.speed_limit, law, ct.roughness_value, q, z, sbad))
+                atomicOr(&section_reject, 1);
             if (sbad) bad = 1;
         }
+    }
+    __syncthreads();
+    if (!section_reject)
+        for (int sg = s0 + threadIdx.x; sg < s1; sg += blockDim.x)
+            if (b.seg_mode[sg] == 11) {
+                bool sbad = false;
+                if (rating_section(m, b, sg, grav, dry, ct.speed_limit, q, z, sbad)) raise_status(ct, stage, ST_FATAL);
+                if (sbad) bad = 1;
+            }
+    if (section_reject) bad = 1;
     if (bad) raise_status(ct, stage, ST_SPATIAL);
     __syncthreads();
     // outlet stock cap, one thread per unique owner, its faces in boundary order

@@ -167,6 +167,70 @@ def build_mesh(points, tri, segment_of_edge):
                 boundary_offset=np.asarray(boff, dtype=np.int32), boundary_faces=boundary_faces)
 
 
+def opening_chains(mesh: Mesh, segment: int):
+    """Ordered face chains of one open segment (connected runs of its faces).
+
+    Two faces of the segment are linked when an end point of one meets an end
+    point of the other (within 128 ulp of the coordinate scale, at least
+    1e-10) and their owners are the same or neighbouring cells; each chain
+    starts at its end face with the smallest face number and walks the links
+    (the section order of river_boundary_components.connected_opening_chains,
+    src/braids_core/sediment/river_boundary_components.py:11-56).
+    """
+    from scipy.spatial import cKDTree
+    owner, neighbour = mesh.owner, mesh.neighbour
+    ids = np.flatnonzero((neighbour < 0) & (mesh.bid == segment))
+    if not len(ids):
+        raise ValueError("segment has no open faces")
+    nx, ny = mesh.normal[0, ids], mesh.normal[1, ids]
+    tangent = np.stack((-ny, nx), axis=1)
+    centre = mesh.mid[:, ids].T
+    half = .5 * mesh.length[ids, None] * tangent
+    ends = np.empty((2 * len(ids), 2))
+    ends[0::2] = centre - half
+    ends[1::2] = centre + half
+    scale = max(1., float(np.max(np.abs(ends))))
+    tol = max(1e-10, 128 * np.spacing(scale))
+    inner = neighbour >= 0
+    linked = set(zip(np.minimum(owner[inner], neighbour[inner]).tolist(),
+                     np.maximum(owner[inner], neighbour[inner]).tolist()))
+    adj = [set() for _ in ids]
+    for a, b in sorted(cKDTree(ends).query_pairs(tol)):
+        i, j = a // 2, b // 2
+        if i == j:
+            raise ValueError("degenerate open face")
+        oi, oj = int(owner[ids[i]]), int(owner[ids[j]])
+        if oi == oj or (min(oi, oj), max(oi, oj)) in linked:
+            adj[i].add(j)
+            adj[j].add(i)
+    if any(len(a) > 2 for a in adj):
+        raise ValueError("a branched opening needs explicit boundary sections")
+    left, chains = set(range(len(ids))), []
+    while left:
+        seed = min(left, key=lambda i: int(ids[i]))
+        stack, comp = [seed], set()
+        while stack:
+            i = stack.pop()
+            if i not in comp:
+                comp.add(i)
+                stack.extend(adj[i] - comp)
+        tips = [i for i in comp if len(adj[i]) <= 1]
+        if not tips:
+            raise ValueError("a closed opening is not a section")
+        at, prev, order = min(tips, key=lambda i: int(ids[i])), -1, []
+        while True:
+            order.append(int(ids[at]))
+            left.discard(at)
+            nxt = adj[at] - {prev}
+            if not nxt:
+                break
+            prev, at = at, next(iter(nxt))
+        if len(order) != len(comp):
+            raise ValueError("could not order the opening")
+        chains.append(order)
+    return chains
+
+
 def geometry_records(mesh: Mesh):
     """Least-squares stencil geometry cached per CSR entry and face side.
 

@@ -245,6 +245,17 @@ def rating_channel(discharge=20.0, knots=((0.0, 2.0), (10.0, 2.6), (20.0, 3.0), 
     return case
 
 
+def normal_channel(discharge=20.0, bed_slope=2e-3, **kw):
+    """The small channel with a normal-depth outlet (mode 10): per connected
+    chain of outlet faces, the level of uniform flow at `bed_slope` with the
+    channel's Manning roughness."""
+    case = small_channel(discharge=discharge, **kw)
+    case["seg_mode"] = np.array([M.MODE_TOTAL_Q, 10], np.int32)
+    case["outlet"] = {1: {"bed_slope": float(bed_slope)}}
+    case["name"] = "normal_channel"
+    return case
+
+
 def lake_at_rest(length=80.0, width=40.0, spacing=4.0, seed=11, islands=True):
     """Variable bed with emerged islands, flat surface at 1.0 m, closed walls (no open segments)."""
     mesh = M.channel_mesh(length, width, spacing, 1.0, seed)
@@ -339,6 +350,9 @@ def case_arrays(case):
         out[f"ctl_{k}"] = np.asarray(v)
     for b, knots in (case.get("rating") or {}).items():
         out[f"rating_{int(b)}"] = np.asarray(knots, dtype=np.float64)
+    for b, params in (case.get("outlet") or {}).items():
+        for name, value in params.items():
+            out[f"outlet_{int(b)}_{name}"] = np.asarray(value, dtype=np.float64)
     return out
 
 
@@ -353,6 +367,13 @@ def case_from_arrays(arrs):
     rating = {int(k[7:]): [tuple(r) for r in np.asarray(v)] for k, v in arrs.items() if k.startswith("rating_")}
     if rating:
         case["rating"] = rating
+    outlet = {}
+    for k, v in arrs.items():
+        if k.startswith("outlet_"):
+            seg, name = k[7:].split("_", 1)
+            outlet.setdefault(int(seg), {})[name] = float(np.asarray(v))
+    if outlet:
+        case["outlet"] = outlet
     return case
 
 

@@ -72,6 +72,30 @@ def rating_tables(cases):
             np.asarray(re_ if re_ else [0.0], np.float64))
 
 
+def normal_chains(cases, face_offset=None):
+    """Face chains of the normal-depth outlets (mode 10) of a batch, in
+    scenario and segment order: (offset (nchain+1), faces (global ids), bed
+    slope per chain). case["outlet"][segment]["bed_slope"] is the slope that
+    stands in for the energy slope (river_normal_outlet.py:20-27)."""
+    from .mesh import opening_chains
+    off, faces, slopes = [0], [], []
+    for i, case in enumerate(cases):
+        F0 = 0 if face_offset is None else int(face_offset[i])
+        modes = np.asarray(case.get("seg_mode", np.zeros(0)), dtype=int)
+        for b in range(case["mesh"].nb):
+            if modes[b] != 10:
+                continue
+            slope = float((case.get("outlet") or {}).get(b, {}).get("bed_slope", 0.0))
+            if not slope > 0:
+                raise ValueError(f"normal-depth outlet segment {b} needs a positive bed_slope")
+            for chain in opening_chains(case["mesh"], b):
+                faces.extend(int(f) + F0 for f in chain)
+                off.append(len(faces))
+                slopes.append(slope)
+    return (np.asarray(off, np.int32), np.asarray(faces if faces else [0], np.int32),
+            np.asarray(slopes, np.float64))
+
+
 def pack(cases):
     """Concatenate scenario meshes into one global index space."""
     out = {k: [] for k in ("owner", "neighbour", "bid", "offset", "faces", "signs", "normal", "length", "area",
@@ -165,6 +189,9 @@ class RiverSolver:
             if np.any(p["seg_mode"] == 11):
                 off, rq, re_ = rating_tables(self.cases)
                 check(self.lib.brx_rating_set(self.h, _ptr(off), _ptr(rq), _ptr(re_)))
+            if np.any(p["seg_mode"] == 10):
+                off, faces, slope = normal_chains(self.cases, p["face_offset"])
+                check(self.lib.brx_outlet_chains_set(self.h, len(slope), _ptr(off), _ptr(faces), _ptr(slope)))
             check(self.lib.brx_boundary_set(self.h, _ptr(p["seg_mode"]), _ptr(p["stage_policy"]),
                                             _ptr(p["exterior_bed"]), _ptr(p["forcing"])))
         else:

@@ -97,8 +97,18 @@ int brx_controls_set(brx_solver *s, int scen, double gravity, double dry, double
  * brx_boundary_set when any segment has mode 11. */
 int brx_rating_set(brx_solver *s, const int *offset, const double *discharge, const double *elevation);
 
+/* Connected face chains of the normal-depth outlets (mode 10): chain c's
+ * faces (global ids, in section order) are faces[offset[c] .. offset[c+1]-1],
+ * its bed slope slope[c] (the reference's NormalOutlet sections,
+ * src/braids_core/sediment/river_normal_outlet.py:16-27, ordered by
+ * connected_opening_chains). Chains in scenario order. Host arrays, copied;
+ * call before brx_boundary_set when any segment has mode 10. */
+int brx_outlet_chains_set(brx_solver *s, int nchain, const int *offset, const int *faces, const double *slope);
+
 /* Open-boundary set-up for all segments: hydraulic mode (2 stage, 3 free
- * outflow, 6 total discharge, 9 discharge + water line, 11 Q-H rating
+ * outflow, 6 total discharge, 9 discharge + water line, 10 normal depth:
+ * per face chain the level at which the outgoing characteristic discharge
+ * equals the uniform-flow conveyance, river_normal_outlet.h; 11 Q-H rating
  * curve: one common water elevation at which the outgoing characteristic
  * discharge equals the curve, river_rating_outlet.h), stage reversal
  * policy, exterior bed per face (nf, read on open faces) and forcing (2,nseg)

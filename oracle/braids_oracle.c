@@ -90,6 +90,11 @@ typedef struct {
      * rating_offset[b] .. rating_offset[b+1]-1 (elevation increasing) */
     const int *rating_offset;                      /* (nb+1) or NULL */
     const double *rating_q, *rating_eta;
+    /* normal-depth outlets (mode 10): connected face chains of their
+     * segments, in segment order, each with its bed slope */
+    int nchain;
+    const int *chain_offset, *chain_face;          /* (nchain+1), faces */
+    const double *chain_slope;                     /* (nchain) */
 } om_ctx;
 
 /* ------------------------------------------------------------------ */
@@ -935,6 +940,173 @@ static int om_rating_outlet(const om_ctx *m, int b, const double *q, const doubl
     return 0;
 }
 
+/* ------------------------------------------------------------------ */
+/* Normal-depth outlet (mode 10): per connected face chain, the section  */
+/* level at which the outgoing characteristic discharge equals the       */
+/* uniform-flow conveyance at the chain's bed slope                      */
+/* (src/braids_core/sediment/river_normal_outlet.h:17-134).              */
+/* ------------------------------------------------------------------ */
+static double om_nout_chezy(int law, double r, double value, double g)
+{
+    if (law == 1) return value;
+    if (law == 2) return pow(r, 1. / 6.) / value;
+    if (law == 3) return sqrt(g) / .41 * log1p(30. * r / (exp(1.) * value));
+    return 18. * log10(12. * fmax(.5, r / value));
+}
+
+static double om_nout_residual(const om_ctx *m, const int *faces, int start, int end, double eta, double slope,
+                               const double *q, const double *z, double *area_out, double *q_out)
+{
+    const int nc = m->nc, nf = m->nf, law = m->roughness_mode;
+    const double g = m->grav, dry = m->dry, *bed = m->exterior_bed;
+    double area = 0., perimeter = 0., rate = 0., drag = 0., prev = 0.;
+    for (int k = start; k < end; ++k) {
+        const int f = faces[k];
+        const double h = fmax(eta - bed[f], 0.);
+        area += h * m->length[f];
+        perimeter += h > dry ? m->length[f] : 0.;
+        if (k == start) perimeter += h; else perimeter += fabs(h - prev);
+        prev = h;
+    }
+    perimeter += prev;
+    if (area <= 0. || perimeter <= 0.) { *area_out = 0.; *q_out = 0.; return 0.; }
+    const double radius = area / perimeter;
+    const double manning_radius = law == 2 ? pow(radius, 1. / 6.) : 0.;
+    for (int k = start; k < end; ++k) {
+        const int f = faces[k], c = m->owner[f];
+        const double h0 = q[c], hi = fmax(h0 + z[c] - bed[f], 0.), h = fmax(eta - bed[f], 0.);
+        double face_rate = 0.;
+        if (h0 > dry && hi > dry) {
+            const double ui = (q[nc + c] * m->normal[f] + q[2 * nc + c] * m->normal[nf + f]) / h0;
+            if (ui >= sqrt(g * hi)) face_rate = ui * hi;
+            else {
+                const double invariant = fmax(ui + 2. * sqrt(g * hi), 0.), sonic = invariant * invariant / (9. * g);
+                if (h < sonic) face_rate = sonic * sqrt(g * sonic);
+                else if (h > dry) face_rate = h * fmax(om_rating_velocity(h, hi, ui, g), 0.);
+            }
+        }
+        rate += face_rate * m->length[f];
+        if (h <= dry) continue;
+        const double left = k == start ? 0. : fmax(eta - bed[faces[k - 1]], 0.);
+        const double right = k + 1 == end ? 0. : fmax(eta - bed[faces[k + 1]], 0.);
+        const double p = m->length[f] + fmax(h - left, 0.) + fmax(h - right, 0.);
+        const double C = law == 2 ? manning_radius / m->roughness_value
+                                  : om_nout_chezy(law, radius, m->roughness_value, g);
+        drag += p / (C * C);
+    }
+    *area_out = area; *q_out = rate;
+    return rate - (drag > 0. ? area * sqrt(area * slope / drag) : 0.);
+}
+
+/* One chain; 0 or the section failure (a trial rejection in the reference). */
+static int om_normal_chain(const om_ctx *m, int ch, const double *q, const double *z, double *trace, double *flux,
+                           int *status)
+{
+    const int nc = m->nc, nf = m->nf;
+    const double g = m->grav, dry = m->dry, speed = m->speed_limit, *bed = m->exterior_bed;
+    const int *faces = m->chain_face;
+    const double slope = m->chain_slope[ch];
+    int cursor = m->chain_offset[ch];
+    const int stop = m->chain_offset[ch + 1];
+    while (cursor < stop) {
+        const int ff = faces[cursor], fc = m->owner[ff];
+        const double fh = q[fc], fgeom = fmax(fh + z[fc] - bed[ff], 0.);
+        if (fh <= dry || fgeom <= dry) {          /* a dry face closes with its owner's pressure */
+            trace[ff] = trace[nf + ff] = trace[2 * nf + ff] = 0.;
+            flux[ff] = 0.;
+            const double pressure = fh > dry ? .5 * g * fh * fh : 0.;
+            flux[nf + ff] = pressure * m->normal[ff]; flux[2 * nf + ff] = pressure * m->normal[nf + ff];
+            ++cursor;
+            continue;
+        }
+        const int start = cursor;
+        while (cursor < stop) {
+            const int f = faces[cursor], c = m->owner[f];
+            const double hh = q[c];
+            if (hh <= dry || hh + z[c] - bed[f] <= dry) break;
+            ++cursor;
+        }
+        const int end = cursor;
+        int wet = 0;
+        double lo = 1e300, hi = -1e300, area = 0., rate = 0.;
+        for (int k = start; k < end; ++k) {
+            const int f = faces[k], c = m->owner[f];
+            const double h0 = q[c], hf = fmax(h0 + z[c] - bed[f], 0.);
+            if (h0 <= dry || hf <= dry) continue;
+            const double u = (q[nc + c] * m->normal[f] + q[2 * nc + c] * m->normal[nf + f]) / h0;
+            if (u >= sqrt(g * hf)) continue;
+            lo = fmin(lo, bed[f] + 2. * dry);
+            hi = fmax(hi, z[c] + h0);
+            ++wet;
+        }
+        double level = 0.;
+        int fallback = 0;
+        if (wet) {
+            hi = fmax(hi, lo + 1.);
+            double r = om_nout_residual(m, faces, start, end, lo, slope, q, z, &area, &rate);
+            if (!isfinite(r)) return 1;
+            if (r < 0.) fallback = 1;             /* supercritical normal flow: keep the outgoing trace */
+            else {
+                double rh = om_nout_residual(m, faces, start, end, hi, slope, q, z, &area, &rate);
+                for (int it = 0; it < 60 && rh > 0.; ++it) {
+                    hi = lo + 2. * (hi - lo);
+                    rh = om_nout_residual(m, faces, start, end, hi, slope, q, z, &area, &rate);
+                }
+                if (!isfinite(rh) || rh > 0.) return 2;
+                for (int it = 0; it < 90; ++it) {
+                    const double mid = .5 * (lo + hi);
+                    if (mid == lo || mid == hi) break;
+                    r = om_nout_residual(m, faces, start, end, mid, slope, q, z, &area, &rate);
+                    if (r > 0.) lo = mid; else hi = mid;
+                }
+                level = .5 * (lo + hi);
+                r = om_nout_residual(m, faces, start, end, level, slope, q, z, &area, &rate);
+                if (!isfinite(r) || fabs(r) > 1e-10 * fmax(1., fabs(rate))) return 3;
+            }
+        }
+        for (int k = start; k < end; ++k) {
+            const int f = faces[k], c = m->owner[f];
+            const double h0 = q[c], geom = fmax(h0 + z[c] - bed[f], 0.);
+            const double nx = m->normal[f], ny = m->normal[nf + f];
+            double ux = 0., uy = 0.;
+            if (h0 > dry) { ux = q[nc + c] / h0; uy = q[2 * nc + c] / h0; }
+            double un = ux * nx + uy * ny, h = geom;
+            const double tx = ux - un * nx, ty = uy - un * ny;
+            if (h0 <= dry || geom <= dry) { h = 0.; un = 0.; }
+            else if (fallback) { }
+            else if (un >= sqrt(g * geom)) { }
+            else {
+                const double incoming = un;
+                h = fmax(level - bed[f], 0.);
+                const double invariant = fmax(incoming + 2. * sqrt(g * geom), 0.), sonic = invariant * invariant / (9. * g);
+                if (h < sonic) { h = sonic; un = sqrt(g * sonic); }
+                else un = h > dry ? om_rating_velocity(h, geom, incoming, g) : 0.;
+                if (un <= 0.) {
+                    double left = dry, right = fmax(geom, 1.);
+                    for (int it = 0; it < 60 && om_rating_velocity(right, geom, incoming, g) > 0.; ++it) right *= 2.;
+                    for (int it = 0; it < 80; ++it) {
+                        const double mid = .5 * (left + right);
+                        if (om_rating_velocity(mid, geom, incoming, g) > 0.) left = mid; else right = mid;
+                    }
+                    h = .5 * (left + right);
+                    un = 0.;
+                }
+            }
+            if (!isfinite(h) || !isfinite(un) || sqrt(un * un + tx * tx + ty * ty) > speed) { status[f] = 3; continue; }
+            double water = 0., fx = 0., fy = 0.;
+            if (h > dry) {
+                trace[f] = h; trace[nf + f] = h * (un * nx + tx); trace[2 * nf + f] = h * (un * ny + ty);
+                water = h * un;
+                fx = water * (un * nx + tx) + .5 * g * h * h * nx;
+                fy = water * (un * ny + ty) + .5 * g * h * h * ny;
+            } else trace[f] = trace[nf + f] = trace[2 * nf + f] = 0.;
+            const double pressure = h0 > dry ? .5 * g * (h0 * h0 - geom * geom) : 0.;
+            flux[f] = water; flux[nf + f] = fx + pressure * nx; flux[2 * nf + f] = fy + pressure * ny;
+        }
+    }
+    return 0;
+}
+
 int om_exterior(om_ctx *m, const double *q, const double *z, double time,
                 double *trace, double *flux, int *status, double *work,
                 double *stage_out, double *total_out)
@@ -1036,7 +1208,13 @@ int om_exterior(om_ctx *m, const double *q, const double *z, double time,
         if (mode == 9 && h <= dry) pressure = h0 > dry ? .5 * gravity * h0 * h0 : 0.;
         flux[i] = water; flux[nf + i] = fx + pressure * nx; flux[2 * nf + i] = fy + pressure * ny;
     }
-    /* section owners of the remaining outlet modes (river_exterior_bed.py:213-217) */
+    /* section owners of the remaining outlet modes, in the reference's order
+     * (river_exterior_bed.py:213-217): a normal-depth failure rejects the
+     * trial before the rating owner runs; a rating failure is fatal */
+    int normal_failed = 0;
+    for (int ch = 0; ch < m->nchain; ++ch)
+        if (om_normal_chain(m, ch, q, z, trace, flux, status)) normal_failed = 1;
+    if (normal_failed) return OM_REJECT_SPATIAL;
     for (int b = 0; b < nb; ++b)
         if (m->seg_mode[b] == 11 && om_rating_outlet(m, b, q, z, trace, flux, status)) return OM_EXTERIOR_FATAL;
     if (!first)

@@ -60,7 +60,8 @@ class Ctx(C.Structure):
                 ("roughness_mode", I), ("roughness_value", D),
                 ("seg_mode", P), ("stage_policy", P), ("exterior_bed", P), ("forcing", P),
                 ("table_len", I), ("table_time", P), ("table_value", P), ("threads", I),
-                ("turb", P), ("rating_offset", P), ("rating_q", P), ("rating_eta", P)]
+                ("turb", P), ("rating_offset", P), ("rating_q", P), ("rating_eta", P),
+                ("nchain", I), ("chain_offset", P), ("chain_face", P), ("chain_slope", P)]
 
 
 class Turbines(C.Structure):
@@ -215,6 +216,13 @@ class Oracle:
             ctx.table_time = k("table_time", _f64(tt))
             ctx.table_value = k("table_value", _f64(case["table_value"]))
         ctx.threads = threads or 0
+        if nb and np.any(seg_mode == 10):
+            from braids_hkt_gb300.solver import normal_chains
+            off, faces, slope = normal_chains([case])
+            ctx.nchain = len(slope)
+            ctx.chain_offset = k("chain_offset", _i32(off))
+            ctx.chain_face = k("chain_face", _i32(faces))
+            ctx.chain_slope = k("chain_slope", _f64(slope))
         if case.get("rating"):
             from braids_hkt_gb300.solver import rating_tables
             off, rq, re_ = rating_tables([case])

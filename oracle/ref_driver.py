@@ -427,6 +427,29 @@ class Ref:
                   g["owner"], g["bid"], g["selected"], self.seg_mode, self.stage_policy, q, self.z,
                   self.exterior_bed, g["normal"], g["length"], self.forcing, weights, total, trace, flux, status)
         # section owners after exterior_flux (ExteriorBed.evaluate, river_exterior_bed.py:213-217)
+        if np.any(self.seg_mode[:nb] == 10):
+            from braids_core.sediment.river_boundary_components import connected_opening_chains
+            if "ref_normal" not in self.libs:
+                self.libs["ref_normal"] = C.CDLL(str(REF / "libref_normal.so"))
+                self.libs["ref_normal"].mobile_threads(C.c_int(os.cpu_count() or 1))
+            m = self.m
+            data = dict(owner=m.owner, neighbour=m.neighbour, bid=m.bid, mid=m.mid, normal=m.normal, length=m.length)
+            chains, slopes = [], []
+            for b in range(nb):
+                if self.seg_mode[b] == 10:
+                    for chain in connected_opening_chains(data, b):
+                        chains.append(chain)
+                        slopes.append(self.case["outlet"][b]["bed_slope"])
+            off = np.ascontiguousarray(np.cumsum([0] + [len(c) for c in chains]), dtype=np.int32)
+            cf = np.ascontiguousarray([f for c in chains for f in c], dtype=np.int32)
+            cnt = len(chains)
+            sec, trans = np.zeros(cnt, np.int32), np.zeros(cnt, np.int32)
+            self.call("ref_normal", "normal_outlet", 0, nf, n, cnt, self.grav, self.dry, self.speed_limit, int(self.rmode),
+                      off, cf, g["owner"], q, self.z, self.exterior_bed, g["normal"], g["length"], self.roughness,
+                      np.ascontiguousarray(slopes, dtype=np.float64), np.zeros(cnt), np.zeros((2, cnt)), trace, flux,
+                      status, sec, trans)
+            if np.any(sec):
+                raise Rejected("normal-depth outlet has no admissible subcritical section root")
         if np.any(self.seg_mode[:nb] == 11):
             from braids_hkt_gb300.solver import rating_tables
             if "ref_rating" not in self.libs:

@@ -137,3 +137,22 @@ def test_rating_outlet_without_a_bracket_fails():
     o = Oracle(case, threads=2)
     st, _, _ = o.advance(case["q"].copy(), 1.0, 0.0)
     assert st == 4
+
+
+def test_normal_depth_outlet_drains_towards_uniform_flow():
+    """Normal-depth outlet (mode 10): the channel, filled to 3 m over its
+    uniform-flow depth for the inflow, drains through the outlet with a
+    discharge falling towards the inflow while staying above it."""
+    case = S.normal_channel()
+    o = Oracle(case, threads=4)
+    q = case["q"].copy()
+    m = case["mesh"]
+    outlet = (m.neighbour < 0) & (m.bid == 1)
+    st, _, _ = o.advance(q, 30.0, 0.0)          # past the first drawdown wave
+    assert st == 0
+    flows = []
+    for k in range(3):
+        st, water, _ = o.advance(q, 10.0, 30.0 + 10.0 * k)
+        assert st == 0
+        flows.append(float(np.sum(water[outlet] * m.length[outlet])))
+    assert flows[0] > flows[1] > flows[2] > 20.0
