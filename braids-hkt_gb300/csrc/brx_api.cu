@@ -473,8 +473,10 @@ extern "C" int brx_boundary_set(brx_solver *s, const int *seg_mode, const int *s
     if (!seg_mode || !stage_policy || !exterior_bed || !forcing) return fail(BRX_ERR_ARGUMENT, "null boundary array");
     for (int sg = 0; sg < nseg; ++sg) {
         const int md = seg_mode[sg];
-        if (md != 2 && md != 3 && md != 6 && md != 9 && md != 10 && md != 11)
-            return fail(BRX_ERR_UNSUPPORTED, "open-boundary mode must be 2, 3, 6, 9, 10 or 11");
+        if (md != 2 && md != 3 && md != 5 && md != 6 && md != 9 && md != 10 && md != 11)
+            return fail(BRX_ERR_UNSUPPORTED, "open-boundary mode must be 2, 3, 5, 6, 9, 10 or 11");
+        if (md == 5 && !s->bnd.weir)
+            return fail(BRX_ERR_STATE, "a free-weir outlet (mode 5) needs its parameters first (brx_weir_set)");
         if (md == 10 && !s->chains_ready)
             return fail(BRX_ERR_STATE, "a normal-depth outlet (mode 10) needs its face chains first (brx_outlet_chains_set)");
         if (md == 11 && (!s->rating_ready || s->h_rating_off[sg + 1] - s->h_rating_off[sg] < 2))
@@ -512,6 +514,15 @@ extern "C" int brx_boundary_set(brx_solver *s, const int *seg_mode, const int *s
         CK(cudaMemcpy(s->d_ccls, s->h_ccls.data(), sizeof(int) * s->nc, cudaMemcpyHostToDevice));
     }
     s->boundary_ready = true;
+    return BRX_OK;
+}
+
+// Per-slot scratch of the 128-lane section solves (face branch, invariant).
+static int ensure_section_scratch(brx_solver *s)
+{
+    if (s->bnd.branch) return BRX_OK;
+    TRY(s->alloc(&s->bnd.branch, std::max(s->nslot, 1)));
+    TRY(s->alloc(&s->bnd.invariant, std::max(s->nslot, 1)));
     return BRX_OK;
 }
 
@@ -578,6 +589,23 @@ extern "C" int brx_outlet_chains_set(brx_solver *s, int nchain, const int *offse
     TRY(s->upload(&p_slot, slot.data(), slot.size())); TRY(s->upload(&p_slope, slope, nchain));
     s->bnd.scen_chain = p_scen; s->bnd.chain_off = p_off; s->bnd.chain_slot = p_slot; s->bnd.chain_slope = p_slope;
     s->chains_ready = true;
+    s->graph_dirty = true;
+    return BRX_OK;
+}
+
+extern "C" int brx_weir_set(brx_solver *s, const double *param)
+{
+    if (!s) return fail(BRX_ERR_ARGUMENT, "null solver");
+    if (!param) return fail(BRX_ERR_ARGUMENT, "null weir parameters");
+    if (s->bnd.weir) return fail(BRX_ERR_STATE, "weir parameters are already installed");
+    const int nseg = s->nseg;
+    if (nseg == 0) return fail(BRX_ERR_ARGUMENT, "no open segments");
+    for (int i = 0; i < 3 * nseg; ++i)
+        if (!std::isfinite(param[i])) return fail(BRX_ERR_ARGUMENT, "weir parameters must be finite");
+    double *p_w;
+    TRY(s->upload(&p_w, param, 3 * (size_t)nseg));
+    TRY(ensure_section_scratch(s));
+    s->bnd.weir = p_w;
     s->graph_dirty = true;
     return BRX_OK;
 }

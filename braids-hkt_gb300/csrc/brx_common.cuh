@@ -174,6 +174,9 @@ struct BoundaryDev {
     const int *scen_chain;   // (nscen+1) normal-depth outlet chains per scenario
     const int *chain_off, *chain_slot;   // (nchain+1), slots in section order
     const double *chain_slope;           // (nchain)
+    const double *weir;      // (3, nseg) free-weir crest, coefficient, effective width
+    int *branch;             // (nslot) section-solve scratch: face branch
+    double *invariant;       // (nslot) section-solve scratch: outgoing invariant / normal speed
 };
 
 // Accepted / stage state buffers.

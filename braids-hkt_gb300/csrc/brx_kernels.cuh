@@ -421,6 +421,204 @@ __device__ int normal_chain(const MeshDev &m, const BoundaryDev &b, int ch, doub
     return 0;
 }
 
+// ---------------------------------------------------------------------------
+// Section solves with 128 logical lanes (river_exterior_outlet.h): the whole
+// boundary CTA works on one section; lane l (threads 0..127) sums entries
+// l, l+128, ... of the section and thread 0 adds the lane sums in lane order,
+// the order of the reference's OpenMP and CUDA forms. Every thread of the
+// CTA calls these functions (they synchronise the block).
+// ---------------------------------------------------------------------------
+constexpr int SECTION_LANES = 128;
+
+struct SectionWork {
+    double part[3][SECTION_LANES];
+    double lo, hi, eta, residual, area, width, rate;
+    int error, done, stagnant, changed, count;
+};
+
+__device__ __forceinline__ double weir_velocity(double h, double hi, double ui, double g)
+{
+    return h > hi ? ui - (h - hi) * sqrt(.5 * g * (1. / h + 1. / hi)) : ui + 2. * (sqrt(g * hi) - sqrt(g * h));
+}
+
+// river_exterior_outlet.h:207-227
+__device__ void weir_residual(SectionWork &w, const MeshDev &m, const BoundaryDev &b, int k0, int k1, double eta,
+                              double g, double dry, double crest, double factor, const double *q, const double *z)
+{
+    for (int lane = threadIdx.x; lane < SECTION_LANES; lane += blockDim.x) {
+        double area = 0., width = 0., rate = 0.;
+        for (int k = k0 + lane; k < k1; k += SECTION_LANES) {
+            if (!b.branch[k]) continue;
+            const int f = b.slot_face[k], c = m.owner[f];
+            const double bed = b.ext_bed[k], h = fmax(eta - bed, 0.), hi = fmax(q[c] + z[c] - bed, 0.);
+            if (h <= dry) continue;
+            const double u = fmax(weir_velocity(h, hi, b.invariant[k], g), 0.);
+            if (u > 0.) { area += h * m.length[f]; width += m.length[f]; rate += h * u * m.length[f]; }
+        }
+        w.part[0][lane] = area; w.part[1][lane] = width; w.part[2][lane] = rate;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        w.area = w.width = w.rate = 0.;
+        for (int lane = 0; lane < SECTION_LANES; ++lane) {
+            w.area += w.part[0][lane]; w.width += w.part[1][lane]; w.rate += w.part[2][lane];
+        }
+        const double head = fmax(eta - crest, 0.);
+        w.residual = w.rate - factor * head * sqrt(head);
+    }
+    __syncthreads();
+}
+
+// Free weir on segment sg (river_exterior_outlet.h:229-360): the common
+// subcritical stage at which the outgoing Lax-curve discharge equals
+// coefficient x width x head^1.5. Returns 0 or the section failure (a trial
+// rejection in the reference); `bad` gets the speed-limit face status.
+__device__ int weir_section(SectionWork &w, const MeshDev &m, const BoundaryDev &b, int sg, double g, double dry,
+                            double speed, const double *q, const double *z, bool &bad)
+{
+    const int nc = m.nc, nf = m.nf, nseg = b.nseg, k0 = b.seg_off[sg], k1 = b.seg_off[sg + 1];
+    const size_t ns = b.nslot;
+    const double tol = 128. * EPS, crest = b.weir[sg], factor = b.weir[nseg + sg] * b.weir[2 * nseg + sg];
+    if (threadIdx.x == 0) { w.error = 0; w.done = 0; w.eta = 0.; w.area = w.width = w.rate = 0.; }
+    for (int lane = threadIdx.x; lane < SECTION_LANES; lane += blockDim.x) {
+        double width = 0.;
+        for (int k = k0 + lane; k < k1; k += SECTION_LANES) {
+            const int f = b.slot_face[k], c = m.owner[f];
+            b.branch[k] = 0; b.invariant[k] = 0.;
+            const double h0 = q[c], h = fmax(h0 + z[c] - b.ext_bed[k], 0.);
+            if (h0 <= dry || h <= dry) continue;
+            const double un = (q[nc + c] * m.normal[f] + q[2 * nc + c] * m.normal[nf + f]) / h0;
+            b.branch[k] = 1; b.invariant[k] = un; width += m.length[f];
+        }
+        w.part[1][lane] = width;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double width = 0.;
+        for (int lane = 0; lane < SECTION_LANES; ++lane) width += w.part[1][lane];
+        if (width == 0.) w.done = 1;
+    }
+    __syncthreads();
+    if (w.done) {
+        for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) b.branch[k] = 0;
+        __syncthreads();
+    } else {
+        for (int lane = threadIdx.x; lane < SECTION_LANES; lane += blockDim.x) {
+            double lo = -INFINITY, hi = -INFINITY;
+            for (int k = k0 + lane; k < k1; k += SECTION_LANES) {
+                if (b.branch[k] != 1) continue;
+                const int c = m.owner[b.slot_face[k]];
+                const double h0 = fmax(q[c] + z[c] - b.ext_bed[k], 0.), u = b.invariant[k];
+                double left = 0., right = fmax(h0, 1.);
+                for (int it = 0; it < 60 && weir_velocity(right, h0, u, g) > sqrt(g * right); ++it) right *= 2.;
+                for (int it = 0; it < 70; ++it) {
+                    const double mid = .5 * (left + right);
+                    if (weir_velocity(mid, h0, u, g) > sqrt(g * mid)) left = mid; else right = mid;
+                }
+                lo = fmax(lo, b.ext_bed[k] + right);
+                hi = fmax(hi, q[c] + z[c]);
+            }
+            w.part[0][lane] = lo; w.part[1][lane] = hi;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            w.lo = -INFINITY; w.hi = -INFINITY;
+            for (int lane = 0; lane < SECTION_LANES; ++lane) { w.lo = fmax(w.lo, w.part[0][lane]); w.hi = fmax(w.hi, w.part[1][lane]); }
+            w.lo = fmax(w.lo, crest);
+            w.hi = fmax(w.hi, w.lo + 1.);
+        }
+        __syncthreads();
+        weir_residual(w, m, b, k0, k1, w.lo, g, dry, crest, factor, q, z);
+        if (threadIdx.x == 0 && (w.residual < 0. || !isfinite(w.residual))) w.error = 1;
+        __syncthreads();
+        if (!w.error) {
+            weir_residual(w, m, b, k0, k1, w.hi, g, dry, crest, factor, q, z);
+            for (int j = 0; j < 60 && w.residual > 0.; ++j) {
+                if (threadIdx.x == 0) w.hi = w.lo + 2. * (w.hi - w.lo);
+                __syncthreads();
+                weir_residual(w, m, b, k0, k1, w.hi, g, dry, crest, factor, q, z);
+            }
+            if (threadIdx.x == 0 && (w.residual > 0. || !isfinite(w.residual))) w.error = 1;
+            __syncthreads();
+        }
+        if (!w.error) {
+            for (int j = 0; j < 90; ++j) {
+                if (threadIdx.x == 0) { w.eta = w.lo + .5 * (w.hi - w.lo); w.stagnant = w.eta == w.lo || w.eta == w.hi; }
+                __syncthreads();
+                if (w.stagnant) break;
+                weir_residual(w, m, b, k0, k1, w.eta, g, dry, crest, factor, q, z);
+                if (threadIdx.x == 0) { if (w.residual > 0.) w.lo = w.eta; else w.hi = w.eta; }
+                __syncthreads();
+            }
+            if (threadIdx.x == 0) w.eta = w.lo + .5 * (w.hi - w.lo);
+            __syncthreads();
+            weir_residual(w, m, b, k0, k1, w.eta, g, dry, crest, factor, q, z);
+            if (threadIdx.x == 0) {
+                const double head = fmax(w.eta - crest, 0.), requested = factor * head * sqrt(head);
+                if (!isfinite(w.residual) || fabs(w.residual) > 1e-10 * fmax(requested, 1.)) w.error = 2;
+            }
+            __syncthreads();
+            for (int lane = threadIdx.x; lane < SECTION_LANES; lane += blockDim.x) {
+                double count = 0.;
+                for (int k = k0 + lane; k < k1; k += SECTION_LANES) {
+                    if (b.branch[k] != 1) continue;
+                    const int c = m.owner[b.slot_face[k]];
+                    const double bed = b.ext_bed[k], hi = fmax(q[c] + z[c] - bed, 0.), h = fmax(w.eta - bed, 0.);
+                    const double u = weir_velocity(h, hi, b.invariant[k], g);
+                    if (h <= dry || u <= 0.) { b.branch[k] = 0; continue; }
+                    // a downstream-only shock may not enter the domain
+                    if (h > hi && b.invariant[k] - h * sqrt(.5 * g * (1. / h + 1. / hi)) > tol) count += 1.;
+                }
+                w.part[0][lane] = count;
+            }
+            __syncthreads();
+            if (threadIdx.x == 0)
+                for (int lane = 0; lane < SECTION_LANES; ++lane) if (w.part[0][lane] > 0.) w.error = 5;
+            __syncthreads();
+        }
+    }
+    const int error = w.error;
+    __syncthreads();
+    if (error) return error;
+    for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+        const int f = b.slot_face[k], c = m.owner[f];
+        const double bed = b.ext_bed[k], h0 = q[c], geom = fmax(h0 + z[c] - bed, 0.);
+        const double nx = m.normal[f], ny = m.normal[nf + f];
+        double h = geom, ux = 0., uy = 0.;
+        if (h0 > dry) { ux = q[nc + c] / h0; uy = q[2 * nc + c] / h0; } else h = 0.;
+        double un = ux * nx + uy * ny;
+        const double tx = ux - un * nx, ty = uy - un * ny;
+        if (b.branch[k] == 0) {
+            // a blocked stream reflects with its stagnation / shock depth
+            if (geom > dry && h0 > dry && un != 0.) {
+                double lo = 0., hi = fmax(geom, 1.);
+                for (int it = 0; it < 60 && weir_velocity(hi, geom, un, g) > 0.; ++it) hi *= 2.;
+                for (int it = 0; it < 80; ++it) {
+                    const double mid = .5 * (lo + hi);
+                    if (weir_velocity(mid, geom, un, g) > 0.) lo = mid; else hi = mid;
+                }
+                h = .5 * (lo + hi);
+            }
+            un = 0.;
+        } else {
+            h = fmax(w.eta - bed, 0.);
+            un = weir_velocity(h, geom, b.invariant[k], g);
+        }
+        if (!isfinite(h) || !isfinite(un) || sqrt(un * un + tx * tx + ty * ty) > speed) { bad = true; continue; }
+        double water = 0., fx = 0., fy = 0., t0 = 0., t1 = 0., t2 = 0.;
+        if (h > dry) {
+            t0 = h; t1 = h * (un * nx + tx); t2 = h * (un * ny + ty);
+            water = t1 * nx + t2 * ny;
+            fx = water * t1 / h + .5 * g * h * h * nx;
+            fy = water * t2 / h + .5 * g * h * h * ny;
+        }
+        const double pressure = h0 > dry ? .5 * g * (h0 * h0 - geom * geom) : 0.;
+        b.trace[k] = t0; b.trace[ns + k] = t1; b.trace[2 * ns + k] = t2;
+        b.flux[k] = water; b.flux[ns + k] = fx + pressure * nx; b.flux[2 * ns + k] = fy + pressure * ny;
+    }
+    return 0;
+}
+
 // stage 1 / 2: the SSPRK stages (state work / q1, its own stock, clock t or
 // t + dt); STAGE_HANCOCK: the HLLC predicted state q1 at t + dt/2, outlet
 // stock of the substep's start state work (hllc.py:91-97), status of stage 1.
@@ -570,9 +768,20 @@ __global__ void k_boundary(MeshDev m, StateDev s, BoundaryDev b, Ctrl *ctrl, int
     // chain without a root rejects the trial before the rating owner runs; a
     // rating section without a solution fails the scenario
     __shared__ int section_reject;
+    __shared__ SectionWork section;
     if (threadIdx.x == 0) section_reject = 0;
     __syncthreads();
-    if (b.scen_chain) {
+    if (b.weir) {
+        for (int sg = s0; sg < s1; ++sg)              // block-uniform: the CTA solves one section at a time
+            if (b.seg_mode[sg] == 5) {
+                bool sbad = false;
+                const int e = weir_section(section, m, b, sg, grav, dry, ct.speed_limit, q, z, sbad);
+                if (threadIdx.x == 0 && e) section_reject = 1;
+                if (sbad) bad = 1;
+            }
+        __syncthreads();
+    }
+    if (b.scen_chain && !section_reject) {
         const int law = ct.roughness_mode;
         for (int ch = b.scen_chain[sid] + threadIdx.x; ch < b.scen_chain[sid + 1]; ch += blockDim.x) {
             bool sbad = false;

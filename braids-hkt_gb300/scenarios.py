@@ -245,6 +245,18 @@ def rating_channel(discharge=20.0, knots=((0.0, 2.0), (10.0, 2.6), (20.0, 3.0), 
     return case
 
 
+def weir_channel(discharge=20.0, crest=2.0, coefficient=1.7, width=24.0, **kw):
+    """The small channel ending in a free weir (mode 5): discharge =
+    coefficient x width x (stage - crest)^1.5 at the common subcritical
+    stage of the opening."""
+    case = small_channel(discharge=discharge, **kw)
+    case["seg_mode"] = np.array([M.MODE_TOTAL_Q, 5], np.int32)
+    case["outlet"] = {1: {"crest_m": float(crest), "coefficient_m_half_s": float(coefficient),
+                          "effective_width_m": float(width)}}
+    case["name"] = "weir_channel"
+    return case
+
+
 def normal_channel(discharge=20.0, bed_slope=2e-3, **kw):
     """The small channel with a normal-depth outlet (mode 10): per connected
     chain of outlet faces, the level of uniform flow at `bed_slope` with the

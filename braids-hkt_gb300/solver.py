@@ -96,6 +96,23 @@ def normal_chains(cases, face_offset=None):
             np.asarray(slopes, np.float64))
 
 
+def weir_parameters(cases):
+    """(3, nseg) crest [m], coefficient [m^0.5/s] and effective width [m] of
+    the free-weir outlets (mode 5) of a batch (FreeWeir's parameters,
+    river_exterior_outlet.py:77-79); zero rows elsewhere.
+    case["outlet"][segment] = {"crest_m", "coefficient_m_half_s", "effective_width_m"}."""
+    cols = []
+    for case in cases:
+        modes = np.asarray(case.get("seg_mode", np.zeros(0)), dtype=int)
+        for b in range(case["mesh"].nb):
+            row = (case.get("outlet") or {}).get(b, {})
+            vals = [float(row.get(k, 0.0)) for k in ("crest_m", "coefficient_m_half_s", "effective_width_m")]
+            if modes[b] == 5 and not (np.isfinite(vals[0]) and vals[1] > 0 and vals[2] > 0):
+                raise ValueError(f"free-weir segment {b} needs a finite crest and positive coefficient and width")
+            cols.append(vals)
+    return np.ascontiguousarray(np.array(cols, dtype=np.float64).T.reshape(3, -1))
+
+
 def pack(cases):
     """Concatenate scenario meshes into one global index space."""
     out = {k: [] for k in ("owner", "neighbour", "bid", "offset", "faces", "signs", "normal", "length", "area",
@@ -189,6 +206,8 @@ class RiverSolver:
             if np.any(p["seg_mode"] == 11):
                 off, rq, re_ = rating_tables(self.cases)
                 check(self.lib.brx_rating_set(self.h, _ptr(off), _ptr(rq), _ptr(re_)))
+            if np.any(p["seg_mode"] == 5):
+                check(self.lib.brx_weir_set(self.h, _ptr(weir_parameters(self.cases))))
             if np.any(p["seg_mode"] == 10):
                 off, faces, slope = normal_chains(self.cases, p["face_offset"])
                 check(self.lib.brx_outlet_chains_set(self.h, len(slope), _ptr(off), _ptr(faces), _ptr(slope)))

@@ -105,8 +105,16 @@ int brx_rating_set(brx_solver *s, const int *offset, const double *discharge, co
  * call before brx_boundary_set when any segment has mode 10. */
 int brx_outlet_chains_set(brx_solver *s, int nchain, const int *offset, const int *faces, const double *slope);
 
+/* Free-weir outlets (mode 5): param (3, nseg) crest [m], coefficient
+ * [m^0.5/s] and effective width [m] per segment (FreeWeir's parameters,
+ * src/braids_core/sediment/river_exterior_outlet.py:73-79). Host array,
+ * copied; call before brx_boundary_set when any segment has mode 5. */
+int brx_weir_set(brx_solver *s, const double *param);
+
 /* Open-boundary set-up for all segments: hydraulic mode (2 stage, 3 free
- * outflow, 6 total discharge, 9 discharge + water line, 10 normal depth:
+ * outflow, 5 free weir: the common subcritical stage whose outgoing Lax-curve
+ * discharge equals coefficient x width x head^1.5, river_exterior_outlet.h;
+ * 6 total discharge, 9 discharge + water line, 10 normal depth:
  * per face chain the level at which the outgoing characteristic discharge
  * equals the uniform-flow conveyance, river_normal_outlet.h; 11 Q-H rating
  * curve: one common water elevation at which the outgoing characteristic

@@ -95,6 +95,9 @@ typedef struct {
     int nchain;
     const int *chain_offset, *chain_face;          /* (nchain+1), faces */
     const double *chain_slope;                     /* (nchain) */
+    /* free-weir outlets (mode 5): per segment crest [m], coefficient
+     * [m^0.5/s], effective width [m] (3, nb) */
+    const double *weir;
 } om_ctx;
 
 /* ------------------------------------------------------------------ */
@@ -1107,6 +1110,168 @@ static int om_normal_chain(const om_ctx *m, int ch, const double *q, const doubl
     return 0;
 }
 
+/* ------------------------------------------------------------------ */
+/* Section solves with 128 logical lanes (river_exterior_outlet.h): lane  */
+/* l sums the section's entries l, l+128, ...; lane sums then add up in   */
+/* lane order, which is what makes the reference's OpenMP and CUDA sums   */
+/* identical. Restated here sequentially.                                 */
+/* ------------------------------------------------------------------ */
+#define OM_LANES 128
+
+static double om_weir_velocity(double h, double hi, double ui, double g)
+{
+    return h > hi ? ui - (h - hi) * sqrt(.5 * g * (1. / h + 1. / hi)) : ui + 2. * (sqrt(g * hi) - sqrt(g * h));
+}
+
+typedef struct { double area, width, rate, residual; } om_section_sum;
+
+/* river_exterior_outlet.h:207-227 */
+static om_section_sum om_weir_residual(const om_ctx *m, const int *faces, int n, double eta, double crest,
+                                       double factor, const int *branch, const double *invariant, const double *q,
+                                       const double *z)
+{
+    const double g = m->grav, dry = m->dry;
+    double part[3][OM_LANES];
+    for (int lane = 0; lane < OM_LANES; ++lane) {
+        double area = 0., width = 0., rate = 0.;
+        for (int k = lane; k < n; k += OM_LANES) {
+            const int f = faces[k], c = m->owner[f];
+            if (!branch[f]) continue;
+            const double bed = m->exterior_bed[f], h = fmax(eta - bed, 0.), hi = fmax(q[c] + z[c] - bed, 0.);
+            if (h <= dry) continue;
+            const double u = fmax(om_weir_velocity(h, hi, invariant[f], g), 0.);
+            if (u > 0.) { area += h * m->length[f]; width += m->length[f]; rate += h * u * m->length[f]; }
+        }
+        part[0][lane] = area; part[1][lane] = width; part[2][lane] = rate;
+    }
+    om_section_sum r = {0., 0., 0., 0.};
+    for (int lane = 0; lane < OM_LANES; ++lane) { r.area += part[0][lane]; r.width += part[1][lane]; r.rate += part[2][lane]; }
+    const double head = fmax(eta - crest, 0.);
+    r.residual = r.rate - factor * head * sqrt(head);
+    return r;
+}
+
+/* Free weir on one segment (river_exterior_outlet.h:229-360); 0 or the
+ * section failure (a trial rejection in the reference). branch / invariant
+ * are per-face scratch. */
+static int om_weir_section(const om_ctx *m, int b, const double *q, const double *z, double *trace, double *flux,
+                           int *status, int *branch, double *invariant)
+{
+    const int nc = m->nc, nf = m->nf, nb = m->nb;
+    const double g = m->grav, dry = m->dry, speed = m->speed_limit;
+    const double tol = 128. * OM_EPS, crest = m->weir[b], factor = m->weir[nb + b] * m->weir[2 * nb + b];
+    const int *faces = m->boundary_faces + m->boundary_offset[b];
+    const int n = m->boundary_offset[b + 1] - m->boundary_offset[b];
+    int error = 0, done = 0;
+    double eta = 0.;
+    {
+        double width = 0.;
+        for (int lane = 0; lane < OM_LANES; ++lane) {
+            double wl = 0.;
+            for (int k = lane; k < n; k += OM_LANES) {
+                const int f = faces[k], c = m->owner[f];
+                branch[f] = 0; invariant[f] = 0.;
+                const double h0 = q[c], h = fmax(h0 + z[c] - m->exterior_bed[f], 0.);
+                if (h0 <= dry || h <= dry) continue;
+                const double un = (q[nc + c] * m->normal[f] + q[2 * nc + c] * m->normal[nf + f]) / h0;
+                branch[f] = 1; invariant[f] = un; wl += m->length[f];
+            }
+            width += wl;
+        }
+        if (width == 0.) done = 1;
+    }
+    if (done) for (int k = 0; k < n; ++k) branch[faces[k]] = 0;
+    else {
+        double lo = -INFINITY, hi = -INFINITY;
+        for (int k = 0; k < n; ++k) {       /* lane maxima, then the maximum over lanes: order-free */
+            const int f = faces[k];
+            if (branch[f] != 1) continue;
+            const int c = m->owner[f];
+            const double h0 = fmax(q[c] + z[c] - m->exterior_bed[f], 0.), u = invariant[f];
+            double left = 0., right = fmax(h0, 1.);
+            for (int it = 0; it < 60 && om_weir_velocity(right, h0, u, g) > sqrt(g * right); ++it) right *= 2.;
+            for (int it = 0; it < 70; ++it) {
+                const double mid = .5 * (left + right);
+                if (om_weir_velocity(mid, h0, u, g) > sqrt(g * mid)) left = mid; else right = mid;
+            }
+            lo = fmax(lo, m->exterior_bed[f] + right);
+            hi = fmax(hi, q[c] + z[c]);
+        }
+        lo = fmax(lo, crest);
+        hi = fmax(hi, lo + 1.);
+        om_section_sum r = om_weir_residual(m, faces, n, lo, crest, factor, branch, invariant, q, z);
+        if (r.residual < 0. || !isfinite(r.residual)) error = 1;
+        if (!error) {
+            r = om_weir_residual(m, faces, n, hi, crest, factor, branch, invariant, q, z);
+            for (int j = 0; j < 60 && r.residual > 0.; ++j) {
+                hi = lo + 2. * (hi - lo);
+                r = om_weir_residual(m, faces, n, hi, crest, factor, branch, invariant, q, z);
+            }
+            if (r.residual > 0. || !isfinite(r.residual)) error = 1;
+        }
+        if (!error) {
+            for (int j = 0; j < 90; ++j) {
+                eta = lo + .5 * (hi - lo);
+                if (eta == lo || eta == hi) break;
+                r = om_weir_residual(m, faces, n, eta, crest, factor, branch, invariant, q, z);
+                if (r.residual > 0.) lo = eta; else hi = eta;
+            }
+            eta = lo + .5 * (hi - lo);
+            r = om_weir_residual(m, faces, n, eta, crest, factor, branch, invariant, q, z);
+            const double head = fmax(eta - crest, 0.), requested = factor * head * sqrt(head);
+            if (!isfinite(r.residual) || fabs(r.residual) > 1e-10 * fmax(requested, 1.)) error = 2;
+            double bad = 0.;
+            for (int k = 0; k < n; ++k) {
+                const int f = faces[k];
+                if (branch[f] != 1) continue;
+                const int c = m->owner[f];
+                const double bed = m->exterior_bed[f], hi2 = fmax(q[c] + z[c] - bed, 0.), h = fmax(eta - bed, 0.);
+                const double u = om_weir_velocity(h, hi2, invariant[f], g);
+                if (h <= dry || u <= 0.) { branch[f] = 0; continue; }
+                if (h > hi2 && invariant[f] - h * sqrt(.5 * g * (1. / h + 1. / hi2)) > tol) bad += 1.;
+            }
+            if (bad > 0.) error = 5;
+        }
+    }
+    if (error) return error;
+    for (int k = 0; k < n; ++k) {
+        const int f = faces[k], c = m->owner[f];
+        const double bed = m->exterior_bed[f], h0 = q[c], geom = fmax(h0 + z[c] - bed, 0.);
+        const double nx = m->normal[f], ny = m->normal[nf + f];
+        double h = geom, ux = 0., uy = 0.;
+        if (h0 > dry) { ux = q[nc + c] / h0; uy = q[2 * nc + c] / h0; } else h = 0.;
+        double un = ux * nx + uy * ny;
+        const double tx = ux - un * nx, ty = uy - un * ny;
+        if (branch[f] == 0) {
+            /* a blocked stream reflects with its stagnation / shock depth */
+            if (geom > dry && h0 > dry && un != 0.) {
+                double lo = 0., hi = fmax(geom, 1.);
+                for (int it = 0; it < 60 && om_weir_velocity(hi, geom, un, g) > 0.; ++it) hi *= 2.;
+                for (int it = 0; it < 80; ++it) {
+                    const double mid = .5 * (lo + hi);
+                    if (om_weir_velocity(mid, geom, un, g) > 0.) lo = mid; else hi = mid;
+                }
+                h = .5 * (lo + hi);
+            }
+            un = 0.;
+        } else {
+            h = fmax(eta - bed, 0.);
+            un = om_weir_velocity(h, geom, invariant[f], g);
+        }
+        if (!isfinite(h) || !isfinite(un) || sqrt(un * un + tx * tx + ty * ty) > speed) { status[f] = 3; continue; }
+        double water = 0., fx = 0., fy = 0.;
+        if (h > dry) {
+            trace[f] = h; trace[nf + f] = h * (un * nx + tx); trace[2 * nf + f] = h * (un * ny + ty);
+            water = trace[nf + f] * nx + trace[2 * nf + f] * ny;
+            fx = water * trace[nf + f] / h + .5 * g * h * h * nx;
+            fy = water * trace[2 * nf + f] / h + .5 * g * h * h * ny;
+        }
+        const double pressure = h0 > dry ? .5 * g * (h0 * h0 - geom * geom) : 0.;
+        flux[f] = water; flux[nf + f] = fx + pressure * nx; flux[2 * nf + f] = fy + pressure * ny;
+    }
+    return 0;
+}
+
 int om_exterior(om_ctx *m, const double *q, const double *z, double time,
                 double *trace, double *flux, int *status, double *work,
                 double *stage_out, double *total_out)
@@ -1211,6 +1376,18 @@ int om_exterior(om_ctx *m, const double *q, const double *z, double time,
     /* section owners of the remaining outlet modes, in the reference's order
      * (river_exterior_bed.py:213-217): a normal-depth failure rejects the
      * trial before the rating owner runs; a rating failure is fatal */
+    if (m->weir) {
+        int *branch = (int *)calloc((size_t)nf, sizeof(int));
+        double *invariant = (double *)calloc((size_t)nf, sizeof(double));
+        int weir_failed = 0;
+        for (int b = 0; b < nb; ++b)
+            if (m->seg_mode[b] == 5 && om_weir_section(m, b, q, z, trace, flux, status, branch, invariant)) {
+                weir_failed = 1;
+                break;
+            }
+        free(branch); free(invariant);
+        if (weir_failed) return OM_REJECT_SPATIAL;
+    }
     int normal_failed = 0;
     for (int ch = 0; ch < m->nchain; ++ch)
         if (om_normal_chain(m, ch, q, z, trace, flux, status)) normal_failed = 1;

@@ -61,7 +61,7 @@ class Ctx(C.Structure):
                 ("seg_mode", P), ("stage_policy", P), ("exterior_bed", P), ("forcing", P),
                 ("table_len", I), ("table_time", P), ("table_value", P), ("threads", I),
                 ("turb", P), ("rating_offset", P), ("rating_q", P), ("rating_eta", P),
-                ("nchain", I), ("chain_offset", P), ("chain_face", P), ("chain_slope", P)]
+                ("nchain", I), ("chain_offset", P), ("chain_face", P), ("chain_slope", P), ("weir", P)]
 
 
 class Turbines(C.Structure):
@@ -223,6 +223,9 @@ class Oracle:
             ctx.chain_offset = k("chain_offset", _i32(off))
             ctx.chain_face = k("chain_face", _i32(faces))
             ctx.chain_slope = k("chain_slope", _f64(slope))
+        if nb and np.any(seg_mode == 5):
+            from braids_hkt_gb300.solver import weir_parameters
+            ctx.weir = k("weir", _f64(weir_parameters([case])))
         if case.get("rating"):
             from braids_hkt_gb300.solver import rating_tables
             off, rq, re_ = rating_tables([case])

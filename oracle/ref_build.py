@@ -23,7 +23,8 @@ Dual-compiled OpenMP headers (their ENTRY/LOOP macros select the host form):
   river_turbine_flow.h, river_hydrokinetic_stress.h (turbine momentum terms),
   river_mpm.h, flow2dh_mobile_kernels.h, bend_methods_v1_kernels.h (Exner / MPM),
   hllc.h, hllc_turbines.h (src/braids_core/hydraulics, the HLLC option),
-  river_rating_outlet.h, river_normal_outlet.h (rating and normal-depth outlets)
+  river_rating_outlet.h, river_normal_outlet.h, river_exterior_outlet.h (rating,
+  normal-depth, critical and free-weir outlets)
 Generated CUDA C also: flow_bed_slope_runtime.cu (src/braids_gpu, Koch-Flokstra slope)
 
 Usage: python oracle/ref_build.py   (exits non-zero when the reference is absent)
@@ -116,6 +117,7 @@ def generate():
         # section owners of the remaining outlet modes
         "ref_rating": (src / "braids_core/sediment/river_rating_outlet.h").read_text(),
         "ref_normal": (src / "braids_core/sediment/river_normal_outlet.h").read_text(),
+        "ref_outlet": (src / "braids_core/sediment/river_exterior_outlet.h").read_text(),
     }
     for name, code in headers.items():
         (OUT / f"{name}.h").write_text(code)

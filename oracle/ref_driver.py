@@ -427,6 +427,19 @@ class Ref:
                   g["owner"], g["bid"], g["selected"], self.seg_mode, self.stage_policy, q, self.z,
                   self.exterior_bed, g["normal"], g["length"], self.forcing, weights, total, trace, flux, status)
         # section owners after exterior_flux (ExteriorBed.evaluate, river_exterior_bed.py:213-217)
+        if np.any(self.seg_mode[:nb] == 5):
+            from braids_hkt_gb300.solver import weir_parameters
+            if "ref_outlet" not in self.libs:
+                self.libs["ref_outlet"] = C.CDLL(str(REF / "libref_outlet.so"))
+                self.libs["ref_outlet"].mobile_threads(C.c_int(os.cpu_count() or 1))
+            control = np.ascontiguousarray((self.seg_mode[:nb] == 5).astype(np.int32))
+            sec = np.zeros(nb, np.int32)
+            self.call("ref_outlet", "exterior_free_weir", 0, nf, n, nb, self.grav, self.dry, self.speed_limit, control,
+                      weir_parameters([self.case]), g["boffset"], g["bfaces"], g["owner"], q, self.z, self.exterior_bed,
+                      g["normal"], g["length"], np.zeros(nf, np.int32), np.zeros(nf), np.zeros(nb), np.zeros((3, nb)),
+                      trace, flux, status, sec)
+            if np.any(sec):
+                raise Rejected("free-weir outlet has no admissible subcritical control")
         if np.any(self.seg_mode[:nb] == 10):
             from braids_core.sediment.river_boundary_components import connected_opening_chains
             if "ref_normal" not in self.libs:

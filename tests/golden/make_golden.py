@@ -35,6 +35,7 @@ CASES = {
     "dam_break_dry": (S.dam_break, lambda c: c["q"], 0.02, 1.0),
     "rating_outlet": (S.rating_channel, lambda c: S.perturbed_state(c, 6, 0.2, 0.4, 0.0), 0.01, 1.0),
     "normal_outlet": (S.normal_channel, lambda c: S.perturbed_state(c, 7, 0.2, 0.4, 0.0), 0.01, 1.0),
+    "weir_outlet": (S.weir_channel, lambda c: S.perturbed_state(c, 8, 0.2, 0.4, 0.0), 0.01, 1.0),
 }
 
 

@@ -1,5 +1,5 @@
-"""Outlet section owners on the GPU: the Q-H rating (mode 11) and normal-depth
-(mode 10) outlets against
+"""Outlet section owners on the GPU: the Q-H rating (mode 11), normal-depth
+(mode 10) and free-weir (mode 5) outlets against
 the oracle (FP64 to 1e-10 with identical substep counts; mixed against FP64
 to 1e-4 in depth) and its failure without a bracket (the scenario fails,
 failed = 5). The reference fixture is checked in test_gpu_parity."""
@@ -38,10 +38,11 @@ def test_rating_outlet_without_a_bracket_fails_the_scenario():
     assert d[0]["failed"] == 0 and d[1]["failed"] == 5
 
 
-def test_normal_depth_outlet_fp64_oracle_and_mixed():
+@pytest.mark.parametrize("make", [S.normal_channel, S.weir_channel], ids=["normal", "weir"])
+def test_section_outlet_fp64_oracle_and_mixed(make):
     from braids_hkt_gb300.solver import RiverSolver
     from oracle import Oracle
-    case = S.normal_channel()
+    case = make()
     a, b = RiverSolver(case, precision="fp64"), RiverSolver(case, precision="mixed")
     o = Oracle(case, threads=4)
     q = case["q"].copy()
@@ -59,7 +60,7 @@ def test_normal_depth_outlet_fp64_oracle_and_mixed():
 def test_outlet_modes_batched_equal_alone():
     """Rating and normal-depth outlets in one batch with the stage-outlet channel: bitwise as alone."""
     from braids_hkt_gb300.solver import RiverSolver
-    cases = [S.small_channel(), S.rating_channel(), S.normal_channel()]
+    cases = [S.small_channel(), S.rating_channel(), S.normal_channel(), S.weir_channel()]
     batch = RiverSolver(cases, precision="mixed")
     batch.advance(2.0, 0.0)
     for i, c in enumerate(cases):

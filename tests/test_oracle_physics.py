@@ -156,3 +156,27 @@ def test_normal_depth_outlet_drains_towards_uniform_flow():
         assert st == 0
         flows.append(float(np.sum(water[outlet] * m.length[outlet])))
     assert flows[0] > flows[1] > flows[2] > 20.0
+
+
+def test_free_weir_outlet_discharges_by_the_weir_law():
+    """Free weir (mode 5): the discharge over a short window equals
+    coefficient x width x (stage - crest)^1.5 at the outlet cells' stage to
+    2%, through the channel's seiche."""
+    case = S.weir_channel()
+    w_ = case["outlet"][1]
+    o = Oracle(case, threads=4)
+    q = case["q"].copy()
+    m = case["mesh"]
+    outlet = (m.neighbour < 0) & (m.bid == 1)
+    owners = m.owner[outlet]
+    t = 0.0
+    for k in range(4):
+        st, _, _ = o.advance(q, 5.0, t)
+        t += 5.0
+        stage = float(np.mean(q[0][owners] + case["z"][owners]))
+        st2, water, _ = o.advance(q, 0.1, t)
+        t += 0.1
+        assert st == 0 and st2 == 0
+        out = float(np.sum(water[outlet] * m.length[outlet]))
+        law = w_["coefficient_m_half_s"] * w_["effective_width_m"] * max(stage - w_["crest_m"], 0.0) ** 1.5
+        assert abs(out - law) <= 0.02 * law
