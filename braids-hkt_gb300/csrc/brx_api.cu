@@ -473,8 +473,10 @@ extern "C" int brx_boundary_set(brx_solver *s, const int *seg_mode, const int *s
     if (!seg_mode || !stage_policy || !exterior_bed || !forcing) return fail(BRX_ERR_ARGUMENT, "null boundary array");
     for (int sg = 0; sg < nseg; ++sg) {
         const int md = seg_mode[sg];
-        if (md != 2 && md != 3 && md != 5 && md != 6 && md != 9 && md != 10 && md != 11)
-            return fail(BRX_ERR_UNSUPPORTED, "open-boundary mode must be 2, 3, 5, 6, 9, 10 or 11");
+        if (md != 2 && md != 3 && md != 4 && md != 5 && md != 6 && md != 9 && md != 10 && md != 11)
+            return fail(BRX_ERR_UNSUPPORTED, "open-boundary mode must be 2, 3, 4, 5, 6, 9, 10 or 11");
+        if (md == 4 && !s->bnd.crit_seg_chain)
+            return fail(BRX_ERR_STATE, "a critical outlet (mode 4) needs its face chains first (brx_critical_chains_set)");
         if (md == 5 && !s->bnd.weir)
             return fail(BRX_ERR_STATE, "a free-weir outlet (mode 5) needs its parameters first (brx_weir_set)");
         if (md == 10 && !s->chains_ready)
@@ -589,6 +591,40 @@ extern "C" int brx_outlet_chains_set(brx_solver *s, int nchain, const int *offse
     TRY(s->upload(&p_slot, slot.data(), slot.size())); TRY(s->upload(&p_slope, slope, nchain));
     s->bnd.scen_chain = p_scen; s->bnd.chain_off = p_off; s->bnd.chain_slot = p_slot; s->bnd.chain_slope = p_slope;
     s->chains_ready = true;
+    s->graph_dirty = true;
+    return BRX_OK;
+}
+
+extern "C" int brx_critical_chains_set(brx_solver *s, const int *seg_chain, const int *offset, const int *faces)
+{
+    if (!s) return fail(BRX_ERR_ARGUMENT, "null solver");
+    if (!seg_chain || !offset || !faces) return fail(BRX_ERR_ARGUMENT, "null chain array");
+    if (s->bnd.crit_seg_chain) return fail(BRX_ERR_STATE, "critical-outlet chains are already installed");
+    const int nseg = s->nseg;
+    if (nseg == 0 || seg_chain[0] != 0) return fail(BRX_ERR_ARGUMENT, "chain ranges must start at 0");
+    const int nchain = seg_chain[nseg];
+    if (offset[0] != 0) return fail(BRX_ERR_ARGUMENT, "chain offsets must start at 0");
+    std::vector<int> bslot(s->nf, -1);
+    for (int k = 0; k < s->nslot; ++k) bslot[s->h_slot_face[k]] = k;
+    std::vector<int> slot(std::max(offset[nchain], 1));
+    for (int sg = 0; sg < nseg; ++sg) {
+        if (seg_chain[sg + 1] < seg_chain[sg]) return fail(BRX_ERR_ARGUMENT, "chain ranges must not decrease");
+        for (int ch = seg_chain[sg]; ch < seg_chain[sg + 1]; ++ch) {
+            if (offset[ch + 1] <= offset[ch]) return fail(BRX_ERR_ARGUMENT, "every chain needs faces");
+            for (int e = offset[ch]; e < offset[ch + 1]; ++e) {
+                const int f = faces[e];
+                if (f < 0 || f >= s->nf || bslot[f] < 0 || s->h_bid[f] != sg)
+                    return fail(BRX_ERR_ARGUMENT, "chain face is not an open face of its segment");
+                slot[e] = bslot[f];
+            }
+        }
+    }
+    int *p_seg, *p_off, *p_slot;
+    TRY(s->upload(&p_seg, seg_chain, nseg + 1)); TRY(s->upload(&p_off, offset, nchain + 1));
+    TRY(s->upload(&p_slot, slot.data(), slot.size()));
+    TRY(ensure_section_scratch(s));
+    TRY(s->alloc(&s->bnd.gslot, std::max(s->nslot, 1))); TRY(s->alloc(&s->bnd.gend, std::max(s->nslot, 1)));
+    s->bnd.crit_seg_chain = p_seg; s->bnd.crit_chain_off = p_off; s->bnd.crit_chain_slot = p_slot;
     s->graph_dirty = true;
     return BRX_OK;
 }

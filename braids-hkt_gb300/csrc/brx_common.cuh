@@ -177,6 +177,9 @@ struct BoundaryDev {
     const double *weir;      // (3, nseg) free-weir crest, coefficient, effective width
     int *branch;             // (nslot) section-solve scratch: face branch
     double *invariant;       // (nslot) section-solve scratch: outgoing invariant / normal speed
+    const int *crit_seg_chain;           // (nseg+1) critical-outlet chains per segment, or null
+    const int *crit_chain_off, *crit_chain_slot;
+    int *gslot, *gend;       // (nslot) wet-group scratch of the critical outlets
 };
 
 // Accepted / stage state buffers.

@@ -619,6 +619,231 @@ __device__ int weir_section(SectionWork &w, const MeshDev &m, const BoundaryDev 
     return 0;
 }
 
+// ---------------------------------------------------------------------------
+// Critical outlet (mode 4): on the controlled faces of an opening the
+// outgoing characteristic discharge equals sqrt(g A^3 / B); faces turning
+// inward or dry leave the control and the root is recomputed
+// (river_exterior_outlet.h:29-175). Slot lists: `slots` null means the
+// segment's own slots k0, k0+1, ...
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double resolved_bed(const MeshDev &m, const BoundaryDev &b, int k, const double *q,
+                                               const double *z)
+{
+    const int c = m.owner[b.slot_face[k]];
+    const double h = fmax(q[c], 0.), bed = b.ext_bed[k];
+    if (h >= 1.e-3) return bed;
+    const double bounded = fmax(bed, z[c] - h);
+    double blend = fmin(1., fmax(0., (h - 1.e-4) / 9.e-4));
+    blend = blend * blend * (3. - 2. * blend);
+    return bed + (bounded - bed) * (1. - blend);
+}
+
+__device__ void crit_residual(SectionWork &w, const MeshDev &m, const BoundaryDev &b, const int *slots, int k0,
+                              int n, double eta, double g, double dry, const double *q, const double *z)
+{
+    for (int lane = threadIdx.x; lane < SECTION_LANES; lane += blockDim.x) {
+        double a = 0., width = 0., rate = 0.;
+        for (int i = lane; i < n; i += SECTION_LANES) {
+            const int k = slots ? slots[i] : k0 + i;
+            if (b.branch[k] != 1) continue;
+            const double h = fmax(eta - resolved_bed(m, b, k, q, z), 0.);
+            if (h <= dry) continue;
+            const double len = m.length[b.slot_face[k]];
+            a += h * len; width += len; rate += h * (b.invariant[k] - 2. * sqrt(g * h)) * len;
+        }
+        w.part[0][lane] = a; w.part[1][lane] = width; w.part[2][lane] = rate;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0., width = 0., rate = 0.;
+        for (int lane = 0; lane < SECTION_LANES; ++lane) { a += w.part[0][lane]; width += w.part[1][lane]; rate += w.part[2][lane]; }
+        w.area = a; w.width = width; w.rate = rate;
+        w.residual = rate - (width > 0. ? sqrt(g * a * a * a / width) : 0.);
+    }
+    __syncthreads();
+}
+
+__device__ int crit_group(SectionWork &w, const MeshDev &m, const BoundaryDev &b, const int *slots, int k0, int n,
+                          double g, double dry, double speed, const double *q, const double *z, bool &bad)
+{
+    const int nc = m.nc, nf = m.nf;
+    const size_t ns = b.nslot;
+    const double tol = 128. * EPS;
+    if (threadIdx.x == 0) { w.error = 0; w.done = 0; w.eta = 0.; w.area = w.width = w.rate = 0.; }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int k = slots ? slots[i] : k0 + i, f = b.slot_face[k], c = m.owner[f];
+        b.branch[k] = 0; b.invariant[k] = 0.;
+        const double h0 = q[c], h = fmax(h0 + z[c] - resolved_bed(m, b, k, q, z), 0.);
+        if (h0 <= dry || h <= dry) continue;
+        const double un = (q[nc + c] * m.normal[f] + q[2 * nc + c] * m.normal[nf + f]) / h0, wave = sqrt(g * h);
+        if (un < -tol * fmax(1., fabs(un))) continue;
+        if (un > wave * (1. + 1e-10)) { b.branch[k] = 2; continue; }
+        b.branch[k] = 1; b.invariant[k] = un + 2. * wave;
+    }
+    __syncthreads();
+    for (int active = 0; active <= n; ++active) {
+        for (int lane = threadIdx.x; lane < SECTION_LANES; lane += blockDim.x) {
+            double lo = INFINITY, hi = -INFINITY, count = 0.;
+            for (int i = lane; i < n; i += SECTION_LANES) {
+                const int k = slots ? slots[i] : k0 + i;
+                if (b.branch[k] != 1) continue;
+                const int c = m.owner[b.slot_face[k]];
+                lo = fmin(lo, resolved_bed(m, b, k, q, z)); hi = fmax(hi, q[c] + z[c]); count += 1.;
+            }
+            w.part[0][lane] = lo; w.part[1][lane] = hi; w.part[2][lane] = count;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            w.lo = INFINITY; w.hi = -INFINITY; w.count = 0;
+            for (int lane = 0; lane < SECTION_LANES; ++lane) {
+                w.lo = fmin(w.lo, w.part[0][lane]); w.hi = fmax(w.hi, w.part[1][lane]); w.count += int(w.part[2][lane]);
+            }
+            if (w.count) w.lo += fmax(2. * dry, tol * fmax(1., fabs(w.lo)));
+            else { w.done = 1; w.area = w.width = w.rate = 0.; }
+        }
+        __syncthreads();
+        if (w.done) break;
+        crit_residual(w, m, b, slots, k0, n, w.lo, g, dry, q, z);
+        if (w.residual < 0.) {                     // unresolved controlled depth: the opening closes
+            for (int i = threadIdx.x; i < n; i += blockDim.x) {
+                const int k = slots ? slots[i] : k0 + i;
+                if (b.branch[k] == 1) b.branch[k] = 0;
+            }
+            if (threadIdx.x == 0) { w.done = 1; w.area = w.width = w.rate = 0.; w.eta = w.lo; }
+            __syncthreads();
+            break;
+        }
+        crit_residual(w, m, b, slots, k0, n, w.hi, g, dry, q, z);
+        for (int j = 0; j < 60 && w.residual > 0.; ++j) {
+            if (threadIdx.x == 0) w.hi = w.lo + 2. * (w.hi - w.lo);
+            __syncthreads();
+            crit_residual(w, m, b, slots, k0, n, w.hi, g, dry, q, z);
+        }
+        if (w.residual > 0. || !isfinite(w.residual)) {
+            if (threadIdx.x == 0) w.error = 1;
+            __syncthreads();
+            break;
+        }
+        for (int j = 0; j < 90; ++j) {
+            if (threadIdx.x == 0) { w.eta = w.lo + .5 * (w.hi - w.lo); w.stagnant = w.eta == w.lo || w.eta == w.hi; }
+            __syncthreads();
+            if (w.stagnant) break;
+            crit_residual(w, m, b, slots, k0, n, w.eta, g, dry, q, z);
+            if (threadIdx.x == 0) { if (w.residual > 0.) w.lo = w.eta; else w.hi = w.eta; }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) w.eta = w.lo + .5 * (w.hi - w.lo);
+        __syncthreads();
+        for (int lane = threadIdx.x; lane < SECTION_LANES; lane += blockDim.x) {
+            double changed = 0.;
+            for (int i = lane; i < n; i += SECTION_LANES) {
+                const int k = slots ? slots[i] : k0 + i;
+                if (b.branch[k] != 1) continue;
+                const double h = fmax(w.eta - resolved_bed(m, b, k, q, z), 0.), un = b.invariant[k] - 2. * sqrt(g * h);
+                if (h <= dry || un < -tol) { b.branch[k] = 0; changed += 1.; }
+            }
+            w.part[0][lane] = changed;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) { w.changed = 0; for (int lane = 0; lane < SECTION_LANES; ++lane) w.changed += int(w.part[0][lane]); }
+        __syncthreads();
+        if (w.changed) continue;
+        crit_residual(w, m, b, slots, k0, n, w.eta, g, dry, q, z);
+        if (threadIdx.x == 0) {
+            const double qc = w.width > 0. ? sqrt(g * w.area * w.area * w.area / w.width) : 0.;
+            if (w.area <= 0. || w.width <= 0. || !isfinite(w.residual) || fabs(w.residual) > 1e-10 * fmax(qc, 1.)) w.error = 2;
+            w.done = 1;
+        }
+        __syncthreads();
+        break;
+    }
+    if (threadIdx.x == 0 && !w.done && !w.error) w.error = 3;
+    __syncthreads();
+    const int error = w.error;
+    __syncthreads();
+    if (error) return error;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int k = slots ? slots[i] : k0 + i, f = b.slot_face[k], c = m.owner[f];
+        const double rbed = resolved_bed(m, b, k, q, z), h0 = q[c], geom = fmax(h0 + z[c] - rbed, 0.);
+        const double nx = m.normal[f], ny = m.normal[nf + f];
+        double h = geom, ux = 0., uy = 0.;
+        if (h0 > dry) { ux = q[nc + c] / h0; uy = q[2 * nc + c] / h0; } else h = 0.;
+        double un = ux * nx + uy * ny;
+        const double tx = ux - un * nx, ty = uy - un * ny;
+        if (b.branch[k] == 0) un = 0.;
+        else if (b.branch[k] == 1) { h = fmax(w.eta - rbed, 0.); un = b.invariant[k] - 2. * sqrt(g * h); }
+        if (!isfinite(h) || !isfinite(un) || sqrt(un * un + tx * tx + ty * ty) > speed) { bad = true; continue; }
+        double water = 0., fx = 0., fy = 0., t0 = 0., t1 = 0., t2 = 0.;
+        if (h > dry) {
+            t0 = h; t1 = h * (un * nx + tx); t2 = h * (un * ny + ty);
+            water = t1 * nx + t2 * ny;
+            fx = water * t1 / h + .5 * g * h * h * nx;
+            fy = water * t2 / h + .5 * g * h * h * ny;
+        }
+        const double pressure = h0 > dry ? .5 * g * (h0 * h0 - geom * geom) : 0.;
+        b.trace[k] = t0; b.trace[ns + k] = t1; b.trace[2 * ns + k] = t2;
+        b.flux[k] = water; b.flux[ns + k] = fx + pressure * nx; b.flux[2 * ns + k] = fy + pressure * ny;
+    }
+    return 0;
+}
+
+// The critical owner of segment sg: the whole opening, then, when dry faces
+// split its chains into several wet groups, each group alone with the dry
+// faces closed at their owners' pressure (river_exterior_outlet.py:37-72).
+__device__ int crit_section(SectionWork &w, const MeshDev &m, const BoundaryDev &b, int sg, double g, double dry,
+                            double speed, const double *q, const double *z, bool &bad)
+{
+    const int nf = m.nf, k0 = b.seg_off[sg], n = b.seg_off[sg + 1] - k0;
+    const size_t ns = b.nslot;
+    bool bad_whole = false;
+    const int err = crit_group(w, m, b, nullptr, k0, n, g, dry, speed, q, z, bad_whole);
+    if (!b.crit_seg_chain) { bad = bad || bad_whole; return err; }
+    __shared__ int ngroup;
+    if (threadIdx.x == 0) {          // wet runs along each chain, as slot lists in the segment's scratch
+        int groups = 0, flat = 0;
+        for (int ch = b.crit_seg_chain[sg]; ch < b.crit_seg_chain[sg + 1]; ++ch) {
+            bool open = false;
+            for (int e = b.crit_chain_off[ch]; e < b.crit_chain_off[ch + 1]; ++e) {
+                const int k = b.crit_chain_slot[e], c = m.owner[b.slot_face[k]];
+                const double h = q[c], geom = h + z[c] - b.ext_bed[k];
+                if ((h > dry) && (geom > dry)) { b.gslot[k0 + flat++] = k; open = true; }
+                else if (open) { b.gend[k0 + groups++] = flat; open = false; }
+            }
+            if (open) b.gend[k0 + groups++] = flat;
+        }
+        ngroup = groups;
+    }
+    __syncthreads();
+    const int groups = ngroup;
+    __syncthreads();
+    if (groups <= 1) { bad = bad || bad_whole; return err; }
+    int worst = 0, start = 0;
+    bool bad_groups = bad_whole;      // a face the groups do not rewrite keeps its earlier status
+    for (int gi = 0; gi < groups; ++gi) {
+        const int end = b.gend[k0 + gi];
+        bool gb = false;
+        const int e = crit_group(w, m, b, b.gslot + k0 + start, 0, end - start, g, dry, speed, q, z, gb);
+        worst = max(worst, e);
+        bad_groups = bad_groups || gb;
+        start = end;
+    }
+    // dry chain faces close at their owners' pressure; their status clears
+    bool any_dry_bad = false;
+    for (int ch = b.crit_seg_chain[sg]; ch < b.crit_seg_chain[sg + 1]; ++ch)
+        for (int e = b.crit_chain_off[ch] + threadIdx.x; e < b.crit_chain_off[ch + 1]; e += blockDim.x) {
+            const int k = b.crit_chain_slot[e], f = b.slot_face[k], c = m.owner[f];
+            const double h = q[c], geom = h + z[c] - b.ext_bed[k];
+            if ((h > dry) && (geom > dry)) continue;
+            const double height = fmax(q[c], 0.), pressure = .5 * g * height * height;
+            b.trace[k] = 0.; b.trace[ns + k] = 0.; b.trace[2 * ns + k] = 0.;
+            b.flux[k] = 0.; b.flux[ns + k] = pressure * m.normal[f]; b.flux[2 * ns + k] = pressure * m.normal[nf + f];
+        }
+    (void)any_dry_bad;
+    __syncthreads();
+    bad = bad || bad_groups;
+    return worst;
+}
+
 // stage 1 / 2: the SSPRK stages (state work / q1, its own stock, clock t or
 // t + dt); STAGE_HANCOCK: the HLLC predicted state q1 at t + dt/2, outlet
 // stock of the substep's start state work (hllc.py:91-97), status of stage 1.
@@ -771,7 +996,18 @@ __global__ void k_boundary(MeshDev m, StateDev s, BoundaryDev b, Ctrl *ctrl, int
     __shared__ SectionWork section;
     if (threadIdx.x == 0) section_reject = 0;
     __syncthreads();
-    if (b.weir) {
+    if (b.branch) {
+        bool crit_failed = false;
+        for (int sg = s0; sg < s1; ++sg)              // block-uniform: the CTA solves one section at a time
+            if (b.seg_mode[sg] == 4) {
+                bool sbad = false;
+                if (crit_section(section, m, b, sg, grav, dry, ct.speed_limit, q, z, sbad)) crit_failed = true;
+                if (sbad) bad = 1;
+            }
+        if (threadIdx.x == 0 && crit_failed) section_reject = 1;
+        __syncthreads();
+    }
+    if (b.weir && !section_reject) {
         for (int sg = s0; sg < s1; ++sg)              // block-uniform: the CTA solves one section at a time
             if (b.seg_mode[sg] == 5) {
                 bool sbad = false;

@@ -245,6 +245,15 @@ def rating_channel(discharge=20.0, knots=((0.0, 2.0), (10.0, 2.6), (20.0, 3.0), 
     return case
 
 
+def critical_channel(discharge=20.0, **kw):
+    """The small channel ending in a critical outlet (mode 4): the outgoing
+    characteristic discharge of the controlled faces equals sqrt(g A^3 / B)."""
+    case = small_channel(discharge=discharge, **kw)
+    case["seg_mode"] = np.array([M.MODE_TOTAL_Q, 4], np.int32)
+    case["name"] = "critical_channel"
+    return case
+
+
 def weir_channel(discharge=20.0, crest=2.0, coefficient=1.7, width=24.0, **kw):
     """The small channel ending in a free weir (mode 5): discharge =
     coefficient x width x (stage - crest)^1.5 at the common subcritical

@@ -96,6 +96,25 @@ def normal_chains(cases, face_offset=None):
             np.asarray(slopes, np.float64))
 
 
+def critical_chains(cases, face_offset=None):
+    """Connected face chains of the critical outlets (mode 4) of a batch:
+    (chain range per packed segment (nseg+1), chain offsets, faces (global
+    ids)) in scenario and segment order (CriticalOutlet's chains,
+    river_exterior_outlet.py:20-21)."""
+    from .mesh import opening_chains
+    segc, off, faces = [0], [0], []
+    for i, case in enumerate(cases):
+        F0 = 0 if face_offset is None else int(face_offset[i])
+        modes = np.asarray(case.get("seg_mode", np.zeros(0)), dtype=int)
+        for b in range(case["mesh"].nb):
+            if modes[b] == 4:
+                for chain in opening_chains(case["mesh"], b):
+                    faces.extend(int(f) + F0 for f in chain)
+                    off.append(len(faces))
+            segc.append(len(off) - 1)
+    return (np.asarray(segc, np.int32), np.asarray(off, np.int32), np.asarray(faces if faces else [0], np.int32))
+
+
 def weir_parameters(cases):
     """(3, nseg) crest [m], coefficient [m^0.5/s] and effective width [m] of
     the free-weir outlets (mode 5) of a batch (FreeWeir's parameters,
@@ -206,6 +225,9 @@ class RiverSolver:
             if np.any(p["seg_mode"] == 11):
                 off, rq, re_ = rating_tables(self.cases)
                 check(self.lib.brx_rating_set(self.h, _ptr(off), _ptr(rq), _ptr(re_)))
+            if np.any(p["seg_mode"] == 4):
+                segc, off, faces = critical_chains(self.cases, p["face_offset"])
+                check(self.lib.brx_critical_chains_set(self.h, _ptr(segc), _ptr(off), _ptr(faces)))
             if np.any(p["seg_mode"] == 5):
                 check(self.lib.brx_weir_set(self.h, _ptr(weir_parameters(self.cases))))
             if np.any(p["seg_mode"] == 10):

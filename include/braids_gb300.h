@@ -105,6 +105,14 @@ int brx_rating_set(brx_solver *s, const int *offset, const double *discharge, co
  * call before brx_boundary_set when any segment has mode 10. */
 int brx_outlet_chains_set(brx_solver *s, int nchain, const int *offset, const int *faces, const double *slope);
 
+/* Connected face chains of the critical outlets (mode 4): segment s's
+ * chains are seg_chain[s] .. seg_chain[s+1]-1, chain c's faces (global ids,
+ * section order) faces[offset[c] .. offset[c+1]-1] (CriticalOutlet's
+ * chains, src/braids_core/sediment/river_exterior_outlet.py:20-21; the
+ * opening is solved whole, then per wet group of each chain when a group
+ * split occurs). Host arrays, copied; before brx_boundary_set. */
+int brx_critical_chains_set(brx_solver *s, const int *seg_chain, const int *offset, const int *faces);
+
 /* Free-weir outlets (mode 5): param (3, nseg) crest [m], coefficient
  * [m^0.5/s] and effective width [m] per segment (FreeWeir's parameters,
  * src/braids_core/sediment/river_exterior_outlet.py:73-79). Host array,
@@ -112,7 +120,9 @@ int brx_outlet_chains_set(brx_solver *s, int nchain, const int *offset, const in
 int brx_weir_set(brx_solver *s, const double *param);
 
 /* Open-boundary set-up for all segments: hydraulic mode (2 stage, 3 free
- * outflow, 5 free weir: the common subcritical stage whose outgoing Lax-curve
+ * outflow, 4 critical: outgoing characteristic discharge sqrt(g A^3 / B)
+ * on the controlled faces, river_exterior_outlet.h; 5 free weir: the
+ * common subcritical stage whose outgoing Lax-curve
  * discharge equals coefficient x width x head^1.5, river_exterior_outlet.h;
  * 6 total discharge, 9 discharge + water line, 10 normal depth:
  * per face chain the level at which the outgoing characteristic discharge

@@ -98,6 +98,10 @@ typedef struct {
     /* free-weir outlets (mode 5): per segment crest [m], coefficient
      * [m^0.5/s], effective width [m] (3, nb) */
     const double *weir;
+    /* critical outlets (mode 4): the connected face chains of their
+     * segments (critical_offset (nb+1) over chains, chain faces) */
+    const int *crit_seg_chain;                     /* (nb+1) chain range per segment, or NULL */
+    const int *crit_chain_offset, *crit_chain_face;
 } om_ctx;
 
 /* ------------------------------------------------------------------ */
@@ -1272,6 +1276,180 @@ static int om_weir_section(const om_ctx *m, int b, const double *q, const double
     return 0;
 }
 
+/* ------------------------------------------------------------------ */
+/* Critical outlet (mode 4): outgoing characteristic discharge equal to  */
+/* sqrt(g A^3 / B) on the controlled faces of the opening, faces that     */
+/* turn inward or dry removed and the root recomputed                     */
+/* (river_exterior_outlet.h:29-175), per wet group of each chain when a   */
+/* dry bar splits the opening (river_exterior_outlet.py:37-72).           */
+/* ------------------------------------------------------------------ */
+static double om_resolved_bed(const om_ctx *m, int f, const double *q, const double *z)
+{
+    const int c = m->owner[f];
+    const double h = fmax(q[c], 0.), bed = m->exterior_bed[f];
+    if (h >= 1.e-3) return bed;
+    const double bounded = fmax(bed, z[c] - h);
+    double blend = fmin(1., fmax(0., (h - 1.e-4) / 9.e-4));
+    blend = blend * blend * (3. - 2. * blend);
+    return bed + (bounded - bed) * (1. - blend);
+}
+
+static om_section_sum om_crit_residual(const om_ctx *m, const int *faces, int n, double eta, const int *branch,
+                                       const double *invariant, const double *q, const double *z)
+{
+    const double g = m->grav, dry = m->dry;
+    double part[3][OM_LANES];
+    for (int lane = 0; lane < OM_LANES; ++lane) {
+        double a = 0., width = 0., rate = 0.;
+        for (int k = lane; k < n; k += OM_LANES) {
+            const int f = faces[k];
+            if (branch[f] != 1) continue;
+            const double h = fmax(eta - om_resolved_bed(m, f, q, z), 0.);
+            if (h <= dry) continue;
+            a += h * m->length[f]; width += m->length[f]; rate += h * (invariant[f] - 2. * sqrt(g * h)) * m->length[f];
+        }
+        part[0][lane] = a; part[1][lane] = width; part[2][lane] = rate;
+    }
+    om_section_sum r = {0., 0., 0., 0.};
+    for (int lane = 0; lane < OM_LANES; ++lane) { r.area += part[0][lane]; r.width += part[1][lane]; r.rate += part[2][lane]; }
+    r.residual = r.rate - (r.width > 0. ? sqrt(g * r.area * r.area * r.area / r.width) : 0.);
+    return r;
+}
+
+/* One critical section over faces[0..n); 0 or its failure (a trial rejection). */
+static int om_crit_group(const om_ctx *m, const int *faces, int n, const double *q, const double *z, double *trace,
+                         double *flux, int *status, int *branch, double *invariant)
+{
+    const int nc = m->nc, nf = m->nf;
+    const double g = m->grav, dry = m->dry, speed = m->speed_limit, tol = 128. * OM_EPS;
+    int error = 0, done = 0;
+    double eta = 0.;
+    for (int k = 0; k < n; ++k) {
+        const int f = faces[k], c = m->owner[f];
+        branch[f] = 0; invariant[f] = 0.;
+        const double h0 = q[c], h = fmax(h0 + z[c] - om_resolved_bed(m, f, q, z), 0.);
+        if (h0 <= dry || h <= dry) continue;
+        const double un = (q[nc + c] * m->normal[f] + q[2 * nc + c] * m->normal[nf + f]) / h0, wave = sqrt(g * h);
+        if (un < -tol * fmax(1., fabs(un))) continue;
+        if (un > wave * (1. + 1e-10)) { branch[f] = 2; continue; }
+        branch[f] = 1; invariant[f] = un + 2. * wave;
+    }
+    for (int active = 0; active <= n; ++active) {
+        double lo = INFINITY, hi = -INFINITY;
+        int count = 0;
+        for (int k = 0; k < n; ++k) {         /* lane min / max / counts: order-free */
+            const int f = faces[k];
+            if (branch[f] != 1) continue;
+            lo = fmin(lo, om_resolved_bed(m, f, q, z));
+            hi = fmax(hi, q[m->owner[f]] + z[m->owner[f]]);
+            ++count;
+        }
+        if (count) lo += fmax(2. * dry, tol * fmax(1., fabs(lo)));
+        else { done = 1; break; }
+        om_section_sum r = om_crit_residual(m, faces, n, lo, branch, invariant, q, z);
+        if (r.residual < 0.) {                /* unresolved controlled depth: the opening closes */
+            for (int k = 0; k < n; ++k) if (branch[faces[k]] == 1) branch[faces[k]] = 0;
+            done = 1; eta = lo;
+            break;
+        }
+        r = om_crit_residual(m, faces, n, hi, branch, invariant, q, z);
+        for (int j = 0; j < 60 && r.residual > 0.; ++j) {
+            hi = lo + 2. * (hi - lo);
+            r = om_crit_residual(m, faces, n, hi, branch, invariant, q, z);
+        }
+        if (r.residual > 0. || !isfinite(r.residual)) { error = 1; break; }
+        for (int j = 0; j < 90; ++j) {
+            eta = lo + .5 * (hi - lo);
+            if (eta == lo || eta == hi) break;
+            r = om_crit_residual(m, faces, n, eta, branch, invariant, q, z);
+            if (r.residual > 0.) lo = eta; else hi = eta;
+        }
+        eta = lo + .5 * (hi - lo);
+        int changed = 0;
+        for (int k = 0; k < n; ++k) {
+            const int f = faces[k];
+            if (branch[f] != 1) continue;
+            const double h = fmax(eta - om_resolved_bed(m, f, q, z), 0.), un = invariant[f] - 2. * sqrt(g * h);
+            if (h <= dry || un < -tol) { branch[f] = 0; ++changed; }
+        }
+        if (changed) continue;
+        r = om_crit_residual(m, faces, n, eta, branch, invariant, q, z);
+        const double qc = r.width > 0. ? sqrt(g * r.area * r.area * r.area / r.width) : 0.;
+        if (r.area <= 0. || r.width <= 0. || !isfinite(r.residual) || fabs(r.residual) > 1e-10 * fmax(qc, 1.)) error = 2;
+        done = 1;
+        break;
+    }
+    if (!done && !error) error = 3;
+    if (error) return error;
+    for (int k = 0; k < n; ++k) {
+        const int f = faces[k], c = m->owner[f];
+        const double rbed = om_resolved_bed(m, f, q, z), h0 = q[c], geom = fmax(h0 + z[c] - rbed, 0.);
+        const double nx = m->normal[f], ny = m->normal[nf + f];
+        double h = geom, ux = 0., uy = 0.;
+        if (h0 > dry) { ux = q[nc + c] / h0; uy = q[2 * nc + c] / h0; } else h = 0.;
+        double un = ux * nx + uy * ny;
+        const double tx = ux - un * nx, ty = uy - un * ny;
+        if (branch[f] == 0) un = 0.;
+        else if (branch[f] == 1) { h = fmax(eta - rbed, 0.); un = invariant[f] - 2. * sqrt(g * h); }
+        if (!isfinite(h) || !isfinite(un) || sqrt(un * un + tx * tx + ty * ty) > speed) { status[f] = 3; continue; }
+        double water = 0., fx = 0., fy = 0.;
+        if (h > dry) {
+            trace[f] = h; trace[nf + f] = h * (un * nx + tx); trace[2 * nf + f] = h * (un * ny + ty);
+            water = trace[nf + f] * nx + trace[2 * nf + f] * ny;
+            fx = water * trace[nf + f] / h + .5 * g * h * h * nx;
+            fy = water * trace[2 * nf + f] / h + .5 * g * h * h * ny;
+        }
+        const double pressure = h0 > dry ? .5 * g * (h0 * h0 - geom * geom) : 0.;
+        flux[f] = water; flux[nf + f] = fx + pressure * nx; flux[2 * nf + f] = fy + pressure * ny;
+    }
+    return 0;
+}
+
+/* The critical owner of segment b: the whole opening, then, when dry faces
+ * split its chains into several wet groups, each group on its own with the
+ * dry faces closed at their owners' pressure. 0 or a failure. */
+static int om_crit_section(const om_ctx *m, int b, const double *q, const double *z, double *trace, double *flux,
+                           int *status, int *branch, double *invariant, int *scratch)
+{
+    const int nf = m->nf;
+    const double g = m->grav, dry = m->dry;
+    const int *faces = m->boundary_faces + m->boundary_offset[b];
+    const int n = m->boundary_offset[b + 1] - m->boundary_offset[b];
+    int err = om_crit_group(m, faces, n, q, z, trace, flux, status, branch, invariant);
+    if (!m->crit_seg_chain) return err;
+    /* wet groups: runs of wet faces along each chain */
+    int ngroup = 0, nflat = 0, *gfaces = scratch, *gend = scratch + n;
+    for (int ch = m->crit_seg_chain[b]; ch < m->crit_seg_chain[b + 1]; ++ch) {
+        int open = 0;
+        for (int k = m->crit_chain_offset[ch]; k < m->crit_chain_offset[ch + 1]; ++k) {
+            const int f = m->crit_chain_face[k], c = m->owner[f];
+            const double h = q[c], geom = h + z[c] - m->exterior_bed[f];
+            const int wet = (h > dry) && (geom > dry);
+            if (wet) { gfaces[nflat++] = f; open = 1; }
+            else if (open) { gend[ngroup++] = nflat; open = 0; }
+        }
+        if (open) gend[ngroup++] = nflat;
+    }
+    if (ngroup <= 1) return err;
+    int worst = 0, start = 0;
+    for (int gi = 0; gi < ngroup; ++gi) {
+        const int e = om_crit_group(m, gfaces + start, gend[gi] - start, q, z, trace, flux, status, branch, invariant);
+        if (e > worst) worst = e;
+        start = gend[gi];
+    }
+    for (int ch = m->crit_seg_chain[b]; ch < m->crit_seg_chain[b + 1]; ++ch)
+        for (int k = m->crit_chain_offset[ch]; k < m->crit_chain_offset[ch + 1]; ++k) {
+            const int f = m->crit_chain_face[k], c = m->owner[f];
+            const double h = q[c], geom = h + z[c] - m->exterior_bed[f];
+            if ((h > dry) && (geom > dry)) continue;
+            const double height = fmax(q[c], 0.), pressure = .5 * g * height * height;
+            trace[f] = trace[nf + f] = trace[2 * nf + f] = 0.;
+            flux[f] = 0.; flux[nf + f] = pressure * m->normal[f]; flux[2 * nf + f] = pressure * m->normal[nf + f];
+            status[f] = 0;
+        }
+    return worst;
+}
+
 int om_exterior(om_ctx *m, const double *q, const double *z, double time,
                 double *trace, double *flux, int *status, double *work,
                 double *stage_out, double *total_out)
@@ -1376,6 +1554,21 @@ int om_exterior(om_ctx *m, const double *q, const double *z, double time,
     /* section owners of the remaining outlet modes, in the reference's order
      * (river_exterior_bed.py:213-217): a normal-depth failure rejects the
      * trial before the rating owner runs; a rating failure is fatal */
+    {
+        int any = 0;
+        for (int b = 0; b < nb; ++b) any = any || m->seg_mode[b] == 4;
+        if (any) {
+            int *branch = (int *)calloc((size_t)nf, sizeof(int));
+            double *invariant = (double *)calloc((size_t)nf, sizeof(double));
+            int *scratch = (int *)calloc(2 * (size_t)nf + 2, sizeof(int));
+            int crit_failed = 0;
+            for (int b = 0; b < nb; ++b)
+                if (m->seg_mode[b] == 4 && om_crit_section(m, b, q, z, trace, flux, status, branch, invariant, scratch))
+                    crit_failed = 1;
+            free(branch); free(invariant); free(scratch);
+            if (crit_failed) return OM_REJECT_SPATIAL;
+        }
+    }
     if (m->weir) {
         int *branch = (int *)calloc((size_t)nf, sizeof(int));
         double *invariant = (double *)calloc((size_t)nf, sizeof(double));

@@ -61,7 +61,8 @@ class Ctx(C.Structure):
                 ("seg_mode", P), ("stage_policy", P), ("exterior_bed", P), ("forcing", P),
                 ("table_len", I), ("table_time", P), ("table_value", P), ("threads", I),
                 ("turb", P), ("rating_offset", P), ("rating_q", P), ("rating_eta", P),
-                ("nchain", I), ("chain_offset", P), ("chain_face", P), ("chain_slope", P), ("weir", P)]
+                ("nchain", I), ("chain_offset", P), ("chain_face", P), ("chain_slope", P), ("weir", P),
+                ("crit_seg_chain", P), ("crit_chain_offset", P), ("crit_chain_face", P)]
 
 
 class Turbines(C.Structure):
@@ -223,6 +224,12 @@ class Oracle:
             ctx.chain_offset = k("chain_offset", _i32(off))
             ctx.chain_face = k("chain_face", _i32(faces))
             ctx.chain_slope = k("chain_slope", _f64(slope))
+        if nb and np.any(seg_mode == 4):
+            from braids_hkt_gb300.solver import critical_chains
+            segc, off, faces = critical_chains([case])
+            ctx.crit_seg_chain = k("crit_seg_chain", _i32(segc))
+            ctx.crit_chain_offset = k("crit_chain_offset", _i32(off))
+            ctx.crit_chain_face = k("crit_chain_face", _i32(faces))
         if nb and np.any(seg_mode == 5):
             from braids_hkt_gb300.solver import weir_parameters
             ctx.weir = k("weir", _f64(weir_parameters([case])))

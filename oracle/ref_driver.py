@@ -427,6 +427,8 @@ class Ref:
                   g["owner"], g["bid"], g["selected"], self.seg_mode, self.stage_policy, q, self.z,
                   self.exterior_bed, g["normal"], g["length"], self.forcing, weights, total, trace, flux, status)
         # section owners after exterior_flux (ExteriorBed.evaluate, river_exterior_bed.py:213-217)
+        if np.any(self.seg_mode[:nb] == 4):
+            self._critical_outlet(q, trace, flux, status)
         if np.any(self.seg_mode[:nb] == 5):
             from braids_hkt_gb300.solver import weir_parameters
             if "ref_outlet" not in self.libs:
@@ -477,6 +479,41 @@ class Ref:
             if np.any(sec):
                 raise Fatal("Q-H outlet has no admissible subcritical solution within the supplied curve")
         return trace, flux, status
+
+    def _critical_outlet(self, q, trace, flux, status):
+        """The reference's own CriticalOutlet owner (river_exterior_outlet.py:10-72)
+        on a stand-in exterior owner, its kernel the host build of river_exterior_outlet.h."""
+        from braids_core.sediment import river_exterior_outlet as RO
+        from braids_core.sediment.bend_methods_v1 import BendTrialRejected
+        m, g, nb = self.m, self.g, self.nb
+        if not hasattr(self, "_crit"):
+            from braids_support.sediment.river_morphodynamics.sediment_wave import WaveEngine
+            lib = C.CDLL(str(REF / "libref_outlet.so"))
+
+            def engine(backend, threads, source=None, names=None):
+                e = WaveEngine.__new__(WaveEngine)
+                e.backend, e.threads = "cpu", threads
+                e.lib, e.fn = lib, {n: getattr(lib, n) for n in names}
+                for fn in e.fn.values():
+                    fn.restype = None
+                e.identity = {}
+                return e
+            RO.WaveEngine = engine
+            ns = SimpleNamespace
+            data = dict(owner=m.owner, neighbour=m.neighbour, bid=m.bid, mid=m.mid, normal=m.normal, length=m.length,
+                        speed_limit=self.speed_limit)
+            p = ns(g=dict(owner=g["owner"], normal=g["normal"], length=g["length"]), nf=m.nf, n=m.nc,
+                   parameters=ns(gravity=self.grav, dry=self.dry), exterior_bed=self.exterior_bed, flow=ns(threads=1))
+            self._crit_ext = ns(p=p, xp=np, nb=nb, a=ns(backend="cpu", data=data), offset=g["boffset"],
+                                faces=g["bfaces"])
+            controls = {str(b): {"method": "outlet.critical" if self.seg_mode[b] == 4 else "outlet.stage"}
+                        for b in range(nb)}
+            self._crit = RO.CriticalOutlet(self._crit_ext, controls)
+        self._crit_ext.trace, self._crit_ext.flux, self._crit_ext.status = trace, flux, status
+        try:
+            self._crit.evaluate(np.ascontiguousarray(q), self.z)
+        except BendTrialRejected as exc:
+            raise Rejected(str(exc))
 
     # -- one spatial residual --------------------------------------------------
     def rate(self, q, dt, time, base):

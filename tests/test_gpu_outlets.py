@@ -1,5 +1,5 @@
 """Outlet section owners on the GPU: the Q-H rating (mode 11), normal-depth
-(mode 10) and free-weir (mode 5) outlets against
+(mode 10), free-weir (mode 5) and critical (mode 4) outlets against
 the oracle (FP64 to 1e-10 with identical substep counts; mixed against FP64
 to 1e-4 in depth) and its failure without a bracket (the scenario fails,
 failed = 5). The reference fixture is checked in test_gpu_parity."""
@@ -38,7 +38,8 @@ def test_rating_outlet_without_a_bracket_fails_the_scenario():
     assert d[0]["failed"] == 0 and d[1]["failed"] == 5
 
 
-@pytest.mark.parametrize("make", [S.normal_channel, S.weir_channel], ids=["normal", "weir"])
+@pytest.mark.parametrize("make", [S.normal_channel, S.weir_channel, S.critical_channel],
+                         ids=["normal", "weir", "critical"])
 def test_section_outlet_fp64_oracle_and_mixed(make):
     from braids_hkt_gb300.solver import RiverSolver
     from oracle import Oracle
@@ -60,7 +61,7 @@ def test_section_outlet_fp64_oracle_and_mixed(make):
 def test_outlet_modes_batched_equal_alone():
     """Rating and normal-depth outlets in one batch with the stage-outlet channel: bitwise as alone."""
     from braids_hkt_gb300.solver import RiverSolver
-    cases = [S.small_channel(), S.rating_channel(), S.normal_channel(), S.weir_channel()]
+    cases = [S.small_channel(), S.rating_channel(), S.normal_channel(), S.weir_channel(), S.critical_channel()]
     batch = RiverSolver(cases, precision="mixed")
     batch.advance(2.0, 0.0)
     for i, c in enumerate(cases):

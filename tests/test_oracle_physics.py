@@ -180,3 +180,29 @@ def test_free_weir_outlet_discharges_by_the_weir_law():
         out = float(np.sum(water[outlet] * m.length[outlet]))
         law = w_["coefficient_m_half_s"] * w_["effective_width_m"] * max(stage - w_["crest_m"], 0.0) ** 1.5
         assert abs(out - law) <= 0.02 * law
+
+
+def test_critical_outlet_passes_critical_flow():
+    """Critical outlet (mode 4): the discharge over a short window equals the
+    critical flow sum(len sqrt(g) (2E/3)^1.5) of the outlet cells' specific
+    energy E = h + un^2 / 2g to 3%, while the channel drains through it."""
+    case = S.critical_channel()
+    o = Oracle(case, threads=4)
+    q = case["q"].copy()
+    m = case["mesh"]
+    g = case["controls"]["grav"]
+    outlet = (m.neighbour < 0) & (m.bid == 1)
+    owners = m.owner[outlet]
+    t = 0.0
+    for k in range(3):
+        st, _, _ = o.advance(q, 10.0, t)
+        t += 10.0
+        h = q[0][owners]
+        un = (q[1][owners] * m.normal[0, outlet] + q[2][owners] * m.normal[1, outlet]) / h
+        energy = h + un * un / (2 * g)
+        critical = float(np.sum(m.length[outlet] * np.sqrt(g) * (2 * energy / 3) ** 1.5))
+        st2, water, _ = o.advance(q, 0.1, t)
+        t += 0.1
+        assert st == 0 and st2 == 0
+        out = float(np.sum(water[outlet] * m.length[outlet]))
+        assert abs(out - critical) <= 0.03 * critical
