@@ -486,10 +486,9 @@ extern "C" int brx_boundary_set(brx_solver *s, const int *seg_mode, const int *s
         if (stage_policy[sg] != 0 && stage_policy[sg] != 1) return fail(BRX_ERR_ARGUMENT, "stage policy must be 0 or 1");
         if (!std::isfinite(forcing[sg]) || !std::isfinite(forcing[nseg + sg])) return fail(BRX_ERR_ARGUMENT, "nonfinite forcing");
     }
-    if (s->method == BRX_METHOD_HLLC)
-        for (int sg = 0; sg < nseg; ++sg)
-            if (seg_mode[sg] == 9) return fail(BRX_ERR_UNSUPPORTED, "the HLLC method has no stage-discharge inlet (mode 9)");
     s->h_seg_mode.assign(seg_mode, seg_mode + nseg);
+    const int inlet = std::count(seg_mode, seg_mode + nseg, 9) > 0;
+    if (inlet != s->bnd.inlet) { s->bnd.inlet = inlet; s->graph_dirty = true; }
     std::vector<int> bmode(nf, 0);
     std::vector<double> ext(std::max(s->nslot, 1));
     for (int k = 0; k < s->nslot; ++k) {
@@ -871,8 +870,6 @@ extern "C" int brx_method_set(brx_solver *s, int method)
         if (s->precision != BRX_FP64) return fail(BRX_ERR_UNSUPPORTED, "the HLLC method runs in the FP64 form");
         if (!s->hllc_ready) return fail(BRX_ERR_STATE, "HLLC stencil not installed (brx_hllc_set)");
         if (s->maxdeg > MAX_CELL_FACES) return fail(BRX_ERR_UNSUPPORTED, "cell with too many faces");
-        for (int md : s->h_seg_mode)
-            if (md == 9) return fail(BRX_ERR_UNSUPPORTED, "the HLLC method has no stage-discharge inlet (mode 9)");
     }
     s->method = method;
     s->turb.balanced = method == BRX_METHOD_FWAVE;

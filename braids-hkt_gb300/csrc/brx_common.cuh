@@ -180,6 +180,7 @@ struct BoundaryDev {
     const int *crit_seg_chain;           // (nseg+1) critical-outlet chains per segment, or null
     const int *crit_chain_off, *crit_chain_slot;
     int *gslot, *gend;       // (nslot) wet-group scratch of the critical outlets
+    int inlet;               // a mode-9 (exact-discharge inlet) segment exists
 };
 
 // Accepted / stage state buffers.

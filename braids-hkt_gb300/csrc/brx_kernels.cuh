@@ -431,8 +431,9 @@ __device__ int normal_chain(const MeshDev &m, const BoundaryDev &b, int ch, doub
 constexpr int SECTION_LANES = 128;
 
 struct SectionWork {
-    double part[3][SECTION_LANES];
+    double part[6][SECTION_LANES];
     double lo, hi, eta, residual, area, width, rate;
+    double velocity, gross, derivative, scale;
     int error, done, stagnant, changed, count;
 };
 
@@ -844,6 +845,231 @@ __device__ int crit_section(SectionWork &w, const MeshDev &m, const BoundaryDev 
     return worst;
 }
 
+// ---------------------------------------------------------------------------
+// Exact-discharge inlet (mode 9, river_exterior_inlet.h): the exact 1-D SWE
+// Riemann solution between a virtual reservoir at the requested water line
+// and each face's interior state; the reservoir's common normal velocity is
+// solved (bracket, then safeguarded Newton with the analytical derivative)
+// so that the net section discharge equals the request.
+// ---------------------------------------------------------------------------
+struct InletRiemann {
+    double h, u, derivative;
+    int iterations, error;
+};
+
+__device__ __forceinline__ void inlet_wave(double h, double hk, double g, double &f, double &df)
+{
+    if (h > hk) {
+        const double a = sqrt(.5 * g * (1. / h + 1. / hk));
+        f = (h - hk) * a;
+        df = a - .25 * g * (h - hk) / (a * h * h);
+    } else {
+        const double c = sqrt(g * h);
+        f = 2. * (c - sqrt(g * hk));
+        df = sqrt(g / h);
+    }
+}
+
+// river_exterior_inlet.h:32-69: left = reservoir, right = interior (normal into the domain)
+__device__ InletRiemann inlet_exact(double hl, double ul, double hr, double ur, double g)
+{
+    InletRiemann r = {0., 0., 0., 0, 0};
+    const double cl = sqrt(g * hl), cr = sqrt(g * hr);
+    if (hl == 0. && hr == 0.) return r;
+    if (hr == 0. || hl == 0. || ur - ul >= 2. * (cl + cr)) {
+        if (hl > 0. && ul - cl >= 0.) { r.h = hl; r.u = ul; r.derivative = hl; }
+        else if (hl > 0. && ul + 2. * cl > 0.) { r.u = (ul + 2. * cl) / 3.; r.h = r.u * r.u / g; r.derivative = r.h; }
+        else if (hr > 0. && ur + cr <= 0.) { r.h = hr; r.u = ur; }
+        else if (hr > 0. && ur - 2. * cr < 0.) { r.u = (ur - 2. * cr) / 3.; r.h = r.u * r.u / g; }
+        return r;
+    }
+    double guess = .5 * (cl + cr) - .25 * (ur - ul);
+    guess = guess * guess / g;
+    double lo = 0., hi = fmax(fmax(hl, hr), guess), fl, fr, dl, dr;
+    inlet_wave(hi, hl, g, fl, dl);
+    inlet_wave(hi, hr, g, fr, dr);
+    for (int j = 0; j < 60 && fl + fr + ur - ul < 0.; ++j) {
+        hi *= 2.;
+        inlet_wave(hi, hl, g, fl, dl);
+        inlet_wave(hi, hr, g, fr, dr);
+    }
+    if (!isfinite(hi) || fl + fr + ur - ul < 0.) { r.error = 1; return r; }
+    const double scale = fmax(1., cl + cr + fabs(ul) + fabs(ur));
+    double h = fmax(fmin(guess, hi), 1e-30), residual = 0.;
+    for (int j = 0; j < 70; ++j) {
+        inlet_wave(h, hl, g, fl, dl);
+        inlet_wave(h, hr, g, fr, dr);
+        residual = fl + fr + ur - ul;
+        r.iterations = j + 1;
+        if (fabs(residual) <= 4e-14 * scale) break;
+        if (residual < 0.) lo = h; else hi = h;
+        double next = h - residual / (dl + dr);
+        if (!(next > lo && next < hi)) next = lo + .5 * (hi - lo);
+        h = next;
+    }
+    inlet_wave(h, hl, g, fl, dl);
+    inlet_wave(h, hr, g, fr, dr);
+    residual = fl + fr + ur - ul;
+    if (!isfinite(h) || fabs(residual) > 2e-11 * scale) { r.error = 2; return r; }
+    const double u = .5 * (ul + ur + fr - fl), c = sqrt(g * h);
+    r.h = h; r.u = u; r.derivative = fmax(0., (u + h * dr) / (dl + dr));
+    if (u >= 0.) {
+        if (h > hl) {
+            if (ul - sqrt(.5 * g * h * (h + hl) / hl) >= 0.) { r.h = hl; r.u = ul; r.derivative = hl; }
+        } else if (ul - cl >= 0.) { r.h = hl; r.u = ul; r.derivative = hl; }
+        else if (u - c > 0.) { r.u = (ul + 2. * cl) / 3.; r.h = r.u * r.u / g; r.derivative = r.h; }
+    } else {
+        if (h > hr) {
+            if (ur + sqrt(.5 * g * h * (h + hr) / hr) <= 0.) { r.h = hr; r.u = ur; r.derivative = 0.; }
+        } else if (ur + cr <= 0.) { r.h = hr; r.u = ur; r.derivative = 0.; }
+        else if (u + c < 0.) { r.u = (ur - 2. * cr) / 3.; r.h = r.u * r.u / g; r.derivative = 0.; }
+    }
+    return r;
+}
+
+// Interior depth above the face's exterior bed and inward normal speed of slot k.
+__device__ __forceinline__ void inlet_interior(const MeshDev &m, const BoundaryDev &b, int k, double dry,
+                                               const double *q, const double *z, double &hi, double &ui)
+{
+    const int nc = m.nc, f = b.slot_face[k], c = m.owner[f];
+    const double h0 = q[c];
+    hi = h0 > dry ? fmax(h0 + z[c] - b.ext_bed[k], 0.) : 0.;
+    if (hi <= dry) hi = 0.;
+    ui = h0 > dry ? -(q[nc + c] * m.normal[f] + q[2 * nc + c] * m.normal[m.nf + f]) / h0 : 0.;
+}
+
+// river_exterior_inlet.h:71-95: section discharge, its derivative and the
+// gross throughflow at the common velocity w.velocity (lane sums, lane order).
+__device__ void inlet_rate(SectionWork &w, const MeshDev &m, const BoundaryDev &b, int k0, int k1, double requested,
+                           double g, double dry, const double *q, const double *z)
+{
+    for (int lane = threadIdx.x; lane < SECTION_LANES; lane += blockDim.x) {
+        double rate = 0., derivative = 0., gross = 0.;
+        int error = 0;
+        for (int k = k0 + lane; k < k1; k += SECTION_LANES) {
+            double hi, ui;
+            inlet_interior(m, b, k, dry, q, z, hi, ui);
+            double hr = fmax(requested - b.ext_bed[k], 0.);
+            if (hr <= dry) hr = 0.;
+            const InletRiemann r = inlet_exact(hr, w.velocity, hi, ui, g);
+            const double len = m.length[b.slot_face[k]];
+            rate += r.h * r.u * len; derivative += r.derivative * len;
+            gross += fabs(r.h * r.u * len);
+            error = max(error, r.error);
+        }
+        w.part[0][lane] = rate; w.part[1][lane] = derivative; w.part[4][lane] = error; w.part[5][lane] = gross;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        w.rate = w.derivative = w.gross = 0.;
+        for (int lane = 0; lane < SECTION_LANES; ++lane) {
+            w.rate += w.part[0][lane]; w.derivative += w.part[1][lane]; w.gross += w.part[5][lane];
+            if (w.part[4][lane] != 0.) w.error = 5;
+        }
+    }
+    __syncthreads();
+}
+
+// river_exterior_inlet.h:97-186: the inlet of segment sg. Returns 0 or the
+// section failure (a trial rejection in the reference); `bad` gets the faces
+// whose Riemann solution failed or exceeds the speed limit (face status 3).
+__device__ int inlet_section(SectionWork &w, const MeshDev &m, const BoundaryDev &b, int sg, double g, double dry,
+                             double speed, const double *q, const double *z, bool &bad)
+{
+    const int nc = m.nc, nf = m.nf, nseg = b.nseg, k0 = b.seg_off[sg], k1 = b.seg_off[sg + 1];
+    const size_t ns = b.nslot;
+    const double Q = b.forcing[sg], requested = b.forcing[nseg + sg];
+    if (threadIdx.x == 0) w.error = 0;
+    for (int lane = threadIdx.x; lane < SECTION_LANES; lane += blockDim.x) {
+        double area = 0., scale = 1.;
+        for (int k = k0 + lane; k < k1; k += SECTION_LANES) {
+            double hi, ui;
+            inlet_interior(m, b, k, dry, q, z, hi, ui);
+            const double hr = fmax(requested - b.ext_bed[k], 0.);
+            if (hr > dry) area += hr * m.length[b.slot_face[k]];
+            scale = fmax(scale, fabs(ui) + 2. * sqrt(g * hi) + 2. * sqrt(g * hr));
+        }
+        w.part[0][lane] = area; w.part[1][lane] = scale;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        w.area = 0.; w.scale = 1.;
+        for (int lane = 0; lane < SECTION_LANES; ++lane) { w.area += w.part[0][lane]; w.scale = fmax(w.scale, w.part[1][lane]); }
+        if (!isfinite(Q) || Q < 0. || !isfinite(requested) || (Q > 0. && w.area <= 0.)) w.error = 1;
+        w.velocity = w.area > 0. ? Q / w.area : 0.;
+        w.scale = fmax(w.scale, 1. + fabs(w.velocity));
+    }
+    __syncthreads();
+    if (Q > 0. && !w.error) {
+        if (threadIdx.x == 0) { w.lo = w.velocity - w.scale; w.hi = w.velocity + w.scale; w.velocity = w.lo; }
+        __syncthreads();
+        inlet_rate(w, m, b, k0, k1, requested, g, dry, q, z);
+        for (int j = 0; j < 60 && w.rate > Q && !w.error; ++j) {
+            if (threadIdx.x == 0) { w.lo -= w.scale; w.scale *= 2.; w.velocity = w.lo; }
+            __syncthreads();
+            inlet_rate(w, m, b, k0, k1, requested, g, dry, q, z);
+        }
+        const bool low_bad = w.rate > Q;
+        __syncthreads();
+        if (threadIdx.x == 0) { if (low_bad) w.error = 2; w.velocity = w.hi; }
+        __syncthreads();
+        inlet_rate(w, m, b, k0, k1, requested, g, dry, q, z);
+        for (int j = 0; j < 60 && w.rate < Q && !w.error; ++j) {
+            if (threadIdx.x == 0) { w.hi += w.scale; w.scale *= 2.; w.velocity = w.hi; }
+            __syncthreads();
+            inlet_rate(w, m, b, k0, k1, requested, g, dry, q, z);
+        }
+        const bool high_bad = w.rate < Q;
+        __syncthreads();
+        if (threadIdx.x == 0) { if (high_bad) w.error = 2; w.velocity = fmin(w.hi, fmax(w.lo, Q / w.area)); }
+        __syncthreads();
+        for (int j = 0; j < 80 && !w.error; ++j) {
+            inlet_rate(w, m, b, k0, k1, requested, g, dry, q, z);
+            // net Q may be far below the signed face throughflow: relative
+            // tolerance plus a double-precision budget on the gross flow
+            if (fabs(w.rate - Q) <= 3e-13 * Q + 256. * EPS * w.gross) break;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                if (w.rate < Q) w.lo = w.velocity; else w.hi = w.velocity;
+                double next = w.derivative > 0. ? w.velocity + (Q - w.rate) / w.derivative : w.lo + .5 * (w.hi - w.lo);
+                if (!(next > w.lo && next < w.hi)) next = w.lo + .5 * (w.hi - w.lo);
+                w.velocity = next;
+            }
+            __syncthreads();
+        }
+        inlet_rate(w, m, b, k0, k1, requested, g, dry, q, z);
+        const bool final_bad = !isfinite(w.rate) || fabs(w.rate - Q) > 1e-10 * Q + 1024. * EPS * w.gross;
+        __syncthreads();
+        if (threadIdx.x == 0 && final_bad) w.error = 3;
+        __syncthreads();
+    }
+    const int error = w.error;
+    const double velocity = w.velocity;
+    __syncthreads();
+    if (error) return error;
+    for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+        const int f = b.slot_face[k], c = m.owner[f];
+        const double nx = m.normal[f], ny = m.normal[nf + f], h0 = q[c];
+        double hi, ui;
+        inlet_interior(m, b, k, dry, q, z, hi, ui);
+        const double vt = h0 > dry ? (-q[nc + c] * ny + q[2 * nc + c] * nx) / h0 : 0.;
+        double hr = fmax(requested - b.ext_bed[k], 0.);
+        if (hr <= dry) hr = 0.;
+        InletRiemann r = Q == 0. ? inlet_exact(h0, -ui, h0, ui, g) : inlet_exact(hr, velocity, hi, ui, g);
+        if (Q == 0.) r.u = 0.;
+        if (r.error || !isfinite(r.h) || !isfinite(r.u) || fabs(r.u) > speed) { bad = true; continue; }
+        const double water = -r.h * r.u, tangent = r.u < 0. ? vt : 0.;
+        b.trace[k] = r.h; b.trace[ns + k] = water * nx - r.h * tangent * ny; b.trace[2 * ns + k] = water * ny + r.h * tangent * nx;
+        const double pressure = Q == 0. ? 0. : .5 * g * (h0 * h0 - hi * hi);
+        const double momentum = r.h * r.u * r.u + .5 * g * r.h * r.h + pressure;
+        b.flux[k] = water;
+        b.flux[ns + k] = momentum * nx - water * tangent * ny;
+        b.flux[2 * ns + k] = momentum * ny + water * tangent * nx;
+    }
+    __syncthreads();
+    return 0;
+}
+
 // stage 1 / 2: the SSPRK stages (state work / q1, its own stock, clock t or
 // t + dt); STAGE_HANCOCK: the HLLC predicted state q1 at t + dt/2, outlet
 // stock of the substep's start state work (hllc.py:91-97), status of stage 1.
@@ -903,10 +1129,7 @@ __global__ void k_boundary(MeshDev m, StateDev s, BoundaryDev b, Ctrl *ctrl, int
         double w = 0.;
         const double bed = b.ext_bed[k];
         const int mode = b.seg_mode[sg];
-        if (mode == 9) {
-            const double h = fmax(b.forcing[nseg + sg] - bed, 0.);
-            if (h > dry) w = h * m.length[f];
-        } else if (mode == 6 && b.seg_sums[nseg + sg] > 0.) {
+        if (mode == 6 && b.seg_sums[nseg + sg] > 0.) {
             const double h = fmax(q[c] + z[c] - bed, 0.);
             const double section = fmax(b.seg_sums[sg] / b.seg_sums[nseg + sg] - bed, 0.);
             if (h > dry && section > 0.)
@@ -925,15 +1148,11 @@ __global__ void k_boundary(MeshDev m, StateDev s, BoundaryDev b, Ctrl *ctrl, int
         const double total = b.seg_sums[2 * (size_t)nseg + sg];
         const double Q = b.forcing[sg], stagev = b.forcing[nseg + sg];
         int st = 0;
-        if (!(mode == 4 || mode == 5 || mode == 10 || mode == 11)) {
+        if (!(mode == 4 || mode == 5 || mode == 9 || mode == 10 || mode == 11)) {
             double h = fmax(h0 + z[c] - bed, 0.), geometric = h, ux = 0., uy = 0.;
             if (h0 > dry) { ux = q[nc + c] / h0; uy = q[2 * nc + c] / h0; }
             double un = ux * nx + uy * ny, tx = ux - un * nx, ty = uy - un * ny, normal_speed = 0.;
-            if (mode == 9) {
-                h = fmax(stagev - bed, 0.); tx = ty = 0.;
-                if (Q > 0. && total <= 0.) st = 1;
-                else if (h > dry && Q > 0.) normal_speed = -Q / total;
-            } else if (mode == 6) {
+            if (mode == 6) {
                 if (Q > 0. && total <= 0.) st = 1;
                 else if (h > dry && Q > 0.) normal_speed = -Q * b.terms[2 * (size_t)b.nslot + k] / (total * h * m.length[f]);
             } else if (mode == 3) {
@@ -979,7 +1198,6 @@ __global__ void k_boundary(MeshDev m, StateDev s, BoundaryDev b, Ctrl *ctrl, int
                     fy = water * tr2 / h + .5 * grav * h * h * ny;
                 }
                 double pressure = h0 > dry ? .5 * grav * (h0 * h0 - geometric * geometric) : 0.;
-                if (mode == 9 && h <= dry) pressure = h0 > dry ? .5 * grav * h0 * h0 : 0.;
                 fl0 = water; fl1 = fx + pressure * nx; fl2 = fy + pressure * ny;
             }
         }
@@ -996,7 +1214,18 @@ __global__ void k_boundary(MeshDev m, StateDev s, BoundaryDev b, Ctrl *ctrl, int
     __shared__ SectionWork section;
     if (threadIdx.x == 0) section_reject = 0;
     __syncthreads();
-    if (b.branch) {
+    if (b.inlet) {
+        bool inlet_failed = false;
+        for (int sg = s0; sg < s1; ++sg)              // block-uniform: the CTA solves one section at a time
+            if (b.seg_mode[sg] == 9) {
+                bool sbad = false;
+                if (inlet_section(section, m, b, sg, grav, dry, ct.speed_limit, q, z, sbad)) inlet_failed = true;
+                if (sbad) bad = 1;
+            }
+        if (threadIdx.x == 0 && inlet_failed) section_reject = 1;
+        __syncthreads();
+    }
+    if (b.branch && !section_reject) {
         bool crit_failed = false;
         for (int sg = s0; sg < s1; ++sg)              // block-uniform: the CTA solves one section at a time
             if (b.seg_mode[sg] == 4) {
@@ -1062,6 +1291,51 @@ __global__ void k_boundary(MeshDev m, StateDev s, BoundaryDev b, Ctrl *ctrl, int
             b.flux[k] = water * scale;
             b.trace[(size_t)b.nslot + k] *= scale;
             b.trace[2 * (size_t)b.nslot + k] *= scale;
+        }
+    }
+    if (!b.inlet) return;
+    // exact-discharge inlet allocation (inlet_feasibility.py:34-57): each
+    // owner's outward inlet debit capped by its stock after its other
+    // boundary debits (owner factor kept per slot in terms), then per inlet
+    // segment the removed outflow taken from its incoming faces; sums in
+    // boundary order, as the reference's bincounts
+    __syncthreads();
+    const size_t ns = b.nslot;
+    for (int u = u0 + threadIdx.x; u < u1; u += blockDim.x) {
+        const int c = b.own_cell[u];
+        double total = 0., reserved = 0.;
+        for (int j = b.own_off[u]; j < b.own_off[u + 1]; ++j) {
+            const int k = b.own_slot[j], f = b.slot_face[k];
+            const double rate = fmax(b.flux[k], 0.) * m.length[f];
+            if (b.seg_mode[m.bid[f]] == 9) total += rate; else reserved += rate;
+        }
+        const double available = fmax(0., base[c] * m.area[c] / ct.trial - reserved);
+        const double ratio = fmin(1., available / fmax(total, 1e-300)) * (1. - 32. * EPS);
+        const double factor = total > available ? ratio : 1.;
+        for (int j = b.own_off[u]; j < b.own_off[u + 1]; ++j) b.terms[b.own_slot[j]] = factor;
+    }
+    __syncthreads();
+    for (int sg = s0 + threadIdx.x; sg < s1; sg += blockDim.x) {
+        if (b.seg_mode[sg] != 9) continue;
+        double removed = 0., incoming = 0.;
+        for (int k = b.seg_off[sg]; k < b.seg_off[sg + 1]; ++k) {
+            const double water = b.flux[k], len = m.length[b.slot_face[k]];
+            removed += water > 0. ? fmax(water, 0.) * len * (1. - b.terms[k]) : 0.;
+            incoming += fmax(-water, 0.) * len;
+        }
+        const bool feasible = removed <= incoming;
+        const double in_scale = incoming > 0. ? 1. - removed / fmax(incoming, 1e-300) : 1.;
+        for (int k = b.seg_off[sg]; k < b.seg_off[sg + 1]; ++k) {
+            const double water = b.flux[k];
+            const double scale = (feasible && water > 0.) ? b.terms[k] : ((feasible && water < 0.) ? in_scale : 1.);
+            const double depth = b.trace[k], denom = fmax(depth, 1e-300);
+            const double ux = depth > 0. ? b.trace[ns + k] / denom : 0.;
+            const double uy = depth > 0. ? b.trace[2 * ns + k] / denom : 0.;
+            b.flux[ns + k] += (scale * scale - 1.) * water * ux;
+            b.flux[2 * ns + k] += (scale * scale - 1.) * water * uy;
+            b.flux[k] = water * scale;
+            b.trace[ns + k] *= scale;
+            b.trace[2 * ns + k] *= scale;
         }
     }
 }

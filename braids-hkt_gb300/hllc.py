@@ -104,8 +104,6 @@ def pack(cases, cell_offset, face_offset):
     """Concatenated HLLC stencil of a scenario batch (global indices)."""
     codes, others, geos, invs = [], [], [], []
     for i, case in enumerate(cases):
-        if np.any(np.asarray(case.get("seg_mode", []), dtype=int) == 9):
-            raise ValueError("the HLLC method has no stage-discharge inlet (mode 9)")
         code, other, geo, inv = entry_records(case["mesh"])
         F0, C0 = int(face_offset[i]), int(cell_offset[i])
         codes.append(np.where(code >= 0, code + F0, ~(~code + F0)).astype(np.int32))

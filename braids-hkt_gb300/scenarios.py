@@ -277,6 +277,19 @@ def normal_channel(discharge=20.0, bed_slope=2e-3, **kw):
     return case
 
 
+def stage_discharge_channel(discharge=20.0, reference_stage=3.05, **kw):
+    """The small channel fed through an exact-discharge inlet (mode 9): the
+    inflow `discharge` is imposed exactly through boundary Riemann solutions
+    against a virtual reservoir whose water line is `reference_stage` [m]; the
+    outlet keeps its fixed stage."""
+    case = small_channel(discharge=discharge, **kw)
+    case["seg_mode"] = np.array([9, M.MODE_STAGE], np.int32)
+    case["forcing"] = case["forcing"].copy()
+    case["forcing"][1, 0] = float(reference_stage)
+    case["name"] = "stage_discharge_channel"
+    return case
+
+
 def lake_at_rest(length=80.0, width=40.0, spacing=4.0, seed=11, islands=True):
     """Variable bed with emerged islands, flat surface at 1.0 m, closed walls (no open segments)."""
     mesh = M.channel_mesh(length, width, spacing, 1.0, seed)
@@ -300,7 +313,7 @@ def hydraulic_jump(length=60.0, width=3.0, spacing=0.5, seed=17, froude=2.5, h1=
     """A stationary hydraulic jump on a flat frictionless channel.
 
     Supercritical inflow of depth h1 at Froude number `froude` through a
-    mode-9 inlet (prescribed water line, uniform normal speed Q / (h W)); the
+    mode-9 inlet (the exact discharge Q with reference water line h1); the
     outlet stage at the conjugate depth h2 = h1 (sqrt(1 + 8 Fr^2) - 1) / 2
     (Belanger); the initial state is the two conjugate states either side of
     mid-channel with the unit discharge q = h1 u1 throughout.

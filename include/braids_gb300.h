@@ -124,7 +124,11 @@ int brx_weir_set(brx_solver *s, const double *param);
  * on the controlled faces, river_exterior_outlet.h; 5 free weir: the
  * common subcritical stage whose outgoing Lax-curve
  * discharge equals coefficient x width x head^1.5, river_exterior_outlet.h;
- * 6 total discharge, 9 discharge + water line, 10 normal depth:
+ * 6 total discharge; 9 exact discharge with a reference water line (the
+ * forcing stage): boundary Riemann solutions against a virtual reservoir at
+ * that line whose common normal velocity makes the net section discharge
+ * exact, then the stock-aware inlet allocation, river_exterior_inlet.h and
+ * src/braids_core/hydraulics/inlet_feasibility.py; 10 normal depth:
  * per face chain the level at which the outgoing characteristic discharge
  * equals the uniform-flow conveyance, river_normal_outlet.h; 11 Q-H rating
  * curve: one common water elevation at which the outgoing characteristic
@@ -274,8 +278,7 @@ long long brx_solver_bytes(const brx_solver *s);
  *                        cell centroid x, y
  *   inverse (3, nc)      pinv of sum d d^T / |d|^2 over neighbours and walls
  *                        (open faces excluded): i11, i12, i22
- * Host arrays, copied. Stage-discharge inlets (mode 9) are not supported by
- * this method (the reference pairs them with its inlet-feasibility owner). */
+ * Host arrays, copied. */
 int brx_hllc_set(brx_solver *s, const int *entry_face, const int *entry_other, const double *entry_geo,
                  const double *inverse);
 

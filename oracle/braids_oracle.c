@@ -118,6 +118,15 @@ static inline int om_open(const om_ctx *m, int f)
     return m->neighbour[f] < 0 && m->bid[f] >= 0;
 }
 
+/* Mode-9 segments exist: the exact-discharge inlet owner and its stock-aware
+ * allocation run (river_exterior_bed.py:103-105, river_explicit_boundary_budget.py:12). */
+static inline int om_has_inlet(const om_ctx *m)
+{
+    for (int b = 0; b < m->nb; ++b)
+        if (m->seg_mode[b] == 9) return 1;
+    return 0;
+}
+
 /* ------------------------------------------------------------------ */
 /* GeoClaw Riemann type (riemanntype, maxiter = 1)                     */
 /* augmented_fwave.cu:33-105                                            */
@@ -1277,6 +1286,253 @@ static int om_weir_section(const om_ctx *m, int b, const double *q, const double
 }
 
 /* ------------------------------------------------------------------ */
+/* Prescribed-discharge inlet with a reference water line (mode 9): the   */
+/* exact one-dimensional SWE Riemann solution between a virtual reservoir */
+/* at the requested line and each face's interior state, the reservoir's  */
+/* common normal velocity solved for the exact net section discharge      */
+/* (src/braids_core/sediment/river_exterior_inlet.h:20-205).              */
+/* ------------------------------------------------------------------ */
+typedef struct { double h, u, derivative; int iterations, error; } om_inlet_riemann;
+
+static void om_inlet_wave(double h, double hk, double g, double *f, double *df)
+{
+    if (h > hk) {
+        const double a = sqrt(.5 * g * (1. / h + 1. / hk));
+        *f = (h - hk) * a;
+        *df = a - .25 * g * (h - hk) / (a * h * h);
+    } else {
+        const double c = sqrt(g * h);
+        *f = 2. * (c - sqrt(g * hk));
+        *df = sqrt(g / h);
+    }
+}
+
+static om_inlet_riemann om_inlet_exact(double hl, double ul, double hr, double ur, double g)
+{
+    om_inlet_riemann r = {0., 0., 0., 0, 0};
+    const double cl = sqrt(g * hl), cr = sqrt(g * hr);
+    if (hl == 0. && hr == 0.) return r;
+    if (hr == 0. || hl == 0. || ur - ul >= 2. * (cl + cr)) {        /* a dry side or vacuum */
+        if (hl > 0. && ul - cl >= 0.) { r.h = hl; r.u = ul; r.derivative = hl; }
+        else if (hl > 0. && ul + 2. * cl > 0.) { r.u = (ul + 2. * cl) / 3.; r.h = r.u * r.u / g; r.derivative = r.h; }
+        else if (hr > 0. && ur + cr <= 0.) { r.h = hr; r.u = ur; }
+        else if (hr > 0. && ur - 2. * cr < 0.) { r.u = (ur - 2. * cr) / 3.; r.h = r.u * r.u / g; }
+        return r;
+    }
+    /* the star depth: safeguarded Newton on the shock / rarefaction curves */
+    double guess = .5 * (cl + cr) - .25 * (ur - ul);
+    guess = guess * guess / g;
+    double lo = 0., hi = fmax(fmax(hl, hr), guess), fl, fr, dl, dr;
+    om_inlet_wave(hi, hl, g, &fl, &dl);
+    om_inlet_wave(hi, hr, g, &fr, &dr);
+    for (int j = 0; j < 60 && fl + fr + ur - ul < 0.; ++j) {
+        hi *= 2.;
+        om_inlet_wave(hi, hl, g, &fl, &dl);
+        om_inlet_wave(hi, hr, g, &fr, &dr);
+    }
+    if (!isfinite(hi) || fl + fr + ur - ul < 0.) { r.error = 1; return r; }
+    double h = fmax(fmin(guess, hi), 1e-30), residual = 0.;
+    for (int j = 0; j < 70; ++j) {
+        om_inlet_wave(h, hl, g, &fl, &dl);
+        om_inlet_wave(h, hr, g, &fr, &dr);
+        residual = fl + fr + ur - ul;
+        r.iterations = j + 1;
+        if (fabs(residual) <= 4e-14 * fmax(1., cl + cr + fabs(ul) + fabs(ur))) break;
+        if (residual < 0.) lo = h; else hi = h;
+        double next = h - residual / (dl + dr);
+        if (!(next > lo && next < hi)) next = lo + .5 * (hi - lo);
+        h = next;
+    }
+    om_inlet_wave(h, hl, g, &fl, &dl);
+    om_inlet_wave(h, hr, g, &fr, &dr);
+    residual = fl + fr + ur - ul;
+    if (!isfinite(h) || fabs(residual) > 2e-11 * fmax(1., cl + cr + fabs(ul) + fabs(ur))) { r.error = 2; return r; }
+    const double u = .5 * (ul + ur + fr - fl), c = sqrt(g * h);
+    r.h = h; r.u = u; r.derivative = fmax(0., (u + h * dr) / (dl + dr));
+    if (u >= 0.) {
+        if (h > hl) {
+            const double shock = ul - sqrt(.5 * g * h * (h + hl) / hl);
+            if (shock >= 0.) { r.h = hl; r.u = ul; r.derivative = hl; }
+        } else if (ul - cl >= 0.) { r.h = hl; r.u = ul; r.derivative = hl; }
+        else if (u - c > 0.) { r.u = (ul + 2. * cl) / 3.; r.h = r.u * r.u / g; r.derivative = r.h; }
+    } else {
+        if (h > hr) {
+            const double shock = ur + sqrt(.5 * g * h * (h + hr) / hr);
+            if (shock <= 0.) { r.h = hr; r.u = ur; r.derivative = 0.; }
+        } else if (ur + cr <= 0.) { r.h = hr; r.u = ur; r.derivative = 0.; }
+        else if (u + c < 0.) { r.u = (ur - 2. * cr) / 3.; r.h = r.u * r.u / g; r.derivative = 0.; }
+    }
+    return r;
+}
+
+typedef struct { double rate, derivative, area, gross; int max_inner, error; } om_inlet_sum;
+
+static om_inlet_sum om_inlet_rate(const om_ctx *m, const int *faces, int n, double velocity, double requested,
+                                  const double *q, const double *z, int max_inner)
+{
+    const int nc = m->nc, nf = m->nf;
+    const double g = m->grav, dry = m->dry;
+    double part[6][OM_LANES];
+    for (int lane = 0; lane < OM_LANES; ++lane) {
+        double rate = 0., derivative = 0., area = 0., inner = 0., error = 0., gross = 0.;
+        for (int k = lane; k < n; k += OM_LANES) {
+            const int f = faces[k], o = m->owner[f];
+            const double bed = m->exterior_bed[f], h0 = q[o];
+            double hi = h0 > dry ? fmax(h0 + z[o] - bed, 0.) : 0.;
+            if (hi <= dry) hi = 0.;
+            const double ui = h0 > dry ? -(q[nc + o] * m->normal[f] + q[2 * nc + o] * m->normal[nf + f]) / h0 : 0.;
+            double hr = fmax(requested - bed, 0.);
+            if (hr <= dry) hr = 0.;
+            const om_inlet_riemann r = om_inlet_exact(hr, velocity, hi, ui, g);
+            rate += r.h * r.u * m->length[f]; derivative += r.derivative * m->length[f]; area += r.h * m->length[f];
+            gross += fabs(r.h * r.u * m->length[f]);
+            inner = fmax(inner, r.iterations); error = fmax(error, r.error);
+        }
+        part[0][lane] = rate; part[1][lane] = derivative; part[2][lane] = area; part[3][lane] = inner;
+        part[4][lane] = error; part[5][lane] = gross;
+    }
+    om_inlet_sum s = {0., 0., 0., 0., max_inner, 0};
+    for (int lane = 0; lane < OM_LANES; ++lane) {
+        s.rate += part[0][lane]; s.derivative += part[1][lane]; s.area += part[2][lane]; s.gross += part[5][lane];
+        s.max_inner = (int)fmax(s.max_inner, part[3][lane]);
+        if (part[4][lane]) s.error = 5;
+    }
+    return s;
+}
+
+/* One mode-9 segment; 0 or its failure (a trial rejection in the reference). */
+static int om_inlet_section(const om_ctx *m, int b, const double *q, const double *z, double *trace, double *flux,
+                            int *status)
+{
+    const int nc = m->nc, nf = m->nf, nb = m->nb;
+    const double g = m->grav, dry = m->dry, speed = m->speed_limit;
+    const double Q = m->forcing[b], requested = m->forcing[nb + b];
+    const int *faces = m->boundary_faces + m->boundary_offset[b];
+    const int n = m->boundary_offset[b + 1] - m->boundary_offset[b];
+    int error = 0, max_inner = 0;
+    double reference_area = 0., scale = 1.;
+    for (int lane = 0; lane < OM_LANES; ++lane) {
+        double area = 0., sc = 1.;
+        for (int k = lane; k < n; k += OM_LANES) {
+            const int f = faces[k], o = m->owner[f];
+            status[f] = 0;
+            const double bed = m->exterior_bed[f], h0 = q[o];
+            double hi = h0 > dry ? fmax(h0 + z[o] - bed, 0.) : 0.;
+            if (hi <= dry) hi = 0.;
+            const double ui = h0 > dry ? -(q[nc + o] * m->normal[f] + q[2 * nc + o] * m->normal[nf + f]) / h0 : 0.;
+            const double hr = fmax(requested - bed, 0.);
+            if (hr > dry) area += hr * m->length[f];
+            sc = fmax(sc, fabs(ui) + 2. * sqrt(g * hi) + 2. * sqrt(g * hr));
+        }
+        reference_area += area;
+        scale = fmax(scale, sc);
+    }
+    if (!isfinite(Q) || Q < 0. || !isfinite(requested) || (Q > 0. && reference_area <= 0.)) error = 1;
+    double velocity = reference_area > 0. ? Q / reference_area : 0.;
+    scale = fmax(scale, 1. + fabs(velocity));
+    if (Q > 0. && !error) {
+        double lo = velocity - scale, hi = velocity + scale;
+        om_inlet_sum r = om_inlet_rate(m, faces, n, lo, requested, q, z, max_inner);
+        max_inner = r.max_inner; if (r.error) error = r.error;
+        for (int j = 0; j < 60 && r.rate > Q && !error; ++j) {
+            lo -= scale; scale *= 2.;
+            r = om_inlet_rate(m, faces, n, lo, requested, q, z, max_inner);
+            max_inner = r.max_inner; if (r.error) error = r.error;
+        }
+        if (r.rate > Q) error = 2;
+        r = om_inlet_rate(m, faces, n, hi, requested, q, z, max_inner);
+        max_inner = r.max_inner; if (r.error) error = r.error;
+        for (int j = 0; j < 60 && r.rate < Q && !error; ++j) {
+            hi += scale; scale *= 2.;
+            r = om_inlet_rate(m, faces, n, hi, requested, q, z, max_inner);
+            max_inner = r.max_inner; if (r.error) error = r.error;
+        }
+        if (r.rate < Q) error = 2;
+        velocity = fmin(hi, fmax(lo, Q / reference_area));
+        for (int j = 0; j < 80 && !error; ++j) {
+            r = om_inlet_rate(m, faces, n, velocity, requested, q, z, max_inner);
+            max_inner = r.max_inner; if (r.error) error = r.error;
+            if (fabs(r.rate - Q) <= 3e-13 * Q + 256. * OM_EPS * r.gross) break;
+            if (r.rate < Q) lo = velocity; else hi = velocity;
+            double next = r.derivative > 0. ? velocity + (Q - r.rate) / r.derivative : lo + .5 * (hi - lo);
+            if (!(next > lo && next < hi)) next = lo + .5 * (hi - lo);
+            velocity = next;
+        }
+        r = om_inlet_rate(m, faces, n, velocity, requested, q, z, max_inner);
+        max_inner = r.max_inner; if (r.error) error = r.error;
+        if (!isfinite(r.rate) || fabs(r.rate - Q) > 1e-10 * Q + 1024. * OM_EPS * r.gross) error = 3;
+    }
+    if (error) return error;
+    for (int k = 0; k < n; ++k) {
+        const int f = faces[k], o = m->owner[f];
+        const double nx = m->normal[f], ny = m->normal[nf + f], bed = m->exterior_bed[f], h0 = q[o];
+        double hi = h0 > dry ? fmax(h0 + z[o] - bed, 0.) : 0.;
+        if (hi <= dry) hi = 0.;
+        const double ui = h0 > dry ? -(q[nc + o] * nx + q[2 * nc + o] * ny) / h0 : 0.;
+        const double vt = h0 > dry ? (-q[nc + o] * ny + q[2 * nc + o] * nx) / h0 : 0.;
+        double hr = fmax(requested - bed, 0.);
+        if (hr <= dry) hr = 0.;
+        om_inlet_riemann r = Q == 0. ? om_inlet_exact(h0, -ui, h0, ui, g) : om_inlet_exact(hr, velocity, hi, ui, g);
+        if (Q == 0.) r.u = 0.;
+        if (r.error || !isfinite(r.h) || !isfinite(r.u) || fabs(r.u) > speed) { status[f] = 3; continue; }
+        const double water = -r.h * r.u, tangent = r.u < 0. ? vt : 0.;
+        trace[f] = r.h; trace[nf + f] = water * nx - r.h * tangent * ny; trace[2 * nf + f] = water * ny + r.h * tangent * nx;
+        const double pressure = Q == 0. ? 0. : .5 * g * (h0 * h0 - hi * hi);
+        const double momentum = r.h * r.u * r.u + .5 * g * r.h * r.h + pressure;
+        flux[f] = water; flux[nf + f] = momentum * nx - water * tangent * ny; flux[2 * nf + f] = momentum * ny + water * tangent * nx;
+    }
+    return 0;
+}
+
+/* Stock-aware allocation of the mode-9 inlets (InletFeasibility.__call__,
+ * src/braids_core/hydraulics/inlet_feasibility.py:35-57): outward inlet
+ * debit capped by each owner's stock after other boundary debits, the
+ * removed outflow taken from the section's incoming faces. Sums follow the
+ * boundary face order. work needs 3*nc + 2*nb doubles. */
+void om_inlet_feasibility(const om_ctx *m, const double *base, double dt, double *flux, double *trace, double *work)
+{
+    const int nc = m->nc, nf = m->nf, nb = m->nb;
+    const int nbf = m->boundary_offset[nb];
+    double *total = work, *reserved = work + nc, *scale_c = work + 2 * (size_t)nc;
+    double *removed_b = work + 3 * (size_t)nc, *incoming_b = removed_b + nb;
+    for (int k = 0; k < nbf; ++k) { const int c = m->owner[m->boundary_faces[k]]; total[c] = 0.; reserved[c] = 0.; }
+    for (int b = 0; b < nb; ++b) { removed_b[b] = 0.; incoming_b[b] = 0.; }
+    for (int k = 0; k < nbf; ++k) {
+        const int f = m->boundary_faces[k], c = m->owner[f];
+        const double rate = fmax(flux[f], 0.) * m->length[f];
+        if (m->seg_mode[m->bid[f]] == 9) total[c] += rate; else reserved[c] += rate;
+    }
+    for (int k = 0; k < nbf; ++k) {
+        const int c = m->owner[m->boundary_faces[k]];
+        const double available = fmax(0., base[c] * m->area[c] / dt - reserved[c]);
+        const double ratio = fmin(1., available / fmax(total[c], 1e-300)) * (1. - 32. * OM_EPS);
+        scale_c[c] = total[c] > available ? ratio : 1.;
+    }
+    for (int k = 0; k < nbf; ++k) {
+        const int f = m->boundary_faces[k], c = m->owner[f], b = m->bid[f];
+        if (m->seg_mode[b] != 9) continue;
+        const double water = flux[f], debit = fmax(water, 0.) * m->length[f];
+        removed_b[b] += water > 0. ? debit * (1. - scale_c[c]) : 0.;
+        incoming_b[b] += fmax(-water, 0.) * m->length[f];
+    }
+    for (int k = 0; k < nbf; ++k) {
+        const int f = m->boundary_faces[k], c = m->owner[f], b = m->bid[f];
+        if (m->seg_mode[b] != 9) continue;
+        const double water = flux[f];
+        const int feasible = removed_b[b] <= incoming_b[b];
+        const double in_scale = incoming_b[b] > 0. ? 1. - removed_b[b] / fmax(incoming_b[b], 1e-300) : 1.;
+        const double sc = (feasible && water > 0.) ? scale_c[c] : ((feasible && water < 0.) ? in_scale : 1.);
+        const double depth = trace[f], denom = fmax(depth, 1e-300);
+        const double ux = depth > 0. ? trace[nf + f] / denom : 0., uy = depth > 0. ? trace[2 * nf + f] / denom : 0.;
+        flux[nf + f] += (sc * sc - 1.) * water * ux;
+        flux[2 * nf + f] += (sc * sc - 1.) * water * uy;
+        flux[f] = water * sc;
+        trace[nf + f] *= sc;
+        trace[2 * nf + f] *= sc;
+    }
+}
+
+/* ------------------------------------------------------------------ */
 /* Critical outlet (mode 4): outgoing characteristic discharge equal to  */
 /* sqrt(g A^3 / B) on the controlled faces of the opening, faces that     */
 /* turn inward or dry removed and the root recomputed                     */
@@ -1492,17 +1748,12 @@ int om_exterior(om_ctx *m, const double *q, const double *z, double time,
         if (!om_open(m, i)) continue;
         const int b = m->bid[i], c = m->owner[i], mode = m->seg_mode[b];
         const double h0 = q[c], nx = m->normal[i], ny = m->normal[nf + i], bed = m->exterior_bed[i];
-        if (mode == 4 || mode == 5 || mode == 10 || mode == 11) continue;
+        if (mode == 4 || mode == 5 || mode == 9 || mode == 10 || mode == 11) continue;
         double h = fmax(h0 + z[c] - bed, 0.), geometric = h, ux = 0., uy = 0.;
         if (h0 > dry) { ux = q[nc + c] / h0; uy = q[2 * nc + c] / h0; }
         double un = ux * nx + uy * ny, tx = ux - un * nx, ty = uy - un * ny, normal_speed = 0.;
         int st = 0;
-        if (mode == 9) {
-            h = fmax(forcing[nb + b] - bed, 0.); tx = ty = 0.;
-            const double Q = forcing[b];
-            if (Q > 0. && total_out[b] <= 0.) st = 1;
-            else if (h > dry && Q > 0.) normal_speed = -Q / total_out[b];
-        } else if (mode == 6) {
+        if (mode == 6) {
             const double Q = forcing[b];
             if (Q > 0. && total_out[b] <= 0.) st = 1;
             else if (h > dry && Q > 0.) normal_speed = -Q * weights[i] / (total_out[b] * h * m->length[i]);
@@ -1548,12 +1799,17 @@ int om_exterior(om_ctx *m, const double *q, const double *z, double time,
             fy = water * trace[2 * nf + i] / h + .5 * gravity * h * h * ny;
         }
         double pressure = h0 > dry ? .5 * gravity * (h0 * h0 - geometric * geometric) : 0.;
-        if (mode == 9 && h <= dry) pressure = h0 > dry ? .5 * gravity * h0 * h0 : 0.;
         flux[i] = water; flux[nf + i] = fx + pressure * nx; flux[2 * nf + i] = fy + pressure * ny;
     }
     /* section owners of the remaining outlet modes, in the reference's order
      * (river_exterior_bed.py:213-217): a normal-depth failure rejects the
      * trial before the rating owner runs; a rating failure is fatal */
+    if (om_has_inlet(m)) {
+        int inlet_failed = 0;
+        for (int b = 0; b < nb; ++b)
+            if (m->seg_mode[b] == 9 && om_inlet_section(m, b, q, z, trace, flux, status)) inlet_failed = 1;
+        if (inlet_failed) return OM_REJECT_SPATIAL;
+    }
     {
         int any = 0;
         for (int b = 0; b < nb; ++b) any = any || m->seg_mode[b] == 4;
@@ -2353,6 +2609,7 @@ int om_rate(om_ctx *m, om_scratch *s, const double *q, const double *z, const do
         if (ex == OM_EXTERIOR_FATAL) return OM_FAIL;
         if (ex) return OM_REJECT_SPATIAL;
         om_outlet_feasibility(m, base, dt, s->ext_flux, s->ext_trace, s->work);
+        if (om_has_inlet(m)) om_inlet_feasibility(m, base, dt, s->ext_flux, s->ext_trace, s->work);
     }
     om_primitive(m, q, z, s->v, s->active, s->pstatus);
     om_cells(m, q, s->v, s->active, s->grad, s->constant);
@@ -2804,6 +3061,7 @@ int om_hllc_single(om_ctx *m, const om_hllc_geo *G, om_scratch *s, om_hllc_scrat
         if (ex == OM_EXTERIOR_FATAL) return OM_FAIL;
         if (ex) return OM_REJECT_SPATIAL;
         om_outlet_feasibility(m, S->work, dt, s->ext_flux, s->ext_trace, s->work);
+        if (om_has_inlet(m)) om_inlet_feasibility(m, S->work, dt, s->ext_flux, s->ext_trace, s->work);
     }
     om_hllc_faces(m, G, S->half, S->grad, ext, ext_trace, S->fl, S->fr, S->speed);
     if (m->turb) om_hllc_turbine_pressure(m, G, S->half, S->grad, S->fl, S->fr);

@@ -107,6 +107,7 @@ def _setup(L):
     L.om_exterior.restype = I
     L.om_exterior.argtypes = [P, P, P, D, P, P, P, P, P, P]
     L.om_outlet_feasibility.argtypes = [P, P, D, P, P, P]
+    L.om_inlet_feasibility.argtypes = [P, P, D, P, P, P]
     L.om_inventory.argtypes = [P, D, P, P, P]
     L.om_reserve.argtypes = [P, D, P, P, P]
     L.om_reserve.restype = I
@@ -247,6 +248,7 @@ class Oracle:
         self.ctx = ctx
         self.cp = C.byref(ctx)
         self.m = m
+        self.seg_mode = np.asarray(case["seg_mode"])
         self.z = _f64(case["z"]).copy()
         self.L.om_set_threads(threads or os.cpu_count() or 1)
         self._scratch = self.L.om_scratch_create(self.cp)
@@ -420,6 +422,18 @@ class Oracle:
         L.om_hllc_update(cp, G, dt, _p(q), _p(o["fl"]), _p(o["fr"]), _p(o["fstatus"]), _p(o["next"]),
                          _p(o["status"]))
         return o
+
+    def boundary_allocation(self, base, dt, flux, trace):
+        """Stock-aware allocation of the open-boundary fluxes in place: the
+        outlet cap, then the exact-discharge inlet allocation when mode-9
+        segments exist (river_explicit_boundary_budget.py:37-39)."""
+        m = self.m
+        work = np.zeros(3 * m.nf + 3 * m.nc)
+        base = _f64(base)
+        assert flux.flags.c_contiguous and trace.flags.c_contiguous
+        self.L.om_outlet_feasibility(self.cp, _p(base), float(dt), _p(flux), _p(trace), _p(work))
+        if np.any(self.seg_mode == 9):
+            self.L.om_inlet_feasibility(self.cp, _p(base), float(dt), _p(flux), _p(trace), _p(work))
 
     # --- single kernels (for pinning against the reference kernels) -------
     def kernels(self, q, z=None):

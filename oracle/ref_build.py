@@ -24,7 +24,8 @@ Dual-compiled OpenMP headers (their ENTRY/LOOP macros select the host form):
   river_mpm.h, flow2dh_mobile_kernels.h, bend_methods_v1_kernels.h (Exner / MPM),
   hllc.h, hllc_turbines.h (src/braids_core/hydraulics, the HLLC option),
   river_rating_outlet.h, river_normal_outlet.h, river_exterior_outlet.h (rating,
-  normal-depth, critical and free-weir outlets)
+  normal-depth, critical and free-weir outlets), river_exterior_inlet.h
+  (exact-discharge inlets)
 Generated CUDA C also: flow_bed_slope_runtime.cu (src/braids_gpu, Koch-Flokstra slope)
 
 Usage: python oracle/ref_build.py   (exits non-zero when the reference is absent)
@@ -118,6 +119,8 @@ def generate():
         "ref_rating": (src / "braids_core/sediment/river_rating_outlet.h").read_text(),
         "ref_normal": (src / "braids_core/sediment/river_normal_outlet.h").read_text(),
         "ref_outlet": (src / "braids_core/sediment/river_exterior_outlet.h").read_text(),
+        # exact-discharge inlets (mode 9)
+        "ref_inlet": (src / "braids_core/sediment/river_exterior_inlet.h").read_text(),
     }
     for name, code in headers.items():
         (OUT / f"{name}.h").write_text(code)

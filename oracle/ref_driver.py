@@ -330,7 +330,10 @@ class Ref:
         data = dict(boundary_faces=np.asarray(m.boundary_faces, np.int32), owner=g["owner"], bid=g["bid"])
         p = SimpleNamespace(g=dict(offset=g["offset"], faces=g["faces"], signs=g["signs"], length=g["length"],
                                    neighbour=g["neighbour"], bid=g["bid"], area=g["area"]))
-        ext = SimpleNamespace(xp=np, p=p, a=SimpleNamespace(data=data), inlet_compatibility=None,
+        # the exact-discharge inlet owner's control (river_exterior_inlet.py:10-11): mode-9 segments
+        inlet = (SimpleNamespace(control=(self.seg_mode[:self.nb] == 9).astype(np.int32))
+                 if np.any(self.seg_mode[:self.nb] == 9) else None)
+        ext = SimpleNamespace(xp=np, p=p, a=SimpleNamespace(data=data), inlet_compatibility=inlet, nb=self.nb,
                               hydraulic_mode=np.asarray(self.seg_mode[:self.nb], np.int32))
         self._ext_stub = ext
         return ExplicitBoundaryBudget(ext)
@@ -427,6 +430,8 @@ class Ref:
                   g["owner"], g["bid"], g["selected"], self.seg_mode, self.stage_policy, q, self.z,
                   self.exterior_bed, g["normal"], g["length"], self.forcing, weights, total, trace, flux, status)
         # section owners after exterior_flux (ExteriorBed.evaluate, river_exterior_bed.py:213-217)
+        if np.any(self.seg_mode[:nb] == 9):
+            self._compatible_inlet(q, trace, flux, status)
         if np.any(self.seg_mode[:nb] == 4):
             self._critical_outlet(q, trace, flux, status)
         if np.any(self.seg_mode[:nb] == 5):
@@ -479,6 +484,41 @@ class Ref:
             if np.any(sec):
                 raise Fatal("Q-H outlet has no admissible subcritical solution within the supplied curve")
         return trace, flux, status
+
+    def _compatible_inlet(self, q, trace, flux, status):
+        """The reference's own CompatibleInlet owner (river_exterior_inlet.py:7-38)
+        on a stand-in exterior owner, its kernel the host build of river_exterior_inlet.h."""
+        from braids_core.sediment import river_exterior_inlet as RI
+        from braids_core.sediment.bend_methods_v1 import BendTrialRejected
+        m, g, nb = self.m, self.g, self.nb
+        if not hasattr(self, "_inlet"):
+            from braids_support.sediment.river_morphodynamics.sediment_wave import WaveEngine
+            lib = C.CDLL(str(REF / "libref_inlet.so"))
+            lib.mobile_threads(C.c_int(os.cpu_count() or 1))
+
+            def engine(backend, threads, source=None, names=None):
+                e = WaveEngine.__new__(WaveEngine)
+                e.backend, e.threads = "cpu", threads
+                e.lib, e.fn = lib, {n: getattr(lib, n) for n in names}
+                for fn in e.fn.values():
+                    fn.restype = None
+                e.identity = {}
+                return e
+            RI.WaveEngine = engine
+            ns = SimpleNamespace
+            p = ns(g=dict(owner=g["owner"], normal=g["normal"], length=g["length"]), nf=m.nf, n=m.nc,
+                   parameters=ns(gravity=self.grav, dry=self.dry), exterior_bed=self.exterior_bed, flow=ns(threads=1))
+            self._inlet_ext = ns(p=p, xp=np, nb=nb, a=ns(backend="cpu", data=dict(speed_limit=self.speed_limit)),
+                                 offset=g["boffset"], faces=g["bfaces"])
+            controls = {str(b): {"method": "inlet.stage_discharge" if self.seg_mode[b] == 9 else "outlet.stage"}
+                        for b in range(nb)}
+            self._inlet = RI.CompatibleInlet(self._inlet_ext, controls)
+        e = self._inlet_ext
+        e.forcing, e.trace, e.flux, e.status = self.forcing, trace, flux, status
+        try:
+            self._inlet.evaluate(np.ascontiguousarray(q), self.z)
+        except BendTrialRejected as exc:
+            raise Rejected(str(exc))
 
     def _critical_outlet(self, q, trace, flux, status):
         """The reference's own CriticalOutlet owner (river_exterior_outlet.py:10-72)
@@ -624,9 +664,16 @@ class Ref:
                 raise BendTrialRejected("Exterior hydraulic boundary rejected")
             return flux, trace
         feasibility = OutletFeasibility(self._ext_stub) if self.nb else None
+        inlet_feasibility = None
+        if self.nb and self._ext_stub.inlet_compatibility is not None:
+            from braids_core.hydraulics.inlet_feasibility import InletFeasibility
+            inlet_feasibility = InletFeasibility(self._ext_stub)
 
         def boundary_correction(q, dt, flux, trace):
+            # feasible_boundary (river_hllc.py:31-33): outlet allocation, then inlet allocation
             feasibility(q, dt, flux, trace)
+            if inlet_feasibility is not None:
+                inlet_feasibility(q, dt, flux, trace)
 
         momentum = correct = None
         if self.rotors:

@@ -37,6 +37,8 @@ CASES = {
     "normal_outlet": (S.normal_channel, lambda c: S.perturbed_state(c, 7, 0.2, 0.4, 0.0), 0.01, 1.0),
     "weir_outlet": (S.weir_channel, lambda c: S.perturbed_state(c, 8, 0.2, 0.4, 0.0), 0.01, 1.0),
     "critical_outlet": (S.critical_channel, lambda c: S.perturbed_state(c, 9, 0.2, 0.4, 0.0), 0.01, 1.0),
+    "stage_discharge_inlet": (S.stage_discharge_channel, lambda c: S.perturbed_state(c, 10, 0.2, 0.4, 0.0),
+                              0.01, 1.0),
 }
 
 

@@ -2,14 +2,14 @@
 
 Run in a checkout that has the reference (default /root/reference):
 
-    python oracle/ref_build.py && python tests/golden/make_hllc_golden.py
+    python oracle/ref_build.py && python tests/golden/make_hllc_golden.py [case ...]
 
 The reference's ``HLLCHydraulics`` class (src/braids_core/hydraulics/hllc.py)
 runs unchanged: its substep controller, its Hancock step and its own kernels
 (hllc.h, hllc_turbines.h, host-compiled by oracle/ref_build.py). Its hooks are
 the ones the reference's river owner installs (river_hllc.py:14-55,
 river_turbines.py:27-51): the exterior boundary owner and the reference's
-OutletFeasibility class, the reference's drag kernel, and for rotors the
+OutletFeasibility and InletFeasibility classes, the reference's drag kernel, and for rotors the
 reference's wet gradients / Thetis sink. Geometry is the product's channel
 meshes (braids_hkt_gb300.scenarios); the operator builds its own incidence
 and least-squares inverse from them.
@@ -43,12 +43,16 @@ def cases():
         "lake": S.lake_at_rest(),                  # closed basin, emerged islands
         "dam_break": S.dam_break(),                # dry bed downstream
         "rotors": S.small_rotor_channel(),         # two rotors: sink + HLLC rotor pressure
+        "stage_discharge": S.stage_discharge_channel(),   # exact-discharge inlet (mode 9) and its allocation
     }
 
 
 def main():
     OUT.mkdir(parents=True, exist_ok=True)
+    only = sys.argv[1:]                           # case names to (re)generate; all when empty
     for name, case in cases().items():
+        if only and name not in only:
+            continue
         ref = Ref(case)
         op = ref.hllc_operator()
         q0 = np.ascontiguousarray(case["q"], dtype=np.float64)

@@ -20,6 +20,7 @@ pytestmark = pytest.mark.gpu
 
 GOLD = Path(__file__).parent / "golden" / "hllc"
 BUILDERS = {"channel": S.small_channel, "lake": S.lake_at_rest, "dam_break": S.dam_break,
+            "stage_discharge": S.stage_discharge_channel,
             "rotors": S.small_rotor_channel}
 
 
@@ -138,7 +139,3 @@ def test_hllc_scope_errors():
     case, _ = case_of("channel")
     with pytest.raises(Exception):
         RiverSolver(case, precision="mixed", method="hllc")
-    c9 = dict(case)
-    c9["seg_mode"] = np.array([9, 2])
-    with pytest.raises(ValueError):
-        RiverSolver(c9, precision="fp64", method="hllc")

@@ -1,5 +1,6 @@
-"""Outlet section owners on the GPU: the Q-H rating (mode 11), normal-depth
-(mode 10), free-weir (mode 5) and critical (mode 4) outlets against
+"""Section owners on the GPU: the Q-H rating (mode 11), normal-depth
+(mode 10), free-weir (mode 5) and critical (mode 4) outlets and the
+exact-discharge inlet (mode 9) against
 the oracle (FP64 to 1e-10 with identical substep counts; mixed against FP64
 to 1e-4 in depth) and its failure without a bracket (the scenario fails,
 failed = 5). The reference fixture is checked in test_gpu_parity."""
@@ -38,8 +39,8 @@ def test_rating_outlet_without_a_bracket_fails_the_scenario():
     assert d[0]["failed"] == 0 and d[1]["failed"] == 5
 
 
-@pytest.mark.parametrize("make", [S.normal_channel, S.weir_channel, S.critical_channel],
-                         ids=["normal", "weir", "critical"])
+@pytest.mark.parametrize("make", [S.normal_channel, S.weir_channel, S.critical_channel, S.stage_discharge_channel],
+                         ids=["normal", "weir", "critical", "stage_discharge_inlet"])
 def test_section_outlet_fp64_oracle_and_mixed(make):
     from braids_hkt_gb300.solver import RiverSolver
     from oracle import Oracle
@@ -61,10 +62,35 @@ def test_section_outlet_fp64_oracle_and_mixed(make):
 def test_outlet_modes_batched_equal_alone():
     """Rating and normal-depth outlets in one batch with the stage-outlet channel: bitwise as alone."""
     from braids_hkt_gb300.solver import RiverSolver
-    cases = [S.small_channel(), S.rating_channel(), S.normal_channel(), S.weir_channel(), S.critical_channel()]
+    cases = [S.small_channel(), S.rating_channel(), S.normal_channel(), S.weir_channel(), S.critical_channel(),
+             S.stage_discharge_channel()]
     batch = RiverSolver(cases, precision="mixed")
     batch.advance(2.0, 0.0)
     for i, c in enumerate(cases):
         one = RiverSolver(c, precision="mixed")
         one.advance(2.0, 0.0)
         np.testing.assert_array_equal(batch.state(i), one.state())
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("discharge", [5.0, 35.0])
+def test_inlet_net_discharge_exact_on_gpu(precision, discharge):
+    """The exact-discharge inlet's boundary water flux of one residual: the
+    net section discharge equals the request within the reference's bound
+    (1e-10 Q + 1024 eps x gross throughflow). The mixed form solves the
+    section in FP64 and carries each open face's water flux in FP32, so its
+    bound adds one FP32 rounding of the gross throughflow (2^-23 x gross)."""
+    from braids_hkt_gb300.solver import RiverSolver
+    case = S.stage_discharge_channel(discharge=discharge)
+    case["q"] = S.perturbed_state(case, 12, 0.2, 0.4, 0.0)
+    s = RiverSolver(case, precision=precision)
+    _, water, status, _ = s.rate(0.01)
+    assert int(status) == 0
+    m = case["mesh"]
+    faces = np.asarray(m.boundary_faces)[m.boundary_offset[0]:m.boundary_offset[1]]
+    flow = -water.cpu().numpy()[faces] * m.length[faces]
+    gross = np.abs(flow).sum()
+    bound = 1e-10 * discharge + 1024 * np.finfo(float).eps * gross
+    if precision == "mixed":
+        bound += 2.0 ** -23 * gross
+    assert abs(flow.sum() - discharge) <= bound

@@ -16,6 +16,7 @@ from oracle import Oracle
 
 GOLD = Path(__file__).resolve().parent / "golden" / "hllc"
 BUILDERS = {"channel": S.small_channel, "lake": S.lake_at_rest, "dam_break": S.dam_break,
+            "stage_discharge": S.stage_discharge_channel,
             "rotors": S.small_rotor_channel}
 
 

@@ -1,0 +1,90 @@
+"""The exact-discharge inlet (mode 9) in the C oracle.
+
+Parity: the inlet section solve is pinned through the reference's own
+CompatibleInlet owner and host-built kernel (tests/golden/
+stage_discharge_inlet.npz, checked bit for bit by test_oracle_golden.py); the
+stock-aware allocation is pinned here against the reference's
+OutletFeasibility + InletFeasibility classes (tests/golden/feasibility, made
+by tests/golden/make_feasibility_golden.py). Known answers: the net section
+discharge of the boundary Riemann fluxes equals the requested Q within the
+reference's acceptance bound (1e-10 Q + 1024 eps x gross throughflow), and a
+zero request closes every inlet face.
+"""
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import braids_hkt_gb300.scenarios as S
+from oracle import Oracle
+
+FEAS = sorted((Path(__file__).parent / "golden" / "feasibility").glob("*.npz"))
+EPS = np.finfo(float).eps
+
+
+@pytest.mark.parametrize("path", FEAS, ids=[p.stem for p in FEAS])
+def test_allocation_matches_reference(path):
+    z = np.load(path)
+    arrs = {k: z[k] for k in z.files}
+    case = S.case_from_arrays(arrs)
+    o = Oracle(case, threads=1)
+    flux, trace = arrs["flux"].copy(), arrs["trace"].copy()
+    o.boundary_allocation(arrs["base"], float(arrs["dt"]), flux, trace)
+    np.testing.assert_array_equal(flux, arrs["flux_out"])
+    np.testing.assert_array_equal(trace, arrs["trace_out"])
+
+
+def test_allocation_fixture_coverage():
+    changed = {p.stem: int(np.sum(np.load(p)["flux_out"] != np.load(p)["flux"])) for p in FEAS}
+    assert changed["cap"] > 0 and changed["infeasible"] == 0 and changed["pass"] == 0
+
+
+def exterior(o, q, time=0.0):
+    m = o.m
+    nf, nb = m.nf, len(o.seg_mode)
+    trace, flux = np.zeros((3, nf)), np.zeros((3, nf))
+    status = np.zeros(nf, np.int32)
+    work = np.zeros(3 * nf + 3 * m.nc)
+    stage, total = np.zeros(2 * nb), np.zeros(nb)
+    p = lambda a: a.ctypes.data_as(C.c_void_p)
+    st = o.L.om_exterior(o.cp, p(np.ascontiguousarray(q)), p(o.z), float(time), p(trace), p(flux), p(status),
+                         p(work), p(stage), p(total))
+    return st, trace, flux, status
+
+
+@pytest.mark.parametrize("discharge", [5.0, 20.0, 60.0])
+def test_net_section_discharge_is_exact(discharge):
+    case = S.stage_discharge_channel(discharge=discharge)
+    o = Oracle(case, threads=1)
+    q = S.perturbed_state(case, 12, 0.2, 0.4, 0.0)
+    st, trace, flux, status = exterior(o, q)
+    assert st == 0 and not status.any()
+    m = case["mesh"]
+    faces = np.asarray(m.boundary_faces)[m.boundary_offset[0]:m.boundary_offset[1]]
+    rate = -flux[0, faces] * m.length[faces]
+    gross = np.abs(rate).sum()
+    assert abs(rate.sum() - discharge) <= 1e-10 * discharge + 1024 * EPS * gross
+    np.testing.assert_array_equal(trace[0, faces] > 0, True)
+
+
+def test_zero_discharge_closes_the_inlet():
+    case = S.stage_discharge_channel(discharge=0.0)
+    o = Oracle(case, threads=1)
+    q = S.perturbed_state(case, 13, 0.2, 0.4, 0.0)
+    st, trace, flux, status = exterior(o, q)
+    assert st == 0
+    m = case["mesh"]
+    faces = np.asarray(m.boundary_faces)[m.boundary_offset[0]:m.boundary_offset[1]]
+    assert np.all(flux[0, faces] == 0.0)
+    # reflected-owner pressure only: the normal momentum flux is 0.5 g h*^2 along the normal
+    assert np.all(np.abs(flux[1:, faces]).sum(axis=0) > 0)
+
+
+def test_dry_reference_line_with_discharge_rejects():
+    """A requested line below every inlet face's bed has no wet reference area:
+    the section has no root and the trial is rejected (nonzero status)."""
+    case = S.stage_discharge_channel(reference_stage=-50.0)
+    o = Oracle(case, threads=1)
+    st, *_ = exterior(o, case["q"])
+    assert st != 0
