@@ -43,6 +43,8 @@ SIGNATURES = {
     "brx_outlet_chains_set": (I, [P, I, P, P, P]),
     "brx_weir_set": (I, [P, P]),
     "brx_critical_chains_set": (I, [P, P, P, P]),
+    "brx_inlet_lines_set": (I, [P, P, P, P, P]),
+    "brx_forcing_get": (I, [P, P]),
     "brx_hllc_set": (I, [P, P, P, P, P]),
     "brx_method_set": (I, [P, I]),
     "brx_launch_shape_set": (I, [P, I, I, I]),

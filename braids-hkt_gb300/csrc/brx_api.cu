@@ -445,6 +445,17 @@ extern "C" int brx_solver_destroy(brx_solver *s)
 // ---------------------------------------------------------------------------
 // set-up calls
 // ---------------------------------------------------------------------------
+// Forget the solved inlet reference lines (their inputs besides the
+// discharge changed): NaN never equals a discharge.
+static int clear_inlet_lines(brx_solver *s)
+{
+    if (s->bnd.line_q) {
+        CK(cudaMemsetAsync(s->bnd.line_q, 0xff, sizeof(double) * s->nseg, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+    }
+    return BRX_OK;
+}
+
 extern "C" int brx_controls_set(brx_solver *s, int scen, double gravity, double dry, double cfl, double speed_limit,
                                 int roughness_mode, double roughness_value)
 {
@@ -461,7 +472,7 @@ extern "C" int brx_controls_set(brx_solver *s, int scen, double gravity, double 
             c.grav = gravity; c.dry = dry; c.cfl = cfl; c.speed_limit = speed_limit;
             c.roughness_mode = roughness_mode; c.roughness_value = roughness_value;
         }
-    return BRX_OK;
+    return clear_inlet_lines(s);
 }
 
 extern "C" int brx_boundary_set(brx_solver *s, const int *seg_mode, const int *stage_policy, const double *exterior_bed,
@@ -489,6 +500,7 @@ extern "C" int brx_boundary_set(brx_solver *s, const int *seg_mode, const int *s
     s->h_seg_mode.assign(seg_mode, seg_mode + nseg);
     const int inlet = std::count(seg_mode, seg_mode + nseg, 9) > 0;
     if (inlet != s->bnd.inlet) { s->bnd.inlet = inlet; s->graph_dirty = true; }
+    TRY(clear_inlet_lines(s));
     std::vector<int> bmode(nf, 0);
     std::vector<double> ext(std::max(s->nslot, 1));
     for (int k = 0; k < s->nslot; ++k) {
@@ -641,6 +653,49 @@ extern "C" int brx_weir_set(brx_solver *s, const double *param)
     TRY(s->upload(&p_w, param, 3 * (size_t)nseg));
     TRY(ensure_section_scratch(s));
     s->bnd.weir = p_w;
+    s->graph_dirty = true;
+    return BRX_OK;
+}
+
+extern "C" int brx_inlet_lines_set(brx_solver *s, const int *kind, const double *slope, const int *left,
+                                   const int *right)
+{
+    if (!s) return fail(BRX_ERR_ARGUMENT, "null solver");
+    if (!kind || !slope || !left || !right) return fail(BRX_ERR_ARGUMENT, "null inlet line array");
+    if (s->pending) return fail(BRX_ERR_STATE, "an asynchronous interval is in flight");
+    const int nseg = s->nseg, nf = s->nf;
+    if (nseg == 0) return fail(BRX_ERR_ARGUMENT, "no open segments");
+    for (int sg = 0; sg < nseg; ++sg) {
+        if (kind[sg] < 0 || kind[sg] > 2) return fail(BRX_ERR_ARGUMENT, "inlet line kind must be 0, 1 or 2");
+        if (kind[sg] == 2 && !(std::isfinite(slope[sg]) && slope[sg] > 0.))
+            return fail(BRX_ERR_ARGUMENT, "a normal-depth inlet line needs a positive energy slope");
+    }
+    std::vector<int> bslot(nf, -1), ls(std::max(s->nslot, 1), -1), rs(std::max(s->nslot, 1), -1);
+    for (int k = 0; k < s->nslot; ++k) bslot[s->h_slot_face[k]] = k;
+    for (int k = 0; k < s->nslot; ++k) {
+        const int f = s->h_slot_face[k], l = left[f], r = right[f];
+        if (l < -1 || l >= nf || r < -1 || r >= nf) return fail(BRX_ERR_ARGUMENT, "inlet neighbour face out of range");
+        if ((l >= 0 && bslot[l] < 0) || (r >= 0 && bslot[r] < 0))
+            return fail(BRX_ERR_ARGUMENT, "inlet neighbour must be an open face");
+        if ((l >= 0 && s->h_bid[l] != s->h_bid[f]) || (r >= 0 && s->h_bid[r] != s->h_bid[f]))
+            return fail(BRX_ERR_ARGUMENT, "inlet neighbours must belong to the same segment");
+        ls[k] = l < 0 ? -1 : bslot[l];
+        rs[k] = r < 0 ? -1 : bslot[r];
+    }
+    if (!s->bnd.line_q) {
+        TRY(s->alloc(&s->bnd.line_q, nseg));
+        TRY(s->alloc(&s->bnd.line_stage, nseg));
+        int *p_kind, *p_l, *p_r;
+        double *p_slope;
+        TRY(s->alloc(&p_kind, nseg)); TRY(s->alloc(&p_slope, nseg));
+        TRY(s->alloc(&p_l, ls.size())); TRY(s->alloc(&p_r, rs.size()));
+        s->bnd.line_kind = p_kind; s->bnd.line_slope = p_slope; s->bnd.line_left = p_l; s->bnd.line_right = p_r;
+    }
+    CK(cudaMemcpy(const_cast<int *>(s->bnd.line_kind), kind, sizeof(int) * nseg, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(const_cast<double *>(s->bnd.line_slope), slope, sizeof(double) * nseg, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(const_cast<int *>(s->bnd.line_left), ls.data(), sizeof(int) * ls.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(const_cast<int *>(s->bnd.line_right), rs.data(), sizeof(int) * rs.size(), cudaMemcpyHostToDevice));
+    TRY(clear_inlet_lines(s));
     s->graph_dirty = true;
     return BRX_OK;
 }
@@ -1059,6 +1114,16 @@ extern "C" int brx_hint_get(brx_solver *s, double *hint)
 {
     if (!s || !hint) return fail(BRX_ERR_ARGUMENT, "null argument");
     for (int i = 0; i < s->nscen; ++i) hint[i] = s->hint[i];
+    return BRX_OK;
+}
+
+extern "C" int brx_forcing_get(brx_solver *s, double *out)
+{
+    if (!s || !out) return fail(BRX_ERR_ARGUMENT, "null argument");
+    if (s->pending) return fail(BRX_ERR_STATE, "an asynchronous interval is in flight");
+    if (s->nseg == 0) return BRX_OK;
+    CK(cudaStreamSynchronize(s->stream));
+    CK(cudaMemcpy(out, s->bnd.forcing, sizeof(double) * 2 * s->nseg, cudaMemcpyDeviceToHost));
     return BRX_OK;
 }
 

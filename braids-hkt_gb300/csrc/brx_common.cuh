@@ -181,6 +181,10 @@ struct BoundaryDev {
     const int *crit_chain_off, *crit_chain_slot;
     int *gslot, *gend;       // (nslot) wet-group scratch of the critical outlets
     int inlet;               // a mode-9 (exact-discharge inlet) segment exists
+    const int *line_kind;    // (nseg) mode-9 reference line: 0 forcing stage, 1 critical, 2 normal; or null
+    const double *line_slope;            // (nseg) energy slope of the normal lines
+    const int *line_left, *line_right;   // (nslot) physical neighbour slots along the section, -1 none
+    double *line_q, *line_stage;         // (nseg) solved line and its discharge (NaN: none)
 };
 
 // Accepted / stage state buffers.

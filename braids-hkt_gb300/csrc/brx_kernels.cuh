@@ -1070,6 +1070,171 @@ __device__ int inlet_section(SectionWork &w, const MeshDev &m, const BoundaryDev
     return 0;
 }
 
+// ---------------------------------------------------------------------------
+// Reference water lines of the exact-discharge inlets, written into the
+// forcing stage before the exterior flux: 1 critical depth
+// (river_exterior_section.h:17-74), 2 normal depth
+// (river_exterior_normal.h:18-104). Every distinct bed level of the section
+// starts one constant-wet-width branch (a candidate); 128 lanes take the
+// candidates and thread 0 reduces the lanes to the lexicographic minimum of
+// (rank, stage), which does not depend on the order. A solved line is kept
+// per segment with its discharge and reused while the discharge is equal
+// (the inputs besides it are fixed; the host clears the cache when it
+// changes them), as the reference's SectionCache.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void line_pick(double rank, double cand, double &best, double &stage)
+{
+    if (rank < best || (rank == best && cand < stage)) { best = rank; stage = cand; }
+}
+
+__device__ void line_critical_candidate(const MeshDev &m, const BoundaryDev &b, int i, int k0, int k1, double Q,
+                                        double g, double dry, double &rank, double &cand)
+{
+    const double level = b.ext_bed[i];
+    double minimum = level, next = INFINITY, width = 0., excess = 0.;
+    for (int k = k0; k < k1; ++k) {
+        const double zb = b.ext_bed[k], len = m.length[b.slot_face[k]];
+        minimum = fmin(minimum, zb);
+        if (zb > level) next = fmin(next, zb);
+        else { width += len; excess += (level - zb) * len; }
+    }
+    rank = INFINITY; cand = 0.;
+    if (Q == 0.) { cand = minimum; rank = 0.; return; }
+    const double area = cbrt(Q * Q * width / g), eta = level + (area - excess) / width;
+    if (!(isfinite(area) && area > 0. && isfinite(eta) && eta > level + dry) || eta > next + dry) return;
+    double actual = 0., wet_width = 0.;
+    for (int k = k0; k < k1; ++k) {
+        const double h = eta - b.ext_bed[k], len = m.length[b.slot_face[k]];
+        if (h > dry) { actual += h * len; wet_width += len; }
+    }
+    if (wet_width != width || !(actual > 0.)) return;
+    const double residual = fabs(Q * Q * wet_width / (g * actual * actual * actual) - 1.);
+    const double tolerance = 1e-10 + 64. * EPS * fmax(1., fabs(eta)) * width / actual;
+    if (residual > tolerance) return;
+    cand = eta;
+    rank = eta - minimum + Q * Q / (2. * g * actual * actual);
+}
+
+// wetted perimeter of slot k: its length plus the wetted steps to its neighbours
+__device__ __forceinline__ double line_perimeter(const MeshDev &m, const BoundaryDev &b, int k, double eta, double dry)
+{
+    const double h = eta - b.ext_bed[k];
+    if (h <= dry) return 0.;
+    const int l = b.line_left[k], r = b.line_right[k];
+    double hl = l < 0 ? 0. : fmax(eta - b.ext_bed[l], 0.), hr = r < 0 ? 0. : fmax(eta - b.ext_bed[r], 0.);
+    if (hl <= dry) hl = 0.;
+    if (hr <= dry) hr = 0.;
+    return m.length[b.slot_face[k]] + fmax(h - hl, 0.) + fmax(h - hr, 0.);
+}
+
+__device__ double line_rate(const MeshDev &m, const BoundaryDev &b, int k0, int k1, double eta, double slope,
+                            double g, double dry, int law, double rough)
+{
+    double area = 0., perimeter = 0., drag = 0.;
+    for (int k = k0; k < k1; ++k) {
+        const double h = eta - b.ext_bed[k];
+        if (h > dry) { area += h * m.length[b.slot_face[k]]; perimeter += line_perimeter(m, b, k, eta, dry); }
+    }
+    if (!(area > 0. && perimeter > 0.)) return 0.;
+    const double c = nout_chezy(law, fmax(area / perimeter, dry), rough, g);
+    for (int k = k0; k < k1; ++k)
+        if (eta - b.ext_bed[k] > dry) drag += line_perimeter(m, b, k, eta, dry) / (c * c);
+    return drag > 0. ? area * sqrt(area * slope / drag) : 0.;
+}
+
+__device__ void line_normal_candidate(const MeshDev &m, const BoundaryDev &b, int i, int k0, int k1, double Q,
+                                      double slope, double g, double dry, int law, double rough, double &rank,
+                                      double &cand)
+{
+    rank = INFINITY; cand = 0.;
+    const double level = b.ext_bed[i];
+    const int fi = b.slot_face[i];
+    double minimum = level, next = INFINITY;
+    for (int k = k0; k < k1; ++k) {
+        const double zb = b.ext_bed[k];
+        minimum = fmin(minimum, zb);
+        if (zb > level) next = fmin(next, zb);
+        if (zb == level && b.slot_face[k] < fi) return;          // one candidate per distinct level
+    }
+    if (Q == 0.) { cand = rank = minimum; return; }
+    const double epsilon = 8. * EPS * fmax(1., fabs(level));
+    double lo = level + dry + epsilon, hi = isfinite(next) ? next + dry : level + fmax(1., 64. * dry);
+    if (!(hi > lo)) return;
+    double rlo = line_rate(m, b, k0, k1, lo, slope, g, dry, law, rough) - Q;
+    double rhi = line_rate(m, b, k0, k1, hi, slope, g, dry, law, rough) - Q;
+    if (!isfinite(next))
+        for (int k = 0; k < 60 && rhi < 0.; ++k) {
+            hi = level + 2. * (hi - level);
+            rhi = line_rate(m, b, k0, k1, hi, slope, g, dry, law, rough) - Q;
+        }
+    if (!isfinite(rlo) || !isfinite(rhi)) return;
+    const double start = lo, end = hi;
+    double previous = rlo;
+    bool found = false;
+    for (int j = 1; j <= 32; ++j) {          // sub-brackets: the lowest sign change of the branch
+        const double at = start + (end - start) * (double(j) / 32.);
+        const double value = j == 32 ? rhi : line_rate(m, b, k0, k1, at, slope, g, dry, law, rough) - Q;
+        if (isfinite(value) && ((previous <= 0. && value >= 0.) || (previous >= 0. && value <= 0.))) {
+            hi = at; rhi = value; rlo = previous; found = true;
+            break;
+        }
+        lo = at; previous = value;
+    }
+    if (!found) return;
+    for (int j = 0; j < 80; ++j) {
+        const double mid = lo + .5 * (hi - lo);
+        if (mid == lo || mid == hi) break;
+        const double value = line_rate(m, b, k0, k1, mid, slope, g, dry, law, rough) - Q;
+        if ((rlo <= 0. && value >= 0.) || (rlo >= 0. && value <= 0.)) { hi = mid; rhi = value; }
+        else { lo = mid; rlo = value; }
+    }
+    const double eta = fabs(rlo) < fabs(rhi) ? lo : hi;
+    const double rate = line_rate(m, b, k0, k1, eta, slope, g, dry, law, rough);
+    const double tolerance = 1e-10 + 128. * EPS * fmax(1., fabs(eta)) / fmax(eta - minimum, dry);
+    if (isfinite(rate) && fabs(rate / Q - 1.) <= tolerance) { cand = eta; rank = eta; }
+}
+
+// The line of segment sg (block-cooperative); false when the section has no
+// resolved root (the reference rejects the trial).
+__device__ bool line_section(SectionWork &w, const MeshDev &m, const BoundaryDev &b, int sg, double g, double dry,
+                             int law, double rough)
+{
+    const int k0 = b.seg_off[sg], k1 = b.seg_off[sg + 1], kind = b.line_kind[sg];
+    const double Q = b.forcing[sg];
+    const bool cached = b.line_q[sg] == Q;
+    __syncthreads();
+    if (cached) {
+        if (threadIdx.x == 0) b.forcing[b.nseg + sg] = b.line_stage[sg];
+        __syncthreads();
+        return true;
+    }
+    for (int lane = threadIdx.x; lane < SECTION_LANES; lane += blockDim.x) {
+        double best = INFINITY, stage = 0.;
+        for (int i = k0 + lane; i < k1; i += SECTION_LANES) {
+            double rank, cand;
+            if (kind == 1) line_critical_candidate(m, b, i, k0, k1, Q, g, dry, rank, cand);
+            else line_normal_candidate(m, b, i, k0, k1, Q, b.line_slope[sg], g, dry, law, rough, rank, cand);
+            line_pick(rank, cand, best, stage);
+        }
+        w.part[0][lane] = best; w.part[1][lane] = stage;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double best = INFINITY, stage = 0.;
+        for (int lane = 0; lane < SECTION_LANES; ++lane) line_pick(w.part[0][lane], w.part[1][lane], best, stage);
+        w.error = !isfinite(best);
+        if (!w.error) {
+            b.forcing[b.nseg + sg] = stage;
+            b.line_q[sg] = Q;
+            b.line_stage[sg] = stage;
+        }
+    }
+    __syncthreads();
+    const bool ok = !w.error;
+    __syncthreads();
+    return ok;
+}
+
 // stage 1 / 2: the SSPRK stages (state work / q1, its own stock, clock t or
 // t + dt); STAGE_HANCOCK: the HLLC predicted state q1 at t + dt/2, outlet
 // stock of the substep's start state work (hllc.py:91-97), status of stage 1.
@@ -1111,6 +1276,18 @@ __global__ void k_boundary(MeshDev m, StateDev s, BoundaryDev b, Ctrl *ctrl, int
                 }
                 b.forcing[(size_t)row * b.nseg + sg] = val;
             }
+    // critical, then normal reference lines of the exact-discharge inlets
+    // (river_exterior_bed.py:199-200); a section without a root rejects the trial
+    __shared__ SectionWork section;
+    bool line_failed = false;
+    if (b.line_kind) {
+        for (int pass = 1; pass <= 2; ++pass)
+            for (int sg = s0; sg < s1; ++sg)          // block-uniform
+                if (b.seg_mode[sg] == 9 && b.line_kind[sg] == pass &&
+                    !line_section(section, m, b, sg, grav, dry, ct.roughness_mode, ct.roughness_value))
+                    line_failed = true;
+        __syncthreads();
+    }
     const int k0 = b.seg_off[s0], k1 = b.seg_off[s1];
     for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
         const int f = b.slot_face[k], c = m.owner[f];
@@ -1211,10 +1388,9 @@ __global__ void k_boundary(MeshDev m, StateDev s, BoundaryDev b, Ctrl *ctrl, int
     // chain without a root rejects the trial before the rating owner runs; a
     // rating section without a solution fails the scenario
     __shared__ int section_reject;
-    __shared__ SectionWork section;
-    if (threadIdx.x == 0) section_reject = 0;
+    if (threadIdx.x == 0) section_reject = line_failed;
     __syncthreads();
-    if (b.inlet) {
+    if (b.inlet && !section_reject) {
         bool inlet_failed = false;
         for (int sg = s0; sg < s1; ++sg)              // block-uniform: the CTA solves one section at a time
             if (b.seg_mode[sg] == 9) {

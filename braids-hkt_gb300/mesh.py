@@ -377,3 +377,39 @@ def channel_mesh(length, width, spacing, jitter, seed, refine=()):
     mesh = build_mesh(pts, tri, segment)
     geometry_records(mesh)
     return mesh
+
+
+def section_neighbours(mesh: Mesh, segment: int):
+    """Physical neighbour faces along one straight inlet section.
+
+    Returns (left, right) for the segment's open faces (arrays over all faces,
+    -1 elsewhere): faces sorted by their station along the section tangent
+    (-ny, nx) of the first face; consecutive faces whose facing ends meet
+    (gap within max(1e-10, 64 ulp of the midpoint scale)) are neighbours, a
+    gap ends a bank. The section must be collinear with one consistent normal
+    (NormalSection's adjacency, src/braids_core/sediment/
+    river_exterior_normal.py:11-27).
+    """
+    nf = len(mesh.owner)
+    left = np.full(nf, -1, np.int32)
+    right = left.copy()
+    ids = np.flatnonzero((mesh.neighbour < 0) & (mesh.bid == segment))
+    if not len(ids):
+        raise ValueError("normal inlet has no physical faces")
+    normal = mesh.normal[:, ids[0]]
+    relative = mesh.mid[:, ids] - mesh.mid[:, ids[0], None]
+    tol = max(1e-10, 64 * np.spacing(max(1., float(np.max(np.abs(mesh.mid[:, ids]))))))
+    if (np.any(np.abs(mesh.normal[:, ids] - normal[:, None]) > 1e-12) or
+            np.any(np.abs(normal @ relative) > tol)):
+        raise ValueError("a normal inlet needs one collinear, consistently oriented section")
+    station = np.array([-normal[1], normal[0]]) @ relative
+    order = np.argsort(station)
+    ids, station = ids[order], station[order]
+    widths = mesh.length[ids]
+    gaps = np.diff(station) - .5 * (widths[:-1] + widths[1:])
+    if np.any(gaps < -tol):
+        raise ValueError("normal inlet faces overlap")
+    for i in np.flatnonzero(np.abs(gaps) <= tol):
+        left[ids[i + 1]] = ids[i]
+        right[ids[i]] = ids[i + 1]
+    return left, right

@@ -290,6 +290,28 @@ def stage_discharge_channel(discharge=20.0, reference_stage=3.05, **kw):
     return case
 
 
+def critical_inlet_channel(discharge=20.0, **kw):
+    """The small channel fed through an exact-discharge inlet whose reference
+    water line is the section's critical-depth level for the inflow
+    (inlet.critical_discharge: Q^2 W / (g A^3) = 1 on the exterior face beds,
+    minimum specific energy among the wet-width branches)."""
+    case = stage_discharge_channel(discharge=discharge, **kw)
+    case["inlet"] = {0: {"line": "critical"}}
+    case["name"] = "critical_inlet_channel"
+    return case
+
+
+def normal_inlet_channel(discharge=20.0, energy_slope=2e-3, **kw):
+    """The small channel fed through an exact-discharge inlet whose reference
+    water line is the section's normal-depth level (inlet.normal_discharge:
+    uniform flow at `energy_slope` with the channel's roughness, wetted
+    vertical steps between neighbouring faces in the perimeter)."""
+    case = stage_discharge_channel(discharge=discharge, **kw)
+    case["inlet"] = {0: {"line": "normal", "energy_slope": float(energy_slope)}}
+    case["name"] = "normal_inlet_channel"
+    return case
+
+
 def lake_at_rest(length=80.0, width=40.0, spacing=4.0, seed=11, islands=True):
     """Variable bed with emerged islands, flat surface at 1.0 m, closed walls (no open segments)."""
     mesh = M.channel_mesh(length, width, spacing, 1.0, seed)
@@ -387,6 +409,9 @@ def case_arrays(case):
     for b, params in (case.get("outlet") or {}).items():
         for name, value in params.items():
             out[f"outlet_{int(b)}_{name}"] = np.asarray(value, dtype=np.float64)
+    for b, params in (case.get("inlet") or {}).items():
+        out[f"inletline_{int(b)}"] = np.asarray(params.get("line", "stage"))
+        out[f"inletslope_{int(b)}"] = np.asarray(float(params.get("energy_slope", 0.0)))
     return out
 
 
@@ -408,6 +433,10 @@ def case_from_arrays(arrs):
             outlet.setdefault(int(seg), {})[name] = float(np.asarray(v))
     if outlet:
         case["outlet"] = outlet
+    inlet = {int(k[10:]): {"line": str(np.asarray(v)), "energy_slope": float(np.asarray(arrs[f"inletslope_{k[10:]}"]))}
+             for k, v in arrs.items() if k.startswith("inletline_")}
+    if inlet:
+        case["inlet"] = inlet
     return case
 
 

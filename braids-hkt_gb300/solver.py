@@ -115,6 +115,51 @@ def critical_chains(cases, face_offset=None):
     return (np.asarray(segc, np.int32), np.asarray(off, np.int32), np.asarray(faces if faces else [0], np.int32))
 
 
+LINES = {"stage": 0, "critical": 1, "normal": 2}
+
+
+def inlet_lines(cases, face_offset=None):
+    """Reference water lines of the exact-discharge inlets (mode 9) of a batch:
+    (kind (nseg): 0 the forcing stage (inlet.stage_discharge /
+    depth_discharge), 1 critical depth (inlet.critical_discharge), 2 normal
+    depth (inlet.normal_discharge); energy slope (nseg); left, right (nf
+    global face ids, -1 none) the physical neighbours along normal-depth
+    sections (river_exterior_section.py, river_exterior_normal.py)).
+    case["inlet"][segment] = {"line": "stage" | "critical" | "normal",
+    "energy_slope": s (normal only, > 0)}."""
+    from .mesh import section_neighbours
+    kind, slope, left, right = [], [], [], []
+    for i, case in enumerate(cases):
+        F0 = 0 if face_offset is None else int(face_offset[i])
+        m = case["mesh"]
+        modes = np.asarray(case.get("seg_mode", np.zeros(0)), dtype=int)
+        lt = np.full(len(m.owner), -1, np.int64)
+        rt = lt.copy()
+        for b in range(m.nb):
+            row = (case.get("inlet") or {}).get(b, {})
+            line = row.get("line", "stage")
+            if line not in LINES:
+                raise ValueError(f"inlet segment {b}: unknown reference line {line!r}")
+            if line != "stage" and modes[b] != 9:
+                raise ValueError(f"segment {b}: a {line} reference line needs an exact-discharge inlet (mode 9)")
+            value = float(row.get("energy_slope", 0.0))
+            if line == "normal":
+                if not (np.isfinite(value) and value > 0):
+                    raise ValueError(f"normal inlet segment {b} needs a positive energy slope")
+                l, r = section_neighbours(m, b)
+                sel = l >= 0
+                lt[sel] = l[sel] + F0
+                sel = r >= 0
+                rt[sel] = r[sel] + F0
+            kind.append(LINES[line])
+            slope.append(value)
+        left.append(lt)
+        right.append(rt)
+    cat = lambda a: np.concatenate(a) if a else np.zeros(0)
+    return (np.asarray(kind, np.int32), np.asarray(slope, np.float64), cat(left).astype(np.int32),
+            cat(right).astype(np.int32))
+
+
 def weir_parameters(cases):
     """(3, nseg) crest [m], coefficient [m^0.5/s] and effective width [m] of
     the free-weir outlets (mode 5) of a batch (FreeWeir's parameters,
@@ -233,6 +278,9 @@ class RiverSolver:
             if np.any(p["seg_mode"] == 10):
                 off, faces, slope = normal_chains(self.cases, p["face_offset"])
                 check(self.lib.brx_outlet_chains_set(self.h, len(slope), _ptr(off), _ptr(faces), _ptr(slope)))
+            if any(case.get("inlet") for case in self.cases):
+                kind, slope, left, right = inlet_lines(self.cases, p["face_offset"])
+                check(self.lib.brx_inlet_lines_set(self.h, _ptr(kind), _ptr(slope), _ptr(left), _ptr(right)))
             check(self.lib.brx_boundary_set(self.h, _ptr(p["seg_mode"]), _ptr(p["stage_policy"]),
                                             _ptr(p["exterior_bed"]), _ptr(p["forcing"])))
         else:
@@ -370,6 +418,13 @@ class RiverSolver:
     def activate(self, mask):
         m = _i32(mask)
         check(self.lib.brx_scenarios_activate(self.h, _ptr(m)))
+
+    def forcing(self):
+        """(2, nseg) discharge and stage of the last evaluated stage (solved inlet lines included)."""
+        nseg = int(self.packed["nseg"])
+        out = np.zeros((2, max(nseg, 1)))
+        check(self.lib.brx_forcing_get(self.h, _ptr(out)))
+        return out[:, :nseg]
 
     def hints(self):
         out = np.zeros(self.nscen)

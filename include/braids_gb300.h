@@ -119,6 +119,25 @@ int brx_critical_chains_set(brx_solver *s, const int *seg_chain, const int *offs
  * copied; call before brx_boundary_set when any segment has mode 5. */
 int brx_weir_set(brx_solver *s, const double *param);
 
+/* Reference water lines of the exact-discharge inlets (mode 9), per
+ * segment kind: 0 the forcing stage (inlet.stage_discharge /
+ * inlet.depth_discharge), 1 critical depth (inlet.critical_discharge:
+ * Q^2 W / (g A^3) = 1 on the exterior face beds, minimum specific energy
+ * among the wet-width branches; CriticalSection,
+ * src/braids_core/sediment/river_exterior_section.py:10-41 and
+ * river_exterior_section.h), 2 normal depth (inlet.normal_discharge: the
+ * lowest level whose uniform flow at the energy slope carries Q, with the
+ * solver's roughness law at the section radius and wetted steps between
+ * neighbouring faces; NormalSection, river_exterior_normal.py:30-74 and
+ * river_exterior_normal.h, without bedform feedback). slope (nseg) the energy
+ * slope of kind-2 lines; left, right (nf) the physical neighbour face of each
+ * face along its section or -1 (NormalSection's adjacency,
+ * river_exterior_normal.py:11-27; the host helper
+ * braids_hkt_gb300.mesh.section_neighbours). The line is solved before the
+ * exterior flux of every stage (kept while the discharge is unchanged); a
+ * section without a root rejects the trial. Host arrays, copied. */
+int brx_inlet_lines_set(brx_solver *s, const int *kind, const double *slope, const int *left, const int *right);
+
 /* Open-boundary set-up for all segments: hydraulic mode (2 stage, 3 free
  * outflow, 4 critical: outgoing characteristic discharge sqrt(g A^3 / B)
  * on the controlled faces, river_exterior_outlet.h; 5 free weir: the
@@ -287,6 +306,12 @@ int brx_hllc_set(brx_solver *s, const int *entry_face, const int *entry_other, c
  * src/braids_core/hydraulics/river_hllc.py:95-101). BRX_METHOD_HLLC needs
  * the FP64 form and brx_hllc_set; brx_rate stays an f-wave residual. */
 int brx_method_set(brx_solver *s, int method);
+
+/* The forcing of the last evaluated stage, host out (2, nseg): rows
+ * discharge and stage as the exterior flux used them (the sampled tables;
+ * for the critical / normal inlet lines the solved reference line), as the
+ * reference's ExteriorBed.forcing after evaluate. */
+int brx_forcing_get(brx_solver *s, double *out);
 
 /* Step hint carried between brx_advance calls (nscen, host; <= 0 = none). */
 int brx_hint_get(brx_solver *s, double *hint);

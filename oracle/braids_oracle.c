@@ -102,6 +102,12 @@ typedef struct {
      * segments (critical_offset (nb+1) over chains, chain faces) */
     const int *crit_seg_chain;                     /* (nb+1) chain range per segment, or NULL */
     const int *crit_chain_offset, *crit_chain_face;
+    /* reference water lines of the mode-9 inlets: 0 the forcing stage,
+     * 1 critical depth, 2 normal depth (energy slope per segment, the
+     * physical neighbour faces along the section, -1 at a gap or an end) */
+    const int *inlet_line;                         /* (nb) or NULL */
+    const double *inlet_slope;                     /* (nb) */
+    const int *line_left, *line_right;             /* (nf) */
 } om_ctx;
 
 /* ------------------------------------------------------------------ */
@@ -1484,6 +1490,179 @@ static int om_inlet_section(const om_ctx *m, int b, const double *q, const doubl
     return 0;
 }
 
+/* Reference water lines written into the forcing stage of mode-9 inlets
+ * before the exterior flux (ExteriorBed.evaluate, river_exterior_bed.py:
+ * 195-200). Each distinct bed level of the section starts one
+ * constant-wet-width branch; the branches' candidates are reduced to the
+ * lexicographic minimum of (rank, stage) (section_critical_partial / _total,
+ * river_exterior_section.h:51-74, a running minimum whose result does not
+ * depend on the tiling). */
+static void om_line_pick(double rank, double cand, double *best, double *stage)
+{
+    if (rank < *best || (rank == *best && cand < *stage)) { *best = rank; *stage = cand; }
+}
+
+/* Critical-depth line (CriticalSection, river_exterior_section.h:17-49):
+ * Q^2 W / (g A^3) = 1 on the branch, the minimum specific energy wins. */
+static int om_line_critical(om_ctx *m, int b)
+{
+    const int nb = m->nb, k0 = m->boundary_offset[b], k1 = m->boundary_offset[b + 1];
+    const int *faces = m->boundary_faces;
+    const double *bed = m->exterior_bed, *length = m->length;
+    const double Q = m->forcing[b], g = m->grav, dry = m->dry;
+    double best = INFINITY, stage = 0.;
+    for (int i = k0; i < k1; ++i) {
+        const double level = bed[faces[i]];
+        double minimum = level, next = INFINITY, width = 0., excess = 0.;
+        for (int k = k0; k < k1; ++k) {
+            const int f = faces[k];
+            const double zb = bed[f];
+            minimum = fmin(minimum, zb);
+            if (zb > level) next = fmin(next, zb);
+            else { width += length[f]; excess += (level - zb) * length[f]; }
+        }
+        double cand = 0., energy = INFINITY;
+        if (Q == 0.) { cand = minimum; energy = 0.; }
+        else {
+            const double area = cbrt(Q * Q * width / g), eta = level + (area - excess) / width;
+            if (isfinite(area) && area > 0. && isfinite(eta) && eta > level + dry && !(eta > next + dry)) {
+                double actual = 0., wet_width = 0.;
+                for (int k = k0; k < k1; ++k) {
+                    const int f = faces[k];
+                    const double h = eta - bed[f];
+                    if (h > dry) { actual += h * length[f]; wet_width += length[f]; }
+                }
+                if (wet_width == width && actual > 0.) {
+                    const double residual = fabs(Q * Q * wet_width / (g * actual * actual * actual) - 1.);
+                    const double tolerance = 1e-10 + 64. * OM_EPS * fmax(1., fabs(eta)) * width / actual;
+                    if (!(residual > tolerance)) { cand = eta; energy = eta - minimum + Q * Q / (2. * g * actual * actual); }
+                }
+            }
+        }
+        om_line_pick(energy, cand, &best, &stage);
+    }
+    if (!isfinite(best)) return 1;
+    m->forcing[nb + b] = stage;
+    return 0;
+}
+
+/* Wetted perimeter of face f at level eta: its length plus the wetted
+ * vertical steps to its physical neighbours (river_exterior_normal.h:25-31). */
+static double om_line_perimeter(const om_ctx *m, int f, double eta)
+{
+    const double *bed = m->exterior_bed, dry = m->dry;
+    const double h = eta - bed[f];
+    if (h <= dry) return 0.;
+    const int l = m->line_left[f], r = m->line_right[f];
+    double hl = l < 0 ? 0. : fmax(eta - bed[l], 0.), hr = r < 0 ? 0. : fmax(eta - bed[r], 0.);
+    if (hl <= dry) hl = 0.;
+    if (hr <= dry) hr = 0.;
+    return m->length[f] + fmax(h - hl, 0.) + fmax(h - hr, 0.);
+}
+
+/* Uniform-flow discharge of the section at level eta (normal_rate,
+ * river_exterior_normal.h:32-57, without bedform feedback). */
+static double om_line_rate(const om_ctx *m, int b, double eta, double slope)
+{
+    const int k0 = m->boundary_offset[b], k1 = m->boundary_offset[b + 1];
+    const int *faces = m->boundary_faces;
+    const double *bed = m->exterior_bed, dry = m->dry;
+    double area = 0., perimeter = 0., drag = 0.;
+    for (int k = k0; k < k1; ++k) {
+        const int f = faces[k];
+        const double h = eta - bed[f];
+        if (h > dry) { area += h * m->length[f]; perimeter += om_line_perimeter(m, f, eta); }
+    }
+    double rate = 0.;
+    if (area > 0. && perimeter > 0.) {
+        const double radius = area / perimeter;
+        const double c = om_nout_chezy(m->roughness_mode, fmax(radius, dry), m->roughness_value, m->grav);
+        for (int k = k0; k < k1; ++k) {
+            const int f = faces[k];
+            if (eta - bed[f] <= dry) continue;
+            drag += om_line_perimeter(m, f, eta) / (c * c);
+        }
+        if (drag > 0.) rate = area * sqrt(area * slope / drag);
+    }
+    return rate;
+}
+
+/* Normal-depth line (NormalSection, river_exterior_normal.h:59-104): per
+ * distinct bed level the lowest bracketed root of rate(eta) = Q (32
+ * sub-brackets, 80 bisections, a final relative check); the lowest root wins. */
+static int om_line_normal(om_ctx *m, int b)
+{
+    const int nb = m->nb, k0 = m->boundary_offset[b], k1 = m->boundary_offset[b + 1];
+    const int *faces = m->boundary_faces;
+    const double *bed = m->exterior_bed;
+    const double Q = m->forcing[b], dry = m->dry, slope = m->inlet_slope[b];
+    double best = INFINITY, stage = 0.;
+    for (int i = k0; i < k1; ++i) {
+        const int fi = faces[i];
+        const double level = bed[fi];
+        double minimum = level, next = INFINITY;
+        int duplicate = 0;
+        for (int k = k0; k < k1; ++k) {
+            const int f = faces[k];
+            const double zb = bed[f];
+            minimum = fmin(minimum, zb);
+            if (zb > level) next = fmin(next, zb);
+            if (zb == level && f < fi) duplicate = 1;
+        }
+        if (duplicate) continue;
+        if (Q == 0.) { om_line_pick(minimum, minimum, &best, &stage); continue; }
+        const double epsilon = 8. * OM_EPS * fmax(1., fabs(level));
+        double lo = level + dry + epsilon, hi = isfinite(next) ? next + dry : level + fmax(1., 64. * dry);
+        if (!(hi > lo)) continue;
+        double rlo = om_line_rate(m, b, lo, slope) - Q, rhi = om_line_rate(m, b, hi, slope) - Q;
+        if (!isfinite(next))
+            for (int k = 0; k < 60 && rhi < 0.; ++k) {
+                hi = level + 2. * (hi - level);
+                rhi = om_line_rate(m, b, hi, slope) - Q;
+            }
+        if (!isfinite(rlo) || !isfinite(rhi)) continue;
+        const double start = lo, end = hi;
+        double previous = rlo;
+        int found = 0;
+        for (int j = 1; j <= 32; ++j) {
+            const double at = start + (end - start) * ((double)j / 32.);
+            const double value = j == 32 ? rhi : om_line_rate(m, b, at, slope) - Q;
+            if (isfinite(value) && ((previous <= 0. && value >= 0.) || (previous >= 0. && value <= 0.))) {
+                hi = at; rhi = value; rlo = previous; found = 1;
+                break;
+            }
+            lo = at; previous = value;
+        }
+        if (!found) continue;
+        for (int j = 0; j < 80; ++j) {
+            const double mid = lo + .5 * (hi - lo);
+            if (mid == lo || mid == hi) break;
+            const double value = om_line_rate(m, b, mid, slope) - Q;
+            if ((rlo <= 0. && value >= 0.) || (rlo >= 0. && value <= 0.)) { hi = mid; rhi = value; }
+            else { lo = mid; rlo = value; }
+        }
+        const double eta = fabs(rlo) < fabs(rhi) ? lo : hi;
+        const double rate = om_line_rate(m, b, eta, slope);
+        const double tolerance = 1e-10 + 128. * OM_EPS * fmax(1., fabs(eta)) / fmax(eta - minimum, dry);
+        if (isfinite(rate) && fabs(rate / Q - 1.) <= tolerance) om_line_pick(eta, eta, &best, &stage);
+    }
+    if (!isfinite(best)) return 1;
+    m->forcing[nb + b] = stage;
+    return 0;
+}
+
+/* Critical lines, then normal lines (river_exterior_bed.py:199-200); 0 or a
+ * trial rejection. */
+static int om_inlet_lines(om_ctx *m)
+{
+    if (!m->inlet_line) return 0;
+    for (int b = 0; b < m->nb; ++b)
+        if (m->seg_mode[b] == 9 && m->inlet_line[b] == 1 && om_line_critical(m, b)) return OM_REJECT_SPATIAL;
+    for (int b = 0; b < m->nb; ++b)
+        if (m->seg_mode[b] == 9 && m->inlet_line[b] == 2 && om_line_normal(m, b)) return OM_REJECT_SPATIAL;
+    return 0;
+}
+
 /* Stock-aware allocation of the mode-9 inlets (InletFeasibility.__call__,
  * src/braids_core/hydraulics/inlet_feasibility.py:35-57): outward inlet
  * debit capped by each owner's stock after other boundary debits, the
@@ -1713,6 +1892,10 @@ int om_exterior(om_ctx *m, const double *q, const double *z, double time,
     const int nc = m->nc, nf = m->nf, nb = m->nb;
     const double dry = m->dry, gravity = m->grav;
     om_sample_forcing(m, time);
+    {
+        const int line = om_inlet_lines(m);
+        if (line) return line;
+    }
     const double *forcing = m->forcing;
     double *terms = work, *weights = work + 2 * (size_t)nf;
     for (int f = 0; f < nf; ++f) {

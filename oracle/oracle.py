@@ -62,7 +62,8 @@ class Ctx(C.Structure):
                 ("table_len", I), ("table_time", P), ("table_value", P), ("threads", I),
                 ("turb", P), ("rating_offset", P), ("rating_q", P), ("rating_eta", P),
                 ("nchain", I), ("chain_offset", P), ("chain_face", P), ("chain_slope", P), ("weir", P),
-                ("crit_seg_chain", P), ("crit_chain_offset", P), ("crit_chain_face", P)]
+                ("crit_seg_chain", P), ("crit_chain_offset", P), ("crit_chain_face", P),
+                ("inlet_line", P), ("inlet_slope", P), ("line_left", P), ("line_right", P)]
 
 
 class Turbines(C.Structure):
@@ -234,6 +235,13 @@ class Oracle:
         if nb and np.any(seg_mode == 5):
             from braids_hkt_gb300.solver import weir_parameters
             ctx.weir = k("weir", _f64(weir_parameters([case])))
+        if case.get("inlet"):
+            from braids_hkt_gb300.solver import inlet_lines
+            kind, slope, left, right = inlet_lines([case])
+            ctx.inlet_line = k("inlet_line", _i32(kind))
+            ctx.inlet_slope = k("inlet_slope", _f64(slope))
+            ctx.line_left = k("line_left", _i32(left))
+            ctx.line_right = k("line_right", _i32(right))
         if case.get("rating"):
             from braids_hkt_gb300.solver import rating_tables
             off, rq, re_ = rating_tables([case])

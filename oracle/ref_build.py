@@ -25,7 +25,8 @@ Dual-compiled OpenMP headers (their ENTRY/LOOP macros select the host form):
   hllc.h, hllc_turbines.h (src/braids_core/hydraulics, the HLLC option),
   river_rating_outlet.h, river_normal_outlet.h, river_exterior_outlet.h (rating,
   normal-depth, critical and free-weir outlets), river_exterior_inlet.h
-  (exact-discharge inlets)
+  (exact-discharge inlets), river_exterior_section.h and
+  river_exterior_normal.h (their critical and normal reference lines)
 Generated CUDA C also: flow_bed_slope_runtime.cu (src/braids_gpu, Koch-Flokstra slope)
 
 Usage: python oracle/ref_build.py   (exits non-zero when the reference is absent)
@@ -121,6 +122,9 @@ def generate():
         "ref_outlet": (src / "braids_core/sediment/river_exterior_outlet.h").read_text(),
         # exact-discharge inlets (mode 9)
         "ref_inlet": (src / "braids_core/sediment/river_exterior_inlet.h").read_text(),
+        # their critical-depth and normal-depth reference lines
+        "ref_section": (src / "braids_core/sediment/river_exterior_section.h").read_text(),
+        "ref_section_normal": (src / "braids_core/sediment/river_exterior_normal.h").read_text(),
     }
     for name, code in headers.items():
         (OUT / f"{name}.h").write_text(code)

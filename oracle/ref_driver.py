@@ -418,6 +418,9 @@ class Ref:
         trace = np.zeros((3, nf))
         flux = np.zeros((3, nf))
         status = np.zeros(nf, np.int32)
+        # reference lines of the critical / normal inlets (river_exterior_bed.py:199-200)
+        if self.case.get("inlet"):
+            self._inlet_lines()
         self.call("exterior", "exterior_stage_terms", 0, nf, n, self.dry, g["owner"], g["selected"], q, self.z,
                   g["length"], terms)
         self._reduce(terms, 2, stage)
@@ -484,6 +487,73 @@ class Ref:
             if np.any(sec):
                 raise Fatal("Q-H outlet has no admissible subcritical solution within the supplied curve")
         return trace, flux, status
+
+    def _inlet_lines(self):
+        """The reference's own CriticalSection and NormalSection owners
+        (river_exterior_section.py, river_exterior_normal.py) on a stand-in
+        exterior owner, their kernels the host builds of their headers."""
+        from braids_core.sediment import river_exterior_section as RS
+        from braids_core.sediment import river_exterior_normal as RN
+        from braids_core.sediment.bend_methods_v1 import BendTrialRejected
+        m, g, nb = self.m, self.g, self.nb
+        if not hasattr(self, "_lines"):
+            from braids_support.sediment.river_morphodynamics.sediment_wave import WaveEngine
+
+            def make(lib):
+                def engine(backend, threads, source=None, names=None):
+                    e = WaveEngine.__new__(WaveEngine)
+                    e.backend, e.threads = "cpu", threads
+                    e.lib, e.fn = lib, {n: getattr(lib, n) for n in names}
+                    for fn in e.fn.values():
+                        fn.restype = None
+                    e.identity = {}
+                    return e
+                return engine
+            libs = {}
+            for name in ("ref_section", "ref_section_normal"):
+                libs[name] = C.CDLL(str(REF / f"lib{name}.so"))
+                libs[name].mobile_threads(C.c_int(os.cpu_count() or 1))
+
+            def normal_engine(backend, threads, source=None, names=None):
+                lib = libs["ref_section" if Path(str(source)).name == "river_exterior_section.h" else "ref_section_normal"]
+                return make(lib)(backend, threads, source, names)
+            RS.WaveEngine = make(libs["ref_section"])
+            RN.WaveEngine = normal_engine
+            ns = SimpleNamespace
+            from braids_core.sediment.river_roughness import KEYS
+            method = {1: "roughness.chezy", 2: "roughness.manning"}.get(int(self.rmode), "roughness.white_colebrook")
+            params = {KEYS[method]: float(self.rvalue)}
+            if method == "roughness.white_colebrook":
+                params["white_colebrook_relation"] = "flow_log_layer" if int(self.rmode) == 3 else "classical_2d"
+            data = dict(owner=m.owner, neighbour=m.neighbour, bid=m.bid, mid=m.mid, normal=m.normal, length=m.length,
+                        mode=self.seg_mode[:nb])
+            p = ns(g=dict(bid=g["bid"], length=g["length"]), nf=m.nf, n=m.nc,
+                   parameters=ns(gravity=self.grav, dry=self.dry), exterior_bed=self.exterior_bed,
+                   flow=ns(threads=1), identity=dict(river_roughness=dict(method=method, parameters=params)))
+            self._lines_ext = ns(p=p, xp=np, nb=nb, tiles=self.tiles, a=ns(backend="cpu", data=data),
+                                 offset=g["boffset"], faces=g["bfaces"], selected=g["selected"], bedforms=None)
+            methods = {"stage": "inlet.stage_discharge", "critical": "inlet.critical_discharge",
+                       "normal": "inlet.normal_discharge"}
+            controls = {}
+            for b in range(nb):
+                row = (self.case.get("inlet") or {}).get(b, {})
+                if self.seg_mode[b] == 9:
+                    controls[str(b)] = {"method": methods[row.get("line", "stage")]}
+                    if row.get("line") == "normal":
+                        controls[str(b)]["energy_slope"] = float(row["energy_slope"])
+                else:
+                    controls[str(b)] = {"method": "outlet.stage"}
+            self._lines = []
+            if any(v["method"] == "inlet.critical_discharge" for v in controls.values()):
+                self._lines.append(RS.CriticalSection(self._lines_ext, controls))
+            if any(v["method"] == "inlet.normal_discharge" for v in controls.values()):
+                self._lines.append(RN.NormalSection(self._lines_ext, controls))
+        self._lines_ext.forcing = self.forcing
+        try:
+            for owner in self._lines:
+                owner.solve()
+        except BendTrialRejected as exc:
+            raise Rejected(str(exc))
 
     def _compatible_inlet(self, q, trace, flux, status):
         """The reference's own CompatibleInlet owner (river_exterior_inlet.py:7-38)

@@ -39,6 +39,8 @@ CASES = {
     "critical_outlet": (S.critical_channel, lambda c: S.perturbed_state(c, 9, 0.2, 0.4, 0.0), 0.01, 1.0),
     "stage_discharge_inlet": (S.stage_discharge_channel, lambda c: S.perturbed_state(c, 10, 0.2, 0.4, 0.0),
                               0.01, 1.0),
+    "critical_inlet": (S.critical_inlet_channel, lambda c: S.perturbed_state(c, 13, 0.2, 0.4, 0.0), 0.01, 1.0),
+    "normal_inlet": (S.normal_inlet_channel, lambda c: S.perturbed_state(c, 14, 0.2, 0.4, 0.0), 0.01, 1.0),
 }
 
 

@@ -1,6 +1,7 @@
 """Section owners on the GPU: the Q-H rating (mode 11), normal-depth
 (mode 10), free-weir (mode 5) and critical (mode 4) outlets and the
-exact-discharge inlet (mode 9) against
+exact-discharge inlet (mode 9, with the forcing, critical-depth and
+normal-depth reference lines) against
 the oracle (FP64 to 1e-10 with identical substep counts; mixed against FP64
 to 1e-4 in depth) and its failure without a bracket (the scenario fails,
 failed = 5). The reference fixture is checked in test_gpu_parity."""
@@ -39,8 +40,9 @@ def test_rating_outlet_without_a_bracket_fails_the_scenario():
     assert d[0]["failed"] == 0 and d[1]["failed"] == 5
 
 
-@pytest.mark.parametrize("make", [S.normal_channel, S.weir_channel, S.critical_channel, S.stage_discharge_channel],
-                         ids=["normal", "weir", "critical", "stage_discharge_inlet"])
+@pytest.mark.parametrize("make", [S.normal_channel, S.weir_channel, S.critical_channel, S.stage_discharge_channel,
+                                  S.critical_inlet_channel, S.normal_inlet_channel],
+                         ids=["normal", "weir", "critical", "stage_discharge_inlet", "critical_inlet", "normal_inlet"])
 def test_section_outlet_fp64_oracle_and_mixed(make):
     from braids_hkt_gb300.solver import RiverSolver
     from oracle import Oracle
@@ -63,7 +65,7 @@ def test_outlet_modes_batched_equal_alone():
     """Rating and normal-depth outlets in one batch with the stage-outlet channel: bitwise as alone."""
     from braids_hkt_gb300.solver import RiverSolver
     cases = [S.small_channel(), S.rating_channel(), S.normal_channel(), S.weir_channel(), S.critical_channel(),
-             S.stage_discharge_channel()]
+             S.stage_discharge_channel(), S.critical_inlet_channel(), S.normal_inlet_channel()]
     batch = RiverSolver(cases, precision="mixed")
     batch.advance(2.0, 0.0)
     for i, c in enumerate(cases):
@@ -94,3 +96,20 @@ def test_inlet_net_discharge_exact_on_gpu(precision, discharge):
     if precision == "mixed":
         bound += 2.0 ** -23 * gross
     assert abs(flow.sum() - discharge) <= bound
+
+
+@pytest.mark.parametrize("make", [S.critical_inlet_channel, S.normal_inlet_channel], ids=["critical", "normal"])
+def test_inlet_line_matches_oracle(make):
+    """The reference line the GPU solved (the forcing stage row after one
+    residual) equals the oracle's line within 1e-12 (cube root, pow and log
+    of the CUDA library against the host's)."""
+    from braids_hkt_gb300.solver import RiverSolver
+    from oracle import Oracle
+    case = make()
+    s = RiverSolver(case, precision="fp64")
+    s.rate(0.01)
+    o = Oracle(case, threads=1)
+    st, _, _, _ = o.rate(case["q"], 0.01)
+    assert st == 0
+    line = s.forcing()[1, 0]
+    assert abs(line - o.forcing[1, 0]) <= 1e-12 * max(1.0, abs(o.forcing[1, 0]))

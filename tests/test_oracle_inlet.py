@@ -88,3 +88,58 @@ def test_dry_reference_line_with_discharge_rejects():
     o = Oracle(case, threads=1)
     st, *_ = exterior(o, case["q"])
     assert st != 0
+
+
+def section(case):
+    m = case["mesh"]
+    faces = np.asarray(m.boundary_faces)[m.boundary_offset[0]:m.boundary_offset[1]]
+    return faces, case["exterior_bed"][faces], m.length[faces]
+
+
+@pytest.mark.parametrize("discharge", [8.0, 20.0, 60.0])
+def test_critical_line_is_critical(discharge):
+    """inlet.critical_discharge: the reference line has Froude one for the
+    section (Q^2 W / (g A^3) = 1 over the wet faces of the exterior beds)."""
+    case = S.critical_inlet_channel(discharge=discharge)
+    o = Oracle(case, threads=1)
+    st, *_ = exterior(o, S.perturbed_state(case, 12, 0.2, 0.4, 0.0))
+    assert st == 0
+    eta = o.forcing[1, 0]
+    _, bed, length = section(case)
+    h = eta - bed
+    wet = h > case["controls"]["dry"]
+    area, width = (h[wet] * length[wet]).sum(), length[wet].sum()
+    g = case["controls"]["grav"]
+    assert abs(discharge ** 2 * width / (g * area ** 3) - 1.0) <= 1e-9
+
+
+@pytest.mark.parametrize("discharge", [8.0, 20.0, 60.0])
+def test_normal_line_carries_the_discharge(discharge):
+    """inlet.normal_discharge: uniform flow at the reference line,
+    A sqrt(A S / sum(P_i / C^2)) with Manning C = R^(1/6) / n at the section
+    radius R = A / P and wetted steps to the neighbouring faces, equals Q."""
+    slope = 2e-3
+    case = S.normal_inlet_channel(discharge=discharge, energy_slope=slope)
+    o = Oracle(case, threads=1)
+    st, *_ = exterior(o, S.perturbed_state(case, 12, 0.2, 0.4, 0.0))
+    assert st == 0
+    eta = o.forcing[1, 0]
+    from braids_hkt_gb300.mesh import section_neighbours
+    faces, bed, length = section(case)
+    left, right = section_neighbours(case["mesh"], 0)
+    ext = case["exterior_bed"]
+    dry = case["controls"]["dry"]
+    depth = lambda f: 0.0 if f < 0 or eta - ext[f] <= dry else max(eta - ext[f], 0.0)
+    area = perimeter = 0.0
+    per = []
+    for f, z, ln in zip(faces, bed, length):
+        h = eta - z
+        p = ln + max(h - depth(left[f]), 0.0) + max(h - depth(right[f]), 0.0) if h > dry else 0.0
+        per.append(p)
+        if h > dry:
+            area += h * ln
+            perimeter += p
+    n = case["controls"]["roughness_value"]
+    chezy = (area / perimeter) ** (1.0 / 6.0) / n
+    rate = area * np.sqrt(area * slope / (sum(per) / chezy ** 2))
+    assert abs(rate / discharge - 1.0) <= 1e-9
