@@ -415,6 +415,53 @@ class RiverSolver:
         v = _f64(value)
         check(self.lib.brx_forcing_table_set(self.h, len(t), _ptr(t), _ptr(v)))
 
+    # ------------------------------------------------------------------
+    def identity(self):
+        """What a checkpoint must match: format, form, method and digests of
+        the packed geometry and boundary set-up."""
+        from .checkpoint import digest
+        p = self.packed
+        geometry = digest(*(p[k] for k in ("cell_offset", "face_offset", "owner", "neighbour", "bid", "offset",
+                                            "faces", "signs", "normal", "length", "area")))
+        boundary = digest(*(p[k] for k in ("seg_mode", "stage_policy", "exterior_bed", "forcing")))
+        return dict(precision=self.precision, method=self.method, scenarios=int(self.nscen), cells=int(self.nc),
+                    faces=int(self.nf), geometry_sha256=geometry, boundary_sha256=boundary)
+
+    def checkpoint_bytes(self, time=0.0, steps=0):
+        """Accepted state q, bed z and step hints as checkpoint bytes
+        (ShorelineSolver.checkpoint_bytes, shoreline_solver.py:374-381)."""
+        from .checkpoint import encode
+        if getattr(self, "_pending", False):
+            raise ValueError("a checkpoint needs the accepted state (an interval is in flight)")
+        self.torch.cuda.current_stream().synchronize()
+        arrays = dict(q=self.q.cpu().numpy(), z=self.z.cpu().numpy(), hints=self.hints())
+        return encode(self.identity(), arrays, time, steps)
+
+    def checkpoint(self, path, time=0.0, steps=0):
+        """Write a checkpoint atomically (temporary file, then os.replace)."""
+        from .checkpoint import write_atomic
+        write_atomic(path, self.checkpoint_bytes(time, steps))
+
+    def restart_bytes(self, payload):
+        """Validate, then load a checkpoint; returns its header (time, steps)
+        (ShorelineSolver.restart, shoreline_solver.py:386-408): nothing
+        changes unless the identity, inventory, shapes, dtypes and hashes all
+        match."""
+        from .checkpoint import decode
+        expected = dict(q=(tuple(self.q.shape), np.float64), z=(tuple(self.z.shape), np.float64),
+                        hints=((self.nscen,), np.float64))
+        arrays, header = decode(payload, self.identity(), expected)
+        self.torch.cuda.current_stream().synchronize()
+        self.q.copy_(self.torch.from_numpy(arrays["q"]))
+        self.z.copy_(self.torch.from_numpy(arrays["z"]))
+        self.set_hints(arrays["hints"])
+        self.torch.cuda.current_stream().synchronize()
+        return header
+
+    def restart(self, path):
+        with open(path, "rb") as f:
+            return self.restart_bytes(f.read())
+
     def activate(self, mask):
         m = _i32(mask)
         check(self.lib.brx_scenarios_activate(self.h, _ptr(m)))
@@ -469,6 +516,7 @@ class RiverSolver:
         t = _f64(np.broadcast_to(time, (self.nscen,)))
         check(self.lib.brx_advance_start(self.h, _ptr(d), _ptr(t)))
         self._async_stats = (AdvanceStats * self.nscen)()
+        self._pending = True
 
     def advance_poll(self):
         """None while the interval runs; per-scenario diagnostics once it has finished."""
@@ -478,6 +526,7 @@ class RiverSolver:
             check(code)
         if not done.value:
             return None
+        self._pending = False
         return [dict(integrator=METHOD_NAMES[self.method], hydraulic_substeps=s.substeps, hydraulic_rejections=s.rejections,
                      hydraulic_minimum_dt=s.min_dt, hydraulic_maximum_dt=s.max_dt,
                      accepted_cfl_max=s.accepted_cfl_max, hydraulic_next_substep_hint_s=s.hint,
