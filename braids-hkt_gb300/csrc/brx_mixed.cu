@@ -63,6 +63,14 @@ struct __align__(16) MxLim {
 };
 
 __device__ __forceinline__ bool finite64(double x) { return (__double2hiint(x) & 0x7ff00000) != 0x7ff00000; }
+// x <= threshold for a positive finite threshold, as a signed 64-bit compare of
+// the bit patterns (the order of non-NaN doubles against a positive value; a
+// NaN depth fails the state's finiteness check wherever this is used). FP64
+// compares issue on the FP64 pipe, a few per clock per SM on this part.
+__device__ __forceinline__ bool le_threshold(double x, double threshold)
+{
+    return __double_as_longlong(x) <= __double_as_longlong(threshold);
+}
 
 // Stage 2 skips a scenario whose first stage failed (status, or the CFL test
 // evaluated once per scenario after the first gather).
@@ -80,7 +88,7 @@ __device__ __forceinline__ bool put_prim(MxPrim *P, int c, double h, double hu, 
     p.ehi = float(eta);
     p.elo = float(eta - double(p.ehi));
     p.h = float(h);
-    const bool wet = h > dry;
+    const bool wet = !le_threshold(h, dry);
     p.u = wet ? float(hu) / p.h : 0.f;
     p.v = wet ? float(hv) / p.h : 0.f;
     p.wet = wet;
@@ -686,7 +694,7 @@ __global__ void __launch_bounds__(256) km_limit(MeshDev m, Ctrl *ctrl, Work w, M
 
 __device__ __forceinline__ void drag_f(const Ctrl &ct, float dtf, double &h, double &hu, double &hv)
 {
-    if (h <= ct.dry) { hu = 0.; hv = 0.; return; }
+    if (le_threshold(h, ct.dry)) { hu = 0.; hv = 0.; return; }
     const float hf = float(h), uf = float(hu), vf = float(hv);
     float c;
     const float val = ct.roughf;
@@ -720,19 +728,24 @@ __global__ void __launch_bounds__(256) km_update(MeshDev m, StateDev s, Ctrl *ct
             mx -= wk * L.cx;
             my -= wk * L.cy;
         }
-        double r1 = double(rate32[c] + mx), r2 = double(rate32[nc + c] + my);
+        float f1 = rate32[c] + mx, f2 = rate32[nc + c] + my;
+        double r1, r2;
         if (turb && t.hkt[sid]) {
-            // ambient stress, actuator sink, balanced pressure (the reference's add_momentum order)
+            // ambient stress and balanced pressure (FP32 face sums, added in
+            // FP32), then the FP64 actuator sink: one conversion per component
             const int k0 = m.offset[c], k1 = m.offset[c + 1];
             if (t.stress[sid]) {
                 float x = 0.f, y = 0.f;
                 for (int k = k0; k < k1; ++k) { const float2 v = g.hs[m.faces[k]]; x += g.cw4[k] * v.x; y += g.cw4[k] * v.y; }
-                r1 += double(x); r2 += double(y);
+                f1 += x; f2 += y;
             }
-            r1 += t.raw[c]; r2 += t.raw[nc + c];
             float x = 0.f, y = 0.f;
             for (int k = k0; k < k1; ++k) { const float2 v = g.hp[m.faces[k]]; x += g.cw4[k] * v.x; y += g.cw4[k] * v.y; }
-            r1 += double(x); r2 += double(y);
+            r1 = double(f1 + x) + t.raw[c];
+            r2 = double(f2 + y) + t.raw[nc + c];
+        } else {
+            r1 = double(f1);
+            r2 = double(f2);
         }
         if (!finite64(mass) || !finite64(r1) || !finite64(r2)) raise_status(ct, stage, ST_RATE);
         if (rate_out) { rate_out[c] = mass; rate_out[nc + c] = r1; rate_out[2 * nc + c] = r2; continue; }
@@ -741,7 +754,7 @@ __global__ void __launch_bounds__(256) km_update(MeshDev m, StateDev s, Ctrl *ct
             const double h = s.work[c] + dt * mass;
             double hu = s.work[nc + c] + dt * r1, hv = s.work[2 * nc + c] + dt * r2;
             if (h < 0) raise_status(ct, 1, ST_ENDPOINT);
-            if (h <= dry) { hu = 0.; hv = 0.; }
+            if (le_threshold(h, dry)) { hu = 0.; hv = 0.; }
             s.q1[c] = h; s.q1[nc + c] = hu; s.q1[2 * nc + c] = hv;
             // the second stage's input; an invalid one fails that stage
             if (!put_prim(P2, c, h, hu, hv, s.z[c], dry) && !(h < 0)) raise_status(ct, 2, ST_SPATIAL);
@@ -750,7 +763,7 @@ __global__ void __launch_bounds__(256) km_update(MeshDev m, StateDev s, Ctrl *ct
             double hu = .5 * s.work[nc + c] + .5 * (s.q1[nc + c] + dt * r1);
             double hv = .5 * s.work[2 * nc + c] + .5 * (s.q1[2 * nc + c] + dt * r2);
             if (!finite64(h) || !finite64(hu) || !finite64(hv) || h < 0) raise_status(ct, 2, ST_ENDPOINT);
-            if (h <= dry) { hu = 0.; hv = 0.; }
+            if (le_threshold(h, dry)) { hu = 0.; hv = 0.; }
             drag_f(ct, .5f * ct.trialf, h, hu, hv);
             double *qn = ct.cur ? s.q[0] : s.q[1];
             qn[c] = h; qn[nc + c] = hu; qn[2 * nc + c] = hv;
