@@ -823,6 +823,13 @@ extern "C" int brx_turbines_set(brx_solver *s, int nrotor, const int *rotor_scen
     TRY(s->upload(&p_slope, slope.data(), ncurve)); TRY(s->upload(&p_flat, flat.data(), nrotor));
     TRY(s->upload(&p_ucell, ucell.data(), ucell.size())); TRY(s->upload(&p_uoff, uoff.data(), uoff.size()));
     TRY(s->upload(&p_uent, uent.data(), uent.size()));
+    {
+        std::vector<unsigned char> foot(nc, 0);
+        for (int c : ucell) foot[c] = 1;
+        unsigned char *p_foot;
+        TRY(s->upload(&p_foot, foot.data(), foot.size()));
+        t.foot = p_foot;
+    }
     TRY(s->upload(&p_dxdy, dxdy, 2 * (size_t)nadj)); TRY(s->upload(&p_inv, inverse, 3 * (size_t)nc));
     TRY(s->upload(&p_xy, xy, 2 * (size_t)nc)); TRY(s->upload(&p_md, mid_disp, 4 * (size_t)nf));
     TRY(s->upload(&p_nu, nu, nc));

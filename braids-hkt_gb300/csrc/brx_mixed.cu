@@ -229,8 +229,14 @@ __global__ void __launch_bounds__(128) km_bed(MeshDev m, StateDev s, MixedGeo g)
 // ---------------------------------------------------------------------------
 // Cells: limited gradients and the cell record
 // ---------------------------------------------------------------------------
+// resident blocks per SM the register allocation of the cell sweep is fitted to
+#ifndef BRX_CELLS_MIN_BLOCKS
+#define BRX_CELLS_MIN_BLOCKS 8
+#endif
+
 template <int MAXF>
-__global__ void __launch_bounds__(128, 8) km_cells(MeshDev m, StateDev s, Ctrl *ctrl, Work w, MixedGeo g, int stage)
+__global__ void __launch_bounds__(128, BRX_CELLS_MIN_BLOCKS) km_cells(MeshDev m, StateDev s, Ctrl *ctrl, Work w,
+                                                                      MixedGeo g, int stage)
 {
     const int nc = m.nc;
     MxRec *rec = reinterpret_cast<MxRec *>(w.rec);
@@ -732,7 +738,8 @@ __global__ void __launch_bounds__(256) km_update(MeshDev m, StateDev s, Ctrl *ct
         double r1, r2;
         if (turb && t.hkt[sid]) {
             // ambient stress and balanced pressure (FP32 face sums, added in
-            // FP32), then the FP64 actuator sink: one conversion per component
+            // FP32), then the FP64 actuator sink of a support cell: one
+            // conversion per component
             const int k0 = m.offset[c], k1 = m.offset[c + 1];
             if (t.stress[sid]) {
                 float x = 0.f, y = 0.f;
@@ -741,8 +748,9 @@ __global__ void __launch_bounds__(256) km_update(MeshDev m, StateDev s, Ctrl *ct
             }
             float x = 0.f, y = 0.f;
             for (int k = k0; k < k1; ++k) { const float2 v = g.hp[m.faces[k]]; x += g.cw4[k] * v.x; y += g.cw4[k] * v.y; }
-            r1 = double(f1 + x) + t.raw[c];
-            r2 = double(f2 + y) + t.raw[nc + c];
+            r1 = double(f1 + x);
+            r2 = double(f2 + y);
+            if (t.foot[c]) { r1 += t.raw[c]; r2 += t.raw[nc + c]; }
         } else {
             r1 = double(f1);
             r2 = double(f2);
@@ -904,7 +912,10 @@ __global__ void __launch_bounds__(128) km_hkt_faces(MeshDev m, Ctrl *ctrl, Mixed
                                   qg * ((da - db) / d) * __fmul_rn(ha - hb, ha + hb) + (ca + cb);
                     delta -= gravity * sx * (wa * ha * G[4 * nc + a] + wb * hb * G[4 * nc + b]);
                     delta -= gravity * sy * (wa * ha * G[5 * nc + a] + wb * hb * G[5 * nc + b]);
-                    delta -= da * db / d * (float(t.raw[a] - t.raw[b]) * nx + float(t.raw[nc + a] - t.raw[nc + b]) * ny);
+                    // the actuator sink difference: FP64 rates, zero outside the rotor
+                    // support cells, so only faces touching one read and subtract them
+                    if (t.foot[a] | t.foot[b])
+                        delta -= da * db / d * (float(t.raw[a] - t.raw[b]) * nx + float(t.raw[nc + a] - t.raw[nc + b]) * ny);
                     const float speed = sqrtf(gravity * h), theta = fminf(1.f, fmaxf(t1.z, t1.w) / speed);
                     delta -= .5f * (1.f - theta) * speed * (2.f * hl * hr / (hl + hr)) * (t1.y - t1.x);
                     pr = make_float2(delta * nx, delta * ny);
