@@ -312,17 +312,17 @@ __global__ void __launch_bounds__(128, BRX_CELLS_MIN_BLOCKS) km_cells(MeshDev m,
                 gx[3] = gb.x; gy[3] = gb.y;
             }
             float theta1 = 1.f, theta2 = 1.f;
-            Slabs<MAXF> S0{}, S3{};
+            // one slab set, filled for the surface, then (stage-outlet cells
+            // only) refilled for the bed: half the live registers of two sets
+            Slabs<MAXF> S{};
             const float b0p = fmaxf(0.f, hi[0]), b0m = fmaxf(0.f, -lo[0]);
-            const float b3p = fmaxf(0.f, hi[3]), b3m = fmaxf(0.f, -lo[3]);
 #pragma unroll (MAXF <= 4 ? MAXF : 1)
             for (int j = 0; j < MAXF; ++j) {
                 if (j >= deg) continue;      // (a break would stop the unrolling)
                 const int k = k0 + j;
-                const int fl = g.cidx[k].y;
                 const float4 ge = g.cent[k];
                 const float rx = ge.z, ry = ge.w;
-                if (outlet && (fl & 2) && wet) {
+                if (outlet && (g.cidx[k].y & 2) && wet) {
                     // an open stage outlet with a subcritical wet owner keeps its bed slope
                     const float2 nn = g.fnorm[m.faces[k]];
                     if (fabsf(u * nn.x + v * nn.y) < sq && fabsf(gx[3] * rx + gy[3] * ry) > bedtol) continue;
@@ -339,16 +339,33 @@ __global__ void __launch_bounds__(128, BRX_CELLS_MIN_BLOCKS) km_cells(MeshDev m,
                 }
                 const float len = sqrtf(rx * rx + ry * ry);
                 if (len <= 0.f) continue;
-                const float il = 1.f / len, ux = rx * il, uy = ry * il;
-                S0.ux[j] = ux; S0.uy[j] = uy; S0.bp[j] = b0p * il; S0.bm[j] = b0m * il;
-                S0.mask |= 1u << j;
-                if (outlet && !(fl & 4)) {          // walls do not bound the bed
-                    S3.ux[j] = ux; S3.uy[j] = uy; S3.bp[j] = b3p * il; S3.bm[j] = b3m * il;
-                    S3.mask |= 1u << j;
-                }
+                const float il = 1.f / len;
+                S.ux[j] = rx * il; S.uy[j] = ry * il; S.bp[j] = b0p * il; S.bm[j] = b0m * il;
+                S.mask |= 1u << j;
             }
-            if (!slabs_feasible(S0, gx[0], gy[0])) slabs_project(S0, gx[0], gy[0]);
-            if (outlet && !slabs_feasible(S3, gx[3], gy[3])) slabs_project(S3, gx[3], gy[3]);
+            if (!slabs_feasible(S, gx[0], gy[0])) slabs_project(S, gx[0], gy[0]);
+            if (outlet) {
+                const float b3p = fmaxf(0.f, hi[3]), b3m = fmaxf(0.f, -lo[3]);
+                S.mask = 0u;
+#pragma unroll (MAXF <= 4 ? MAXF : 1)
+                for (int j = 0; j < MAXF; ++j) {
+                    if (j >= deg) continue;
+                    const int k = k0 + j;
+                    const int fl = g.cidx[k].y;
+                    const float4 ge = g.cent[k];
+                    const float rx = ge.z, ry = ge.w;
+                    if ((fl & 2) && wet) {
+                        const float2 nn = g.fnorm[m.faces[k]];
+                        if (fabsf(u * nn.x + v * nn.y) < sq && fabsf(gx[3] * rx + gy[3] * ry) > bedtol) continue;
+                    }
+                    const float len = sqrtf(rx * rx + ry * ry);
+                    if (len <= 0.f || (fl & 4)) continue;          // walls do not bound the bed
+                    const float il = 1.f / len;
+                    S.ux[j] = rx * il; S.uy[j] = ry * il; S.bp[j] = b3p * il; S.bm[j] = b3m * il;
+                    S.mask |= 1u << j;
+                }
+                if (!slabs_feasible(S, gx[3], gy[3])) slabs_project(S, gx[3], gy[3]);
+            }
             gx[1] *= fmaxf(0.f, theta1); gy[1] *= fmaxf(0.f, theta1);
             gx[2] *= fmaxf(0.f, theta2); gy[2] *= fmaxf(0.f, theta2);
         }
