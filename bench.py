@@ -31,6 +31,12 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 METRIC = "cell-updates/s"
 BYTES_PER_CELL_UPDATE = {"fp64": 680.0, "mixed": 384.0}   # algorithmic bytes, two-sweep design
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per cell of one
+# launch of each mixed-form sweep, from one ncu --set full capture of the
+# 24-scenario subset with rotors (scenarios 20..43, 1,967,962 cells, inputs
+# larger than L2): a launch of the full batch is scaled by its cells
+TRAFFIC_BYTES_PER_CELL = {"mixed": {"cells": 204.57, "faces": 194.97, "gather": 145.71, "update": 171.57,
+                                    "drag": 62.27}}
 KERNEL_NAMES = ["drag", "boundary", "cells", "faces", "gather", "limit", "update", "control"]
 
 
@@ -390,14 +396,14 @@ def main():
     dom_bytes = algorithmic_bytes(dom, nc, nf, nadj, nslot, precision)
     peak, peak_kind = peaks()
     achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", f"traffic_{args.workload}.json")
-    if os.path.exists(tpath):
-        with open(tpath) as f:
-            traffic = json.load(f).get(dom)
+    per_cell = TRAFFIC_BYTES_PER_CELL.get(precision, {}).get(dom)
+    traffic = per_cell * nc if per_cell is not None and args.workload == "config4" else None
     total_ms = sum(sum(v) for v in per_kind.values())
     roofline = {"bound": "hbm", "kernel": f"k_{dom}", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                "frac": achieved / peak, "traffic": traffic,
+                "traffic_source": ("ncu DRAM bytes per cell of a 24-scenario subset capture, scaled by cells"
+                                   if traffic is not None else None),
+                "peak_source": peak_kind,
                 "kernel_ms": dom_ms, "kernel_share_of_substep": sum(per_kind[dom]) / total_ms,
                 "substep_kernels_ms": {k: [round(v, 4) for v in vs] for k, vs in per_kind.items()},
                 "algorithmic_bytes_per_launch": dom_bytes,
