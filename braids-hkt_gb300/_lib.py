@@ -45,6 +45,7 @@ SIGNATURES = {
     "brx_critical_chains_set": (I, [P, P, P, P]),
     "brx_inlet_lines_set": (I, [P, P, P, P, P]),
     "brx_forcing_get": (I, [P, P]),
+    "brx_ledger_get": (I, [P, P]),
     "brx_hllc_set": (I, [P, P, P, P, P]),
     "brx_method_set": (I, [P, I]),
     "brx_launch_shape_set": (I, [P, I, I, I]),

@@ -1134,6 +1134,14 @@ extern "C" int brx_forcing_get(brx_solver *s, double *out)
     return BRX_OK;
 }
 
+extern "C" int brx_ledger_get(brx_solver *s, double *out)
+{
+    if (!s || !out) return fail(BRX_ERR_ARGUMENT, "null argument");
+    if (s->pending) return fail(BRX_ERR_STATE, "an asynchronous interval is in flight");
+    for (int i = 0; i < s->nscen; ++i) out[i] = s->h_ctrl[i].ledger;
+    return BRX_OK;
+}
+
 extern "C" int brx_hint_set(brx_solver *s, const double *hint)
 {
     if (!s || !hint) return fail(BRX_ERR_ARGUMENT, "null argument");
@@ -1370,6 +1378,8 @@ static void begin_interval_each(brx_solver *s, const double *dt_each, const doub
         c.floor_ = std::ldexp(dt, -20);
         c.substeps = c.rejections = c.done = c.failed = c.cur = 0;
         c.min_dt = c.max_dt = c.cfl_max = 0.0;
+        c.bflux[0] = c.bflux[1] = c.ledger = 0.0;
+        c.one_stage = s->method == BRX_METHOD_HLLC;
         c.done = !c.active;
         host_set_trial(c);
     }

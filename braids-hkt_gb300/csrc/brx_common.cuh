@@ -56,13 +56,17 @@ struct Ctrl {
     // interval
     double dt_outer, time0, elapsed, hint, floor_, trial;
     int truncated, substeps, rejections, done;
-    int failed, cur, max_substeps, pad0;
+    int failed, cur, max_substeps, one_stage;   // one_stage: a one-evaluation method (HLLC / Hancock)
     // this trial
     unsigned status1, status2;
     unsigned long long peak1, peak2;  // bit patterns of nonnegative doubles
     // diagnostics
     double min_dt, max_dt, cfl_max;
     double accepted_water_time;       // sum of accepted trial lengths (== elapsed)
+    // water budget: each stage's sum over open faces of (outward water flux x
+    // length) as the update uses it, and the interval's boundary ledger, the
+    // net inflow volume of the accepted substeps (shoreline_solver.py:353-355)
+    double bflux[2], ledger;
     // FP32 copies for the mixed form's sweeps, refreshed with every trial
     float gravf, dryf, trialf, roughf;
     int cfl1, pad1;                         // stage 1 exceeded the CFL limit (mixed form, set after its gather)

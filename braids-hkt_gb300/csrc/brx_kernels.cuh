@@ -1235,6 +1235,77 @@ __device__ bool line_section(SectionWork &w, const MeshDev &m, const BoundaryDev
     return ok;
 }
 
+// Exact-discharge inlet allocation of one scenario (boundary CTA, after the outlet cap).
+__device__ void inlet_allocation(const MeshDev &m, const BoundaryDev &b, const Ctrl &ct, const double *base, int s0,
+                                 int s1, int u0, int u1)
+{
+    // exact-discharge inlet allocation (inlet_feasibility.py:34-57): each
+    // owner's outward inlet debit capped by its stock after its other
+    // boundary debits (owner factor kept per slot in terms), then per inlet
+    // segment the removed outflow taken from its incoming faces; sums in
+    // boundary order, as the reference's bincounts
+    __syncthreads();
+    const size_t ns = b.nslot;
+    for (int u = u0 + threadIdx.x; u < u1; u += blockDim.x) {
+        const int c = b.own_cell[u];
+        double total = 0., reserved = 0.;
+        for (int j = b.own_off[u]; j < b.own_off[u + 1]; ++j) {
+            const int k = b.own_slot[j], f = b.slot_face[k];
+            const double rate = fmax(b.flux[k], 0.) * m.length[f];
+            if (b.seg_mode[m.bid[f]] == 9) total += rate; else reserved += rate;
+        }
+        const double available = fmax(0., base[c] * m.area[c] / ct.trial - reserved);
+        const double ratio = fmin(1., available / fmax(total, 1e-300)) * (1. - 32. * EPS);
+        const double factor = total > available ? ratio : 1.;
+        for (int j = b.own_off[u]; j < b.own_off[u + 1]; ++j) b.terms[b.own_slot[j]] = factor;
+    }
+    __syncthreads();
+    for (int sg = s0 + threadIdx.x; sg < s1; sg += blockDim.x) {
+        if (b.seg_mode[sg] != 9) continue;
+        double removed = 0., incoming = 0.;
+        for (int k = b.seg_off[sg]; k < b.seg_off[sg + 1]; ++k) {
+            const double water = b.flux[k], len = m.length[b.slot_face[k]];
+            removed += water > 0. ? fmax(water, 0.) * len * (1. - b.terms[k]) : 0.;
+            incoming += fmax(-water, 0.) * len;
+        }
+        const bool feasible = removed <= incoming;
+        const double in_scale = incoming > 0. ? 1. - removed / fmax(incoming, 1e-300) : 1.;
+        for (int k = b.seg_off[sg]; k < b.seg_off[sg + 1]; ++k) {
+            const double water = b.flux[k];
+            const double scale = (feasible && water > 0.) ? b.terms[k] : ((feasible && water < 0.) ? in_scale : 1.);
+            const double depth = b.trace[k], denom = fmax(depth, 1e-300);
+            const double ux = depth > 0. ? b.trace[ns + k] / denom : 0.;
+            const double uy = depth > 0. ? b.trace[2 * ns + k] / denom : 0.;
+            b.flux[ns + k] += (scale * scale - 1.) * water * ux;
+            b.flux[2 * ns + k] += (scale * scale - 1.) * water * uy;
+            b.flux[k] = water * scale;
+            b.trace[ns + k] *= scale;
+            b.trace[2 * ns + k] *= scale;
+        }
+    }
+}
+
+// The scenario's sum over its open faces of (outward water flux x length),
+// with each face's water as the update consumes it (the mixed form carries
+// it in FP32: F(flux)); per-thread strided sums added by thread 0 in thread
+// order. The controller turns the stage sums into the boundary ledger.
+constexpr int BOUNDARY_THREADS = 256;
+template <class F>
+__device__ void boundary_water(const MeshDev &m, const BoundaryDev &b, Ctrl &ct, int stage, int k0, int k1)
+{
+    __shared__ double part[BOUNDARY_THREADS];
+    __syncthreads();
+    double acc = 0.;
+    for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) acc += double(F(b.flux[k])) * m.length[b.slot_face[k]];
+    if (threadIdx.x < BOUNDARY_THREADS) part[threadIdx.x] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double total = 0.;
+        for (int i = 0; i < (int)blockDim.x && i < BOUNDARY_THREADS; ++i) total += part[i];
+        ct.bflux[stage - 1] = total;
+    }
+}
+
 // stage 1 / 2: the SSPRK stages (state work / q1, its own stock, clock t or
 // t + dt); STAGE_HANCOCK: the HLLC predicted state q1 at t + dt/2, outlet
 // stock of the substep's start state work (hllc.py:91-97), status of stage 1.
@@ -1469,51 +1540,8 @@ __global__ void k_boundary(MeshDev m, StateDev s, BoundaryDev b, Ctrl *ctrl, int
             b.trace[2 * (size_t)b.nslot + k] *= scale;
         }
     }
-    if (!b.inlet) return;
-    // exact-discharge inlet allocation (inlet_feasibility.py:34-57): each
-    // owner's outward inlet debit capped by its stock after its other
-    // boundary debits (owner factor kept per slot in terms), then per inlet
-    // segment the removed outflow taken from its incoming faces; sums in
-    // boundary order, as the reference's bincounts
-    __syncthreads();
-    const size_t ns = b.nslot;
-    for (int u = u0 + threadIdx.x; u < u1; u += blockDim.x) {
-        const int c = b.own_cell[u];
-        double total = 0., reserved = 0.;
-        for (int j = b.own_off[u]; j < b.own_off[u + 1]; ++j) {
-            const int k = b.own_slot[j], f = b.slot_face[k];
-            const double rate = fmax(b.flux[k], 0.) * m.length[f];
-            if (b.seg_mode[m.bid[f]] == 9) total += rate; else reserved += rate;
-        }
-        const double available = fmax(0., base[c] * m.area[c] / ct.trial - reserved);
-        const double ratio = fmin(1., available / fmax(total, 1e-300)) * (1. - 32. * EPS);
-        const double factor = total > available ? ratio : 1.;
-        for (int j = b.own_off[u]; j < b.own_off[u + 1]; ++j) b.terms[b.own_slot[j]] = factor;
-    }
-    __syncthreads();
-    for (int sg = s0 + threadIdx.x; sg < s1; sg += blockDim.x) {
-        if (b.seg_mode[sg] != 9) continue;
-        double removed = 0., incoming = 0.;
-        for (int k = b.seg_off[sg]; k < b.seg_off[sg + 1]; ++k) {
-            const double water = b.flux[k], len = m.length[b.slot_face[k]];
-            removed += water > 0. ? fmax(water, 0.) * len * (1. - b.terms[k]) : 0.;
-            incoming += fmax(-water, 0.) * len;
-        }
-        const bool feasible = removed <= incoming;
-        const double in_scale = incoming > 0. ? 1. - removed / fmax(incoming, 1e-300) : 1.;
-        for (int k = b.seg_off[sg]; k < b.seg_off[sg + 1]; ++k) {
-            const double water = b.flux[k];
-            const double scale = (feasible && water > 0.) ? b.terms[k] : ((feasible && water < 0.) ? in_scale : 1.);
-            const double depth = b.trace[k], denom = fmax(depth, 1e-300);
-            const double ux = depth > 0. ? b.trace[ns + k] / denom : 0.;
-            const double uy = depth > 0. ? b.trace[2 * ns + k] / denom : 0.;
-            b.flux[ns + k] += (scale * scale - 1.) * water * ux;
-            b.flux[2 * ns + k] += (scale * scale - 1.) * water * uy;
-            b.flux[k] = water * scale;
-            b.trace[ns + k] *= scale;
-            b.trace[2 * ns + k] *= scale;
-        }
-    }
+    if (b.inlet) inlet_allocation(m, b, ct, base, s0, s1, u0, u1);
+    boundary_water<F>(m, b, ct, stage, k0, k1);
 }
 
 // ---------------------------------------------------------------------------
@@ -2102,6 +2130,7 @@ __device__ void control_one(Ctrl &c)
     } else {
         c.cur ^= 1;
         c.elapsed += c.trial;
+        c.ledger -= c.trial * (c.one_stage ? c.bflux[0] : .5 * (c.bflux[0] + c.bflux[1]));
         c.substeps++;
         if (c.substeps == 1 || c.trial < c.min_dt) c.min_dt = c.trial;
         if (c.trial > c.max_dt) c.max_dt = c.trial;

@@ -115,6 +115,26 @@ def critical_chains(cases, face_offset=None):
     return (np.asarray(segc, np.int32), np.asarray(off, np.int32), np.asarray(faces if faces else [0], np.int32))
 
 
+class WaterBudgetError(RuntimeError):
+    """A step whose volume change differs from its boundary ledger (the reference's BendTrialRejected)."""
+
+
+def water_budget(v0, v1, ledger, inventory=None, gross=None):
+    """The owner's water-budget test per scenario (shoreline_solver.py:29-39,
+    353-360): residual = (V1 - V0) - ledger against the FP64 roundoff
+    allowance max(1e-10, 64 eps max(1, inventory, gross)). Without per-cell
+    data the inventory is max(V0, V1) and the gross boundary volume |ledger|.
+    Returns (residual, allowance, ok)."""
+    v0, v1, ledger = (np.asarray(a, dtype=np.float64) for a in (v0, v1, ledger))
+    residual = (v1 - v0) - ledger
+    inventory = np.maximum(v0, v1) if inventory is None else np.asarray(inventory, dtype=np.float64)
+    gross = np.abs(ledger) if gross is None else np.asarray(gross, dtype=np.float64)
+    scale = np.maximum(1.0, np.maximum(np.abs(inventory), np.abs(gross)))
+    allowance = np.maximum(1e-10, 64 * np.finfo(float).eps * scale)
+    ok = np.isfinite(residual) & (np.abs(residual) <= allowance)
+    return residual, allowance, ok
+
+
 LINES = {"stage": 0, "critical": 1, "normal": 2}
 
 
@@ -536,11 +556,41 @@ class RiverSolver:
         """Device memory the solver holds (its allocations plus the bound state)."""
         return int(self.lib.brx_solver_bytes(self.h)) + self.q.numel() * 8 + self.z.numel() * 8
 
+    def ledger(self):
+        """Net inflow volume [m3] through the open faces over the last interval, per scenario."""
+        out = np.zeros(self.nscen)
+        check(self.lib.brx_ledger_get(self.h, _ptr(out)))
+        return out
+
     def step(self, dt):
-        """Advance by dt from the owner clock (ShorelineSolver.step)."""
-        diag = self.advance(dt, self.time[0])
+        """Advance by dt from the owner clock with the owner's water-budget
+        check (ShorelineSolver.step, shoreline_solver.py:345-372): the volume
+        change of every scenario must equal its boundary ledger within the
+        FP64 roundoff allowance, else the state is restored and
+        WaterBudgetError raised; on success the ledger is committed."""
+        self.torch.cuda.current_stream().synchronize()
+        q0, z0, hints0 = self.q.clone(), self.z.clone(), self.hints()
+        v0 = np.atleast_2d(self.totals())[:, 0]
+        try:
+            diag = self.advance(dt, self.time[0])
+        except BaseException:
+            self.q.copy_(q0); self.z.copy_(z0); self.set_hints(hints0)
+            raise
+        v1 = np.atleast_2d(self.totals())[:, 0]
+        ledger = self.ledger()
+        residual, roundoff, ok = water_budget(v0, v1, ledger)
+        if not ok.all():
+            self.q.copy_(q0); self.z.copy_(z0); self.set_hints(hints0)
+            i = int(np.flatnonzero(~ok)[0])
+            raise WaterBudgetError(f"scenario {i}: water budget failed: residual={residual[i]:.6e} m3, "
+                                   f"roundoff={roundoff[i]:.6e} m3")
+        self.water_ledger = getattr(self, "water_ledger", np.zeros(self.nscen)) + ledger
         self.time += dt
         self.steps += 1
+        rows = diag if isinstance(diag, list) else [diag]
+        for r, res, lim in zip(rows, residual, roundoff):
+            r["water_residual_m3"] = float(res)
+            r["water_increment_roundoff_limit_m3"] = float(lim)
         return dict(q=self.q, z=self.z, diagnostics=diag)
 
     def substep(self, dt, time=0.0):

@@ -313,6 +313,14 @@ int brx_method_set(brx_solver *s, int method);
  * reference's ExteriorBed.forcing after evaluate. */
 int brx_forcing_get(brx_solver *s, double *out);
 
+/* Boundary ledger of the last interval, host out (nscen): the net volume
+ * [m3] that entered through open faces over the accepted substeps,
+ * -sum_k dt_k sum_f water_f length_f with each stage's water as the update
+ * used it (SSPRK: the mean of the two stages; HLLC: its one evaluation). The
+ * owner's water budget (ShorelineSolver.step, shoreline_solver.py:353-360)
+ * compares it with the volume change (brx_totals before and after). */
+int brx_ledger_get(brx_solver *s, double *out);
+
 /* Step hint carried between brx_advance calls (nscen, host; <= 0 = none). */
 int brx_hint_get(brx_solver *s, double *hint);
 int brx_hint_set(brx_solver *s, const double *hint);
