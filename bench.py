@@ -50,6 +50,20 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def aggregate(seconds, updates, dist=None, device="cpu"):
+    """Whole-job figures over ranks: the slowest rank's timed seconds and the
+    sum of every rank's cell-updates (each rank advances its own scenarios,
+    no exchange on the data path)."""
+    if dist is None:
+        return seconds, updates
+    import torch
+    t = torch.tensor([float(seconds)], dtype=torch.float64, device=device)
+    u = torch.tensor([float(updates)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(t.item()), int(u.item())
+
+
 def build_workload(name, rank=0, world=1, subset=None):
     """(cases, precision, outer dt [s], config dict). Built before CUDA starts (spawn pool)."""
     import braids_hkt_gb300.scenarios as S
@@ -354,13 +368,7 @@ def main():
     cfg["substeps_per_interval"] = {"min": int(subs.min()), "median": float(np.median(subs)), "max": int(subs.max()),
                                     "cell_weighted_mean": float((subs * cells).sum() / cells.sum())}
     clock_info = clocks.stop()
-    t_max = device_ms / 1e3
-    if dist is not None:
-        t = torch.tensor([t_max, float(updates)], device="cuda", dtype=torch.float64)
-        tmax = t[:1].clone()
-        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
-        dist.all_reduce(t[1:], op=dist.ReduceOp.SUM)
-        t_max, updates = float(tmax.item()), int(t[1].item())
+    t_max, updates = aggregate(device_ms / 1e3, updates, dist, "cuda")
     value = updates / t_max
 
     state_after_timed = solver.q.cpu().numpy()       # for the accuracy check against FP64 below
