@@ -860,9 +860,8 @@ extern "C" int brx_turbines_set(brx_solver *s, int nrotor, const int *rotor_scen
         TRY(s->upload(&p_hdxy, hdxy.data(), nadj)); TRY(s->upload(&p_hcc, hcc.data(), nf));
         TRY(s->upload(&p_hmd, hmd.data(), nf));
         s->mx.hdxy = p_hdxy; s->mx.hcc = p_hcc; s->mx.hmd = p_hmd;
-        TRY(s->alloc(&s->mx.htr, 2 * (size_t)nf)); TRY(s->alloc(&s->mx.hgrad, 6 * (size_t)nc));
+        TRY(s->alloc(&s->mx.hgrad, 6 * (size_t)nc));
         TRY(s->alloc(&s->mx.hp, nf)); TRY(s->alloc(&s->mx.hs, nf));
-        CK(cudaMemset(s->mx.htr, 0, sizeof(float4) * 2 * (size_t)nf));
         CK(cudaMemset(s->mx.hgrad, 0, sizeof(float) * 6 * (size_t)nc));
         CK(cudaMemset(s->mx.hp, 0, sizeof(float2) * nf)); CK(cudaMemset(s->mx.hs, 0, sizeof(float2) * nf));
     } else {
@@ -1280,9 +1279,13 @@ static void enqueue_stage(brx_solver *s, int stage, double *rate_out)
     }
     s->launches += launch_kernel(s, K_CELLS, stage, nullptr);
     if (fork) cudaStreamWaitEvent(s->stream, s->join, 0);
+    // the mixed face sweep computes the rotor face terms in its tail: it
+    // needs the rotor cell terms (wet gradients, actuator sink) first
+    const bool mixed = s->precision == BRX_MIXED;
+    if (fork && mixed) cudaStreamWaitEvent(s->stream, s->join2, 0);
     for (int kind : {(int)K_FACES, (int)K_GATHER, (int)K_LIMIT})
         s->launches += launch_kernel(s, kind, stage, kind == K_LIMIT ? rate_out : nullptr);
-    if (fork) cudaStreamWaitEvent(s->stream, s->join2, 0);
+    if (fork && !mixed) cudaStreamWaitEvent(s->stream, s->join2, 0);
     s->launches += launch_turbines(s, stage, s->stream, TURB_FACES);
     s->launches += launch_kernel(s, K_UPDATE, stage, rate_out);
 }
@@ -1646,10 +1649,13 @@ extern "C" int brx_profile_substep(brx_solver *s, double dt, double time, int ca
         for (int kind : HLLC_SEQUENCE)
             if (const int nl = launch_hllc(s, kind)) { mark(kind); extra += nl - 1; }
     } else {
+        // the mixed face sweep reads the rotor cell terms: they come first there
+        const bool mixed = s->precision == BRX_MIXED;
         for (int stage = 1; stage <= 2; ++stage)
-            for (int kind : {(int)K_BOUNDARY, (int)K_CELLS, (int)K_FACES, (int)K_GATHER, (int)K_LIMIT, (int)K_TURB,
-                             (int)K_UPDATE})
-                if (const int nl = launch_kernel(s, kind, stage, nullptr)) { mark(kind); extra += nl - 1; }
+            for (int kind : {(int)K_BOUNDARY, mixed ? (int)K_TURB : -1, (int)K_CELLS, (int)K_FACES, (int)K_GATHER,
+                             (int)K_LIMIT, mixed ? -1 : (int)K_TURB, (int)K_UPDATE})
+                if (kind >= 0)
+                    if (const int nl = launch_kernel(s, kind, stage, nullptr)) { mark(kind); extra += nl - 1; }
     }
     k_control<<<1, 256, 0, st>>>(s->d_ctrl, s->nscen, s->mesh.act); mark(7);
     k_commit<<<s->grid_c256, 256, 0, st>>>(s->mesh, s->state, s->d_ctrl);

@@ -27,7 +27,6 @@ struct MixedGeo {
     const float2 *hdxy;      // (nadj) centre offsets of the flow least-squares metric
     const float4 *hmd;       // (nf) face-midpoint displacement: owner x, y; neighbour x, y
     const float2 *hcc;       // (nf) neighbour centroid - owner centroid
-    float4 *htr;             // (2 nf) face traces: (hl, hr, common bed, constant flags), (un_l, un_r, |u|_l, |u|_r)
     float *hgrad;            // (6, nc) wet gradients of u, v, eta
     float2 *hp, *hs;         // (nf) balanced-pressure correction, ambient stress
 };

@@ -433,6 +433,62 @@ __device__ __forceinline__ float hydro_perturbation(float dh, float hL, float h,
     return __fadd_rn(__fmul_rn(dh, hL + h), __fmul_rn(h + raw, db));
 }
 
+// Rotor face terms of one interior face between two wet cells (the balanced
+// pressure correction and the ambient stress, river_turbine_flow.h:13-82,
+// river_hydrokinetic_stress.h:13-35), from the cell records and the face's
+// hydrostatic traces t0 (hl, hr, common bed, constant flags) and t1 (un_l,
+// un_r, |u|_l, |u|_r): computed in the face sweep's tail, so the traces never
+// leave registers.
+__device__ __forceinline__ void hkt_face_terms(const MxRec &pa, const MxRec &pb, float4 t0, float4 t1, int f, int a,
+                                               int b, int sid, float gravity, float dry, const MixedGeo &g,
+                                               const TurbDev &t, int nc, float2 &pr, float2 &st)
+{
+    const float2 nn = g.fnorm[f], di = g.fdist[f];
+    const float nx = nn.x, ny = nn.y, da = di.x, db = di.y, d = da + db, wa = db / d, wb = da / d;
+    const float zb = g.fdb[f];
+    const float ea = pa.h, eb = pa.h + ((pb.ehi - pa.ehi) + (pb.elo - pa.elo));
+    if (t.stress[sid]) {
+        float h = fminf(pa.h, pb.h);
+        h = fminf(h, fmaxf(0.f, .5f * (ea + eb) - fmaxf(0.f, zb)));
+        const float visc = wa * float(t.nu[a]) + wb * float(t.nu[b]);
+        const float2 dd = g.hcc[f];
+        const float dn = dd.x * nx + dd.y * ny;
+        const float du = pb.u - pa.u, dv = pb.v - pa.v;
+        const float *G = g.hgrad;
+        float ux = wa * G[a] + wb * G[b], uy = wa * G[nc + a] + wb * G[nc + b];
+        float vx = wa * G[2 * nc + a] + wb * G[2 * nc + b], vy = wa * G[3 * nc + a] + wb * G[3 * nc + b];
+        const float cu = (du - ux * dd.x - uy * dd.y) / dn, cv = (dv - vx * dd.x - vy * dd.y) / dn;
+        ux += cu * nx; uy += cu * ny; vx += cv * nx; vy += cv * ny;
+        st = make_float2(visc * h * (2.f * ux * nx + (uy + vx) * ny), visc * h * ((uy + vx) * nx + 2.f * vy * ny));
+    }
+    const int cf = __float_as_int(t0.w);
+    const float top = t0.z, bed = fmaxf(fmaxf(0.f, zb), top);
+    const float ha = fmaxf(0.f, ea - bed), hb = fmaxf(0.f, eb - bed);
+    const float hl = fmaxf(0.f, (top + t0.x) - bed), hr = fmaxf(0.f, (top + t0.y) - bed);
+    const float h = .5f * (hl + hr);
+    const float qg = .25f * gravity;
+    const float ca = (cf & 1) ? qg * __fmul_rn(ha - hl, ha + hl) : 0.f;
+    const float cb = (cf & 2) ? qg * __fmul_rn(hb - hr, hb + hr) : 0.f;
+    const float scale = qg * (hl * hl + hr * hr);                       // |po|, |pn| to first order
+    if (!(fminf(fminf(ha, hb), fminf(hl, hr)) <= dry) && !(fabsf(hr - hl) > .005f * h) &&
+        !(fabsf(2.f * (ca - cb)) > 128.f * FEPS * fmaxf(1.f, scale))) {
+        const float4 md = g.hmd[f];
+        const float sx = wa * md.x + wb * md.z, sy = wa * md.y + wb * md.w;
+        const float *G = g.hgrad;
+        float delta = qg * (__fmul_rn(hl - ha, hl + ha) + __fmul_rn(hr - hb, hr + hb)) +
+                      qg * ((da - db) / d) * __fmul_rn(ha - hb, ha + hb) + (ca + cb);
+        delta -= gravity * sx * (wa * ha * G[4 * nc + a] + wb * hb * G[4 * nc + b]);
+        delta -= gravity * sy * (wa * ha * G[5 * nc + a] + wb * hb * G[5 * nc + b]);
+        // the actuator sink difference: FP64 rates, zero outside the rotor
+        // support cells, so only faces touching one read and subtract them
+        if (t.foot[a] | t.foot[b])
+            delta -= da * db / d * (float(t.raw[a] - t.raw[b]) * nx + float(t.raw[nc + a] - t.raw[nc + b]) * ny);
+        const float speed = sqrtf(gravity * h), theta = fminf(1.f, fmaxf(t1.z, t1.w) / speed);
+        delta -= .5f * (1.f - theta) * speed * (2.f * hl * hr / (hl + hr)) * (t1.y - t1.x);
+        pr = make_float2(delta * nx, delta * ny);
+    }
+}
+
 __global__ void __launch_bounds__(128, 8) km_faces(MeshDev m, StateDev s, BoundaryDev b, Ctrl *ctrl, Work w,
                                                 MixedGeo g, int stage, TurbDev t, int turb)
 {
@@ -441,10 +497,12 @@ __global__ void __launch_bounds__(128, 8) km_faces(MeshDev m, StateDev s, Bounda
     float2 *ws = reinterpret_cast<float2 *>(w.ws);
     float4 *gf = reinterpret_cast<float4 *>(w.gf);
     FOR_ACTIVE_FACES(m.act, f) {
-        Ctrl &ct = ctrl[m.face_sid[f]];
+        const int sid = m.face_sid[f];
+        Ctrl &ct = ctrl[sid];
         if (mx_skip(ct, stage)) continue;
         const float dry = ct.dryf, grav = ct.gravf;
         const float half_g = 0.5f * grav;
+        const bool rotors = turb && t.hkt[sid];
         const int c = m.owner[f], n = m.neighbour[f];
         const float2 nn = g.fnorm[f];
         const float nx = nn.x, ny = nn.y;
@@ -463,6 +521,10 @@ __global__ void __launch_bounds__(128, 8) km_faces(MeshDev m, StateDev s, Bounda
                                             sqrt(gd * hb) : 0.;
             ws[f] = make_float2(float(fl0), float(fmax(a, bb)));
             gf[f] = make_float4(float(fl1 - pc * dn), float(fl2 - pc * dm), 0.f, 0.f);
+            if (rotors) {
+                g.hp[f] = make_float2(0.f, 0.f);
+                if (t.stress[sid]) g.hs[f] = make_float2(0.f, 0.f);
+            }
             continue;
         }
         MxRec rn;
@@ -478,6 +540,7 @@ __global__ void __launch_bounds__(128, 8) km_faces(MeshDev m, StateDev s, Bounda
         if (n >= 0) R = mx_side(rn, dsp.z, dsp.w, dry, kind == 0, bad);
         float water = 0.f, speed = 0.f;
         float gl1 = 0.f, gl2 = 0.f, gr1 = 0.f, gr2 = 0.f;
+        bool rotor_face = false;       // the rotor face terms were formed in the flux branch
         if (kind != 0) {
             float hL = L.h, xL = L.hu, yL = L.hv;
             float hR = R.h, xR = R.hu, yR = R.hv;
@@ -497,6 +560,7 @@ __global__ void __launch_bounds__(128, 8) km_faces(MeshDev m, StateDev s, Bounda
             const float unL = xL * nx + yL * ny, utL = xL * (-ny) + yL * nx;
             const float unR = xRr * nx + yRr * ny, utR = xRr * (-ny) + yRr * nx;
             float loc[8] = {hL, unL, utL, 0.f, hR, unR, utR, 0.f};
+            float top_bed = 0.f;           // the face's common bed (kind 1), for the rotor terms
             if (kind == 1) {
                 const float top = fmaxf(bLr, bRr);
                 const float bc = rc.ehi - hc;      // the owner's bed, as a tolerance scale
@@ -509,14 +573,7 @@ __global__ void __launch_bounds__(128, 8) km_faces(MeshDev m, StateDev s, Bounda
                 loc[2] = hL > dry ? utL * (hl / hL) : 0.f;
                 loc[5] = hR > dry ? unR * (hr / hR) : 0.f;
                 loc[6] = hR > dry ? utR * (hr / hR) : 0.f;
-                if (turb && t.hkt[m.face_sid[f]]) {
-                    // traces for the rotor pressure correction (beds relative to the owner's)
-                    const int fl = (rc.flags & 1) | ((rn.flags & 1) << 1);
-                    g.htr[f] = make_float4(hl, hr, top, __int_as_float(fl));
-                    g.htr[nf + f] = make_float4(hl > 0.f ? loc[1] / hl : 0.f, hr > 0.f ? loc[5] / hr : 0.f,
-                                                hl > 0.f ? hypotf(loc[1], loc[2]) / hl : 0.f,
-                                                hr > 0.f ? hypotf(loc[5], loc[6]) / hr : 0.f);
-                }
+                top_bed = top;
             }
             bool closed = false;
             if (kind == 1 && !(fminf(hc, hn) > dry)) {
@@ -589,12 +646,21 @@ __global__ void __launch_bounds__(128, 8) km_faces(MeshDev m, StateDev s, Bounda
             }
             water = dl0;
             if (!isfinite(water) || !isfinite(gl1) || !isfinite(gl2) || !isfinite(gr1) || !isfinite(gr2)) bad = 1;
-        } else {
-            if (turb && n >= 0 && t.hkt[m.face_sid[f]]) {
-                const int fl = (rc.flags & 1) | ((rn.flags & 1) << 1);
-                g.htr[f] = make_float4(0.f, 0.f, 0.f, __int_as_float(fl));
-                g.htr[nf + f] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (rotors && kind == 1 && wc && wn) {
+                // traces for the rotor pressure correction (beds relative to the
+                // owner's; loc holds the hydrostatic face states, fwave reads it only)
+                const float hl = loc[0], hr = loc[4];
+                const float4 t0 = make_float4(hl, hr, top_bed, __int_as_float((rc.flags & 1) | ((rn.flags & 1) << 1)));
+                const float4 t1 = make_float4(hl > 0.f ? loc[1] / hl : 0.f, hr > 0.f ? loc[5] / hr : 0.f,
+                                              hl > 0.f ? hypotf(loc[1], loc[2]) / hl : 0.f,
+                                              hr > 0.f ? hypotf(loc[5], loc[6]) / hr : 0.f);
+                float2 pr = make_float2(0.f, 0.f), st = make_float2(0.f, 0.f);
+                hkt_face_terms(rec[c], rec[n], t0, t1, f, c, n, sid, grav, dry, g, t, nc, pr, st);
+                g.hp[f] = pr;
+                if (t.stress[sid]) g.hs[f] = st;
+                rotor_face = true;
             }
+        } else {
             // dry face: zero flux, the cells' own pressure still enters the gather
             gl1 = -half_g * hc * hc * nx; gl2 = -half_g * hc * hc * ny;
             gr1 = -half_g * hn * hn * nx; gr2 = -half_g * hn * hn * ny;
@@ -602,6 +668,10 @@ __global__ void __launch_bounds__(128, 8) km_faces(MeshDev m, StateDev s, Bounda
         if (bad) raise_status(ct, stage, ST_SPATIAL);
         ws[f] = make_float2(water, speed);
         gf[f] = make_float4(gl1, gl2, gr1, gr2);
+        if (rotors && !rotor_face) {
+            g.hp[f] = make_float2(0.f, 0.f);
+            if (t.stress[sid]) g.hs[f] = make_float2(0.f, 0.f);
+        }
     }
 }
 
@@ -877,73 +947,6 @@ __global__ void __launch_bounds__(128) km_hkt_gradients(MeshDev m, Ctrl *ctrl, M
 // (algebraically the reference's 1/2 (po + pn) - 1/2 g (wa ha^2 + wb hb^2)),
 // so a surface at rest gives exactly zero and FP32 carries only the small
 // differences.
-__global__ void __launch_bounds__(128) km_hkt_faces(MeshDev m, Ctrl *ctrl, MixedGeo g, TurbDev t, int stage)
-{
-    const int nf = m.nf, nc = m.nc;
-    const MxPrim *P = reinterpret_cast<const MxPrim *>(stage == 1 ? g.prim[0] : g.prim[1]);
-    FOR_ACTIVE_FACES(m.act, f) {
-        const int sid = m.face_sid[f];
-        if (!t.hkt[sid]) continue;
-        const Ctrl &ct = ctrl[sid];
-        if (mx_skip(ct, stage)) continue;
-        const float gravity = ct.gravf, dry = ct.dryf;
-        const int a = m.owner[f], b = m.neighbour[f];
-        float2 pr = make_float2(0.f, 0.f), st = make_float2(0.f, 0.f);
-        if (b >= 0) {
-            const MxPrim pa = P[a], pb = P[b];
-            if (pa.wet && pb.wet) {
-                const float2 nn = g.fnorm[f], di = g.fdist[f];
-                const float nx = nn.x, ny = nn.y, da = di.x, db = di.y, d = da + db, wa = db / d, wb = da / d;
-                const float zb = g.fdb[f];
-                const float ea = pa.h, eb = pa.h + ((pb.ehi - pa.ehi) + (pb.elo - pa.elo));
-                if (t.stress[sid]) {
-                    float h = fminf(pa.h, pb.h);
-                    h = fminf(h, fmaxf(0.f, .5f * (ea + eb) - fmaxf(0.f, zb)));
-                    const float visc = wa * float(t.nu[a]) + wb * float(t.nu[b]);
-                    const float2 dd = g.hcc[f];
-                    const float dn = dd.x * nx + dd.y * ny;
-                    const float du = pb.u - pa.u, dv = pb.v - pa.v;
-                    const float *G = g.hgrad;
-                    float ux = wa * G[a] + wb * G[b], uy = wa * G[nc + a] + wb * G[nc + b];
-                    float vx = wa * G[2 * nc + a] + wb * G[2 * nc + b], vy = wa * G[3 * nc + a] + wb * G[3 * nc + b];
-                    const float cu = (du - ux * dd.x - uy * dd.y) / dn, cv = (dv - vx * dd.x - vy * dd.y) / dn;
-                    ux += cu * nx; uy += cu * ny; vx += cv * nx; vy += cv * ny;
-                    st = make_float2(visc * h * (2.f * ux * nx + (uy + vx) * ny), visc * h * ((uy + vx) * nx + 2.f * vy * ny));
-                }
-                const float4 t0 = g.htr[f], t1 = g.htr[nf + f];
-                const int cf = __float_as_int(t0.w);
-                const float top = t0.z, bed = fmaxf(fmaxf(0.f, zb), top);
-                const float ha = fmaxf(0.f, ea - bed), hb = fmaxf(0.f, eb - bed);
-                const float hl = fmaxf(0.f, (top + t0.x) - bed), hr = fmaxf(0.f, (top + t0.y) - bed);
-                const float h = .5f * (hl + hr);
-                const float qg = .25f * gravity;
-                const float ca = (cf & 1) ? qg * __fmul_rn(ha - hl, ha + hl) : 0.f;
-                const float cb = (cf & 2) ? qg * __fmul_rn(hb - hr, hb + hr) : 0.f;
-                const float scale = qg * (hl * hl + hr * hr);                       // |po|, |pn| to first order
-                if (!(fminf(fminf(ha, hb), fminf(hl, hr)) <= dry) && !(fabsf(hr - hl) > .005f * h) &&
-                    !(fabsf(2.f * (ca - cb)) > 128.f * FEPS * fmaxf(1.f, scale))) {
-                    const float4 md = g.hmd[f];
-                    const float sx = wa * md.x + wb * md.z, sy = wa * md.y + wb * md.w;
-                    const float *G = g.hgrad;
-                    float delta = qg * (__fmul_rn(hl - ha, hl + ha) + __fmul_rn(hr - hb, hr + hb)) +
-                                  qg * ((da - db) / d) * __fmul_rn(ha - hb, ha + hb) + (ca + cb);
-                    delta -= gravity * sx * (wa * ha * G[4 * nc + a] + wb * hb * G[4 * nc + b]);
-                    delta -= gravity * sy * (wa * ha * G[5 * nc + a] + wb * hb * G[5 * nc + b]);
-                    // the actuator sink difference: FP64 rates, zero outside the rotor
-                    // support cells, so only faces touching one read and subtract them
-                    if (t.foot[a] | t.foot[b])
-                        delta -= da * db / d * (float(t.raw[a] - t.raw[b]) * nx + float(t.raw[nc + a] - t.raw[nc + b]) * ny);
-                    const float speed = sqrtf(gravity * h), theta = fminf(1.f, fmaxf(t1.z, t1.w) / speed);
-                    delta -= .5f * (1.f - theta) * speed * (2.f * hl * hr / (hl + hr)) * (t1.y - t1.x);
-                    pr = make_float2(delta * nx, delta * ny);
-                }
-            }
-        }
-        g.hp[f] = pr;
-        if (t.stress[sid]) g.hs[f] = st;
-    }
-}
-
 }  // namespace brx_mx
 
 // The boundary CTA of the mixed form is the FP64 kernel (few faces, FP64 sums).
@@ -964,7 +967,6 @@ int mixed_max_block(int kind, int maxdeg)
     case K_LIMIT: fn = (const void *)brx_mx::km_limit; break;
     case K_UPDATE: fn = (const void *)brx_mx::km_update; break;
     case K_HKT_GRAD: fn = (const void *)brx_mx::km_hkt_gradients; break;
-    case K_HKT_FACES: fn = (const void *)brx_mx::km_hkt_faces; break;
     default: return 0;
     }
     cudaFuncAttributes a;
@@ -1019,9 +1021,8 @@ int mixed_kernel(const Launch &L, int kind, int stage, double *out)
     case K_HKT_GRAD:
         brx_mx::km_hkt_gradients<<<SHAPE(K_HKT_GRAD, nc), 0, st>>>(L.mesh, L.ctrl, L.mx, L.turb, stage);
         return 1;
-    case K_HKT_FACES:
-        brx_mx::km_hkt_faces<<<SHAPE(K_HKT_FACES, nf), 0, st>>>(L.mesh, L.ctrl, L.mx, L.turb, stage);
-        return 1;
+    case K_HKT_FACES:       // fused into the face sweep's tail
+        return 0;
     }
 #undef SHAPE
     return 0;
