@@ -35,8 +35,8 @@ BYTES_PER_CELL_UPDATE = {"fp64": 680.0, "mixed": 384.0}   # algorithmic bytes, t
 # launch of each mixed-form sweep, from one ncu --set full capture of the
 # 24-scenario subset with rotors (scenarios 20..43, 1,967,962 cells, inputs
 # larger than L2): a launch of the full batch is scaled by its cells
-TRAFFIC_BYTES_PER_CELL = {"mixed": {"cells": 204.57, "faces": 194.97, "gather": 145.71, "update": 171.57,
-                                    "drag": 62.27}}
+TRAFFIC_BYTES_PER_CELL = {"mixed": {"cells": 204.54, "faces": 213.13, "gather": 145.74, "update": 171.42,
+                                    "drag": 62.03}}
 KERNEL_NAMES = ["drag", "boundary", "cells", "faces", "gather", "limit", "update", "control"]
 
 
@@ -146,19 +146,23 @@ def flush_l2(torch, buf):
     buf.fill_(1.0)            # 256 MiB write evicts the 129 MB L2
 
 
-def algorithmic_bytes(kernel, nc, nf, nadj, nslot, precision="fp64"):
+def algorithmic_bytes(kernel, nc, nf, nadj, nslot, precision="fp64", rotor_cells=0, rotor_faces=0):
     """Compulsory unique bytes one launch of each kernel reads and writes.
 
     Every array a kernel touches counts once per element (neighbour gathers
     that re-read a cell already counted are free), for the layout of the given
-    arithmetic form.
+    arithmetic form. rotor_cells / rotor_faces: cells and faces of scenarios
+    with rotor arrays, whose face terms the mixed face sweep forms in its tail.
     """
     i4, d8 = 4, 8
     if precision == "mixed":
         if kernel == "cells":    # state, bed, id, CSR, LS inverse, record out; per entry: index, geometry, weight
             return nc * (3 * d8 + d8 + i4 + i4 + 16 + 64) + nadj * (8 + 16 + 4)
-        if kernel == "faces":    # two records (each cell once), face ids/geometry, water/speed + 4 momentum out
-            return nc * 64 + nf * (2 * i4 + i4 + i4 + 8 + 16 + 8) + nf * (8 + 16)
+        if kernel == "faces":    # two records (each cell once), face ids/geometry, water/speed + 4 momentum out;
+            # rotor tail: two wet-gradient components and the support mask per cell, midpoint
+            # displacements in and the pressure correction out per face
+            return (nc * 64 + nf * (2 * i4 + i4 + i4 + 8 + 16 + 8) + nf * (8 + 16) +
+                    rotor_cells * (2 * 4 + 1) + rotor_faces * (16 + 8))
         if kernel == "gather":   # id, CSR, record flags, stock, rate/theta out; per entry weight; face fluxes
             return nc * (i4 + i4 + 4 + d8 + 3 * d8 + d8 + i4) + nadj * (i4 + d8) + nf * (8 + 16)
         if kernel == "limit":
@@ -401,7 +405,10 @@ def main():
         per_kind.setdefault(name, []).append(ms)
     dom = max(per_kind, key=lambda k: sum(per_kind[k]))
     dom_ms = float(np.mean(per_kind[dom]))
-    dom_bytes = algorithmic_bytes(dom, nc, nf, nadj, nslot, precision)
+    with_rotors = [i for i, c in enumerate(cases) if c.get("turbines")]
+    rotor_cells = sum(int(solver.packed["cell_offset"][i + 1] - solver.packed["cell_offset"][i]) for i in with_rotors)
+    rotor_faces = sum(int(solver.packed["face_offset"][i + 1] - solver.packed["face_offset"][i]) for i in with_rotors)
+    dom_bytes = algorithmic_bytes(dom, nc, nf, nadj, nslot, precision, rotor_cells, rotor_faces)
     peak, peak_kind = peaks()
     achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
     per_cell = TRAFFIC_BYTES_PER_CELL.get(precision, {}).get(dom)

@@ -1287,21 +1287,24 @@ __device__ void inlet_allocation(const MeshDev &m, const BoundaryDev &b, const C
 
 // The scenario's sum over its open faces of (outward water flux x length),
 // with each face's water as the update consumes it (the mixed form carries
-// it in FP32: F(flux)); per-thread strided sums added by thread 0 in thread
-// order. The controller turns the stage sums into the boundary ledger.
-constexpr int BOUNDARY_THREADS = 256;
+// it in FP32: F(flux)); per-thread strided sums, a butterfly within each
+// warp, then thread 0 adds the warp sums in warp order (a fixed order: the
+// same value on every run). The controller turns the stage sums into the
+// boundary ledger.
+constexpr int BOUNDARY_WARPS = 32;
 template <class F>
 __device__ void boundary_water(const MeshDev &m, const BoundaryDev &b, Ctrl &ct, int stage, int k0, int k1)
 {
-    __shared__ double part[BOUNDARY_THREADS];
+    __shared__ double part[BOUNDARY_WARPS];
     __syncthreads();
     double acc = 0.;
     for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) acc += double(F(b.flux[k])) * m.length[b.slot_face[k]];
-    if (threadIdx.x < BOUNDARY_THREADS) part[threadIdx.x] = acc;
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
     __syncthreads();
     if (threadIdx.x == 0) {
         double total = 0.;
-        for (int i = 0; i < (int)blockDim.x && i < BOUNDARY_THREADS; ++i) total += part[i];
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) total += part[i];
         ct.bflux[stage - 1] = total;
     }
 }
