@@ -438,7 +438,13 @@ __device__ __forceinline__ float hydro_perturbation(float dh, float hL, float h,
 // river_hydrokinetic_stress.h:13-35), from the cell records and the face's
 // hydrostatic traces t0 (hl, hr, common bed, constant flags) and t1 (un_l,
 // un_r, |u|_l, |u|_r): computed in the face sweep's tail, so the traces never
-// leave registers.
+// leave registers. Heights are relative to the owner's bed; the hydrostatic
+// part of the pressure correction is written in difference form,
+//   1/4 g [(hl-ha)(hl+ha) + (hr-hb)(hr+hb)] + 1/4 g (da-db)/d (ha-hb)(ha+hb)
+//   + 1/4 g [ca (ha-hl)(ha+hl) + cb (hb-hr)(hb+hr)]
+// (algebraically the reference's 1/2 (po + pn) - 1/2 g (wa ha^2 + wb hb^2)),
+// so a surface at rest gives exactly zero and FP32 carries only the small
+// differences.
 __device__ __forceinline__ void hkt_face_terms(const MxRec &pa, const MxRec &pb, float4 t0, float4 t1, int f, int a,
                                                int b, int sid, float gravity, float dry, const MixedGeo &g,
                                                const TurbDev &t, int nc, float2 &pr, float2 &st)
@@ -940,13 +946,6 @@ __global__ void __launch_bounds__(128) km_hkt_gradients(MeshDev m, Ctrl *ctrl, M
     }
 }
 
-// Heights relative to the owner's bed. The hydrostatic part of the pressure
-// correction is written in difference form,
-//   1/4 g [(hl-ha)(hl+ha) + (hr-hb)(hr+hb)] + 1/4 g (da-db)/d (ha-hb)(ha+hb)
-//   + 1/4 g [ca (ha-hl)(ha+hl) + cb (hb-hr)(hb+hr)]
-// (algebraically the reference's 1/2 (po + pn) - 1/2 g (wa ha^2 + wb hb^2)),
-// so a surface at rest gives exactly zero and FP32 carries only the small
-// differences.
 }  // namespace brx_mx
 
 // The boundary CTA of the mixed form is the FP64 kernel (few faces, FP64 sums).
