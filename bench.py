@@ -156,11 +156,14 @@ def algorithmic_bytes(kernel, nc, nf, nadj, nslot, precision="fp64", rotor_cells
     """
     i4, d8 = 4, 8
     if precision == "mixed":
-        if kernel == "cells":    # state, bed, id, CSR, LS inverse, record out; per entry: index, geometry, weight
-            return nc * (3 * d8 + d8 + i4 + i4 + 16 + 64) + nadj * (8 + 16 + 4)
+        if kernel == "cells":    # state, bed, id, CSR, LS inverse, record out; per entry: index, geometry, weight;
+            # rotor tail: wet gradients out (6 floats) per cell, flow-metric offsets per entry
+            return (nc * (3 * d8 + d8 + i4 + i4 + 16 + 64) + nadj * (8 + 16 + 4) +
+                    rotor_cells * (6 * 4 + 3 * 8))
         if kernel == "faces":    # two records (each cell once), face ids/geometry, water/speed + 4 momentum out;
             # rotor tail: two wet-gradient components and the support mask per cell, midpoint
-            # displacements in and the pressure correction out per face
+            # displacements in and the pressure correction out per face (rotor_cells x 3 CSR entries
+            # in the cell sweep above: triangles)
             return (nc * 64 + nf * (2 * i4 + i4 + i4 + 8 + 16 + 8) + nf * (8 + 16) +
                     rotor_cells * (2 * 4 + 1) + rotor_faces * (16 + 8))
         if kernel == "gather":   # id, CSR, record flags, stock, rate/theta out; per entry weight; face fluxes

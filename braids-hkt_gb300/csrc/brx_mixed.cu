@@ -234,9 +234,40 @@ __global__ void __launch_bounds__(128) km_bed(MeshDev m, StateDev s, MixedGeo g)
 #define BRX_CELLS_MIN_BLOCKS 8
 #endif
 
+// Wet least-squares gradients of u, v and the surface for the rotor face
+// terms (river_turbine_flow.h:13-35): wet neighbours only, weights 1/|d|^2 of
+// the flow metric's centre offsets. Called in the cell sweep's tail, after
+// the cell record is written, so its sums are not live in the limiter; the
+// neighbour primitives were just read and come from L1.
+__device__ __forceinline__ void hkt_cell_gradients(const MeshDev &m, const MixedGeo &g, const MxPrim *P,
+                                                   const MxPrim &pc, int c, int nc)
+{
+    float xx = 0.f, xy = 0.f, yy = 0.f, bx[3] = {0.f, 0.f, 0.f}, by[3] = {0.f, 0.f, 0.f};
+    if (pc.wet)
+        for (int k = m.offset[c]; k < m.offset[c + 1]; ++k) {
+            const int n = g.cidx[k].x;
+            if (n < 0) continue;
+            const MxPrim pn = P[n];
+            if (!pn.wet) continue;
+            const float2 d = g.hdxy[k];
+            const float w = 1.f / (d.x * d.x + d.y * d.y);
+            xx += w * d.x * d.x; xy += w * d.x * d.y; yy += w * d.y * d.y;
+            const float dv[3] = {pn.u - pc.u, pn.v - pc.v, (pn.ehi - pc.ehi) + (pn.elo - pc.elo)};
+#pragma unroll
+            for (int p = 0; p < 3; ++p) { bx[p] += w * d.x * dv[p]; by[p] += w * d.y * dv[p]; }
+        }
+    const float det = xx * yy - xy * xy;
+    const bool solve = det > 1e-6f * fmaxf(1.f, xx * yy);
+#pragma unroll
+    for (int p = 0; p < 3; ++p) {
+        g.hgrad[(2 * p) * nc + c] = solve ? (yy * bx[p] - xy * by[p]) / det : 0.f;
+        g.hgrad[(2 * p + 1) * nc + c] = solve ? (xx * by[p] - xy * bx[p]) / det : 0.f;
+    }
+}
+
 template <int MAXF>
 __global__ void __launch_bounds__(128, BRX_CELLS_MIN_BLOCKS) km_cells(MeshDev m, StateDev s, Ctrl *ctrl, Work w,
-                                                                      MixedGeo g, int stage)
+                                                                      MixedGeo g, int stage, TurbDev t, int turb)
 {
     const int nc = m.nc;
     MxRec *rec = reinterpret_cast<MxRec *>(w.rec);
@@ -385,6 +416,7 @@ __global__ void __launch_bounds__(128, BRX_CELLS_MIN_BLOCKS) km_cells(MeshDev m,
         for (int p = 0; p < 4; ++p) { r.gx[p] = gx[p]; r.gy[p] = gy[p]; }
         r.pad0 = 0.f; r.pad1 = 0.f;
         rec[c] = r;
+        if (turb && t.hkt[m.cell_sid[c]]) hkt_cell_gradients(m, g, P, pc, c, nc);
     }
 }
 
@@ -908,44 +940,6 @@ __global__ void km_water_out(MeshDev m, Work w, double *water)
     for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < m.nf; f += gridDim.x * blockDim.x) water[f] = lim[f].water;
 }
 
-// ---------------------------------------------------------------------------
-// Rotor arrays in the mixed form: FP32 wet gradients and face terms
-// (river_turbine_flow.h:13-82, river_hydrokinetic_stress.h:13-35)
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) km_hkt_gradients(MeshDev m, Ctrl *ctrl, MixedGeo g, TurbDev t, int stage)
-{
-    const int nc = m.nc;
-    const MxPrim *P = reinterpret_cast<const MxPrim *>(stage == 1 ? g.prim[0] : g.prim[1]);
-    FOR_ACTIVE_CELLS(m.act, c) {
-        const int sid = m.cell_sid[c];
-        if (!t.hkt[sid]) continue;
-        const Ctrl &ct = ctrl[sid];
-        if (mx_skip(ct, stage)) continue;
-        const MxPrim pc = P[c];
-        float xx = 0.f, xy = 0.f, yy = 0.f, bx[3] = {0.f, 0.f, 0.f}, by[3] = {0.f, 0.f, 0.f};
-        if (pc.wet)
-            for (int k = m.offset[c]; k < m.offset[c + 1]; ++k) {
-                const int n = g.cidx[k].x;
-                if (n < 0) continue;
-                const MxPrim pn = P[n];
-                if (!pn.wet) continue;
-                const float2 d = g.hdxy[k];
-                const float w = 1.f / (d.x * d.x + d.y * d.y);
-                xx += w * d.x * d.x; xy += w * d.x * d.y; yy += w * d.y * d.y;
-                const float dv[3] = {pn.u - pc.u, pn.v - pc.v, (pn.ehi - pc.ehi) + (pn.elo - pc.elo)};
-#pragma unroll
-                for (int p = 0; p < 3; ++p) { bx[p] += w * d.x * dv[p]; by[p] += w * d.y * dv[p]; }
-            }
-        const float det = xx * yy - xy * xy;
-        const bool solve = det > 1e-6f * fmaxf(1.f, xx * yy);
-#pragma unroll
-        for (int p = 0; p < 3; ++p) {
-            g.hgrad[(2 * p) * nc + c] = solve ? (yy * bx[p] - xy * by[p]) / det : 0.f;
-            g.hgrad[(2 * p + 1) * nc + c] = solve ? (xx * by[p] - xy * bx[p]) / det : 0.f;
-        }
-    }
-}
-
 }  // namespace brx_mx
 
 // The boundary CTA of the mixed form is the FP64 kernel (few faces, FP64 sums).
@@ -965,7 +959,6 @@ int mixed_max_block(int kind, int maxdeg)
     case K_GATHER: fn = (const void *)brx_mx::km_gather; break;
     case K_LIMIT: fn = (const void *)brx_mx::km_limit; break;
     case K_UPDATE: fn = (const void *)brx_mx::km_update; break;
-    case K_HKT_GRAD: fn = (const void *)brx_mx::km_hkt_gradients; break;
     default: return 0;
     }
     cudaFuncAttributes a;
@@ -988,8 +981,12 @@ int mixed_kernel(const Launch &L, int kind, int stage, double *out)
         brx_mixb::k_boundary<float><<<L.nscen, 256, 0, st>>>(L.mesh, L.state, L.bnd, L.ctrl, stage);
         return 1;
     case K_CELLS:
-        if (small) brx_mx::km_cells<4><<<SHAPE(K_CELLS, nc), 0, st>>>(L.mesh, L.state, L.ctrl, L.work, L.mx, stage);
-        else brx_mx::km_cells<MAX_CELL_FACES><<<SHAPE(K_CELLS, nc), 0, st>>>(L.mesh, L.state, L.ctrl, L.work, L.mx, stage);
+        if (small)
+            brx_mx::km_cells<4><<<SHAPE(K_CELLS, nc), 0, st>>>(L.mesh, L.state, L.ctrl, L.work, L.mx, stage, L.turb,
+                                                              L.has_turb);
+        else
+            brx_mx::km_cells<MAX_CELL_FACES><<<SHAPE(K_CELLS, nc), 0, st>>>(L.mesh, L.state, L.ctrl, L.work, L.mx,
+                                                                            stage, L.turb, L.has_turb);
         return 1;
     case K_FACES:
         brx_mx::km_faces<<<SHAPE(K_FACES, nf), 0, st>>>(L.mesh, L.state, L.bnd, L.ctrl, L.work, L.mx, stage, L.turb,
@@ -1017,9 +1014,8 @@ int mixed_kernel(const Launch &L, int kind, int stage, double *out)
     case K_WATER:
         brx_mx::km_water_out<<<L.grid_f256, 256, 0, st>>>(L.mesh, L.work, out);
         return 1;
-    case K_HKT_GRAD:
-        brx_mx::km_hkt_gradients<<<SHAPE(K_HKT_GRAD, nc), 0, st>>>(L.mesh, L.ctrl, L.mx, L.turb, stage);
-        return 1;
+    case K_HKT_GRAD:        // fused into the cell sweep's tail
+        return 0;
     case K_HKT_FACES:       // fused into the face sweep's tail
         return 0;
     }
