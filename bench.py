@@ -35,8 +35,8 @@ BYTES_PER_CELL_UPDATE = {"fp64": 680.0, "mixed": 384.0}   # algorithmic bytes, t
 # launch of each mixed-form sweep, from one ncu --set full capture of the
 # 24-scenario subset with rotors (scenarios 20..43, 1,967,962 cells, inputs
 # larger than L2): a launch of the full batch is scaled by its cells
-TRAFFIC_BYTES_PER_CELL = {"mixed": {"cells": 204.54, "faces": 213.13, "gather": 145.74, "update": 171.42,
-                                    "drag": 62.03}}
+TRAFFIC_BYTES_PER_CELL = {"mixed": {"cells": 244.24, "faces": 213.26, "gather": 145.79, "update": 171.48,
+                                    "drag": 62.05, "limit": 46.90}}
 KERNEL_NAMES = ["drag", "boundary", "cells", "faces", "gather", "limit", "update", "control"]
 
 
