@@ -527,7 +527,12 @@ __device__ __forceinline__ void hkt_face_terms(const MxRec &pa, const MxRec &pb,
     }
 }
 
-__global__ void __launch_bounds__(128, 8) km_faces(MeshDev m, StateDev s, BoundaryDev b, Ctrl *ctrl, Work w,
+// resident blocks per SM the register allocation of the face sweep is fitted to
+#ifndef BRX_FACES_MIN_BLOCKS
+#define BRX_FACES_MIN_BLOCKS 8
+#endif
+
+__global__ void __launch_bounds__(128, BRX_FACES_MIN_BLOCKS) km_faces(MeshDev m, StateDev s, BoundaryDev b, Ctrl *ctrl, Work w,
                                                 MixedGeo g, int stage, TurbDev t, int turb)
 {
     const int nf = m.nf, nc = m.nc;
