@@ -243,7 +243,7 @@ def cpu_baseline(cases, outer, seconds=10.0, threads=None):
         updates += stats["substeps"] * nc
         sim += interval
     el = time.perf_counter() - t0
-    return {"value": updates / el, "unit": METRIC, "cores": threads, "kind": "port",
+    return {"value": updates / el, "unit": METRIC, "cores": threads, "kind": "port", "seconds": el,
             "sample": f"{cases[0].get('name', 'case')}: {sim:g} s simulated ({updates} cell-updates) "
                       f"from the initial state, oracle port with OpenMP on {threads} threads"}
 
@@ -263,7 +263,8 @@ def reference_arm(args):
         per_step.append(cpu_baseline(cases, outer, seconds=max(5.0, 60.0 / max(args.steps, 1)), threads=threads))
     value = float(np.mean([p["value"] for p in per_step]))
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "ms_per_step": float(np.mean([p["seconds"] for p in per_step])) * 1e3,
+            "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg, "impl": "reference",
             "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
                              "sample": per_step[-1]["sample"]},
@@ -571,6 +572,7 @@ def main():
     if not args.no_cpu_baseline:
         median = sorted(cases, key=lambda c: c["mesh"].nc)[len(cases) // 2]
         line["cpu_baseline"] = cpu_baseline([median], outer)
+        line["cpu_baseline"].pop("seconds", None)
     print(json.dumps(line), flush=True)
 
 
