@@ -143,3 +143,38 @@ def test_normal_line_carries_the_discharge(discharge):
     chezy = (area / perimeter) ** (1.0 / 6.0) / n
     rate = area * np.sqrt(area * slope / (sum(per) / chezy ** 2))
     assert abs(rate / discharge - 1.0) <= 1e-9
+
+
+def test_section_neighbours_follow_the_reference_rules():
+    """NormalSection's adjacency (river_exterior_normal.py:11-27): faces of a
+    straight section sorted by station, neighbours where the facing ends
+    meet; a section that is not one straight, consistently oriented line is
+    refused."""
+    from braids_hkt_gb300.mesh import section_neighbours
+    case = S.normal_inlet_channel()
+    m = case["mesh"]
+    left, right = section_neighbours(m, 0)
+    ids = np.flatnonzero((m.neighbour < 0) & (m.bid == 0))
+    assert np.sum(left[ids] < 0) == 1 and np.sum(right[ids] < 0) == 1      # one bank at each end
+    for f in ids:
+        if right[f] >= 0:
+            assert left[right[f]] == f
+    bent = S.normal_inlet_channel()
+    mb = bent["mesh"]
+    g = np.flatnonzero((mb.neighbour < 0) & (mb.bid == 0))[0]
+    mb.normal = mb.normal.copy()
+    mb.normal[:, g] = [np.sqrt(0.5), np.sqrt(0.5)]
+    with pytest.raises(ValueError):
+        section_neighbours(mb, 0)
+
+
+def test_inlet_line_host_validation():
+    from braids_hkt_gb300.solver import inlet_lines
+    case = S.normal_inlet_channel()
+    case["inlet"] = {0: {"line": "normal", "energy_slope": 0.0}}
+    with pytest.raises(ValueError):
+        inlet_lines([case])
+    case = S.small_channel()
+    case["inlet"] = {1: {"line": "critical"}}                  # segment 1 is a stage outlet
+    with pytest.raises(ValueError):
+        inlet_lines([case])
