@@ -909,7 +909,11 @@ __global__ void __launch_bounds__(256) km_update(MeshDev m, StateDev s, Ctrl *ct
     }
 }
 
-// First drag half-step: work = drag(accepted, trial/2), and the first stage's primitives.
+// First drag half-step: work = drag(accepted, trial/2), and the first stage's
+// primitives. The drag factor scales the FP64 momenta; the FP32 velocities
+// of the primitives are the FP32 momenta times the same factor over the
+// depth, so the scaled FP64 momenta are not converted back (two fewer FP64-
+// pipe conversions per cell in this FP64-pipe-bound sweep).
 __global__ void __launch_bounds__(256) km_open_drag(MeshDev m, StateDev s, Ctrl *ctrl, MixedGeo g)
 {
     const int nc = m.nc;
@@ -918,10 +922,35 @@ __global__ void __launch_bounds__(256) km_open_drag(MeshDev m, StateDev s, Ctrl 
         Ctrl &ct = ctrl[m.cell_sid[c]];
         if (!ct.active || ct.done) continue;
         const double *q = ct.cur ? s.q[1] : s.q[0];
-        double h = q[c], hu = q[nc + c], hv = q[2 * nc + c];
-        drag_f(ct, .5f * ct.trialf, h, hu, hv);
+        const double h = q[c], z = s.z[c];
+        double hu = q[nc + c], hv = q[2 * nc + c];
+        const bool wet = !le_threshold(h, ct.dry);
+        const float hf = float(h);
+        float uf = 0.f, vf = 0.f;
+        if (!wet) { hu = 0.; hv = 0.; }
+        else {
+            const float mu = float(hu), mv = float(hv);
+            float cz;
+            const float val = ct.roughf;
+            if (ct.roughness_mode == 1) cz = val;
+            else if (ct.roughness_mode == 2) cz = powf(hf, 1.f / 6.f) / val;
+            else if (ct.roughness_mode == 3) cz = sqrtf(9.81f) / .41f * log1pf(30.f * hf / (2.718281828459045f * val));
+            else cz = 18.f * log10f(12.f * fmaxf(.5f, hf / val));
+            const float speed = sqrtf(mu * mu + mv * mv) / hf;
+            const float factor = 1.f / (1.f + .5f * ct.trialf * ct.gravf * speed / (cz * cz * hf));
+            const double fd = double(factor);
+            hu *= fd; hv *= fd;
+            uf = mu * factor / hf; vf = mv * factor / hf;
+        }
         s.work[c] = h; s.work[nc + c] = hu; s.work[2 * nc + c] = hv;
-        if (!put_prim(P1, c, h, hu, hv, s.z[c], ct.dry)) raise_status(ct, 1, ST_SPATIAL);
+        const double eta = h + z;
+        MxPrim p;
+        p.ehi = float(eta);
+        p.elo = float(eta - double(p.ehi));
+        p.h = hf; p.u = uf; p.v = vf; p.wet = wet;
+        p.pad0 = 0.f; p.pad1 = 0.f;
+        P1[c] = p;
+        if (!(!(h < 0.0) && finite64(h) && finite64(hu) && finite64(hv) && finite64(z))) raise_status(ct, 1, ST_SPATIAL);
     }
 }
 
