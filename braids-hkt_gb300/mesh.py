@@ -167,6 +167,68 @@ def build_mesh(points, tri, segment_of_edge):
                 boundary_offset=np.asarray(boff, dtype=np.int32), boundary_faces=boundary_faces)
 
 
+def cartesian_mesh(length, width, spacing):
+    """Face/CSR topology of a Cartesian quadrilateral channel mesh.
+
+    Square cells of side ``spacing`` over [0, length] x [0, width]; the left
+    edge is open segment 0, the right edge open segment 1, the long sides are
+    walls. Cells are Morton sorted; faces are numbered by first visit over
+    the sorted cells, each cell's edges in counter-clockwise order (bottom,
+    right, top, left), owner = the first visitor with its outward normal.
+    The same records a cut-cell or quadtree exporter hands over for its
+    uncut cells (four faces per cell instead of three).
+    """
+    nx, ny = int(round(length / spacing)), int(round(width / spacing))
+    if nx < 1 or ny < 1:
+        raise ValueError("channel smaller than one cell")
+    dx, dy = length / nx, width / ny
+    I, J = np.meshgrid(np.arange(nx), np.arange(ny), indexing="ij")
+    I, J = I.ravel(), J.ravel()
+    cx, cy = (I + 0.5) * dx, (J + 0.5) * dy
+    order = morton_order(cx, cy)
+    I, J, cx, cy = I[order], J[order], cx[order], cy[order]
+    nc = nx * ny
+    cell_of = np.full((nx, ny), -1, dtype=np.int64)
+    cell_of[I, J] = np.arange(nc)
+    # local edges: (di, dj) of the other cell, outward normal, midpoint offset, length
+    local = [((0, -1), (0.0, -1.0), (0.0, -0.5 * dy), dx), ((1, 0), (1.0, 0.0), (0.5 * dx, 0.0), dy),
+             ((0, 1), (0.0, 1.0), (0.0, 0.5 * dy), dx), ((-1, 0), (-1.0, 0.0), (-0.5 * dx, 0.0), dy)]
+    face_id = {}
+    owner, neighbour, normal, mid, flen, bid = [], [], [], [], [], []
+    faces = np.empty(4 * nc, dtype=np.int32)
+    signs = np.empty(4 * nc, dtype=np.int32)
+    for c in range(nc):
+        i, j = int(I[c]), int(J[c])
+        for e, ((di, dj), nrm, moff, ln) in enumerate(local):
+            key = (2 * i + 1 + di, 2 * j + 1 + dj)            # edge midpoint on the doubled grid
+            if key not in face_id:
+                oi, oj = i + di, j + dj
+                other = int(cell_of[oi, oj]) if 0 <= oi < nx and 0 <= oj < ny else -1
+                face_id[key] = len(owner)
+                owner.append(c); neighbour.append(other); normal.append(nrm)
+                mid.append((cx[c] + moff[0], cy[c] + moff[1])); flen.append(ln)
+                bid.append(-1 if other >= 0 or dj != 0 else (0 if di < 0 else 1))
+            f = face_id[key]
+            faces[4 * c + e] = f
+            signs[4 * c + e] = 1 if owner[f] == c else -1
+    owner = np.asarray(owner, dtype=np.int32)
+    neighbour = np.asarray(neighbour, dtype=np.int32)
+    bid = np.asarray(bid, dtype=np.int32)
+    mid = np.ascontiguousarray(np.asarray(mid).T)
+    bfaces, boff = [], [0]
+    for sgm in range(2):
+        ids = np.flatnonzero(bid == sgm)
+        ids = ids[np.argsort(mid[1, ids], kind="stable")]
+        bfaces.append(ids)
+        boff.append(boff[-1] + len(ids))
+    return Mesh(points=np.zeros((0, 2)), tri=np.zeros((0, 3), np.int32), owner=owner, neighbour=neighbour, bid=bid,
+                normal=np.ascontiguousarray(np.asarray(normal).T), length=np.asarray(flen, dtype=np.float64),
+                mid=mid, area=np.full(nc, dx * dy), xy=np.ascontiguousarray(np.stack((cx, cy))),
+                offset=(4 * np.arange(nc + 1)).astype(np.int32), faces=faces, signs=signs,
+                boundary_offset=np.asarray(boff, dtype=np.int32),
+                boundary_faces=np.concatenate(bfaces).astype(np.int32))
+
+
 def opening_chains(mesh: Mesh, segment: int):
     """Ordered face chains of one open segment (connected runs of its faces).
 
@@ -279,6 +341,53 @@ def geometry_records(mesh: Mesh):
                distance=np.ascontiguousarray(distance))
     mesh.records.update(rec)
     return rec
+
+
+RECORD_KEYS = ("owner", "neighbour", "bid", "normal", "length", "mid", "area", "xy", "offset", "faces", "signs",
+               "boundary_offset", "boundary_faces", "ls_matrix", "ls_weight", "ls_delta", "displacement", "distance")
+
+
+def mesh_from_records(d, points=None, tri=None):
+    """A Mesh over a reference owner's geometry records.
+
+    ``d`` holds the arrays the reference's flow owner reads from its records
+    (river_mesh_records.initialize, the geometry cache ``g``): owner,
+    neighbour, bid, normal (2,nf), length, mid (2,nf), area, xy (2,nc), the
+    CSR offset / faces / signs, boundary_offset / boundary_faces, ls_matrix
+    (4,nc), ls_weight, ls_delta (2,nadj), displacement (2,2,nf), distance
+    (2,nf). Cells may be any polygons (cut cells, quadtree); no geometry is
+    recomputed, so the solver sees the reference's own bits. Rotor arrays
+    need the cell polygons as triangles (points, tri); without them a case
+    takes no rotors.
+    """
+    missing = [k for k in RECORD_KEYS if k not in d]
+    if missing:
+        raise ValueError(f"records lack {missing}")
+    i32 = lambda a: np.ascontiguousarray(a, dtype=np.int32)
+    f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+    nc, nf = len(d["area"]), len(d["owner"])
+    if len(d["offset"]) != nc + 1 or np.asarray(d["normal"]).shape != (2, nf) or np.asarray(d["xy"]).shape != (2, nc):
+        raise ValueError("records have inconsistent sizes")
+    disp = f64(d["displacement"])
+    mesh = Mesh(points=np.zeros((0, 2)) if points is None else f64(points),
+                tri=np.zeros((0, 3), np.int64) if tri is None else np.asarray(tri, dtype=np.int64),
+                owner=i32(d["owner"]), neighbour=i32(d["neighbour"]), bid=i32(d["bid"]), normal=f64(d["normal"]),
+                length=f64(d["length"]), mid=f64(d["mid"]), area=f64(d["area"]), xy=f64(d["xy"]),
+                offset=i32(d["offset"]), faces=i32(d["faces"]), signs=i32(d["signs"]),
+                boundary_offset=i32(d["boundary_offset"]), boundary_faces=i32(d["boundary_faces"]))
+    mesh.records = dict(ls_matrix=f64(d["ls_matrix"]), ls_weight=f64(d["ls_weight"]), ls_delta=f64(d["ls_delta"]),
+                        disp=disp, disp_len=np.ascontiguousarray(np.hypot(disp[0], disp[1])),
+                        distance=f64(d["distance"]))
+    return mesh
+
+
+def records_of(mesh: Mesh):
+    """The records dict of a Mesh under the reference's key names (the inverse of mesh_from_records)."""
+    r = mesh.records
+    d = {k: getattr(mesh, k) for k in RECORD_KEYS[:13]}
+    d.update(ls_matrix=r["ls_matrix"], ls_weight=r["ls_weight"], ls_delta=r["ls_delta"], displacement=r["disp"],
+             distance=r["distance"])
+    return d
 
 
 # ---------------------------------------------------------------------------

@@ -277,6 +277,27 @@ def normal_channel(discharge=20.0, bed_slope=2e-3, **kw):
     return case
 
 
+def cartesian_channel(length=120.0, width=24.0, spacing=3.0, seed=7, sigma=0.15, corr=8.0, discharge=20.0,
+                      stage=3.0, outlet_bed=-1.0, slope=2e-3, cfl=0.9):
+    """The small channel on Cartesian square cells (four faces per cell, the
+    shape of the reference's uncut Cartesian cells): sloped bed plus a
+    Gaussian field, total-discharge inlet, stage outlet, lake at rest at
+    `stage` initially."""
+    mesh = M.cartesian_mesh(length, width, spacing)
+    M.geometry_records(mesh)
+    rng = np.random.default_rng(seed + 1000003)
+    x, y = mesh.xy
+    z = outlet_bed + slope * (length - x)
+    if sigma > 0:
+        z = z + M.sample_field(M.gaussian_field(length, width, sigma, corr, rng, 0.5), x, y)
+    z = np.ascontiguousarray(np.where(x > length - 3 * spacing, outlet_bed, z))
+    h = np.maximum(stage - z, 0.0)
+    q = np.ascontiguousarray(np.stack((h, np.zeros_like(h), np.zeros_like(h))))
+    return dict(mesh=mesh, z=z, q=q, seg_mode=np.array([M.MODE_TOTAL_Q, M.MODE_STAGE], np.int32),
+                stage_policy=np.zeros(2, np.int32), forcing=np.array([[discharge, 0.0], [0.0, stage]]),
+                exterior_bed=_exterior_bed(mesh, z), controls=controls(cfl, 0.03), name="cartesian_channel")
+
+
 def stage_discharge_channel(discharge=20.0, reference_stage=3.05, **kw):
     """The small channel fed through an exact-discharge inlet (mode 9): the
     inflow `discharge` is imposed exactly through boundary Riemann solutions
