@@ -39,3 +39,14 @@ def test_channel_water_budget():
     ledger = -5.0 * float(np.sum(water[openf] * m.length[openf]))
     v1 = float(np.sum(q[0] * m.area))
     assert abs((v1 - v0) - ledger) <= max(1e-10, 64 * np.finfo(float).eps * max(v0, v1))
+
+
+def test_hllc_lake_at_rest_holds():
+    case = S.cartesian_channel()
+    case["forcing"] = np.array([[0.0, 0.0], [0.0, 3.0]])
+    q = case["q"].copy()
+    st, _, _ = Oracle(case, threads=2).hllc_advance(q, 3.0, 0.0)
+    assert st == 0
+    wet = q[0] > 1e-6
+    assert np.ptp((q[0] + case["z"])[wet]) <= 1e-12
+    assert np.abs(q[1:]).max() <= 1e-12
