@@ -41,6 +41,7 @@ CASES = {
                               0.01, 1.0),
     "critical_inlet": (S.critical_inlet_channel, lambda c: S.perturbed_state(c, 13, 0.2, 0.4, 0.0), 0.01, 1.0),
     "normal_inlet": (S.normal_inlet_channel, lambda c: S.perturbed_state(c, 14, 0.2, 0.4, 0.0), 0.01, 1.0),
+    "cartesian_channel": (S.cartesian_channel, lambda c: S.perturbed_state(c, 15, 0.3, 0.5, 0.1), 0.01, 1.0),
 }
 
 
