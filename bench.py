@@ -191,6 +191,18 @@ def algorithmic_bytes(kernel, nc, nf, nadj, nslot, precision="fp64", rotor_cells
     return 0
 
 
+def fma_peaks(lib):
+    """Measured FMA throughput of this GPU (brx_fma_rate): the compute
+    roofline of the FP64 form and of the FP32 sweeps, TFLOP/s."""
+    import ctypes as C
+    out = {}
+    for name, prec in (("fp64_tflops", 0), ("fp32_tflops", 1)):
+        t, ms = C.c_double(0.0), C.c_double(0.0)
+        if lib.brx_fma_rate(prec, C.byref(t), C.byref(ms)) == 0:
+            out[name] = t.value
+    return out
+
+
 def serving_session(cases, precision, rate=20.0, window=4.0, duration=5.0, interval=2.5, budget=150e9, seed=5):
     """Config 5, scaled: Poisson arrivals of requests drawn from the config-4
     scenario pool (mesh and rotor layout from the pool, discharge U(100, 1500)),
@@ -556,6 +568,8 @@ def main():
                            "what": "device time of one outer interval of the whole batch"},
             "e2e": {"value": e2e_updates / e2e_s, "unit": METRIC, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": h2d}}
+    line["compute_peaks"] = dict(fma_peaks(solver.lib), source="brx_fma_rate: 8 independent FMA chains per "
+                                 "thread at full occupancy, CUDA events, best of 5")
     if plain is not None:
         line["plain_fp64"] = plain
         line["batched_vs_plain_fp64"] = value / plain["value"]

@@ -46,6 +46,7 @@ SIGNATURES = {
     "brx_inlet_lines_set": (I, [P, P, P, P, P]),
     "brx_forcing_get": (I, [P, P]),
     "brx_ledger_get": (I, [P, P]),
+    "brx_ledger_gross_get": (I, [P, P]),
     "brx_hllc_set": (I, [P, P, P, P, P]),
     "brx_method_set": (I, [P, I]),
     "brx_launch_shape_set": (I, [P, I, I, I]),
@@ -54,6 +55,7 @@ SIGNATURES = {
     "brx_hint_set": (I, [P, P]),
     "brx_graph_chunk_set": (I, [P, I]),
     "brx_profile_substep": (I, [P, D, D, I, P, P, P]),
+    "brx_fma_rate": (I, [I, P, P]),
     "brx_rate_noalloc": (I, [I, I, I, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P, D, D, D, D, P, P, P, P,
                              P]),
     "brx_launch_count": (C.c_longlong, [P]),

@@ -8,6 +8,7 @@
 // launch sequence whose clock lives in device memory, captured once into a
 // CUDA graph of `chunk` substeps and replayed until every scenario reports
 // done. The host reads the control blocks back once per replay.
+#include <cuda.h>             // driver types for the context query of the allocation-free entry
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cmath>
@@ -1141,6 +1142,14 @@ extern "C" int brx_ledger_get(brx_solver *s, double *out)
     return BRX_OK;
 }
 
+extern "C" int brx_ledger_gross_get(brx_solver *s, double *out)
+{
+    if (!s || !out) return fail(BRX_ERR_ARGUMENT, "null argument");
+    if (s->pending) return fail(BRX_ERR_STATE, "an asynchronous interval is in flight");
+    for (int i = 0; i < s->nscen; ++i) out[i] = s->h_ctrl[i].gross;
+    return BRX_OK;
+}
+
 extern "C" int brx_hint_set(brx_solver *s, const double *hint)
 {
     if (!s || !hint) return fail(BRX_ERR_ARGUMENT, "null argument");
@@ -1382,6 +1391,7 @@ static void begin_interval_each(brx_solver *s, const double *dt_each, const doub
         c.substeps = c.rejections = c.done = c.failed = c.cur = 0;
         c.min_dt = c.max_dt = c.cfl_max = 0.0;
         c.bflux[0] = c.bflux[1] = c.ledger = 0.0;
+        c.bgross[0] = c.bgross[1] = c.gross = 0.0;
         c.one_stage = s->method == BRX_METHOD_HLLC;
         c.done = !c.active;
         host_set_trial(c);
@@ -1676,6 +1686,75 @@ extern "C" int brx_profile_substep(brx_solver *s, double dt, double time, int ca
 }
 
 // ---------------------------------------------------------------------------
+// FMA throughput probe (no counterpart in the reference): the compute
+// roofline of the FP64 form and of the FP32 sweeps. Every thread runs eight
+// independent FMA chains with the grid at full occupancy, so issue rate,
+// not latency, bounds the loop. Measured with CUDA events on its own stream.
+// ---------------------------------------------------------------------------
+static __device__ double g_fma_sink[2];
+
+template <class T>
+__device__ __forceinline__ T fma_probe_rn(T a, T b, T c);
+template <>
+__device__ __forceinline__ double fma_probe_rn<double>(double a, double b, double c) { return __fma_rn(a, b, c); }
+template <>
+__device__ __forceinline__ float fma_probe_rn<float>(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+
+template <class T>
+__global__ void __launch_bounds__(256) k_fma_probe(int iters, T seed, int slot)
+{
+    T a[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) a[j] = seed + T(threadIdx.x + j);
+    const T b = T(0.999999), c = T(1e-7);
+#pragma unroll 4
+    for (int i = 0; i < iters; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) a[j] = fma_probe_rn<T>(a[j], b, c);
+    T sum = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) sum += a[j];
+    if (sum == T(-1.2345)) g_fma_sink[slot] = double(sum);    // never true: keeps the chains live
+}
+
+extern "C" int brx_fma_rate(int precision, double *tflops, double *ms_out)
+{
+    if (!tflops || (precision != 0 && precision != 1)) return fail(BRX_ERR_ARGUMENT, "precision 0 (FP64) or 1 (FP32)");
+    int dev = 0, sms = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int blocks = sms * 8, threads = 256;
+    const int iters = precision == 0 ? 1 << 12 : 1 << 16;
+    cudaStream_t st;
+    CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 0.f;
+    for (int rep = 0; rep < 6; ++rep) {
+        cudaEventRecord(e0, st);
+        if (precision == 0) k_fma_probe<double><<<blocks, threads, 0, st>>>(iters, 1.0, 0);
+        else k_fma_probe<float><<<blocks, threads, 0, st>>>(iters, 1.f, 1);
+        cudaEventRecord(e1, st);
+        cudaError_t e = cudaEventSynchronize(e1);
+        if (e != cudaSuccess) {
+            cudaEventDestroy(e0); cudaEventDestroy(e1); cudaStreamDestroy(st);
+            return fail(BRX_ERR_CUDA, std::string("FMA probe: ") + cudaGetErrorString(e));
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && (best == 0.f || ms < best)) best = ms;      // the first launch warms up
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaStreamDestroy(st);
+    const double flops = 2.0 * 8.0 * double(iters) * double(blocks) * double(threads);
+    *tflops = flops / (double(best) * 1e-3) / 1e12;
+    if (ms_out) *ms_out = best;
+    return BRX_OK;
+}
+
+// ---------------------------------------------------------------------------
 // Allocation-free residual: brx_rate_noalloc
 //
 // For callers that may not allocate device memory once they are running:
@@ -1710,22 +1789,53 @@ constexpr size_t NOALLOC_BYTES = NA_ACT + noalloc_align(sizeof(int) * 16);   // 
 
 static __device__ __align__(256) unsigned char brx_noalloc_scratch[NOALLOC_BYTES];
 
-// Device address of the static scratch, looked up once per device.
+// Device address of the static scratch, looked up once per CUDA context.
+// The array's address belongs to the module loaded into a context: after a
+// cudaDeviceReset (or with another context current on the same device) the
+// module is loaded again and the array may move, so the cache is keyed on
+// the driver's context ID, which is unique for the life of the process. The
+// two driver calls come through the runtime's entry-point query, so the
+// library does not link against the driver library itself.
 static std::mutex g_noalloc_mutex;
-static std::map<int, unsigned char *> g_noalloc_address;
+static std::map<unsigned long long, unsigned char *> g_noalloc_address;
+typedef CUresult (CUDAAPI *ctx_get_current_fn)(CUcontext *);
+typedef CUresult (CUDAAPI *ctx_get_id_fn)(CUcontext, unsigned long long *);
+
+static int current_context_id(unsigned long long *id)
+{
+    static ctx_get_current_fn get_current = nullptr;
+    static ctx_get_id_fn get_id = nullptr;
+    if (!get_current || !get_id) {
+        void *a = nullptr, *b = nullptr;
+        cudaDriverEntryPointQueryResult qa, qb;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) != cudaSuccess ||
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) != cudaSuccess ||
+            qa != cudaDriverEntryPointSuccess || qb != cudaDriverEntryPointSuccess || !a || !b)
+            return fail(BRX_ERR_CUDA, "the driver's cuCtxGetCurrent / cuCtxGetId are unavailable");
+        get_current = (ctx_get_current_fn)a;
+        get_id = (ctx_get_id_fn)b;
+    }
+    CUcontext ctx = nullptr;
+    if (get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, id) != CUDA_SUCCESS)
+        return fail(BRX_ERR_CUDA, "no current CUDA context");
+    return BRX_OK;
+}
 
 static int noalloc_address(unsigned char **out)
 {
     int dev = 0;
     CK(cudaGetDevice(&dev));
+    CK(cudaSetDevice(dev));          // makes the device's primary context current (no allocation)
+    unsigned long long id = 0;
+    TRY(current_context_id(&id));
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    auto it = g_noalloc_address.find(dev);
+    auto it = g_noalloc_address.find(id);
     if (it != g_noalloc_address.end()) { *out = it->second; return BRX_OK; }
     void *ptr = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&ptr, brx_noalloc_scratch);
     if (e != cudaSuccess || !ptr)
         return fail(BRX_ERR_CUDA, std::string("cudaGetSymbolAddress(brx_noalloc_scratch): ") + cudaGetErrorString(e));
-    g_noalloc_address[dev] = (unsigned char *)ptr;
+    g_noalloc_address[id] = (unsigned char *)ptr;
     *out = (unsigned char *)ptr;
     return BRX_OK;
 }
@@ -1775,6 +1885,14 @@ __global__ void k_noalloc_tables(MeshDev m, Ctrl *ctrl, int *cell_sid, int *cfla
         }
         if (bad) { ctrl->active = 0; atomicOr(&ctrl->status1, ST_SPATIAL); }
     }
+}
+
+// Limited water flux of the call into the caller's buffer, only when the
+// topology check passed: a rejected call leaves the buffer as it was.
+__global__ void k_noalloc_water(MeshDev m, Work w, const Ctrl *ctrl, double *water)
+{
+    if (!ctrl->active) return;
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < m.nf; f += gridDim.x * blockDim.x) water[f] = w.lim[f].x;
 }
 
 extern "C" int brx_rate_noalloc(int nc, int nf, int nadj, const int *owner, const int *neighbour, const int *offset,
@@ -1837,7 +1955,7 @@ extern "C" int brx_rate_noalloc(int nc, int nf, int nadj, const int *owner, cons
     k_gather<<<(nc + 255) / 256, 256, 0, st>>>(m, sd, ctrl, w, 1);
     k_limit<<<(nf + 255) / 256, 256, 0, st>>>(m, sd, ctrl, w, 1);
     k_update<double><<<(nc + 255) / 256, 256, 0, st>>>(m, sd, ctrl, w, 1, rate, TurbDev{}, 0);
-    k_water_out<<<(nf + 255) / 256, 256, 0, st>>>(m, w, water);
+    k_noalloc_water<<<(nf + 255) / 256, 256, 0, st>>>(m, w, ctrl, water);
     CK(cudaGetLastError());
     Ctrl out{};
     CK(cudaMemcpyAsync(&out, ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, st));

@@ -65,8 +65,12 @@ struct Ctrl {
     double accepted_water_time;       // sum of accepted trial lengths (== elapsed)
     // water budget: each stage's sum over open faces of (outward water flux x
     // length) as the update uses it, and the interval's boundary ledger, the
-    // net inflow volume of the accepted substeps (shoreline_solver.py:353-355)
+    // net inflow volume of the accepted substeps (shoreline_solver.py:353-355);
+    // bgross / gross: the same with |water x length| per face, an upper bound
+    // of the reference's gross boundary volume sum_f |ledger_f| (the triangle
+    // inequality), which scales its roundoff allowance
     double bflux[2], ledger;
+    double bgross[2], gross;
     // FP32 copies for the mixed form's sweeps, refreshed with every trial
     float gravf, dryf, trialf, roughf;
     int cfl1, pad1;                         // stage 1 exceeded the CFL limit (mixed form, set after its gather)

@@ -1295,17 +1295,25 @@ constexpr int BOUNDARY_WARPS = 32;
 template <class F>
 __device__ void boundary_water(const MeshDev &m, const BoundaryDev &b, Ctrl &ct, int stage, int k0, int k1)
 {
-    __shared__ double part[BOUNDARY_WARPS];
+    __shared__ double part[BOUNDARY_WARPS], apart[BOUNDARY_WARPS];
     __syncthreads();
-    double acc = 0.;
-    for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) acc += double(F(b.flux[k])) * m.length[b.slot_face[k]];
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+    double acc = 0., aacc = 0.;
+    for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+        const double v = double(F(b.flux[k])) * m.length[b.slot_face[k]];
+        acc += v;
+        aacc += fabs(v);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        aacc += __shfl_xor_sync(0xffffffffu, aacc, o);
+    }
+    if ((threadIdx.x & 31) == 0) { part[threadIdx.x >> 5] = acc; apart[threadIdx.x >> 5] = aacc; }
     __syncthreads();
     if (threadIdx.x == 0) {
-        double total = 0.;
-        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) total += part[i];
+        double total = 0., gross = 0.;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) { total += part[i]; gross += apart[i]; }
         ct.bflux[stage - 1] = total;
+        ct.bgross[stage - 1] = gross;
     }
 }
 
@@ -2134,6 +2142,7 @@ __device__ void control_one(Ctrl &c)
         c.cur ^= 1;
         c.elapsed += c.trial;
         c.ledger -= c.trial * (c.one_stage ? c.bflux[0] : .5 * (c.bflux[0] + c.bflux[1]));
+        c.gross += c.trial * (c.one_stage ? c.bgross[0] : .5 * (c.bgross[0] + c.bgross[1]));
         c.substeps++;
         if (c.substeps == 1 || c.trial < c.min_dt) c.min_dt = c.trial;
         if (c.trial > c.max_dt) c.max_dt = c.trial;

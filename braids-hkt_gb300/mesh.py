@@ -350,15 +350,21 @@ RECORD_KEYS = ("owner", "neighbour", "bid", "normal", "length", "mid", "area", "
 def mesh_from_records(d, points=None, tri=None):
     """A Mesh over a reference owner's geometry records.
 
-    ``d`` holds the arrays the reference's flow owner reads from its records
-    (river_mesh_records.initialize, the geometry cache ``g``): owner,
-    neighbour, bid, normal (2,nf), length, mid (2,nf), area, xy (2,nc), the
-    CSR offset / faces / signs, boundary_offset / boundary_faces, ls_matrix
-    (4,nc), ls_weight, ls_delta (2,nadj), displacement (2,2,nf), distance
-    (2,nf). Cells may be any polygons (cut cells, quadtree); no geometry is
-    recomputed, so the solver sees the reference's own bits. Rotor arrays
-    need the cell polygons as triangles (points, tri); without them a case
-    takes no rotors.
+    ``d`` holds owner, neighbour, bid, normal (2,nf), length, mid (2,nf),
+    area, xy (2,nc), the CSR offset / faces / signs, boundary_offset /
+    boundary_faces (river_mesh_records.initialize), and the f-wave
+    reconstruction's least-squares records in the layout the reference's
+    FP64 GPU kernels take them (reconstruction.cu:43-60): ls_matrix (4,nc),
+    ls_weight (nadj), ls_delta (2,nadj), distance (2,nf) (the owner-side and
+    neighbour-side normal distances) and displacement, the face midpoint
+    minus the cell centre, either as (2,2,nf) [component, side, face] (the
+    Fortran exporter's face_displacement) or as (4,nf) side-major rows owner
+    x, owner y, neighbour x, neighbour y (the geometry cache's
+    ``displacement``, bend_methods_v1.py:125-128), which is converted. Every
+    shape is checked; any other layout is refused. Cells may be any polygons
+    (cut cells, quadtree); no geometry is recomputed, so the solver sees the
+    reference's own bits. Rotor arrays need the cell polygons as triangles
+    (points, tri); without them a case takes no rotors.
     """
     missing = [k for k in RECORD_KEYS if k not in d]
     if missing:
@@ -366,9 +372,20 @@ def mesh_from_records(d, points=None, tri=None):
     i32 = lambda a: np.ascontiguousarray(a, dtype=np.int32)
     f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64)
     nc, nf = len(d["area"]), len(d["owner"])
-    if len(d["offset"]) != nc + 1 or np.asarray(d["normal"]).shape != (2, nf) or np.asarray(d["xy"]).shape != (2, nc):
-        raise ValueError("records have inconsistent sizes")
+    nadj = len(d["faces"])
+    shapes = dict(owner=(nf,), neighbour=(nf,), bid=(nf,), normal=(2, nf), length=(nf,), mid=(2, nf), area=(nc,),
+                  xy=(2, nc), offset=(nc + 1,), faces=(nadj,), signs=(nadj,), ls_matrix=(4, nc),
+                  ls_weight=(nadj,), ls_delta=(2, nadj), distance=(2, nf))
+    bad = [f"{k} {np.shape(d[k])} (expected {v})" for k, v in shapes.items() if np.shape(d[k]) != v]
+    if bad:
+        raise ValueError("records have inconsistent shapes: " + ", ".join(bad))
+    if int(np.asarray(d["offset"])[-1]) != nadj:
+        raise ValueError("records: offset[-1] differs from the number of CSR entries")
     disp = f64(d["displacement"])
+    if disp.shape == (4, nf):           # side-major rows: owner x, y; neighbour x, y
+        disp = np.ascontiguousarray(np.stack((disp[[0, 2]], disp[[1, 3]])))
+    elif disp.shape != (2, 2, nf):
+        raise ValueError(f"records: displacement {disp.shape} is neither (2,2,nf) nor (4,nf)")
     mesh = Mesh(points=np.zeros((0, 2)) if points is None else f64(points),
                 tri=np.zeros((0, 3), np.int64) if tri is None else np.asarray(tri, dtype=np.int64),
                 owner=i32(d["owner"]), neighbour=i32(d["neighbour"]), bid=i32(d["bid"]), normal=f64(d["normal"]),
@@ -420,19 +437,26 @@ def jittered_channel_points(length, width, spacing, jitter, rng, refine=()):
         y0, y1 = max(0.0, y0), min(width, y1)
         inside = (pts[0][:, 0] > x0 - spacing * 0.5) & (pts[0][:, 0] < x1 + spacing * 0.5) & \
                  (pts[0][:, 1] > y0 - spacing * 0.5) & (pts[0][:, 1] < y1 + spacing * 0.5)
-        keep &= ~inside | onx | ony
+        # coarse points inside the box are replaced by the fine grid; a box
+        # that reaches an edge of the domain also replaces that edge's coarse
+        # points (the domain corners stay)
+        keep &= ~inside | (onx & ony)
         fx = np.arange(x0, x1 + 1e-9, s)
         fy = np.arange(y0, y1 + 1e-9, s)
         FX, FY = np.meshgrid(fx, fy, indexing="ij")
         FX = FX.ravel()
         FY = FY.ravel()
         fj = 0.25 * s
-        FX = FX + rng.uniform(-fj, fj, FX.size)
-        FY = FY + rng.uniform(-fj, fj, FY.size)
-        ok = (FX > 0.0) & (FX < length) & (FY > 0.0) & (FY < width)
+        jx = rng.uniform(-fj, fj, FX.size)
+        jy = rng.uniform(-fj, fj, FY.size)
+        # fine points on an edge of the domain slide only along that edge
+        edge_x = (FX <= 0.0) | (FX >= length)
+        edge_y = (FY <= 0.0) | (FY >= width)
+        FX = np.where(edge_x, FX, FX + jx)
+        FY = np.where(edge_y, FY, FY + jy)
+        ok = (FX >= 0.0) & (FX <= length) & (FY >= 0.0) & (FY <= width) & ~(edge_x & edge_y)
         pts.append(np.c_[FX[ok], FY[ok]])
     base = pts[0][keep]
-    # Boundary points of refined boxes: keep them on the boundary lines only.
     out = np.concatenate([base] + pts[1:])
     _, unique = np.unique(np.round(out, 9), axis=0, return_index=True)
     return out[np.sort(unique)]

@@ -101,7 +101,9 @@ def rotor_rows(case, centres, diameter=5.0, control=None, bed_clearance=0.5, sur
 
 
 def config2(seed=2, refine_spacing=1.0, control=None):
-    """Config-1 channel with 3 tandem rotors on the centreline 150 m apart, refined wakes (about 120k cells).
+    """Config-1 channel with 3 tandem rotors on the centreline 150 m apart and
+    the mesh refined to 1 m across the channel from 5 m upstream to 60 m
+    downstream of each rotor (about 120k cells).
 
     Rotors: D = 5 m, Ct = 0.8 with Cp(U) = min(0.4, 500 kW / (1/2 rho A U^3))
     referenced to the incident speed (rated near 5.0 m/s), hub 0.75 m above
@@ -110,7 +112,7 @@ def config2(seed=2, refine_spacing=1.0, control=None):
     from . import turbines as TB
     length, width = 2000.0, 200.0
     xs = [700.0, 850.0, 1000.0]
-    boxes = [(x - 10.0, x + 60.0, 0.5 * width - 15.0, 0.5 * width + 15.0, refine_spacing) for x in xs]
+    boxes = [(x - 5.0, x + 60.0, 0.0, width, refine_spacing) for x in xs]
     case = channel(length, width, seed=seed, refine=boxes)
     control = control or TB.rated_power_curve(5.0, 0.8, 0.4, 500e3)
     case["turbines"] = rotor_rows(case, [(x, 0.5 * width) for x in xs], control=control)

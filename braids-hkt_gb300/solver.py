@@ -429,6 +429,20 @@ class RiverSolver:
             rows = [r for r in rows if r["scenario"] == scenario]
         return rows
 
+    def performance_history(self, duration, interval):
+        """Per-rotor thrust and power at fixed output times, as the reference
+        worker publishes them (TURBINE_PERFORMANCE rows,
+        adaptive_river_worker.py:577-587): owner steps of ``interval`` (each
+        with its water-budget check) up to ``duration``; after each step one
+        row per rotor with time_s, turbine_id, thrust_N, useful_power_W,
+        hydraulic_work_W and the rest of the rotor's diagnostics."""
+        rows = []
+        for _ in range(int(round(duration / interval))):
+            self.step(interval)
+            for r in self.turbines():
+                rows.append(dict(r, time_s=float(self.time[r["scenario"]])))
+        return rows
+
     def set_forcing_table(self, time, value):
         """value (2, nseg, len): discharge and stage tables for every segment."""
         t = _f64(time)
@@ -562,11 +576,27 @@ class RiverSolver:
         check(self.lib.brx_ledger_get(self.h, _ptr(out)))
         return out
 
+    def gross_boundary_volume(self):
+        """Sum over the last interval's accepted substeps of dt x sum |face water x length| [m3],
+        per scenario: an upper bound of the reference's gross boundary volume."""
+        out = np.zeros(self.nscen)
+        check(self.lib.brx_ledger_gross_get(self.h, _ptr(out)))
+        return out
+
+    def _inventory(self, h0, h1):
+        """sum(max(h0, h1) area) per scenario (shoreline_solver.py:356): the
+        water inventory that scales the roundoff allowance."""
+        a = self.packed["area"]
+        v = np.maximum(h0, h1) * a
+        return np.add.reduceat(v, self.packed["cell_offset"][:-1].astype(np.int64))
+
     def step(self, dt):
         """Advance by dt from the owner clock with the owner's water-budget
         check (ShorelineSolver.step, shoreline_solver.py:345-372): the volume
         change of every scenario must equal its boundary ledger within the
-        FP64 roundoff allowance, else the state is restored and
+        FP64 roundoff allowance max(1e-10, 64 eps max(1, inventory, gross))
+        with the inventory sum(max(h0, h1) A) as the reference's and the gross
+        boundary volume bounded from above; else the state is restored and
         WaterBudgetError raised; on success the ledger is committed."""
         self.torch.cuda.current_stream().synchronize()
         q0, z0, hints0 = self.q.clone(), self.z.clone(), self.hints()
@@ -578,7 +608,8 @@ class RiverSolver:
             raise
         v1 = np.atleast_2d(self.totals())[:, 0]
         ledger = self.ledger()
-        residual, roundoff, ok = water_budget(v0, v1, ledger)
+        inventory = self._inventory(q0[0].cpu().numpy(), self.q[0].cpu().numpy())
+        residual, roundoff, ok = water_budget(v0, v1, ledger, inventory, self.gross_boundary_volume())
         if not ok.all():
             self.q.copy_(q0); self.z.copy_(z0); self.set_hints(hints0)
             i = int(np.flatnonzero(~ok)[0])

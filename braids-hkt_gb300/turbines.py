@@ -449,5 +449,7 @@ def diagnostics_rows(diag, names, water_density=WATER_DENSITY):
         d["inactive_reason"] = None if d["active"] else REASONS[int(d["reason"])]
         d["thrust_N"] = d["force_per_density_m4_s2"] * water_density
         d["power_W"] = d["useful_power_per_density_m5_s3"] * water_density
+        d["useful_power_W"] = d["power_W"]
+        d["hydraulic_work_W"] = d["hydraulic_power_removed_per_density_m5_s3"] * water_density
         out.append(d)
     return out

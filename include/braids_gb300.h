@@ -321,6 +321,13 @@ int brx_forcing_get(brx_solver *s, double *out);
  * compares it with the volume change (brx_totals before and after). */
 int brx_ledger_get(brx_solver *s, double *out);
 
+/* Gross boundary volume of the last interval, host out (nscen): the sum over
+ * the accepted substeps of dt_k sum_f |water_f length_f| (SSPRK: the mean of
+ * the two stages' sums). It bounds the reference's gross volume
+ * sum_f |ledger_f| from above and scales the owner's FP64 roundoff allowance
+ * (water_increment_roundoff_limit, shoreline_solver.py:29-39, 356-357). */
+int brx_ledger_gross_get(brx_solver *s, double *out);
+
 /* Step hint carried between brx_advance calls (nscen, host; <= 0 = none). */
 int brx_hint_get(brx_solver *s, double *hint);
 int brx_hint_set(brx_solver *s, const double *hint);
@@ -348,6 +355,14 @@ int brx_launch_shape_get(brx_solver *s, int kind, int *block, int *blocks_per_sm
  * of launches. The bound state is advanced as by brx_substep. */
 int brx_profile_substep(brx_solver *s, double dt, double time, int cap, double *ms, int *kind, int *count);
 
+/* FMA throughput of the current device (no counterpart in the reference):
+ * precision 0 FP64, 1 FP32. Eight independent FMA chains per thread at full
+ * occupancy, timed with CUDA events (best of five launches after one warm-
+ * up). tflops gets 2 x FMAs / s / 1e12, ms (may be NULL) the launch time. It
+ * is the compute roofline of the FP64 form and of the mixed form's FP32
+ * sweeps. */
+int brx_fma_rate(int precision, double *tflops, double *ms);
+
 /* Allocation-free spatial residual of one closed scenario (walls only, no
  * open boundaries). It has no counterpart in the reference: it exists for
  * callers that may not allocate device memory once running - hosts that hand
@@ -361,15 +376,18 @@ int brx_profile_substep(brx_solver *s, double dt, double time, int cap, double *
  * pointers (may be NULL). At most 16384 cells and 32768 faces: larger meshes
  * get BRX_ERR_UNSUPPORTED. The stage scratch is one static device array of
  * about 7.4 MB that every GPU loading this library holds until process exit.
- * The first call on each device looks up that array's device address
- * (cudaGetSymbolAddress) with the device current; make that first call
- * before any stream capture. Calls share the array and rewrite what they
- * read, so consecutive calls are independent, but calls that overlap on the
- * GPU (other streams, other host threads) race on it. The call runs on
- * `stream` (cudaStream_t as void*, NULL for the default stream) and returns
- * after it has finished. Invalid device topology (index out of range, a
- * cell with more than 32 faces) is detected on the device and reported as
- * BRX_ERR_ARGUMENT without touching the mesh further. */
+ * The first call in each CUDA context (each device's primary context, and
+ * again after a cudaDeviceReset, which loads the module anew) looks up that
+ * array's device address (cudaGetSymbolAddress) with the device current;
+ * make that first call before any stream capture. Calls share the array and
+ * rewrite what they read, so consecutive calls are independent, but calls
+ * that overlap on the GPU (other streams, other host threads) race on it.
+ * The call runs on `stream` (cudaStream_t as void*, NULL for the default
+ * stream) and returns after it has finished. Invalid device topology (index
+ * out of range, a cell with more than 32 faces) is detected on the device
+ * and reported as BRX_ERR_ARGUMENT with the spatial status bit, without
+ * touching the mesh further; on any nonzero return rate and water are not
+ * written. */
 int brx_rate_noalloc(int nc, int nf, int nadj, const int *owner, const int *neighbour, const int *offset,
                      const int *faces, const int *signs, const double *normal, const double *length,
                      const double *area, const double *ls_matrix, const double *ls_weight, const double *ls_delta,

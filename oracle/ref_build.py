@@ -1,7 +1,7 @@
 """Build the reference's own hot-path kernels for the host, into oracle/_ref/.
 
-TEST INFRASTRUCTURE ONLY. This recipe reads the reference checkout (default
-/root/reference, or $BRAIDS_REFERENCE), runs the reference's own source
+TEST INFRASTRUCTURE ONLY. This recipe reads the reference checkout
+($BRAIDS_REFERENCE, else a ``reference`` folder beside this repository), runs the reference's own source
 transforms exactly as its GPU owner does before compiling, and compiles the
 result as host C++ with the reference's CPU flags (``-O3 -fopenmp
 -ffp-contract=off``, src/braids_support/sediment/river_morphodynamics/
@@ -41,7 +41,8 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
-REFERENCE = Path(os.environ.get("BRAIDS_REFERENCE", "/root/reference"))
+# the reference checkout: $BRAIDS_REFERENCE, else a `reference` folder beside this repository
+REFERENCE = Path(os.environ.get("BRAIDS_REFERENCE") or HERE.parent.parent / "reference")
 FLAGS = ["-x", "c++", "-std=c++17", "-O3", "-fopenmp", "-shared", "-fPIC", "-ffp-contract=off"]
 DECLSPEC = '-D__declspec(x)=__attribute__((visibility("default")))'
 

@@ -38,7 +38,8 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 REF = HERE / "_ref"
-REFERENCE = Path(os.environ.get("BRAIDS_REFERENCE", "/root/reference"))
+# the reference checkout: $BRAIDS_REFERENCE, else a `reference` folder beside this repository
+REFERENCE = Path(os.environ.get("BRAIDS_REFERENCE") or HERE.parent.parent / "reference")
 
 
 class Rejected(Exception):

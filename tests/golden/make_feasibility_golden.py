@@ -1,6 +1,7 @@
 """Generate the boundary-allocation fixtures from the reference's own classes.
 
-Run in a checkout that has the reference (default /root/reference):
+Run where the reference checkout is present ($BRAIDS_REFERENCE, else a
+``reference`` folder beside this repository):
 
     python tests/golden/make_feasibility_golden.py
 
@@ -24,7 +25,7 @@ import numpy as np
 
 ROOT = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(ROOT))
-REFERENCE = Path(os.environ.get("BRAIDS_REFERENCE", "/root/reference"))
+REFERENCE = Path(os.environ.get("BRAIDS_REFERENCE") or ROOT.parent / "reference")
 sys.path.insert(0, str(REFERENCE / "src"))
 
 import braids_hkt_gb300.scenarios as S  # noqa: E402

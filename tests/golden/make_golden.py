@@ -1,6 +1,7 @@
 """Generate the golden fixtures from the reference's own kernels.
 
-Run in a checkout that has the reference (default /root/reference):
+Run where the reference checkout is present ($BRAIDS_REFERENCE, else a
+``reference`` folder beside this repository):
 
     python oracle/ref_build.py && python tests/golden/make_golden.py
 

@@ -1,6 +1,7 @@
 """Golden vectors for the HLLC / MUSCL-Hancock option, from the reference's own operator.
 
-Run in a checkout that has the reference (default /root/reference):
+Run where the reference checkout is present ($BRAIDS_REFERENCE, else a
+``reference`` folder beside this repository):
 
     python oracle/ref_build.py && python tests/golden/make_hllc_golden.py [case ...]
 

@@ -1,6 +1,7 @@
 """Golden vectors for the rotor array, from the reference's own turbine code.
 
-Run in a checkout that has the reference (default /root/reference):
+Run where the reference checkout is present ($BRAIDS_REFERENCE, else a
+``reference`` folder beside this repository):
 
     python oracle/ref_build.py && python tests/golden/make_turbine_golden.py
 

@@ -36,3 +36,24 @@ def test_incomplete_records_refused():
     del d["distance"]
     with pytest.raises(ValueError):
         mesh_from_records(d)
+
+
+def test_side_major_displacement_converted():
+    """The geometry cache's (4, nf) displacement (owner x, y, neighbour x, y)
+    gives the same mesh as the exporter's (2, 2, nf) layout."""
+    m = S.small_channel()["mesh"]
+    d = records_of(m)
+    disp = d["displacement"]
+    d["displacement"] = np.stack((disp[0, 0], disp[1, 0], disp[0, 1], disp[1, 1]))
+    m2 = mesh_from_records(d)
+    for k in ("disp", "disp_len"):
+        np.testing.assert_array_equal(m2.records[k], m.records[k], err_msg=k)
+
+
+@pytest.mark.parametrize("key,shape", [("displacement", (3, 7)), ("ls_matrix", (3, 5)), ("ls_delta", (4, 2)),
+                                       ("ls_weight", (9,)), ("distance", (1, 4))])
+def test_misshapen_records_refused(key, shape):
+    d = records_of(S.small_channel()["mesh"])
+    d[key] = np.zeros(shape)
+    with pytest.raises(ValueError):
+        mesh_from_records(d)
