@@ -37,7 +37,7 @@ from .build import BUILD
 # tunable kernel kinds (brx_profile_substep kinds) per method; the rotor
 # gradient / face kernels (12, 13) are timed inside the rotor group (11)
 KINDS = {
-    "fwave": {0: "drag", 2: "cells", 3: "faces", 4: "gather", 5: "limit", 6: "update", 11: "rotors"},
+    "fwave": {0: "drag", 2: "cells", 3: "faces", 4: "gather", 6: "update", 11: "rotors"},
     "hllc": {0: "drag", 20: "hllc_cells", 21: "hllc_predict", 23: "hllc_faces", 24: "hllc_budget",
              26: "hllc_update"},
 }

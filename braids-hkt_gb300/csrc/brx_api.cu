@@ -367,6 +367,8 @@ extern "C" int brx_solver_create(int nscen, const int *cell_offset, const int *f
                     int flags = 0;
                     if (bid[f] >= 0) flags |= 1;
                     if (neighbour[f] < 0 && bid[f] < 0) flags |= 4;
+                    if (bslot[f] >= 0) flags |= 8;          // an exterior-owner face: never donor-limited
+                    if (signs[k] > 0) flags |= 16;          // this cell owns the face
                     s->h_cidx[k] = make_int2(other, flags);
                     // LS weight times offset, rounded as the FP32 sweep would form it
                     const float wt = float(ls_weight[k]);
@@ -1292,8 +1294,9 @@ static void enqueue_stage(brx_solver *s, int stage, double *rate_out)
     // needs the rotor cell terms (wet gradients, actuator sink) first
     const bool mixed = s->precision == BRX_MIXED;
     if (fork && mixed) cudaStreamWaitEvent(s->stream, s->join2, 0);
-    for (int kind : {(int)K_FACES, (int)K_GATHER, (int)K_LIMIT})
-        s->launches += launch_kernel(s, kind, stage, kind == K_LIMIT ? rate_out : nullptr);
+    // the donor limiter runs inside the update (owner computes): no limit pass
+    for (int kind : {(int)K_FACES, (int)K_GATHER})
+        s->launches += launch_kernel(s, kind, stage, nullptr);
     if (fork && !mixed) cudaStreamWaitEvent(s->stream, s->join2, 0);
     s->launches += launch_turbines(s, stage, s->stream, TURB_FACES);
     s->launches += launch_kernel(s, K_UPDATE, stage, rate_out);
@@ -1614,6 +1617,8 @@ extern "C" int brx_rate(brx_solver *s, double dt, double time, double *rate_devi
     refresh_bed(s);
     if (s->precision == BRX_MIXED) s->launches += launch_kernel(s, K_PRIM, 1, nullptr);
     enqueue_stage(s, 1, rate_device);
+    // the limited water flux of each face, for the caller's water buffer
+    s->launches += launch_kernel(s, K_LIMIT, 1, nullptr);
     if (s->precision == BRX_MIXED) {
         s->launches += launch_kernel(s, K_WATER, 1, water_device);
     } else {
@@ -1663,7 +1668,7 @@ extern "C" int brx_profile_substep(brx_solver *s, double dt, double time, int ca
         const bool mixed = s->precision == BRX_MIXED;
         for (int stage = 1; stage <= 2; ++stage)
             for (int kind : {(int)K_BOUNDARY, mixed ? (int)K_TURB : -1, (int)K_CELLS, (int)K_FACES, (int)K_GATHER,
-                             (int)K_LIMIT, mixed ? -1 : (int)K_TURB, (int)K_UPDATE})
+                             mixed ? -1 : (int)K_TURB, (int)K_UPDATE})
                 if (kind >= 0)
                     if (const int nl = launch_kernel(s, kind, stage, nullptr)) { mark(kind); extra += nl - 1; }
     }

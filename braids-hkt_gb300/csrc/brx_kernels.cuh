@@ -1762,7 +1762,14 @@ __device__ __forceinline__ Side face_side(const CellRec &r, double rx_, double r
 }
 
 template <class F>
-__global__ void __launch_bounds__(128) k_faces(MeshDev m, StateDev s, BoundaryDev b, Ctrl *ctrl, Work w, int stage,
+// Four resident blocks of 128 threads (at most 128 registers): a single
+// 75k-face scenario then fits the 152 SMs in one wave of 16 warps each; with
+// the unconstrained 168 registers it took 1.3 waves at 12 warps per SM and
+// the FP64 pipe sat idle in the tail.
+#ifndef BRX_FP64_FACES_MIN_BLOCKS
+#define BRX_FP64_FACES_MIN_BLOCKS 4
+#endif
+__global__ void __launch_bounds__(128, BRX_FP64_FACES_MIN_BLOCKS) k_faces(MeshDev m, StateDev s, BoundaryDev b, Ctrl *ctrl, Work w, int stage,
                                                double *trace, const int *hkt)
 {
     const int nf = m.nf, nc = m.nc;
@@ -2005,11 +2012,17 @@ __global__ void __launch_bounds__(256) k_limit(MeshDev m, StateDev s, Ctrl *ctrl
 
 // midpoint_gather + stage combination (+ closing drag on the second stage).
 // With rate_out set, the final rate is stored there and no state is written.
+// Owner computes: each cell forms the donor-limited flux of its faces itself
+// (midpoint_faces, river_midpoint.h:30-41), with the same operations as
+// k_limit, so both cells of a face use the same value and no limited-flux
+// buffer goes through memory (k_limit still fills one for the water output
+// of a single residual).
 template <class F>
 __global__ void __launch_bounds__(256) k_update(MeshDev m, StateDev s, Ctrl *ctrl, Work w, int stage,
                                                 double *rate_out, TurbDev t, int turb)
 {
     const int nc = m.nc;
+    const double *q = stage == 1 ? s.work : s.q1;
     FOR_ACTIVE_CELLS(m.act, c) {
         const int sid = m.cell_sid[c];
         Ctrl &ct = ctrl[sid];
@@ -2019,8 +2032,23 @@ __global__ void __launch_bounds__(256) k_update(MeshDev m, StateDev s, Ctrl *ctr
         for (int k = m.offset[c]; k < m.offset[c + 1]; ++k) {
             const int f = m.faces[k];
             const double wt = m.signs[k] * m.length[f] / area;
-            const double4_32a L = w.lim[f];
-            mass -= wt * L.x; mx -= wt * L.y; my -= wt * L.z;
+            double water = w.ws[f].x;
+            if (water != 0. && m.bslot[f] < 0) {
+                const int donor = water < 0. ? m.neighbour[f] : m.owner[f];
+                if (donor >= 0) {
+                    const double th = w.theta[donor];
+                    if (th != 1.) {
+                        const double delta = (th - 1.) * water;
+                        water *= th;
+                        const double hd = q[donor];
+                        if (hd > ct.dry) {
+                            mx -= wt * (delta * q[nc + donor] / hd);
+                            my -= wt * (delta * q[2 * nc + donor] / hd);
+                        }
+                    }
+                }
+            }
+            mass -= wt * water;
         }
         const double r0 = mass;
         double r1 = w.rate[nc + c] + mx, r2 = w.rate[2 * nc + c] + my;

@@ -9,7 +9,8 @@ namespace brx {
 // FP32 geometry and tables of the mixed form, packed for the sweep that reads them.
 struct MixedGeo {
     const float4 *cinv;      // (nc) inverse LS normal matrix (i11, i12, i22, 0); zero when no gradient
-    const int2 *cidx;        // (nadj) other cell (-1 none), flags: bit0 open face, bit1 stage outlet, bit2 wall
+    const int2 *cidx;        // (nadj) other cell (-1 none), flags: bit0 open face, bit1 stage outlet, bit2 wall,
+                             //   bit3 exterior-owner face (boundary slot), bit4 this cell owns the face
     const float4 *cent;      // (nadj) LS weight * ls_delta x, y; this side's face displacement x, y
     const float *cw4;        // (nadj) signed length / area, FP32 (momentum, outflow and CFL sums)
     const double *cw8;       // (nadj) signed length / area, FP64 (mass)

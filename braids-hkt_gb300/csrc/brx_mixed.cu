@@ -844,12 +844,26 @@ __device__ __forceinline__ void drag_f(const Ctrl &ct, float dtf, double &h, dou
     hv *= factor;
 }
 
+// Update (owner computes): each cell forms the donor-limited water flux of
+// its faces itself (river_midpoint.h:30-41) from the face sweep's FP32 water
+// and the donor's factor, exactly as the face pass km_limit does: both cells
+// of a face compute the same FP64 value double(w) * double(theta), so mass
+// still telescopes, and no limited-flux buffer goes through memory. After
+// the first gather, block 0 also evaluates each scenario's first-stage CFL
+// test (the second stage's kernels read it).
 __global__ void __launch_bounds__(256) km_update(MeshDev m, StateDev s, Ctrl *ctrl, Work w, MixedGeo g, int stage,
                                                  double *rate_out, TurbDev t, int turb)
 {
     const int nc = m.nc;
-    const MxLim *lim = reinterpret_cast<const MxLim *>(w.lim);
+    if (stage == 1 && blockIdx.x == 0)
+        for (int i = threadIdx.x; i < m.nscen; i += blockDim.x) {
+            Ctrl &c = ctrl[i];
+            c.cfl1 = c.trial * bits_to_double(c.peak1) > c.cfl * (1 + 1e-12);
+        }
+    const float2 *ws = reinterpret_cast<const float2 *>(w.ws);
+    const float *theta32 = reinterpret_cast<const float *>(w.theta);
     const float *rate32 = reinterpret_cast<const float *>(w.rate);
+    const MxPrim *P = reinterpret_cast<const MxPrim *>((stage == 1 ? g.prim[0] : g.prim[1]));
     MxPrim *P2 = reinterpret_cast<MxPrim *>(g.prim[1]);
     FOR_ACTIVE_CELLS(m.act, c) {
         const int sid = m.cell_sid[c];
@@ -858,11 +872,24 @@ __global__ void __launch_bounds__(256) km_update(MeshDev m, StateDev s, Ctrl *ct
         double mass = 0.;
         float mx = 0.f, my = 0.f;
         for (int k = m.offset[c]; k < m.offset[c + 1]; ++k) {
-            const MxLim L = lim[m.faces[k]];
-            mass -= g.cw8[k] * L.water;
+            const float wf = ws[m.faces[k]].x;
             const float wk = g.cw4[k];
-            mx -= wk * L.cx;
-            my -= wk * L.cy;
+            double water = double(wf);
+            if (wf != 0.f) {
+                const int2 id = g.cidx[k];
+                // the donor is the owner for outward (positive) water, else the neighbour
+                const int donor = (wf > 0.f) == ((id.y & 16) != 0) ? c : id.x;
+                if (!(id.y & 8) && donor >= 0) {
+                    const float th = theta32[donor];
+                    if (th != 1.f) {
+                        const float delta = (th - 1.f) * wf;
+                        water = double(wf) * double(th);          // exact product
+                        const MxPrim pd = P[donor];
+                        if (pd.wet) { mx -= wk * (delta * pd.u); my -= wk * (delta * pd.v); }
+                    }
+                }
+            }
+            mass -= g.cw8[k] * water;
         }
         float f1 = rate32[c] + mx, f2 = rate32[nc + c] + my;
         double r1, r2;
