@@ -21,5 +21,6 @@ def test_choose_keeps_the_default_on_ties_and_skips_empty_kinds():
 
 
 def test_tunable_kinds_are_profile_kinds():
-    assert set(KINDS["fwave"]) == {0, 2, 3, 4, 5, 6, 11}
+    # the donor limiter runs inside the update: no limit kind (5) in a substep
+    assert set(KINDS["fwave"]) == {0, 2, 3, 4, 6, 11}
     assert set(KINDS["hllc"]) == {0, 20, 21, 23, 24, 26}
