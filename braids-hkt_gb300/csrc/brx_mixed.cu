@@ -234,25 +234,72 @@ __global__ void __launch_bounds__(128) km_bed(MeshDev m, StateDev s, MixedGeo g)
 #define BRX_CELLS_MIN_BLOCKS 8
 #endif
 
+// CSR entries of one cell as the cell sweep reads them: the other cell and
+// its flags, the LS weight x offset and face displacement, the bed
+// difference, and the other cell's stage primitives (wet bit, eta pair,
+// velocities). GlobalEntries reads them from the packed tables as it goes;
+// StagedEntries from the tile's shared-memory copy (km_cells_tile).
+struct GlobalEntries {
+    const MixedGeo &g;
+    const MxPrim *P;
+    int k0;
+    __device__ __forceinline__ int2 id(int j) const { return g.cidx[k0 + j]; }
+    __device__ __forceinline__ float4 ge(int j) const { return g.cent[k0 + j]; }
+    __device__ __forceinline__ float db(int j) const { return g.cdb[k0 + j]; }
+    // other cell's primitives: (ehi, elo, u, v) and the wet bit (valid for id.x >= 0)
+    __device__ __forceinline__ float4 pn(int j, int n) const
+    {
+        const MxPrim q = P[n];
+        return make_float4(q.ehi, q.elo, q.u, q.v);
+    }
+    __device__ __forceinline__ bool wet(int j, int n) const { return P[n].wet != 0; }
+};
+
+// Tile staging of the cell sweep: per thread, its cell's CSR entries in
+// entry-major slots [j][thread] (consecutive threads read consecutive
+// records: no bank conflicts); the wet bit of the other cell rides in bit 5
+// of the flags.
+constexpr int CELL_TILE = 128;
+constexpr int WET_BIT = 32;
+template <int MAXF>
+struct CellStage {
+    float4 pn[MAXF][CELL_TILE];
+    float4 ge[MAXF][CELL_TILE];
+    int2 id[MAXF][CELL_TILE];
+    float db[MAXF][CELL_TILE];
+};
+
+template <int MAXF>
+struct StagedEntries {
+    const CellStage<MAXF> &S;
+    int t;
+    __device__ __forceinline__ int2 id(int j) const { return S.id[j][t]; }
+    __device__ __forceinline__ float4 ge(int j) const { return S.ge[j][t]; }
+    __device__ __forceinline__ float db(int j) const { return S.db[j][t]; }
+    __device__ __forceinline__ float4 pn(int j, int) const { return S.pn[j][t]; }
+    __device__ __forceinline__ bool wet(int j, int) const { return (S.id[j][t].y & WET_BIT) != 0; }
+};
+
 // Wet least-squares gradients of u, v and the surface for the rotor face
 // terms (river_turbine_flow.h:13-35): wet neighbours only, weights 1/|d|^2 of
 // the flow metric's centre offsets. Called in the cell sweep's tail, after
-// the cell record is written, so its sums are not live in the limiter; the
-// neighbour primitives were just read and come from L1.
-__device__ __forceinline__ void hkt_cell_gradients(const MeshDev &m, const MixedGeo &g, const MxPrim *P,
-                                                   const MxPrim &pc, int c, int nc)
+// the cell record is written, so its sums are not live in the limiter.
+template <class E>
+__device__ __forceinline__ void hkt_cell_gradients(const MeshDev &m, const MixedGeo &g, const E &A, const MxPrim &pc,
+                                                   int c, int deg, int nc)
 {
     float xx = 0.f, xy = 0.f, yy = 0.f, bx[3] = {0.f, 0.f, 0.f}, by[3] = {0.f, 0.f, 0.f};
+    const int k0 = m.offset[c];
     if (pc.wet)
-        for (int k = m.offset[c]; k < m.offset[c + 1]; ++k) {
-            const int n = g.cidx[k].x;
+        for (int j = 0; j < deg; ++j) {
+            const int n = A.id(j).x;
             if (n < 0) continue;
-            const MxPrim pn = P[n];
-            if (!pn.wet) continue;
-            const float2 d = g.hdxy[k];
+            if (!A.wet(j, n)) continue;
+            const float4 pn = A.pn(j, n);
+            const float2 d = g.hdxy[k0 + j];
             const float w = 1.f / (d.x * d.x + d.y * d.y);
             xx += w * d.x * d.x; xy += w * d.x * d.y; yy += w * d.y * d.y;
-            const float dv[3] = {pn.u - pc.u, pn.v - pc.v, (pn.ehi - pc.ehi) + (pn.elo - pc.elo)};
+            const float dv[3] = {pn.z - pc.u, pn.w - pc.v, (pn.x - pc.ehi) + (pn.y - pc.elo)};
 #pragma unroll
             for (int p = 0; p < 3; ++p) { bx[p] += w * d.x * dv[p]; by[p] += w * d.y * dv[p]; }
         }
@@ -265,6 +312,155 @@ __device__ __forceinline__ void hkt_cell_gradients(const MeshDev &m, const Mixed
     }
 }
 
+// One cell of the cell sweep: limited gradients and the cell record (the
+// reference's reconstruction_cells with the wall_bed_hydraulics transforms,
+// reconstruction.cu:43-168), reading its CSR entries through A.
+template <int MAXF, class E>
+__device__ __forceinline__ void cell_record(const MeshDev &m, const StateDev &s, const Ctrl &ct, const MixedGeo &g,
+                                            const E &A, const MxPrim &pc, int c, int deg, MxRec *rec)
+{
+    const float dry = ct.dryf;
+    const bool wet = pc.wet != 0;
+    const float hf = pc.h, u = pc.u, v = pc.v;
+    const bool outlet = g.ccls[c] & 1;   // a stage outlet face: the bed gradient is formed here
+    const int k0 = m.offset[c];
+    // bounds of eta and b relative to the cell (centre = 0), of u and v absolute
+    float lo[4] = {0.f, u, v, 0.f}, hi[4] = {0.f, u, v, 0.f};
+    float bx[4] = {0.f, 0.f, 0.f, 0.f}, by[4] = {0.f, 0.f, 0.f, 0.f};
+    bool active = wet;
+    for (int j = 0; j < deg; ++j) {
+        const int2 id = A.id(j);
+        const int n = id.x;
+        if (n < 0) {
+            if (id.y & 1) active = true;
+            else if ((id.y & 4) && wet) {
+                // a wall bounds the velocities by the mirrored cell velocity
+                const float2 nn = g.fnorm[m.faces[k0 + j]];
+                const float un = u * nn.x + v * nn.y;
+                const float mx = u - 2.f * un * nn.x, my = v - 2.f * un * nn.y;
+                lo[1] = fminf(lo[1], mx); hi[1] = fmaxf(hi[1], mx);
+                lo[2] = fminf(lo[2], my); hi[2] = fmaxf(hi[2], my);
+            }
+            continue;
+        }
+        const float4 pn = A.pn(j, n);
+        const bool wetn = A.wet(j, n);
+        if (wetn) active = true;
+        const float ddb = A.db(j);
+        float d[4];
+        d[0] = (pn.x - pc.ehi) + (pn.y - pc.elo);
+        d[1] = pn.z - u;
+        d[2] = pn.w - v;
+        d[3] = ddb;
+        // a dry neighbour whose bed rises above the wet surface contributes the surface
+        if (wet && !wetn && ddb >= hf) d[0] = 0.f;
+        const float4 ge = A.ge(j);     // LS weight * (dx, dy), face displacement
+#pragma unroll
+        for (int p = 0; p < 3; ++p) {
+            bx[p] += ge.x * d[p];
+            by[p] += ge.y * d[p];
+            const float val = (p == 1 || p == 2) ? d[p] + (p == 1 ? u : v) : d[p];
+            lo[p] = fminf(lo[p], val); hi[p] = fmaxf(hi[p], val);
+        }
+        if (outlet) {
+            bx[3] += ge.x * d[3]; by[3] += ge.y * d[3];
+            lo[3] = fminf(lo[3], d[3]); hi[3] = fmaxf(hi[3], d[3]);
+        }
+    }
+    float gx[4] = {0.f, 0.f, 0.f, 0.f}, gy[4] = {0.f, 0.f, 0.f, 0.f};
+    const float4 inv = g.cinv[c];
+    if (active && (inv.x != 0.f || inv.y != 0.f || inv.z != 0.f)) {
+#pragma unroll
+        for (int p = 0; p < 3; ++p) {
+            gx[p] = inv.x * bx[p] + inv.y * by[p];
+            gy[p] = inv.y * bx[p] + inv.z * by[p];
+        }
+        float bedtol = 0.f, sq = 0.f;
+        if (outlet) {
+            gx[3] = inv.x * bx[3] + inv.y * by[3];
+            gy[3] = inv.y * bx[3] + inv.z * by[3];
+            bedtol = 64.f * FEPS * fmaxf(1.f, fabsf(float(s.z[c])));
+            sq = wet ? sqrtf(ct.gravf * hf) : 0.f;
+        } else {
+            const float2 gb = g.gbed[c];
+            gx[3] = gb.x; gy[3] = gb.y;
+        }
+        float theta1 = 1.f, theta2 = 1.f;
+        // one slab set, filled for the surface, then (stage-outlet cells
+        // only) refilled for the bed: half the live registers of two sets
+        Slabs<MAXF> S{};
+        const float b0p = fmaxf(0.f, hi[0]), b0m = fmaxf(0.f, -lo[0]);
+#pragma unroll (MAXF <= 4 ? MAXF : 1)
+        for (int j = 0; j < MAXF; ++j) {
+            if (j >= deg) continue;      // (a break would stop the unrolling)
+            const float4 ge = A.ge(j);
+            const float rx = ge.z, ry = ge.w;
+            if (outlet && (A.id(j).y & 2) && wet) {
+                // an open stage outlet with a subcritical wet owner keeps its bed slope
+                const float2 nn = g.fnorm[m.faces[k0 + j]];
+                if (fabsf(u * nn.x + v * nn.y) < sq && fabsf(gx[3] * rx + gy[3] * ry) > bedtol) continue;
+            }
+#pragma unroll
+            for (int p = 1; p < 3; ++p) {
+                const float dd = gx[p] * rx + gy[p] * ry;
+                const float ctr = p == 1 ? u : v;
+                if (fabsf(dd) <= 64.f * FEPS * fmaxf(1.f, fmaxf(fabsf(ctr), fmaxf(fabsf(lo[p]), fabsf(hi[p])))))
+                    continue;
+                float &th = p == 1 ? theta1 : theta2;
+                if (dd > 0.f) th = fminf(th, (hi[p] - ctr) / dd);
+                if (dd < 0.f) th = fminf(th, (lo[p] - ctr) / dd);
+            }
+            const float len = sqrtf(rx * rx + ry * ry);
+            if (len <= 0.f) continue;
+            const float il = 1.f / len;
+            S.ux[j] = rx * il; S.uy[j] = ry * il; S.bp[j] = b0p * il; S.bm[j] = b0m * il;
+            S.mask |= 1u << j;
+        }
+        if (!slabs_feasible(S, gx[0], gy[0])) slabs_project(S, gx[0], gy[0]);
+        if (outlet) {
+            const float b3p = fmaxf(0.f, hi[3]), b3m = fmaxf(0.f, -lo[3]);
+            S.mask = 0u;
+#pragma unroll (MAXF <= 4 ? MAXF : 1)
+            for (int j = 0; j < MAXF; ++j) {
+                if (j >= deg) continue;
+                const int fl = A.id(j).y;
+                const float4 ge = A.ge(j);
+                const float rx = ge.z, ry = ge.w;
+                if ((fl & 2) && wet) {
+                    const float2 nn = g.fnorm[m.faces[k0 + j]];
+                    if (fabsf(u * nn.x + v * nn.y) < sq && fabsf(gx[3] * rx + gy[3] * ry) > bedtol) continue;
+                }
+                const float len = sqrtf(rx * rx + ry * ry);
+                if (len <= 0.f || (fl & 4)) continue;          // walls do not bound the bed
+                const float il = 1.f / len;
+                S.ux[j] = rx * il; S.uy[j] = ry * il; S.bp[j] = b3p * il; S.bm[j] = b3m * il;
+                S.mask |= 1u << j;
+            }
+            if (!slabs_feasible(S, gx[3], gy[3])) slabs_project(S, gx[3], gy[3]);
+        }
+        gx[1] *= fmaxf(0.f, theta1); gy[1] *= fmaxf(0.f, theta1);
+        gx[2] *= fmaxf(0.f, theta2); gy[2] *= fmaxf(0.f, theta2);
+    }
+    bool flatten = !wet;
+    if (!flatten) {
+        for (int j = 0; j < deg; ++j) {
+            const float4 ge = A.ge(j);
+            const float de = gx[0] * ge.z + gy[0] * ge.w, db = gx[3] * ge.z + gy[3] * ge.w;
+            if (hf + (de - db) <= dry || fabsf(db) >= hf) { flatten = true; break; }
+        }
+    }
+    MxRec r;
+    r.h = hf;
+    r.flags = (flatten ? 1 : 0) | (active ? 2 : 0) | (wet ? 4 : 0);
+    r.ehi = pc.ehi; r.elo = pc.elo; r.u = u; r.v = v;
+#pragma unroll
+    for (int p = 0; p < 4; ++p) { r.gx[p] = gx[p]; r.gy[p] = gy[p]; }
+    r.pad0 = 0.f; r.pad1 = 0.f;
+    rec[c] = r;
+}
+
+// Cell sweep, general polygons (any number of faces up to MAX_CELL_FACES):
+// one thread per cell, entries read from the packed tables as it goes.
 template <int MAXF>
 __global__ void __launch_bounds__(128, BRX_CELLS_MIN_BLOCKS) km_cells(MeshDev m, StateDev s, Ctrl *ctrl, Work w,
                                                                       MixedGeo g, int stage, TurbDev t, int turb)
@@ -275,150 +471,65 @@ __global__ void __launch_bounds__(128, BRX_CELLS_MIN_BLOCKS) km_cells(MeshDev m,
     FOR_ACTIVE_CELLS(m.act, c) {
         const Ctrl &ct = ctrl[m.cell_sid[c]];
         if (mx_skip(ct, stage)) continue;
-        const float dry = ct.dryf;
         const MxPrim pc = P[c];
-        const bool wet = pc.wet != 0;
-        const float hf = pc.h, u = pc.u, v = pc.v;
-        const bool outlet = g.ccls[c] & 1;   // a stage outlet face: the bed gradient is formed here
-        // bounds of eta and b relative to the cell (centre = 0), of u and v absolute
-        float lo[4] = {0.f, u, v, 0.f}, hi[4] = {0.f, u, v, 0.f};
-        float bx[4] = {0.f, 0.f, 0.f, 0.f}, by[4] = {0.f, 0.f, 0.f, 0.f};
         const int k0 = m.offset[c], deg = m.offset[c + 1] - k0;
-        bool active = wet;
-        for (int k = k0; k < k0 + deg; ++k) {
-            const int2 id = g.cidx[k];
-            const int n = id.x;
-            if (n < 0) {
-                if (id.y & 1) active = true;
-                else if ((id.y & 4) && wet) {
-                    // a wall bounds the velocities by the mirrored cell velocity
-                    const float2 nn = g.fnorm[m.faces[k]];
-                    const float un = u * nn.x + v * nn.y;
-                    const float mx = u - 2.f * un * nn.x, my = v - 2.f * un * nn.y;
-                    lo[1] = fminf(lo[1], mx); hi[1] = fmaxf(hi[1], mx);
-                    lo[2] = fminf(lo[2], my); hi[2] = fmaxf(hi[2], my);
-                }
-                continue;
-            }
-            const MxPrim pn = P[n];
-            const bool wetn = pn.wet != 0;
-            if (wetn) active = true;
-            const float ddb = g.cdb[k];
-            float d[4];
-            d[0] = (pn.ehi - pc.ehi) + (pn.elo - pc.elo);
-            d[1] = pn.u - u;
-            d[2] = pn.v - v;
-            d[3] = ddb;
-            // a dry neighbour whose bed rises above the wet surface contributes the surface
-            if (wet && !wetn && ddb >= hf) d[0] = 0.f;
-            const float4 ge = g.cent[k];     // LS weight * (dx, dy), face displacement
-#pragma unroll
-            for (int p = 0; p < 3; ++p) {
-                bx[p] += ge.x * d[p];
-                by[p] += ge.y * d[p];
-                const float val = (p == 1 || p == 2) ? d[p] + (p == 1 ? u : v) : d[p];
-                lo[p] = fminf(lo[p], val); hi[p] = fmaxf(hi[p], val);
-            }
-            if (outlet) {
-                bx[3] += ge.x * d[3]; by[3] += ge.y * d[3];
-                lo[3] = fminf(lo[3], d[3]); hi[3] = fmaxf(hi[3], d[3]);
-            }
-        }
-        float gx[4] = {0.f, 0.f, 0.f, 0.f}, gy[4] = {0.f, 0.f, 0.f, 0.f};
-        const float4 inv = g.cinv[c];
-        if (active && (inv.x != 0.f || inv.y != 0.f || inv.z != 0.f)) {
-#pragma unroll
-            for (int p = 0; p < 3; ++p) {
-                gx[p] = inv.x * bx[p] + inv.y * by[p];
-                gy[p] = inv.y * bx[p] + inv.z * by[p];
-            }
-            float bedtol = 0.f, sq = 0.f;
-            if (outlet) {
-                gx[3] = inv.x * bx[3] + inv.y * by[3];
-                gy[3] = inv.y * bx[3] + inv.z * by[3];
-                bedtol = 64.f * FEPS * fmaxf(1.f, fabsf(float(s.z[c])));
-                sq = wet ? sqrtf(ct.gravf * hf) : 0.f;
-            } else {
-                const float2 gb = g.gbed[c];
-                gx[3] = gb.x; gy[3] = gb.y;
-            }
-            float theta1 = 1.f, theta2 = 1.f;
-            // one slab set, filled for the surface, then (stage-outlet cells
-            // only) refilled for the bed: half the live registers of two sets
-            Slabs<MAXF> S{};
-            const float b0p = fmaxf(0.f, hi[0]), b0m = fmaxf(0.f, -lo[0]);
-#pragma unroll (MAXF <= 4 ? MAXF : 1)
-            for (int j = 0; j < MAXF; ++j) {
-                if (j >= deg) continue;      // (a break would stop the unrolling)
-                const int k = k0 + j;
-                const float4 ge = g.cent[k];
-                const float rx = ge.z, ry = ge.w;
-                if (outlet && (g.cidx[k].y & 2) && wet) {
-                    // an open stage outlet with a subcritical wet owner keeps its bed slope
-                    const float2 nn = g.fnorm[m.faces[k]];
-                    if (fabsf(u * nn.x + v * nn.y) < sq && fabsf(gx[3] * rx + gy[3] * ry) > bedtol) continue;
-                }
-#pragma unroll
-                for (int p = 1; p < 3; ++p) {
-                    const float dd = gx[p] * rx + gy[p] * ry;
-                    const float ctr = p == 1 ? u : v;
-                    if (fabsf(dd) <= 64.f * FEPS * fmaxf(1.f, fmaxf(fabsf(ctr), fmaxf(fabsf(lo[p]), fabsf(hi[p])))))
-                        continue;
-                    float &th = p == 1 ? theta1 : theta2;
-                    if (dd > 0.f) th = fminf(th, (hi[p] - ctr) / dd);
-                    if (dd < 0.f) th = fminf(th, (lo[p] - ctr) / dd);
-                }
-                const float len = sqrtf(rx * rx + ry * ry);
-                if (len <= 0.f) continue;
-                const float il = 1.f / len;
-                S.ux[j] = rx * il; S.uy[j] = ry * il; S.bp[j] = b0p * il; S.bm[j] = b0m * il;
-                S.mask |= 1u << j;
-            }
-            if (!slabs_feasible(S, gx[0], gy[0])) slabs_project(S, gx[0], gy[0]);
-            if (outlet) {
-                const float b3p = fmaxf(0.f, hi[3]), b3m = fmaxf(0.f, -lo[3]);
-                S.mask = 0u;
-#pragma unroll (MAXF <= 4 ? MAXF : 1)
-                for (int j = 0; j < MAXF; ++j) {
-                    if (j >= deg) continue;
-                    const int k = k0 + j;
-                    const int fl = g.cidx[k].y;
-                    const float4 ge = g.cent[k];
-                    const float rx = ge.z, ry = ge.w;
-                    if ((fl & 2) && wet) {
-                        const float2 nn = g.fnorm[m.faces[k]];
-                        if (fabsf(u * nn.x + v * nn.y) < sq && fabsf(gx[3] * rx + gy[3] * ry) > bedtol) continue;
-                    }
-                    const float len = sqrtf(rx * rx + ry * ry);
-                    if (len <= 0.f || (fl & 4)) continue;          // walls do not bound the bed
-                    const float il = 1.f / len;
-                    S.ux[j] = rx * il; S.uy[j] = ry * il; S.bp[j] = b3p * il; S.bm[j] = b3m * il;
-                    S.mask |= 1u << j;
-                }
-                if (!slabs_feasible(S, gx[3], gy[3])) slabs_project(S, gx[3], gy[3]);
-            }
-            gx[1] *= fmaxf(0.f, theta1); gy[1] *= fmaxf(0.f, theta1);
-            gx[2] *= fmaxf(0.f, theta2); gy[2] *= fmaxf(0.f, theta2);
-        }
-        bool flatten = !wet;
-        if (!flatten) {
-            for (int k = k0; k < k0 + deg; ++k) {
-                const float4 ge = g.cent[k];
-                const float de = gx[0] * ge.z + gy[0] * ge.w, db = gx[3] * ge.z + gy[3] * ge.w;
-                if (hf + (de - db) <= dry || fabsf(db) >= hf) { flatten = true; break; }
-            }
-        }
-        MxRec r;
-        r.h = hf;
-        r.flags = (flatten ? 1 : 0) | (active ? 2 : 0) | (wet ? 4 : 0);
-        r.ehi = pc.ehi; r.elo = pc.elo; r.u = u; r.v = v;
-#pragma unroll
-        for (int p = 0; p < 4; ++p) { r.gx[p] = gx[p]; r.gy[p] = gy[p]; }
-        r.pad0 = 0.f; r.pad1 = 0.f;
-        rec[c] = r;
-        if (turb && t.hkt[m.cell_sid[c]]) hkt_cell_gradients(m, g, P, pc, c, nc);
+        const GlobalEntries A{g, P, k0};
+        cell_record<MAXF>(m, s, ct, g, A, pc, c, deg, rec);
+        if (turb && t.hkt[m.cell_sid[c]]) hkt_cell_gradients(m, g, A, pc, c, deg, nc);
     }
 }
+
+// Cell sweep of meshes with at most MAXF (4) faces per cell, one tile of up
+// to CELL_TILE active cells per block and grid-stride step. Every thread
+// first issues the loads of its cell's entries (the other cell, geometry,
+// bed difference) and then of the other cells' primitives, all independent,
+// into its shared-memory slots; only then does it reconstruct. The cell
+// sweep otherwise walks a chain of dependent global loads per entry
+// (offset -> entry -> neighbour), which left it waiting on memory; here one
+// round trip covers all of a cell's neighbours. Results are those of
+// km_cells bit for bit (the same arithmetic on the same values).
+template <int MAXF>
+__global__ void __launch_bounds__(CELL_TILE, BRX_CELLS_MIN_BLOCKS) km_cells_tile(MeshDev m, StateDev s, Ctrl *ctrl,
+                                                                                Work w, MixedGeo g, int stage,
+                                                                                TurbDev t, int turb)
+{
+    __shared__ CellStage<MAXF> S;
+    const int nc = m.nc;
+    MxRec *rec = reinterpret_cast<MxRec *>(w.rec);
+    const MxPrim *P = reinterpret_cast<const MxPrim *>((stage == 1 ? g.prim[0] : g.prim[1]));
+    const int tid = threadIdx.x;
+    FOR_ACTIVE_CELLS(m.act, c) {
+        const int sid = m.cell_sid[c];
+        const Ctrl &ct = ctrl[sid];
+        if (mx_skip(ct, stage)) continue;
+        const int k0 = m.offset[c], deg = m.offset[c + 1] - k0;
+        const MxPrim pc = P[c];
+        int2 id[MAXF];
+#pragma unroll
+        for (int j = 0; j < MAXF; ++j)
+            if (j < deg) {
+                id[j] = g.cidx[k0 + j];
+                S.ge[j][tid] = g.cent[k0 + j];
+                S.db[j][tid] = g.cdb[k0 + j];
+            }
+#pragma unroll
+        for (int j = 0; j < MAXF; ++j)
+            if (j < deg) {
+                int2 e = id[j];
+                if (e.x >= 0) {
+                    const MxPrim q = P[e.x];
+                    S.pn[j][tid] = make_float4(q.ehi, q.elo, q.u, q.v);
+                    if (q.wet) e.y |= WET_BIT;
+                }
+                S.id[j][tid] = e;
+            }
+        // each thread reads only its own slots: no barrier needed
+        const StagedEntries<MAXF> A{S, tid};
+        cell_record<MAXF>(m, s, ct, g, A, pc, c, deg, rec);
+        if (turb && t.hkt[sid]) hkt_cell_gradients(m, g, A, pc, c, deg, nc);
+    }
+}
+
 
 // ---------------------------------------------------------------------------
 // Faces
@@ -1015,7 +1126,7 @@ int mixed_max_block(int kind, int maxdeg)
     const void *fn = nullptr;
     switch (kind) {
     case K_DRAG: fn = (const void *)brx_mx::km_open_drag; break;
-    case K_CELLS: fn = small ? (const void *)brx_mx::km_cells<4> : (const void *)brx_mx::km_cells<MAX_CELL_FACES>; break;
+    case K_CELLS: fn = small ? (const void *)brx_mx::km_cells_tile<4> : (const void *)brx_mx::km_cells<MAX_CELL_FACES>; break;
     case K_FACES: fn = (const void *)brx_mx::km_faces; break;
     case K_GATHER: fn = (const void *)brx_mx::km_gather; break;
     case K_LIMIT: fn = (const void *)brx_mx::km_limit; break;
@@ -1043,7 +1154,7 @@ int mixed_kernel(const Launch &L, int kind, int stage, double *out)
         return 1;
     case K_CELLS:
         if (small)
-            brx_mx::km_cells<4><<<SHAPE(K_CELLS, nc), 0, st>>>(L.mesh, L.state, L.ctrl, L.work, L.mx, stage, L.turb,
+            brx_mx::km_cells_tile<4><<<SHAPE(K_CELLS, nc), 0, st>>>(L.mesh, L.state, L.ctrl, L.work, L.mx, stage, L.turb,
                                                               L.has_turb);
         else
             brx_mx::km_cells<MAX_CELL_FACES><<<SHAPE(K_CELLS, nc), 0, st>>>(L.mesh, L.state, L.ctrl, L.work, L.mx,
