@@ -72,6 +72,50 @@ __device__ __forceinline__ bool le_threshold(double x, double threshold)
     return __double_as_longlong(x) <= __double_as_longlong(threshold);
 }
 
+// x < 0 as a compare of the bit pattern (false for -0 and NaN, as the FP64
+// compare): the sign bit with a magnitude in (0, inf].
+__device__ __forceinline__ bool lt_zero(double x)
+{
+    const long long b = __double_as_longlong(x);
+    const long long mag = b & 0x7fffffffffffffffLL;
+    return b < 0 && mag != 0 && mag <= 0x7ff0000000000000LL;
+}
+
+// Float <-> double conversions on the integer pipe. This part issues FP64
+// instructions, conversions included, at about two lanes per clock per SM,
+// a few percent of its integer rate, and the update and drag sweeps spent
+// half of their FP64 issue slots converting between the FP32 sweep values
+// and the FP64 state. These re-encode the IEEE bit patterns exactly (float
+// to double is exact; double to float rounds to nearest even, as the
+// hardware conversion does); zeros take the same integer path, and the rare
+// operands outside the float normal range (subnormals, results that would
+// underflow or overflow, infinities, NaN) take the hardware conversion, so
+// every result equals the hardware's bit for bit.
+__device__ __forceinline__ double f2d(float f)
+{
+    const unsigned b = __float_as_uint(f);
+    const unsigned e = (b >> 23) & 0xffu;
+    if ((b & 0x7fffffffu) == 0u) return __hiloint2double((int)(b & 0x80000000u), 0);
+    if (e == 0u || e == 0xffu) return double(f);
+    const unsigned hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3);
+    return __hiloint2double((int)hi, (int)(b << 29));
+}
+
+__device__ __forceinline__ float d2f(double x)
+{
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    if (((hi & 0x7fffffffu) | lo) == 0u) return __uint_as_float(hi & 0x80000000u);
+    const unsigned e = (hi >> 20) & 0x7ffu;
+    if (e < 897u || e > 1150u) return float(x);
+    // 52-bit fraction: its top 23 bits are kept, the low 29 decide the rounding
+    const unsigned top = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const unsigned rem = lo & 0x1fffffffu;
+    unsigned r = (hi & 0x80000000u) | ((e - 896u) << 23) | top;
+    // to nearest, ties to even; a carry into the exponent is the correct result (up to infinity)
+    if (rem > 0x10000000u || (rem == 0x10000000u && (top & 1u))) r += 1u;
+    return __uint_as_float(r);
+}
+
 // Stage 2 skips a scenario whose first stage failed (status, or the CFL test
 // evaluated once per scenario after the first gather).
 __device__ __forceinline__ bool mx_skip(const Ctrl &c, int stage)
@@ -85,16 +129,16 @@ __device__ __forceinline__ bool put_prim(MxPrim *P, int c, double h, double hu, 
 {
     const double eta = h + z;
     MxPrim p;
-    p.ehi = float(eta);
-    p.elo = float(eta - double(p.ehi));
-    p.h = float(h);
+    p.ehi = d2f(eta);
+    p.elo = d2f(eta - f2d(p.ehi));
+    p.h = d2f(h);
     const bool wet = !le_threshold(h, dry);
-    p.u = wet ? float(hu) / p.h : 0.f;
-    p.v = wet ? float(hv) / p.h : 0.f;
+    p.u = wet ? d2f(hu) / p.h : 0.f;
+    p.v = wet ? d2f(hv) / p.h : 0.f;
     p.wet = wet;
     p.pad0 = 0.f; p.pad1 = 0.f;
     P[c] = p;
-    return !(h < 0.0) && finite64(h) && finite64(hu) && finite64(hv) && finite64(z);
+    return !lt_zero(h) && finite64(h) && finite64(hu) && finite64(hv) && finite64(z);
 }
 
 // Per-scenario CFL peak: FP32 warp maximum, one atomic per scenario group.
@@ -237,8 +281,7 @@ __global__ void __launch_bounds__(128) km_bed(MeshDev m, StateDev s, MixedGeo g)
 // CSR entries of one cell as the cell sweep reads them: the other cell and
 // its flags, the LS weight x offset and face displacement, the bed
 // difference, and the other cell's stage primitives (wet bit, eta pair,
-// velocities). GlobalEntries reads them from the packed tables as it goes;
-// StagedEntries from the tile's shared-memory copy (km_cells_tile).
+// velocities), read from the packed tables as the sweep goes.
 struct GlobalEntries {
     const MixedGeo &g;
     const MxPrim *P;
@@ -253,31 +296,6 @@ struct GlobalEntries {
         return make_float4(q.ehi, q.elo, q.u, q.v);
     }
     __device__ __forceinline__ bool wet(int j, int n) const { return P[n].wet != 0; }
-};
-
-// Tile staging of the cell sweep: per thread, its cell's CSR entries in
-// entry-major slots [j][thread] (consecutive threads read consecutive
-// records: no bank conflicts); the wet bit of the other cell rides in bit 5
-// of the flags.
-constexpr int CELL_TILE = 128;
-constexpr int WET_BIT = 32;
-template <int MAXF>
-struct CellStage {
-    float4 pn[MAXF][CELL_TILE];
-    float4 ge[MAXF][CELL_TILE];
-    int2 id[MAXF][CELL_TILE];
-    float db[MAXF][CELL_TILE];
-};
-
-template <int MAXF>
-struct StagedEntries {
-    const CellStage<MAXF> &S;
-    int t;
-    __device__ __forceinline__ int2 id(int j) const { return S.id[j][t]; }
-    __device__ __forceinline__ float4 ge(int j) const { return S.ge[j][t]; }
-    __device__ __forceinline__ float db(int j) const { return S.db[j][t]; }
-    __device__ __forceinline__ float4 pn(int j, int) const { return S.pn[j][t]; }
-    __device__ __forceinline__ bool wet(int j, int) const { return (S.id[j][t].y & WET_BIT) != 0; }
 };
 
 // Wet least-squares gradients of u, v and the surface for the rotor face
@@ -478,58 +496,6 @@ __global__ void __launch_bounds__(128, BRX_CELLS_MIN_BLOCKS) km_cells(MeshDev m,
         if (turb && t.hkt[m.cell_sid[c]]) hkt_cell_gradients(m, g, A, pc, c, deg, nc);
     }
 }
-
-// Cell sweep of meshes with at most MAXF (4) faces per cell, one tile of up
-// to CELL_TILE active cells per block and grid-stride step. Every thread
-// first issues the loads of its cell's entries (the other cell, geometry,
-// bed difference) and then of the other cells' primitives, all independent,
-// into its shared-memory slots; only then does it reconstruct. The cell
-// sweep otherwise walks a chain of dependent global loads per entry
-// (offset -> entry -> neighbour), which left it waiting on memory; here one
-// round trip covers all of a cell's neighbours. Results are those of
-// km_cells bit for bit (the same arithmetic on the same values).
-template <int MAXF>
-__global__ void __launch_bounds__(CELL_TILE, BRX_CELLS_MIN_BLOCKS) km_cells_tile(MeshDev m, StateDev s, Ctrl *ctrl,
-                                                                                Work w, MixedGeo g, int stage,
-                                                                                TurbDev t, int turb)
-{
-    __shared__ CellStage<MAXF> S;
-    const int nc = m.nc;
-    MxRec *rec = reinterpret_cast<MxRec *>(w.rec);
-    const MxPrim *P = reinterpret_cast<const MxPrim *>((stage == 1 ? g.prim[0] : g.prim[1]));
-    const int tid = threadIdx.x;
-    FOR_ACTIVE_CELLS(m.act, c) {
-        const int sid = m.cell_sid[c];
-        const Ctrl &ct = ctrl[sid];
-        if (mx_skip(ct, stage)) continue;
-        const int k0 = m.offset[c], deg = m.offset[c + 1] - k0;
-        const MxPrim pc = P[c];
-        int2 id[MAXF];
-#pragma unroll
-        for (int j = 0; j < MAXF; ++j)
-            if (j < deg) {
-                id[j] = g.cidx[k0 + j];
-                S.ge[j][tid] = g.cent[k0 + j];
-                S.db[j][tid] = g.cdb[k0 + j];
-            }
-#pragma unroll
-        for (int j = 0; j < MAXF; ++j)
-            if (j < deg) {
-                int2 e = id[j];
-                if (e.x >= 0) {
-                    const MxPrim q = P[e.x];
-                    S.pn[j][tid] = make_float4(q.ehi, q.elo, q.u, q.v);
-                    if (q.wet) e.y |= WET_BIT;
-                }
-                S.id[j][tid] = e;
-            }
-        // each thread reads only its own slots: no barrier needed
-        const StagedEntries<MAXF> A{S, tid};
-        cell_record<MAXF>(m, s, ct, g, A, pc, c, deg, rec);
-        if (turb && t.hkt[sid]) hkt_cell_gradients(m, g, A, pc, c, deg, nc);
-    }
-}
-
 
 // ---------------------------------------------------------------------------
 // Faces
@@ -942,7 +908,7 @@ __global__ void __launch_bounds__(256) km_limit(MeshDev m, Ctrl *ctrl, Work w, M
 __device__ __forceinline__ void drag_f(const Ctrl &ct, float dtf, double &h, double &hu, double &hv)
 {
     if (le_threshold(h, ct.dry)) { hu = 0.; hv = 0.; return; }
-    const float hf = float(h), uf = float(hu), vf = float(hv);
+    const float hf = d2f(h), uf = d2f(hu), vf = d2f(hv);
     float c;
     const float val = ct.roughf;
     if (ct.roughness_mode == 1) c = val;
@@ -951,8 +917,9 @@ __device__ __forceinline__ void drag_f(const Ctrl &ct, float dtf, double &h, dou
     else c = 18.f * log10f(12.f * fmaxf(.5f, hf / val));
     const float speed = sqrtf(uf * uf + vf * vf) / hf;
     const float factor = 1.f / (1.f + dtf * ct.gravf * speed / (c * c * hf));
-    hu *= factor;
-    hv *= factor;
+    const double fd = f2d(factor);
+    hu *= fd;
+    hv *= fd;
 }
 
 // Update (owner computes): each cell forms the donor-limited water flux of
@@ -985,7 +952,7 @@ __global__ void __launch_bounds__(256) km_update(MeshDev m, StateDev s, Ctrl *ct
         for (int k = m.offset[c]; k < m.offset[c + 1]; ++k) {
             const float wf = ws[m.faces[k]].x;
             const float wk = g.cw4[k];
-            double water = double(wf);
+            double water = f2d(wf);
             if (wf != 0.f) {
                 const int2 id = g.cidx[k];
                 // the donor is the owner for outward (positive) water, else the neighbour
@@ -994,7 +961,7 @@ __global__ void __launch_bounds__(256) km_update(MeshDev m, StateDev s, Ctrl *ct
                     const float th = theta32[donor];
                     if (th != 1.f) {
                         const float delta = (th - 1.f) * wf;
-                        water = double(wf) * double(th);          // exact product
+                        water = f2d(wf) * f2d(th);                // exact product
                         const MxPrim pd = P[donor];
                         if (pd.wet) { mx -= wk * (delta * pd.u); my -= wk * (delta * pd.v); }
                     }
@@ -1016,12 +983,12 @@ __global__ void __launch_bounds__(256) km_update(MeshDev m, StateDev s, Ctrl *ct
             }
             float x = 0.f, y = 0.f;
             for (int k = k0; k < k1; ++k) { const float2 v = g.hp[m.faces[k]]; x += g.cw4[k] * v.x; y += g.cw4[k] * v.y; }
-            r1 = double(f1 + x);
-            r2 = double(f2 + y);
+            r1 = f2d(f1 + x);
+            r2 = f2d(f2 + y);
             if (t.foot[c]) { r1 += t.raw[c]; r2 += t.raw[nc + c]; }
         } else {
-            r1 = double(f1);
-            r2 = double(f2);
+            r1 = f2d(f1);
+            r2 = f2d(f2);
         }
         if (!finite64(mass) || !finite64(r1) || !finite64(r2)) raise_status(ct, stage, ST_RATE);
         if (rate_out) { rate_out[c] = mass; rate_out[nc + c] = r1; rate_out[2 * nc + c] = r2; continue; }
@@ -1029,16 +996,16 @@ __global__ void __launch_bounds__(256) km_update(MeshDev m, StateDev s, Ctrl *ct
         if (stage == 1) {
             const double h = s.work[c] + dt * mass;
             double hu = s.work[nc + c] + dt * r1, hv = s.work[2 * nc + c] + dt * r2;
-            if (h < 0) raise_status(ct, 1, ST_ENDPOINT);
+            if (lt_zero(h)) raise_status(ct, 1, ST_ENDPOINT);
             if (le_threshold(h, dry)) { hu = 0.; hv = 0.; }
             s.q1[c] = h; s.q1[nc + c] = hu; s.q1[2 * nc + c] = hv;
             // the second stage's input; an invalid one fails that stage
-            if (!put_prim(P2, c, h, hu, hv, s.z[c], dry) && !(h < 0)) raise_status(ct, 2, ST_SPATIAL);
+            if (!put_prim(P2, c, h, hu, hv, s.z[c], dry) && !lt_zero(h)) raise_status(ct, 2, ST_SPATIAL);
         } else {
             double h = .5 * s.work[c] + .5 * (s.q1[c] + dt * mass);
             double hu = .5 * s.work[nc + c] + .5 * (s.q1[nc + c] + dt * r1);
             double hv = .5 * s.work[2 * nc + c] + .5 * (s.q1[2 * nc + c] + dt * r2);
-            if (!finite64(h) || !finite64(hu) || !finite64(hv) || h < 0) raise_status(ct, 2, ST_ENDPOINT);
+            if (!finite64(h) || !finite64(hu) || !finite64(hv) || lt_zero(h)) raise_status(ct, 2, ST_ENDPOINT);
             if (le_threshold(h, dry)) { hu = 0.; hv = 0.; }
             drag_f(ct, .5f * ct.trialf, h, hu, hv);
             double *qn = ct.cur ? s.q[0] : s.q[1];
@@ -1063,11 +1030,11 @@ __global__ void __launch_bounds__(256) km_open_drag(MeshDev m, StateDev s, Ctrl 
         const double h = q[c], z = s.z[c];
         double hu = q[nc + c], hv = q[2 * nc + c];
         const bool wet = !le_threshold(h, ct.dry);
-        const float hf = float(h);
+        const float hf = d2f(h);
         float uf = 0.f, vf = 0.f;
         if (!wet) { hu = 0.; hv = 0.; }
         else {
-            const float mu = float(hu), mv = float(hv);
+            const float mu = d2f(hu), mv = d2f(hv);
             float cz;
             const float val = ct.roughf;
             if (ct.roughness_mode == 1) cz = val;
@@ -1076,19 +1043,19 @@ __global__ void __launch_bounds__(256) km_open_drag(MeshDev m, StateDev s, Ctrl 
             else cz = 18.f * log10f(12.f * fmaxf(.5f, hf / val));
             const float speed = sqrtf(mu * mu + mv * mv) / hf;
             const float factor = 1.f / (1.f + .5f * ct.trialf * ct.gravf * speed / (cz * cz * hf));
-            const double fd = double(factor);
+            const double fd = f2d(factor);
             hu *= fd; hv *= fd;
             uf = mu * factor / hf; vf = mv * factor / hf;
         }
         s.work[c] = h; s.work[nc + c] = hu; s.work[2 * nc + c] = hv;
         const double eta = h + z;
         MxPrim p;
-        p.ehi = float(eta);
-        p.elo = float(eta - double(p.ehi));
+        p.ehi = d2f(eta);
+        p.elo = d2f(eta - f2d(p.ehi));
         p.h = hf; p.u = uf; p.v = vf; p.wet = wet;
         p.pad0 = 0.f; p.pad1 = 0.f;
         P1[c] = p;
-        if (!(!(h < 0.0) && finite64(h) && finite64(hu) && finite64(hv) && finite64(z))) raise_status(ct, 1, ST_SPATIAL);
+        if (!(!lt_zero(h) && finite64(h) && finite64(hu) && finite64(hv) && finite64(z))) raise_status(ct, 1, ST_SPATIAL);
     }
 }
 
@@ -1126,7 +1093,7 @@ int mixed_max_block(int kind, int maxdeg)
     const void *fn = nullptr;
     switch (kind) {
     case K_DRAG: fn = (const void *)brx_mx::km_open_drag; break;
-    case K_CELLS: fn = small ? (const void *)brx_mx::km_cells_tile<4> : (const void *)brx_mx::km_cells<MAX_CELL_FACES>; break;
+    case K_CELLS: fn = small ? (const void *)brx_mx::km_cells<4> : (const void *)brx_mx::km_cells<MAX_CELL_FACES>; break;
     case K_FACES: fn = (const void *)brx_mx::km_faces; break;
     case K_GATHER: fn = (const void *)brx_mx::km_gather; break;
     case K_LIMIT: fn = (const void *)brx_mx::km_limit; break;
@@ -1154,7 +1121,7 @@ int mixed_kernel(const Launch &L, int kind, int stage, double *out)
         return 1;
     case K_CELLS:
         if (small)
-            brx_mx::km_cells_tile<4><<<SHAPE(K_CELLS, nc), 0, st>>>(L.mesh, L.state, L.ctrl, L.work, L.mx, stage, L.turb,
+            brx_mx::km_cells<4><<<SHAPE(K_CELLS, nc), 0, st>>>(L.mesh, L.state, L.ctrl, L.work, L.mx, stage, L.turb,
                                                               L.has_turb);
         else
             brx_mx::km_cells<MAX_CELL_FACES><<<SHAPE(K_CELLS, nc), 0, st>>>(L.mesh, L.state, L.ctrl, L.work, L.mx,
