@@ -62,57 +62,91 @@ struct __align__(16) MxLim {
     float cx, cy;                // momentum correction
 };
 
-__device__ __forceinline__ bool finite64(double x) { return (__double2hiint(x) & 0x7ff00000) != 0x7ff00000; }
-// x <= threshold for a positive finite threshold, as a signed 64-bit compare of
-// the bit patterns (the order of non-NaN doubles against a positive value; a
-// NaN depth fails the state's finiteness check wherever this is used). FP64
-// compares issue on the FP64 pipe, a few per clock per SM on this part.
+// Bit-level tests and conversions of FP64 values on the integer pipe. This
+// part issues FP64 instructions (compares and conversions included) at about
+// two lanes per clock per SM, a few percent of its integer rate, and the
+// update and drag sweeps spent most of their FP64 issue slots on compares
+// and conversions between the FP32 sweep values and the FP64 state. The
+// 64-bit register is split and joined with inline mov.b64, which the
+// optimizer treats as opaque, so it cannot fold these tests back into FP64
+// compares and conversions.
+__device__ __forceinline__ void dsplit(double x, unsigned &hi, unsigned &lo)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=r"(lo), "=r"(hi) : "d"(x));
+}
+__device__ __forceinline__ double djoin(unsigned hi, unsigned lo)
+{
+    double x;
+    asm("mov.b64 %0, {%1, %2};" : "=d"(x) : "r"(lo), "r"(hi));
+    return x;
+}
+
+// x is neither infinite nor NaN
+__device__ __forceinline__ bool finite64(double x)
+{
+    unsigned hi, lo;
+    dsplit(x, hi, lo);
+    return (hi & 0x7ff00000u) != 0x7ff00000u;
+}
+
+// x <= threshold for a positive finite threshold, as a signed 64-bit compare
+// of the bit patterns (the order of non-NaN doubles against a positive
+// value; a NaN depth fails the state's finiteness check wherever this is used)
 __device__ __forceinline__ bool le_threshold(double x, double threshold)
 {
-    return __double_as_longlong(x) <= __double_as_longlong(threshold);
+    unsigned xh, xl, th, tl;
+    dsplit(x, xh, xl);
+    dsplit(threshold, th, tl);
+    return (int)xh < (int)th || (xh == th && xl <= tl);
 }
 
-// x < 0 as a compare of the bit pattern (false for -0 and NaN, as the FP64
-// compare): the sign bit with a magnitude in (0, inf].
+// x < 0 (false for -0 and NaN, as the FP64 compare): the sign bit with a
+// magnitude in (0, inf]
 __device__ __forceinline__ bool lt_zero(double x)
 {
-    const long long b = __double_as_longlong(x);
-    const long long mag = b & 0x7fffffffffffffffLL;
-    return b < 0 && mag != 0 && mag <= 0x7ff0000000000000LL;
+    unsigned hi, lo;
+    dsplit(x, hi, lo);
+    const unsigned mh = hi & 0x7fffffffu;
+    return (int)hi < 0 && (mh | lo) != 0u && (mh < 0x7ff00000u || (mh == 0x7ff00000u && lo == 0u));
 }
 
-// Float <-> double conversions on the integer pipe. This part issues FP64
-// instructions, conversions included, at about two lanes per clock per SM,
-// a few percent of its integer rate, and the update and drag sweeps spent
-// half of their FP64 issue slots converting between the FP32 sweep values
-// and the FP64 state. These re-encode the IEEE bit patterns exactly (float
-// to double is exact; double to float rounds to nearest even, as the
-// hardware conversion does); zeros take the same integer path, and the rare
-// operands outside the float normal range (subnormals, results that would
-// underflow or overflow, infinities, NaN) take the hardware conversion, so
-// every result equals the hardware's bit for bit.
+// float -> double, exact (every float is a double): the sign, the exponent
+// rebased by 1023 - 127, the 23 fraction bits at the top of the 52;
+// subnormals normalised; infinities and NaN keep their payload.
 __device__ __forceinline__ double f2d(float f)
 {
     const unsigned b = __float_as_uint(f);
-    const unsigned e = (b >> 23) & 0xffu;
-    if ((b & 0x7fffffffu) == 0u) return __hiloint2double((int)(b & 0x80000000u), 0);
-    if (e == 0u || e == 0xffu) return double(f);
-    const unsigned hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3);
-    return __hiloint2double((int)hi, (int)(b << 29));
+    const unsigned sign = b & 0x80000000u, e = (b >> 23) & 0xffu, m = b & 0x7fffffu;
+    unsigned hi = sign | ((e + 896u) << 20) | (m >> 3), lo = m << 29;
+    if (e == 0xffu) hi = sign | 0x7ff00000u | (m >> 3);
+    if (e == 0u) {
+        if (m == 0u) { hi = sign; lo = 0u; }
+        else {
+            const int p = 31 - __clz(m);                       // leading bit of the subnormal fraction
+            const unsigned long long frac = (unsigned long long)(m ^ (1u << p)) << (52 - p);
+            hi = sign | ((unsigned)(p + 874) << 20) | (unsigned)(frac >> 32);
+            lo = (unsigned)frac;
+        }
+    }
+    return djoin(hi, lo);
 }
 
+// double -> float, to nearest with ties to even, as this unit's flush-to-zero
+// conversion: the top 23 of the 52 fraction bits kept and the low 29 deciding
+// the rounding (a carry into the exponent is the correct result, up to
+// infinity); results below the float normal range flush to a signed zero,
+// results above it are infinite, NaN stays NaN.
 __device__ __forceinline__ float d2f(double x)
 {
-    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
-    if (((hi & 0x7fffffffu) | lo) == 0u) return __uint_as_float(hi & 0x80000000u);
-    const unsigned e = (hi >> 20) & 0x7ffu;
-    if (e < 897u || e > 1150u) return float(x);
-    // 52-bit fraction: its top 23 bits are kept, the low 29 decide the rounding
-    const unsigned top = ((hi & 0xfffffu) << 3) | (lo >> 29);
-    const unsigned rem = lo & 0x1fffffffu;
-    unsigned r = (hi & 0x80000000u) | ((e - 896u) << 23) | top;
-    // to nearest, ties to even; a carry into the exponent is the correct result (up to infinity)
+    unsigned hi, lo;
+    dsplit(x, hi, lo);
+    const unsigned sign = hi & 0x80000000u, e = (hi >> 20) & 0x7ffu;
+    const unsigned top = ((hi & 0xfffffu) << 3) | (lo >> 29), rem = lo & 0x1fffffffu;
+    unsigned r = sign | (((e - 896u) & 0xffu) << 23) | top;
     if (rem > 0x10000000u || (rem == 0x10000000u && (top & 1u))) r += 1u;
+    if (e < 896u || (r & 0x7f800000u) == 0u) r = sign;                        // flushed
+    if (e > 1150u) r = sign | 0x7f800000u;                                     // overflow
+    if (e == 0x7ffu && ((hi & 0xfffffu) | lo)) r = sign | 0x7fc00000u;        // NaN
     return __uint_as_float(r);
 }
 
@@ -278,46 +312,25 @@ __global__ void __launch_bounds__(128) km_bed(MeshDev m, StateDev s, MixedGeo g)
 #define BRX_CELLS_MIN_BLOCKS 8
 #endif
 
-// CSR entries of one cell as the cell sweep reads them: the other cell and
-// its flags, the LS weight x offset and face displacement, the bed
-// difference, and the other cell's stage primitives (wet bit, eta pair,
-// velocities), read from the packed tables as the sweep goes.
-struct GlobalEntries {
-    const MixedGeo &g;
-    const MxPrim *P;
-    int k0;
-    __device__ __forceinline__ int2 id(int j) const { return g.cidx[k0 + j]; }
-    __device__ __forceinline__ float4 ge(int j) const { return g.cent[k0 + j]; }
-    __device__ __forceinline__ float db(int j) const { return g.cdb[k0 + j]; }
-    // other cell's primitives: (ehi, elo, u, v) and the wet bit (valid for id.x >= 0)
-    __device__ __forceinline__ float4 pn(int j, int n) const
-    {
-        const MxPrim q = P[n];
-        return make_float4(q.ehi, q.elo, q.u, q.v);
-    }
-    __device__ __forceinline__ bool wet(int j, int n) const { return P[n].wet != 0; }
-};
-
 // Wet least-squares gradients of u, v and the surface for the rotor face
 // terms (river_turbine_flow.h:13-35): wet neighbours only, weights 1/|d|^2 of
 // the flow metric's centre offsets. Called in the cell sweep's tail, after
-// the cell record is written, so its sums are not live in the limiter.
-template <class E>
-__device__ __forceinline__ void hkt_cell_gradients(const MeshDev &m, const MixedGeo &g, const E &A, const MxPrim &pc,
-                                                   int c, int deg, int nc)
+// the cell record is written, so its sums are not live in the limiter; the
+// neighbour primitives were just read and come from L1.
+__device__ __forceinline__ void hkt_cell_gradients(const MeshDev &m, const MixedGeo &g, const MxPrim *P,
+                                                   const MxPrim &pc, int c, int nc)
 {
     float xx = 0.f, xy = 0.f, yy = 0.f, bx[3] = {0.f, 0.f, 0.f}, by[3] = {0.f, 0.f, 0.f};
-    const int k0 = m.offset[c];
     if (pc.wet)
-        for (int j = 0; j < deg; ++j) {
-            const int n = A.id(j).x;
+        for (int k = m.offset[c]; k < m.offset[c + 1]; ++k) {
+            const int n = g.cidx[k].x;
             if (n < 0) continue;
-            if (!A.wet(j, n)) continue;
-            const float4 pn = A.pn(j, n);
-            const float2 d = g.hdxy[k0 + j];
+            const MxPrim pn = P[n];
+            if (!pn.wet) continue;
+            const float2 d = g.hdxy[k];
             const float w = 1.f / (d.x * d.x + d.y * d.y);
             xx += w * d.x * d.x; xy += w * d.x * d.y; yy += w * d.y * d.y;
-            const float dv[3] = {pn.z - pc.u, pn.w - pc.v, (pn.x - pc.ehi) + (pn.y - pc.elo)};
+            const float dv[3] = {pn.u - pc.u, pn.v - pc.v, (pn.ehi - pc.ehi) + (pn.elo - pc.elo)};
 #pragma unroll
             for (int p = 0; p < 3; ++p) { bx[p] += w * d.x * dv[p]; by[p] += w * d.y * dv[p]; }
         }
@@ -330,155 +343,6 @@ __device__ __forceinline__ void hkt_cell_gradients(const MeshDev &m, const Mixed
     }
 }
 
-// One cell of the cell sweep: limited gradients and the cell record (the
-// reference's reconstruction_cells with the wall_bed_hydraulics transforms,
-// reconstruction.cu:43-168), reading its CSR entries through A.
-template <int MAXF, class E>
-__device__ __forceinline__ void cell_record(const MeshDev &m, const StateDev &s, const Ctrl &ct, const MixedGeo &g,
-                                            const E &A, const MxPrim &pc, int c, int deg, MxRec *rec)
-{
-    const float dry = ct.dryf;
-    const bool wet = pc.wet != 0;
-    const float hf = pc.h, u = pc.u, v = pc.v;
-    const bool outlet = g.ccls[c] & 1;   // a stage outlet face: the bed gradient is formed here
-    const int k0 = m.offset[c];
-    // bounds of eta and b relative to the cell (centre = 0), of u and v absolute
-    float lo[4] = {0.f, u, v, 0.f}, hi[4] = {0.f, u, v, 0.f};
-    float bx[4] = {0.f, 0.f, 0.f, 0.f}, by[4] = {0.f, 0.f, 0.f, 0.f};
-    bool active = wet;
-    for (int j = 0; j < deg; ++j) {
-        const int2 id = A.id(j);
-        const int n = id.x;
-        if (n < 0) {
-            if (id.y & 1) active = true;
-            else if ((id.y & 4) && wet) {
-                // a wall bounds the velocities by the mirrored cell velocity
-                const float2 nn = g.fnorm[m.faces[k0 + j]];
-                const float un = u * nn.x + v * nn.y;
-                const float mx = u - 2.f * un * nn.x, my = v - 2.f * un * nn.y;
-                lo[1] = fminf(lo[1], mx); hi[1] = fmaxf(hi[1], mx);
-                lo[2] = fminf(lo[2], my); hi[2] = fmaxf(hi[2], my);
-            }
-            continue;
-        }
-        const float4 pn = A.pn(j, n);
-        const bool wetn = A.wet(j, n);
-        if (wetn) active = true;
-        const float ddb = A.db(j);
-        float d[4];
-        d[0] = (pn.x - pc.ehi) + (pn.y - pc.elo);
-        d[1] = pn.z - u;
-        d[2] = pn.w - v;
-        d[3] = ddb;
-        // a dry neighbour whose bed rises above the wet surface contributes the surface
-        if (wet && !wetn && ddb >= hf) d[0] = 0.f;
-        const float4 ge = A.ge(j);     // LS weight * (dx, dy), face displacement
-#pragma unroll
-        for (int p = 0; p < 3; ++p) {
-            bx[p] += ge.x * d[p];
-            by[p] += ge.y * d[p];
-            const float val = (p == 1 || p == 2) ? d[p] + (p == 1 ? u : v) : d[p];
-            lo[p] = fminf(lo[p], val); hi[p] = fmaxf(hi[p], val);
-        }
-        if (outlet) {
-            bx[3] += ge.x * d[3]; by[3] += ge.y * d[3];
-            lo[3] = fminf(lo[3], d[3]); hi[3] = fmaxf(hi[3], d[3]);
-        }
-    }
-    float gx[4] = {0.f, 0.f, 0.f, 0.f}, gy[4] = {0.f, 0.f, 0.f, 0.f};
-    const float4 inv = g.cinv[c];
-    if (active && (inv.x != 0.f || inv.y != 0.f || inv.z != 0.f)) {
-#pragma unroll
-        for (int p = 0; p < 3; ++p) {
-            gx[p] = inv.x * bx[p] + inv.y * by[p];
-            gy[p] = inv.y * bx[p] + inv.z * by[p];
-        }
-        float bedtol = 0.f, sq = 0.f;
-        if (outlet) {
-            gx[3] = inv.x * bx[3] + inv.y * by[3];
-            gy[3] = inv.y * bx[3] + inv.z * by[3];
-            bedtol = 64.f * FEPS * fmaxf(1.f, fabsf(float(s.z[c])));
-            sq = wet ? sqrtf(ct.gravf * hf) : 0.f;
-        } else {
-            const float2 gb = g.gbed[c];
-            gx[3] = gb.x; gy[3] = gb.y;
-        }
-        float theta1 = 1.f, theta2 = 1.f;
-        // one slab set, filled for the surface, then (stage-outlet cells
-        // only) refilled for the bed: half the live registers of two sets
-        Slabs<MAXF> S{};
-        const float b0p = fmaxf(0.f, hi[0]), b0m = fmaxf(0.f, -lo[0]);
-#pragma unroll (MAXF <= 4 ? MAXF : 1)
-        for (int j = 0; j < MAXF; ++j) {
-            if (j >= deg) continue;      // (a break would stop the unrolling)
-            const float4 ge = A.ge(j);
-            const float rx = ge.z, ry = ge.w;
-            if (outlet && (A.id(j).y & 2) && wet) {
-                // an open stage outlet with a subcritical wet owner keeps its bed slope
-                const float2 nn = g.fnorm[m.faces[k0 + j]];
-                if (fabsf(u * nn.x + v * nn.y) < sq && fabsf(gx[3] * rx + gy[3] * ry) > bedtol) continue;
-            }
-#pragma unroll
-            for (int p = 1; p < 3; ++p) {
-                const float dd = gx[p] * rx + gy[p] * ry;
-                const float ctr = p == 1 ? u : v;
-                if (fabsf(dd) <= 64.f * FEPS * fmaxf(1.f, fmaxf(fabsf(ctr), fmaxf(fabsf(lo[p]), fabsf(hi[p])))))
-                    continue;
-                float &th = p == 1 ? theta1 : theta2;
-                if (dd > 0.f) th = fminf(th, (hi[p] - ctr) / dd);
-                if (dd < 0.f) th = fminf(th, (lo[p] - ctr) / dd);
-            }
-            const float len = sqrtf(rx * rx + ry * ry);
-            if (len <= 0.f) continue;
-            const float il = 1.f / len;
-            S.ux[j] = rx * il; S.uy[j] = ry * il; S.bp[j] = b0p * il; S.bm[j] = b0m * il;
-            S.mask |= 1u << j;
-        }
-        if (!slabs_feasible(S, gx[0], gy[0])) slabs_project(S, gx[0], gy[0]);
-        if (outlet) {
-            const float b3p = fmaxf(0.f, hi[3]), b3m = fmaxf(0.f, -lo[3]);
-            S.mask = 0u;
-#pragma unroll (MAXF <= 4 ? MAXF : 1)
-            for (int j = 0; j < MAXF; ++j) {
-                if (j >= deg) continue;
-                const int fl = A.id(j).y;
-                const float4 ge = A.ge(j);
-                const float rx = ge.z, ry = ge.w;
-                if ((fl & 2) && wet) {
-                    const float2 nn = g.fnorm[m.faces[k0 + j]];
-                    if (fabsf(u * nn.x + v * nn.y) < sq && fabsf(gx[3] * rx + gy[3] * ry) > bedtol) continue;
-                }
-                const float len = sqrtf(rx * rx + ry * ry);
-                if (len <= 0.f || (fl & 4)) continue;          // walls do not bound the bed
-                const float il = 1.f / len;
-                S.ux[j] = rx * il; S.uy[j] = ry * il; S.bp[j] = b3p * il; S.bm[j] = b3m * il;
-                S.mask |= 1u << j;
-            }
-            if (!slabs_feasible(S, gx[3], gy[3])) slabs_project(S, gx[3], gy[3]);
-        }
-        gx[1] *= fmaxf(0.f, theta1); gy[1] *= fmaxf(0.f, theta1);
-        gx[2] *= fmaxf(0.f, theta2); gy[2] *= fmaxf(0.f, theta2);
-    }
-    bool flatten = !wet;
-    if (!flatten) {
-        for (int j = 0; j < deg; ++j) {
-            const float4 ge = A.ge(j);
-            const float de = gx[0] * ge.z + gy[0] * ge.w, db = gx[3] * ge.z + gy[3] * ge.w;
-            if (hf + (de - db) <= dry || fabsf(db) >= hf) { flatten = true; break; }
-        }
-    }
-    MxRec r;
-    r.h = hf;
-    r.flags = (flatten ? 1 : 0) | (active ? 2 : 0) | (wet ? 4 : 0);
-    r.ehi = pc.ehi; r.elo = pc.elo; r.u = u; r.v = v;
-#pragma unroll
-    for (int p = 0; p < 4; ++p) { r.gx[p] = gx[p]; r.gy[p] = gy[p]; }
-    r.pad0 = 0.f; r.pad1 = 0.f;
-    rec[c] = r;
-}
-
-// Cell sweep, general polygons (any number of faces up to MAX_CELL_FACES):
-// one thread per cell, entries read from the packed tables as it goes.
 template <int MAXF>
 __global__ void __launch_bounds__(128, BRX_CELLS_MIN_BLOCKS) km_cells(MeshDev m, StateDev s, Ctrl *ctrl, Work w,
                                                                       MixedGeo g, int stage, TurbDev t, int turb)
@@ -489,11 +353,148 @@ __global__ void __launch_bounds__(128, BRX_CELLS_MIN_BLOCKS) km_cells(MeshDev m,
     FOR_ACTIVE_CELLS(m.act, c) {
         const Ctrl &ct = ctrl[m.cell_sid[c]];
         if (mx_skip(ct, stage)) continue;
+        const float dry = ct.dryf;
         const MxPrim pc = P[c];
+        const bool wet = pc.wet != 0;
+        const float hf = pc.h, u = pc.u, v = pc.v;
+        const bool outlet = g.ccls[c] & 1;   // a stage outlet face: the bed gradient is formed here
+        // bounds of eta and b relative to the cell (centre = 0), of u and v absolute
+        float lo[4] = {0.f, u, v, 0.f}, hi[4] = {0.f, u, v, 0.f};
+        float bx[4] = {0.f, 0.f, 0.f, 0.f}, by[4] = {0.f, 0.f, 0.f, 0.f};
         const int k0 = m.offset[c], deg = m.offset[c + 1] - k0;
-        const GlobalEntries A{g, P, k0};
-        cell_record<MAXF>(m, s, ct, g, A, pc, c, deg, rec);
-        if (turb && t.hkt[m.cell_sid[c]]) hkt_cell_gradients(m, g, A, pc, c, deg, nc);
+        bool active = wet;
+        for (int k = k0; k < k0 + deg; ++k) {
+            const int2 id = g.cidx[k];
+            const int n = id.x;
+            if (n < 0) {
+                if (id.y & 1) active = true;
+                else if ((id.y & 4) && wet) {
+                    // a wall bounds the velocities by the mirrored cell velocity
+                    const float2 nn = g.fnorm[m.faces[k]];
+                    const float un = u * nn.x + v * nn.y;
+                    const float mx = u - 2.f * un * nn.x, my = v - 2.f * un * nn.y;
+                    lo[1] = fminf(lo[1], mx); hi[1] = fmaxf(hi[1], mx);
+                    lo[2] = fminf(lo[2], my); hi[2] = fmaxf(hi[2], my);
+                }
+                continue;
+            }
+            const MxPrim pn = P[n];
+            const bool wetn = pn.wet != 0;
+            if (wetn) active = true;
+            const float ddb = g.cdb[k];
+            float d[4];
+            d[0] = (pn.ehi - pc.ehi) + (pn.elo - pc.elo);
+            d[1] = pn.u - u;
+            d[2] = pn.v - v;
+            d[3] = ddb;
+            // a dry neighbour whose bed rises above the wet surface contributes the surface
+            if (wet && !wetn && ddb >= hf) d[0] = 0.f;
+            const float4 ge = g.cent[k];     // LS weight * (dx, dy), face displacement
+#pragma unroll
+            for (int p = 0; p < 3; ++p) {
+                bx[p] += ge.x * d[p];
+                by[p] += ge.y * d[p];
+                const float val = (p == 1 || p == 2) ? d[p] + (p == 1 ? u : v) : d[p];
+                lo[p] = fminf(lo[p], val); hi[p] = fmaxf(hi[p], val);
+            }
+            if (outlet) {
+                bx[3] += ge.x * d[3]; by[3] += ge.y * d[3];
+                lo[3] = fminf(lo[3], d[3]); hi[3] = fmaxf(hi[3], d[3]);
+            }
+        }
+        float gx[4] = {0.f, 0.f, 0.f, 0.f}, gy[4] = {0.f, 0.f, 0.f, 0.f};
+        const float4 inv = g.cinv[c];
+        if (active && (inv.x != 0.f || inv.y != 0.f || inv.z != 0.f)) {
+#pragma unroll
+            for (int p = 0; p < 3; ++p) {
+                gx[p] = inv.x * bx[p] + inv.y * by[p];
+                gy[p] = inv.y * bx[p] + inv.z * by[p];
+            }
+            float bedtol = 0.f, sq = 0.f;
+            if (outlet) {
+                gx[3] = inv.x * bx[3] + inv.y * by[3];
+                gy[3] = inv.y * bx[3] + inv.z * by[3];
+                bedtol = 64.f * FEPS * fmaxf(1.f, fabsf(float(s.z[c])));
+                sq = wet ? sqrtf(ct.gravf * hf) : 0.f;
+            } else {
+                const float2 gb = g.gbed[c];
+                gx[3] = gb.x; gy[3] = gb.y;
+            }
+            float theta1 = 1.f, theta2 = 1.f;
+            // one slab set, filled for the surface, then (stage-outlet cells
+            // only) refilled for the bed: half the live registers of two sets
+            Slabs<MAXF> S{};
+            const float b0p = fmaxf(0.f, hi[0]), b0m = fmaxf(0.f, -lo[0]);
+#pragma unroll (MAXF <= 4 ? MAXF : 1)
+            for (int j = 0; j < MAXF; ++j) {
+                if (j >= deg) continue;      // (a break would stop the unrolling)
+                const int k = k0 + j;
+                const float4 ge = g.cent[k];
+                const float rx = ge.z, ry = ge.w;
+                if (outlet && (g.cidx[k].y & 2) && wet) {
+                    // an open stage outlet with a subcritical wet owner keeps its bed slope
+                    const float2 nn = g.fnorm[m.faces[k]];
+                    if (fabsf(u * nn.x + v * nn.y) < sq && fabsf(gx[3] * rx + gy[3] * ry) > bedtol) continue;
+                }
+#pragma unroll
+                for (int p = 1; p < 3; ++p) {
+                    const float dd = gx[p] * rx + gy[p] * ry;
+                    const float ctr = p == 1 ? u : v;
+                    if (fabsf(dd) <= 64.f * FEPS * fmaxf(1.f, fmaxf(fabsf(ctr), fmaxf(fabsf(lo[p]), fabsf(hi[p])))))
+                        continue;
+                    float &th = p == 1 ? theta1 : theta2;
+                    if (dd > 0.f) th = fminf(th, (hi[p] - ctr) / dd);
+                    if (dd < 0.f) th = fminf(th, (lo[p] - ctr) / dd);
+                }
+                const float len = sqrtf(rx * rx + ry * ry);
+                if (len <= 0.f) continue;
+                const float il = 1.f / len;
+                S.ux[j] = rx * il; S.uy[j] = ry * il; S.bp[j] = b0p * il; S.bm[j] = b0m * il;
+                S.mask |= 1u << j;
+            }
+            if (!slabs_feasible(S, gx[0], gy[0])) slabs_project(S, gx[0], gy[0]);
+            if (outlet) {
+                const float b3p = fmaxf(0.f, hi[3]), b3m = fmaxf(0.f, -lo[3]);
+                S.mask = 0u;
+#pragma unroll (MAXF <= 4 ? MAXF : 1)
+                for (int j = 0; j < MAXF; ++j) {
+                    if (j >= deg) continue;
+                    const int k = k0 + j;
+                    const int fl = g.cidx[k].y;
+                    const float4 ge = g.cent[k];
+                    const float rx = ge.z, ry = ge.w;
+                    if ((fl & 2) && wet) {
+                        const float2 nn = g.fnorm[m.faces[k]];
+                        if (fabsf(u * nn.x + v * nn.y) < sq && fabsf(gx[3] * rx + gy[3] * ry) > bedtol) continue;
+                    }
+                    const float len = sqrtf(rx * rx + ry * ry);
+                    if (len <= 0.f || (fl & 4)) continue;          // walls do not bound the bed
+                    const float il = 1.f / len;
+                    S.ux[j] = rx * il; S.uy[j] = ry * il; S.bp[j] = b3p * il; S.bm[j] = b3m * il;
+                    S.mask |= 1u << j;
+                }
+                if (!slabs_feasible(S, gx[3], gy[3])) slabs_project(S, gx[3], gy[3]);
+            }
+            gx[1] *= fmaxf(0.f, theta1); gy[1] *= fmaxf(0.f, theta1);
+            gx[2] *= fmaxf(0.f, theta2); gy[2] *= fmaxf(0.f, theta2);
+        }
+        bool flatten = !wet;
+        if (!flatten) {
+            for (int k = k0; k < k0 + deg; ++k) {
+                const float4 ge = g.cent[k];
+                const float de = gx[0] * ge.z + gy[0] * ge.w, db = gx[3] * ge.z + gy[3] * ge.w;
+                if (hf + (de - db) <= dry || fabsf(db) >= hf) { flatten = true; break; }
+            }
+        }
+        MxRec r;
+        r.h = hf;
+        r.flags = (flatten ? 1 : 0) | (active ? 2 : 0) | (wet ? 4 : 0);
+        r.ehi = pc.ehi; r.elo = pc.elo; r.u = u; r.v = v;
+#pragma unroll
+        for (int p = 0; p < 4; ++p) { r.gx[p] = gx[p]; r.gy[p] = gy[p]; }
+        r.pad0 = 0.f; r.pad1 = 0.f;
+        rec[c] = r;
+        if (turb && t.hkt[m.cell_sid[c]]) hkt_cell_gradients(m, g, P, pc, c, nc);
     }
 }
 
