@@ -632,6 +632,57 @@ class RiverSolver:
         check(self.lib.brx_substep(self.h, float(dt), float(time), _ptr(status), _ptr(peak)))
         return (status[0], peak[0]) if self.single else (status, peak)
 
+    def advance_recorded(self, dt, time, hint=None):
+        """Advance one scenario over [time, time + dt] with the substep
+        controller run on the host (RiverExplicit.advance's rules,
+        river_explicit.py:121-154: trial = min(hint, remaining); reject on a
+        status or dt * peak > CFL and retry at min(dt / 2, 0.98 CFL / peak);
+        on acceptance grow the hint to 2 dt, capped by 0.98 CFL / peak).
+        Returns (accepted substep lengths, next hint). With advance_replay,
+        two arithmetic forms can run one substep sequence, which separates
+        round-off from the two controllers choosing different sequences."""
+        if not self.single:
+            raise ValueError("advance_recorded drives one scenario")
+        cfl = self.cases[0]["controls"]["cfl"]
+        hint = float(dt if hint is None else hint)
+        elapsed, dts, rejections = 0.0, [], 0
+        while elapsed < dt - 1e-13 * max(1.0, dt):
+            trial = min(hint, dt - elapsed)
+            truncated = trial < hint * (1 - 1e-12)
+            status, peak = self.substep(trial, time + elapsed)
+            if status:
+                rejections += 1
+                if rejections > 100 or trial < dt * 2.0 ** -20:
+                    raise RuntimeError(f"substep controller failed at t={time + elapsed}: status {status}")
+                hint = min(0.5 * trial, 0.98 * cfl / peak) if peak > 0 else 0.5 * trial
+                continue
+            elapsed += trial
+            dts.append(trial)
+            growth = hint if truncated else 2.0 * trial
+            hint = min(growth, 0.98 * cfl / peak) if peak > 0 else growth
+        return dts, hint
+
+    def advance_replay(self, dts, time):
+        """Advance one scenario by exactly the substep lengths ``dts`` from
+        ``time``. The CFL acceptance test is lifted (limit 1) for the replay;
+        any other rejection raises. Returns the number of substeps."""
+        if not self.single:
+            raise ValueError("advance_replay drives one scenario")
+        c = self.cases[0]["controls"]
+        check(self.lib.brx_controls_set(self.h, 0, c["grav"], c["dry"], 1.0, c["speed_limit"],
+                                        int(c["roughness_mode"]), c["roughness_value"]))
+        try:
+            t = float(time)
+            for dt in dts:
+                status, _ = self.substep(dt, t)
+                if int(status):
+                    raise RuntimeError(f"replayed substep rejected at t={t}: status {int(status)}")
+                t += dt
+        finally:
+            check(self.lib.brx_controls_set(self.h, 0, c["grav"], c["dry"], c["cfl"], c["speed_limit"],
+                                            int(c["roughness_mode"]), c["roughness_value"]))
+        return len(dts)
+
     def rate(self, dt, time=0.0):
         """One spatial residual of the current state: (rate (3,nc), water (nf), status, frequency)."""
         torch = self.torch
