@@ -684,11 +684,31 @@ __global__ void __launch_bounds__(128, BRX_FACES_MIN_BLOCKS) km_faces(MeshDev m,
             float top_bed = 0.f;           // the face's common bed (kind 1), for the rotor terms
             if (kind == 1) {
                 const float top = fmaxf(bLr, bRr);
-                const float bc = rc.ehi - hc;      // the owner's bed, as a tolerance scale
-                const float tol = 16.f * FEPS * fmaxf(dry, fmaxf(fabsf(bc + top), fmaxf(fabsf(bc + hL + bLr), fabsf(bc + hR + bRr))));
                 float hl = hL > 0.f ? fmaxf(0.f, sL - top) : 0.f, hr = hR > 0.f ? fmaxf(0.f, sR - top) : 0.f;
-                if (hl <= dry + tol) hl = 0.f;
-                if (hr <= dry + tol) hr = 0.f;
+                // The FP32 depths above the common bed are differences of
+                // values relative to the owner's bed, good to a few FP32 ulps
+                // of those values. Within that band of the dry threshold the
+                // decision is taken in FP64 from the FP64 state and bed, with
+                // the reference's roundoff tolerance (16 eps of the absolute
+                // elevations, face_activity.py:33-37); outside it, FP32 and
+                // FP64 agree. A film just above the dry depth is then active
+                // in both forms (an elevation-scaled FP32 tolerance would
+                // close it, and the face would carry a different flux every
+                // substep).
+                const float band = 16.f * FEPS * fmaxf(dry, fmaxf(fmaxf(fabsf(sL), fabsf(sR)), fabsf(top)));
+                if ((hl > 0.f && fabsf(hl - dry) <= band) || (hr > 0.f && fabsf(hr - dry) <= band)) {
+                    const double *q = stage == 1 ? s.work : s.q1;
+                    const double zc = s.z[c], zn = s.z[n];
+                    const double etaL = zc + q[c] + double(L.de), etaR = zn + q[n] + double(R.de);
+                    const double topd = fmax(zc + double(L.db), zn + double(R.db));
+                    const double tol64 = 16. * EPS * fmax(ct.dry, fmax(fabs(topd), fmax(fabs(etaL), fabs(etaR))));
+                    const double hld = hL > 0.f ? fmax(0., etaL - topd) : 0., hrd = hR > 0.f ? fmax(0., etaR - topd) : 0.;
+                    hl = hld <= ct.dry + tol64 ? 0.f : float(hld);
+                    hr = hrd <= ct.dry + tol64 ? 0.f : float(hrd);
+                } else {
+                    if (hl <= dry) hl = 0.f;
+                    if (hr <= dry) hr = 0.f;
+                }
                 loc[0] = hl; loc[4] = hr;
                 loc[1] = hL > dry ? unL * (hl / hL) : 0.f;
                 loc[2] = hL > dry ? utL * (hl / hL) : 0.f;
