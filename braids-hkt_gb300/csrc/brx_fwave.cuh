@@ -17,6 +17,13 @@
 
 namespace brx {
 
+// Division of the Riemann arithmetic. The FP64 form keeps the reference's
+// correctly rounded division (its operation order decides bits); the FP32
+// form uses the fast reciprocal-multiply (2 ulp; every divisor here is a
+// depth, a speed sum or a wave-speed difference well inside its range).
+template <class F> __device__ __forceinline__ F quo(F a, F b) { return a / b; }
+template <> __device__ __forceinline__ float quo<float>(float a, float b) { return __fdividef(a, b); }
+
 template <class F> struct RType { F hm, s1m, s2m; };
 
 template <class F>
@@ -32,33 +39,33 @@ __device__ __forceinline__ RType<F> riemann_type(F hL, F hR, F uL, F uR, F dryto
         return o;
     }
     const F fmn = delu + two * (sqrt(g * hmin) - sqrt(g * hmax));
-    const F fmx = delu + (hmax - hmin) * sqrt(half * g * (hmax + hmin) / (hmax * hmin));
+    const F fmx = delu + (hmax - hmin) * sqrt(quo<F>(half * g * (hmax + hmin), hmax * hmin));
     if (fmn > F(0)) {
         const F root = fmax(F(0), -delu + two * (sqrt(g * hL) + sqrt(g * hR)));
-        o.hm = (F(1) / (F(16) * g)) * (root * root);
+        o.hm = quo<F>(F(1), F(16) * g) * (root * root);
         o.s1m = uL + two * sqrt(g * hL) - three * sqrt(g * o.hm);
         o.s2m = uR - two * sqrt(g * hR) + three * sqrt(g * o.hm);
     } else if (fmx <= F(0)) {
         F h0 = hmax;
-        const F gL = sqrt(half * g * (F(1) / h0 + F(1) / hL));
-        const F gR = sqrt(half * g * (F(1) / h0 + F(1) / hR));
+        const F gL = sqrt(half * g * (quo<F>(F(1), h0) + quo<F>(F(1), hL)));
+        const F gR = sqrt(half * g * (quo<F>(F(1), h0) + quo<F>(F(1), hR)));
         const F F0 = delu + (h0 - hL) * gL + (h0 - hR) * gR;
-        const F dfdh = gL - g * (h0 - hL) / (F(4) * (h0 * h0) * gL) +
-                       gR - g * (h0 - hR) / (F(4) * (h0 * h0) * gR);
+        const F dfdh = gL - quo<F>(g * (h0 - hL), F(4) * (h0 * h0) * gL) +
+                       gR - quo<F>(g * (h0 - hR), F(4) * (h0 * h0) * gR);
         const F slope = two * sqrt(h0) * dfdh;
-        const F root = sqrt(h0) - F0 / slope;
+        const F root = sqrt(h0) - quo<F>(F0, slope);
         h0 = root * root;
         o.hm = h0;
-        const F u1m = uL - (o.hm - hL) * sqrt((half * g) * (F(1) / o.hm + F(1) / hL));
-        const F u2m = uR + (o.hm - hR) * sqrt((half * g) * (F(1) / o.hm + F(1) / hR));
+        const F u1m = uL - (o.hm - hL) * sqrt((half * g) * (quo<F>(F(1), o.hm) + quo<F>(F(1), hL)));
+        const F u2m = uR + (o.hm - hR) * sqrt((half * g) * (quo<F>(F(1), o.hm) + quo<F>(F(1), hR)));
         o.s1m = u1m - sqrt(g * o.hm);
         o.s2m = u2m + sqrt(g * o.hm);
     } else {
         F h0 = hmin;
         const F F0 = delu + two * (sqrt(g * h0) - sqrt(g * hmax)) +
-                     (h0 - hmin) * sqrt(half * g * (F(1) / h0 + F(1) / hmin));
-        const F slope = (fmx - F0) / (hmax - hmin);
-        h0 = h0 - F0 / slope;
+                     (h0 - hmin) * sqrt(half * g * (quo<F>(F(1), h0) + quo<F>(F(1), hmin)));
+        const F slope = quo<F>(fmx - F0, hmax - hmin);
+        h0 = h0 - quo<F>(F0, slope);
         o.hm = h0;
         if (hL > hR) {
             o.s1m = uL + two * sqrt(g * hL) - three * sqrt(g * o.hm);
@@ -106,12 +113,12 @@ __device__ __forceinline__ int fwave(const F in[8], F grav, F drytol, FWaveOut<F
     if (hL <= drytol && hR <= drytol) return status;
     F uL, uR, vL, vR, phiL, phiR;
     if (hR > drytol) {
-        uR = huR / hR; vR = hvR / hR;
-        phiR = half * grav * (hR * hR) + (huR * huR) / hR;
+        uR = quo<F>(huR, hR); vR = quo<F>(hvR, hR);
+        phiR = half * grav * (hR * hR) + quo<F>(huR * huR, hR);
     } else { hR = zero; huR = zero; hvR = zero; uR = zero; vR = zero; phiR = zero; }
     if (hL > drytol) {
-        uL = huL / hL; vL = hvL / hL;
-        phiL = half * grav * (hL * hL) + (huL * huL) / hL;
+        uL = quo<F>(huL, hL); vL = quo<F>(hvL, hL);
+        phiL = half * grav * (hL * hL) + quo<F>(huL * huL, hL);
     } else { hL = zero; huL = zero; hvL = zero; uL = zero; vL = zero; phiL = zero; }
     F w0 = F(1), w1 = F(1), w2 = F(1);
     if (hR <= drytol) {
@@ -131,7 +138,7 @@ __device__ __forceinline__ int fwave(const F in[8], F grav, F drytol, FWaveOut<F
     }
     const F sqL = sqrt(grav * hL), sqR = sqrt(grav * hR);
     const F sL = uL - sqL, sR = uR + sqR;
-    const F uhat = (sqL * uL + sqR * uR) / (sqR + sqL);
+    const F uhat = quo<F>(sqL * uL + sqR * uR, sqR + sqL);
     const F chat = sqrt(grav * half * (hR + hL));
     F sE1 = fmin(sL, uhat - chat), sE2 = fmax(sR, uhat + chat);
 
@@ -143,7 +150,7 @@ __device__ __forceinline__ int fwave(const F in[8], F grav, F drytol, FWaveOut<F
     const F lam2 = fmax(sE2, s1m);
     sE1 = lam0;
     sE2 = lam2;
-    const F hstarHLL = fmax((huL - huR + sE2 * hR - sE1 * hL) / (sE2 - sE1), zero);
+    const F hstarHLL = fmax(quo<F>(huL - huR + sE2 * hR - sE1 * hL, sE2 - sE1), zero);
     // eigenvectors: r(:,0) = (1, lam0, lam0^2), r(:,1) = (0, 0, 1), r(:,2) = (1, lam2, lam2^2)
     const F r10 = lam0, r20 = lam0 * lam0, r12 = lam2, r22 = lam2 * lam2;
     const F lam1 = half * (lam0 + lam2);
@@ -165,27 +172,37 @@ __device__ __forceinline__ int fwave(const F in[8], F grav, F drytol, FWaveOut<F
     else if ((uL - sqL) * (uR - sqR) < zero) sonic = true;
     else sonic = false;
 
-    F deldelh = sonic ? -delb : delb * g * hbar / s1s2bar;
+    F deldelh = sonic ? -delb : quo<F>(delb * g * hbar, s1s2bar);
     if (sE1 < -crit && sE2 > crit) {
-        deldelh = fmin(deldelh, hstarHLL * (sE2 - sE1) / sE2);
-        deldelh = fmax(deldelh, hstarHLL * (sE2 - sE1) / sE1);
+        deldelh = fmin(deldelh, quo<F>(hstarHLL * (sE2 - sE1), sE2));
+        deldelh = fmax(deldelh, quo<F>(hstarHLL * (sE2 - sE1), sE1));
     } else if (sE1 >= crit) {
-        deldelh = fmin(deldelh, hstarHLL * (sE2 - sE1) / sE1);
+        deldelh = fmin(deldelh, quo<F>(hstarHLL * (sE2 - sE1), sE1));
         deldelh = fmax(deldelh, -hL);
     } else if (sE2 <= -crit) {
         deldelh = fmin(deldelh, hR);
-        deldelh = fmax(deldelh, hstarHLL * (sE2 - sE1) / sE2);
+        deldelh = fmax(deldelh, quo<F>(hstarHLL * (sE2 - sE1), sE2));
     }
-    F deldelphi = sonic ? -g * hbar * delb : -delb * g * hbar * s1s2tilde / s1s2bar;
+    F deldelphi = sonic ? -g * hbar * delb : quo<F>(-delb * g * hbar * s1s2tilde, s1s2bar);
     deldelphi = fmin(deldelphi, g * fmax(-hL * delb, -hR * delb));
     deldelphi = fmax(deldelphi, g * fmin(-hL * delb, -hR * delb));
     const F d0 = delh - deldelh, d1 = delhu, d2 = delphi - deldelphi;
-    // Cramer's rule on [r0 r1 r2] beta = delta.
+    // Cramer's rule on [r0 r1 r2] beta = delta. The FP64 form evaluates the
+    // cofactor expansions with their unit and zero entries as the reference
+    // does; the FP32 form folds them (det = lam0 - lam2).
     const F one = F(1);
-    const F det = det3<F>(one, zero, one, r10, zero, r12, r20, one, r22);
-    const F beta0 = det3<F>(d0, zero, one, d1, zero, r12, d2, one, r22) / det;
-    const F beta1 = det3<F>(one, d0, one, r10, d1, r12, r20, d2, r22) / det;
-    const F beta2 = det3<F>(one, zero, d0, r10, zero, d1, r20, one, d2) / det;
+    F beta0, beta1, beta2;
+    if constexpr (sizeof(F) == 4) {
+        const F rdet = quo<F>(one, r10 - r12);
+        beta0 = (d1 - d0 * r12) * rdet;
+        beta1 = ((d1 * r22 - r12 * d2) - d0 * (r10 * r22 - r12 * r20) + (r10 * d2 - d1 * r20)) * rdet;
+        beta2 = (d0 * r10 - d1) * rdet;
+    } else {
+        const F det = det3<F>(one, zero, one, r10, zero, r12, r20, one, r22);
+        beta0 = det3<F>(d0, zero, one, d1, zero, r12, d2, one, r22) / det;
+        beta1 = det3<F>(one, d0, one, r10, d1, r12, r20, d2, r22) / det;
+        beta2 = det3<F>(one, zero, d0, r10, zero, d1, r20, one, d2) / det;
+    }
     F fw00 = beta0 * r10, fw01 = beta0 * r20, fw02 = beta0 * r10;
     F fw10 = beta1 * zero, fw11 = beta1 * one;
     F fw20 = beta2 * r12, fw21 = beta2 * r22, fw22 = beta2 * r12;
@@ -227,18 +244,18 @@ template <class F>
 __device__ __forceinline__ F wall_pressure(F h, F momentum, F g, F dry)
 {
     if (h <= dry) return F(0);
-    const F c = sqrt(g * h), v = momentum / h / c;
+    const F c = sqrt(g * h), v = quo<F>(quo<F>(momentum, h), c);
     F ratio;
     if (v <= F(0)) { const F a = fmax(F(0), F(1) + F(0.5) * v); ratio = a * a; }
     else {
         F lo = F(1), hi = F(1) + sqrt(F(2)) * v, rr = F(1) + v;
         for (int k = 0; k < 32; ++k) {
-            const F s = sqrt(F(0.5) * (F(1) + F(1) / rr));
+            const F s = sqrt(F(0.5) * (F(1) + quo<F>(F(1), rr)));
             const F f = (rr - F(1)) * s - v;
             if (fabs(f) <= F(2.e-15) * fmax(F(1), v)) break;
             if (f > F(0)) hi = rr; else lo = rr;
-            const F df = s - (rr - F(1)) / (F(4) * s * rr * rr);
-            const F trial = rr - f / df;
+            const F df = s - quo<F>(rr - F(1), F(4) * s * rr * rr);
+            const F trial = rr - quo<F>(f, df);
             rr = (trial > lo && trial < hi) ? trial : F(0.5) * (lo + hi);
         }
         ratio = rr;

@@ -184,7 +184,7 @@ __device__ __forceinline__ void warp_max_peak_f(unsigned long long *peak_of_sid0
     const unsigned top = __reduce_max_sync(same, bits);
     if (valid && (int)(threadIdx.x & 31) == __ffs(same) - 1) {
         unsigned long long *addr = (unsigned long long *)((char *)peak_of_sid0 + stride_bytes * (size_t)sid);
-        atomicMax(addr, (unsigned long long)__double_as_longlong(double(__uint_as_float(top))));
+        atomicMax(addr, (unsigned long long)__double_as_longlong(f2d(__uint_as_float(top))));
     }
 }
 
@@ -710,10 +710,11 @@ __global__ void __launch_bounds__(128, BRX_FACES_MIN_BLOCKS) km_faces(MeshDev m,
                     if (hr <= dry) hr = 0.f;
                 }
                 loc[0] = hl; loc[4] = hr;
-                loc[1] = hL > dry ? unL * (hl / hL) : 0.f;
-                loc[2] = hL > dry ? utL * (hl / hL) : 0.f;
-                loc[5] = hR > dry ? unR * (hr / hR) : 0.f;
-                loc[6] = hR > dry ? utR * (hr / hR) : 0.f;
+                const float sl = hL > dry ? __fdividef(hl, hL) : 0.f, sr = hR > dry ? __fdividef(hr, hR) : 0.f;
+                loc[1] = unL * sl;
+                loc[2] = utL * sl;
+                loc[5] = unR * sr;
+                loc[6] = utR * sr;
                 top_bed = top;
             }
             bool closed = false;
@@ -753,8 +754,8 @@ __global__ void __launch_bounds__(128, BRX_FACES_MIN_BLOCKS) km_faces(MeshDev m,
                 if (hR > dry) speed = fmaxf(speed, fabsf(loc[5] / hR) + sqrtf(grav * hR));
             } else {
                 const float starL = loc[0], starR = loc[4];
-                if (starL > dry) { dl0 = loc[1]; dl1 = loc[1] * loc[1] / starL; dl2 = loc[1] * loc[2] / starL; }
-                if (starR > dry) { dr0 = loc[5]; dr1 = loc[5] * loc[5] / starR; dr2 = loc[5] * loc[6] / starR; }
+                if (starL > dry) { const float r = __fdividef(loc[1], starL); dl0 = loc[1]; dl1 = loc[1] * r; dl2 = loc[2] * r; }
+                if (starR > dry) { const float r = __fdividef(loc[5], starR); dr0 = loc[5]; dr1 = loc[5] * r; dr2 = loc[6] * r; }
                 dl0 += fwo.amdq[0]; dl1 += fwo.amdq[1]; dl2 += fwo.amdq[2];
                 dr0 -= fwo.apdq[0]; dr1 -= fwo.apdq[1]; dr2 -= fwo.apdq[2];
                 // the HR pressures 1/2 g star^2 and their side corrections 1/2 g (h^2 - star^2) add up to 1/2 g h^2
