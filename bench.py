@@ -71,6 +71,18 @@ def build_workload(name, rank=0, world=1, subset=None):
         return [S.config1()], "fp64", 1.0, dict(workload="config1: straight channel 2000x200 m, 4 m jittered "
                                                "Delaunay, 50k triangles, Q=400 m3/s, stage 3.0 m, Manning 0.03, "
                                                "CFL 0.9, FP64 plain form")
+    if name == "config2":
+        return [S.config2()], "fp64", 0.5, dict(workload="config2: the config-1 channel with 3 tandem rotors 150 m "
+                                               "apart (D 5 m, Ct 0.8, incident-speed power curve rated 500 kW), "
+                                               "refined to 1 m across the channel downstream of each rotor "
+                                               "(124k triangles), FP64 plain form")
+    if name == "config3":
+        return [S.config3()], "mixed", 1.0, dict(workload="config3: braided river 10 km x 1.5 km, 5 seeded sinuous "
+                                                "channels, 3.87 m jittered Delaunay (about 2M triangles), "
+                                                "hydrograph 200 -> 2000 m3/s over 3600 s, stage outlet, MPM bed "
+                                                "update (d50 20 mm, porosity 0.4) after every interval, 12 "
+                                                "rotors, mixed FP32/FP64 form; the FP64 form over the same "
+                                                "intervals for the error")
     if name == "config4":
         params = S.config4_params(64, seed=4 + rank)
         if subset:
@@ -191,6 +203,67 @@ def algorithmic_bytes(kernel, nc, nf, nadj, nslot, precision="fp64", rotor_cells
     return 0
 
 
+def prepare(solver, cases):
+    """Forcing tables of the workload (hydrograph), before any interval."""
+    if len(cases) == 1 and cases[0].get("table_time") is not None:
+        solver.set_forcing_table(cases[0]["table_time"], cases[0]["table_value"])
+
+
+def outer_step(solver, dt, t, raise_on_failure=False):
+    """One outer interval of the owner: the adaptive hydraulic substeps, then
+    the Exner bed update where the workload has a bed model
+    (ShorelineSolver.step -> finish, shoreline_solver.py:345-372)."""
+    diags = solver.advance(dt, t, raise_on_failure=raise_on_failure)
+    if solver.bed_model is not None:
+        solver.morphology(dt)
+    return diags
+
+
+def fp64_comparison(cases, outer, steps, mixed_state, mixed_z, mixed_rotors, torch):
+    """The same single-scenario workload in the FP64 form over the same
+    intervals from the same initial state: its throughput and the mixed
+    form's error against it after the last interval."""
+    from braids_hkt_gb300.solver import RiverSolver
+    import braids_hkt_gb300.turbines as TB
+    case = cases[0]
+    one = RiverSolver(case, precision="fp64")
+    prepare(one, cases)
+    t, ms, ups = 0.0, 0.0, 0
+    for _ in range(steps):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(one.stream)
+        d = outer_step(one, outer, t)
+        e1.record(one.stream)
+        e1.synchronize()
+        ms += e0.elapsed_time(e1)
+        ups += int(d["hydraulic_substeps"]) * one.nc
+        t += outer
+    q64 = one.q.cpu().numpy()
+    h64, hmx = q64[0], mixed_state[0]
+    deep = h64 > 0.05
+    rel = np.abs(hmx - h64) / np.maximum(h64, 1e-3)
+    area = case["mesh"].area
+    out = {"fp64_value": ups / (ms / 1e3), "unit": METRIC, "after_sim_s": steps * outer,
+           "depth_rel_max_deep": float(rel[deep].max()), "depth_rel_p99_deep": float(np.percentile(rel[deep], 99)),
+           "depth_abs_max_over_depth_max": float(np.abs(hmx - h64).max() / h64.max()),
+           "unit_discharge_rel_max": float(np.abs(mixed_state[1:] - q64[1:]).max() / max(np.abs(q64[1:]).max(), 1e-12)),
+           "volume_rel": float(abs(np.sum(hmx * area) - np.sum(h64 * area)) / np.sum(h64 * area)),
+           "deep": "cells deeper than 5 cm", "stated_tolerance": 1e-4}
+    if one.bed_model is not None and mixed_z is not None:
+        z64 = one.z.cpu().numpy()
+        scale = max(float(np.abs(z64 - case["z"]).max()), 1e-12)
+        out["bed_abs_max_over_bed_change_max"] = float(np.abs(mixed_z - z64).max() / scale)
+    if one.rotors is not None and mixed_rotors is not None:
+        col = TB.DIAG_FIELDS.index("useful_power_per_density_m5_s3")
+        p64 = one.turbine_record()[:, col]
+        out["rotor_power_abs_max_over_max"] = float(np.abs(mixed_rotors[:, col] - p64).max() /
+                                                    max(float(np.abs(p64).max()), 1e-30))
+        out["rotor_power_max_W"] = float(np.abs(p64).max() * TB.WATER_DENSITY)
+    one.close()
+    return out
+
+
 def fma_peaks(lib):
     """Measured FMA throughput of this GPU (brx_fma_rate): the compute
     roofline of the FP64 form and of the FP32 sweeps, TFLOP/s."""
@@ -247,7 +320,8 @@ def cpu_baseline(cases, outer, seconds=10.0, threads=None):
     q = cases[0]["q"].copy()
     nc = cases[0]["mesh"].nc
     updates, t0, sim = 0, time.perf_counter(), 0.0
-    interval = min(outer, 0.5)
+    # short intervals on large meshes, so the sample stays near its time bound
+    interval = min(outer, 0.5, 0.5 * 2.0e5 / nc)
     while time.perf_counter() - t0 < seconds:
         st, _, stats = o.advance(q, interval, sim)
         if st:
@@ -329,6 +403,7 @@ def main():
     from braids_hkt_gb300.solver import RiverSolver
 
     solver = RiverSolver(cases, precision=precision)
+    prepare(solver, cases)
     nc, nf = solver.nc, solver.nf
     nadj = int(solver.packed["nadj"])
     nslot = len(solver.packed["boundary_faces"])
@@ -343,7 +418,7 @@ def main():
     sim_time = 0.0
     failed = set()
     for _ in range(args.warmup):
-        diags = solver.advance(outer, sim_time, raise_on_failure=False)
+        diags = outer_step(solver, outer, sim_time)
         diags = diags if isinstance(diags, list) else [diags]
         failed |= {i for i, d in enumerate(diags) if d["failed"]}
         sim_time += outer
@@ -368,7 +443,7 @@ def main():
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        diags = solver.advance(outer, sim_time, raise_on_failure=False)
+        diags = outer_step(solver, outer, sim_time)
         e1.record(stream)
         e1.synchronize()
         step_ms.append(e0.elapsed_time(e1))
@@ -392,6 +467,7 @@ def main():
     value = updates / t_max
 
     state_after_timed = solver.q.cpu().numpy()       # for the accuracy check against FP64 below
+    bed_after_timed = solver.z.cpu().numpy()
     rotors_after_timed = solver.turbine_record() if solver.rotors is not None else None
     sim_after_timed = sim_time
     # end to end through the public API with host buffers: H2D of the step's
@@ -404,7 +480,7 @@ def main():
     t0 = time.perf_counter()
     for _ in range(max(1, args.steps)):
         solver.q.copy_(q_host, non_blocking=True)
-        diags = solver.advance(outer, sim_time)
+        diags = outer_step(solver, outer, sim_time, raise_on_failure=True)
         out_host.copy_(solver.q, non_blocking=True)
         torch.cuda.synchronize()
         sim_time += outer
@@ -443,7 +519,7 @@ def main():
     # the same scenarios one by one in the plain FP64 form, from the same initial state over the same
     # intervals: FP64 throughput and the mixed form's depth error against it
     plain = None
-    if precision == "mixed" and args.plain > 0:
+    if precision == "mixed" and args.plain > 0 and len(cases) > 1:
         # smallest / median / largest scenario among those with rotors (all, without rotors)
         pool = [i for i, c in enumerate(cases) if c.get("turbines")] or list(range(len(cases)))
         order = sorted(pool, key=lambda i: cases[i]["mesh"].nc)
@@ -524,8 +600,14 @@ def main():
                                    "stated_tolerance": 1e-4,
                                    "rotor_power_rel_max": max(perr) if perr else None,
                                    "rotors_compared": len(perr)}
+    if precision == "mixed" and len(cases) == 1:
+        # config 3: the FP64 form over the warm-up and timed intervals, from the same initial state
+        cfg["accuracy_vs_fp64"] = fp64_comparison(cases, outer, args.warmup + args.steps, state_after_timed,
+                                                  bed_after_timed, rotors_after_timed, torch)
+        plain = {"value": cfg["accuracy_vs_fp64"]["fp64_value"], "unit": METRIC,
+                 "note": "the same scenario in the FP64 form over the same intervals"}
     hllc_batch = None
-    if args.hllc and precision == "mixed":
+    if args.hllc and precision == "mixed" and len(cases) > 1:
         # the whole batch with the HLLC method (FP64 form): one warm-up and up to two timed intervals
         hs = RiverSolver(cases, precision="fp64", method="hllc")
         from braids_hkt_gb300 import autotune
@@ -575,7 +657,7 @@ def main():
         line["batched_vs_plain_fp64"] = value / plain["value"]
     if hllc_batch is not None:
         line["hllc_fp64_batch"] = hllc_batch
-    if precision == "mixed" and not args.no_serving:
+    if precision == "mixed" and not args.no_serving and len(cases) > 1:
         solver.close()
         try:
             line["serving"] = serving_session(cases, precision)

@@ -17,7 +17,7 @@ Mixed against FP64 with each form's own controller over three seconds: at
 floodplain; there FP32 flux rounding is of the order of a film's own
 momentum, the face wave speeds of the two forms differ (CFL peaks 544 and
 1091 per second), their controllers take different substeps and the forms
-differ by truncation error and front timing near the front (measured 6.9e-4
+differ by truncation error and front timing near the front (measured 1.4e-4
 relative on cells deeper than 5 cm after 3 s, bound 2e-3; bed 5e-3 of the
 largest change, bound 2e-2). The steady config-4 channels stay within 1e-4
 (bench).
