@@ -703,6 +703,21 @@ extern "C" int brx_inlet_lines_set(brx_solver *s, const int *kind, const double 
     return BRX_OK;
 }
 
+// New constant forcing (2, nseg) of the open segments, keeping every other
+// boundary table: a serving loop re-uses a resident scenario slot for a
+// request with its own discharge or stage.
+extern "C" int brx_forcing_set(brx_solver *s, const double *forcing)
+{
+    if (!s || !forcing) return fail(BRX_ERR_ARGUMENT, "null argument");
+    if (s->pending) return fail(BRX_ERR_STATE, "an asynchronous interval is in flight");
+    if (!s->boundary_ready) return fail(BRX_ERR_STATE, "open boundaries not configured (brx_boundary_set)");
+    if (!s->nseg) return BRX_OK;
+    for (int k = 0; k < 2 * s->nseg; ++k)
+        if (!std::isfinite(forcing[k])) return fail(BRX_ERR_ARGUMENT, "nonfinite forcing");
+    CK(cudaMemcpy(s->bnd.forcing, forcing, sizeof(double) * 2 * s->nseg, cudaMemcpyHostToDevice));
+    return clear_inlet_lines(s);
+}
+
 extern "C" int brx_forcing_table_set(brx_solver *s, int len, const double *time, const double *value)
 {
     if (!s) return fail(BRX_ERR_ARGUMENT, "null solver");

@@ -48,6 +48,7 @@ class Request:
     rotors: np.ndarray | None = None
     failed: int = 0
     substeps: int = 0
+    base: int = 0                    # pool mesh of a slot-serving request
 
     @property
     def latency(self):
@@ -237,6 +238,165 @@ class ServingEngine:
                 "throughput_cell_updates_s": self.cell_updates / wall if wall > 0 else None,
                 "wall_s": wall, "peak_bytes": self.peak_bytes, "budget_bytes": self.budget,
                 "bytes_per_cell": self.bytes_per_cell}
+
+
+class SlotServingEngine:
+    """Continuous batching over one resident batch of scenario slots.
+
+    The engine builds one RiverSolver once: ``copies`` slots of every mesh in
+    the pool (a prepared scenario mesh with its rotor layout), as many copies
+    as the HBM budget holds. A request names a pool mesh, its own discharge
+    (in its case's forcing) and a simulated duration. Between two intervals
+    of the batch, queued requests take free slots of their mesh (first fit,
+    any queue position): the slot's state, forcing and step hint are loaded
+    (RiverSolver.load_scenario) and the slot joins the next interval; a slot
+    whose request is done goes idle (dt 0: the device active set skips it at
+    no cost) and is free for the next request. So requests that arrive while
+    others run join the resident batch within one interval, nothing is
+    rebuilt, and state stays on the device until a request finishes.
+    """
+
+    def __init__(self, pool, precision="mixed", interval=0.5, budget_bytes=150e9, copies=None, max_copies=4,
+                 clock=time.perf_counter):
+        from .solver import RiverSolver
+        self.pool = list(pool)
+        self.precision = precision
+        self.interval = float(interval)
+        self.budget = float(budget_bytes)
+        self.clock = clock
+        if copies is None:
+            # device bytes per cell from the smallest pool mesh, 10% margin
+            small = min(self.pool, key=lambda c: c["mesh"].nc)
+            probe = RiverSolver(small, precision=precision)
+            per_cell = 1.1 * probe.device_bytes() / small["mesh"].nc
+            probe.close()
+            per_copy = per_cell * sum(c["mesh"].nc for c in self.pool)
+            copies = int(max(1, min(max_copies, self.budget // max(per_copy, 1.0))))
+        self.copies = int(copies)
+        self.slot_mesh = [i for i in range(len(self.pool)) for _ in range(self.copies)]
+        self.solver = RiverSolver([self.pool[i] for i in self.slot_mesh], precision=precision)
+        self.bytes = self.solver.device_bytes()
+        if self.bytes > self.budget:
+            self.solver.close()
+            raise MemoryError(f"{self.copies} copies of the pool take {self.bytes} B, above the budget")
+        n = len(self.slot_mesh)
+        self.free = {i: deque(k for k in range(n) if self.slot_mesh[k] == i) for i in range(len(self.pool))}
+        self.req = [None] * n
+        self.t = np.zeros(n)
+        self.queue = deque()
+        self.done = []
+        self.cell_updates = 0
+        self.running = False
+        self.t0 = None
+        self.trace = []                  # (engine time, queued, running requests) per interval
+        off = self.solver.packed["cell_offset"]
+        self.cells = np.diff(off).astype(np.int64)
+
+    def now(self):
+        return self.clock() - self.t0
+
+    def _admit(self):
+        left = deque()
+        now = self.now()
+        while self.queue:
+            r = self.queue.popleft()
+            slots = self.free[r.base]
+            if not slots:
+                left.append(r)
+                continue
+            k = slots.popleft()
+            self.solver.load_scenario(k, r.case["q"], r.case.get("forcing"))
+            self.req[k] = r
+            self.t[k] = 0.0
+            r.admitted = now
+        self.queue = left
+
+    def _start(self):
+        dt = np.zeros(len(self.req))
+        for k, r in enumerate(self.req):
+            if r is not None:
+                dt[k] = min(self.interval, r.duration - self.t[k])
+        if not (dt > 0).any():
+            return False
+        self._dt = dt
+        self.solver.advance_start(dt, self.t)
+        self.running = True
+        self.trace.append((self.now(), len(self.queue), int((dt > 0).sum())))
+        return True
+
+    def _finish(self, diags):
+        self.running = False
+        finished = []
+        for k, (r, d) in enumerate(zip(self.req, diags)):
+            if r is None or self._dt[k] <= 0:
+                continue
+            r.substeps += d["hydraulic_substeps"]
+            self.cell_updates += d["hydraulic_substeps"] * int(self.cells[k])
+            if d["failed"]:
+                r.failed = d["failed"]
+                self.t[k] = r.duration
+            else:
+                self.t[k] += self._dt[k]
+            if self.t[k] >= r.duration - 1e-9 * max(1.0, r.duration):
+                finished.append(k)
+        if finished:
+            rec = self.solver.turbine_record() if self.solver.rotors is not None else None
+            now = self.now()
+            for k in finished:
+                r = self.req[k]
+                r.state = self.solver.state(k).copy()
+                if rec is not None:
+                    r.rotors = rec[np.flatnonzero(self.solver.rotors["scenario"] == k)].copy()
+                r.finished = now
+                self.done.append(r)
+                self.req[k] = None
+                self.free[self.slot_mesh[k]].append(k)
+
+    def run(self, arrivals, idle_sleep=2e-4, max_wall=None):
+        """Serve requests (each with ``base``, the pool index of its mesh) whose
+        ``arrival`` is an engine-clock time; returns the finished requests."""
+        pending = sorted(arrivals, key=lambda r: r.arrival)
+        self.t0 = self.clock()
+        k = 0
+        while k < len(pending) or self.queue or self.running or any(r is not None for r in self.req):
+            now = self.now()
+            if max_wall is not None and now > max_wall:
+                raise TimeoutError(f"serving loop exceeded {max_wall} s with {len(self.queue)} queued")
+            while k < len(pending) and pending[k].arrival <= now:
+                self.queue.append(pending[k])
+                k += 1
+            if self.running:
+                diags = self.solver.advance_poll()
+                if diags is None:
+                    time.sleep(idle_sleep)
+                    continue
+                self._finish(diags if isinstance(diags, list) else [diags])
+            self._admit()
+            if not self._start():
+                time.sleep(idle_sleep)
+        return self.done
+
+    def report(self):
+        lat = np.array([r.latency for r in self.done if r.latency is not None])
+        wait = np.array([r.admitted - r.arrival for r in self.done if r.admitted is not None])
+        wall = max((r.finished for r in self.done), default=0.0)
+        q = np.array([x[1] for x in self.trace]) if self.trace else np.zeros(1)
+        act = np.array([x[2] for x in self.trace]) if self.trace else np.zeros(1)
+        return {"requests": len(self.done), "failed": sum(1 for r in self.done if r.failed),
+                "latency_s": {"p50": float(np.percentile(lat, 50)) if len(lat) else None,
+                              "p99": float(np.percentile(lat, 99)) if len(lat) else None,
+                              "max": float(lat.max()) if len(lat) else None},
+                "admission_wait_s": {"p50": float(np.percentile(wait, 50)) if len(wait) else None,
+                                     "p99": float(np.percentile(wait, 99)) if len(wait) else None},
+                "queue_length": {"mean": float(q.mean()), "max": int(q.max()),
+                                 "by_decile": [int(x) for x in q[np.linspace(0, len(q) - 1, 10).astype(int)]]},
+                "running_requests": {"mean": float(act.mean()), "max": int(act.max())},
+                "throughput_cell_updates_s": self.cell_updates / wall if wall > 0 else None,
+                "wall_s": wall, "intervals": len(self.trace), "slots": len(self.req), "copies": self.copies,
+                "resident_bytes": self.bytes, "budget_bytes": self.budget}
+
+    def close(self):
+        self.solver.close()
 
 
 def poisson_arrivals(rate, window, seed):

@@ -698,6 +698,27 @@ class RiverSolver:
         return rate, water, status, freq
 
     # ------------------------------------------------------------------
+    def load_scenario(self, i, q, forcing=None):
+        """Re-use scenario slot i for a new run: its state (3, nc_i) into the
+        resident buffer, its open-boundary forcing (2, nseg_i) when given, and
+        its step hint cleared (the next interval starts at its full length, as
+        a new solver does). Between intervals only."""
+        a, b = int(self.packed["cell_offset"][i]), int(self.packed["cell_offset"][i + 1])
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        if q.shape != (3, b - a):
+            raise ValueError(f"scenario {i} takes a (3, {b - a}) state")
+        self.torch.cuda.current_stream().synchronize()
+        self.q[:, a:b].copy_(self.torch.from_numpy(q))
+        if forcing is not None:
+            s0, s1 = int(self.packed["seg_offset"][i]), int(self.packed["seg_offset"][i + 1])
+            f = self.packed["forcing"]
+            f[:, s0:s1] = np.asarray(forcing, dtype=np.float64)[:, :s1 - s0]
+            check(self.lib.brx_forcing_set(self.h, _ptr(f)))
+        hints = self.hints()
+        hints[i] = 0.0
+        self.set_hints(hints)
+        self.torch.cuda.current_stream().synchronize()
+
     def set_state(self, q):
         self.q.copy_(self.torch.from_numpy(_f64(q)))
 

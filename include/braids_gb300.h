@@ -158,6 +158,15 @@ int brx_inlet_lines_set(brx_solver *s, const int *kind, const double *slope, con
 int brx_boundary_set(brx_solver *s, const int *seg_mode, const int *stage_policy,
                      const double *exterior_bed, const double *forcing);
 
+/* Replace the constant forcing of every open segment, host forcing (2, nseg)
+ * in the layout of brx_boundary_set (row 0 discharge, row 1 stage), keeping
+ * modes, exterior beds and section tables; solved inlet reference lines are
+ * cleared. For serving loops that re-use a resident scenario slot for a
+ * request with its own discharge (the reference sets a scenario's forcing
+ * once, river_exterior_bed.py:189-235). Not while an asynchronous interval
+ * is in flight. */
+int brx_forcing_set(brx_solver *s, const double *forcing);
+
 /* Piecewise-linear forcing tables: time (len >= 2, increasing), value
  * (2,nseg,len) rows discharge and stage. len = 0 returns to constant forcing.
  * Replaces RiverHydraulicSchedule.sample
