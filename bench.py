@@ -32,12 +32,13 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 METRIC = "cell-updates/s"
 BYTES_PER_CELL_UPDATE = {"fp64": 680.0, "mixed": 384.0}   # algorithmic bytes, two-sweep design
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per cell of one
-# launch of each mixed-form sweep, from one ncu --set full capture of the
-# 24-scenario subset with rotors (scenarios 20..43, 1,967,962 cells, inputs
-# larger than L2): a launch of the full batch is scaled by its cells
-TRAFFIC_BYTES_PER_CELL = {"mixed": {"cells": 244.24, "faces": 213.26, "gather": 145.79, "update": 171.48,
-                                    "drag": 62.05, "limit": 46.90}}
-KERNEL_NAMES = ["drag", "boundary", "cells", "faces", "gather", "limit", "update", "control"]
+# launch of each mixed-form sweep, each kernel captured alone (ncu --set full,
+# one launch) on the 24-scenario subset with rotors (scenarios 20..43 sorted
+# by size, 1,967,962 cells, inputs larger than L2): a launch of the full batch
+# is scaled by its cells
+TRAFFIC_BYTES_PER_CELL = {"mixed": {"cells": 244.21, "faces": 213.25, "gather": 145.97, "update": 190.15,
+                                    "drag": 63.07}}
+KERNEL_NAMES = ["drag", "boundary", "cells", "faces", "gather", "update", "control"]
 
 
 def peaks():
@@ -180,10 +181,9 @@ def algorithmic_bytes(kernel, nc, nf, nadj, nslot, precision="fp64", rotor_cells
                     rotor_cells * (2 * 4 + 1) + rotor_faces * (16 + 8))
         if kernel == "gather":   # id, CSR, record flags, stock, rate/theta out; per entry weight; face fluxes
             return nc * (i4 + i4 + 4 + d8 + 3 * d8 + d8 + i4) + nadj * (i4 + d8) + nf * (8 + 16)
-        if kernel == "limit":
-            return nf * (8 + 2 * i4 + i4 + i4 + 16) + nc * (d8 + 3 * d8)
-        if kernel == "update":
-            return nc * (i4 + i4 + 3 * d8 + 6 * d8 + 3 * d8) + nadj * (i4 + d8) + nf * 16
+        if kernel == "update":    # id, CSR, rate, stage states in/out, primitives out, donor factors; per
+            # entry face id, FP64 and FP32 weights, other cell + flags; per face the FP32 water
+            return nc * (i4 + i4 + 2 * 4 + 3 * d8 + 3 * d8 + d8 + 32 + 4) + nadj * (i4 + d8 + 4 + 8) + nf * 8
         if kernel == "drag":
             return nc * (i4 + 6 * d8)
         return 0
