@@ -618,36 +618,54 @@ def main():
                                                   bed_after_timed, rotors_after_timed, torch)
         plain = {"value": cfg["accuracy_vs_fp64"]["fp64_value"], "unit": METRIC,
                  "note": "the same scenario in the FP64 form over the same intervals"}
-    hllc_batch = None
+    hllc_batch, hllc_mixed = None, None
     if args.hllc and precision == "mixed" and len(cases) > 1:
-        # the whole batch with the HLLC method (FP64 form): one warm-up and up to two timed intervals
-        hs = RiverSolver(cases, precision="fp64", method="hllc")
+        # the whole batch with the HLLC method, FP64 form then mixed form: one warm-up and up to two timed
+        # intervals each, from the same initial state, so the mixed form's depth is compared after the same
+        # intervals
         from braids_hkt_gb300 import autotune
-        htuned = autotune.tune(hs, cache=False)
-        t_sim, ms, ups, hfail = 0.0, 0.0, 0, set()
-        for k in range(1 + max(1, min(args.steps, 2))):
-            flush_l2(torch, flush)
-            torch.cuda.synchronize()
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(hs.stream)
-            ds = hs.advance(outer, t_sim, raise_on_failure=False)
-            e1.record(hs.stream)
-            e1.synchronize()
-            t_sim += outer
-            hfail |= {i for i, d in enumerate(ds) if d["failed"]}
-            if k >= 1:
-                ms += e0.elapsed_time(e1)
-                ups += sum(int(d["hydraulic_substeps"]) * int(hs.packed["cell_offset"][i + 1] - hs.packed["cell_offset"][i])
-                           for i, d in enumerate(ds))
-        hprof = hs.profile_substep(0.5 * min(d["hydraulic_next_substep_hint_s"] for d in ds), t_sim)
-        hllc_batch = {"value": ups / (ms / 1e3), "unit": METRIC, "ms_per_interval": ms / max(1, min(args.steps, 2)),
-                      "failed_scenarios": sorted(hfail),
-                      "substep_kernels_ms": [(n, round(v, 4)) for n, v in hprof],
-                      "autotune": {k: htuned[k] for k in ("kernels", "chunk", "substep_ms_default", "substep_ms_tuned")},
-                      "note": "the whole batch (rotors included) with the HLLC MUSCL-Hancock method, FP64 form; "
-                              "one cell-update = one cell advanced by one accepted Hancock substep"}
-        hs.close()
+        legs, finals = {}, {}
+        for hprec in ("fp64", "mixed"):
+            hs = RiverSolver(cases, precision=hprec, method="hllc")
+            htuned = autotune.tune(hs, cache=False)
+            t_sim, ms, ups, hfail = 0.0, 0.0, 0, set()
+            for k in range(1 + max(1, min(args.steps, 2))):
+                flush_l2(torch, flush)
+                torch.cuda.synchronize()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(hs.stream)
+                ds = hs.advance(outer, t_sim, raise_on_failure=False)
+                e1.record(hs.stream)
+                e1.synchronize()
+                t_sim += outer
+                hfail |= {i for i, d in enumerate(ds) if d["failed"]}
+                if k >= 1:
+                    ms += e0.elapsed_time(e1)
+                    ups += sum(int(d["hydraulic_substeps"]) *
+                               int(hs.packed["cell_offset"][i + 1] - hs.packed["cell_offset"][i])
+                               for i, d in enumerate(ds))
+            finals[hprec] = hs.q.cpu().numpy()
+            hprof = hs.profile_substep(0.5 * min(d["hydraulic_next_substep_hint_s"] for d in ds), t_sim)
+            legs[hprec] = {"value": ups / (ms / 1e3), "unit": METRIC,
+                           "ms_per_interval": ms / max(1, min(args.steps, 2)), "failed_scenarios": sorted(hfail),
+                           "substep_kernels_ms": [(n, round(v, 4)) for n, v in hprof],
+                           "autotune": {k: htuned[k] for k in ("kernels", "chunk", "substep_ms_default",
+                                                              "substep_ms_tuned")},
+                           "note": f"the whole batch (rotors included) with the HLLC MUSCL-Hancock method, {hprec} "
+                                   "form; one cell-update = one cell advanced by one accepted Hancock substep"}
+            hs.close()
+        hllc_batch, hllc_mixed = legs["fp64"], legs["mixed"]
+        h64, hmx = finals["fp64"][0], finals["mixed"][0]
+        rel = np.abs(hmx - h64) / np.maximum(h64, 1e-3)
+        deep = h64 > 0.05
+        hllc_mixed["accuracy_vs_fp64"] = {"depth_rel_max": float(rel.max()),
+                                          "depth_rel_p99_deep": float(np.percentile(rel[deep], 99)),
+                                          "unit_discharge_rel_max": float(np.abs(finals["mixed"][1:] - finals["fp64"][1:]).max() /
+                                                                          max(np.abs(finals["fp64"][1:]).max(), 1e-12)),
+                                          "after_sim_s": (1 + max(1, min(args.steps, 2))) * outer,
+                                          "stated_tolerance": 1e-4}
+        hllc_mixed["speedup_vs_fp64_hllc"] = hllc_mixed["value"] / hllc_batch["value"]
     if rank != 0:
         return
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
@@ -669,6 +687,8 @@ def main():
         line["batched_vs_plain_fp64"] = value / plain["value"]
     if hllc_batch is not None:
         line["hllc_fp64_batch"] = hllc_batch
+    if hllc_mixed is not None:
+        line["hllc_mixed_batch"] = hllc_mixed
     if precision == "mixed" and not args.no_serving and len(cases) > 1:
         solver.close()
         try:

@@ -69,6 +69,7 @@ struct brx_solver {
     std::vector<int> active;
     std::vector<int> cell_offset, face_offset, seg_offset;
     std::vector<int> h_bid, h_owner, h_neighbour, h_slot_face, h_offset;
+    std::vector<double> h_length, h_area;   // host copies for the mixed HLLC stencil tables
     int *d_bmode_rw = nullptr;       // writable alias of mesh.bmode
     int *d_seg_mode_rw = nullptr, *d_stage_policy_rw = nullptr;
     double *d_ext_bed_rw = nullptr, *d_table_time = nullptr, *d_table_value = nullptr;
@@ -233,6 +234,8 @@ extern "C" int brx_solver_create(int nscen, const int *cell_offset, const int *f
         s->h_owner.assign(owner, owner + nf);
         s->h_neighbour.assign(neighbour, neighbour + nf);
         s->h_offset.assign(offset, offset + nc + 1);
+        s->h_length.assign(length, length + nf);
+        s->h_area.assign(area, area + nc);
         // derived host tables
         std::vector<int> csid(nc), fsid(nf), bslot(nf, -1), cflags(nc, 0);
         for (int i = 0; i < nscen; ++i) {
@@ -936,6 +939,32 @@ extern "C" int brx_hllc_set(brx_solver *s, const int *entry_face, const int *ent
     TRY(s->upload(&p_ent, ent.data(), nadj)); TRY(s->upload(&p_geo, geo.data(), nadj));
     TRY(s->upload(&p_inv, inverse, 3 * (size_t)nc));
     s->hllc.ent = p_ent; s->hllc.geo = p_geo; s->hllc.inverse = p_inv;
+    if (s->precision == BRX_MIXED) {
+        // FP32 stencil of the mixed form: LS offset over its squared length
+        // (zero for coincident centres), midpoint offset, the LS inverse, and
+        // signed length / area in FP32 and FP64 per entry
+        std::vector<float4> hgeo(nadj), hinv(nc);
+        std::vector<float> hw4(nadj);
+        std::vector<double> hw8(nadj);
+        for (int c = 0; c < nc; ++c) {
+            hinv[c] = make_float4(float(inverse[c]), float(inverse[nc + c]), float(inverse[2 * (size_t)nc + c]), 0.f);
+            for (int k = s->h_offset[c]; k < s->h_offset[c + 1]; ++k) {
+                const double dx = geo[k].x, dy = geo[k].y, d2 = dx * dx + dy * dy;
+                hgeo[k] = d2 > 0. ? make_float4(float(dx / d2), float(dy / d2), float(geo[k].z), float(geo[k].w))
+                                  : make_float4(0.f, 0.f, float(geo[k].z), float(geo[k].w));
+                const int x = ent[k].x, f = x >= 0 ? x : ~x;
+                hw8[k] = (x >= 0 ? 1. : -1.) * s->h_length[f] / s->h_area[c];
+                hw4[k] = float(hw8[k]);
+            }
+        }
+        float4 *p_hgeo, *p_hinv;
+        float *p_hw4;
+        double *p_hw8;
+        TRY(s->upload(&p_hgeo, hgeo.data(), nadj)); TRY(s->upload(&p_hinv, hinv.data(), nc));
+        TRY(s->upload(&p_hw4, hw4.data(), nadj)); TRY(s->upload(&p_hw8, hw8.data(), nadj));
+        TRY(s->alloc(&s->mx.hcdb, nadj));
+        s->mx.hent = p_ent; s->mx.hgeo = p_hgeo; s->mx.hinv = p_hinv; s->mx.hw4 = p_hw4; s->mx.hw8 = p_hw8;
+    }
     s->hllc_ready = true;
     return BRX_OK;
 }
@@ -946,8 +975,9 @@ extern "C" int brx_method_set(brx_solver *s, int method)
     if (s->pending) return fail(BRX_ERR_STATE, "an asynchronous interval is in flight");
     if (method != BRX_METHOD_FWAVE && method != BRX_METHOD_HLLC) return fail(BRX_ERR_ARGUMENT, "unknown method");
     if (method == BRX_METHOD_HLLC) {
-        if (s->precision != BRX_FP64) return fail(BRX_ERR_UNSUPPORTED, "the HLLC method runs in the FP64 form");
         if (!s->hllc_ready) return fail(BRX_ERR_STATE, "HLLC stencil not installed (brx_hllc_set)");
+        if (s->precision == BRX_MIXED && s->any_stress)
+            return fail(BRX_ERR_UNSUPPORTED, "the mixed HLLC form has no rotor ambient stress (nu > 0)");
         if (s->maxdeg > MAX_CELL_FACES) return fail(BRX_ERR_UNSUPPORTED, "cell with too many faces");
     }
     s->method = method;
@@ -964,7 +994,7 @@ extern "C" int brx_method_set(brx_solver *s, int method)
 static int max_block(const brx_solver *s, int kind)
 {
     if (kind < 0 || kind >= NSHAPE) return 0;
-    if (s->precision == BRX_MIXED) return kind >= 20 ? 0 : mixed_max_block(kind, s->maxdeg);
+    if (s->precision == BRX_MIXED) return mixed_max_block(kind, s->maxdeg);
     const bool small = s->maxdeg <= 4;
     const void *fn = nullptr;
     switch (kind) {
@@ -1318,12 +1348,20 @@ static void enqueue_stage(brx_solver *s, int stage, double *rate_out)
 }
 
 // HLLC / MUSCL-Hancock kernels of one substep (kinds of the profile), on st.
-enum HllcKind { KH_CELLS = 20, KH_PREDICT = 21, KH_BOUNDARY = 22, KH_FACES = 23, KH_BUDGET = 24, KH_TURB = 25,
-                KH_UPDATE = 26, KH_TURB0 = 27 };
 
 static int launch_hllc(brx_solver *s, int kind, cudaStream_t st = nullptr)
 {
     if (!st) st = s->stream;
+    if (s->precision == BRX_MIXED) {
+        // the mixed form: its own cell, predictor, face, budget and update
+        // kernels; the exterior owner is the mixed boundary CTA at t + dt/2
+        switch (kind) {
+        case KH_TURB0: return s->has_turb ? launch_turbines(s, 1, st) : 0;
+        case KH_TURB: return s->has_turb ? launch_turbines(s, 2, st) : 0;
+        case KH_BOUNDARY: return mixed_kernel(make_launch(s, st), K_BOUNDARY, STAGE_HANCOCK, nullptr);
+        default: return mixed_hllc_kernel(make_launch(s, st), kind);
+        }
+    }
     HCell *rec = reinterpret_cast<HCell *>(s->work.rec);      // 96 of the 128 bytes per cell
     switch (kind) {
     case KH_CELLS:

@@ -30,7 +30,18 @@ struct MixedGeo {
     const float2 *hcc;       // (nf) neighbour centroid - owner centroid
     float *hgrad;            // (6, nc) wet gradients of u, v, eta
     float2 *hp, *hs;         // (nf) balanced-pressure correction, ambient stress
+    // HLLC / MUSCL-Hancock method (its own incidence, faces ascending per cell)
+    const int2 *hent;        // (nadj) face or ~face (neighbour side); other cell, -1 wall, -2 open face
+    const float4 *hgeo;      // (nadj) LS offset over its squared length (x, y); face midpoint - centroid (x, y)
+    const float4 *hinv;      // (nc) least-squares inverse (i11, i12, i22, 0)
+    const float *hw4;        // (nadj) signed length / area, FP32 (momentum, outflow and CFL sums)
+    const double *hw8;       // (nadj) signed length / area, FP64 (mass)
+    float *hcdb;             // (nadj) bed of the other cell - own bed (0 for walls and open faces)
 };
+
+// HLLC kinds of one substep (their launch-shape slots), shared by both forms.
+enum HllcKind { KH_CELLS = 20, KH_PREDICT = 21, KH_BOUNDARY = 22, KH_FACES = 23, KH_BUDGET = 24, KH_TURB = 25,
+                KH_UPDATE = 26, KH_TURB0 = 27 };
 
 // Launch shape of one kernel kind: threads per block and the grid cap in
 // resident blocks per SM (grid = min(ceil(n / block), per_sm * SMs); the
@@ -80,5 +91,10 @@ int mixed_kernel(const Launch &L, int kind, int stage, double *out);
 // Largest block the mixed form's kernel of this kind accepts (its launch
 // bounds and registers), 0 for a kind without a tunable kernel.
 int mixed_max_block(int kind, int maxdeg);
+
+// Mixed form of the HLLC / MUSCL-Hancock method: launch one kernel of the
+// given HLLC kind (cells, predictor source, faces, budget, update; the
+// boundary, drag and rotor kinds are the f-wave's). Returns launches.
+int mixed_hllc_kernel(const Launch &L, int kind);
 
 }  // namespace brx

@@ -280,6 +280,11 @@ __global__ void __launch_bounds__(128) km_bed(MeshDev m, StateDev s, MixedGeo g)
             }
             g.cdb[k] = d;
         }
+        if (g.hent)          // the HLLC incidence (faces ascending per cell)
+            for (int k = k0; k < k0 + deg; ++k) {
+                const int o = g.hent[k].y;
+                g.hcdb[k] = o >= 0 ? float(s.z[o] - zc) : 0.f;
+            }
         float2 gb = make_float2(0.f, 0.f);
         const float4 inv = g.cinv[c];
         if (inv.x != 0.f || inv.y != 0.f || inv.z != 0.f) {
@@ -1101,6 +1106,8 @@ __global__ void km_water_out(MeshDev m, Work w, double *water)
     for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < m.nf; f += gridDim.x * blockDim.x) water[f] = lim[f].water;
 }
 
+#include "brx_hllc_mixed.cuh"
+
 }  // namespace brx_mx
 
 // The boundary CTA of the mixed form is the FP64 kernel (few faces, FP64 sums).
@@ -1120,11 +1127,46 @@ int mixed_max_block(int kind, int maxdeg)
     case K_GATHER: fn = (const void *)brx_mx::km_gather; break;
     case K_LIMIT: fn = (const void *)brx_mx::km_limit; break;
     case K_UPDATE: fn = (const void *)brx_mx::km_update; break;
+    case KH_CELLS: fn = (const void *)brx_mx::km_hllc_cells; break;
+    case KH_PREDICT: fn = (const void *)brx_mx::km_hllc_predict; break;
+    case KH_FACES: fn = (const void *)brx_mx::km_hllc_faces; break;
+    case KH_BUDGET: fn = (const void *)brx_mx::km_hllc_budget; break;
+    case KH_UPDATE: fn = (const void *)brx_mx::km_hllc_update; break;
     default: return 0;
     }
     cudaFuncAttributes a;
     if (cudaFuncGetAttributes(&a, fn) != cudaSuccess) return 0;
     return a.maxThreadsPerBlock;
+}
+
+int mixed_hllc_kernel(const Launch &L, int kind)
+{
+    cudaStream_t st = L.stream;
+    const int nc = L.mesh.nc, nf = L.mesh.nf;
+    brx_mx::HCellF *rec = reinterpret_cast<brx_mx::HCellF *>(L.work.rec);
+#define SHAPE(kind_, n_) shape_grid(L, kind_, n_), L.shape[kind_].block
+    switch (kind) {
+    case KH_CELLS:
+        brx_mx::km_hllc_cells<<<SHAPE(KH_CELLS, nc), 0, st>>>(L.mesh, L.state, L.ctrl, L.mx, rec);
+        return 1;
+    case KH_PREDICT:
+        if (!L.has_turb) return 0;
+        brx_mx::km_hllc_predict<<<SHAPE(KH_PREDICT, nc), 0, st>>>(L.mesh, L.state, L.turb, L.ctrl, rec);
+        return 1;
+    case KH_FACES:
+        brx_mx::km_hllc_faces<<<SHAPE(KH_FACES, nf), 0, st>>>(L.mesh, L.state, L.bnd, L.ctrl, L.work, L.mx, L.turb,
+                                                              L.has_turb, rec);
+        return 1;
+    case KH_BUDGET:
+        brx_mx::km_hllc_budget<<<SHAPE(KH_BUDGET, nc), 0, st>>>(L.mesh, L.state, L.ctrl, L.work, L.mx);
+        return 1;
+    case KH_UPDATE:
+        brx_mx::km_hllc_update<<<SHAPE(KH_UPDATE, nc), 0, st>>>(L.mesh, L.state, L.ctrl, L.work, L.mx, L.turb,
+                                                                L.has_turb);
+        return 1;
+    }
+#undef SHAPE
+    return 0;
 }
 
 int mixed_kernel(const Launch &L, int kind, int stage, double *out)

@@ -135,7 +135,9 @@ def test_hllc_rotor_record_after_advance():
 
 
 def test_hllc_scope_errors():
+    """The mixed HLLC form has no rotor ambient stress: a rotor array with a
+    positive ambient viscosity is refused there."""
     from braids_hkt_gb300.solver import RiverSolver
-    case, _ = case_of("channel")
+    case = S.small_rotor_channel(nu=0.005)
     with pytest.raises(Exception):
         RiverSolver(case, precision="mixed", method="hllc")
