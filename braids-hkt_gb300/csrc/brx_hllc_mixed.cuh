@@ -55,7 +55,10 @@ __device__ __forceinline__ void hllc_riemann_f(float hl, float ul, float vl, flo
     if (sl >= 0.f) { out[0] = fl0; out[1] = fl1; out[2] = fl2; return; }
     if (sr <= 0.f) { out[0] = fr0; out[1] = fr1; out[2] = fr2; return; }
     const float a = hl * (sl - ul), b = hr * (sr - ur), den = a - b;
-    const float sm = fabsf(den) > 1e-30f ? __fdividef(.5f * g * (hr * hr - hl * hl) + a * ul - b * ur, den) : 0.f;
+    // (hr - hl)(hr + hl), not hr^2 - hl^2: a contracted hr * hr - hl * hl
+    // leaves the rounding residual of hl^2 for equal depths, a spurious
+    // contact speed and water flux on a surface at rest
+    const float sm = fabsf(den) > 1e-30f ? __fdividef(.5f * g * ((hr - hl) * (hr + hl)) + a * ul - b * ur, den) : 0.f;
     if (hl > dry && hr > dry && sl < sm && sm < sr) {
         // star depth minus side depth, h (s_m - u) / (s - s_m): zero for a state at rest
         const float dl = __fdividef(hl * (sm - ul), sl - sm), dr = __fdividef(hr * (sm - ur), sr - sm);
