@@ -25,6 +25,7 @@ SIGNATURES = {
     "brx_boundary_set": (I, [P, P, P, P, P]),
     "brx_forcing_table_set": (I, [P, I, P, P]),
     "brx_forcing_set": (I, [P, P]),
+    "brx_viscosity_set": (I, [P, P, P, P, P]),
     "brx_state_bind": (I, [P, P, P]),
     "brx_advance": (I, [P, D, D, P]),
     "brx_advance_batch": (I, [P, P, P, P]),

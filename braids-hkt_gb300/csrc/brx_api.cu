@@ -91,6 +91,7 @@ struct brx_solver {
     TurbDev turb{};                  // rotor arrays
     bool has_turb = false;
     bool any_stress = false;         // some rotor scenario has a positive ambient viscosity
+    bool any_visc = false;           // some scenario has the wet-bank viscosity
     int nrotor = 0;
     double *d_tdiag_out = nullptr;   // (nrotor, 16) diagnostics of brx_turbines_diagnose
     ExnerDev exner{};                // bed model (valid when has_exner)
@@ -969,6 +970,38 @@ extern "C" int brx_hllc_set(brx_solver *s, const int *entry_face, const int *ent
     return BRX_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Conservative wet-bank viscosity (shoreline_viscosity.py:46-72)
+// ---------------------------------------------------------------------------
+extern "C" int brx_viscosity_set(brx_solver *s, const double *nu, const double *dxdy, const double *inverse,
+                                 const double *xy)
+{
+    if (!s || !nu || !dxdy || !inverse || !xy) return fail(BRX_ERR_ARGUMENT, "null argument");
+    if (s->pending) return fail(BRX_ERR_STATE, "an asynchronous interval is in flight");
+    if (s->method == BRX_METHOD_HLLC) return fail(BRX_ERR_UNSUPPORTED, "the wet-bank viscosity runs with the f-wave method");
+    bool any = false;
+    for (int i = 0; i < s->nscen; ++i) {
+        if (!std::isfinite(nu[i]) || nu[i] < 0) return fail(BRX_ERR_ARGUMENT, "viscosity coefficients must be finite and >= 0");
+        any = any || nu[i] > 0;
+    }
+    const int nc = s->nc, nf = s->nf, nadj = s->nadj;
+    for (size_t k = 0; k < 3 * (size_t)nc; ++k)
+        if (!std::isfinite(inverse[k])) return fail(BRX_ERR_ARGUMENT, "nonfinite least-squares inverse");
+    ViscDev &v = s->work.visc;
+    if (!v.nu) {
+        double *p_nu, *p_dxdy, *p_inv, *p_xy;
+        TRY(s->upload(&p_nu, nu, s->nscen)); TRY(s->upload(&p_dxdy, dxdy, 2 * (size_t)nadj));
+        TRY(s->upload(&p_inv, inverse, 3 * (size_t)nc)); TRY(s->upload(&p_xy, xy, 2 * (size_t)nc));
+        TRY(s->alloc(&v.grad, 4 * (size_t)nc)); TRY(s->alloc(&v.face, 2 * (size_t)nf));
+        v.nu = p_nu; v.dxdy = p_dxdy; v.inverse = p_inv; v.xy = p_xy;
+    } else {
+        CK(cudaMemcpy(const_cast<double *>(v.nu), nu, sizeof(double) * s->nscen, cudaMemcpyHostToDevice));
+    }
+    s->any_visc = any;
+    s->graph_dirty = true;
+    return BRX_OK;
+}
+
 extern "C" int brx_method_set(brx_solver *s, int method)
 {
     if (!s) return fail(BRX_ERR_ARGUMENT, "null solver");
@@ -978,6 +1011,7 @@ extern "C" int brx_method_set(brx_solver *s, int method)
         if (!s->hllc_ready) return fail(BRX_ERR_STATE, "HLLC stencil not installed (brx_hllc_set)");
         if (s->precision == BRX_MIXED && s->any_stress)
             return fail(BRX_ERR_UNSUPPORTED, "the mixed HLLC form has no rotor ambient stress (nu > 0)");
+        if (s->any_visc) return fail(BRX_ERR_UNSUPPORTED, "the wet-bank viscosity runs with the f-wave method");
         if (s->maxdeg > MAX_CELL_FACES) return fail(BRX_ERR_UNSUPPORTED, "cell with too many faces");
     }
     s->method = method;
@@ -1285,6 +1319,13 @@ static int launch_kernel(brx_solver *s, int kind, int stage, double *rate_out, c
 {
     if (!st) st = s->stream;
     if (kind == K_TURB) return launch_turbines(s, stage, st);
+    if (kind == K_VISC) {
+        if (!s->any_visc) return 0;
+        const double *q = stage == 1 ? s->state.work : s->state.q1;
+        k_visc_grad<<<s->grid_c256, 256, 0, st>>>(s->mesh, s->work, q, s->d_ctrl, stage);
+        k_visc_faces<<<s->grid_f256, 256, 0, st>>>(s->mesh, s->work, q, s->state.z, s->d_ctrl, stage);
+        return 2;
+    }
     if (s->precision == BRX_MIXED) return mixed_kernel(make_launch(s, st), kind, stage, rate_out);
     switch (kind) {
     case K_DRAG:
@@ -1344,6 +1385,7 @@ static void enqueue_stage(brx_solver *s, int stage, double *rate_out)
         s->launches += launch_kernel(s, kind, stage, nullptr);
     if (fork && !mixed) cudaStreamWaitEvent(s->stream, s->join2, 0);
     s->launches += launch_turbines(s, stage, s->stream, TURB_FACES);
+    s->launches += launch_kernel(s, K_VISC, stage, nullptr);
     s->launches += launch_kernel(s, K_UPDATE, stage, rate_out);
 }
 
@@ -1721,7 +1763,7 @@ extern "C" int brx_profile_substep(brx_solver *s, double dt, double time, int ca
         const bool mixed = s->precision == BRX_MIXED;
         for (int stage = 1; stage <= 2; ++stage)
             for (int kind : {(int)K_BOUNDARY, mixed ? (int)K_TURB : -1, (int)K_CELLS, (int)K_FACES, (int)K_GATHER,
-                             mixed ? -1 : (int)K_TURB, (int)K_UPDATE})
+                             mixed ? -1 : (int)K_TURB, (int)K_VISC, (int)K_UPDATE})
                 if (kind >= 0)
                     if (const int nl = launch_kernel(s, kind, stage, nullptr)) { mark(kind); extra += nl - 1; }
     }

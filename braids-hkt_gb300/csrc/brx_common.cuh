@@ -213,7 +213,20 @@ struct __align__(16) CellRec {
 };
 static_assert(sizeof(CellRec) == 128, "cell record is one 128-byte line");
 
+// Conservative wet-bank viscosity (shoreline_viscosity.py:46-72) of the
+// scenarios with a positive coefficient: the flow engines' least-squares
+// metric, cell centres, and the stage's velocity gradients and face stresses.
+struct ViscDev {
+    const double *nu;        // (nscen) coefficient [m2/s]; null: no scenario has one
+    const double *dxdy;      // (2, nadj) centre offsets per CSR entry
+    const double *inverse;   // (3, nc) least-squares pseudo-inverse
+    const double *xy;        // (2, nc)
+    double *grad;            // (4, nc) u_x, u_y, v_x, v_y of the safe state
+    double *face;            // (2, nf) shared-face stress
+};
+
 struct Work {
+    ViscDev visc;
     CellRec *rec;            // (nc)
     double2 *ws;             // (nf) water, CFL speed
     double4_32a *gf;             // (nf) pressure-deviation momentum flux: left x,y, right x,y

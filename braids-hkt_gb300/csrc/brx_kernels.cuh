@@ -2010,6 +2010,90 @@ __global__ void __launch_bounds__(256) k_limit(MeshDev m, StateDev s, Ctrl *ctrl
     }
 }
 
+// ---------------------------------------------------------------------------
+// Conservative wet-bank viscosity (shoreline_viscosity.py:57-72): velocity
+// gradients of the safe state by the flow engines' least squares
+// (bend_methods_v1_kernels.h:23-39, rows u and v; dry columns read as depth
+// 0.001001 without momentum, secondary_vector_ops.py:39-48), then the
+// shared-face stress of wet columns (shoreline_viscosity.h:14-33); the
+// updates gather it as sum(s len stress) / area after the rotor terms.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_visc_grad(MeshDev m, Work w, const double *q, Ctrl *ctrl, int stage)
+{
+    const int n = m.nc, na = m.nadj;
+    const ViscDev v = w.visc;
+    FOR_ACTIVE_CELLS(m.act, i) {
+        const int sid = m.cell_sid[i];
+        if (!(v.nu[sid] > 0.) || skip_stage(ctrl[sid], stage)) continue;
+        const double dry = ctrl[sid].dry;
+        const bool wi = q[i] > dry;
+        const double hi = wi ? q[i] : .001001;
+        const double x0 = (wi ? q[n + i] : 0.) / hi, x1 = (wi ? q[2 * n + i] : 0.) / hi;
+        double bx0 = 0., bx1 = 0., by0 = 0., by1 = 0.;
+        for (int k = m.offset[i]; k < m.offset[i + 1]; ++k) {
+            const int f = m.faces[k], j = m.owner[f] == i ? m.neighbour[f] : m.owner[f];
+            if (j < 0) continue;
+            const double dx = v.dxdy[k], dy = v.dxdy[na + k], wt = 1. / (dx * dx + dy * dy);
+            const bool wj = q[j] > dry;
+            const double hj = wj ? q[j] : .001001;
+            const double y0 = (wj ? q[n + j] : 0.) / hj, y1 = (wj ? q[2 * n + j] : 0.) / hj;
+            bx0 += wt * dx * (y0 - x0); by0 += wt * dy * (y0 - x0);
+            bx1 += wt * dx * (y1 - x1); by1 += wt * dy * (y1 - x1);
+        }
+        v.grad[i] = v.inverse[i] * bx0 + v.inverse[n + i] * by0;
+        v.grad[n + i] = v.inverse[n + i] * bx0 + v.inverse[2 * n + i] * by0;
+        v.grad[2 * n + i] = v.inverse[i] * bx1 + v.inverse[n + i] * by1;
+        v.grad[3 * n + i] = v.inverse[n + i] * bx1 + v.inverse[2 * n + i] * by1;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_visc_faces(MeshDev m, Work w, const double *q, const double *z, Ctrl *ctrl,
+                                                    int stage)
+{
+    const int n = m.nc, nf = m.nf;
+    const ViscDev v = w.visc;
+    FOR_ACTIVE_FACES(m.act, i) {
+        const int sid = m.face_sid[i];
+        const double nu = v.nu[sid];
+        if (!(nu > 0.) || skip_stage(ctrl[sid], stage)) continue;
+        const double dry = ctrl[sid].dry;
+        double sx = 0., sy = 0.;
+        const int o = m.owner[i], j = m.neighbour[i];
+        if (j >= 0 && q[o] > dry && q[j] > dry) {
+            double h = fmin(q[o], q[j]);
+            h = fmin(h, fmax(0., .5 * (q[o] + z[o] + q[j] + z[j]) - fmax(z[o], z[j])));
+            const double d = m.distance[i] + m.distance[nf + i], wo = m.distance[nf + i] / d, wj = m.distance[i] / d;
+            const double nx = m.normal[i], ny = m.normal[nf + i], dx = v.xy[j] - v.xy[o], dy = v.xy[n + j] - v.xy[n + o];
+            const double dn = dx * nx + dy * ny;
+            const double tx = dx - dn * nx, ty = dy - dn * ny;
+            const double du = q[n + j] / q[j] - q[n + o] / q[o], dv = q[2 * n + j] / q[j] - q[2 * n + o] / q[o];
+            const double ux = wo * v.grad[o] + wj * v.grad[j], uy = wo * v.grad[n + o] + wj * v.grad[n + j];
+            const double vx = wo * v.grad[2 * n + o] + wj * v.grad[2 * n + j];
+            const double vy = wo * v.grad[3 * n + o] + wj * v.grad[3 * n + j];
+            sx = nu * h * (du - ux * tx - uy * ty) / dn;
+            sy = nu * h * (dv - vx * tx - vy * ty) / dn;
+        }
+        v.face[i] = sx;
+        v.face[nf + i] = sy;
+    }
+}
+
+// The wet-bank viscosity's momentum rate of one cell: sum(s len stress) / area
+// with unit weights (flow2dh_fixed_bed_kernels.h:54-60).
+__device__ __forceinline__ void add_viscosity(const MeshDev &m, const ViscDev &v, int c, double area, double &r1,
+                                              double &r2)
+{
+    const int nf = m.nf;
+    double x = 0., y = 0.;
+    for (int k = m.offset[c]; k < m.offset[c + 1]; ++k) {
+        const int f = m.faces[k];
+        x += m.signs[k] * m.length[f] * v.face[f];
+        y += m.signs[k] * m.length[f] * v.face[nf + f];
+    }
+    r1 += 1. * x / area;
+    r2 += 1. * y / area;
+}
+
 // midpoint_gather + stage combination (+ closing drag on the second stage).
 // With rate_out set, the final rate is stored there and no state is written.
 // Owner computes: each cell forms the donor-limited flux of its faces itself
@@ -2053,6 +2137,7 @@ __global__ void __launch_bounds__(256) k_update(MeshDev m, StateDev s, Ctrl *ctr
         const double r0 = mass;
         double r1 = w.rate[nc + c] + mx, r2 = w.rate[2 * nc + c] + my;
         if (turb && t.hkt[sid]) add_rotor_momentum(m, t, sid, c, area, r1, r2);
+        if (w.visc.nu && w.visc.nu[sid] > 0.) add_viscosity(m, w.visc, c, area, r1, r2);
         if (!isfinite(r0) || !isfinite(r1) || !isfinite(r2)) raise_status(ct, stage, ST_RATE);
         if (rate_out) { rate_out[c] = r0; rate_out[nc + c] = r1; rate_out[2 * nc + c] = r2; continue; }
         const double dt = ct.trial, dry = ct.dry;

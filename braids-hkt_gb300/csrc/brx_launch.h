@@ -81,6 +81,8 @@ enum KernelKind { K_DRAG = 0, K_BOUNDARY = 1, K_CELLS = 2, K_FACES = 3, K_GATHER
 enum MixedAux { K_PRIM = 8, K_BED = 9, K_WATER = 10, K_HKT_GRAD = 12, K_HKT_FACES = 13 };
 // Rotor-array terms of one stage (both forms; FP64 kernels of the FP64 unit).
 enum { K_TURB = 11 };
+// Wet-bank viscosity of one stage (both forms; FP64 kernels of the FP64 unit).
+enum { K_VISC = 14 };
 
 // Mixed form (FP32 sweeps, FP64 stage pair, depth and mass): launch one kernel
 // of the given kind for the given stage; out is the rate buffer of K_UPDATE or

@@ -1017,6 +1017,16 @@ __global__ void __launch_bounds__(256) km_update(MeshDev m, StateDev s, Ctrl *ct
             r1 = f2d(f1);
             r2 = f2d(f2);
         }
+        if (w.visc.nu && w.visc.nu[sid] > 0.) {
+            // the wet-bank viscosity's FP64 face stresses, FP64 signed weights
+            double x = 0., y = 0.;
+            for (int k = m.offset[c]; k < m.offset[c + 1]; ++k) {
+                const int f = m.faces[k];
+                x += g.cw8[k] * w.visc.face[f];
+                y += g.cw8[k] * w.visc.face[m.nf + f];
+            }
+            r1 += x; r2 += y;
+        }
         if (!finite64(mass) || !finite64(r1) || !finite64(r2)) raise_status(ct, stage, ST_RATE);
         if (rate_out) { rate_out[c] = mass; rate_out[nc + c] = r1; rate_out[2 * nc + c] = r2; continue; }
         const double dt = ct.trial, dry = ct.dry;

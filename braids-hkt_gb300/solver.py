@@ -322,6 +322,15 @@ class RiverSolver:
                 _ptr(tp["support_cell"]), _ptr(tp["support_weight"]), _ptr(tp["support_density"]),
                 _ptr(tp["plane_offset"]), _ptr(tp["plane_cell"]), _ptr(tp["plane_delta"]), _ptr(tp["dxdy"]),
                 _ptr(tp["inverse"]), _ptr(tp["xy"]), _ptr(tp["mid_disp"]), _ptr(tp["nu"]), _ptr(tp["hkt"])))
+        if any(c.get("viscosity", 0.0) > 0.0 for c in self.cases):
+            # the wet-bank viscosity (shoreline_viscosity.py:46-72) and its least-squares metric
+            from .turbines import flow_geometry
+            nu = _f64([float(c.get("viscosity", 0.0)) for c in self.cases])
+            geo = [flow_geometry(c["mesh"]) for c in self.cases]
+            dxdy = _f64(np.concatenate([g[0] for g in geo], axis=1))
+            inverse = _f64(np.concatenate([g[1] for g in geo], axis=1))
+            xy = _f64(np.concatenate([c["mesh"].xy for c in self.cases], axis=1))
+            check(self.lib.brx_viscosity_set(self.h, _ptr(nu), _ptr(dxdy), _ptr(inverse), _ptr(xy)))
         self.method = method
         if method not in METHODS:
             raise ValueError(f"unknown hydraulic method {method!r}")

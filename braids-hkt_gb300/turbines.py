@@ -309,7 +309,7 @@ def flow_geometry(mesh):
     has = other >= 0
     delta = np.zeros((2, nadj))
     delta[:, has] = mesh.xy[:, other[has]] - mesh.xy[:, cell[has]]
-    rr = np.sum(delta * delta, axis=0)
+    rr = np.vecdot(delta.T, delta.T)      # d @ d as the reference forms it (numpy's dot, contracted)
     a = np.zeros((nc, 2, 2))
     outer = np.where(has, delta[:, None, :] * delta[None, :, :] / np.where(has, rr, 1.0), 0.0)   # (2, 2, nadj)
     for i in range(2):

@@ -310,6 +310,16 @@ long long brx_solver_bytes(const brx_solver *s);
 int brx_hllc_set(brx_solver *s, const int *entry_face, const int *entry_other, const double *entry_geo,
                  const double *inverse);
 
+/* Conservative wet-bank viscosity of each scenario (replaces the reference's
+ * shoreline_viscosity.install, src/braids_core/sediment/shoreline_viscosity.py:
+ * 46-72, whose add_momentum hook it computes every spatial evaluation after
+ * the rotor terms): nu (nscen) coefficient [m2/s], 0 for none; the flow
+ * engines' least-squares metric of the packed mesh (bend_methods_v1.py:
+ * 100-128): dxdy (2, nadj) centre offsets per CSR entry, inverse (3, nc)
+ * pseudo-inverse (i11, i12, i22), and cell centres xy (2, nc). The f-wave
+ * method only (BRX_ERR_UNSUPPORTED with HLLC). Both arithmetic forms. */
+int brx_viscosity_set(brx_solver *s, const double *nu, const double *dxdy, const double *inverse, const double *xy);
+
 /* Select the hydraulic method advanced by brx_advance / brx_advance_batch /
  * brx_advance_start / brx_substep (replaces the reference's river_hllc.install,
  * src/braids_core/hydraulics/river_hllc.py:95-101). BRX_METHOD_HLLC needs

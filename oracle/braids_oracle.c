@@ -108,6 +108,14 @@ typedef struct {
     const int *inlet_line;                         /* (nb) or NULL */
     const double *inlet_slope;                     /* (nb) */
     const int *line_left, *line_right;             /* (nf) */
+    /* conservative wet-bank viscosity (shoreline_viscosity.py:46-72): its
+     * coefficient [m2/s] (0: not installed), the flow engines' unweighted
+     * least-squares metric (bend_methods_v1.py:100-128: centre offsets per
+     * CSR entry, pseudo-inverse per cell), cell centres, and scratch for the
+     * velocity gradients (4, nc) and face stresses (2, nf) */
+    double visc;
+    const double *vdxdy, *vinv, *xy;
+    double *vgrad, *vface;
 } om_ctx;
 
 /* ------------------------------------------------------------------ */
@@ -2778,6 +2786,68 @@ int om_exner(const om_ctx *m, const om_exner_params *ex, const double *q, const 
 /* One spatial residual (RiverMidpoint.rate + RiverExplicit.rate).
  * q is the stage state, base the interval-start stock. Writes rate (3,nc)
  * and the limited water flux (nf); *freq_out gets the max CFL frequency. */
+/* Conservative wet-bank viscosity of a state (shoreline_viscosity.py:57-72):
+ * the velocity gradients of the safe state (dry columns: depth 0.001001,
+ * no momentum; secondary_vector_ops.py:39-48) by the flow engines' least
+ * squares (bend_methods_v1_kernels.h:23-39, rows u and v), the shared-face
+ * stress of wet columns (shoreline_viscosity.h:14-33), gathered as
+ * sum(s len stress) / area with unit weights (flow2dh_fixed_bed_kernels.h:
+ * 54-60) into the momentum rate. */
+void om_shoreline_viscosity(const om_ctx *m, const double *q, const double *z, double *rate)
+{
+    const int n = m->nc, nf = m->nf, na = m->nadj;
+    const double dry = m->dry, nu = m->visc;
+    double *grad = m->vgrad, *out = m->vface;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; ++i) {
+        const int wi = q[i] > dry;
+        const double hi = wi ? q[i] : .001001;
+        const double x[2] = {(wi ? q[n + i] : 0.) / hi, (wi ? q[2 * n + i] : 0.) / hi};
+        double bx[2] = {0., 0.}, by[2] = {0., 0.};
+        for (int k = m->offset[i]; k < m->offset[i + 1]; ++k) {
+            const int f = m->faces[k], j = m->owner[f] == i ? m->neighbour[f] : m->owner[f];
+            if (j < 0) continue;
+            const double dx = m->vdxdy[k], dy = m->vdxdy[na + k], wt = 1. / (dx * dx + dy * dy);
+            const int wj = q[j] > dry;
+            const double hj = wj ? q[j] : .001001;
+            const double y[2] = {(wj ? q[n + j] : 0.) / hj, (wj ? q[2 * n + j] : 0.) / hj};
+            for (int c = 0; c < 2; ++c) { bx[c] += wt * dx * (y[c] - x[c]); by[c] += wt * dy * (y[c] - x[c]); }
+        }
+        for (int c = 0; c < 2; ++c) {
+            grad[(2 * c) * n + i] = m->vinv[i] * bx[c] + m->vinv[n + i] * by[c];
+            grad[(2 * c + 1) * n + i] = m->vinv[n + i] * bx[c] + m->vinv[2 * n + i] * by[c];
+        }
+    }
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < nf; ++i) {
+        out[i] = 0.; out[nf + i] = 0.;
+        const int o = m->owner[i], j = m->neighbour[i];
+        if (j < 0 || q[o] <= dry || q[j] <= dry) continue;
+        double h = fmin(q[o], q[j]);
+        h = fmin(h, fmax(0., .5 * (q[o] + z[o] + q[j] + z[j]) - fmax(z[o], z[j])));
+        const double d = m->distance[i] + m->distance[nf + i], wo = m->distance[nf + i] / d, wj = m->distance[i] / d;
+        const double nx = m->normal[i], ny = m->normal[nf + i], dx = m->xy[j] - m->xy[o], dy = m->xy[n + j] - m->xy[n + o];
+        const double dn = dx * nx + dy * ny;
+        const double tx = dx - dn * nx, ty = dy - dn * ny;
+        const double du = q[n + j] / q[j] - q[n + o] / q[o], dv = q[2 * n + j] / q[j] - q[2 * n + o] / q[o];
+        const double ux = wo * grad[o] + wj * grad[j], uy = wo * grad[n + o] + wj * grad[n + j];
+        const double vx = wo * grad[2 * n + o] + wj * grad[2 * n + j], vy = wo * grad[3 * n + o] + wj * grad[3 * n + j];
+        out[i] = nu * h * (du - ux * tx - uy * ty) / dn;
+        out[nf + i] = nu * h * (dv - vx * tx - vy * ty) / dn;
+    }
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; ++i) {
+        double x = 0., y = 0.;
+        for (int k = m->offset[i]; k < m->offset[i + 1]; ++k) {
+            const int f = m->faces[k];
+            x += m->signs[k] * m->length[f] * out[f];
+            y += m->signs[k] * m->length[f] * out[nf + f];
+        }
+        rate[n + i] += 1. * x / m->area[i];
+        rate[2 * n + i] += 1. * y / m->area[i];
+    }
+}
+
 int om_rate(om_ctx *m, om_scratch *s, const double *q, const double *z, const double *base,
             double dt, double time, double *rate, double *water, double *freq_out)
 {
@@ -2818,6 +2888,7 @@ int om_rate(om_ctx *m, om_scratch *s, const double *q, const double *z, const do
     om_limit_faces(m, q, s->theta, water, s->correction);
     om_limit_gather(m, water, s->correction, rate);
     if (m->turb && om_turbine_momentum(m, s, q, z, rate)) return OM_FAIL;
+    if (m->visc > 0.) om_shoreline_viscosity(m, q, z, rate);
     for (int i = 0; i < 3 * nc; ++i) if (!isfinite(rate[i])) return OM_REJECT_SPATIAL;
     const double freq = om_frequency(m, q, s->speed, s->ext_trace, s->freq);
     *freq_out = freq;

@@ -63,7 +63,8 @@ class Ctx(C.Structure):
                 ("turb", P), ("rating_offset", P), ("rating_q", P), ("rating_eta", P),
                 ("nchain", I), ("chain_offset", P), ("chain_face", P), ("chain_slope", P), ("weir", P),
                 ("crit_seg_chain", P), ("crit_chain_offset", P), ("crit_chain_face", P),
-                ("inlet_line", P), ("inlet_slope", P), ("line_left", P), ("line_right", P)]
+                ("inlet_line", P), ("inlet_slope", P), ("line_left", P), ("line_right", P),
+                ("visc", D), ("vdxdy", P), ("vinv", P), ("xy", P), ("vgrad", P), ("vface", P)]
 
 
 class Turbines(C.Structure):
@@ -130,6 +131,8 @@ def _setup(L):
     L.om_exner.argtypes = [P, P, P, P, D, P, P]
     L.om_exner.restype = I
     L.om_turbine_diagnose.argtypes = [P, P, P]
+    L.om_shoreline_viscosity.argtypes = [P, P, P, P]
+    L.om_shoreline_viscosity.restype = None
     L.om_turbine_diagnose.restype = I
     L.om_hkt_gradients.argtypes = [P, P, P, P, P]
     L.om_hkt_gradients.restype = None
@@ -248,6 +251,16 @@ class Oracle:
             ctx.rating_offset = k("rating_offset", _i32(off))
             ctx.rating_q = k("rating_q", _f64(rq))
             ctx.rating_eta = k("rating_eta", _f64(re_))
+        if case.get("viscosity", 0.0) > 0.0:
+            # the wet-bank viscosity's least-squares metric (bend_methods_v1.py:100-128)
+            from braids_hkt_gb300.turbines import flow_geometry
+            delta, inverse, _ = flow_geometry(m)
+            ctx.visc = float(case["viscosity"])
+            ctx.vdxdy = k("vdxdy", _f64(delta))
+            ctx.vinv = k("vinv", _f64(inverse))
+            ctx.xy = k("xy", _f64(m.xy))
+            ctx.vgrad = k("vgrad", np.zeros((4, m.nc)))
+            ctx.vface = k("vface", np.zeros((2, m.nf)))
         self.turbines = None
         self.case_exner = case.get("exner")
         if case.get("turbines"):
@@ -366,6 +379,14 @@ class Oracle:
         stats = Stats()
         st = self.L.om_advance(self.cp, _p(q), _p(self.z), dt, time, C.byref(self.hint), _p(water), C.byref(stats))
         return st, water, {f: getattr(stats, f) for f, _ in Stats._fields_}
+
+    def viscosity_rate(self, q):
+        """The wet-bank viscosity's momentum-rate increment (3, nc) of a state alone."""
+        assert self.ctx.visc > 0.0
+        q = _f64(q)
+        rate = np.zeros_like(q)
+        self.L.om_shoreline_viscosity(self.cp, _p(q), _p(self.z), _p(rate))
+        return rate
 
     # --- HLLC / MUSCL-Hancock option ----------------------------------------
     def _hllc(self):

@@ -21,7 +21,8 @@ Dual-compiled OpenMP headers (their ENTRY/LOOP macros select the host form):
   river_midpoint.h, river_explicit.h, river_exterior_bed.h,
   river_hydraulic_drag.source() (src/braids_core/sediment/river_hydraulic_drag.py:11-15),
   river_turbine_flow.h, river_hydrokinetic_stress.h (turbine momentum terms),
-  river_mpm.h, flow2dh_mobile_kernels.h, bend_methods_v1_kernels.h (Exner / MPM),
+  river_mpm.h, flow2dh_mobile_kernels.h, bend_methods_v1_kernels.h (Exner / MPM, and the
+  flow engines' least-squares gradients), shoreline_viscosity.h (wet-bank viscosity),
   hllc.h, hllc_turbines.h (src/braids_core/hydraulics, the HLLC option),
   river_rating_outlet.h, river_normal_outlet.h, river_exterior_outlet.h (rating,
   normal-depth, critical and free-weir outlets), river_exterior_inlet.h
@@ -114,6 +115,8 @@ def generate():
         "ref_mpm": (src / "braids_core/sediment/river_mpm.h").read_text(),
         "ref_mobile": (src / "braids_core/sediment/flow2dh_mobile_kernels.h").read_text(),
         "ref_bend": (src / "braids_core/sediment/bend_methods_v1_kernels.h").read_text(),
+        # conservative wet-bank viscosity (shoreline_viscosity.py)
+        "ref_visc": (src / "braids_core/sediment/shoreline_viscosity.h").read_text(),
         # HLLC / MUSCL-Hancock option and its rotor pressure correction
         "ref_hllc": (src / "braids_core/hydraulics/hllc.h").read_text(),
         "ref_hllc_turbines": (src / "braids_core/hydraulics/hllc_turbines.h").read_text(),

@@ -194,6 +194,41 @@ class Ref:
         fn.restype = None
         fn(*[_arg(a) for a in args])
 
+    # -- conservative wet-bank viscosity, the reference's kernels ---------------
+    def viscosity_momentum(self, q, nu, rate):
+        """The add_momentum increment of the reference's wet-bank viscosity
+        owner (shoreline_viscosity.py:57-72) for a state q: the safe state of
+        secondary_vector_ops.safe, the flow engines' gradients
+        (bend_methods_v1_kernels.h:23-39) on the reference's own prepared
+        geometry (bend_methods_v1.prepared_geometry), shoreline_viscous_faces
+        (shoreline_viscosity.h) and flow_momentum_gather with unit weights;
+        rate[1:] gets the increment."""
+        from braids_core.sediment.bend_methods_v1 import prepared_geometry
+        from braids_core.sediment.secondary_vector_ops import safe as ref_safe
+        m, g = self.m, self.g
+        n, nf = m.nc, m.nf
+        for name, fn in (("bend", "bend_threads"), ("visc", "mobile_threads"), ("flow", "flow_threads")):
+            if name not in self.libs:
+                self.libs[name] = C.CDLL(str(REF / f"libref_{name}.so"))
+            getattr(self.libs[name], fn)(C.c_int(1))
+        if not hasattr(self, "pg"):
+            data = dict(xy=m.xy, area=m.area, owner=m.owner, neighbour=m.neighbour, normal=m.normal,
+                        length=m.length, mid=m.mid, offset=m.offset, faces=m.faces, signs=m.signs,
+                        distance=m.records["distance"], bid=m.bid)
+            self.pg = prepared_geometry(data)
+        pg = self.pg
+        f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+        q = f64(q)
+        safe, _ = ref_safe(np, q, float(self.dry))
+        grad = np.zeros((10, n))
+        self._invoke(self.libs["bend"].gradients, n, f64(safe), self.z, np.zeros(n), np.zeros(n), pg["offset"],
+                     pg["faces"], pg["owner"], pg["neighbour"], f64(pg["dxdy"]), f64(pg["inverse"]), grad)
+        face = np.zeros((2, nf))
+        self._invoke(self.libs["visc"].shoreline_viscous_faces, nf, n, float(nu), float(self.dry), q, self.z, grad,
+                     g["owner"], g["neighbour"], g["normal"], f64(m.records["distance"]), f64(m.xy), face)
+        self._momentum_gather(face, rate)
+        return grad, face
+
     # -- Exner bed update with MPM transport, the reference's kernels -----------
     def exner(self, q, z0, dt):
         """One bed update over dt (ShorelinePhysics.finish with morphology):
