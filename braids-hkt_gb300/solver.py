@@ -772,7 +772,7 @@ def _profile(self, dt, time=0.0, kinds=False):
     """Per-kernel durations (ms) of one trial launched without a graph: [(kernel name, ms), ...]
     (kernel kind ids instead of names with kinds=True)."""
     names = {0: "drag", 1: "boundary", 2: "cells", 3: "faces", 4: "gather", 5: "limit", 6: "update",
-             7: "control", 11: "rotors",
+             7: "control", 11: "rotors", 14: "viscosity",
              20: "hllc_cells", 21: "hllc_predict", 22: "boundary", 23: "hllc_faces", 24: "hllc_budget",
              25: "rotors", 26: "hllc_update", 27: "rotors_start"}
     self.torch.cuda.current_stream().synchronize()
