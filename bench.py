@@ -39,6 +39,13 @@ BYTES_PER_CELL_UPDATE = {"fp64": 680.0, "mixed": 384.0}   # algorithmic bytes, t
 TRAFFIC_BYTES_PER_CELL = {"mixed": {"cells": 244.21, "faces": 213.25, "gather": 145.97, "update": 190.15,
                                     "drag": 63.07}}
 KERNEL_NAMES = ["drag", "boundary", "cells", "faces", "gather", "update", "control"]
+# FP64 flops (2 DFMA + DMUL + DADD thread instructions) per cell (per face for
+# the face sweep) of one launch of each FP64-form sweep, each kernel captured
+# alone on config 1 (ncu, one launch from the initial state), and their sum
+# over one substep per cell-update
+FP64_FLOPS = {"cells": ("cell", 995.0), "faces": ("face", 1190.0), "gather": ("cell", 97.0),
+              "update": ("cell", 89.0), "drag": ("cell", 259.0)}
+FP64_FLOPS_PER_CELL_UPDATE = 6220.0
 
 
 def peaks():
@@ -219,6 +226,28 @@ def outer_step(solver, dt, t, raise_on_failure=False):
     return diags
 
 
+def run_step(solver, dt, t, chain, raise_on_failure=False):
+    """One bench step: `chain` outer intervals of dt, chained on the device
+    when chain > 1 (brx_advance_chain; workloads without a per-interval bed
+    update), else one owner interval. Returns the diagnostics of the step's
+    last interval per scenario, the step's cell-updates, the failed scenarios
+    and the simulated time after the step (advanced interval by interval, as
+    the chain forms its start times)."""
+    cells = np.diff(solver.packed["cell_offset"]).astype(np.int64)
+    if chain > 1:
+        rows = solver.advance_chain(dt, t, chain, raise_on_failure=raise_on_failure)
+        rows = [rows] if solver.single else rows
+        for _ in range(chain):
+            t += dt
+        updates = sum(int(r["hydraulic_substeps"]) * int(cells[i]) for i, rr in enumerate(rows) for r in rr)
+        failed = {i for i, rr in enumerate(rows) if any(r["failed"] for r in rr)}
+        return [rr[-1] for rr in rows], updates, failed, t
+    diags = outer_step(solver, dt, t, raise_on_failure=raise_on_failure)
+    diags = diags if isinstance(diags, list) else [diags]
+    updates = sum(int(d["hydraulic_substeps"]) * int(cells[i]) for i, d in enumerate(diags))
+    return diags, updates, {i for i, d in enumerate(diags) if d["failed"]}, t + dt
+
+
 def fp64_comparison(cases, outer, steps, mixed_state, mixed_z, mixed_rotors, torch):
     """The same single-scenario workload in the FP64 form over the same
     intervals from the same initial state: its throughput and the mixed
@@ -262,6 +291,24 @@ def fp64_comparison(cases, outer, steps, mixed_state, mixed_z, mixed_rotors, tor
         out["rotor_power_max_W"] = float(np.abs(p64).max() * TB.WATER_DENSITY)
     one.close()
     return out
+
+
+def fp64_roofline(per_kind, nc, nf, value, peak_tflops):
+    """Compute roofline of the FP64 form: the FP64 flops of the slower of the
+    two FP64 sweeps over its live duration, and of the whole step at the
+    measured throughput, against the measured FP64 FMA rate."""
+    dom = max(("cells", "faces"), key=lambda k: sum(per_kind.get(k, [0.0])))
+    unit, per = FP64_FLOPS[dom]
+    flops = per * (nf if unit == "face" else nc)
+    ms = float(np.mean(per_kind[dom]))
+    achieved = flops / (ms * 1e-3) / 1e12
+    step = value * FP64_FLOPS_PER_CELL_UPDATE / 1e12
+    return {"bound": "fp64", "kernel": f"k_{dom}", "achieved": achieved, "peak": peak_tflops, "unit": "TFLOP/s",
+            "frac": achieved / peak_tflops, "kernel_ms": ms, "flops_per_launch": flops,
+            "flops_source": f"ncu FP64 thread-instruction counts per {unit} of a config-1 capture, scaled",
+            "peak_source": "brx_fma_rate (measured FP64 FMA rate of this GPU)",
+            "step_flops_per_cell_update": FP64_FLOPS_PER_CELL_UPDATE, "step_achieved_tflops": step,
+            "step_frac": step / peak_tflops}
 
 
 def fma_peaks(lib):
@@ -375,6 +422,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
     ap.add_argument("--workload", default="config4")
     ap.add_argument("--plain", type=int, default=3, help="scenarios re-run one by one in plain FP64")
+    ap.add_argument("--chain", type=int, default=1,
+                    help="outer intervals per bench step, chained on the device (1: one interval per step; "
+                         "the chained form is then timed as a separate leg)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true", help="skip the config-5 serving session")
     ap.add_argument("--serving-rate", type=float, default=20.0, help="Poisson arrivals per second")
@@ -443,7 +493,9 @@ def main():
                           cache=False)
     cfg["autotune"] = {k: tuned[k] for k in ("kernels", "chunk", "chunk_ms", "substep_ms_default",
                                              "substep_ms_tuned", "tuning_s")}
-    # timed region: K outer steps, device time by events on the solver stream
+    # timed region: K steps of `chain` outer intervals each, device time by
+    # events on the solver stream
+    chain = max(1, args.chain) if solver.bed_model is None else 1
     clocks = ClockSampler(local)
     clocks.start()
     launches0 = solver.launches()
@@ -458,16 +510,13 @@ def main():
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        diags = outer_step(solver, outer, sim_time)
+        diags, n_up, f, sim_time = run_step(solver, outer, sim_time, chain)
         e1.record(stream)
         e1.synchronize()
         step_ms.append(e0.elapsed_time(e1))
         device_ms += step_ms[-1]
-        sim_time += outer
-        diags = diags if isinstance(diags, list) else [diags]
-        failed |= {i for i, d in enumerate(diags) if d["failed"]}
-        updates += sum(int(d["hydraulic_substeps"]) * int(solver.packed["cell_offset"][i + 1] - solver.packed["cell_offset"][i])
-                       for i, d in enumerate(diags))
+        failed |= f
+        updates += n_up
     barrier()
     wall = time.perf_counter() - wall0
     gpu_launches = solver.launches() - launches0
@@ -475,8 +524,10 @@ def main():
     # graph substeps as its slowest scenario needs
     subs = np.array([int(d["hydraulic_substeps"]) for d in diags])
     cells = np.diff(solver.packed["cell_offset"]).astype(np.int64)
+    rej = np.array([int(d["hydraulic_rejections"]) for d in diags])
     cfg["substeps_per_interval"] = {"min": int(subs.min()), "median": float(np.median(subs)), "max": int(subs.max()),
-                                    "cell_weighted_mean": float((subs * cells).sum() / cells.sum())}
+                                    "cell_weighted_mean": float((subs * cells).sum() / cells.sum()),
+                                    "rejected_trials_cell_weighted_mean": float((rej * cells).sum() / cells.sum())}
     clock_info = clocks.stop()
     t_max, updates = aggregate(device_ms / 1e3, updates, dist, "cuda")
     value = updates / t_max
@@ -495,15 +546,42 @@ def main():
     t0 = time.perf_counter()
     for _ in range(max(1, args.steps)):
         solver.q.copy_(q_host, non_blocking=True)
-        diags = outer_step(solver, outer, sim_time, raise_on_failure=True)
+        diags, n_up, _, sim_time = run_step(solver, outer, sim_time, chain, raise_on_failure=True)
         out_host.copy_(solver.q, non_blocking=True)
         torch.cuda.synchronize()
-        sim_time += outer
-        diags = diags if isinstance(diags, list) else [diags]
-        e2e_updates += sum(int(d["hydraulic_substeps"]) * int(solver.packed["cell_offset"][i + 1] - solver.packed["cell_offset"][i])
-                           for i, d in enumerate(diags))
+        e2e_updates += n_up
     e2e_s = time.perf_counter() - t0
     h2d = int(q_host.numel() * 8)
+    # the other schedule of the same batch: interval by interval when the
+    # steps were chained (each interval waits for the batch's slowest
+    # scenario), else the steps' intervals chained on the device in one call
+    interval_ms, iv_updates, chained = [], 0, None
+    for _ in range(max(1, args.steps) if chain > 1 else 0):
+        flush_l2(torch, flush)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        diags, n_up, _, sim_time = run_step(solver, outer, sim_time, 1)
+        e1.record(stream)
+        e1.synchronize()
+        interval_ms.append(e0.elapsed_time(e1))
+        iv_updates += n_up
+    if chain == 1 and solver.bed_model is None and len(cases) > 1:
+        k = max(2, args.steps)
+        flush_l2(torch, flush)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        diags, n_up, _, sim_time = run_step(solver, outer, sim_time, k)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        chained = {"value": n_up / (ms / 1e3), "unit": METRIC, "intervals": k, "ms_per_interval": ms / k,
+                   "note": "the same batch over the same number of outer intervals in one brx_advance_chain "
+                           "call: each scenario begins its next interval on the device as soon as it has "
+                           "finished one"}
 
     # live per-kernel timing of one substep for the roofline of the dominant kernel
     prof = solver.profile_substep(0.5 * min(d["hydraulic_next_substep_hint_s"] for d in diags), sim_time)
@@ -546,7 +624,7 @@ def main():
                 rotor_first.setdefault(int(sid), []).append(k)
         batch_state = state_after_timed
         off = solver.packed["cell_offset"]
-        nsteps = args.warmup + args.steps
+        nsteps = args.warmup + args.steps * chain
         h_updates, h_ms, h_failed = 0, 0.0, False
         for i in pick:
             if args.hllc:
@@ -617,7 +695,7 @@ def main():
                                    "rotors_compared": len(perr)}
     if precision == "mixed" and len(cases) == 1:
         # config 3: the FP64 form over the warm-up and timed intervals, from the same initial state
-        cfg["accuracy_vs_fp64"] = fp64_comparison(cases, outer, args.warmup + args.steps, state_after_timed,
+        cfg["accuracy_vs_fp64"] = fp64_comparison(cases, outer, args.warmup + args.steps * chain, state_after_timed,
                                                   bed_after_timed, rotors_after_timed, torch)
         plain = {"value": cfg["accuracy_vs_fp64"]["fp64_value"], "unit": METRIC,
                  "note": "the same scenario in the FP64 form over the same intervals"}
@@ -674,17 +752,39 @@ def main():
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": device_ms / max(args.steps, 1), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if precision == "fp64" else "f32/f64 mixed",
-            "data": "synthetic", "config": dict(cfg, cells=nc, faces=nf, outer_dt_s=outer,
+            "data": "synthetic", "config": dict(cfg, cells=nc, faces=nf, outer_dt_s=outer, intervals_per_step=chain,
+                                                step=(f"{chain} outer intervals per scenario, chained on the device "
+                                                      "(brx_advance_chain)" if chain > 1 else "one outer interval"),
                                                 failed_scenarios=sorted(failed),
                                                 l2="flushed between steps (256 MiB write)",
                                                 wall_s=wall),
             "roofline": roofline, "clocks": clock_info, "gpu_launches": int(gpu_launches),
-            "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99)),
-                           "what": "device time of one outer interval of the whole batch"},
+            "latency_ms": ({"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99)),
+                            "what": "device time of one outer interval of the whole batch"} if chain == 1 else
+                           {"p50": float(np.percentile(interval_ms, 50)), "p99": float(np.percentile(interval_ms, 99)),
+                            "what": "device time of one outer interval of the whole batch, run interval by interval",
+                            "step_p50": float(np.percentile(step_ms, 50))}),
             "e2e": {"value": e2e_updates / e2e_s, "unit": METRIC, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": h2d}}
     line["compute_peaks"] = dict(fma_peaks(solver.lib), source="brx_fma_rate: 8 independent FMA chains per "
                                  "thread at full occupancy, CUDA events, best of 5")
+    fp64_peak = line["compute_peaks"]["fp64_tflops"]
+    if precision == "fp64":
+        line["roofline_fp64"] = fp64_roofline(per_kind, nc, nf, value, fp64_peak)
+    if plain is not None:
+        plain["roofline_fp64"] = {"achieved": plain["value"] * FP64_FLOPS_PER_CELL_UPDATE / 1e12, "peak": fp64_peak,
+                                  "unit": "TFLOP/s",
+                                  "frac": plain["value"] * FP64_FLOPS_PER_CELL_UPDATE / 1e12 / fp64_peak,
+                                  "step_flops_per_cell_update": FP64_FLOPS_PER_CELL_UPDATE,
+                                  "flops_source": "ncu FP64 thread-instruction counts per cell-update of config 1"}
+        line["roofline_fp64"] = dict(plain["roofline_fp64"], leg="plain_fp64")
+    if chained is not None:
+        line["chained"] = chained
+    if interval_ms:
+        line["interval_by_interval"] = {"value": iv_updates / (sum(interval_ms) / 1e3), "unit": METRIC,
+                                        "intervals": len(interval_ms),
+                                        "note": "the same batch advanced one outer interval per call: every "
+                                                "interval waits for the batch's slowest scenario"}
     if plain is not None:
         line["plain_fp64"] = plain
         line["batched_vs_plain_fp64"] = value / plain["value"]

@@ -29,6 +29,7 @@ SIGNATURES = {
     "brx_state_bind": (I, [P, P, P]),
     "brx_advance": (I, [P, D, D, P]),
     "brx_advance_batch": (I, [P, P, P, P]),
+    "brx_advance_chain": (I, [P, P, P, I, P, P, P]),
     "brx_substep": (I, [P, D, D, P, P]),
     "brx_rate": (I, [P, D, D, P, P, P, P]),
     "brx_scenarios_activate": (I, [P, P]),

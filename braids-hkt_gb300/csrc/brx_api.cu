@@ -99,6 +99,9 @@ struct brx_solver {
     int *d_cell_off = nullptr, *d_face_off = nullptr;
     double *d_exdt = nullptr;
     double *d_totals = nullptr;      // (nscen, 2) brx_totals output
+    IvStat *d_hist = nullptr;        // (nscen, hist_cap) interval records of brx_advance_chain
+    IvStat *h_hist = nullptr;        // pinned mirror
+    size_t hist_cap = 0;
     int method = BRX_METHOD_FWAVE;   // hydraulic method of the substep graph
     HllcDev hllc{};                  // HLLC stencil (valid when hllc_ready)
     bool hllc_ready = false;
@@ -439,6 +442,7 @@ extern "C" int brx_solver_destroy(brx_solver *s)
     if (s->graph) cudaGraphExecDestroy(s->graph);
     for (void *p : s->allocations) cudaFree(p);
     if (s->h_ctrl) cudaFreeHost(s->h_ctrl);
+    if (s->h_hist) cudaFreeHost(s->h_hist);
     if (s->fork) cudaEventDestroy(s->fork);
     if (s->polled) cudaEventDestroy(s->polled);
     if (s->join) cudaEventDestroy(s->join);
@@ -1492,6 +1496,8 @@ static void begin_interval_each(brx_solver *s, const double *dt_each, const doub
         c.bgross[0] = c.bgross[1] = c.gross = 0.0;
         c.one_stage = s->method == BRX_METHOD_HLLC;
         c.done = !c.active;
+        c.chain_left = c.chain_pos = 0;
+        c.hist = nullptr;
         host_set_trial(c);
     }
 }
@@ -1641,6 +1647,82 @@ static int advance_impl(brx_solver *s, const double *dt, const double *time, brx
         for (int i = 0; i < s->nscen; ++i) all_done = all_done && s->h_ctrl[i].done;
     }
     return finish_interval(s, stats);
+}
+
+// Consecutive intervals per scenario, chained on the device (the owner's
+// outer loop of steps at a fixed interval, adaptive_river_worker.py:646-667,
+// with no host round trip between the steps): a scenario that completes an
+// interval records it and begins the next at once (chain_next), so the batch
+// stays full until the last interval's tail instead of draining at the end
+// of every interval.
+extern "C" int brx_advance_chain(brx_solver *s, const double *dt, const double *time, int intervals,
+                                 brx_advance_stats *stats, double *ledger, double *gross)
+{
+    TRY(ensure_ready(s));
+    if (!dt || !time) return fail(BRX_ERR_ARGUMENT, "null interval arrays");
+    if (intervals < 1) return fail(BRX_ERR_ARGUMENT, "intervals must be at least 1");
+    if (s->pending) return fail(BRX_ERR_STATE, "an asynchronous interval is already in flight");
+    for (int i = 0; i < s->nscen; ++i)
+        if (!std::isfinite(dt[i]) || !std::isfinite(time[i])) return fail(BRX_ERR_ARGUMENT, "nonfinite interval");
+    const size_t need = (size_t)s->nscen * (size_t)intervals;
+    if (need > s->hist_cap) {
+        const size_t cap = std::max(need, 2 * s->hist_cap);
+        TRY(s->alloc(&s->d_hist, cap));
+        if (s->h_hist) cudaFreeHost(s->h_hist);
+        s->h_hist = nullptr;
+        CK(cudaMallocHost(&s->h_hist, sizeof(IvStat) * cap));
+        s->hist_cap = cap;
+    }
+    if (s->graph_dirty || !s->graph) TRY(build_graph(s));
+    begin_interval_each(s, dt, time, false);
+    for (int i = 0; i < s->nscen; ++i) {
+        Ctrl &c = s->h_ctrl[i];
+        c.chain_left = c.active ? intervals - 1 : 0;
+        c.hist = s->d_hist + (size_t)i * intervals;
+    }
+    refresh_bed(s);
+    upload_ctrl(s);
+    // every interval ends within max_substeps accepted + 101 rejected trials
+    const int max_replays = intervals * ((4096 + 102) / s->graph_chunk + 2);
+    bool all_done = false;
+    for (int r = 0; r < max_replays && !all_done; ++r) {
+        CK(cudaGraphLaunch(s->graph, s->stream));
+        s->launches += (long long)s->launches_per_substep * s->graph_chunk;
+        CK(cudaMemcpyAsync(s->h_ctrl, s->d_ctrl, sizeof(Ctrl) * s->nscen, cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        all_done = true;
+        for (int i = 0; i < s->nscen; ++i) all_done = all_done && s->h_ctrl[i].done;
+    }
+    CK(cudaMemcpyAsync(s->h_hist, s->d_hist, sizeof(IvStat) * need, cudaMemcpyDeviceToHost, s->stream));
+    std::vector<brx_advance_stats> last(s->nscen);
+    const int rc = finish_interval(s, last.data());
+    // the recorded intervals, then the one the chain ended in, then those not run
+    for (int i = 0; i < s->nscen; ++i) {
+        const Ctrl &c = s->h_ctrl[i];
+        for (int k = 0; k < intervals; ++k) {
+            const size_t o = (size_t)i * intervals + k;
+            brx_advance_stats st{};
+            double led = 0., gro = 0.;
+            if (!c.active) {
+                st = last[i];
+            } else if (k < c.chain_pos) {
+                const IvStat &r = s->h_hist[o];
+                st.substeps = r.substeps; st.rejections = r.rejections; st.failed = 0;
+                st.min_dt = r.min_dt; st.max_dt = r.max_dt; st.accepted_cfl_max = r.cfl_max; st.hint = r.hint;
+                led = r.ledger; gro = r.gross;
+            } else if (k == c.chain_pos) {
+                st = last[i];
+                led = c.ledger; gro = c.gross;
+            } else {
+                st.failed = 3;
+            }
+            if (stats) stats[o] = st;
+            if (ledger) ledger[o] = led;
+            if (gross) gross[o] = gro;
+        }
+    }
+    for (int i = 0; i < s->nscen; ++i) s->h_ctrl[i].chain_left = s->h_ctrl[i].chain_pos = 0;
+    return rc;
 }
 
 // Commit every scenario's accepted state into the bound buffer and report.

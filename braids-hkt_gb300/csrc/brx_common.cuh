@@ -48,6 +48,14 @@ enum : unsigned {
     ST_PRE = ST_SPATIAL | ST_BUDGET | ST_RATE | ST_FREQ | ST_TURBINE | ST_FATAL,
 };
 
+// Record of one completed interval of a device-chained run
+// (brx_advance_chain): the leading fields are brx_advance_stats' layout.
+struct IvStat {
+    int substeps, rejections, failed, pad;
+    double min_dt, max_dt, cfl_max, hint;
+    double ledger, gross;              // the interval's net inflow and gross boundary volume
+};
+
 // Per-scenario clock and controls, resident on the device.
 struct Ctrl {
     // controls
@@ -74,6 +82,10 @@ struct Ctrl {
     // FP32 copies for the mixed form's sweeps, refreshed with every trial
     float gravf, dryf, trialf, roughf;
     int cfl1, pad1;                         // stage 1 exceeded the CFL limit (mixed form, set after its gather)
+    // device-chained intervals: how many follow this one, this one's index,
+    // and where a completed interval is recorded (null outside a chain)
+    int chain_left, chain_pos;
+    IvStat *hist;
 };
 
 // Scenarios taking part in the current trial, packed: every sweep visits only

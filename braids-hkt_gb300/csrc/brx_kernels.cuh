@@ -2227,6 +2227,27 @@ __global__ void k_control(Ctrl *ctrl, int nscen, ActiveDev a)
     active_rebuild(ctrl, nscen, a);
 }
 
+// A chained scenario has completed an interval: record it and begin the
+// next one as the host begins an interval (begin_interval_each), with the
+// start time advanced by one interval and the controller's hint carried
+// over, so the chain reproduces consecutive intervals bit for bit. The
+// accepted state stays in the buffer it is in (the kernels read q[cur]).
+__device__ __forceinline__ void chain_next(Ctrl &c)
+{
+    IvStat &r = c.hist[c.chain_pos];
+    r.substeps = c.substeps; r.rejections = c.rejections; r.failed = 0; r.pad = 0;
+    r.min_dt = c.min_dt; r.max_dt = c.max_dt; r.cfl_max = c.cfl_max; r.hint = c.hint;
+    r.ledger = c.ledger; r.gross = c.gross;
+    c.time0 += c.dt_outer;
+    c.elapsed = 0.0;
+    c.substeps = c.rejections = 0;
+    c.min_dt = c.max_dt = c.cfl_max = 0.0;
+    c.bflux[0] = c.bflux[1] = c.ledger = 0.0;
+    c.bgross[0] = c.bgross[1] = c.gross = 0.0;
+    --c.chain_left;
+    ++c.chain_pos;
+}
+
 __device__ void control_one(Ctrl &c)
 {
     if (!c.active || c.done) return;
@@ -2263,7 +2284,10 @@ __device__ void control_one(Ctrl &c)
         const double growth = c.truncated ? c.hint : 2 * c.trial;
         c.hint = peak > 0 ? fmin(growth, .98 * c.cfl / peak) : growth;
         if (c.substeps > c.max_substeps) { c.failed = 2; c.done = 1; return; }
-        if (!(c.elapsed < c.dt_outer - 1e-13 * fmax(1., c.dt_outer))) { c.done = 1; return; }
+        if (!(c.elapsed < c.dt_outer - 1e-13 * fmax(1., c.dt_outer))) {
+            if (c.chain_left <= 0) { c.done = 1; return; }
+            chain_next(c);
+        }
     }
     set_trial(c);
 }

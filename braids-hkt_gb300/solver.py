@@ -551,6 +551,39 @@ class RiverSolver:
                             failed=s.failed))
         return out[0] if self.single else out
 
+    def advance_chain(self, dt, time, intervals, raise_on_failure=True):
+        """`intervals` consecutive intervals of dt per scenario from `time`,
+        chained on the device: a scenario that completes an interval begins
+        the next at once (interval k starts at time + dt + ... + dt, k terms
+        added one by one). Returns per scenario a list of per-interval
+        diagnostics (as advance gives them, plus the interval's boundary
+        ledger and gross boundary volume); each interval is the one that
+        `intervals` consecutive advance calls with those start times give.
+        """
+        self.torch.cuda.current_stream().synchronize()
+        k = int(intervals)
+        d = _f64(np.broadcast_to(dt, (self.nscen,)))
+        t = _f64(np.broadcast_to(self.time if time is None else time, (self.nscen,)))
+        stats = (AdvanceStats * (self.nscen * k))()
+        ledger = np.zeros(self.nscen * k)
+        gross = np.zeros(self.nscen * k)
+        code = self.lib.brx_advance_chain(self.h, _ptr(d), _ptr(t), k, stats, _ptr(ledger), _ptr(gross))
+        if code and (raise_on_failure or code != 4):
+            check(code)
+        out = []
+        for i in range(self.nscen):
+            rows = []
+            for j in range(k):
+                s = stats[i * k + j]
+                rows.append(dict(integrator=METHOD_NAMES[self.method], hydraulic_substeps=s.substeps,
+                                 hydraulic_rejections=s.rejections, hydraulic_minimum_dt=s.min_dt,
+                                 hydraulic_maximum_dt=s.max_dt, accepted_cfl_max=s.accepted_cfl_max,
+                                 hydraulic_next_substep_hint_s=s.hint, failed=s.failed,
+                                 boundary_ledger_m3=float(ledger[i * k + j]),
+                                 gross_boundary_volume_m3=float(gross[i * k + j])))
+            out.append(rows)
+        return out[0] if self.single else out
+
     # --- asynchronous intervals (serving loops) ---------------------------
     def advance_start(self, dt, time):
         """Launch one interval per scenario (arrays; dt <= 0 idles a scenario) and return at once."""

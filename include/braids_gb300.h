@@ -191,6 +191,24 @@ int brx_advance(brx_solver *s, double dt, double time, brx_advance_stats *stats)
  * idle. Scenarios keep independent clocks inside the same launches. */
 int brx_advance_batch(brx_solver *s, const double *dt, const double *time, brx_advance_stats *stats);
 
+/* Several consecutive intervals per scenario in one call: scenario i
+ * advances over [t_k, t_k + dt[i]] for k = 0 .. intervals-1, with t_0 =
+ * time[i] and t_{k+1} = t_k + dt[i] (the owner's outer loop of steps at a
+ * fixed interval, src/braids_core/sediment/adaptive_river_worker.py:646-667,
+ * without the host between the steps). A scenario that completes an
+ * interval begins its next one on the device at once, so the batch does not
+ * drain at every interval end. Each interval's substeps, state, controller
+ * statistics and boundary ledger are those of `intervals` consecutive
+ * brx_advance_batch calls with the same start times. stats (host, nscen x
+ * intervals, scenario-major, may be NULL) as brx_advance; ledger and gross
+ * (host, nscen x intervals, may be NULL) each interval's net inflow volume
+ * and gross boundary volume as brx_ledger_get / brx_ledger_gross_get give
+ * them after one interval (those getters then report the last interval).
+ * An interval after a failed one reports failed = 3 (not run). Returns
+ * BRX_ERR_REJECTED if any scenario failed. */
+int brx_advance_chain(brx_solver *s, const double *dt, const double *time, int intervals,
+                      brx_advance_stats *stats, double *ledger, double *gross);
+
 /* One SSPRK(2,2) trial of exactly dt on every active scenario
  * (RiverExplicit._single, river_explicit.py:94-119). On acceptance the bound
  * state is replaced; status (nscen, host) gets the rejection bits (0 =
