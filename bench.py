@@ -491,8 +491,8 @@ def main():
     from braids_hkt_gb300 import autotune
     tuned = autotune.tune(solver, dt=0.25 * min(d["hydraulic_next_substep_hint_s"] for d in diags), time0=sim_time,
                           cache=False)
-    cfg["autotune"] = {k: tuned[k] for k in ("kernels", "chunk", "chunk_ms", "substep_ms_default",
-                                             "substep_ms_tuned", "tuning_s")}
+    cfg["autotune"] = {k: tuned.get(k) for k in ("kernels", "chunk", "chunk_ms", "tile", "substep_ms_default",
+                                                 "substep_ms_tuned", "tuning_s")}
     # timed region: K steps of `chain` outer intervals each, device time by
     # events on the solver stream
     chain = max(1, args.chain) if solver.bed_model is None else 1

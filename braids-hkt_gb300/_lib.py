@@ -30,6 +30,8 @@ SIGNATURES = {
     "brx_advance": (I, [P, D, D, P]),
     "brx_advance_batch": (I, [P, P, P, P]),
     "brx_advance_chain": (I, [P, P, P, I, P, P, P]),
+    "brx_tile_set": (I, [P, I]),
+    "brx_tile_get": (I, [P, P, P]),
     "brx_substep": (I, [P, D, D, P, P]),
     "brx_rate": (I, [P, D, D, P, P, P, P]),
     "brx_scenarios_activate": (I, [P, P]),

@@ -8,7 +8,10 @@ and hydraulic method):
     kernel's own limit) and the grid cap (resident blocks per SM), through
     brx_launch_shape_set;
   * the CUDA-graph chunk: how many substeps one graph replay carries before
-    the host reads the scenario clocks back (brx_graph_chunk_set).
+    the host reads the scenario clocks back (brx_graph_chunk_set);
+  * mixed f-wave form, cells of at most four faces: the cell tile of the
+    tile sweep (brx_tile_set: cells per tile, 0 for the separate cell, face
+    and gather sweeps) and its grid cap.
 
 How: every candidate shape is applied to all tunable kinds at once and one
 trial substep is timed kernel by kernel with CUDA events
@@ -16,7 +19,9 @@ trial substep is timed kernel by kernel with CUDA events
 minimum over repetitions). Kernels are grid-stride sweeps whose results do
 not depend on the shape, and the state, the step hints and the clock are
 restored after every trial, so tuning changes nothing but speed. The chunk is
-then chosen by timing a short fixed interval per candidate. Choices are cached
+then chosen by timing a short fixed interval per candidate, and so is the
+cell tile (the tile sweep waits for the boundary and rotor kernels that the
+separate cell sweep overlaps, so only whole intervals compare them). Choices are cached
 per (device, form, method, cells, faces, scenarios) in a JSON file beside the
 built library, so a solver of the same shape is tuned once.
 
@@ -45,6 +50,9 @@ ROTOR_MEMBERS = (12, 13)
 BLOCKS = (64, 128, 256, 512)
 PER_SM = (4, 8, 16, 32)
 CHUNKS = (4, 8, 16, 32)
+TILES = (128, 256, 512)            # cells per tile (0, the separate sweeps, is always a candidate)
+TILE_PER_SM = (2, 4)
+K_TILE = 15
 CACHE = BUILD / "autotune.json"
 
 
@@ -94,8 +102,55 @@ def _trial(solver, dt, saved_q, time0):
     return per
 
 
+def _tune_tile(solver, saved_q, saved_hints, dt, time0, interval, tiles):
+    """Cells per tile and grid cap of the tile sweep, or 0 (separate sweeps):
+    the fastest of a short fixed interval, each candidate run twice from the
+    same state (the first run builds its graph). None where the solver has
+    no tile sweep (FP64 form, HLLC, cells of more than four faces)."""
+    import torch
+    if solver.precision != "mixed" or solver.method != "fwave":
+        return None
+    try:
+        solver.set_tile(0)
+    except Exception:
+        return None
+    hints = np.where(np.asarray(saved_hints) > 0, saved_hints, dt)
+    span = interval if interval is not None else 32 * float(np.median(hints))
+
+    def run():
+        solver.q.copy_(saved_q)
+        solver.set_hints(hints)
+        solver.advance(span, time0, raise_on_failure=False)        # builds the graph
+        solver.q.copy_(saved_q)
+        solver.set_hints(hints)
+        torch.cuda.synchronize()
+        w0 = time.perf_counter()
+        solver.advance(span, time0, raise_on_failure=False)
+        torch.cuda.synchronize()
+        return (time.perf_counter() - w0) * 1e3
+
+    table = {"0": run()}
+    best = (table["0"], 0, 0)
+    for cells in tiles:
+        try:
+            solver.set_tile(cells)
+        except Exception:
+            continue
+        for p in TILE_PER_SM:
+            solver.set_launch_shape(K_TILE, 256, p)
+            ms = run()
+            table[f"{cells}x{p}"] = ms
+            if ms < best[0]:
+                best = (ms, cells, p)
+    _, cells, p = best
+    solver.set_tile(cells)
+    if cells:
+        solver.set_launch_shape(K_TILE, 256, p)
+    return {"cells": int(cells), "per_sm": int(p), "interval_ms": {k: round(v, 3) for k, v in table.items()}}
+
+
 def tune(solver, dt=1e-3, time0=0.0, reps=2, blocks=BLOCKS, per_sm=PER_SM, chunks=CHUNKS, interval=None,
-         cache=True, verbose=False):
+         cache=True, verbose=False, tiles=TILES):
     """Tune the solver's launch shapes and graph chunk in place; returns a summary dict."""
     import torch
     key = _key(solver)
@@ -111,6 +166,8 @@ def tune(solver, dt=1e-3, time0=0.0, reps=2, blocks=BLOCKS, per_sm=PER_SM, chunk
         for k, (b, p) in entry["shapes"].items():
             solver.set_launch_shape(int(k), b, p)
         solver.set_graph_chunk(entry["chunk"])
+        if entry.get("tile"):
+            solver.set_tile(entry["tile"]["cells"])
         return dict(entry, cached=True)
     t0 = time.perf_counter()
     torch.cuda.synchronize()
@@ -172,6 +229,8 @@ def tune(solver, dt=1e-3, time0=0.0, reps=2, blocks=BLOCKS, per_sm=PER_SM, chunk
         solver.set_graph_chunk(chunk)
     else:
         chunk = solver.graph_chunk
+    # cell tile of the tile sweep: whole intervals from the same state per candidate
+    tile = _tune_tile(solver, saved_q, saved_hints, dt, time0, interval, tiles) if tiles else None
     solver.q.copy_(saved_q)
     solver.set_hints(saved_hints)
     torch.cuda.synchronize()
@@ -179,7 +238,9 @@ def tune(solver, dt=1e-3, time0=0.0, reps=2, blocks=BLOCKS, per_sm=PER_SM, chunk
     for k, (b, p, ms, base_ms) in picked.items():
         for m in slots[k]:
             shapes[str(m)] = [b, p]
-    entry = dict(shapes=shapes, chunk=int(chunk),
+    if tile is not None and tile["cells"]:
+        shapes[str(K_TILE)] = [256, tile["per_sm"]]
+    entry = dict(shapes=shapes, chunk=int(chunk), tile=tile,
                  kernels={kinds[k]: dict(block=b, per_sm=p, ms=round(ms, 4), default_ms=round(base_ms, 4))
                           for k, (b, p, ms, base_ms) in picked.items()},
                  substep_ms_default=round(sum(v[3] for v in picked.values()), 4),

@@ -17,6 +17,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/braids_gb300.h"
@@ -53,6 +54,7 @@ struct brx_solver {
     int device = 0, sms = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t side = nullptr;       // boundary CTAs run here, concurrent with the cell sweep
+    cudaStream_t side2 = nullptr;      // rotor cell terms run here, concurrent with both
     cudaEvent_t fork = nullptr, join = nullptr, join2 = nullptr;   // side-stream fork / joins of a stage
     std::vector<void *> allocations;
     size_t bytes = 0;                // device bytes held (sum of allocations)
@@ -99,6 +101,12 @@ struct brx_solver {
     int *d_cell_off = nullptr, *d_face_off = nullptr;
     double *d_exdt = nullptr;
     double *d_totals = nullptr;      // (nscen, 2) brx_totals output
+    int tile_cells = 0;              // mixed f-wave: cells per tile of the tile sweep (0: separate sweeps)
+    TileDev tiles{};                 // tile tables (valid when tile_smem > 0)
+    int tile_smem = 0;
+    bool tiles_dirty = false;        // the entry flags changed since the tables were built
+    std::vector<void *> tile_allocs; // the tables' device buffers (replaced on rebuild)
+    size_t tile_bytes = 0;
     IvStat *d_hist = nullptr;        // (nscen, hist_cap) interval records of brx_advance_chain
     IvStat *h_hist = nullptr;        // pinned mirror
     size_t hist_cap = 0;
@@ -226,6 +234,7 @@ extern "C" int brx_solver_create(int nscen, const int *cell_offset, const int *f
         CK(cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, s->device));
         CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
         CK(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
+        CK(cudaStreamCreateWithFlags(&s->side2, cudaStreamNonBlocking));
         CK(cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&s->join, cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&s->join2, cudaEventDisableTiming));
@@ -429,6 +438,7 @@ extern "C" int brx_solver_create(int nscen, const int *cell_offset, const int *f
         for (int k : {(int)K_CELLS, (int)K_FACES, (int)KH_CELLS_SHAPE, (int)KH_FACES_SHAPE, (int)K_HKT_FACES})
             s->shape[k].block = 128;
         if (precision == BRX_MIXED) s->shape[K_HKT_GRAD].block = 128;
+        s->shape[K_TILE] = {TILE_THREADS, 4};
         return BRX_OK;
     }();
     if (rc) { brx_solver_destroy(s); return rc; }
@@ -441,6 +451,7 @@ extern "C" int brx_solver_destroy(brx_solver *s)
     if (!s) return BRX_OK;
     if (s->graph) cudaGraphExecDestroy(s->graph);
     for (void *p : s->allocations) cudaFree(p);
+    for (void *p : s->tile_allocs) cudaFree(p);
     if (s->h_ctrl) cudaFreeHost(s->h_ctrl);
     if (s->h_hist) cudaFreeHost(s->h_hist);
     if (s->fork) cudaEventDestroy(s->fork);
@@ -448,6 +459,7 @@ extern "C" int brx_solver_destroy(brx_solver *s)
     if (s->join) cudaEventDestroy(s->join);
     if (s->join2) cudaEventDestroy(s->join2);
     if (s->side) cudaStreamDestroy(s->side);
+    if (s->side2) cudaStreamDestroy(s->side2);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return BRX_OK;
@@ -536,6 +548,7 @@ extern "C" int brx_boundary_set(brx_solver *s, const int *seg_mode, const int *s
             }
         CK(cudaMemcpy(s->d_cidx, s->h_cidx.data(), sizeof(int2) * s->h_cidx.size(), cudaMemcpyHostToDevice));
         CK(cudaMemcpy(s->d_ccls, s->h_ccls.data(), sizeof(int) * s->nc, cudaMemcpyHostToDevice));
+        s->tiles_dirty = true;
     }
     s->boundary_ready = true;
     return BRX_OK;
@@ -1081,6 +1094,153 @@ extern "C" int brx_launch_shape_get(brx_solver *s, int kind, int *block, int *bl
 }
 
 // ---------------------------------------------------------------------------
+// Cell tiles of the mixed f-wave stage sweep
+// ---------------------------------------------------------------------------
+// Tiles of tile_cells consecutive cells within each scenario; per tile its
+// first ring of neighbours (whose records its edge faces read) and second
+// ring (whose primitives those records read), the local slot of every
+// neighbour an entry names, and the list of its cells' faces.
+static int build_tiles(brx_solver *s)
+{
+    for (void *p : s->tile_allocs) cudaFree(p);
+    s->tile_allocs.clear();
+    s->bytes -= s->tile_bytes;
+    s->tile_bytes = 0;
+    s->tile_smem = 0;
+    s->tiles = TileDev{};
+    const int T = s->tile_cells;
+    if (T <= 0) return BRX_OK;
+    const int nc = s->nc, nf = s->nf, nadj = s->nadj;
+    const std::vector<int> &off = s->h_offset, &fcsr = s->h_faces_csr;
+    std::vector<int4> info, info2, tface;
+    std::vector<int> halo, tfslot(nadj, -1);
+    std::vector<int2> tent(nadj, make_int2(-1, 0)), hent;
+    std::vector<int> loc(nc, -1), fslot(nf, -1), r1, r2;
+    int cap_p = 0, cap_r = 0, cap_f = 0, r1base = 0;
+    for (int sc = 0; sc < s->nscen; ++sc)
+        for (int c0 = s->cell_offset[sc]; c0 < s->cell_offset[sc + 1]; c0 += T) {
+            const int c1 = std::min(c0 + T, s->cell_offset[sc + 1]), nt = c1 - c0;
+            r1.clear(); r2.clear();
+            for (int c = c0; c < c1; ++c) loc[c] = c - c0;
+            for (int c = c0; c < c1; ++c)
+                for (int k = off[c]; k < off[c + 1]; ++k) {
+                    const int o = s->h_cidx[k].x;
+                    if (o >= 0 && loc[o] < 0) { loc[o] = nt + (int)r1.size(); r1.push_back(o); }
+                }
+            const int n1 = (int)r1.size();
+            for (int r : r1)
+                for (int k = off[r]; k < off[r + 1]; ++k) {
+                    const int o = s->h_cidx[k].x;
+                    if (o >= 0 && loc[o] < 0) { loc[o] = nt + n1 + (int)r2.size(); r2.push_back(o); }
+                }
+            const int n2 = (int)r2.size();
+            const int h0 = (int)halo.size(), fa0 = (int)tface.size();
+            halo.insert(halo.end(), r1.begin(), r1.end());
+            halo.insert(halo.end(), r2.begin(), r2.end());
+            for (int c = c0; c < c1; ++c)
+                for (int k = off[c]; k < off[c + 1]; ++k) {
+                    const int2 id = s->h_cidx[k];
+                    tent[k] = make_int2(id.x >= 0 ? loc[id.x] : -1, id.y);
+                    const int f = fcsr[k];
+                    if (fslot[f] < 0) {
+                        fslot[f] = (int)tface.size() - fa0;
+                        const int o = s->h_owner[f], n = s->h_neighbour[f];
+                        tface.push_back(make_int4(f, loc[o], n >= 0 ? loc[n] : -1, 0));
+                    }
+                    tfslot[k] = fslot[f];
+                }
+            for (int r : r1) {
+                const int deg = off[r + 1] - off[r];
+                if (deg > 4) return fail(BRX_ERR_UNSUPPORTED, "tile sweep: a cell has more than four faces");
+                for (int j = 0; j < 4; ++j) {
+                    if (j < deg) {
+                        const int2 id = s->h_cidx[off[r] + j];
+                        hent.push_back(make_int2(id.x >= 0 ? loc[id.x] : -1, id.y));
+                    } else {
+                        hent.push_back(make_int2(-1, 0));
+                    }
+                }
+            }
+            const int nface = (int)tface.size() - fa0;
+            info.push_back(make_int4(c0, c1, h0, fa0));
+            info2.push_back(make_int4(n1, n2, nface, r1base));
+            r1base += n1;
+            cap_p = std::max(cap_p, nt + n1 + n2);
+            cap_r = std::max(cap_r, nt + n1);
+            cap_f = std::max(cap_f, nface);
+            for (int c = c0; c < c1; ++c) loc[c] = -1;
+            for (int r : r1) loc[r] = -1;
+            for (int r : r2) loc[r] = -1;
+            for (int j = fa0; j < (int)tface.size(); ++j) fslot[tface[j].x] = -1;
+        }
+    cap_f += cap_f & 1;                // the face buffers' second half starts 16-byte aligned
+    const int smem = mixed_tile_smem(cap_p, cap_r, cap_f);
+    int limit = 0;
+    CK(cudaDeviceGetAttribute(&limit, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device));
+    if (smem > limit) return fail(BRX_ERR_ARGUMENT, "tile sweep: the tiles need more shared memory than a block has");
+    auto put = [&](auto **dst, const auto &v) -> int {
+        using T_ = typename std::remove_pointer<typename std::remove_reference<decltype(*dst)>::type>::type;
+        void *p = nullptr;
+        const size_t n = std::max<size_t>(1, v.size());
+        if (cudaMalloc(&p, sizeof(T_) * n) != cudaSuccess) return fail(BRX_ERR_CUDA, "cudaMalloc of the tile tables");
+        s->tile_allocs.push_back(p);
+        s->tile_bytes += sizeof(T_) * n;
+        if (!v.empty() && cudaMemcpy(p, v.data(), sizeof(T_) * v.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+            return fail(BRX_ERR_CUDA, "upload of the tile tables");
+        *dst = reinterpret_cast<T_ *>(p);
+        return BRX_OK;
+    };
+    const int4 *d_info, *d_info2, *d_tface;
+    const int *d_halo, *d_tfslot;
+    const int2 *d_tent, *d_hent;
+    TRY(put(&d_info, info)); TRY(put(&d_info2, info2)); TRY(put(&d_tface, tface));
+    TRY(put(&d_halo, halo)); TRY(put(&d_tfslot, tfslot)); TRY(put(&d_tent, tent)); TRY(put(&d_hent, hent));
+    s->bytes += s->tile_bytes;
+    CK((cudaError_t)mixed_tile_prepare(smem));
+    TileDev &t = s->tiles;
+    t.ntiles = (int)info.size(); t.cells = T;
+    t.cap_prims = cap_p; t.cap_recs = cap_r; t.cap_faces = cap_f;
+    t.info = d_info; t.info2 = d_info2; t.halo = d_halo; t.tent = d_tent; t.hent = d_hent;
+    t.tfslot = d_tfslot; t.tface = d_tface;
+    s->tile_smem = smem;
+    s->tiles_dirty = false;
+    return BRX_OK;
+}
+
+// Rebuild the tile tables when the entry flags changed since they were made.
+static int ensure_tiles(brx_solver *s)
+{
+    if (s->tile_cells > 0 && s->tiles_dirty) {
+        TRY(build_tiles(s));
+        s->graph_dirty = true;
+    }
+    return BRX_OK;
+}
+
+extern "C" int brx_tile_set(brx_solver *s, int cells)
+{
+    if (!s) return fail(BRX_ERR_ARGUMENT, "null solver");
+    if (s->pending) return fail(BRX_ERR_STATE, "an asynchronous interval is in flight");
+    if (cells != 0 && (cells < 32 || cells > 4096)) return fail(BRX_ERR_ARGUMENT, "cells per tile must be 0 or 32..4096");
+    if (cells != 0 && s->precision != BRX_MIXED) return fail(BRX_ERR_UNSUPPORTED, "the tile sweep is the mixed form's");
+    if (cells != 0 && s->maxdeg > 4) return fail(BRX_ERR_UNSUPPORTED, "the tile sweep needs cells of at most four faces");
+    if (cells == s->tile_cells && !s->tiles_dirty) return BRX_OK;
+    s->tile_cells = cells;
+    s->graph_dirty = true;
+    const int rc = build_tiles(s);
+    if (rc) { s->tile_cells = 0; build_tiles(s); }
+    return rc;
+}
+
+extern "C" int brx_tile_get(const brx_solver *s, int *cells, int *smem_bytes)
+{
+    if (!s || !cells) return fail(BRX_ERR_ARGUMENT, "null argument");
+    *cells = s->tile_cells;
+    if (smem_bytes) *smem_bytes = s->tile_cells > 0 ? s->tile_smem : 0;
+    return BRX_OK;
+}
+
+// ---------------------------------------------------------------------------
 // Exner bed update
 // ---------------------------------------------------------------------------
 extern "C" int brx_exner_set(brx_solver *s, const int *enabled, const double *param, const int *bedbc,
@@ -1268,6 +1428,8 @@ static Launch make_launch(brx_solver *s, cudaStream_t st)
     L.mx = s->mx;
     L.turb = s->turb;
     L.has_turb = s->has_turb;
+    L.tiles = s->tiles;
+    L.tile_smem = s->tile_cells > 0 ? s->tile_smem : 0;
     return L;
 }
 
@@ -1371,23 +1533,38 @@ static void enqueue_stage(brx_solver *s, int stage, double *rate_out)
 {
     const bool fork = s->nslot > 0 || s->has_turb;
     if (fork) {
+        // the boundary owners and the rotor cell terms read only the stage
+        // input: each on its own side stream, so neither waits for the other
+        // (one scenario's boundary CTA and its rotors' CTAs are the critical
+        // path of a substep once few scenarios remain in the interval)
         cudaEventRecord(s->fork, s->stream);
         cudaStreamWaitEvent(s->side, s->fork, 0);
         s->launches += launch_kernel(s, K_BOUNDARY, stage, nullptr, s->side);
         cudaEventRecord(s->join, s->side);
-        s->launches += launch_turbines(s, stage, s->side, TURB_CELLS);
-        cudaEventRecord(s->join2, s->side);
+        cudaStreamWaitEvent(s->side2, s->fork, 0);
+        s->launches += launch_turbines(s, stage, s->side2, TURB_CELLS);
+        cudaEventRecord(s->join2, s->side2);
     }
-    s->launches += launch_kernel(s, K_CELLS, stage, nullptr);
-    if (fork) cudaStreamWaitEvent(s->stream, s->join, 0);
-    // the mixed face sweep computes the rotor face terms in its tail: it
-    // needs the rotor cell terms (wet gradients, actuator sink) first
     const bool mixed = s->precision == BRX_MIXED;
-    if (fork && mixed) cudaStreamWaitEvent(s->stream, s->join2, 0);
-    // the donor limiter runs inside the update (owner computes): no limit pass
-    for (int kind : {(int)K_FACES, (int)K_GATHER})
-        s->launches += launch_kernel(s, kind, stage, nullptr);
-    if (fork && !mixed) cudaStreamWaitEvent(s->stream, s->join2, 0);
+    if (mixed && s->tile_cells > 0) {
+        // one pass over cell tiles: its face phase reads the exterior owner's
+        // fluxes and the rotor cell terms
+        if (fork) {
+            cudaStreamWaitEvent(s->stream, s->join, 0);
+            cudaStreamWaitEvent(s->stream, s->join2, 0);
+        }
+        s->launches += launch_kernel(s, K_TILE, stage, nullptr);
+    } else {
+        s->launches += launch_kernel(s, K_CELLS, stage, nullptr);
+        if (fork) cudaStreamWaitEvent(s->stream, s->join, 0);
+        // the mixed face sweep computes the rotor face terms in its tail: it
+        // needs the rotor cell terms (wet gradients, actuator sink) first
+        if (fork && mixed) cudaStreamWaitEvent(s->stream, s->join2, 0);
+        // the donor limiter runs inside the update (owner computes): no limit pass
+        for (int kind : {(int)K_FACES, (int)K_GATHER})
+            s->launches += launch_kernel(s, kind, stage, nullptr);
+        if (fork && !mixed) cudaStreamWaitEvent(s->stream, s->join2, 0);
+    }
     s->launches += launch_turbines(s, stage, s->stream, TURB_FACES);
     s->launches += launch_kernel(s, K_VISC, stage, nullptr);
     s->launches += launch_kernel(s, K_UPDATE, stage, rate_out);
@@ -1525,6 +1702,7 @@ static int ensure_ready(brx_solver *s)
 
 static int build_graph(brx_solver *s)
 {
+    TRY(ensure_tiles(s));
     if (s->graph) { cudaGraphExecDestroy(s->graph); s->graph = nullptr; }
     const long long before = s->launches;
     cudaGraph_t g;
@@ -1754,6 +1932,7 @@ extern "C" int brx_substep(brx_solver *s, double dt, double time, unsigned *stat
 {
     TRY(ensure_ready(s));
     if (!(dt > 0) || !std::isfinite(dt)) return fail(BRX_ERR_ARGUMENT, "dt must be finite and positive");
+    TRY(ensure_tiles(s));
     begin_interval(s, dt, time, true);
     refresh_bed(s);
     for (int i = 0; i < s->nscen; ++i) s->h_ctrl[i].max_substeps = 4096;
@@ -1788,6 +1967,7 @@ extern "C" int brx_rate(brx_solver *s, double dt, double time, double *rate_devi
     TRY(ensure_ready(s));
     if (!rate_device || !water_device) return fail(BRX_ERR_ARGUMENT, "null output buffer");
     if (s->method != BRX_METHOD_FWAVE) return fail(BRX_ERR_UNSUPPORTED, "brx_rate is the f-wave spatial residual");
+    TRY(ensure_tiles(s));
     begin_interval(s, dt, time, true);
     upload_ctrl(s);
     CK(cudaMemcpyAsync(s->state.work, s->state.q[0], sizeof(double) * 3 * s->nc, cudaMemcpyDeviceToDevice, s->stream));
@@ -1821,6 +2001,7 @@ extern "C" int brx_profile_substep(brx_solver *s, double dt, double time, int ca
     TRY(ensure_ready(s));
     if (!ms || !kind || !count || cap < 1) return fail(BRX_ERR_ARGUMENT, "null or empty profile buffers");
     if (!(dt > 0) || !std::isfinite(dt)) return fail(BRX_ERR_ARGUMENT, "dt must be finite and positive");
+    TRY(ensure_tiles(s));
     begin_interval(s, dt, time, true);
     refresh_bed(s);
     upload_ctrl(s);
@@ -1842,9 +2023,10 @@ extern "C" int brx_profile_substep(brx_solver *s, double dt, double time, int ca
             if (const int nl = launch_hllc(s, kind)) { mark(kind); extra += nl - 1; }
     } else {
         // the mixed face sweep reads the rotor cell terms: they come first there
-        const bool mixed = s->precision == BRX_MIXED;
+        const bool mixed = s->precision == BRX_MIXED, tiled = mixed && s->tile_cells > 0;
         for (int stage = 1; stage <= 2; ++stage)
-            for (int kind : {(int)K_BOUNDARY, mixed ? (int)K_TURB : -1, (int)K_CELLS, (int)K_FACES, (int)K_GATHER,
+            for (int kind : {(int)K_BOUNDARY, mixed ? (int)K_TURB : -1, tiled ? (int)K_TILE : (int)K_CELLS,
+                             tiled ? -1 : (int)K_FACES, tiled ? -1 : (int)K_GATHER,
                              mixed ? -1 : (int)K_TURB, (int)K_VISC, (int)K_UPDATE})
                 if (kind >= 0)
                     if (const int nl = launch_kernel(s, kind, stage, nullptr)) { mark(kind); extra += nl - 1; }

@@ -39,6 +39,21 @@ struct MixedGeo {
     float *hcdb;             // (nadj) bed of the other cell - own bed (0 for walls and open faces)
 };
 
+// Cell tiles of the mixed f-wave stage sweep (km_tile): consecutive cells of
+// one scenario, with the ring of neighbours whose records the tile's faces
+// need (ring 1) and the ring their records read (ring 2). A tile's local
+// slots: [0, T) its cells, then ring 1, then ring 2.
+struct TileDev {
+    int ntiles, cells;       // tiles, cells per tile (the last tile of a scenario may be shorter)
+    int cap_prims, cap_recs, cap_faces;   // shared-memory slots: max over tiles
+    const int4 *info;        // (ntiles) first cell, end cell, start in halo, start in face list
+    const int4 *info2;       // (ntiles) ring-1 cells, ring-2 cells, faces, start of the ring-1 entries (x4)
+    const int *halo;         // ring-1 then ring-2 cell ids of each tile
+    const int2 *tent;        // (nadj) entries of each cell in its own tile: neighbour's local slot (-1 none), flags
+    const int2 *hent;        // (4 per ring-1 cell) the same for the ring-1 cells of each tile
+    const int *tfslot;       // (nadj) the face-list slot of each entry in its cell's tile
+    const int4 *tface;       // face lists: face, owner's local slot, neighbour's local slot (-1 none), 0
+};
 // HLLC kinds of one substep (their launch-shape slots), shared by both forms.
 enum HllcKind { KH_CELLS = 20, KH_PREDICT = 21, KH_BOUNDARY = 22, KH_FACES = 23, KH_BUDGET = 24, KH_TURB = 25,
                 KH_UPDATE = 26, KH_TURB0 = 27 };
@@ -65,6 +80,8 @@ struct Launch {
     int has_turb;
     int sms;
     LaunchShape shape[NSHAPE];
+    TileDev tiles;           // valid when tile_smem > 0
+    int tile_smem;           // dynamic shared memory of the tile sweep (0: the separate sweeps)
 };
 
 inline int shape_grid(const Launch &L, int kind, int n)
@@ -83,6 +100,14 @@ enum MixedAux { K_PRIM = 8, K_BED = 9, K_WATER = 10, K_HKT_GRAD = 12, K_HKT_FACE
 enum { K_TURB = 11 };
 // Wet-bank viscosity of one stage (both forms; FP64 kernels of the FP64 unit).
 enum { K_VISC = 14 };
+// Mixed form: cells, faces and gather of one stage in one pass over cell
+// tiles staged in shared memory (meshes of at most four faces per cell).
+enum { K_TILE = 15 };
+constexpr int TILE_THREADS = 256;
+// Shared memory of the tile sweep for the given slot capacities, and its
+// one-time attribute set-up (outside stream capture). Returns a CUDA error code.
+int mixed_tile_smem(int cap_prims, int cap_recs, int cap_faces);
+int mixed_tile_prepare(int smem_bytes);
 
 // Mixed form (FP32 sweeps, FP64 stage pair, depth and mass): launch one kernel
 // of the given kind for the given stage; out is the rate buffer of K_UPDATE or

@@ -29,6 +29,7 @@
 //     signed weights s*len/area, so mass telescopes exactly.
 //
 // This unit is compiled with FMA contraction and fast FP32 division / sqrt.
+#include <algorithm>
 #include "brx_launch.h"
 #include "brx_fwave.cuh"
 
@@ -322,15 +323,16 @@ __global__ void __launch_bounds__(128) km_bed(MeshDev m, StateDev s, MixedGeo g)
 // the flow metric's centre offsets. Called in the cell sweep's tail, after
 // the cell record is written, so its sums are not live in the limiter; the
 // neighbour primitives were just read and come from L1.
-__device__ __forceinline__ void hkt_cell_gradients(const MeshDev &m, const MixedGeo &g, const MxPrim *P,
+template <class Nbr>
+__device__ __forceinline__ void hkt_cell_gradients(const MeshDev &m, const MixedGeo &g, const Nbr &nb,
                                                    const MxPrim &pc, int c, int nc)
 {
     float xx = 0.f, xy = 0.f, yy = 0.f, bx[3] = {0.f, 0.f, 0.f}, by[3] = {0.f, 0.f, 0.f};
     if (pc.wet)
-        for (int k = m.offset[c]; k < m.offset[c + 1]; ++k) {
-            const int n = g.cidx[k].x;
+        for (int k0 = m.offset[c], k = k0; k < m.offset[c + 1]; ++k) {
+            const int n = nb.id(k, k - k0).x;
             if (n < 0) continue;
-            const MxPrim pn = P[n];
+            const MxPrim pn = nb.prim(n);
             if (!pn.wet) continue;
             const float2 d = g.hdxy[k];
             const float w = 1.f / (d.x * d.x + d.y * d.y);
@@ -348,28 +350,33 @@ __device__ __forceinline__ void hkt_cell_gradients(const MeshDev &m, const Mixed
     }
 }
 
-template <int MAXF>
-__global__ void __launch_bounds__(128, BRX_CELLS_MIN_BLOCKS) km_cells(MeshDev m, StateDev s, Ctrl *ctrl, Work w,
-                                                                      MixedGeo g, int stage, TurbDev t, int turb)
+// Neighbour access of the cell record: entry j (global entry k) of the cell
+// and the primitive record of the neighbour it names. The grid sweep reads
+// the mesh's entries and the stage primitives in global memory.
+struct GlobalNbr {
+    const int2 *cidx;
+    const MxPrim *P;
+    __device__ __forceinline__ int2 id(int k, int) const { return cidx[k]; }
+    __device__ __forceinline__ MxPrim prim(int n) const { return P[n]; }
+};
+
+// Cell record of one cell (limited gradients and flags) from its primitives
+// pc and its neighbours' through nb: the body of the cell sweep.
+template <int MAXF, class Nbr>
+__device__ __forceinline__ MxRec mx_record(const MeshDev &m, const StateDev &s, const Ctrl &ct, const MixedGeo &g,
+                                           const MxPrim &pc, int c, int k0, int deg, const Nbr &nb)
 {
-    const int nc = m.nc;
-    MxRec *rec = reinterpret_cast<MxRec *>(w.rec);
-    const MxPrim *P = reinterpret_cast<const MxPrim *>((stage == 1 ? g.prim[0] : g.prim[1]));
-    FOR_ACTIVE_CELLS(m.act, c) {
-        const Ctrl &ct = ctrl[m.cell_sid[c]];
-        if (mx_skip(ct, stage)) continue;
+    {
         const float dry = ct.dryf;
-        const MxPrim pc = P[c];
         const bool wet = pc.wet != 0;
         const float hf = pc.h, u = pc.u, v = pc.v;
         const bool outlet = g.ccls[c] & 1;   // a stage outlet face: the bed gradient is formed here
         // bounds of eta and b relative to the cell (centre = 0), of u and v absolute
         float lo[4] = {0.f, u, v, 0.f}, hi[4] = {0.f, u, v, 0.f};
         float bx[4] = {0.f, 0.f, 0.f, 0.f}, by[4] = {0.f, 0.f, 0.f, 0.f};
-        const int k0 = m.offset[c], deg = m.offset[c + 1] - k0;
         bool active = wet;
         for (int k = k0; k < k0 + deg; ++k) {
-            const int2 id = g.cidx[k];
+            const int2 id = nb.id(k, k - k0);
             const int n = id.x;
             if (n < 0) {
                 if (id.y & 1) active = true;
@@ -383,7 +390,7 @@ __global__ void __launch_bounds__(128, BRX_CELLS_MIN_BLOCKS) km_cells(MeshDev m,
                 }
                 continue;
             }
-            const MxPrim pn = P[n];
+            const MxPrim pn = nb.prim(n);
             const bool wetn = pn.wet != 0;
             if (wetn) active = true;
             const float ddb = g.cdb[k];
@@ -436,7 +443,7 @@ __global__ void __launch_bounds__(128, BRX_CELLS_MIN_BLOCKS) km_cells(MeshDev m,
                 const int k = k0 + j;
                 const float4 ge = g.cent[k];
                 const float rx = ge.z, ry = ge.w;
-                if (outlet && (g.cidx[k].y & 2) && wet) {
+                if (outlet && (nb.id(k, j).y & 2) && wet) {
                     // an open stage outlet with a subcritical wet owner keeps its bed slope
                     const float2 nn = g.fnorm[m.faces[k]];
                     if (fabsf(u * nn.x + v * nn.y) < sq && fabsf(gx[3] * rx + gy[3] * ry) > bedtol) continue;
@@ -465,7 +472,7 @@ __global__ void __launch_bounds__(128, BRX_CELLS_MIN_BLOCKS) km_cells(MeshDev m,
                 for (int j = 0; j < MAXF; ++j) {
                     if (j >= deg) continue;
                     const int k = k0 + j;
-                    const int fl = g.cidx[k].y;
+                    const int fl = nb.id(k, j).y;
                     const float4 ge = g.cent[k];
                     const float rx = ge.z, ry = ge.w;
                     if ((fl & 2) && wet) {
@@ -498,8 +505,25 @@ __global__ void __launch_bounds__(128, BRX_CELLS_MIN_BLOCKS) km_cells(MeshDev m,
 #pragma unroll
         for (int p = 0; p < 4; ++p) { r.gx[p] = gx[p]; r.gy[p] = gy[p]; }
         r.pad0 = 0.f; r.pad1 = 0.f;
-        rec[c] = r;
-        if (turb && t.hkt[m.cell_sid[c]]) hkt_cell_gradients(m, g, P, pc, c, nc);
+        return r;
+    }
+}
+
+template <int MAXF>
+__global__ void __launch_bounds__(128, BRX_CELLS_MIN_BLOCKS) km_cells(MeshDev m, StateDev s, Ctrl *ctrl, Work w,
+                                                                      MixedGeo g, int stage, TurbDev t, int turb)
+{
+    const int nc = m.nc;
+    MxRec *rec = reinterpret_cast<MxRec *>(w.rec);
+    const MxPrim *P = reinterpret_cast<const MxPrim *>((stage == 1 ? g.prim[0] : g.prim[1]));
+    const GlobalNbr nb{g.cidx, P};
+    FOR_ACTIVE_CELLS(m.act, c) {
+        const Ctrl &ct = ctrl[m.cell_sid[c]];
+        if (mx_skip(ct, stage)) continue;
+        const MxPrim pc = P[c];
+        const int k0 = m.offset[c], deg = m.offset[c + 1] - k0;
+        rec[c] = mx_record<MAXF>(m, s, ct, g, pc, c, k0, deg, nb);
+        if (turb && t.hkt[m.cell_sid[c]]) hkt_cell_gradients(m, g, nb, pc, c, nc);
     }
 }
 
@@ -610,51 +634,24 @@ __device__ __forceinline__ void hkt_face_terms(const MxRec &pa, const MxRec &pb,
     }
 }
 
-// resident blocks per SM the register allocation of the face sweep is fitted to
-#ifndef BRX_FACES_MIN_BLOCKS
-#define BRX_FACES_MIN_BLOCKS 8
-#endif
+// Fluxes of one interior or wall face from its cells' records (the body of
+// the face sweep): the FP32 water flux and CFL speed, both sides' momentum
+// fluxes; the rotor face terms go to g.hp / g.hs. n < 0: a wall (rn unused).
+struct MxFaceOut {
+    float water, speed, gl1, gl2, gr1, gr2;
+};
 
-__global__ void __launch_bounds__(128, BRX_FACES_MIN_BLOCKS) km_faces(MeshDev m, StateDev s, BoundaryDev b, Ctrl *ctrl, Work w,
-                                                MixedGeo g, int stage, TurbDev t, int turb)
+__device__ __forceinline__ MxFaceOut mx_face(const MeshDev &m, const StateDev &s, Ctrl &ct, const MixedGeo &g,
+                                             int stage, const TurbDev &t, bool rotors, int sid, int f, int c, int n,
+                                             const MxRec &rc, const MxRec &rn)
 {
-    const int nf = m.nf, nc = m.nc;
-    const MxRec *rec = reinterpret_cast<const MxRec *>(w.rec);
-    float2 *ws = reinterpret_cast<float2 *>(w.ws);
-    float4 *gf = reinterpret_cast<float4 *>(w.gf);
-    FOR_ACTIVE_FACES(m.act, f) {
-        const int sid = m.face_sid[f];
-        Ctrl &ct = ctrl[sid];
-        if (mx_skip(ct, stage)) continue;
-        const float dry = ct.dryf, grav = ct.gravf;
-        const float half_g = 0.5f * grav;
-        const bool rotors = turb && t.hkt[sid];
-        const int c = m.owner[f], n = m.neighbour[f];
-        const float2 nn = g.fnorm[f];
-        const float nx = nn.x, ny = nn.y;
-        const MxRec rc = rec[c];
-        const float hc = rc.h;
-        const int slot = m.bslot[f];
-        if (slot >= 0) {
-            // open face: the exterior owner's flux and the owner/exterior CFL speed (FP64, few faces)
-            const double *q = stage == 1 ? s.work : s.q1;
-            const double dn = m.normal[f], dm = m.normal[nf + f], gd = ct.grav, dd = ct.dry;
-            const double fl0 = b.flux[slot], fl1 = b.flux[(size_t)b.nslot + slot], fl2 = b.flux[2 * (size_t)b.nslot + slot];
-            const double hb = b.trace[slot], hq = q[c];
-            const double pc = .5 * gd * hq * hq;
-            const double a = hq > dd ? fabs((q[nc + c] * dn + q[2 * nc + c] * dm) / hq) + sqrt(gd * hq) : 0.;
-            const double bb = hb > dd ? fabs((b.trace[(size_t)b.nslot + slot] * dn + b.trace[2 * (size_t)b.nslot + slot] * dm) / hb) +
-                                            sqrt(gd * hb) : 0.;
-            ws[f] = make_float2(float(fl0), float(fmax(a, bb)));
-            gf[f] = make_float4(float(fl1 - pc * dn), float(fl2 - pc * dm), 0.f, 0.f);
-            if (rotors) {
-                g.hp[f] = make_float2(0.f, 0.f);
-                if (t.stress[sid]) g.hs[f] = make_float2(0.f, 0.f);
-            }
-            continue;
-        }
-        MxRec rn;
-        if (n >= 0) rn = rec[n];
+    const int nc = m.nc;
+    const float dry = ct.dryf, grav = ct.gravf;
+    const float half_g = 0.5f * grav;
+    const float2 nn = g.fnorm[f];
+    const float nx = nn.x, ny = nn.y;
+    const float hc = rc.h;
+    {
         const bool wc = rc.flags & 4, wn = n >= 0 && (rn.flags & 4);
         int kind = n >= 0 ? 1 : 2;
         if (!wc && !wn) kind = 0;
@@ -802,7 +799,7 @@ __global__ void __launch_bounds__(128, BRX_FACES_MIN_BLOCKS) km_faces(MeshDev m,
                                               hl > 0.f ? hypotf(loc[1], loc[2]) / hl : 0.f,
                                               hr > 0.f ? hypotf(loc[5], loc[6]) / hr : 0.f);
                 float2 pr = make_float2(0.f, 0.f), st = make_float2(0.f, 0.f);
-                hkt_face_terms(rec[c], rec[n], t0, t1, f, c, n, sid, grav, dry, g, t, nc, pr, st);
+                hkt_face_terms(rc, rn, t0, t1, f, c, n, sid, grav, dry, g, t, nc, pr, st);
                 g.hp[f] = pr;
                 if (t.stress[sid]) g.hs[f] = st;
                 rotor_face = true;
@@ -813,12 +810,67 @@ __global__ void __launch_bounds__(128, BRX_FACES_MIN_BLOCKS) km_faces(MeshDev m,
             gr1 = -half_g * hn * hn * nx; gr2 = -half_g * hn * hn * ny;
         }
         if (bad) raise_status(ct, stage, ST_SPATIAL);
-        ws[f] = make_float2(water, speed);
-        gf[f] = make_float4(gl1, gl2, gr1, gr2);
         if (rotors && !rotor_face) {
             g.hp[f] = make_float2(0.f, 0.f);
             if (t.stress[sid]) g.hs[f] = make_float2(0.f, 0.f);
         }
+        return MxFaceOut{water, speed, gl1, gl2, gr1, gr2};
+    }
+}
+
+// Open face: the exterior owner's flux and the owner/exterior CFL speed (FP64, few faces).
+__device__ __forceinline__ void mx_open_face(const MeshDev &m, const StateDev &s, const BoundaryDev &b, const Ctrl &ct,
+                                             int stage, int f, int c, int slot, float2 &wsf, float4 &gff)
+{
+    const int nf = m.nf, nc = m.nc;
+    const double *q = stage == 1 ? s.work : s.q1;
+    const double dn = m.normal[f], dm = m.normal[nf + f], gd = ct.grav, dd = ct.dry;
+    const double fl0 = b.flux[slot], fl1 = b.flux[(size_t)b.nslot + slot], fl2 = b.flux[2 * (size_t)b.nslot + slot];
+    const double hb = b.trace[slot], hq = q[c];
+    const double pc = .5 * gd * hq * hq;
+    const double a = hq > dd ? fabs((q[nc + c] * dn + q[2 * nc + c] * dm) / hq) + sqrt(gd * hq) : 0.;
+    const double bb = hb > dd ? fabs((b.trace[(size_t)b.nslot + slot] * dn + b.trace[2 * (size_t)b.nslot + slot] * dm) / hb) +
+                                    sqrt(gd * hb) : 0.;
+    wsf = make_float2(float(fl0), float(fmax(a, bb)));
+    gff = make_float4(float(fl1 - pc * dn), float(fl2 - pc * dm), 0.f, 0.f);
+}
+
+// resident blocks per SM the register allocation of the face sweep is fitted to
+#ifndef BRX_FACES_MIN_BLOCKS
+#define BRX_FACES_MIN_BLOCKS 8
+#endif
+
+__global__ void __launch_bounds__(128, BRX_FACES_MIN_BLOCKS) km_faces(MeshDev m, StateDev s, BoundaryDev b, Ctrl *ctrl, Work w,
+                                                MixedGeo g, int stage, TurbDev t, int turb)
+{
+    const MxRec *rec = reinterpret_cast<const MxRec *>(w.rec);
+    float2 *ws = reinterpret_cast<float2 *>(w.ws);
+    float4 *gf = reinterpret_cast<float4 *>(w.gf);
+    FOR_ACTIVE_FACES(m.act, f) {
+        const int sid = m.face_sid[f];
+        Ctrl &ct = ctrl[sid];
+        if (mx_skip(ct, stage)) continue;
+        const bool rotors = turb && t.hkt[sid];
+        const int c = m.owner[f], n = m.neighbour[f];
+        const int slot = m.bslot[f];
+        if (slot >= 0) {
+            float2 wsf;
+            float4 gff;
+            mx_open_face(m, s, b, ct, stage, f, c, slot, wsf, gff);
+            ws[f] = wsf;
+            gf[f] = gff;
+            if (rotors) {
+                g.hp[f] = make_float2(0.f, 0.f);
+                if (t.stress[sid]) g.hs[f] = make_float2(0.f, 0.f);
+            }
+            continue;
+        }
+        const MxRec rc = rec[c];
+        MxRec rn;
+        if (n >= 0) rn = rec[n];
+        const MxFaceOut o = mx_face(m, s, ct, g, stage, t, rotors, sid, f, c, n, rc, rn);
+        ws[f] = make_float2(o.water, o.speed);
+        gf[f] = make_float4(o.gl1, o.gl2, o.gr1, o.gr2);
     }
 }
 
@@ -830,14 +882,70 @@ __global__ void __launch_bounds__(128, BRX_FACES_MIN_BLOCKS) km_faces(MeshDev m,
 // have at most MAX_CELL_FACES faces.
 constexpr double DONOR_MARGIN = 64.0 * (double)FEPS;
 
+// Face values of a cell's entries for the gather: the grid sweep reads the
+// face sweep's arrays through the cell's face list.
+struct GlobalFaces {
+    const int *faces;
+    const float2 *ws;
+    const float4 *gf;
+    __device__ __forceinline__ float2 ws_at(int k) const { return ws[faces[k]]; }
+    __device__ __forceinline__ float4 gf_at(int k) const { return gf[faces[k]]; }
+};
+
+// Gather of one cell (the body of the gather sweep): its momentum rates and
+// donor factor into rate32 / theta32 and its face-sum CFL frequency in fr;
+// hf = the record's (depth, flags). Returns whether fr is valid.
+template <class FaceAt>
+__device__ __forceinline__ bool mx_gather_cell(const MeshDev &m, const StateDev &s, Ctrl &ct, const MixedGeo &g,
+                                               int stage, int c, float2 hf, const FaceAt &fa, float *rate32,
+                                               float *theta32, float &fr)
+{
+    const int nc = m.nc;
+    const bool active = __float_as_int(hf.y) & 2;
+    const bool owns_open = m.cflags[c] & 1;
+    float out = 0.f, ext = 0.f, interior = 0.f, sum1 = 0.f, sum2 = 0.f, freq = 0.f;
+    for (int k = m.offset[c]; k < m.offset[c + 1]; ++k) {
+        const float wk = g.cw4[k];            // s * len / area
+        const float2 wsf = fa.ws_at(k);
+        const float4 gff = fa.gf_at(k);
+        const float debit = fmaxf(wk * wsf.x, 0.f);   // outward water rate of this cell
+        if (wk > 0.f) { sum1 += wk * gff.x; sum2 += wk * gff.y; }
+        else { sum1 += wk * gff.z; sum2 += wk * gff.w; }
+        out += debit;
+        if (owns_open) { if (m.bslot[m.faces[k]] >= 0) ext += debit; else interior += debit; }
+        freq += fabsf(wk) * wsf.y;
+    }
+    rate32[c] = active ? -sum1 : 0.f;
+    rate32[nc + c] = active ? -sum2 : 0.f;
+    float theta = 1.f;
+    // donor factor: an FP32 test that is conservative, the value in FP64
+    if (out > 0.f && ct.trialf * out >= 0.999f * hf.x) {
+        const double hb = (stage == 1 ? s.work : s.q1)[c];
+        const double cap = ct.trial * double(out) * (1. + DONOR_MARGIN);
+        if (cap >= hb) theta = float(fmin(1., hb / cap) * (1. - 32. * EPS));
+    }
+    if (owns_open) {
+        const double hb = (stage == 1 ? s.work : s.q1)[c];
+        const double available = hb / ct.trial;
+        const double e = double(ext), e_hi = e * (1. + DONOR_MARGIN);
+        const double in_hi = double(interior) * (1. + DONOR_MARGIN);
+        if (e > available) raise_status(ct, stage, ST_BUDGET);
+        const double factor = fmin(1., (available - e_hi) / fmax(in_hi, 1e-300)) * (1. - 32. * EPS);
+        theta = (interior > 0.f && in_hi >= available - e_hi) ? float(fmax(factor, 0.)) : 1.f;
+    }
+    theta32[c] = theta;
+    fr = freq;
+    if (isnan(fr)) { raise_status(ct, stage, ST_FREQ); return false; }
+    return true;
+}
+
 __global__ void __launch_bounds__(256) km_gather(MeshDev m, StateDev s, Ctrl *ctrl, Work w, MixedGeo g, int stage)
 {
     const int nc = m.nc;
-    const float2 *ws = reinterpret_cast<const float2 *>(w.ws);
-    const float4 *gf = reinterpret_cast<const float4 *>(w.gf);
     const MxRec *rec = reinterpret_cast<const MxRec *>(w.rec);
     float *rate32 = reinterpret_cast<float *>(w.rate);      // (2, nc) momentum rates
     float *theta32 = reinterpret_cast<float *>(w.theta);
+    const GlobalFaces fa{m.faces, reinterpret_cast<const float2 *>(w.ws), reinterpret_cast<const float4 *>(w.gf)};
     const int stride = gridDim.x * blockDim.x;
     const int na = m.act.count[1];
     for (int first = blockIdx.x * blockDim.x; first < na; first += stride) {   // warp-uniform trip count
@@ -848,49 +956,118 @@ __global__ void __launch_bounds__(256) km_gather(MeshDev m, StateDev s, Ctrl *ct
         if (c < nc) {
             sid = m.cell_sid[c];
             Ctrl &ct = ctrl[sid];
-            if (!mx_skip(ct, stage)) {
-                const float2 hf = *reinterpret_cast<const float2 *>(&rec[c]);   // depth, flags
-                const bool active = __float_as_int(hf.y) & 2;
-                const bool owns_open = m.cflags[c] & 1;
-                float out = 0.f, ext = 0.f, interior = 0.f, sum1 = 0.f, sum2 = 0.f, freq = 0.f;
-                for (int k = m.offset[c]; k < m.offset[c + 1]; ++k) {
-                    const int f = m.faces[k];
-                    const float wk = g.cw4[k];            // s * len / area
-                    const float2 wsf = ws[f];
-                    const float4 gff = gf[f];
-                    const float debit = fmaxf(wk * wsf.x, 0.f);   // outward water rate of this cell
-                    if (wk > 0.f) { sum1 += wk * gff.x; sum2 += wk * gff.y; }
-                    else { sum1 += wk * gff.z; sum2 += wk * gff.w; }
-                    out += debit;
-                    if (owns_open) { if (m.bslot[f] >= 0) ext += debit; else interior += debit; }
-                    freq += fabsf(wk) * wsf.y;
-                }
-                rate32[c] = active ? -sum1 : 0.f;
-                rate32[nc + c] = active ? -sum2 : 0.f;
-                float theta = 1.f;
-                // donor factor: an FP32 test that is conservative, the value in FP64
-                if (out > 0.f && ct.trialf * out >= 0.999f * hf.x) {
-                    const double hb = (stage == 1 ? s.work : s.q1)[c];
-                    const double cap = ct.trial * double(out) * (1. + DONOR_MARGIN);
-                    if (cap >= hb) theta = float(fmin(1., hb / cap) * (1. - 32. * EPS));
-                }
-                if (owns_open) {
-                    const double hb = (stage == 1 ? s.work : s.q1)[c];
-                    const double available = hb / ct.trial;
-                    const double e = double(ext), e_hi = e * (1. + DONOR_MARGIN);
-                    const double in_hi = double(interior) * (1. + DONOR_MARGIN);
-                    if (e > available) raise_status(ct, stage, ST_BUDGET);
-                    const double factor = fmin(1., (available - e_hi) / fmax(in_hi, 1e-300)) * (1. - 32. * EPS);
-                    theta = (interior > 0.f && in_hi >= available - e_hi) ? float(fmax(factor, 0.)) : 1.f;
-                }
-                theta32[c] = theta;
-                fr = freq;
-                if (isnan(fr)) raise_status(ct, stage, ST_FREQ);
-                else have = true;
-            }
+            if (!mx_skip(ct, stage))
+                have = mx_gather_cell(m, s, ct, g, stage, c, *reinterpret_cast<const float2 *>(&rec[c]), fa, rate32,
+                                      theta32, fr);
         }
         unsigned long long *peak0 = stage == 1 ? &ctrl[0].peak1 : &ctrl[0].peak2;
         warp_max_peak_f(peak0, sizeof(Ctrl), sid, have, fr);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Tile sweep: cells, faces and gather of one stage over cell tiles staged in
+// shared memory
+// ---------------------------------------------------------------------------
+// Neighbour access of a tile's cells: the entry's local slot and flags from
+// the tile tables, the neighbour's primitives from shared memory.
+struct TileNbr {
+    const int2 *ent;         // the cell's entries, in entry order
+    const MxPrim *sP;
+    __device__ __forceinline__ int2 id(int, int j) const { return ent[j]; }
+    __device__ __forceinline__ MxPrim prim(int l) const { return sP[l]; }
+};
+
+// Face values of a tile cell's entries: the tile's face buffers in shared memory.
+struct TileFaces {
+    const int *tfslot;
+    const float2 *sW;
+    const float4 *sG;
+    __device__ __forceinline__ float2 ws_at(int k) const { return sW[tfslot[k]]; }
+    __device__ __forceinline__ float4 gf_at(int k) const { return sG[tfslot[k]]; }
+};
+
+// One block per tile (grid-stride over the tiles). The tile's primitives,
+// with two rings of neighbours, go to shared memory; the block forms the
+// records of its cells and of the first ring (whose records its edge faces
+// read), then every face of its cells, then its cells' gathers, all from
+// shared memory. The arithmetic of each record, face and gather is the
+// separate sweeps' own (mx_record, mx_face, mx_gather_cell), so the results
+// are theirs; a face on a tile edge is formed by both tiles alike. Only what
+// the update reads leaves the block: the water flux and CFL speed per face,
+// the momentum rates and donor factor per cell, the rotor face terms.
+template <int MAXF>
+__global__ void __launch_bounds__(TILE_THREADS, 4) km_tile(MeshDev m, StateDev s, BoundaryDev b, Ctrl *ctrl, Work w,
+                                                           MixedGeo g, int stage, TurbDev t, int turb, TileDev td)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    MxPrim *sP = reinterpret_cast<MxPrim *>(smem);
+    MxRec *sR = reinterpret_cast<MxRec *>(sP + td.cap_prims);
+    float2 *sW = reinterpret_cast<float2 *>(sR + td.cap_recs);
+    float4 *sG = reinterpret_cast<float4 *>(sW + td.cap_faces);
+    const MxPrim *P = reinterpret_cast<const MxPrim *>((stage == 1 ? g.prim[0] : g.prim[1]));
+    float2 *ws = reinterpret_cast<float2 *>(w.ws);
+    float *rate32 = reinterpret_cast<float *>(w.rate);
+    float *theta32 = reinterpret_cast<float *>(w.theta);
+    unsigned long long *peak0 = stage == 1 ? &ctrl[0].peak1 : &ctrl[0].peak2;
+    const TileFaces fa{td.tfslot, sW, sG};
+    for (int tile = blockIdx.x; tile < td.ntiles; tile += gridDim.x) {
+        const int4 I = td.info[tile], I2 = td.info2[tile];
+        const int c0 = I.x, nt = I.y - I.x, n1 = I2.x, n2 = I2.y, nface = I2.z;
+        const int sid = m.cell_sid[c0];
+        Ctrl &ct = ctrl[sid];
+        if (mx_skip(ct, stage)) continue;                 // uniform over the block
+        const bool rotors = turb && t.hkt[sid];
+        // primitives of the tile and its two rings
+        for (int i = threadIdx.x; i < nt + n1 + n2; i += blockDim.x)
+            sP[i] = P[i < nt ? c0 + i : td.halo[I.z + i - nt]];
+        __syncthreads();
+        // records of the tile's cells and of ring 1
+        for (int i = threadIdx.x; i < nt + n1; i += blockDim.x) {
+            const int c = i < nt ? c0 + i : td.halo[I.z + i - nt];
+            const int k0 = m.offset[c], deg = m.offset[c + 1] - k0;
+            const TileNbr nb{i < nt ? td.tent + k0 : td.hent + 4 * (I2.w + i - nt), sP};
+            sR[i] = mx_record<MAXF>(m, s, ct, g, sP[i], c, k0, deg, nb);
+            if (rotors) hkt_cell_gradients(m, g, nb, sP[i], c, m.nc);
+        }
+        __syncthreads();
+        // every face of the tile's cells
+        for (int j = threadIdx.x; j < nface; j += blockDim.x) {
+            const int4 F = td.tface[I.w + j];
+            const int f = F.x, c = m.owner[f], n = m.neighbour[f];
+            const int slot = m.bslot[f];
+            float2 wsf;
+            float4 gff;
+            if (slot >= 0) {
+                mx_open_face(m, s, b, ct, stage, f, c, slot, wsf, gff);
+                if (rotors) {
+                    g.hp[f] = make_float2(0.f, 0.f);
+                    if (t.stress[sid]) g.hs[f] = make_float2(0.f, 0.f);
+                }
+            } else {
+                const MxRec rc = sR[F.y];
+                MxRec rn;
+                if (F.z >= 0) rn = sR[F.z];
+                const MxFaceOut o = mx_face(m, s, ct, g, stage, t, rotors, sid, f, c, n, rc, rn);
+                wsf = make_float2(o.water, o.speed);
+                gff = make_float4(o.gl1, o.gl2, o.gr1, o.gr2);
+            }
+            sW[j] = wsf;
+            sG[j] = gff;
+            ws[f] = wsf;
+        }
+        __syncthreads();
+        // gathers of the tile's cells (warp-uniform trip count for the CFL peak)
+        for (int first = 0; first < nt; first += blockDim.x) {
+            const int i = first + (int)threadIdx.x;
+            bool have = false;
+            float fr = 0.f;
+            if (i < nt)
+                have = mx_gather_cell(m, s, ct, g, stage, c0 + i, make_float2(sR[i].h, __int_as_float(sR[i].flags)),
+                                      fa, rate32, theta32, fr);
+            warp_max_peak_f(peak0, sizeof(Ctrl), sid, have, fr);
+        }
+        __syncthreads();                                  // the next tile refills the buffers
     }
 }
 
@@ -1142,6 +1319,7 @@ int mixed_max_block(int kind, int maxdeg)
     case KH_FACES: fn = (const void *)brx_mx::km_hllc_faces; break;
     case KH_BUDGET: fn = (const void *)brx_mx::km_hllc_budget; break;
     case KH_UPDATE: fn = (const void *)brx_mx::km_hllc_update; break;
+    case K_TILE: return small ? TILE_THREADS : 0;          // the block is fixed; the grid cap is tunable
     default: return 0;
     }
     cudaFuncAttributes a;
@@ -1208,6 +1386,12 @@ int mixed_kernel(const Launch &L, int kind, int stage, double *out)
     case K_GATHER:
         brx_mx::km_gather<<<SHAPE(K_GATHER, nc), 0, st>>>(L.mesh, L.state, L.ctrl, L.work, L.mx, stage);
         return 1;
+    case K_TILE: {
+        const int grid = std::max(1, std::min(L.tiles.ntiles, L.shape[K_TILE].per_sm * L.sms));
+        brx_mx::km_tile<4><<<grid, TILE_THREADS, L.tile_smem, st>>>(L.mesh, L.state, L.bnd, L.ctrl, L.work, L.mx,
+                                                                   stage, L.turb, L.has_turb, L.tiles);
+        return 1;
+    }
     case K_LIMIT:
         brx_mx::km_limit<<<SHAPE(K_LIMIT, nf), 0, st>>>(L.mesh, L.ctrl, L.work, L.mx, stage);
         return 1;
@@ -1234,6 +1418,17 @@ int mixed_kernel(const Launch &L, int kind, int stage, double *out)
     }
 #undef SHAPE
     return 0;
+}
+
+int mixed_tile_smem(int cap_prims, int cap_recs, int cap_faces)
+{
+    return (int)(sizeof(brx_mx::MxPrim) * cap_prims + sizeof(brx_mx::MxRec) * cap_recs +
+                 (sizeof(float2) + sizeof(float4)) * cap_faces);
+}
+
+int mixed_tile_prepare(int smem_bytes)
+{
+    return (int)cudaFuncSetAttribute(brx_mx::km_tile<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
 }
 
 }  // namespace brx

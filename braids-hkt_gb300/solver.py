@@ -805,7 +805,7 @@ def _profile(self, dt, time=0.0, kinds=False):
     """Per-kernel durations (ms) of one trial launched without a graph: [(kernel name, ms), ...]
     (kernel kind ids instead of names with kinds=True)."""
     names = {0: "drag", 1: "boundary", 2: "cells", 3: "faces", 4: "gather", 5: "limit", 6: "update",
-             7: "control", 11: "rotors", 14: "viscosity",
+             7: "control", 11: "rotors", 14: "viscosity", 15: "tile",
              20: "hllc_cells", 21: "hllc_predict", 22: "boundary", 23: "hllc_faces", 24: "hllc_budget",
              25: "rotors", 26: "hllc_update", 27: "rotors_start"}
     self.torch.cuda.current_stream().synchronize()
@@ -830,6 +830,18 @@ def _set_shape(self, kind, block, per_sm):
     check(self.lib.brx_launch_shape_set(self.h, int(kind), int(block), int(per_sm)))
 
 
+def _set_tile(self, cells):
+    """Cells per tile of the mixed f-wave tile sweep (0: the separate cell, face and gather sweeps)."""
+    check(self.lib.brx_tile_set(self.h, int(cells)))
+
+
+def _tile(self):
+    """(cells per tile, shared memory bytes of the tile sweep); (0, 0) for the separate sweeps."""
+    cells, smem = C.c_int(), C.c_int()
+    check(self.lib.brx_tile_get(self.h, C.byref(cells), C.byref(smem)))
+    return cells.value, smem.value
+
+
 def _set_chunk(self, substeps):
     check(self.lib.brx_graph_chunk_set(self.h, int(substeps)))
     self.graph_chunk = int(substeps)
@@ -839,3 +851,5 @@ RiverSolver.profile_substep = _profile
 RiverSolver.launch_shape = _shape
 RiverSolver.set_launch_shape = _set_shape
 RiverSolver.set_graph_chunk = _set_chunk
+RiverSolver.set_tile = _set_tile
+RiverSolver.tile = _tile

@@ -191,6 +191,20 @@ int brx_advance(brx_solver *s, double dt, double time, brx_advance_stats *stats)
  * idle. Scenarios keep independent clocks inside the same launches. */
 int brx_advance_batch(brx_solver *s, const double *dt, const double *time, brx_advance_stats *stats);
 
+/* Mixed f-wave form, cells of at most four faces: run the cell, face and
+ * gather sweeps of each stage as one pass over tiles of `cells` consecutive
+ * cells of a scenario (0 = the separate sweeps, the default). Each block
+ * stages its tile's primitives with two rings of neighbours in shared
+ * memory, forms the records of the tile and of the first ring, the fluxes
+ * of every face of the tile's cells and the tile's gathers there; records
+ * and momentum fluxes no longer pass through device memory. The arithmetic
+ * of every record, face and gather is the separate sweeps'. No reference
+ * counterpart (its GPU path runs one kernel per sweep,
+ * src/braids_support/gpu_fwave/resident_update.cu); the tile size is what
+ * the autotuner picks. */
+int brx_tile_set(brx_solver *s, int cells);
+int brx_tile_get(const brx_solver *s, int *cells, int *smem_bytes);
+
 /* Several consecutive intervals per scenario in one call: scenario i
  * advances over [t_k, t_k + dt[i]] for k = 0 .. intervals-1, with t_0 =
  * time[i] and t_{k+1} = t_k + dt[i] (the owner's outer loop of steps at a

@@ -1,7 +1,8 @@
 """Mixed-precision form (FP32 fluxes/updates, FP64 stage, pressure, bed source, mass).
 
 Stated accuracy (spec target): depth within 1e-4 relative of the FP64
-form, mass conserved to 1e-12 relative, lake at rest preserved.
+form, mass conserved to 1e-12 relative, lake at rest preserved; with the
+separate cell / face / gather sweeps and with the tile sweep.
 """
 import numpy as np
 import pytest
@@ -14,14 +15,18 @@ DEPTH_RTOL = 1e-4
 MASS_RTOL = 1e-12
 
 
-def solver(case, precision):
+def solver(case, precision, tile=0):
     from braids_hkt_gb300.solver import RiverSolver
-    return RiverSolver(case, precision=precision)
+    s = RiverSolver(case, precision=precision)
+    if tile:
+        s.set_tile(tile)
+    return s
 
 
-def test_mixed_lake_at_rest():
+@pytest.mark.parametrize("tile", [0, 128])
+def test_mixed_lake_at_rest(tile):
     case = S.lake_at_rest()
-    s = solver(case, "mixed")
+    s = solver(case, "mixed", tile)
     d = s.advance(5.0, 0.0)
     assert d["failed"] == 0
     q = s.state()
@@ -31,19 +36,21 @@ def test_mixed_lake_at_rest():
     assert np.abs(q[1:]).max() < 1e-11
 
 
-def test_mixed_mass_conserved():
+@pytest.mark.parametrize("tile", [0, 128])
+def test_mixed_mass_conserved(tile):
     case = S.lake_at_rest()
-    s = solver(case, "mixed")
+    s = solver(case, "mixed", tile)
     s.set_state(S.perturbed_state(case, 9, 0.4, 0.6, 0.05))
     v0 = s.mass()
     s.advance(3.0, 0.0)
     assert abs(s.mass() - v0) <= MASS_RTOL * v0
 
 
-def test_mixed_depth_matches_fp64():
+@pytest.mark.parametrize("tile", [0, 128])
+def test_mixed_depth_matches_fp64(tile):
     case = S.small_channel(length=400.0, width=60.0, spacing=3.0, discharge=60.0)
     a = solver(case, "fp64")
-    b = solver(case, "mixed")
+    b = solver(case, "mixed", tile)
     for k in range(3):
         a.step(1.0)
         b.step(1.0)
