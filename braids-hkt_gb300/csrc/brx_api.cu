@@ -1078,6 +1078,7 @@ extern "C" int brx_launch_shape_set(brx_solver *s, int kind, int block, int bloc
     const int mb = max_block(s, kind);
     if (mb <= 0) return fail(BRX_ERR_ARGUMENT, "kernel kind has no tunable launch shape");
     if (block < 32 || block % 32 || block > mb) return fail(BRX_ERR_ARGUMENT, "block must be a multiple of 32 within the kernel's limit");
+    if (kind == K_TILE && block != TILE_THREADS) return fail(BRX_ERR_ARGUMENT, "the tile sweep's block is fixed at 256 threads");
     if (blocks_per_sm < 1 || blocks_per_sm > 64) return fail(BRX_ERR_ARGUMENT, "blocks per SM must be in 1..64");
     s->shape[kind] = {block, blocks_per_sm};
     s->graph_dirty = true;

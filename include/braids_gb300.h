@@ -388,7 +388,9 @@ int brx_graph_chunk_set(brx_solver *s, int substeps);
 
 /* Launch shape of one kernel kind (the kinds of brx_profile_substep: 0 drag,
  * 2 cells, 3 faces, 4 gather, 5 limit, 6 update, 12 / 13 rotor gradients /
- * face terms; HLLC 20 cells, 21 predictor, 23 faces, 24 budget, 26 update):
+ * face terms, 15 the mixed tile sweep (block fixed at 256, one tile per block
+ * and grid-stride step); HLLC 20 cells, 21 predictor, 23 faces, 24 budget,
+ * 26 update):
  * threads per block (a multiple of 32 up to the kernel's limit) and the grid
  * cap in blocks per SM. Every sweep is a grid-stride loop, so results do not
  * depend on the shape. The autotuner (braids_hkt_gb300.autotune) sets these;
