@@ -1,6 +1,6 @@
 """Mixed-precision form (FP32 fluxes/updates, FP64 stage, pressure, bed source, mass).
 
-Stated accuracy (spec target): depth within 1e-4 relative of the FP64
+Stated accuracy (the mixed form's target): depth within 1e-4 relative of the FP64
 form, mass conserved to 1e-12 relative, lake at rest preserved; with the
 separate cell / face / gather sweeps and with the tile sweep.
 """

@@ -2,7 +2,7 @@
 
 FP64 form: the residual matches the oracle to 1e-12 relative of each row's
 scale (bitwise in practice), an adaptive advance to 1e-10 with the same
-substep count, per-rotor power and thrust to 1e-8 relative (north-star
+substep count, per-rotor power and thrust to 1e-8 relative (the stated
 tolerance; the per-rotor sums differ from the oracle only in order).
 Mixed form: depth within 1e-4 relative of the FP64 form, per-rotor power
 within 1e-3 relative (power goes with the cube of the FP32-carried speed).
