@@ -816,15 +816,23 @@ extern "C" int brx_turbines_set(brx_solver *s, int nrotor, const int *rotor_scen
     std::vector<std::pair<int, int>> pairs(ns);
     for (int e = 0; e < ns; ++e) pairs[e] = {support_cell[e], e};
     std::sort(pairs.begin(), pairs.end());
-    std::vector<int> ucell, uoff{0}, uent;
-    for (int e = 0; e < ns; ++e) {
-        if (e == 0 || pairs[e].first != pairs[e - 1].first) {
-            if (e) uoff.push_back(e);
-            ucell.push_back(pairs[e].first);
+    // a cell of one entry gets its actuator sink from its rotor's sample CTA;
+    // the cells of several entries (overlapping supports) from k_turbine_raw
+    std::vector<int> ucell, uoff{0}, uent, allcells;
+    std::vector<unsigned char> single(ns, 0);
+    for (int e0 = 0; e0 < ns;) {
+        int e1 = e0 + 1;
+        while (e1 < ns && pairs[e1].first == pairs[e0].first) ++e1;
+        allcells.push_back(pairs[e0].first);
+        if (e1 - e0 == 1) {
+            single[pairs[e0].second] = 1;
+        } else {
+            ucell.push_back(pairs[e0].first);
+            for (int e = e0; e < e1; ++e) uent.push_back(pairs[e].second);
+            uoff.push_back((int)uent.size());
         }
-        uent.push_back(pairs[e].second);
+        e0 = e1;
     }
-    uoff.push_back(ns);
     std::vector<int> stress(s->nscen, 0), sid(nrotor);
     for (int i = 0; i < s->nscen; ++i)
         for (int c = s->cell_offset[i]; c < s->cell_offset[i + 1]; ++c)
@@ -863,8 +871,13 @@ extern "C" int brx_turbines_set(brx_solver *s, int nrotor, const int *rotor_scen
     TRY(s->upload(&p_ucell, ucell.data(), ucell.size())); TRY(s->upload(&p_uoff, uoff.data(), uoff.size()));
     TRY(s->upload(&p_uent, uent.data(), uent.size()));
     {
+        unsigned char *p_single;
+        TRY(s->upload(&p_single, single.data(), single.size()));
+        t.single = p_single;
+    }
+    {
         std::vector<unsigned char> foot(nc, 0);
-        for (int c : ucell) foot[c] = 1;
+        for (int c : allcells) foot[c] = 1;
         unsigned char *p_foot;
         TRY(s->upload(&p_foot, foot.data(), foot.size()));
         t.foot = p_foot;
@@ -1468,9 +1481,12 @@ static int launch_turbines(brx_solver *s, int stage, cudaStream_t st, int part =
             ++n;
         }
         k_turbine_sample<<<t.nr, TURB_THREADS, 0, st>>>(s->mesh, t, q, s->state.z, s->d_ctrl, stage, t.diag);
-        k_turbine_raw<<<std::max(1, std::min((t.nucell + 255) / 256, s->sms * 8)), 256, 0, st>>>(s->mesh, t, q,
-                                                                                               s->d_ctrl, stage);
-        n += 2;
+        ++n;
+        if (t.nucell > 0) {            // cells shared by overlapping supports
+            k_turbine_raw<<<std::max(1, std::min((t.nucell + 255) / 256, s->sms * 8)), 256, 0, st>>>(s->mesh, t, q,
+                                                                                                   s->d_ctrl, stage);
+            ++n;
+        }
     }
     if (part & TURB_FACES) {
         if (mixed) n += mixed_kernel(make_launch(s, st), K_HKT_FACES, stage, nullptr);

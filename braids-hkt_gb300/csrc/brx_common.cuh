@@ -162,7 +162,8 @@ struct TurbDev {
     const double *curve_x, *curve_y;
     const double *curve_slope;                      // (y[k+1]-y[k])/(x[k+1]-x[k]) of each table knot
     const int *flat_thrust;                         // (nr) 1: the rotor's thrust table is constant
-    const int *ucell, *uoff, *uent;                 // unique support cells -> their entries, rotor order
+    const int *ucell, *uoff, *uent;                 // support cells of two or more entries -> their entries, rotor order
+    const unsigned char *single;                    // (ns) 1: the entry's cell is in no other support entry
     const unsigned char *foot;                      // (nc) 1: a support cell (its actuator sink may be nonzero)
     const double *dxdy, *inverse, *xy, *mdisp, *nu; // (2,nadj) (3,nc) (2,nc) (4,nf) (nc)
     double *grad;               // (8, nc) wet gradients: u, v, eta, b (x, y)

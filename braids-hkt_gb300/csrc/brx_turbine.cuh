@@ -275,6 +275,21 @@ __global__ void __launch_bounds__(TURB_THREADS) k_turbine_sample(MeshDev m, Turb
         d[TD_ERROR] = flags[2];
         if (flags[2] && stage) raise_status(ct, stage, ST_TURBINE);
     }
+    // actuator sink of the support cells no other rotor's support holds:
+    // 0 - k |u| u from this rotor alone (k_turbine_raw's sum with one term);
+    // each thread reads the coefficients it wrote itself
+    if (stage)
+        for (int e = t.support_offset[r] + tid; e < t.support_offset[r + 1]; e += TURB_THREADS) {
+            if (!t.single[e]) continue;
+            const int c = t.support_cell[e];
+            const double h = q[c], u = q[n + c] / fmax(h, dry), v = q[2 * n + c] / fmax(h, dry);
+            const double speed = hypot(u, v);
+            const double kc = t.kcell[e];
+            double rx = 0., ry = 0.;
+            rx -= kc * speed * u;
+            ry -= kc * speed * v;
+            t.raw[c] = rx; t.raw[n + c] = ry;
+        }
 }
 
 // Actuator sink per support cell: 0 - sum over its rotors of k |u| u.
