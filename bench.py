@@ -436,9 +436,9 @@ def main():
                     help="skip the HLLC MUSCL-Hancock legs (per-scenario and whole batch, FP64 form)")
     ap.add_argument("--profile-only", type=int, default=0,
                     help="only time N substeps kernel by kernel (brx_profile_substep) and exit")
-    ap.add_argument("--profile-method", default="fwave", choices=("fwave", "hllc", "hllc-mixed"),
-                    help="hydraulic method of --profile-only (hllc runs the FP64 form, hllc-mixed the "
-                         "mixed FP32/FP64 form)")
+    ap.add_argument("--profile-method", default="fwave", choices=("fwave", "fwave-fp64", "hllc", "hllc-mixed"),
+                    help="hydraulic method of --profile-only (fwave runs the workload's form, fwave-fp64 the FP64 "
+                         "form, hllc the FP64 form, hllc-mixed the mixed FP32/FP64 form)")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
@@ -455,6 +455,8 @@ def main():
             solver = RiverSolver(cases, precision="fp64", method="hllc")
         elif args.profile_method == "hllc-mixed":
             solver = RiverSolver(cases, precision="mixed", method="hllc")
+        elif args.profile_method == "fwave-fp64":
+            solver = RiverSolver(cases, precision="fp64")
         else:
             solver = RiverSolver(cases, precision=precision)
         dt = 1e-3                   # one trial of every kernel from the initial state, no interval before it
