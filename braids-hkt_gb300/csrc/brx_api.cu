@@ -1855,7 +1855,7 @@ extern "C" int brx_advance_chain(brx_solver *s, const double *dt, const double *
 {
     TRY(ensure_ready(s));
     if (!dt || !time) return fail(BRX_ERR_ARGUMENT, "null interval arrays");
-    if (intervals < 1) return fail(BRX_ERR_ARGUMENT, "intervals must be at least 1");
+    if (intervals < 1 || intervals > 65536) return fail(BRX_ERR_ARGUMENT, "intervals must be in 1..65536");
     if (s->pending) return fail(BRX_ERR_STATE, "an asynchronous interval is already in flight");
     for (int i = 0; i < s->nscen; ++i)
         if (!std::isfinite(dt[i]) || !std::isfinite(time[i])) return fail(BRX_ERR_ARGUMENT, "nonfinite interval");

@@ -218,8 +218,8 @@ int brx_tile_get(const brx_solver *s, int *cells, int *smem_bytes);
  * (host, nscen x intervals, may be NULL) each interval's net inflow volume
  * and gross boundary volume as brx_ledger_get / brx_ledger_gross_get give
  * them after one interval (those getters then report the last interval).
- * An interval after a failed one reports failed = 3 (not run). Returns
- * BRX_ERR_REJECTED if any scenario failed. */
+ * An interval after a failed one reports failed = 3 (not run); intervals
+ * is 1..65536. Returns BRX_ERR_REJECTED if any scenario failed. */
 int brx_advance_chain(brx_solver *s, const double *dt, const double *time, int intervals,
                       brx_advance_stats *stats, double *ledger, double *gross);
 
