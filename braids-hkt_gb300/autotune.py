@@ -102,12 +102,15 @@ def _trial(solver, dt, saved_q, time0):
     return per
 
 
-def _tune_tile(solver, saved_q, saved_hints, dt, time0, interval, tiles):
+def _tune_tile(solver, saved_q, saved_hints, dt, time0, interval, tiles, sync=None, clock=time.perf_counter):
     """Cells per tile and grid cap of the tile sweep, or 0 (separate sweeps):
     the fastest of a short fixed interval, each candidate run twice from the
     same state (the first run builds its graph). None where the solver has
-    no tile sweep (FP64 form, HLLC, cells of more than four faces)."""
-    import torch
+    no tile sweep (FP64 form, HLLC, cells of more than four faces). sync
+    waits for the device (torch.cuda.synchronize by default)."""
+    if sync is None:
+        import torch
+        sync = torch.cuda.synchronize
     if solver.precision != "mixed" or solver.method != "fwave":
         return None
     try:
@@ -123,11 +126,11 @@ def _tune_tile(solver, saved_q, saved_hints, dt, time0, interval, tiles):
         solver.advance(span, time0, raise_on_failure=False)        # builds the graph
         solver.q.copy_(saved_q)
         solver.set_hints(hints)
-        torch.cuda.synchronize()
-        w0 = time.perf_counter()
+        sync()
+        w0 = clock()
         solver.advance(span, time0, raise_on_failure=False)
-        torch.cuda.synchronize()
-        return (time.perf_counter() - w0) * 1e3
+        sync()
+        return (clock() - w0) * 1e3
 
     table = {"0": run()}
     best = (table["0"], 0, 0)
